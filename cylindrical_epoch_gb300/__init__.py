@@ -1,0 +1,16 @@
+"""GB300-native quasi-3D (x, r, theta-mode) PIC step of cylindrical EPOCH.
+
+The hot path (fused gather / Boris push / charge-conserving per-mode
+deposit, per-mode Yee solver with the r = 0 axis rules, laser injection,
+particle boundaries, moving window) runs as hand-written sm_103a kernels in
+libcylpic.so behind the C ABI of include/cylpic.h.  This package is the
+host-side mirror of the reference driver: deck descriptions, the loader and
+the run handle.
+"""
+from . import abi, deck
+from .deck import Deck, Laser, Species, thermal_plasma, wakefield, large_wakefield
+from .lib import load
+from .run import Particles, Run, host_load
+
+__all__ = ["abi", "deck", "Deck", "Laser", "Species", "thermal_plasma", "wakefield",
+           "large_wakefield", "load", "Particles", "Run", "host_load"]

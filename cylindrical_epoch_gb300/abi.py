@@ -1,0 +1,139 @@
+"""ctypes mirror of include/cylpic.h.
+
+The structures below are field-for-field copies of the C descriptors, so a
+Python caller builds exactly what a Fortran caller would pass through
+ISO_C_BINDING.  Constants carry the values of the reference's
+constants.F90:56-84.
+"""
+import ctypes as C
+
+NG = 5
+
+CYL_OK = 0
+CYL_ERR_BAD_ARG = 1
+CYL_ERR_CUDA = 2
+CYL_ERR_NO_DEVICE = 3
+CYL_ERR_CAPACITY = 4
+CYL_ERR_UNSUPPORTED = 5
+CYL_ERR_DEVICE_FLAG = 6
+CYL_ERR_TIMEOUT = 7
+CYL_ERR_OUT_OF_MEMORY = 8
+
+ERROR_NAMES = {
+    CYL_ERR_BAD_ARG: "bad argument",
+    CYL_ERR_CUDA: "CUDA runtime error",
+    CYL_ERR_NO_DEVICE: "no CUDA device",
+    CYL_ERR_CAPACITY: "particle capacity exceeded",
+    CYL_ERR_UNSUPPORTED: "unsupported option",
+    CYL_ERR_DEVICE_FLAG: "device error flag raised",
+    CYL_ERR_TIMEOUT: "timed out waiting for the GPU",
+    CYL_ERR_OUT_OF_MEMORY: "device out of memory",
+}
+
+BC_PERIODIC = 1
+BC_OTHER = 2
+BC_SIMPLE_LASER = 3
+BC_SIMPLE_OUTFLOW = 4
+BC_OPEN = 5
+BC_ZERO_GRADIENT = 7
+BC_CLAMP = 8
+BC_REFLECT = 9
+BC_CONDUCT = 10
+BC_ZERO_B = 16
+
+BD_X_MIN, BD_X_MAX, BD_Y_MIN, BD_Y_MAX = 0, 1, 2, 3
+
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+FIELD_NAMES = ["exm", "erm", "etm", "bxm", "brm", "btm", "jxm", "jrm", "jtm",
+               "bxm_old", "brm_old", "btm_old", "jxm_old", "jrm_old", "jtm_old"]
+FIELD_INDEX = {n: i for i, n in enumerate(FIELD_NAMES)}
+
+
+class GridDesc(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int32), ("ny", C.c_int32), ("n_mode", C.c_int32),
+        ("precision", C.c_int32),
+        ("x_min", C.c_double), ("x_max", C.c_double), ("y_max", C.c_double),
+        ("dt", C.c_double),
+        ("bc_field", C.c_int32 * 4),
+        ("move_window", C.c_int32),
+        ("window_v_x", C.c_double), ("window_start_time", C.c_double),
+        ("window_stop_time", C.c_double),
+        ("bc_after_move", C.c_int32 * 4),
+        ("smooth_currents", C.c_int32), ("smooth_its", C.c_int32),
+        ("smooth_comp_its", C.c_int32), ("smooth_stride", C.c_int32),
+    ]
+
+
+class SpeciesDesc(C.Structure):
+    _fields_ = [
+        ("charge", C.c_double), ("mass", C.c_double),
+        ("immobile", C.c_int32),
+        ("bc_particle", C.c_int32 * 4),
+        ("capacity", C.c_int64),
+        ("npart_per_cell", C.c_double),
+        ("density_kind", C.c_int32),
+        ("density", C.c_double), ("ramp_x0", C.c_double), ("ramp_length", C.c_double),
+        ("density_min", C.c_double), ("density_max", C.c_double),
+        ("temp", C.c_double * 3),
+        ("drift", C.c_double * 3),
+    ]
+
+
+class LaserDesc(C.Structure):
+    _fields_ = [
+        ("boundary", C.c_int32), ("t_profile", C.c_int32),
+        ("amp", C.c_double), ("omega", C.c_double), ("pol_angle", C.c_double),
+        ("t_start", C.c_double), ("t_end", C.c_double),
+        ("t0", C.c_double), ("tw", C.c_double),
+        ("profile", C.POINTER(C.c_double)),
+        ("phase", C.POINTER(C.c_double)),
+    ]
+
+
+class RngState(C.Structure):
+    _fields_ = [
+        ("x", C.c_int32), ("y", C.c_int32), ("z", C.c_int32), ("w", C.c_int32),
+        ("box_muller_cached", C.c_int32),
+        ("cached_random_value", C.c_double),
+    ]
+
+
+class RunState(C.Structure):
+    _fields_ = [
+        ("time", C.c_double), ("step", C.c_int64),
+        ("x_grid_min", C.c_double), ("xb_min", C.c_double),
+        ("x_min", C.c_double), ("x_max", C.c_double),
+        ("window_shift_fraction", C.c_double),
+        ("window_started", C.c_int32),
+        ("bc_field", C.c_int32 * 4),
+        ("n_live", C.c_int64 * 8),
+        ("n_shifts", C.c_int64),
+    ]
+
+
+class Diag(C.Structure):
+    _fields_ = [
+        ("kinetic_energy", C.c_double),
+        ("field_energy_e", C.c_double),
+        ("field_energy_b", C.c_double),
+        ("jsum_abs", C.c_double),
+        ("n_live", C.c_int64),
+        ("device_error", C.c_int32),
+    ]
+
+
+class CylError(RuntimeError):
+    """Raised when an entry point returns a non-zero status."""
+
+    def __init__(self, func, code):
+        super().__init__(f"{func} failed: status {code} ({ERROR_NAMES.get(code, 'unknown')})")
+        self.code = code
+
+
+def check(func, code):
+    if code != CYL_OK:
+        raise CylError(func, code)
+    return code

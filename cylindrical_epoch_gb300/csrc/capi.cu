@@ -1,0 +1,904 @@
+// capi.cu -- the C ABI of include/cylpic.h: run handle, host-side scalar
+// bookkeeping and the per-step kernel sequence.
+//
+// The Fortran module scalars that the hot path reads (time, grid position of
+// the moving window, field boundary codes, laser phases) are advanced on the
+// host in the reference's order and shipped to the GPU as one StepRec per
+// step, together with the laser source vectors and the particles the window
+// injects.  All array state (fields, currents, particles) stays resident in
+// HBM.  Steps are enqueued in chunks; a chunk of CHUNK steps can be captured
+// once into a CUDA graph and replayed.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "cyl_common.cuh"
+#include "cyl_kernels.cuh"
+#include "host_deck.h"
+
+namespace cyl {
+
+constexpr int CHUNK = 16;
+
+#define CK(call)                                  \
+  do {                                            \
+    cudaError_t e_ = (call);                      \
+    if (e_ != cudaSuccess) {                      \
+      h->last_cuda_error = e_;                    \
+      return CYL_ERR_CUDA;                        \
+    }                                             \
+  } while (0)
+
+struct HostLaser {
+  cyl_laser_desc d;
+  std::vector<double> profile, phase;
+  double current_integral_phase = 0.0;
+};
+
+// push-mixed.cu (mixed precision form)
+void launch_push_mixed(cudaStream_t s, const FieldSet& F, const GeomTables& g, const SpeciesPtrs& sp,
+                       SpeciesCounters* cnt, const StepRec* rec, const RunConst& rc, int apply_bcs,
+                       int* err, int nblocks);
+
+struct Handle {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  cudaError_t last_cuda_error = cudaSuccess;
+  cyl_grid_desc gd;
+  HostGrid g;
+  RunConst rc;
+  int prec = CYL_PREC_FP64;
+  size_t fcount = 0;  // complex elements per mode array
+  cplx* fbuf = nullptr;
+  cplx* F[16] = {};   // 15 arrays + smoothing work array
+  int jpar = 0;       // 0: J in slots 6..8, J_old in 12..14; 1: swapped
+  cplx* cols = nullptr;
+  double* geom_buf = nullptr;
+  GeomTables geom;
+  int nsp = 0;
+  cyl_species_desc sd[MAX_SPECIES];
+  SpeciesPtrs sp[MAX_SPECIES];
+  SpeciesCounters* d_cnt = nullptr;
+  SortScratch sc;
+  double* sort_buf = nullptr;
+  int64_t next_id = 0;
+  // host bookkeeping (module globals)
+  double time = 0.0;
+  int64_t step = 0;
+  int bc_deck[4], bc_field[4], add_laser[4], bc_after_move[4];
+  int bc_allspecies[4];
+  bool move_window = false, window_started = false;
+  double window_v_x = 0, window_start_time = 0, window_stop_time = 0, wsf = 0;
+  int64_t n_shifts = 0;
+  std::vector<HostLaser> lasers;
+  KissRng rng;
+  // staging
+  StepRec* h_rec = nullptr;
+  StepRec* d_rec = nullptr;
+  double* h_src = nullptr;
+  double* d_src = nullptr;
+  double* h_inj = nullptr;
+  double* d_inj = nullptr;
+  int64_t inj_cap = 0;  // particles per chunk
+  size_t src_per_step = 0;
+  cudaEvent_t ev_copy = nullptr;
+  bool copy_pending = false;
+  int* d_err = nullptr;
+  double* d_red = nullptr;
+  // graph
+  cudaGraphExec_t gexec = nullptr;
+  int graph_parity = -1;
+  // timing of the push kernel (events around each push in eager mode and in graphs)
+  cudaEvent_t ev_push[CHUNK][2];
+  int push_events_used = 0;
+  double push_ms_sum = 0.0;
+  int64_t push_launches = 0;
+  int nblocks = 152 * 8;
+  int64_t kernel_launches = 0;
+  int64_t graph_launches = 0;
+};
+
+static void setup_boundaries(Handle* h) {
+  // boundary.F90:30-75
+  for (int i = 0; i < 4; ++i) {
+    int b = h->bc_deck[i];
+    h->add_laser[i] = 0;
+    if (b == CYL_BC_OTHER) b = CYL_BC_CLAMP;
+    if (b == CYL_BC_SIMPLE_LASER) h->add_laser[i] = 1;
+    if (b == CYL_BC_REFLECT) b = CYL_BC_CLAMP;
+    if (b == CYL_BC_OPEN) b = CYL_BC_SIMPLE_OUTFLOW;
+    h->bc_field[i] = b;
+  }
+}
+
+static int map_particle_bc(int b) {
+  // setup_particle_boundary (boundary.F90:100-140)
+  if (b == CYL_BC_OTHER || b == CYL_BC_CONDUCT) b = CYL_BC_REFLECT;
+  if (b == CYL_BC_SIMPLE_LASER || b == CYL_BC_SIMPLE_OUTFLOW) b = CYL_BC_OPEN;
+  return b;
+}
+
+static FieldSet fieldset(const Handle* h, int jpar) {
+  auto v = [&](int k) { return FView{h->F[k], h->rc.nxg, h->rc.nyg}; };
+  FieldSet F;
+  F.ex = v(0); F.er = v(1); F.et = v(2);
+  F.bx = v(3); F.br = v(4); F.bt = v(5);
+  F.bxo = v(9); F.bro = v(10); F.bto = v(11);
+  const int j0 = jpar ? 12 : 6, jo = jpar ? 6 : 12;
+  F.jx = v(j0); F.jr = v(j0 + 1); F.jt = v(j0 + 2);
+  F.jxo = v(jo); F.jro = v(jo + 1); F.jto = v(jo + 2);
+  return F;
+}
+
+// Slot of a public field index under the current J parity.
+static int field_slot(const Handle* h, int which) {
+  if (h->jpar && which >= 6 && which <= 8) return which + 6;
+  if (h->jpar && which >= 12 && which <= 14) return which - 6;
+  return which;
+}
+
+// Laser sources at the handle's current time (laser.f90:444-461):
+// out[side*2*(ny+1) + {0, ny+1} + ir] = source1, source2.
+static void laser_sources(Handle* h, double* out) {
+  const int ny = h->g.ny;
+  std::memset(out, 0, sizeof(double) * 4 * (ny + 1));
+  for (auto& L : h->lasers) L.current_integral_phase = L.d.omega * h->time;  // update_laser_omegas
+  for (int side = 0; side < 2; ++side) {
+    const int bd = side == 0 ? CYL_BD_X_MIN : CYL_BD_X_MAX;
+    if (!h->add_laser[bd]) continue;
+    double* s1 = out + side * 2 * (ny + 1);
+    double* s2 = s1 + (ny + 1);
+    for (auto& L : h->lasers) {
+      if (L.d.boundary != bd) continue;
+      if (h->time >= L.d.t_start && h->time <= L.d.t_end) {
+        double tp = 1.0;
+        if (L.d.t_profile == 1) {
+          const double v = (h->time - L.d.t0) / L.d.tw;
+          tp = std::exp(-(v * v));
+        }
+        const double t_env = tp * L.d.amp;
+        for (int ir = 0; ir <= ny; ++ir) {
+          const double base = t_env * L.profile[ir] * std::sin(L.current_integral_phase + L.phase[ir]);
+          s1[ir] = s1[ir] + base * std::cos(L.d.pol_angle);
+          s2[ir] = s2[ir] + base * std::sin(L.d.pol_angle);
+        }
+      }
+    }
+  }
+}
+
+static void fill_grid(StepRec& r, const HostGrid& g, bool after) {
+  if (!after) {
+    r.x_grid_min = g.x_grid_min;
+    r.x_min = g.x_min;
+    r.x_max = g.x_max;
+    r.x_min_local = g.x_min_local;
+    r.x_max_local = g.x_max_local;
+  } else {
+    r.x_grid_min_after = g.x_grid_min;
+    r.x_min_after = g.x_min;
+    r.x_max_after = g.x_max;
+    r.x_min_local_after = g.x_min_local;
+    r.x_max_local_after = g.x_max_local;
+  }
+}
+
+// Advance the host scalars through one driver-loop iteration and describe it
+// (epoch2d.F90:213-265 with moving_window, window.F90:330-376).
+static void prepare_step(Handle* h, int k, int64_t& inj_used) {
+  StepRec& r = h->h_rec[k];
+  std::memset(&r, 0, sizeof(r));
+  r.time_half = h->time;
+  fill_grid(r, h->g, false);
+  for (int i = 0; i < 4; ++i) {
+    r.bc_field[i] = h->bc_field[i];
+    r.add_laser[i] = h->add_laser[i];
+  }
+  h->step++;
+  h->time = h->time + h->g.dt / 2.0;
+  h->time = h->time + h->g.dt / 2.0;
+  r.time_final = h->time;
+  r.src_off = (int64_t)k * (int64_t)h->src_per_step;
+  laser_sources(h, h->h_src + r.src_off);
+  for (int s = 0; s < h->nsp; ++s) {
+    r.inject_off[s] = inj_used;
+    r.inject_cnt[s] = 0;
+  }
+  int nshift = 0;
+  if (h->move_window) {
+    if (!h->window_started) {
+      if (h->time >= h->window_start_time && h->time < h->window_stop_time) {
+        for (int i = 0; i < 4; ++i) h->bc_deck[i] = h->bc_after_move[i];
+        setup_boundaries(h);
+        h->wsf = 0.0;
+        h->window_started = true;
+      }
+    }
+    if (h->window_started && !(h->time >= h->window_stop_time) && h->window_v_x > 0.0) {
+      h->wsf = h->wsf + h->g.dt * h->window_v_x / h->g.dx;
+      const int cells = (int)std::floor(h->wsf);
+      if (cells > 0) {
+        std::vector<HostParticle> batch;
+        // one buffer region per species: inject all species for every shift
+        std::vector<std::vector<HostParticle>> per(h->nsp);
+        for (int c = 0; c < cells; ++c) {
+          for (int s = 0; s < h->nsp; ++s)
+            host_insert_particles(h->g, h->sd[s], h->rng, h->next_id, per[s]);
+          h->g.x_grid_min = h->g.xg(1) + h->g.dx;
+          h->g.xb_min = h->g.xb_min + h->g.dx;
+          h->g.x_min = h->g.xb_min + h->g.dx * 0.0;
+          h->g.x_max = (h->g.xb_min + (double)(h->g.nx + 1 - 1) * h->g.dx) - h->g.dx * 0.0;
+          h->g.setup_grid_x();
+          h->n_shifts++;
+          nshift++;
+        }
+        for (int s = 0; s < h->nsp; ++s) {
+          r.inject_off[s] = inj_used;
+          r.inject_cnt[s] = (int64_t)per[s].size();
+          for (auto& p : per[s]) {
+            double* q = h->h_inj + inj_used * 8;
+            for (int t = 0; t < 7; ++t) q[t] = p.v[t];
+            std::memcpy(&q[7], &p.id, 8);
+            inj_used++;
+          }
+        }
+        h->wsf = h->wsf - (double)cells;
+      }
+    }
+  }
+  r.nshift = nshift;
+  for (int i = 0; i < 4; ++i) r.bc_field_after[i] = h->bc_field[i];
+  fill_grid(r, h->g, true);
+}
+
+static void count_launch(Handle* h, int n) { h->kernel_launches += n; }
+
+static void push_species(Handle* h, cudaStream_t s, const FieldSet& F, int i, const StepRec* rec,
+                         int apply_bcs) {
+#ifdef CYL_WITH_MIXED
+  if (h->prec == CYL_PREC_MIXED) {
+    launch_push_mixed(s, F, h->geom, h->sp[i], h->d_cnt + i, rec, h->rc, apply_bcs, h->d_err, h->nblocks);
+    return;
+  }
+#endif
+  launch_push_fp64(s, F, h->geom, h->sp[i], h->d_cnt + i, rec, h->rc, apply_bcs, h->d_err, h->nblocks);
+}
+
+// Enqueue the kernels of one step; rec/src point at this step's records.
+static void enqueue_step(Handle* h, const StepRec* rec, const double* src, int k_in_chunk,
+                         bool timing, bool capturing) {
+  const unsigned evflag = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+  cudaStream_t s = h->st;
+  const RunConst& rc = h->rc;
+  FieldSet F = fieldset(h, h->jpar);
+  // update_eb_fields_half (fields.f90:316-337)
+  launch_update_e(s, F, rc);
+  launch_e_axis_bcs(s, F, rec, rc);
+  launch_update_b(s, F, 1, rc);
+  launch_b_axis_bcs(s, F, rec, rc);
+  count_launch(h, 4);
+  // push_particles: J_old = J, J = 0 (particles.F90:163-169) by buffer swap
+  h->jpar ^= 1;
+  F = fieldset(h, h->jpar);
+  const size_t bytes = h->fcount * sizeof(cplx);
+  cudaMemsetAsync(F.jx.p, 0, bytes, s);
+  cudaMemsetAsync(F.jr.p, 0, bytes, s);
+  cudaMemsetAsync(F.jt.p, 0, bytes, s);
+  if (timing) cudaEventRecordWithFlags(h->ev_push[k_in_chunk][0], s, evflag);
+  for (int i = 0; i < h->nsp; ++i) {
+    if (h->sp[i].immobile) continue;
+    push_species(h, s, F, i, rec, 1);
+    count_launch(h, 1);
+  }
+  if (timing) cudaEventRecordWithFlags(h->ev_push[k_in_chunk][1], s, evflag);
+  // current_bcs_r_min_final + current_finish
+  FView wk{h->F[15], rc.nxg, rc.nyg};
+  launch_current_finish(s, F, rec, rc, h->gd.smooth_currents, h->gd.smooth_its, h->gd.smooth_comp_its,
+                        h->gd.smooth_stride > 0 ? h->gd.smooth_stride : 1, wk);
+  count_launch(h, 1);
+  // update_eb_fields_final (fields.f90:341-353)
+  launch_update_b(s, F, 0, rc);
+  launch_b_final_bcs(s, F, rec, src, h->cols, 1, rc.dt, rc);
+  launch_update_e(s, F, rc);
+  launch_e_axis_bcs(s, F, rec, rc);
+  count_launch(h, 4);
+  // moving_window
+  if (h->move_window) {
+    for (int i = 0; i < h->nsp; ++i) {
+      launch_window_particles(s, h->sp[i], h->d_cnt + i, h->d_inj, rec, i, rc, h->d_err, h->nblocks);
+      count_launch(h, 3);
+    }
+    launch_shift_fields(s, F, h->cols, rec, 0, rc);
+    launch_shift_fields(s, F, h->cols, rec, 1, rc);
+    count_launch(h, 2);
+  }
+}
+
+// Counting sort of every species by cell; xgm points at the device copy of
+// the current x_grid_min (the grid moves with the window).
+static void enqueue_sort(Handle* h, const double* xgm) {
+  for (int i = 0; i < h->nsp; ++i) {
+    sort_species(h->st, h->sp[i], h->d_cnt + i, h->sc, xgm, h->rc, h->nblocks);
+    count_launch(h, 7);
+  }
+}
+
+static int alloc_species(Handle* h, int i, const cyl_species_desc& d) {
+  SpeciesPtrs& p = h->sp[i];
+  const int64_t cap = d.capacity > 0 ? d.capacity : 1;
+  double* buf = nullptr;
+  if (cudaMalloc(&buf, (size_t)cap * 8 * sizeof(double)) != cudaSuccess) return CYL_ERR_OUT_OF_MEMORY;
+  p.x = buf;
+  p.y = buf + cap;
+  p.z = buf + 2 * cap;
+  p.px = buf + 3 * cap;
+  p.py = buf + 4 * cap;
+  p.pz = buf + 5 * cap;
+  p.w = buf + 6 * cap;
+  p.id = (int64_t*)(buf + 7 * cap);
+  p.cap = cap;
+  p.charge = d.charge;
+  p.mass = d.mass;
+  p.immobile = d.immobile;
+  for (int k = 0; k < 4; ++k) p.bc[k] = map_particle_bc(d.bc_particle[k]);
+  return CYL_OK;
+}
+
+// Geometry tables of push_particles (particles.F90:189-217)
+static void make_geom(const HostGrid& g, std::vector<double>& out) {
+  const int ny = g.ny, n1 = ny + 2 * JNG, n0 = ny + 2 * JNG + 1;
+  out.assign((size_t)n1 * 3 + n0, 0.0);
+  double* rt = out.data();
+  double* xt = rt + n1;
+  double* vol = xt + n0;
+  double* rat = vol + n1;
+  const double dy = g.dy, dx = g.dx;
+  double r_low = g.y_grid_min - JNG * dy;
+  xt[0] = 1.0 / (2.0 * PI * std::fabs(r_low) * dx);
+  for (int iy = 1 - JNG; iy <= ny + JNG; ++iy) {
+    if (std::nearbyint(2.0 * r_low / dy) == -1.0)
+      rt[iy - (1 - JNG)] = 1.0 / (PI * ((0.5 * dy) * (0.5 * dy)));
+    else
+      rt[iy - (1 - JNG)] = 1.0 / (PI * std::fabs((r_low + dy) * (r_low + dy) - r_low * r_low));
+    xt[iy - (0 - JNG)] = 1.0 / (2.0 * PI * std::fabs(r_low + dy) * dx);
+    r_low = r_low + dy;
+  }
+  for (int iy = 1 - JNG; iy <= ny + JNG; ++iy) {
+    vol[iy - (1 - JNG)] = rt[iy - (1 - JNG)] / dx;
+    rat[iy - (1 - JNG)] = xt[iy - (0 - JNG)] / xt[iy - 1 - (0 - JNG)];
+  }
+}
+
+static int sync_and_check(Handle* h) {
+  CK(cudaStreamSynchronize(h->st));
+  int err = 0;
+  CK(cudaMemcpy(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err) return CYL_ERR_DEVICE_FLAG;
+  return CYL_OK;
+}
+
+static void collect_push_timing(Handle* h, int nsteps) {
+  for (int k = 0; k < nsteps; ++k) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, h->ev_push[k][0], h->ev_push[k][1]) == cudaSuccess) {
+      h->push_ms_sum += ms;
+      h->push_launches += 1;
+    }
+  }
+}
+
+static int run_chunk(Handle* h, int k, bool use_graph) {
+  // staging buffers are reused: wait until the previous chunk's copies are done
+  if (h->copy_pending) CK(cudaEventSynchronize(h->ev_copy));
+  int64_t inj_used = 0;
+  for (int i = 0; i < k; ++i) prepare_step(h, i, inj_used);
+  CK(cudaMemcpyAsync(h->d_rec, h->h_rec, sizeof(StepRec) * k, cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(h->d_src, h->h_src, sizeof(double) * h->src_per_step * k, cudaMemcpyHostToDevice, h->st));
+  if (inj_used > 0)
+    CK(cudaMemcpyAsync(h->d_inj, h->h_inj, sizeof(double) * 8 * inj_used, cudaMemcpyHostToDevice, h->st));
+  CK(cudaEventRecord(h->ev_copy, h->st));
+  h->copy_pending = true;
+  const double* xgm = &h->d_rec[k - 1].x_grid_min_after;
+  if (use_graph && k == CHUNK) {
+    const int par0 = h->jpar;
+    if (!h->gexec || h->graph_parity != par0) {
+      if (h->gexec) {
+        cudaGraphExecDestroy(h->gexec);
+        h->gexec = nullptr;
+      }
+      cudaGraph_t graph;
+      const int64_t launches0 = h->kernel_launches;
+      CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+      for (int i = 0; i < k; ++i)
+        enqueue_step(h, h->d_rec + i, h->d_src + h->src_per_step * i, i, true, true);
+      enqueue_sort(h, xgm);
+      CK(cudaStreamEndCapture(h->st, &graph));
+      CK(cudaGraphInstantiate(&h->gexec, graph, 0));
+      cudaGraphDestroy(graph);
+      h->graph_parity = par0;
+      h->graph_launches = h->kernel_launches - launches0;
+      h->kernel_launches = launches0;
+      h->jpar = par0;
+    }
+    CK(cudaGraphLaunch(h->gexec, h->st));
+    h->kernel_launches += h->graph_launches;
+    // a chunk swaps J and J_old an even number of times
+    h->jpar = h->graph_parity ^ (CHUNK & 1);
+  } else {
+    for (int i = 0; i < k; ++i)
+      enqueue_step(h, h->d_rec + i, h->d_src + h->src_per_step * i, i, true, false);
+    enqueue_sort(h, xgm);
+  }
+  CK(cudaEventSynchronize(h->ev_push[k - 1][1]));
+  collect_push_timing(h, k);
+  return CYL_OK;
+}
+
+}  // namespace cyl
+
+using namespace cyl;
+
+struct cyl_handle_s {
+  Handle h;
+};
+
+extern "C" {
+
+int cyl_create(const cyl_grid_desc* gd, const cyl_species_desc* spd, int32_t nsp,
+               const cyl_laser_desc* las, int32_t nlas, const cyl_rng_state* rng, cyl_handle* out) {
+  if (!gd || !out || (nsp > 0 && !spd) || (nlas > 0 && !las)) return CYL_ERR_BAD_ARG;
+  if (gd->nx < 8 || gd->ny < 8 || gd->n_mode < 1 || gd->n_mode > MAX_MODES) return CYL_ERR_BAD_ARG;
+  if (nsp < 0 || nsp > MAX_SPECIES || nlas < 0 || nlas > MAX_LASERS) return CYL_ERR_BAD_ARG;
+  if (!(gd->dt > 0.0) || !(gd->x_max > gd->x_min) || !(gd->y_max > 0.0)) return CYL_ERR_BAD_ARG;
+  if (gd->precision != CYL_PREC_FP64 && gd->precision != CYL_PREC_MIXED) return CYL_ERR_BAD_ARG;
+#ifndef CYL_WITH_MIXED
+  if (gd->precision == CYL_PREC_MIXED) return CYL_ERR_UNSUPPORTED;
+#endif
+  for (int i = 0; i < nlas; ++i) {
+    if (las[i].boundary != CYL_BD_X_MIN && las[i].boundary != CYL_BD_X_MAX) return CYL_ERR_UNSUPPORTED;
+    if (!las[i].profile || !las[i].phase) return CYL_ERR_BAD_ARG;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return CYL_ERR_NO_DEVICE;
+  cyl_handle_s* hs = new cyl_handle_s();
+  Handle* h = &hs->h;
+  cudaGetDevice(&h->device);
+  h->gd = *gd;
+  h->prec = gd->precision;
+  h->g.init(*gd);
+  RunConst& rc = h->rc;
+  rc.nx = gd->nx;
+  rc.ny = gd->ny;
+  rc.M = gd->n_mode;
+  rc.nxg = gd->nx + 2 * NG;
+  rc.nyg = gd->ny + 2 * NG;
+  rc.dx = h->g.dx;
+  rc.dy = h->g.dy;
+  rc.dt = gd->dt;
+  rc.y_grid_min = h->g.y_grid_min;
+  rc.y_max = h->g.y_max;
+  rc.y_max_local = h->g.y_max_local;
+  rc.length_x = h->g.length_x;
+  rc.length_y = h->g.length_y;
+  for (int i = 0; i < 4; ++i) {
+    h->bc_deck[i] = gd->bc_field[i];
+    h->bc_after_move[i] = gd->bc_after_move[i];
+  }
+  setup_boundaries(h);
+  h->move_window = gd->move_window != 0;
+  h->window_v_x = gd->window_v_x;
+  h->window_start_time = gd->window_start_time;
+  h->window_stop_time = gd->window_stop_time;
+  h->nsp = nsp;
+  int rcode = CYL_OK;
+  for (int i = 0; i < nsp; ++i) {
+    h->sd[i] = spd[i];
+    for (int k = 0; k < 4; ++k) {
+      int b = map_particle_bc(spd[i].bc_particle[k]);
+      if (k != CYL_BD_Y_MIN && b != CYL_BC_PERIODIC && b != CYL_BC_REFLECT && b != CYL_BC_OPEN)
+        rcode = CYL_ERR_UNSUPPORTED;
+    }
+  }
+  // bc_allspecies (deck_species_block.F90:182-199)
+  for (int idx = 0; idx < 4; ++idx) {
+    h->bc_allspecies[idx] = CYL_BC_OPEN;
+    for (int i = 0; i < nsp; ++i) {
+      int b = map_particle_bc(spd[i].bc_particle[idx]);
+      if (b != CYL_BC_REFLECT && b != CYL_BC_PERIODIC) b = CYL_BC_OPEN;
+      if (i == 0) h->bc_allspecies[idx] = b;
+      else if (h->bc_allspecies[idx] != b) rcode = CYL_ERR_UNSUPPORTED;  // mixed per-species bcs
+    }
+    rc.bc_allspecies[idx] = h->bc_allspecies[idx];
+  }
+  if (rcode != CYL_OK) {
+    delete hs;
+    return rcode;
+  }
+  for (int i = 0; i < nlas; ++i) {
+    HostLaser L;
+    L.d = las[i];
+    L.profile.assign(las[i].profile, las[i].profile + gd->ny + 1);
+    L.phase.assign(las[i].phase, las[i].phase + gd->ny + 1);
+    L.d.profile = nullptr;
+    L.d.phase = nullptr;
+    h->lasers.push_back(L);
+  }
+  if (rng) h->rng.from_state(rng);
+  else h->rng.seed(7842432);
+
+  cudaError_t e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete hs;
+    return CYL_ERR_CUDA;
+  }
+  int nsm = 152;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device);
+  h->nblocks = nsm * 8;
+  // fields: 15 arrays + one work array, one allocation
+  h->fcount = (size_t)rc.nxg * rc.nyg * rc.M;
+  if (cudaMalloc(&h->fbuf, h->fcount * 16 * sizeof(cplx)) != cudaSuccess) {
+    cyl_destroy((cyl_handle)hs);
+    return CYL_ERR_OUT_OF_MEMORY;
+  }
+  cudaMemset(h->fbuf, 0, h->fcount * 16 * sizeof(cplx));
+  for (int k = 0; k < 16; ++k) h->F[k] = h->fbuf + h->fcount * k;
+  const size_t ncolv = (size_t)(rc.ny + 2 * NG) * rc.M;
+  cudaMalloc(&h->cols, ncolv * 12 * sizeof(cplx));
+  cudaMemset(h->cols, 0, ncolv * 12 * sizeof(cplx));
+  std::vector<double> geo;
+  make_geom(h->g, geo);
+  cudaMalloc(&h->geom_buf, geo.size() * sizeof(double));
+  cudaMemcpy(h->geom_buf, geo.data(), geo.size() * sizeof(double), cudaMemcpyHostToDevice);
+  {
+    const int n1 = rc.ny + 2 * JNG, n0 = n1 + 1;
+    h->geom.inv_area_rt = h->geom_buf;
+    h->geom.inv_area_xt = h->geom_buf + n1;
+    h->geom.inv_volume = h->geom_buf + n1 + n0;
+    h->geom.ratio_area_xt = h->geom_buf + 2 * n1 + n0;
+  }
+  int64_t maxcap = 1;
+  for (int i = 0; i < nsp; ++i) {
+    if (alloc_species(h, i, spd[i]) != CYL_OK) {
+      cyl_destroy((cyl_handle)hs);
+      return CYL_ERR_OUT_OF_MEMORY;
+    }
+    if (h->sp[i].cap > maxcap) maxcap = h->sp[i].cap;
+  }
+  cudaMalloc(&h->d_cnt, sizeof(SpeciesCounters) * MAX_SPECIES);
+  cudaMemset(h->d_cnt, 0, sizeof(SpeciesCounters) * MAX_SPECIES);
+  // sort scratch: keys, histogram, block sums, 7 doubles + id per particle
+  h->sc.ncells = rc.nxg * rc.nyg;
+  h->sc.cap = maxcap;
+  const size_t sort_bytes = (size_t)maxcap * (4 + 8 * 8) + (size_t)(h->sc.ncells + 2) * 4 +
+                            (size_t)((h->sc.ncells + 4096) / 4096 + 64) * 8;
+  if (cudaMalloc(&h->sort_buf, sort_bytes) != cudaSuccess) {
+    cyl_destroy((cyl_handle)hs);
+    return CYL_ERR_OUT_OF_MEMORY;
+  }
+  {
+    char* p = (char*)h->sort_buf;
+    h->sc.tmp = (double*)p;
+    p += (size_t)maxcap * 7 * 8;
+    h->sc.tmp_id = (int64_t*)p;
+    p += (size_t)maxcap * 8;
+    h->sc.perm = (int64_t*)p;
+    p += (size_t)((h->sc.ncells + 4096) / 4096 + 64) * 8;
+    h->sc.keys = (int32_t*)p;
+    p += (size_t)maxcap * 4;
+    h->sc.hist = (int32_t*)p;
+  }
+  cudaMalloc(&h->d_err, sizeof(int));
+  cudaMemset(h->d_err, 0, sizeof(int));
+  cudaMalloc(&h->d_red, 8 * sizeof(double));
+  // staging for CHUNK steps
+  h->src_per_step = (size_t)4 * (rc.ny + 1);
+  int64_t per_step_inj = 0;
+  const double shifts_max = std::floor(gd->dt * std::fabs(gd->window_v_x) / h->g.dx) + 1.0;
+  for (int i = 0; i < nsp; ++i)
+    per_step_inj += (int64_t)(shifts_max * (double)rc.ny * (std::floor(spd[i].npart_per_cell) + 1.0));
+  h->inj_cap = h->move_window ? per_step_inj * CHUNK + 1 : 1;
+  cudaMallocHost(&h->h_rec, sizeof(StepRec) * CHUNK);
+  cudaMalloc(&h->d_rec, sizeof(StepRec) * (CHUNK + 1));
+  cudaMallocHost(&h->h_src, sizeof(double) * h->src_per_step * CHUNK);
+  cudaMalloc(&h->d_src, sizeof(double) * h->src_per_step * CHUNK);
+  cudaMallocHost(&h->h_inj, sizeof(double) * 8 * h->inj_cap);
+  cudaMalloc(&h->d_inj, sizeof(double) * 8 * h->inj_cap);
+  cudaEventCreateWithFlags(&h->ev_copy, cudaEventDisableTiming);
+  for (int k = 0; k < CHUNK; ++k) {
+    cudaEventCreate(&h->ev_push[k][0]);
+    cudaEventCreate(&h->ev_push[k][1]);
+  }
+  if (cudaDeviceSynchronize() != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+    cyl_destroy((cyl_handle)hs);
+    return CYL_ERR_OUT_OF_MEMORY;
+  }
+  *out = (cyl_handle)hs;
+  return CYL_OK;
+}
+
+int cyl_destroy(cyl_handle hh) {
+  if (!hh) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  if (h->st) cudaStreamSynchronize(h->st);
+  if (h->gexec) cudaGraphExecDestroy(h->gexec);
+  for (int i = 0; i < h->nsp; ++i)
+    if (h->sp[i].x) cudaFree(h->sp[i].x);
+  cudaFree(h->fbuf);
+  cudaFree(h->cols);
+  cudaFree(h->geom_buf);
+  cudaFree(h->d_cnt);
+  cudaFree(h->sort_buf);
+  cudaFree(h->d_err);
+  cudaFree(h->d_red);
+  cudaFreeHost(h->h_rec);
+  cudaFree(h->d_rec);
+  cudaFreeHost(h->h_src);
+  cudaFree(h->d_src);
+  cudaFreeHost(h->h_inj);
+  cudaFree(h->d_inj);
+  if (h->ev_copy) cudaEventDestroy(h->ev_copy);
+  for (int k = 0; k < CHUNK; ++k) {
+    if (h->ev_push[k][0]) cudaEventDestroy(h->ev_push[k][0]);
+    if (h->ev_push[k][1]) cudaEventDestroy(h->ev_push[k][1]);
+  }
+  if (h->st) cudaStreamDestroy(h->st);
+  delete hh;
+  return CYL_OK;
+}
+
+int cyl_upload_particles(cyl_handle hh, int32_t isp, const double* x, const double* y, const double* z,
+                         const double* px, const double* py, const double* pz, const double* w,
+                         const int64_t* id, int64_t n) {
+  if (!hh) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  if (isp < 0 || isp >= h->nsp || n < 0) return CYL_ERR_BAD_ARG;
+  if (n > 0 && (!x || !y || !z || !px || !py || !pz || !w || !id)) return CYL_ERR_BAD_ARG;
+  SpeciesPtrs& p = h->sp[isp];
+  if (n > p.cap) return CYL_ERR_CAPACITY;
+  cudaStream_t s = h->st;
+  const size_t b = (size_t)n * 8;
+  if (n > 0) {
+    CK(cudaMemcpyAsync(p.x, x, b, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(p.y, y, b, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(p.z, z, b, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(p.px, px, b, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(p.py, py, b, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(p.pz, pz, b, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(p.w, w, b, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(p.id, id, b, cudaMemcpyHostToDevice, s));
+  }
+  SpeciesCounters c{n, 0};
+  CK(cudaMemcpyAsync(h->d_cnt + isp, &c, sizeof(c), cudaMemcpyHostToDevice, s));
+  for (int64_t i = 0; i < n; ++i)
+    if (id[i] >= h->next_id) h->next_id = id[i] + 1;
+  CK(cudaStreamSynchronize(s));
+  return CYL_OK;
+}
+
+int cyl_download_particles(cyl_handle hh, int32_t isp, double* x, double* y, double* z, double* px,
+                           double* py, double* pz, double* w, int64_t* id, int64_t* n_inout) {
+  if (!hh || !n_inout) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  if (isp < 0 || isp >= h->nsp) return CYL_ERR_BAD_ARG;
+  CK(cudaStreamSynchronize(h->st));
+  SpeciesCounters c;
+  CK(cudaMemcpy(&c, h->d_cnt + isp, sizeof(c), cudaMemcpyDeviceToHost));
+  const int64_t n = c.n_used;
+  std::vector<double> buf((size_t)n * 8);
+  SpeciesPtrs& p = h->sp[isp];
+  double* srcs[7] = {p.x, p.y, p.z, p.px, p.py, p.pz, p.w};
+  for (int k = 0; k < 7; ++k)
+    CK(cudaMemcpy(buf.data() + (size_t)k * n, srcs[k], (size_t)n * 8, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(buf.data() + (size_t)7 * n, p.id, (size_t)n * 8, cudaMemcpyDeviceToHost));
+  int64_t live = 0;
+  for (int64_t i = 0; i < n; ++i)
+    if (!std::isnan(buf[i])) live++;
+  if (!x) {
+    *n_inout = live;
+    return CYL_OK;
+  }
+  if (*n_inout < live) return CYL_ERR_CAPACITY;
+  int64_t k = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    if (std::isnan(buf[i])) continue;
+    x[k] = buf[i];
+    y[k] = buf[n + i];
+    z[k] = buf[2 * n + i];
+    px[k] = buf[3 * n + i];
+    py[k] = buf[4 * n + i];
+    pz[k] = buf[5 * n + i];
+    w[k] = buf[6 * n + i];
+    std::memcpy(&id[k], &buf[7 * n + i], 8);
+    ++k;
+  }
+  *n_inout = k;
+  return CYL_OK;
+}
+
+int cyl_upload_field(cyl_handle hh, int32_t which, const double* data) {
+  if (!hh || !data || which < 0 || which >= CYL_NFIELDS) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  CK(cudaMemcpyAsync(h->F[field_slot(h, which)], data, h->fcount * sizeof(cplx), cudaMemcpyHostToDevice,
+                     h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return CYL_OK;
+}
+
+int cyl_download_field(cyl_handle hh, int32_t which, double* data) {
+  if (!hh || !data || which < 0 || which >= CYL_NFIELDS) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  CK(cudaStreamSynchronize(h->st));
+  CK(cudaMemcpy(data, h->F[field_slot(h, which)], h->fcount * sizeof(cplx), cudaMemcpyDeviceToHost));
+  return CYL_OK;
+}
+
+int cyl_initialise(cyl_handle hh) {
+  if (!hh) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  if (h->copy_pending) CK(cudaEventSynchronize(h->ev_copy));
+  StepRec& r = h->h_rec[0];
+  std::memset(&r, 0, sizeof(r));
+  fill_grid(r, h->g, false);
+  fill_grid(r, h->g, true);
+  for (int i = 0; i < 4; ++i) {
+    r.bc_field[i] = h->bc_field[i];
+    r.add_laser[i] = h->add_laser[i];
+    r.bc_field_after[i] = h->bc_field[i];
+  }
+  // epoch2d.F90:157-161: dt halved, time advanced by it, bfield_final_bcs
+  const double dt_half = h->g.dt / 2.0;
+  h->time = h->time + dt_half;
+  r.time_final = h->time;
+  laser_sources(h, h->h_src);
+  CK(cudaMemcpyAsync(h->d_rec, h->h_rec, sizeof(StepRec), cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(h->d_src, h->h_src, sizeof(double) * h->src_per_step, cudaMemcpyHostToDevice, h->st));
+  for (int i = 0; i < h->nsp; ++i) launch_particle_bcs(h->st, h->sp[i], h->d_cnt + i, h->d_rec, 0, h->rc, h->nblocks);
+  FieldSet F = fieldset(h, h->jpar);
+  launch_efield_bcs(h->st, F, h->d_rec, h->rc);
+  launch_b_final_bcs(h->st, F, h->d_rec, h->d_src, h->cols, 0, dt_half, h->rc);
+  return sync_and_check(h);
+}
+
+static int step_impl(cyl_handle hh, int32_t nsteps, bool graph) {
+  if (!hh || nsteps < 0) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  while (nsteps > 0) {
+    const int k = nsteps < CHUNK ? nsteps : CHUNK;
+    int r = run_chunk(h, k, graph);
+    if (r != CYL_OK) return r;
+    nsteps -= k;
+  }
+  return sync_and_check(h);
+}
+
+int cyl_step(cyl_handle hh, int32_t nsteps) { return step_impl(hh, nsteps, false); }
+int cyl_step_graph(cyl_handle hh, int32_t nsteps) { return step_impl(hh, nsteps, true); }
+
+int cyl_push_only(cyl_handle hh) {
+  if (!hh) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  if (h->copy_pending) CK(cudaEventSynchronize(h->ev_copy));
+  StepRec& r = h->h_rec[0];
+  std::memset(&r, 0, sizeof(r));
+  fill_grid(r, h->g, false);
+  fill_grid(r, h->g, true);
+  for (int i = 0; i < 4; ++i) r.bc_field[i] = r.bc_field_after[i] = h->bc_field[i];
+  CK(cudaMemcpyAsync(h->d_rec, h->h_rec, sizeof(StepRec), cudaMemcpyHostToDevice, h->st));
+  h->jpar ^= 1;
+  FieldSet F = fieldset(h, h->jpar);
+  const size_t bytes = h->fcount * sizeof(cplx);
+  cudaMemsetAsync(F.jx.p, 0, bytes, h->st);
+  cudaMemsetAsync(F.jr.p, 0, bytes, h->st);
+  cudaMemsetAsync(F.jt.p, 0, bytes, h->st);
+  CK(cudaEventRecord(h->ev_push[0][0], h->st));
+  for (int i = 0; i < h->nsp; ++i) {
+    if (h->sp[i].immobile) continue;
+    push_species(h, h->st, F, i, h->d_rec, 0);
+  }
+  CK(cudaEventRecord(h->ev_push[0][1], h->st));
+  CK(cudaEventSynchronize(h->ev_push[0][1]));
+  collect_push_timing(h, 1);
+  return sync_and_check(h);
+}
+
+int cyl_kernel_timing(cyl_handle hh, double* push_ms_avg, int64_t* launches) {
+  if (!hh) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  if (push_ms_avg) *push_ms_avg = h->push_launches ? h->push_ms_sum / (double)h->push_launches : 0.0;
+  if (launches) *launches = h->kernel_launches;
+  h->push_ms_sum = 0.0;
+  h->push_launches = 0;
+  h->kernel_launches = 0;
+  return CYL_OK;
+}
+
+int cyl_get_run_state(cyl_handle hh, cyl_run_state* out) {
+  if (!hh || !out) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  CK(cudaStreamSynchronize(h->st));
+  std::memset(out, 0, sizeof(*out));
+  out->time = h->time;
+  out->step = h->step;
+  out->x_grid_min = h->g.x_grid_min;
+  out->xb_min = h->g.xb_min;
+  out->x_min = h->g.x_min;
+  out->x_max = h->g.x_max;
+  out->window_shift_fraction = h->wsf;
+  out->window_started = h->window_started ? 1 : 0;
+  for (int i = 0; i < 4; ++i) out->bc_field[i] = h->bc_field[i];
+  SpeciesCounters c[MAX_SPECIES];
+  CK(cudaMemcpy(c, h->d_cnt, sizeof(SpeciesCounters) * MAX_SPECIES, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < h->nsp && i < 8; ++i) out->n_live[i] = c[i].n_used - c[i].n_dead;
+  out->n_shifts = h->n_shifts;
+  return CYL_OK;
+}
+
+int cyl_diagnostics(cyl_handle hh, cyl_diag* out) {
+  if (!hh || !out) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  CK(cudaMemsetAsync(h->d_red, 0, 8 * sizeof(double), h->st));
+  for (int i = 0; i < h->nsp; ++i) launch_energy(h->st, h->sp[i], h->d_cnt + i, h->d_red, h->nblocks);
+  launch_field_energy(h->st, fieldset(h, h->jpar), h->rc, h->d_red + 2);
+  double red[8];
+  CK(cudaMemcpyAsync(red, h->d_red, sizeof(red), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  int err = 0;
+  CK(cudaMemcpy(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  out->kinetic_energy = red[0];
+  out->n_live = (int64_t)(red[1] + 0.5);
+  out->field_energy_e = 0.5 * EPS0 * red[2];
+  out->field_energy_b = 0.5 / (4.0e-7 * PI) * red[3];
+  out->jsum_abs = red[4];
+  out->device_error = err;
+  return CYL_OK;
+}
+
+int cyl_get_rng_state(cyl_handle hh, cyl_rng_state* out) {
+  if (!hh || !out) return CYL_ERR_BAD_ARG;
+  hh->h.rng.to_state(out);
+  return CYL_OK;
+}
+
+int cyl_sort_particles(cyl_handle hh) {
+  if (!hh) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  CK(cudaMemcpyAsync(h->d_red + 7, &h->g.x_grid_min, sizeof(double), cudaMemcpyHostToDevice, h->st));
+  enqueue_sort(h, h->d_red + 7);
+  return sync_and_check(h);
+}
+
+int cyl_cell_indices(cyl_handle hh, int32_t isp, int32_t* cx, int32_t* cy, int64_t* n_inout) {
+  if (!hh || !n_inout) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  if (isp < 0 || isp >= h->nsp) return CYL_ERR_BAD_ARG;
+  CK(cudaStreamSynchronize(h->st));
+  SpeciesCounters c;
+  CK(cudaMemcpy(&c, h->d_cnt + isp, sizeof(c), cudaMemcpyDeviceToHost));
+  const int64_t n = c.n_used;
+  if (!cx) {
+    *n_inout = n - c.n_dead;
+    return CYL_OK;
+  }
+  int32_t* d = nullptr;
+  CK(cudaMalloc(&d, (size_t)n * 12 + 16));
+  launch_cell_indices(h->st, h->sp[isp], h->d_cnt + isp, h->g.x_grid_min, h->rc, d, d + n, d + 2 * n,
+                      h->nblocks);
+  std::vector<int32_t> b((size_t)n * 3);
+  cudaError_t e = cudaMemcpyAsync(b.data(), d, (size_t)n * 12, cudaMemcpyDeviceToHost, h->st);
+  cudaStreamSynchronize(h->st);
+  cudaFree(d);
+  if (e != cudaSuccess) return CYL_ERR_CUDA;
+  int64_t k = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    if (!b[2 * n + i]) continue;
+    if (k >= *n_inout) return CYL_ERR_CAPACITY;
+    cx[k] = b[i];
+    cy[k] = b[n + i];
+    ++k;
+  }
+  *n_inout = k;
+  return CYL_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,122 @@
+// cyl_common.cuh -- shared definitions of the GB300 quasi-3D PIC step.
+//
+// Complex arithmetic follows the operation trees of the reference Fortran
+// (gfortran evaluates left to right; a real operand of a complex product is
+// applied component-wise).  The FP64 kernels are compiled with --fmad=false
+// so each operation rounds once, as in the reference build.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/cylpic.h"
+
+#define CYL_HD __host__ __device__ __forceinline__
+
+namespace cyl {
+
+constexpr int NG = CYL_NG;  // ghost width of every mode array
+constexpr int JNG = CYL_NG;
+constexpr int PNG = 3;
+constexpr int MAX_SPECIES = 8;
+constexpr int MAX_LASERS = 8;
+constexpr int MAX_MODES = 8;
+
+// constants.F90:171-181
+constexpr double PI = 3.141592653589793238462643383279503;
+constexpr double CLIGHT = 2.99792458e8;
+constexpr double KB = 1.3806488e-23;
+constexpr double EPS0 = 8.854187817620389850536563031710750e-12;
+
+struct cplx {
+  double re, im;
+};
+CYL_HD cplx mk(double r, double i) { return {r, i}; }
+CYL_HD cplx operator+(cplx a, cplx b) { return {a.re + b.re, a.im + b.im}; }
+CYL_HD cplx operator-(cplx a, cplx b) { return {a.re - b.re, a.im - b.im}; }
+CYL_HD cplx operator-(cplx a) { return {-a.re, -a.im}; }
+CYL_HD cplx operator*(cplx a, cplx b) {
+  return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+CYL_HD cplx operator*(double s, cplx a) { return {s * a.re, s * a.im}; }
+CYL_HD cplx operator*(cplx a, double s) { return {a.re * s, a.im * s}; }
+CYL_HD cplx operator/(cplx a, double s) { return {a.re / s, a.im / s}; }
+CYL_HD cplx operator+(cplx a, double s) { return {a.re + s, a.im}; }
+CYL_HD cplx operator-(cplx a, double s) { return {a.re - s, a.im}; }
+CYL_HD cplx operator-(double s, cplx a) { return {s - a.re, -a.im}; }
+CYL_HD cplx operator+(double s, cplx a) { return {s + a.re, a.im}; }
+// 1/z by range-reduced (Smith) division, real numerator 1.
+CYL_HD cplx crecip(cplx z) {
+  double c = z.re, d = z.im;
+  if (fabs(c) < fabs(d)) {
+    double ratio = c / d;
+    double div = c * ratio + d;
+    return {(1.0 * ratio + 0.0) / div, (0.0 * ratio - 1.0) / div};
+  } else {
+    double ratio = d / c;
+    double div = d * ratio + c;
+    return {(0.0 * ratio + 1.0) / div, (0.0 - 1.0 * ratio) / div};
+  }
+}
+constexpr cplx IMAGI = {0.0, 1.0};
+
+// Layout of one complex mode array in HBM: Fortran order with ghosts,
+// F(1-ng:nx+ng, 1-ng:ny+ng, 0:M-1), element (re, im) as 16 bytes.
+struct FView {
+  cplx* p;
+  int nxg, nyg;
+  CYL_HD cplx& operator()(int ix, int iy, int m) const {
+    return p[(int64_t)(ix + NG - 1) + (int64_t)nxg * ((int64_t)(iy + NG - 1) + (int64_t)nyg * m)];
+  }
+};
+
+// Stagger table (setup.F90:126-136 with constants.F90:291-296).
+// which: 0 exm, 1 erm, 2 etm, 3 bxm, 4 brm, 5 btm
+CYL_HD bool stag_x(int w) { return w == 1 || w == 2 || w == 3; }
+CYL_HD bool stag_y(int w) { return w == 0 || w == 2 || w == 4; }
+
+// Scalars of one step, prepared on the host in the reference's order
+// (the Fortran module globals time, x_grid_min, bc_field, ... at the point
+// where each stage reads them).
+struct StepRec {
+  double time_half;          // time during update_eb_fields_half and the push
+  double time_final;         // time during update_eb_fields_final
+  double x_grid_min;         // grid of this step's push (before any shift)
+  double x_min, x_max;       // system extent before any shift
+  double x_min_local, x_max_local;
+  int32_t bc_field[4];       // field bcs during this step (after mapping)
+  int32_t add_laser[4];
+  int32_t nshift;            // window shifts at the end of the step
+  int32_t pad0;
+  int32_t bc_field_after[4]; // field bcs after moving_window's start switch
+  double x_grid_min_after;   // grid after the shifts
+  double x_min_after, x_max_after, x_min_local_after, x_max_local_after;
+  int64_t inject_off[MAX_SPECIES];  // offsets into the injection batch
+  int64_t inject_cnt[MAX_SPECIES];
+  int64_t src_off;           // offset of this step's laser source vectors
+};
+
+// Run-constant geometry and physics parameters (pushed by value).
+struct RunConst {
+  int nx, ny, M, nxg, nyg;
+  double dx, dy, dt;
+  double y_grid_min, y_max, y_max_local;
+  double length_x, length_y;
+  int bc_allspecies[4];
+};
+
+struct SpeciesPtrs {
+  double *x, *y, *z, *px, *py, *pz, *w;
+  int64_t* id;
+  int64_t cap;
+  double charge, mass;
+  int immobile;
+  int bc[4];
+};
+
+// Device error word bits.
+constexpr int ERR_CAPACITY = 1;
+constexpr int ERR_CELL_RANGE = 2;    // particle stencil left the ghosted grid
+constexpr int ERR_NONFINITE = 4;
+
+}  // namespace cyl

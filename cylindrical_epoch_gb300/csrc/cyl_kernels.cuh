@@ -1,0 +1,70 @@
+// cyl_kernels.cuh -- launch interface between the C ABI layer and the kernels.
+#pragma once
+
+#include "cyl_common.cuh"
+
+namespace cyl {
+
+struct FieldSet {
+  FView ex, er, et, bx, br, bt, jx, jr, jt, bxo, bro, bto, jxo, jro, jto;
+};
+
+// Geometry tables of push_particles (particles.F90:189-217), run constant.
+struct GeomTables {
+  const double* inv_area_rt;    // index iy - (1-jng)
+  const double* inv_area_xt;    // index iy - (0-jng)
+  const double* inv_volume;     // index iy - (1-jng)
+  const double* ratio_area_xt;  // index iy - (1-jng)
+};
+
+// Per-species counters kept on the device.
+struct SpeciesCounters {
+  int64_t n_used;  // slots in use (live + removed holes)
+  int64_t n_dead;  // removed particles still occupying a slot
+};
+
+// fields.cu
+void launch_update_e(cudaStream_t s, const FieldSet& F, const RunConst& rc);
+void launch_update_b(cudaStream_t s, const FieldSet& F, int save_old, const RunConst& rc);
+void launch_e_axis_bcs(cudaStream_t s, const FieldSet& F, const StepRec* rec, const RunConst& rc);
+void launch_efield_bcs(cudaStream_t s, const FieldSet& F, const StepRec* rec, const RunConst& rc);
+void launch_b_axis_bcs(cudaStream_t s, const FieldSet& F, const StepRec* rec, const RunConst& rc);
+void launch_b_final_bcs(cudaStream_t s, const FieldSet& F, const StepRec* rec, const double* src,
+                        const cplx* cols, int do_axis, double dt, const RunConst& rc);
+void launch_current_finish(cudaStream_t s, const FieldSet& F, const StepRec* rec, const RunConst& rc,
+                           int smooth, int its, int comp_its, int stride, FView wk);
+void launch_shift_fields(cudaStream_t s, const FieldSet& F, const cplx* cols, const StepRec* rec,
+                         int which, const RunConst& rc);
+
+// push_fp64.cu
+void launch_push_fp64(cudaStream_t s, const FieldSet& F, const GeomTables& g, const SpeciesPtrs& sp,
+                      SpeciesCounters* cnt, const StepRec* rec, const RunConst& rc, int apply_bcs,
+                      int* err, int nblocks);
+
+// particles.cu
+void launch_particle_bcs(cudaStream_t s, const SpeciesPtrs& sp, SpeciesCounters* cnt,
+                         const StepRec* rec, int after_shift, const RunConst& rc, int nblocks);
+void launch_window_particles(cudaStream_t s, const SpeciesPtrs& sp, SpeciesCounters* cnt,
+                             const double* inject, const StepRec* rec, int isp, const RunConst& rc,
+                             int* err, int nblocks);
+void launch_cell_indices(cudaStream_t s, const SpeciesPtrs& sp, const SpeciesCounters* cnt,
+                         double x_grid_min, const RunConst& rc, int32_t* cx, int32_t* cy,
+                         int32_t* live, int nblocks);
+void launch_energy(cudaStream_t s, const SpeciesPtrs& sp, const SpeciesCounters* cnt, double* out,
+                   int nblocks);
+void launch_field_energy(cudaStream_t s, const FieldSet& F, const RunConst& rc, double* out);
+// Counting sort of one species by cell; scratch holds the keys, histogram and
+// a second copy of the particle arrays.  Removes dead slots.
+struct SortScratch {
+  int32_t* keys;
+  int32_t* hist;     // ncells + 1
+  int64_t* perm;
+  double* tmp;       // 7 * cap doubles
+  int64_t* tmp_id;
+  int64_t cap;
+  int ncells;
+};
+void sort_species(cudaStream_t s, const SpeciesPtrs& sp, SpeciesCounters* cnt, SortScratch& sc,
+                  const double* x_grid_min, const RunConst& rc, int nblocks);
+
+}  // namespace cyl

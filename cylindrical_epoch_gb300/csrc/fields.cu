@@ -1,0 +1,742 @@
+// fields.cu -- per-mode r-z Yee update, r = 0 axis rules and field/current
+// boundary kernels of the quasi-3D step.
+//
+// Bulk updates (update_e_field / update_b_field bulk loops,
+// fields.f90:67-108, 203-241) are grid-wide elementwise kernels over
+// (ix, ir, m), coalesced along x.  Everything that touches only ghost slabs,
+// the axis rows or one boundary column (axis rules fields.f90:116-180,
+// 249-310; efield_bcs / bfield_bcs / bfield_final_bcs boundary.F90:1355-1537;
+// laser.f90:411-690; current_bcs_r_min_final boundary.F90:1909-1959;
+// current_finish current_smooth.F90:29-45) is O(perimeter) work whose
+// sub-steps depend on each other at the domain corners; each such call is one
+// single-CTA kernel whose phases are separated by __syncthreads, in the
+// reference's order.
+#include "cyl_common.cuh"
+#include "cyl_kernels.cuh"
+
+namespace cyl {
+
+// ----------------------------------------------------------------- bulk
+
+__global__ void k_update_e(FView ex, FView er, FView et, FView bx, FView br, FView bt,
+                           FView jx, FView jr, FView jt, RunConst rc) {
+  const int ix = blockIdx.x * blockDim.x + threadIdx.x;  // 0..nx
+  const int ir = 1 + blockIdx.y;                         // 1..ny
+  const int im = blockIdx.z;
+  if (ix > rc.nx) return;
+  const double dx = rc.dx, dy = rc.dy, dt = rc.dt, c2 = CLIGHT * CLIGHT;
+  const double r_d = fabs((double)(ir - 1) * dy + rc.y_grid_min);
+  const double r_p = r_d + 0.5 * dy;
+  const double fac_x = c2 / r_p;
+  const cplx im_fac_x = (IMAGI * (double)im) * fac_x;
+  const cplx im_fac_r = ((IMAGI * (double)im) * c2) / r_d;
+  const cplx bt0 = bt(ix, ir, im), bt1 = bt(ix, ir + 1, im), btx = bt(ix + 1, ir, im);
+  const cplx br0 = br(ix, ir, im), brx = br(ix + 1, ir, im);
+  const cplx bx0 = bx(ix, ir, im), bx1 = bx(ix, ir + 1, im);
+  ex(ix, ir, im) = ex(ix, ir, im) +
+      ((((fac_x * 0.5) * (bt1 + bt0) + im_fac_x * br0) + (c2 * (bt1 - bt0)) / dy) -
+       jx(ix, ir, im) / EPS0) * 0.5 * dt;
+  er(ix, ir, im) = er(ix, ir, im) +
+      ((-(im_fac_r * bx0) - (c2 * (btx - bt0)) / dx) - jr(ix, ir, im) / EPS0) * 0.5 * dt;
+  et(ix, ir, im) = et(ix, ir, im) +
+      (((c2 * (brx - br0)) / dx - (c2 * (bx1 - bx0)) / dy) - jt(ix, ir, im) / EPS0) * 0.5 * dt;
+}
+
+// B update over the whole ghosted array: optionally saves B into B_old
+// (fields.f90:326-328), then updates ix = 0..nx, ir = 1..ny-1 (y_max_boundary).
+__global__ void k_update_b(FView ex, FView er, FView et, FView bx, FView br, FView bt,
+                           FView bxo, FView bro, FView bto, int save_old, RunConst rc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;  // 0..nxg-1
+  const int j = blockIdx.y;                             // 0..nyg-1
+  const int im = blockIdx.z;
+  if (i >= rc.nxg) return;
+  const int ix = i + 1 - NG, ir = j + 1 - NG;
+  if (save_old) {
+    bxo(ix, ir, im) = bx(ix, ir, im);
+    bro(ix, ir, im) = br(ix, ir, im);
+    bto(ix, ir, im) = bt(ix, ir, im);
+  }
+  if (ix < 0 || ix > rc.nx || ir < 1 || ir > rc.ny - 1) return;
+  const double dx = rc.dx, dy = rc.dy, dt = rc.dt;
+  const double r_d = fabs((double)(ir - 1) * dy + rc.y_grid_min);
+  const double r_p = r_d + 0.5 * dy;
+  const cplx im_fac_x = (IMAGI * (double)im) / r_d;
+  const cplx im_fac_r = (IMAGI * (double)im) / r_p;
+  const cplx et0 = et(ix, ir, im), etm1 = et(ix, ir - 1, im), etxm = et(ix - 1, ir, im);
+  const cplx er0 = er(ix, ir, im), erxm = er(ix - 1, ir, im);
+  const cplx ex0 = ex(ix, ir, im), exm1 = ex(ix, ir - 1, im);
+  bx(ix, ir, im) = bx(ix, ir, im) -
+      ((im_fac_x * er0 + (0.5 * (et0 + etm1)) / r_d) + (et0 - etm1) / dy) * 0.5 * dt;
+  br(ix, ir, im) = br(ix, ir, im) + (im_fac_r * ex0 + (et0 - etxm) / dx) * 0.5 * dt;
+  bt(ix, ir, im) = bt(ix, ir, im) + (-((er0 - erxm) / dx) + (ex0 - exm1) / dy) * 0.5 * dt;
+}
+
+// --------------------------------------------------- single-CTA helpers
+
+constexpr int CTA_THREADS = 512;
+#define CTA_FOR(var, n) for (int var = threadIdx.x; var < (n); var += blockDim.x)
+
+// halo_x: periodic-x self wrap of rows [j0, j1] (boundary.F90:500-593 on one rank)
+__device__ void halo_x(FView f, int j0, int j1, const int* bcf, const RunConst& rc) {
+  const int nrow = j1 - j0 + 1;
+  if (bcf[CYL_BD_X_MAX] == CYL_BC_PERIODIC) {
+    CTA_FOR(t, nrow * rc.M * NG) {
+      int i = 1 + t % NG, r = t / NG;
+      int j = j0 + r % nrow, m = r / nrow;
+      f(rc.nx + i, j, m) = f(i, j, m);
+    }
+  }
+  __syncthreads();
+  if (bcf[CYL_BD_X_MIN] == CYL_BC_PERIODIC) {
+    CTA_FOR(t, nrow * rc.M * NG) {
+      int i = 1 - NG + t % NG, r = t / NG;
+      int j = j0 + r % nrow, m = r / nrow;
+      f(i, j, m) = f(rc.nx + i, j, m);
+    }
+  }
+  __syncthreads();
+}
+
+// field_mode_zero_gradient (boundary.F90:654-707) on one boundary
+__device__ void zero_gradient(FView f, int st, int bd, const int* bcf, const RunConst& rc) {
+  if (bcf[bd] == CYL_BC_PERIODIC) return;
+  const int nx = rc.nx, ny = rc.ny, M = rc.M;
+  if (bd == CYL_BD_X_MIN || bd == CYL_BD_X_MAX) {
+    const int nrow = ny + 2 * NG;
+    CTA_FOR(t, nrow * M) {
+      int j = 1 - NG + t % nrow, m = t / nrow;
+      if (bd == CYL_BD_X_MIN) {
+        if (stag_x(st)) for (int i = 1; i <= NG - 1; ++i) f(i - NG, j, m) = f(NG - i, j, m);
+        else for (int i = 1; i <= NG; ++i) f(i - NG, j, m) = f(NG + 1 - i, j, m);
+      } else {
+        if (stag_x(st)) for (int i = 1; i <= NG - 1; ++i) f(nx + i, j, m) = f(nx - i, j, m);
+        else for (int i = 1; i <= NG; ++i) f(nx + i, j, m) = f(nx + 1 - i, j, m);
+      }
+    }
+  } else if (bd == CYL_BD_Y_MAX) {
+    const int ncol = nx + 2 * NG;
+    CTA_FOR(t, ncol * M) {
+      int ix = 1 - NG + t % ncol, m = t / ncol;
+      if (stag_y(st)) for (int i = 1; i <= NG - 1; ++i) f(ix, ny + i, m) = f(ix, ny - i, m);
+      else for (int i = 1; i <= NG; ++i) f(ix, ny + i, m) = f(ix, ny + 1 - i, m);
+    }
+  }
+}
+
+// field_mode_clamp_zero (boundary.F90:772-829) on one boundary
+__device__ void clamp_zero(FView f, int st, int bd, const int* bcf, const RunConst& rc) {
+  if (bcf[bd] == CYL_BC_PERIODIC) return;
+  const int nx = rc.nx, ny = rc.ny, M = rc.M;
+  const cplx Z = mk(0.0, 0.0);
+  if (bd == CYL_BD_X_MIN || bd == CYL_BD_X_MAX) {
+    const int nrow = ny + 2 * NG;
+    CTA_FOR(t, nrow * M) {
+      int j = 1 - NG + t % nrow, m = t / nrow;
+      if (bd == CYL_BD_X_MIN) {
+        if (stag_x(st)) {
+          for (int i = 1; i <= NG - 1; ++i) f(i - NG, j, m) = -f(NG - i, j, m);
+          f(0, j, m) = Z;
+        } else {
+          for (int i = 1; i <= NG; ++i) f(i - NG, j, m) = -f(NG + 1 - i, j, m);
+        }
+      } else {
+        if (stag_x(st)) {
+          f(nx, j, m) = Z;
+          for (int i = 1; i <= NG - 1; ++i) f(nx + i, j, m) = -f(nx - i, j, m);
+        } else {
+          for (int i = 1; i <= NG; ++i) f(nx + i, j, m) = -f(nx + 1 - i, j, m);
+        }
+      }
+    }
+  } else if (bd == CYL_BD_Y_MAX) {
+    const int ncol = nx + 2 * NG;
+    CTA_FOR(t, ncol * M) {
+      int ix = 1 - NG + t % ncol, m = t / ncol;
+      if (stag_y(st)) {
+        f(ix, ny, m) = Z;
+        for (int i = 1; i <= NG - 1; ++i) f(ix, ny + i, m) = -f(ix, ny - i, m);
+      } else {
+        for (int i = 1; i <= NG; ++i) f(ix, ny + i, m) = -f(ix, ny + 1 - i, m);
+      }
+    }
+  }
+}
+
+// efield_bcs (boundary.F90:1355-1413)
+__device__ void efield_bcs_dev(FView ex, FView er, FView et, const int* bcf, const RunConst& rc) {
+  __syncthreads();
+  halo_x(ex, 1 - NG, rc.ny + NG - 1, bcf, rc);
+  halo_x(er, 1 - NG, rc.ny + NG, bcf, rc);
+  halo_x(et, 1 - NG, rc.ny + NG - 1, bcf, rc);
+  for (int i = CYL_BD_X_MIN; i <= CYL_BD_X_MAX; ++i) {
+    if (bcf[i] == CYL_BC_CONDUCT) {
+      clamp_zero(ex, 0, i, bcf, rc);
+      zero_gradient(er, 1, i, bcf, rc);
+      zero_gradient(et, 2, i, bcf, rc);
+    }
+    __syncthreads();
+  }
+  if (bcf[CYL_BD_Y_MAX] == CYL_BC_CONDUCT) {
+    zero_gradient(ex, 0, CYL_BD_Y_MAX, bcf, rc);
+    clamp_zero(er, 1, CYL_BD_Y_MAX, bcf, rc);
+    zero_gradient(et, 2, CYL_BD_Y_MAX, bcf, rc);
+  }
+  __syncthreads();
+  for (int i = 0; i < 4; ++i) {
+    if (i == CYL_BD_Y_MIN) continue;
+    int b = bcf[i];
+    if (b == CYL_BC_CLAMP || b == CYL_BC_SIMPLE_LASER || b == CYL_BC_SIMPLE_OUTFLOW) {
+      clamp_zero(ex, 0, i, bcf, rc);
+      clamp_zero(er, 1, i, bcf, rc);
+      clamp_zero(et, 2, i, bcf, rc);
+    }
+    if (b == CYL_BC_ZERO_GRADIENT) {
+      zero_gradient(ex, 0, i, bcf, rc);
+      zero_gradient(er, 1, i, bcf, rc);
+      zero_gradient(et, 2, i, bcf, rc);
+    }
+    __syncthreads();
+  }
+}
+
+// bfield_bcs (boundary.F90:1417-1476)
+__device__ void bfield_bcs_dev(FView bx, FView br, FView bt, bool mpi_only, const int* bcf,
+                               const RunConst& rc) {
+  __syncthreads();
+  halo_x(bx, 1 - NG, rc.ny + NG, bcf, rc);
+  halo_x(br, 1 - NG, rc.ny + NG - 1, bcf, rc);
+  halo_x(bt, 1 - NG, rc.ny + NG, bcf, rc);
+  if (mpi_only) return;
+  for (int i = CYL_BD_X_MIN; i <= CYL_BD_X_MAX; ++i) {
+    if (bcf[i] == CYL_BC_CONDUCT) {
+      zero_gradient(bx, 3, i, bcf, rc);
+      clamp_zero(br, 4, i, bcf, rc);
+      clamp_zero(bt, 5, i, bcf, rc);
+    }
+    __syncthreads();
+  }
+  if (bcf[CYL_BD_Y_MAX] == CYL_BC_CONDUCT) {
+    clamp_zero(bx, 3, CYL_BD_Y_MAX, bcf, rc);
+    zero_gradient(br, 4, CYL_BD_Y_MAX, bcf, rc);
+    clamp_zero(bt, 5, CYL_BD_Y_MAX, bcf, rc);
+  }
+  __syncthreads();
+  for (int i = 0; i < 4; ++i) {
+    if (i == CYL_BD_Y_MIN) continue;
+    int b = bcf[i];
+    if (b == CYL_BC_CLAMP || b == CYL_BC_SIMPLE_LASER || b == CYL_BC_SIMPLE_OUTFLOW) {
+      clamp_zero(bx, 3, i, bcf, rc);
+      clamp_zero(br, 4, i, bcf, rc);
+      clamp_zero(bt, 5, i, bcf, rc);
+    }
+    if (b == CYL_BC_ZERO_GRADIENT) {
+      zero_gradient(bx, 3, i, bcf, rc);
+      zero_gradient(br, 4, i, bcf, rc);
+      zero_gradient(bt, 5, i, bcf, rc);
+    }
+    __syncthreads();
+  }
+}
+
+// Axis rules of update_e_field (fields.f90:116-180), one column per thread.
+__device__ void e_axis_dev(FView ex, FView er, FView et, FView jx, FView bt, const RunConst& rc) {
+  const int M = rc.M;
+  const double dy = rc.dy, dt = rc.dt, c2 = CLIGHT * CLIGHT;
+  const int ncol = rc.nx + 2 * NG;
+  CTA_FOR(t, ncol) {
+    const int ix = 1 - NG + t;
+    ex(ix, 0, 0) = ex(ix, 0, 0) + ((4.0 * c2 / dy) * bt(ix, 1, 0) - jx(ix, 0, 0) / EPS0) * 0.5 * dt;
+    et(ix, 0, 0) = mk(0.0, 0.0);
+    er(ix, 0, 0) = -er(ix, 1, 0);
+    for (int ir = 1 - NG; ir <= -1; ++ir) {
+      et(ix, ir, 0) = -et(ix, -ir, 0);
+      er(ix, ir, 0) = -er(ix, -ir + 1, 0);
+      ex(ix, ir, 0) = ex(ix, -ir, 0);
+    }
+    if (M > 1) {
+      ex(ix, 0, 1) = mk(0.0, 0.0);
+      er(ix, 0, 1) = (2.0 * IMAGI) * et(ix, 0, 1) - er(ix, 1, 1);
+      et(ix, 0, 1) = (-IMAGI / 8.0) * (9.0 * er(ix, 1, 1) - er(ix, 2, 1));
+      for (int ir = 1 - NG; ir <= -1; ++ir) {
+        et(ix, ir, 1) = et(ix, -ir, 1);
+        er(ix, ir, 1) = er(ix, -ir + 1, 1);
+        ex(ix, ir, 1) = -ex(ix, -ir, 1);
+      }
+    }
+    double mode_sign = 1.0;
+    for (int im = 2; im < M; ++im) {
+      ex(ix, 0, im) = mk(0.0, 0.0);
+      et(ix, 0, im) = mk(0.0, 0.0);
+      er(ix, 0, im) = -er(ix, 1, im);
+      er(ix, 1, im) = er(ix, 2, im) / 9.0;
+      for (int ir = 1 - NG; ir <= -1; ++ir) {
+        et(ix, ir, im) = (-mode_sign) * et(ix, -ir, im);
+        er(ix, ir, im) = (-mode_sign) * er(ix, -ir + 1, im);
+        ex(ix, ir, im) = mode_sign * ex(ix, -ir, im);
+      }
+      mode_sign = -mode_sign;
+    }
+  }
+}
+
+// Axis rules of update_b_field (fields.f90:249-310).
+__device__ void b_axis_dev(FView bx, FView br, FView bt, FView ex, FView et, const RunConst& rc) {
+  const int M = rc.M;
+  const double dx = rc.dx, dy = rc.dy, dt = rc.dt;
+  const int ncol = rc.nx + 2 * NG;
+  CTA_FOR(t, ncol) {
+    const int ix = 1 - NG + t;
+    br(ix, 0, 0) = mk(0.0, 0.0);
+    bx(ix, 0, 0) = bx(ix, 1, 0);
+    bt(ix, 0, 0) = -bt(ix, 1, 0);
+    for (int ir = 1 - NG; ir <= -1; ++ir) {
+      bt(ix, ir, 0) = -bt(ix, -ir + 1, 0);
+      br(ix, ir, 0) = -br(ix, -ir, 0);
+      bx(ix, ir, 0) = bx(ix, -ir + 1, 0);
+    }
+    if (M > 1) {
+      bx(ix, 0, 1) = -bx(ix, 1, 1);
+      if (ix >= 2 - NG)
+        br(ix, 0, 1) = br(ix, 0, 1) +
+            ((IMAGI / dy) * ex(ix, 0, 1) + (et(ix, 0, 1) - et(ix - 1, 0, 1)) / dx) * 0.5 * dt;
+      bt(ix, 0, 1) = (-2.0 * IMAGI) * br(ix, 0, 1) - bt(ix, 1, 1);
+      for (int ir = 1 - NG; ir <= -1; ++ir) {
+        bt(ix, ir, 1) = bt(ix, -ir + 1, 1);
+        br(ix, ir, 1) = br(ix, -ir, 1);
+        bx(ix, ir, 1) = -bx(ix, -ir + 1, 1);
+      }
+    }
+    double mode_sign = 1.0;
+    for (int im = 2; im < M; ++im) {
+      bx(ix, 0, im) = -bx(ix, 1, im);
+      br(ix, 0, im) = mk(0.0, 0.0);
+      bt(ix, 0, im) = -bt(ix, 1, im);
+      for (int ir = 1 - NG; ir <= -1; ++ir) {
+        bt(ix, ir, im) = (-mode_sign) * bt(ix, -ir + 1, im);
+        br(ix, ir, im) = (-mode_sign) * br(ix, -ir, im);
+        bx(ix, ir, im) = mode_sign * bx(ix, -ir + 1, im);
+      }
+      mode_sign = -mode_sign;
+    }
+  }
+}
+
+// update_e_field axis rules + efield_bcs (one CTA)
+__global__ void __launch_bounds__(CTA_THREADS) k_e_axis_bcs(FView ex, FView er, FView et, FView jx, FView bt,
+                             const StepRec* rec, RunConst rc) {
+  __shared__ int bcf[4];
+  if (threadIdx.x < 4) bcf[threadIdx.x] = rec->bc_field[threadIdx.x];
+  __syncthreads();
+  e_axis_dev(ex, er, et, jx, bt, rc);
+  efield_bcs_dev(ex, er, et, bcf, rc);
+}
+
+// update_b_field axis rules + bfield_bcs(.TRUE.) (one CTA)
+__global__ void __launch_bounds__(CTA_THREADS) k_b_axis_bcs(FView bx, FView br, FView bt, FView ex, FView et,
+                             const StepRec* rec, RunConst rc) {
+  __shared__ int bcf[4];
+  if (threadIdx.x < 4) bcf[threadIdx.x] = rec->bc_field[threadIdx.x];
+  __syncthreads();
+  b_axis_dev(bx, br, bt, ex, et, rc);
+  bfield_bcs_dev(bx, br, bt, true, bcf, rc);
+}
+
+// efield_bcs alone (start-up, epoch2d.F90:144)
+__global__ void __launch_bounds__(CTA_THREADS) k_efield_bcs(FView ex, FView er, FView et, const StepRec* rec, RunConst rc) {
+  __shared__ int bcf[4];
+  if (threadIdx.x < 4) bcf[threadIdx.x] = rec->bc_field[threadIdx.x];
+  __syncthreads();
+  efield_bcs_dev(ex, er, et, bcf, rc);
+}
+
+// update_b_field axis rules + bfield_final_bcs (boundary.F90:1505-1537),
+// with the x boundary laser / outflow (laser.f90:411-633) and r_max
+// outflow (laser.f90:637-690).  src holds this step's Cartesian laser
+// sources (source1, source2 for x_min then x_max, each ny+1 values), which
+// the host evaluates from the deck's time and transverse profiles.
+__global__ void __launch_bounds__(CTA_THREADS) k_b_axis_final_bcs(FieldSet F, const StepRec* rec, const double* src,
+                                   const cplx* cols, int do_axis, double dt, RunConst rc) {
+  __shared__ int bcf[4];
+  __shared__ int addl[4];
+  if (threadIdx.x < 4) {
+    bcf[threadIdx.x] = rec->bc_field[threadIdx.x];
+    addl[threadIdx.x] = rec->add_laser[threadIdx.x];
+  }
+  __syncthreads();
+  rc.dt = dt;
+  const int nx = rc.nx, ny = rc.ny, M = rc.M;
+  if (do_axis) b_axis_dev(F.bx, F.br, F.bt, F.ex, F.et, rc);
+  bfield_bcs_dev(F.bx, F.br, F.bt, false, bcf, rc);
+  __syncthreads();
+  const double c2 = CLIGHT * CLIGHT;
+  const double dtc2 = dt * c2, lx = dtc2 / rc.dx, lr = dtc2 / rc.dy;
+  const double sum = 1.0 / (lx + CLIGHT), diff = lx - CLIGHT, dt_eps = dt / EPS0;
+  const int ncolv = ny + 2 * NG;  // boundary column arrays are (1-ng:ny+ng, M)
+  for (int side = 0; side < 2; ++side) {
+    const int bd = side == 0 ? CYL_BD_X_MIN : CYL_BD_X_MAX;
+    if (!(addl[bd] || bcf[bd] == CYL_BC_SIMPLE_OUTFLOW)) continue;
+    // cols: 12 arrays [ex,er,et,bx,br,bt]_x_min then _x_max, each ncolv*M
+    const cplx* bxb = cols + (size_t)(side * 6 + 3) * ncolv * M;
+    const cplx* erb = cols + (size_t)(side * 6 + 1) * ncolv * M;
+    const cplx* etb = cols + (size_t)(side * 6 + 2) * ncolv * M;
+    const cplx* brb = cols + (size_t)(side * 6 + 4) * ncolv * M;
+    const cplx* btb = cols + (size_t)(side * 6 + 5) * ncolv * M;
+    const int xc = side == 0 ? 0 : nx;
+    CTA_FOR(t, (ny + 1) * M) {
+      int ir = t % (ny + 1), m = t / (ny + 1);
+      F.bx(xc, ir, m) = bxb[(ir + NG - 1) + ncolv * m];
+    }
+    __syncthreads();
+    const double* s1 = src + (size_t)side * 2 * (ny + 1);
+    const double* s2 = s1 + (ny + 1);
+    CTA_FOR(t, ny * M) {
+      const int ir = 1 + t % ny, m = t / ny;
+      const cplx imc = ((IMAGI * (double)m) * c2) * dt;
+      // Bt row: ir pairs with r_d_vals(ir-1) (whole array inside a 1:ny section)
+      const double rdv = fabs((double)(ir - 2) * rc.dy + rc.y_grid_min);
+      cplx nbt;
+      if (side == 0) {
+        cplx st = mk(0.0, 0.0);
+        if (m == 1) st = s1[ir] + IMAGI * s2[ir];
+        nbt = sum * (((((4.0 * st + 2.0 * (erb[(ir + NG - 1) + ncolv * m] + CLIGHT * btb[(ir + NG - 1) + ncolv * m])) -
+                        2.0 * F.er(1, ir, m)) +
+                       (imc * F.bx(1, ir, m)) / rdv) +
+                      dt_eps * F.jr(1, ir, m)) +
+                     diff * F.bt(2, ir, m));
+      } else {
+        // source_t whole array (0:ny) inside the 1:ny section: index ir-1
+        cplx st = mk(0.0, 0.0);
+        if (m == 1) st = s1[ir - 1] + IMAGI * s2[ir - 1];
+        nbt = sum * ((((((-4.0) * st - 2.0 * (erb[(ir + NG - 1) + ncolv * m] + CLIGHT * btb[(ir + NG - 1) + ncolv * m])) +
+                        2.0 * F.er(nx - 1, ir, m)) -
+                       (imc * F.bx(nx - 1, ir, m)) / rdv) -
+                      dt_eps * F.jr(nx - 1, ir, m)) +
+                     diff * F.bt(nx - 1, ir, m));
+      }
+      cplx nbr = mk(0.0, 0.0);
+      const bool do_br = ir <= ny - 1;
+      if (do_br) {
+        cplx sr = mk(0.0, 0.0);
+        if (m == 1) sr = (-IMAGI) * s1[ir] + s2[ir];
+        if (side == 0) {
+          nbr = sum * (((((((-4.0) * sr - 2.0 * (etb[(ir + NG - 1) + ncolv * m] + CLIGHT * brb[(ir + NG - 1) + ncolv * m])) +
+                           2.0 * F.et(1, ir, m)) -
+                          lr * (F.bx(1, ir + 1, m) - F.bx(1, ir, m))) -
+                         dt_eps * F.jt(1, ir, m)) +
+                        diff * F.br(2, ir, m)));
+        } else {
+          nbr = sum * (((((4.0 * sr + 2.0 * (etb[(ir + NG - 1) + ncolv * m] + CLIGHT * brb[(ir + NG - 1) + ncolv * m])) -
+                          2.0 * F.et(nx - 1, ir, m)) +
+                         lr * (F.bx(nx - 1, ir + 1, m) - F.bx(nx - 1, ir, m))) +
+                        dt_eps * F.jt(nx - 1, ir, m)) +
+                       diff * F.br(nx - 1, ir, m));
+        }
+      }
+      // every read above is of columns other than the one written below
+      if (side == 0) {
+        F.bt(1, ir, m) = nbt;
+        if (do_br) F.br(1, ir, m) = nbr;
+      } else {
+        F.bt(nx, ir, m) = nbt;
+        if (do_br) F.br(nx, ir, m) = nbr;
+      }
+    }
+    __syncthreads();
+  }
+  if (bcf[CYL_BD_Y_MAX] == CYL_BC_SIMPLE_OUTFLOW) {
+    // outflow_bcs_r_max (laser.f90:637-690)
+    const double inv_r = 1.0 / ((double)((float)ny - 1.5f) * rc.dy + rc.y_grid_min);
+    const double dtc2_4r = 0.25 * dtc2 * inv_r;
+    const cplx icdt_2r = ((0.5 * IMAGI) * CLIGHT) * dt * inv_r;
+    const double ly = dtc2 / rc.dy;
+    const double sum_x = 1.0 / (ly + CLIGHT), sum_t = 1.0 / ((ly + CLIGHT) + dtc2_4r);
+    const double dt_2eps = 0.5 * dt / EPS0;
+    // new values depend on row ny-1 and the old arrays only: compute, sync, store
+    const int n = nx * M;
+    for (int base = 0; base < n; base += blockDim.x) {
+      const int t = base + threadIdx.x;
+      cplx nbx = mk(0, 0), nbt = mk(0, 0);
+      int ix = 0, m = 0;
+      if (t < n) {
+        ix = 1 + t % nx;
+        m = t / nx;
+        const cplx icm = icdt_2r * (double)m;
+        if (ix <= nx - 1) {
+          cplx v = (-F.bx(ix, ny - 1, m)) * (CLIGHT - ly);
+          v = v - F.bxo(ix, ny, m) * ((-CLIGHT) + ly);
+          v = v - F.bxo(ix, ny - 1, m) * ((-CLIGHT) - ly);
+          v = v - ((CLIGHT * dt) * inv_r) * F.et(ix, ny - 1, m);
+          v = v + (0.5 * lx) * (((F.br(ix + 1, ny - 1, m) - F.br(ix, ny - 1, m)) + F.bro(ix + 1, ny - 1, m)) -
+                                F.bro(ix, ny - 1, m));
+          v = v - icm * (F.er(ix, ny, m) + F.er(ix, ny - 1, m));
+          v = v - dt_2eps * (F.jt(ix, ny - 1, m) + F.jto(ix, ny - 1, m));
+          nbx = sum_x * v;
+        }
+        cplx v = (-F.bt(ix, ny - 1, m)) * ((CLIGHT - ly) + dtc2_4r);
+        v = v - F.bto(ix, ny, m) * (((-CLIGHT) + ly) + dtc2_4r);
+        v = v - F.bto(ix, ny - 1, m) * (((-CLIGHT) - ly) + dtc2_4r);
+        v = v - ((0.5 * lx) / CLIGHT) * (((F.er(ix, ny, m) + F.er(ix, ny - 1, m)) - F.er(ix - 1, ny, m)) -
+                                         F.er(ix - 1, ny - 1, m));
+        v = v - (icm * CLIGHT) * (F.br(ix, ny - 1, m) + F.bro(ix, ny - 1, m));
+        v = v + dt_2eps * (F.jx(ix, ny - 1, m) + F.jxo(ix, ny - 1, m));
+        nbt = sum_t * v;
+      }
+      if (t < n) {
+        if (ix <= nx - 1) F.bx(ix, ny, m) = nbx;
+        F.bt(ix, ny, m) = nbt;
+      }
+    }
+  } else if (bcf[CYL_BD_Y_MAX] == CYL_BC_ZERO_B) {
+    CTA_FOR(t, (nx + 2 * NG) * M) {
+      int ix = 1 - NG + t % (nx + 2 * NG), m = t / (nx + 2 * NG);
+      F.bx(ix, ny, m) = mk(0, 0);
+      F.br(ix, ny, m) = mk(0, 0);
+      F.bt(ix, ny, m) = mk(0, 0);
+    }
+  }
+  __syncthreads();
+  bfield_bcs_dev(F.bx, F.br, F.bt, true, bcf, rc);
+}
+
+// ------------------------------------------------------------- currents
+
+// particle_reflection_bcs_complex (boundary.F90:918-1015) for one side
+__device__ void reflect_side(FView f, int flip, int bd, const RunConst& rc) {
+  const int nx = rc.nx, ny = rc.ny, M = rc.M;
+  const cplx Z = mk(0, 0);
+  if (bd == CYL_BD_X_MIN || bd == CYL_BD_X_MAX) {
+    const int nrow = ny + 2 * NG;
+    CTA_FOR(t, nrow * M) {
+      int j = 1 - NG + t % nrow, m = t / nrow;
+      if (bd == CYL_BD_X_MIN) {
+        if (flip == 1) {
+          for (int i = 1; i <= NG - 1; ++i) { f(i, j, m) = f(i, j, m) - f(1 - i, j, m); f(1 - i, j, m) = Z; }
+        } else {
+          for (int i = 1; i <= NG - 1; ++i) { f(i, j, m) = f(i, j, m) + f(-i, j, m); f(-i, j, m) = Z; }
+        }
+      } else {
+        if (flip == 1) {
+          for (int i = 1; i <= NG; ++i) { f(nx + 1 - i, j, m) = f(nx + 1 - i, j, m) - f(nx + i, j, m); f(nx + i, j, m) = Z; }
+        } else {
+          for (int i = 1; i <= NG; ++i) { f(nx - i, j, m) = f(nx - i, j, m) + f(nx + i, j, m); f(nx + i, j, m) = Z; }
+        }
+      }
+    }
+  } else {
+    const int ncol = nx + 2 * NG;
+    const double r_max = rc.y_grid_min + ((double)ny - 0.5) * rc.dy;
+    CTA_FOR(t, ncol * M) {
+      int ix = 1 - NG + t % ncol, m = t / ncol;
+      for (int i = 1; i <= NG; ++i) {
+        if (flip == 2) {
+          f(ix, ny + 1 - i, m) = f(ix, ny + 1 - i, m) -
+              (f(ix, ny + i, m) * (r_max + ((double)i - 0.5) * rc.dy)) / (r_max - ((double)i - 0.5) * rc.dy);
+        } else if (flip == 1) {
+          f(ix, ny - i, m) = f(ix, ny - i, m) +
+              (f(ix, ny + i, m) * (r_max + (double)i * rc.dy)) / (r_max - (double)i * rc.dy);
+        } else {
+          f(ix, ny - i, m) = f(ix, ny - i, m) + f(ix, ny + i, m);
+        }
+        f(ix, ny + i, m) = Z;
+      }
+    }
+  }
+}
+
+// current_bcs_r_min_final (boundary.F90:1909-1959), per column
+__device__ void j_rmin_dev(FView jx, FView jr, FView jt, const RunConst& rc) {
+  const int ncol = rc.nx + 2 * NG;
+  CTA_FOR(t, ncol) {
+    const int ix = 1 - NG + t;
+    double mode_sign = 1.0;
+    for (int im = 0; im < rc.M; ++im) {
+      for (int j = 2; j <= JNG; ++j) {
+        jx(ix, j - 1, im) = jx(ix, j - 1, im) + mode_sign * jx(ix, 1 - j, im);
+        jr(ix, j, im) = jr(ix, j, im) - mode_sign * jr(ix, 1 - j, im);
+        jt(ix, j - 1, im) = jt(ix, j - 1, im) - mode_sign * jt(ix, 1 - j, im);
+        jx(ix, 1 - j, im) = mk(0, 0);
+        jr(ix, 1 - j, im) = mk(0, 0);
+        jt(ix, 1 - j, im) = mk(0, 0);
+      }
+      jr(ix, 1, im) = jr(ix, 1, im) - mode_sign * jr(ix, 0, im);
+      mode_sign = -mode_sign;
+    }
+    for (int im = 0; im < rc.M; ++im) {
+      if (im > 0) jx(ix, 0, im) = mk(0, 0);
+      else jx(ix, 0, im) = (4.0 * jx(ix, 1, im) - jx(ix, 2, im)) / 3.0;
+      if (im == 1) {
+        jt(ix, 0, im) = ((-IMAGI) * (9.0 * jr(ix, 1, im) - jr(ix, 2, im))) / 8.0;
+        jr(ix, 0, im) = (2.0 * IMAGI) * jt(ix, 0, im) - jr(ix, 1, im);
+      } else {
+        jt(ix, 0, im) = mk(0, 0);
+        jr(ix, 0, im) = -jr(ix, 1, im);
+      }
+    }
+  }
+}
+
+// particle_periodic_bcs_complex on one rank (boundary.F90:1133-1245)
+__device__ void periodic_sum_dev(FView f, const RunConst& rc) {
+  if (rc.bc_allspecies[CYL_BD_X_MIN] != CYL_BC_PERIODIC) return;
+  const int nrow = rc.ny + 2 * NG;
+  const int nx = rc.nx;
+  CTA_FOR(t, nrow * rc.M * NG) {
+    int i = 1 + t % NG, r = t / NG;
+    int j = 1 - NG + r % nrow, m = r / nrow;
+    f(i, j, m) = f(i, j, m) + f(nx + i, j, m);
+  }
+  __syncthreads();
+  CTA_FOR(t, nrow * rc.M * NG) {
+    int i = 1 + t % NG, r = t / NG;
+    int j = 1 - NG + r % nrow, m = r / nrow;
+    f(nx - NG + i, j, m) = f(nx - NG + i, j, m) + f(i - NG, j, m);
+  }
+}
+
+// current_bcs_r_min_final, then current_finish (current_smooth.F90:29-45)
+// without smoothing (one CTA).
+__global__ void __launch_bounds__(CTA_THREADS) k_current_finish(FView jx, FView jr, FView jt, const StepRec* rec, RunConst rc) {
+  __shared__ int bcf[4];
+  if (threadIdx.x < 4) bcf[threadIdx.x] = rec->bc_field[threadIdx.x];
+  __syncthreads();
+  j_rmin_dev(jx, jr, jt, rc);
+  __syncthreads();
+  const int bds[3] = {CYL_BD_X_MIN, CYL_BD_X_MAX, CYL_BD_Y_MAX};
+  for (int k = 0; k < 3; ++k) {
+    if (rc.bc_allspecies[bds[k]] == CYL_BC_REFLECT) {
+      reflect_side(jx, 1, bds[k], rc);
+      reflect_side(jr, 2, bds[k], rc);
+      reflect_side(jt, 3, bds[k], rc);
+    }
+    __syncthreads();
+  }
+  periodic_sum_dev(jx, rc);
+  periodic_sum_dev(jr, rc);
+  periodic_sum_dev(jt, rc);
+  __syncthreads();
+  halo_x(jx, 1 - NG, rc.ny + NG, bcf, rc);
+  halo_x(jr, 1 - NG, rc.ny + NG, bcf, rc);
+  halo_x(jt, 1 - NG, rc.ny + NG, bcf, rc);
+}
+
+// One pass of smooth_mode_array (current_smooth.F90:172-190): the halo of wk
+// is done by k_halo_rows before this; reads wk, writes f (interior).
+__global__ void k_smooth_pass(FView f, FView wk, double alpha, double beta, int cs, RunConst rc) {
+  const int ix = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int iy = 1 + blockIdx.y;
+  const int im = blockIdx.z;
+  if (ix > rc.nx) return;
+  f(ix, iy, im) = alpha * wk(ix, iy, im) +
+      (((wk(ix - cs, iy, im) + wk(ix + cs, iy, im)) + wk(ix, iy - cs, im)) + wk(ix, iy + cs, im)) * beta;
+}
+__global__ void k_copy_interior(FView dst, FView src, RunConst rc) {
+  const int ix = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int iy = 1 + blockIdx.y;
+  const int im = blockIdx.z;
+  if (ix > rc.nx) return;
+  dst(ix, iy, im) = src(ix, iy, im);
+}
+__global__ void __launch_bounds__(CTA_THREADS) k_halo_rows(FView f, const StepRec* rec, RunConst rc) {
+  __shared__ int bcf[4];
+  if (threadIdx.x < 4) bcf[threadIdx.x] = rec->bc_field[threadIdx.x];
+  __syncthreads();
+  halo_x(f, 1 - NG, rc.ny + NG, bcf, rc);
+}
+
+// -------------------------------------------------------- moving window
+
+// shift_fields (window.F90:98-132): one block per (row j, mode m); the row is
+// staged in shared memory so the in-place left shift is race free.  The
+// periodic self-wrap of shift_field_modes and the x_max column fix-ups act
+// within the same row.
+__global__ void k_shift_fields(FieldSet F, const cplx* cols, const StepRec* rec, int which, RunConst rc) {
+  extern __shared__ cplx row[];
+  const int j = 1 - NG + (int)blockIdx.x;
+  const int m = blockIdx.y;
+  const int nxg = rc.nxg, nx = rc.nx;
+  __shared__ int bcf[4];
+  if (threadIdx.x < 4) bcf[threadIdx.x] = rec->bc_field_after[threadIdx.x];
+  if (rec->nshift <= which) return;
+  FView arr[9] = {F.ex, F.er, F.et, F.bx, F.br, F.bt, F.jx, F.jr, F.jt};
+  for (int a = 0; a < 9; ++a) {
+    FView f = arr[a];
+    __syncthreads();
+    for (int i = threadIdx.x; i < nxg; i += blockDim.x) row[i] = f(1 - NG + i, j, m);
+    __syncthreads();
+    for (int i = threadIdx.x; i < nxg - 1; i += blockDim.x) f(1 - NG + i, j, m) = row[i + 1];
+    __syncthreads();
+    // periodic self-wrap (field_mode_bc) within this row
+    if (bcf[CYL_BD_X_MAX] == CYL_BC_PERIODIC)
+      for (int i = 1 + threadIdx.x; i <= NG; i += blockDim.x) f(nx + i, j, m) = f(i, j, m);
+    __syncthreads();
+    if (bcf[CYL_BD_X_MIN] == CYL_BC_PERIODIC)
+      for (int i = 1 - NG + threadIdx.x; i <= 0; i += blockDim.x) f(i, j, m) = f(nx + i, j, m);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int ncolv = rc.ny + 2 * NG;
+    auto cv = [&](int a) { return cols[(size_t)(6 + a) * ncolv * rc.M + (j + NG - 1) + (size_t)ncolv * m]; };
+    F.ex(nx + 1, j, m) = cv(0);
+    F.er(nx, j, m) = cv(1);
+    F.et(nx, j, m) = cv(2);
+    F.ex(nx, j, m) = 0.5 * (F.ex(nx - 1, j, m) + F.ex(nx + 1, j, m));
+    F.er(nx - 1, j, m) = 0.5 * (F.er(nx - 2, j, m) + F.er(nx, j, m));
+    F.et(nx - 1, j, m) = 0.5 * (F.et(nx - 2, j, m) + F.et(nx, j, m));
+    F.bx(nx, j, m) = cv(3);
+    F.br(nx + 1, j, m) = cv(4);
+    F.bt(nx + 1, j, m) = cv(5);
+    F.bx(nx - 1, j, m) = 0.5 * (F.bx(nx - 2, j, m) + F.bx(nx, j, m));
+    F.br(nx, j, m) = 0.5 * (F.br(nx - 1, j, m) + F.br(nx + 1, j, m));
+    F.bt(nx, j, m) = 0.5 * (F.bt(nx - 1, j, m) + F.bt(nx + 1, j, m));
+  }
+}
+
+// ------------------------------------------------------------ launchers
+
+void launch_update_e(cudaStream_t s, const FieldSet& F, const RunConst& rc) {
+  dim3 blk(128), grd((rc.nx + 1 + 127) / 128, rc.ny, rc.M);
+  k_update_e<<<grd, blk, 0, s>>>(F.ex, F.er, F.et, F.bx, F.br, F.bt, F.jx, F.jr, F.jt, rc);
+}
+void launch_update_b(cudaStream_t s, const FieldSet& F, int save_old, const RunConst& rc) {
+  dim3 blk(128), grd((rc.nxg + 127) / 128, rc.nyg, rc.M);
+  k_update_b<<<grd, blk, 0, s>>>(F.ex, F.er, F.et, F.bx, F.br, F.bt, F.bxo, F.bro, F.bto, save_old, rc);
+}
+void launch_e_axis_bcs(cudaStream_t s, const FieldSet& F, const StepRec* rec, const RunConst& rc) {
+  k_e_axis_bcs<<<1, CTA_THREADS, 0, s>>>(F.ex, F.er, F.et, F.jx, F.bt, rec, rc);
+}
+void launch_efield_bcs(cudaStream_t s, const FieldSet& F, const StepRec* rec, const RunConst& rc) {
+  k_efield_bcs<<<1, CTA_THREADS, 0, s>>>(F.ex, F.er, F.et, rec, rc);
+}
+void launch_b_axis_bcs(cudaStream_t s, const FieldSet& F, const StepRec* rec, const RunConst& rc) {
+  k_b_axis_bcs<<<1, CTA_THREADS, 0, s>>>(F.bx, F.br, F.bt, F.ex, F.et, rec, rc);
+}
+void launch_b_final_bcs(cudaStream_t s, const FieldSet& F, const StepRec* rec, const double* src,
+                        const cplx* cols, int do_axis, double dt, const RunConst& rc) {
+  k_b_axis_final_bcs<<<1, CTA_THREADS, 0, s>>>(F, rec, src, cols, do_axis, dt, rc);
+}
+void launch_current_finish(cudaStream_t s, const FieldSet& F, const StepRec* rec, const RunConst& rc,
+                           int smooth, int its, int comp_its, int stride, FView wk) {
+  k_current_finish<<<1, CTA_THREADS, 0, s>>>(F.jx, F.jr, F.jt, rec, rc);
+  if (!smooth) return;
+  FView js[3] = {F.jx, F.jr, F.jt};
+  dim3 blk(128), grd((rc.nx + 127) / 128, rc.ny, rc.M);
+  const size_t bytes = (size_t)rc.nxg * rc.nyg * rc.M * sizeof(cplx);
+  for (int a = 0; a < 3; ++a) {
+    cudaMemcpyAsync(wk.p, js[a].p, bytes, cudaMemcpyDeviceToDevice, s);
+    double alpha = 0.5, beta = (1.0 - alpha) * 0.25;
+    for (int it = 1; it <= its + comp_its; ++it) {
+      k_halo_rows<<<1, CTA_THREADS, 0, s>>>(wk, rec, rc);
+      k_smooth_pass<<<grd, blk, 0, s>>>(js[a], wk, alpha, beta, stride, rc);
+      k_copy_interior<<<grd, blk, 0, s>>>(wk, js[a], rc);
+      if (it > its) alpha = (double)its * 0.5 + 1.0;
+    }
+    k_copy_interior<<<grd, blk, 0, s>>>(js[a], wk, rc);
+  }
+}
+void launch_shift_fields(cudaStream_t s, const FieldSet& F, const cplx* cols, const StepRec* rec,
+                         int which, const RunConst& rc) {
+  dim3 grd(rc.nyg, rc.M);
+  k_shift_fields<<<grd, 256, (size_t)rc.nxg * sizeof(cplx), s>>>(F, cols, rec, which, rc);
+}
+
+}  // namespace cyl

@@ -1,0 +1,57 @@
+// host_deck.h -- host-side stand-ins for the Fortran driver's deck work:
+// the global KISS generator, the particle loader and the moving-window
+// injector.  These run on the CPU exactly as the reference does (the
+// reference evaluates deck expressions and draws random numbers serially on
+// the host); the GPU receives their output.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "../../include/cylpic.h"
+
+namespace cyl {
+
+// KISS + polar Box-Muller (random_generator.f90:45-173)
+struct KissRng {
+  int32_t x = 0, y = 0, z = 0, w = 0;
+  bool cached = false;
+  double cval = 0.0;
+  void seed(int32_t s);
+  double random();
+  double box_muller(double stdev, double mu);
+  void to_state(cyl_rng_state* s) const;
+  void from_state(const cyl_rng_state* s);
+};
+
+// Grid scalars of one run, as setup_grid / setup_grid_x / setup_grid_y
+// (setup.F90:164-206, utilities.f90:343-409) compute them, cpml_thickness = 0.
+struct HostGrid {
+  int nx = 0, ny = 0, M = 0;
+  double dx = 0, dy = 0, dt = 0;
+  double length_x = 0, length_y = 0;
+  double x_min = 0, x_max = 0, y_max = 0;
+  double x_grid_min = 0, xb_min = 0, x_grid_max = 0;
+  double y_grid_min = 0, y_grid_max = 0;
+  double x_min_local = 0, x_max_local = 0, y_min_local = 0, y_max_local = 0;
+  void init(const cyl_grid_desc& g);
+  void setup_grid_x();
+  void setup_grid_y();
+  double xg(int ix) const { return x_grid_min + (double)(ix - 1) * dx; }
+  double yg(int iy) const { return y_grid_min + (double)(iy - 1) * dy; }
+};
+
+// A particle produced on the host: x, y, z, px, py, pz, w, id
+struct HostParticle {
+  double v[7];
+  int64_t id;
+};
+
+double species_density(const cyl_species_desc& d, double x);
+
+// insert_particles (window.F90:157-300) for one species at the current grid
+// (before the shift): appends to out, advances rng and next_id.
+void host_insert_particles(const HostGrid& g, const cyl_species_desc& d, KissRng& rng,
+                           int64_t& next_id, std::vector<HostParticle>& out);
+
+}  // namespace cyl

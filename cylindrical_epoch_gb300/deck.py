@@ -1,0 +1,286 @@
+"""Deck descriptions of the runs this package is measured and tested on.
+
+A Deck holds what the reference's Fortran driver has after it read an input
+deck (control, boundaries, species, laser and window blocks) and ran set_dt:
+the descriptors of include/cylpic.h plus the host-evaluated laser profile.
+The builders below write the benchmark decks in the reference's deck
+vocabulary; ``set_dt`` restates setup.F90:573-670.
+"""
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy as np
+
+from . import abi
+
+# constants.F90:171-181
+PI = 3.141592653589793238462643383279503
+Q0 = 1.602176565e-19
+M0 = 9.10938291e-31
+CL = 2.99792458e8
+KB = 1.3806488e-23
+EPS0 = 8.854187817620389850536563031710750e-12
+EV = Q0
+C_TINY = 2.2250738585072014e-308  # TINY(1.0_num)
+C_EPS = 2.220446049250313e-16      # EPSILON(1.0_num), the density_min default
+C_HUGE = 1.7976931348623157e308
+
+
+@dataclass
+class Species:
+    name: str
+    charge: float
+    mass: float
+    npart_per_cell: float
+    density: float
+    temp_k: tuple = (0.0, 0.0, 0.0)
+    drift: tuple = (0.0, 0.0, 0.0)
+    bc: tuple = (abi.BC_PERIODIC, abi.BC_PERIODIC, abi.BC_OTHER, abi.BC_REFLECT)
+    immobile: bool = False
+    density_kind: int = 0          # 0 uniform, 1 linear ramp
+    ramp_x0: float = 0.0
+    ramp_length: float = 1.0
+    density_min: float = C_EPS
+    density_max: float = C_HUGE
+    capacity: int = 0
+
+    def desc(self):
+        d = abi.SpeciesDesc()
+        d.charge = self.charge
+        d.mass = self.mass
+        d.immobile = 1 if self.immobile else 0
+        for i in range(4):
+            d.bc_particle[i] = self.bc[i]
+        d.capacity = int(self.capacity)
+        d.npart_per_cell = self.npart_per_cell
+        d.density_kind = self.density_kind
+        d.density = self.density
+        d.ramp_x0 = self.ramp_x0
+        d.ramp_length = self.ramp_length
+        d.density_min = self.density_min
+        d.density_max = self.density_max
+        for i in range(3):
+            d.temp[i] = self.temp_k[i]
+            d.drift[i] = self.drift[i]
+        return d
+
+    def density_at(self, x):
+        if self.density_kind == 1:
+            f = (np.asarray(x, dtype=np.float64) - self.ramp_x0) / self.ramp_length
+            return self.density * np.clip(f, 0.0, 1.0)
+        return np.full_like(np.asarray(x, dtype=np.float64), self.density)
+
+
+@dataclass
+class Laser:
+    boundary: int
+    amp: float
+    omega: float
+    profile: np.ndarray            # ny+1 values at y(ir), ir = 0..ny
+    phase: np.ndarray
+    pol_angle: float = 0.0
+    t_start: float = 0.0
+    t_end: float = C_HUGE
+    t_profile: int = 0             # 0 constant, 1 gauss(time, t0, tw)
+    t0: float = 0.0
+    tw: float = 1.0
+
+
+@dataclass
+class Deck:
+    name: str
+    nx: int
+    ny: int
+    n_mode: int
+    x_min: float
+    x_max: float
+    y_max: float
+    bc_field: tuple
+    species: List[Species]
+    lasers: List[Laser] = field(default_factory=list)
+    nsteps: int = 100
+    precision: int = abi.PREC_FP64
+    dt_multiplier: float = 0.95
+    move_window: bool = False
+    window_v_x: float = 0.0
+    window_start_time: float = 0.0
+    window_stop_time: float = 1.0e300
+    bc_after_move: Optional[tuple] = None
+    smooth_currents: int = 0
+    smooth_its: int = 1
+    smooth_comp_its: int = 0
+    smooth_stride: int = 1
+    seed: int = 7842432
+    dt: float = 0.0
+
+    @property
+    def dx(self):
+        return (self.x_max - self.x_min) / float(self.nx)
+
+    @property
+    def dy(self):
+        return (self.y_max - 0.0) / float(self.ny)
+
+    def y_grid(self, ir):
+        """Cell-centred radial grid y(ir) (setup.F90:196-200)."""
+        ygm = (0.0 - self.dy * 0.0) + self.dy / 2.0
+        return ygm + (np.asarray(ir, dtype=np.float64) - 1.0) * self.dy
+
+    def grid_desc(self):
+        g = abi.GridDesc()
+        g.nx, g.ny, g.n_mode = self.nx, self.ny, self.n_mode
+        g.precision = self.precision
+        g.x_min, g.x_max, g.y_max = self.x_min, self.x_max, self.y_max
+        g.dt = self.dt if self.dt > 0 else set_dt(self)
+        for i in range(4):
+            g.bc_field[i] = self.bc_field[i]
+        g.move_window = 1 if self.move_window else 0
+        g.window_v_x = self.window_v_x
+        g.window_start_time = self.window_start_time
+        g.window_stop_time = self.window_stop_time
+        after = self.bc_after_move or self.bc_field
+        for i in range(4):
+            g.bc_after_move[i] = after[i]
+        g.smooth_currents = self.smooth_currents
+        g.smooth_its = self.smooth_its
+        g.smooth_comp_its = self.smooth_comp_its
+        g.smooth_stride = self.smooth_stride
+        return g
+
+    def species_descs(self):
+        arr = (abi.SpeciesDesc * max(1, len(self.species)))()
+        for i, s in enumerate(self.species):
+            arr[i] = s.desc()
+        return arr
+
+    def laser_descs(self):
+        """Descriptor array plus the numpy buffers it points into (keep both alive)."""
+        arr = (abi.LaserDesc * max(1, len(self.lasers)))()
+        keep = []
+        for i, L in enumerate(self.lasers):
+            prof = np.ascontiguousarray(L.profile, dtype=np.float64)
+            ph = np.ascontiguousarray(L.phase, dtype=np.float64)
+            keep += [prof, ph]
+            d = arr[i]
+            d.boundary, d.t_profile = L.boundary, L.t_profile
+            d.amp, d.omega, d.pol_angle = L.amp, L.omega, L.pol_angle
+            d.t_start, d.t_end, d.t0, d.tw = L.t_start, L.t_end, L.t0, L.tw
+            d.profile = prof.ctypes.data_as(C.POINTER(C.c_double))
+            d.phase = ph.ctypes.data_as(C.POINTER(C.c_double))
+        return arr, keep
+
+    def mobile_particles_estimate(self):
+        n = 0
+        for s in self.species:
+            if not s.immobile:
+                n += int(math.floor(s.npart_per_cell)) * self.nx * self.ny
+        return n
+
+
+def set_dt(deck: Deck) -> float:
+    """dt of set_dt (setup.F90:629-670) with set_plasma_frequency_dt
+    (setup.F90:573-625) and set_laser_dt (laser.f90:368-407)."""
+    dx, dy = deck.dx, deck.dy
+    min_dt = 1000000.0
+    k_max = 2.0 * PI / min(dx, dy)
+    xg = (deck.x_min - dx * 0.0) + dx / 2.0 + (np.arange(1, deck.nx + 1) - 1.0) * dx
+    for s in deck.species:
+        fac1 = Q0 ** 2 / s.mass / EPS0
+        fac2 = 3.0 * k_max ** 2 * KB / s.mass
+        dens = s.density_at(xg)
+        if s.density_max > 0:
+            dens = np.minimum(dens, s.density_max)
+        omega2 = fac1 * dens + fac2 * max(s.temp_k)
+        omega2 = omega2[omega2 > C_TINY]
+        if omega2.size:
+            omega = np.sqrt(omega2)
+            cand = (2.0 * PI / omega).min()
+            if cand < min_dt:
+                min_dt = float(cand)
+    dt_plasma = min_dt / 2.0
+    dt_laser = C_HUGE
+    for L in deck.lasers:
+        dt_laser = min(dt_laser, 2.0 * PI / L.omega)
+    dt_laser = dt_laser / 2.0
+    dt = 0.9 * min(dx, dy) / math.sqrt(2.0) / CL
+    if dt_plasma > C_TINY:
+        dt = min(dt, dt_plasma)
+    if dt_laser > C_TINY:
+        dt = min(dt, dt_laser)
+    return deck.dt_multiplier * dt
+
+
+# ---------------------------------------------------------------- decks
+
+def thermal_plasma(nx=256, ny=64, ppc=16, n_mode=2, nsteps=200, precision=abi.PREC_FP64):
+    """Uniform 1 keV thermal electron plasma, n = 1e25 m^-3, dz = dr = 50 nm,
+    periodic in z, conducting outer r boundary, immobile neutralising ions
+    (not loaded: they carry no current), CFL 0.95."""
+    d = 0.05e-6
+    t_k = 1000.0 * EV / KB  # temp_ev (deck_species_block.F90:835-844)
+    e = Species("electron", -Q0, M0, ppc, 1.0e25, temp_k=(t_k, t_k, t_k),
+                bc=(abi.BC_PERIODIC, abi.BC_PERIODIC, abi.BC_OTHER, abi.BC_CONDUCT))
+    deck = Deck("thermal_plasma", nx, ny, n_mode, 0.0, nx * d, ny * d,
+                (abi.BC_PERIODIC, abi.BC_PERIODIC, abi.BC_OTHER, abi.BC_CONDUCT),
+                [e], nsteps=nsteps, precision=precision)
+    e.capacity = int(ppc * nx * ny * 1.05) + 1024
+    return deck
+
+
+def wakefield(nx=2048, ny=256, n_mode=2, ppc=8, a0=2.0, lam=0.8e-6, waist=10.0e-6,
+              t_fwhm=30.0e-15, density=1.0e24, ramp=50.0e-6, nsteps=2000,
+              precision=abi.PREC_FP64, circular=False, ions=None):
+    """Laser wakefield deck: Gaussian laser injected at z-min (simple_laser),
+    electron plasma with a linear up-ramp, moving window at c.
+
+    The time envelope and the window start follow the reference's own
+    wakefield example deck conventions (example_decks/
+    Wakefield_Lifschitz09_JCompPhys228.deck): t_profile = gauss(time, t0, wt)
+    with wt = 0.60056 t_fwhm and t0 = 0.5 * 1.8226 t_fwhm; the window starts
+    once the pulse has fully entered (time 2 t0) and the x boundaries become
+    simple_outflow after the move."""
+    dx = lam / 32.0 if nx == 2048 else lam / 32.0
+    dy = lam / 8.0
+    omega = 2.0 * PI * CL / lam
+    amp = a0 * M0 * CL * omega / Q0
+    wt = t_fwhm * 0.60056
+    t0 = 0.5 * t_fwhm * 1.8226
+    deck = Deck("wakefield", nx, ny, n_mode, 0.0, nx * dx, ny * dy,
+                (abi.BC_SIMPLE_LASER, abi.BC_OPEN, abi.BC_OTHER, abi.BC_OPEN),
+                [], nsteps=nsteps, precision=precision)
+    yv = deck.y_grid(np.arange(0, ny + 1))
+    prof = np.exp(-((yv - 0.0) / waist) ** 2)  # gauss(y, 0, waist)
+    phase = np.zeros(ny + 1)
+    if circular:
+        deck.lasers = [
+            Laser(abi.BD_X_MIN, amp / math.sqrt(2.0), omega, prof, phase, 0.0, t_profile=1, t0=t0, tw=wt),
+            Laser(abi.BD_X_MIN, amp / math.sqrt(2.0), omega, prof, phase + PI / 2.0, PI / 2.0,
+                  t_profile=1, t0=t0, tw=wt),
+        ]
+    else:
+        deck.lasers = [Laser(abi.BD_X_MIN, amp, omega, prof, phase, 0.0, t_profile=1, t0=t0, tw=wt)]
+    e = Species("electron", -Q0, M0, ppc, density, density_kind=1, ramp_x0=0.0, ramp_length=ramp,
+                bc=(abi.BC_SIMPLE_LASER, abi.BC_OPEN, abi.BC_OTHER, abi.BC_OPEN))
+    deck.species = [e]
+    if ions is not None:
+        deck.species.append(ions)
+    deck.move_window = True
+    deck.window_v_x = CL
+    deck.window_start_time = 2.0 * t0
+    deck.bc_after_move = (abi.BC_SIMPLE_OUTFLOW, abi.BC_SIMPLE_OUTFLOW, abi.BC_OTHER, abi.BC_OPEN)
+    for s in deck.species:
+        s.capacity = int(math.floor(s.npart_per_cell) * nx * ny * 1.10) + 4096
+    return deck
+
+
+def large_wakefield(precision=abi.PREC_MIXED, nsteps=3000):
+    """m = 0..3, a0 = 4, circular polarisation, waist 8 um, 3e24 m^-3 electrons
+    plus a mobile helium-like ion species (Z = 2, 4 amu) at 1 % of n_e,
+    4096 x 512 cells, 32 electrons per cell (the ion species uses 2 per cell)."""
+    ions = Species("helium2+", 2.0 * Q0, 4.0 * 1.66053886e-27, 2, 0.01 * 3.0e24, density_kind=1,
+                   ramp_x0=0.0, ramp_length=50.0e-6,
+                   bc=(abi.BC_SIMPLE_LASER, abi.BC_OPEN, abi.BC_OTHER, abi.BC_OPEN))
+    return wakefield(nx=4096, ny=512, n_mode=4, ppc=32, a0=4.0, waist=8.0e-6, density=3.0e24,
+                     nsteps=nsteps, precision=precision, circular=True, ions=ions)

@@ -1,0 +1,70 @@
+"""Loader and ctypes signatures of libcylpic.so (include/cylpic.h).
+
+There is no fallback: if the library is missing the import of ``load()``
+raises, and every entry point that needs a GPU returns CYL_ERR_NO_DEVICE on
+a machine without one.
+"""
+import ctypes as C
+import os
+
+from . import abi
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libcylpic.so")
+
+_lib = None
+
+P = C.POINTER
+D = C.c_double
+I32 = C.c_int32
+I64 = C.c_int64
+PD = P(C.c_double)
+PI64 = P(C.c_int64)
+PI32 = P(C.c_int32)
+H = C.c_void_p
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "cyl_create": (C.c_int, [P(abi.GridDesc), P(abi.SpeciesDesc), I32, P(abi.LaserDesc), I32,
+                             P(abi.RngState), P(H)]),
+    "cyl_destroy": (C.c_int, [H]),
+    "cyl_upload_particles": (C.c_int, [H, I32, PD, PD, PD, PD, PD, PD, PD, PI64, I64]),
+    "cyl_download_particles": (C.c_int, [H, I32, PD, PD, PD, PD, PD, PD, PD, PI64, PI64]),
+    "cyl_upload_field": (C.c_int, [H, I32, PD]),
+    "cyl_download_field": (C.c_int, [H, I32, PD]),
+    "cyl_initialise": (C.c_int, [H]),
+    "cyl_step": (C.c_int, [H, I32]),
+    "cyl_step_graph": (C.c_int, [H, I32]),
+    "cyl_get_run_state": (C.c_int, [H, P(abi.RunState)]),
+    "cyl_diagnostics": (C.c_int, [H, P(abi.Diag)]),
+    "cyl_get_rng_state": (C.c_int, [H, P(abi.RngState)]),
+    "cyl_sort_particles": (C.c_int, [H]),
+    "cyl_cell_indices": (C.c_int, [H, I32, PI32, PI32, PI64]),
+    "cyl_push_only": (C.c_int, [H]),
+    "cyl_kernel_timing": (C.c_int, [H, PD, PI64]),
+    "cyl_rng_init": (None, [P(abi.RngState), I32]),
+    "cyl_rng_random": (C.c_double, [P(abi.RngState)]),
+    "cyl_rng_box_muller": (C.c_double, [P(abi.RngState), D, D]),
+    "cyl_host_load_species": (C.c_int, [P(abi.GridDesc), P(abi.SpeciesDesc), P(abi.RngState), I64,
+                                        PD, PD, PD, PD, PD, PD, PD, PI64, PI64]),
+}
+
+
+def load(path=None):
+    """Load libcylpic.so (build it first with cylindrical_epoch_gb300.build)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(
+            f"{p} is missing: build the CUDA library with "
+            "`python -m cylindrical_epoch_gb300.build` (there is no CPU fallback)")
+    lib = C.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib

@@ -1,0 +1,202 @@
+"""Host-side driver of one run on the GPU.
+
+``Run`` plays the part of the reference's Fortran driver (epoch2d.F90): it
+loads the species on the host (auto_load), hands particles and fields to the
+C ABI, performs the start-up sequence and advances steps.  All calls go
+through libcylpic.so; there is no CPU path.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from .deck import Deck
+from .lib import load
+
+PD = C.POINTER(C.c_double)
+PI64 = C.POINTER(C.c_int64)
+PI32 = C.POINTER(C.c_int32)
+
+
+def _p(a, t=PD):
+    return a.ctypes.data_as(t)
+
+
+class Particles:
+    """SoA host copy of one species (positions m, momenta kg m/s)."""
+
+    __slots__ = ("x", "y", "z", "px", "py", "pz", "w", "id")
+
+    def __init__(self, n):
+        for k in ("x", "y", "z", "px", "py", "pz", "w"):
+            setattr(self, k, np.zeros(n, dtype=np.float64))
+        self.id = np.zeros(n, dtype=np.int64)
+
+    @property
+    def n(self):
+        return self.x.shape[0]
+
+    def resize(self, n):
+        for k in self.__slots__:
+            setattr(self, k, getattr(self, k)[:n].copy())
+        return self
+
+    def sorted_by_id(self):
+        o = np.argsort(self.id, kind="stable")
+        out = Particles(0)
+        for k in self.__slots__:
+            setattr(out, k, getattr(self, k)[o])
+        return out
+
+    def arrays(self):
+        return [getattr(self, k) for k in self.__slots__]
+
+
+def host_load(deck: Deck, rng=None):
+    """Load every species as auto_load does; returns (list of Particles, rng)."""
+    lib = load()
+    if rng is None:
+        rng = abi.RngState()
+        lib.cyl_rng_init(C.byref(rng), deck.seed)
+    g = deck.grid_desc()
+    out = []
+    id_base = 0
+    for s in deck.species:
+        d = s.desc()
+        n = C.c_int64(0)
+        abi.check("cyl_host_load_species",
+                  lib.cyl_host_load_species(C.byref(g), C.byref(d), C.byref(rng), id_base,
+                                            None, None, None, None, None, None, None, None, C.byref(n)))
+        p = Particles(n.value)
+        if s.immobile:
+            out.append(Particles(0))
+            continue
+        abi.check("cyl_host_load_species",
+                  lib.cyl_host_load_species(C.byref(g), C.byref(d), C.byref(rng), id_base,
+                                            _p(p.x), _p(p.y), _p(p.z), _p(p.px), _p(p.py), _p(p.pz),
+                                            _p(p.w), _p(p.id, PI64), C.byref(n)))
+        p.resize(n.value)
+        id_base += n.value
+        out.append(p)
+    return out, rng
+
+
+class Run:
+    """One simulation resident on the GPU, driven through the C ABI."""
+
+    def __init__(self, deck: Deck, particles=None, rng=None, fields=None, initialise=True):
+        self.lib = load()
+        self.deck = deck
+        if particles is None:
+            particles, rng = host_load(deck, rng)
+        g = deck.grid_desc()
+        self.dt = g.dt
+        sp = deck.species_descs()
+        for i, s in enumerate(deck.species):
+            need = particles[i].n if i < len(particles) else 0
+            if sp[i].capacity < need + 1024:
+                sp[i].capacity = int(need * 1.1) + 4096
+        las, self._keep = deck.laser_descs()
+        h = C.c_void_p()
+        abi.check("cyl_create", self.lib.cyl_create(C.byref(g), sp, len(deck.species), las,
+                                                    len(deck.lasers), C.byref(rng) if rng else None,
+                                                    C.byref(h)))
+        self.h = h
+        self.nxg = deck.nx + 2 * abi.NG
+        self.nyg = deck.ny + 2 * abi.NG
+        for i, p in enumerate(particles):
+            self.upload_particles(i, p)
+        if fields:
+            for name, arr in fields.items():
+                self.upload_field(name, arr)
+        if initialise:
+            abi.check("cyl_initialise", self.lib.cyl_initialise(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.cyl_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- data movement
+    def upload_particles(self, isp, p: Particles):
+        abi.check("cyl_upload_particles",
+                  self.lib.cyl_upload_particles(self.h, isp, _p(p.x), _p(p.y), _p(p.z), _p(p.px),
+                                                _p(p.py), _p(p.pz), _p(p.w), _p(p.id, PI64), p.n))
+
+    def particles(self, isp=0):
+        n = C.c_int64(0)
+        abi.check("cyl_download_particles",
+                  self.lib.cyl_download_particles(self.h, isp, None, None, None, None, None, None,
+                                                  None, None, C.byref(n)))
+        p = Particles(n.value)
+        abi.check("cyl_download_particles",
+                  self.lib.cyl_download_particles(self.h, isp, _p(p.x), _p(p.y), _p(p.z), _p(p.px),
+                                                  _p(p.py), _p(p.pz), _p(p.w), _p(p.id, PI64),
+                                                  C.byref(n)))
+        return p.resize(n.value)
+
+    def field(self, name):
+        """Complex mode array F(1-ng:nx+ng, 1-ng:ny+ng, 0:M-1) as numpy
+        complex128 with shape (M, ny+2ng, nx+2ng) (Fortran order reversed)."""
+        which = abi.FIELD_INDEX[name] if isinstance(name, str) else name
+        a = np.zeros((self.deck.n_mode, self.nyg, self.nxg), dtype=np.complex128)
+        abi.check("cyl_download_field", self.lib.cyl_download_field(self.h, which, _p(a.view(np.float64))))
+        return a
+
+    def upload_field(self, name, arr):
+        which = abi.FIELD_INDEX[name] if isinstance(name, str) else name
+        a = np.ascontiguousarray(arr, dtype=np.complex128)
+        abi.check("cyl_upload_field", self.lib.cyl_upload_field(self.h, which, _p(a.view(np.float64))))
+
+    # ---- stepping
+    def step(self, n=1, graph=False):
+        fn = self.lib.cyl_step_graph if graph else self.lib.cyl_step
+        abi.check("cyl_step", fn(self.h, n))
+
+    def push_only(self):
+        abi.check("cyl_push_only", self.lib.cyl_push_only(self.h))
+
+    def sort(self):
+        abi.check("cyl_sort_particles", self.lib.cyl_sort_particles(self.h))
+
+    def state(self):
+        s = abi.RunState()
+        abi.check("cyl_get_run_state", self.lib.cyl_get_run_state(self.h, C.byref(s)))
+        return s
+
+    def diagnostics(self):
+        d = abi.Diag()
+        abi.check("cyl_diagnostics", self.lib.cyl_diagnostics(self.h, C.byref(d)))
+        return d
+
+    def rng_state(self):
+        r = abi.RngState()
+        abi.check("cyl_get_rng_state", self.lib.cyl_get_rng_state(self.h, C.byref(r)))
+        return r
+
+    def kernel_timing(self):
+        ms = C.c_double(0.0)
+        n = C.c_int64(0)
+        abi.check("cyl_kernel_timing", self.lib.cyl_kernel_timing(self.h, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    def cell_indices(self, isp=0):
+        n = C.c_int64(0)
+        abi.check("cyl_cell_indices", self.lib.cyl_cell_indices(self.h, isp, None, None, C.byref(n)))
+        cx = np.zeros(max(1, n.value), dtype=np.int32)
+        cy = np.zeros(max(1, n.value), dtype=np.int32)
+        abi.check("cyl_cell_indices", self.lib.cyl_cell_indices(self.h, isp, _p(cx, PI32), _p(cy, PI32),
+                                                                C.byref(n)))
+        return cx[:n.value], cy[:n.value]

@@ -1,0 +1,267 @@
+/*
+ * cylpic.h -- C ABI of the GB300 quasi-3D (x, r, theta-mode) PIC step.
+ *
+ * This is the drop-in boundary for the hot path of cylindrical EPOCH
+ * (epoch_axial).  In the reference the path is a set of argument-less Fortran
+ * module subroutines acting on module globals, called from the driver loop
+ * (epoch_axial/src/epoch2d.F90:213-265):
+ *
+ *   update_eb_fields_half  (epoch_axial/src/fields.f90:316)
+ *   push_particles         (epoch_axial/src/particles.F90:28)
+ *   current_finish         (epoch_axial/src/housekeeping/current_smooth.F90:29)
+ *   update_eb_fields_final (epoch_axial/src/fields.f90:341)
+ *   moving_window          (epoch_axial/src/housekeeping/window.F90:330)
+ *
+ * Here the state those routines share (complex mode fields, particle lists,
+ * window position, laser phases) is owned by an opaque handle that lives on
+ * one GPU.  Every entry point returns an int status: CYL_OK (0) or one of the
+ * CYL_ERR_* codes.  Host arrays are caller-owned and are only read or written
+ * during the call; no pointer is retained.  One handle per host thread.
+ *
+ * Units are SI throughout, exactly as in the reference.  Field arrays are
+ * complex FP64 in the reference's Fortran layout
+ *   F(1-ng:nx+ng, 1-ng:ny+ng, 0:n_mode-1),  ng = 5  (constants.F90:535-545)
+ * i.e. x fastest, interleaved (re, im) pairs, so a Fortran caller can pass
+ * C_LOC(exm) directly.
+ */
+#ifndef CYLPIC_H
+#define CYLPIC_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Ghost width of every mode array (triangle shape: png=3, ng=png+2,
+ * jng=MAX(ng,png); constants.F90:535-545). */
+#define CYL_NG 5
+
+/* ---- status codes (the reference aborts through abort_code(errcode),
+ *      utilities.f90:261; codes constants.F90:94-130) ---------------------- */
+#define CYL_OK 0
+#define CYL_ERR_BAD_ARG 1        /* null pointer, size out of range          */
+#define CYL_ERR_CUDA 2           /* a CUDA runtime call failed               */
+#define CYL_ERR_NO_DEVICE 3      /* no CUDA device visible                   */
+#define CYL_ERR_CAPACITY 4       /* particle capacity of a species exceeded  */
+#define CYL_ERR_UNSUPPORTED 5    /* option outside the implemented subset    */
+#define CYL_ERR_DEVICE_FLAG 6    /* a kernel raised its device error word    */
+#define CYL_ERR_TIMEOUT 7        /* a bounded host wait on the GPU ran out   */
+#define CYL_ERR_OUT_OF_MEMORY 8  /* device allocation failed                 */
+
+/* ---- boundary codes: the values of constants.F90:56-72 ------------------- */
+#define CYL_BC_PERIODIC 1
+#define CYL_BC_OTHER 2
+#define CYL_BC_SIMPLE_LASER 3
+#define CYL_BC_SIMPLE_OUTFLOW 4
+#define CYL_BC_OPEN 5
+#define CYL_BC_ZERO_GRADIENT 7
+#define CYL_BC_CLAMP 8
+#define CYL_BC_REFLECT 9
+#define CYL_BC_CONDUCT 10
+#define CYL_BC_ZERO_B 16
+
+/* Index of a boundary in the bc arrays below.  The reference numbers them
+ * c_bd_x_min=1 .. c_bd_y_max=4 (constants.F90:81-84); here they are 0-based. */
+#define CYL_BD_X_MIN 0
+#define CYL_BD_X_MAX 1
+#define CYL_BD_Y_MIN 2
+#define CYL_BD_Y_MAX 3
+
+/* Arithmetic form of the step. */
+#define CYL_PREC_FP64 0   /* plain form: FP64 everywhere, no FMA contraction */
+#define CYL_PREC_MIXED 1  /* int cell + FP32 offset, FP32 push/deposit      */
+
+/* Field array selectors for cyl_upload_field / cyl_download_field.  The
+ * order follows the module globals of shared_data.F90:474-478. */
+#define CYL_F_EXM 0
+#define CYL_F_ERM 1
+#define CYL_F_ETM 2
+#define CYL_F_BXM 3
+#define CYL_F_BRM 4
+#define CYL_F_BTM 5
+#define CYL_F_JXM 6
+#define CYL_F_JRM 7
+#define CYL_F_JTM 8
+#define CYL_F_BXM_OLD 9
+#define CYL_F_BRM_OLD 10
+#define CYL_F_BTM_OLD 11
+#define CYL_F_JXM_OLD 12
+#define CYL_F_JRM_OLD 13
+#define CYL_F_JTM_OLD 14
+#define CYL_NFIELDS 15
+
+/* Grid, boundaries and moving window.  Mirrors the control, boundaries and
+ * window deck blocks (deck_control_block.F90:236-476, window block
+ * deck_window_block.f90) after the deck has been evaluated by the host. */
+typedef struct cyl_grid_desc {
+  int32_t nx, ny;          /* cells along x (axis) and r                    */
+  int32_t n_mode;          /* azimuthal modes m = 0 .. n_mode-1             */
+  int32_t precision;       /* CYL_PREC_*                                     */
+  double x_min, x_max;     /* axial extent (m); cell-centred grid, setup.F90:164-206 */
+  double y_max;            /* radial extent (m); y_min = 0 is forced (deck_control_block.F90:74-75) */
+  double dt;               /* time step (s), as set_dt (setup.F90:629-670) computes it */
+  int32_t bc_field[4];     /* deck field bcs, before setup_boundaries mapping */
+  int32_t move_window;     /* window block: move_window                      */
+  double window_v_x;       /* window speed (m/s)                             */
+  double window_start_time, window_stop_time;
+  int32_t bc_after_move[4];/* bc_*_after_move (deck_window_block.f90:48-55)   */
+  int32_t smooth_currents; /* current_smooth.F90:37 (0 = off, the default)   */
+  int32_t smooth_its, smooth_comp_its, smooth_stride;
+} cyl_grid_desc;
+
+/* Particle species (deck species block).  The density/temperature profile
+ * is what insert_particles (window.F90:157-300) evaluates at the x_max
+ * column when the window moves; density_kind 0 is uniform, 1 a linear
+ * up-ramp n(x) = density * clamp((x - ramp_x0) / ramp_length, 0, 1). */
+typedef struct cyl_species_desc {
+  double charge, mass;      /* SI: C, kg                                      */
+  int32_t immobile;
+  int32_t bc_particle[4];   /* deck particle bcs                              */
+  int64_t capacity;         /* device particle capacity (>= live count)       */
+  double npart_per_cell;
+  int32_t density_kind;
+  double density, ramp_x0, ramp_length;
+  double density_min, density_max;  /* defaults EPSILON(1.0), HUGE (helper.F90:184-185) */
+  double temp[3];           /* temperature per direction (K)                   */
+  double drift[3];          /* momentum drift per direction (kg m/s)           */
+} cyl_species_desc;
+
+/* A laser on an x boundary (laser deck block, deck_laser_block.f90:90-260).
+ * The transverse profile and phase are the host-evaluated deck expressions
+ * at y(ir), ir = 0..ny (laser.f90:230-253).  The time envelope is either
+ * constant (t_profile 0) or gauss(time, t0, tw) = exp(-((time-t0)/tw)^2)
+ * (evaluator_blocks.F90:988-992), evaluated on the device every step. */
+typedef struct cyl_laser_desc {
+  int32_t boundary;          /* CYL_BD_X_MIN or CYL_BD_X_MAX                */
+  int32_t t_profile;         /* 0 = constant, 1 = gauss                     */
+  double amp, omega, pol_angle, t_start, t_end;
+  double t0, tw;
+  const double* profile;     /* ny+1 values                                 */
+  const double* phase;       /* ny+1 values                                 */
+} cyl_laser_desc;
+
+/* State of the reference's global KISS generator (random_generator.f90:28-33),
+ * carried across the host loader, the handle and the window injector. */
+typedef struct cyl_rng_state {
+  int32_t x, y, z, w;
+  int32_t box_muller_cached;
+  double cached_random_value;
+} cyl_rng_state;
+
+/* Scalars of a run that the Fortran module globals hold. */
+typedef struct cyl_run_state {
+  double time;
+  int64_t step;
+  double x_grid_min, xb_min, x_min, x_max;   /* moving window bookkeeping   */
+  double window_shift_fraction;
+  int32_t window_started;
+  int32_t bc_field[4];                       /* current, after mapping       */
+  int64_t n_live[8];                         /* live particles per species   */
+  int64_t n_shifts;                          /* window shifts so far         */
+} cyl_run_state;
+
+/* Diagnostics of the current state (calc_df.F90:1225-1321 for the kinetic
+ * energy; the field energy is the per-mode form of the cylindrical grid). */
+typedef struct cyl_diag {
+  double kinetic_energy;       /* sum w m c^2 (gamma-1), FP64               */
+  double field_energy_e;       /* sum over cells and modes of the E energy   */
+  double field_energy_b;
+  double jsum_abs;             /* sum |J| over interior (sanity)             */
+  int64_t n_live;
+  int32_t device_error;        /* device error word (0 = none)               */
+} cyl_diag;
+
+typedef struct cyl_handle_s* cyl_handle;
+
+/* ---- lifetime --------------------------------------------------------- */
+
+/* Allocate the device state of one run.  Replaces the allocation in
+ * mpi_initialise (mpi_routines.F90:385-400) and setup_boundaries
+ * (boundary.F90:30-75) for one GPU.  rng is the state of the global KISS
+ * generator after loading (it continues into window injection). */
+int cyl_create(const cyl_grid_desc* grid, const cyl_species_desc* species,
+               int32_t nspecies, const cyl_laser_desc* lasers, int32_t nlasers,
+               const cyl_rng_state* rng, cyl_handle* out);
+int cyl_destroy(cyl_handle h);
+
+/* Upload one species' particles (SoA host arrays of length n: Cartesian
+ * position x, y, z (m), momentum px, py, pz (kg m/s), weight, id).  The
+ * Fortran side packs these from its list (shared_data.F90:93-142). */
+int cyl_upload_particles(cyl_handle h, int32_t ispecies, const double* x,
+                         const double* y, const double* z, const double* px,
+                         const double* py, const double* pz, const double* w,
+                         const int64_t* id, int64_t n);
+/* Download the live particles of one species, in device order.  n_inout in:
+ * capacity of the host arrays; out: particles written. */
+int cyl_download_particles(cyl_handle h, int32_t ispecies, double* x, double* y,
+                           double* z, double* px, double* py, double* pz,
+                           double* w, int64_t* id, int64_t* n_inout);
+/* Copy one complex mode array (Fortran layout with ghosts, interleaved
+ * re/im, (nx+2ng)*(ny+2ng)*n_mode complex values). */
+int cyl_upload_field(cyl_handle h, int32_t which, const double* data);
+int cyl_download_field(cyl_handle h, int32_t which, double* data);
+
+/* Start-up sequence of epoch2d.F90:143-162 for a run that is not a restart:
+ * particle_bcs, efield_bcs, then bfield_final_bcs with dt halved and the
+ * time advanced to dt/2. */
+int cyl_initialise(cyl_handle h);
+
+/* Advance nsteps full PIC steps, i.e. nsteps iterations of the driver loop
+ * body epoch2d.F90:213-265: update_eb_fields_half, push_particles (with
+ * current_bcs_r_min_final and particle_bcs), current_finish,
+ * update_eb_fields_final, moving_window.  Window injection is generated by
+ * the handle's own KISS stream exactly as insert_particles does. */
+int cyl_step(cyl_handle h, int32_t nsteps);
+
+/* Same as cyl_step but the steps are captured once into a CUDA graph and
+ * replayed (one graph launch per call after the first). */
+int cyl_step_graph(cyl_handle h, int32_t nsteps);
+
+int cyl_get_run_state(cyl_handle h, cyl_run_state* out);
+int cyl_diagnostics(cyl_handle h, cyl_diag* out);
+int cyl_get_rng_state(cyl_handle h, cyl_rng_state* out);
+
+/* Sort each species' particles by cell tile and drop removed particles
+ * (the device analogue of reorder_particles_to_grid, split_particle.F90:29-73). */
+int cyl_sort_particles(cyl_handle h);
+
+/* Cell-sort indices of the live particles, in device order:
+ * cell_x = FLOOR((x - x_grid_min_local)/dx + 1.5),
+ * cell_y = FLOOR((r - y_grid_min_local)/dy + 1.5)  (split_particle.F90:61-62). */
+int cyl_cell_indices(cyl_handle h, int32_t ispecies, int32_t* cell_x,
+                     int32_t* cell_y, int64_t* n_inout);
+
+/* Push-and-deposit only (the body of push_particles, particles.F90:163-734,
+ * without current_bcs_r_min_final and particle_bcs): used by the parity tests
+ * and by the kernel benchmark to time the dominant kernel alone. */
+int cyl_push_only(cyl_handle h);
+
+/* Average duration (ms) of the push/deposit kernel over the launches since
+ * the last call, measured with CUDA events on the launching stream. */
+int cyl_kernel_timing(cyl_handle h, double* push_ms_avg, int64_t* launches);
+
+/* ---- host-side deck helpers (stand in for the Fortran loader) ---------- */
+
+/* KISS generator and polar Box-Muller of random_generator.f90:45-173. */
+void cyl_rng_init(cyl_rng_state* s, int32_t seed);
+double cyl_rng_random(cyl_rng_state* s);
+double cyl_rng_box_muller(cyl_rng_state* s, double stdev, double mu);
+
+/* Load one species the way auto_load does for a thermal species
+ * (helper.F90:95-169, 373-663, 669-811; particle_temperature.F90:30-81):
+ * uniform random positions per valid cell, weights from the triangle shape
+ * and the macro-particle volume, Maxwellian momenta by Box-Muller.  Two
+ * calls: with x == NULL it only returns the particle count in *n_inout
+ * (without touching the RNG); otherwise it fills the arrays (capacity
+ * *n_inout) and advances the RNG. */
+int cyl_host_load_species(const cyl_grid_desc* grid, const cyl_species_desc* sp,
+                          cyl_rng_state* rng, int64_t id_base, double* x,
+                          double* y, double* z, double* px, double* py,
+                          double* pz, double* w, int64_t* id, int64_t* n_inout);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CYLPIC_H */

@@ -1,0 +1,127 @@
+"""Parity of the CUDA FP64 path against the CPU oracle (through the C ABI).
+
+Tolerances (the benchmark spec): particle counts and cell-sort indices bit-exact;
+positions and momenta bit-exact after a push from identical state (the FP64
+kernels are built without FMA contraction); per-mode fields and currents
+within 1e-10 relative L2, the slack being the order of the FP64 atomic
+current adds.
+"""
+import numpy as np
+import pytest
+
+import cylindrical_epoch_gb300 as cg
+from tests.helpers import match_by_id, random_fields, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL_FIELD = 1.0e-10
+
+
+def _pair(deck, fields=None, initialise=True):
+    from oracle.oracle import Oracle
+    parts, rng = cg.host_load(deck)
+    gpu = cg.Run(deck, particles=parts, rng=rng, fields=fields, initialise=False)
+    orc = Oracle(deck, particles=parts, rng=rng)
+    if fields:
+        for k, v in fields.items():
+            orc.set_field(k, v)
+    if initialise:
+        gpu.lib.cyl_initialise(gpu.h)
+        orc.initialise()
+    return gpu, orc
+
+
+def _cmp_fields(gpu, orc, names, tol=TOL_FIELD):
+    worst = {}
+    for n in names:
+        a, b = gpu.field(n), orc.field(n)
+        for m in range(a.shape[0]):
+            if np.all(b[m] == 0) and np.all(a[m] == 0):
+                continue
+            e = rel_l2(a[m], b[m])
+            worst[f"{n}[m={m}]"] = e
+            assert e < tol, f"{n} mode {m}: rel L2 {e:.3e}"
+    return worst
+
+
+def test_push_bit_exact_positions(gpu_lib):
+    deck = cg.thermal_plasma(nx=48, ny=24, ppc=6)
+    flds = random_fields(deck, 1)
+    gpu, orc = _pair(deck, fields=flds, initialise=False)
+    gpu.push_only()
+    orc.stage("push")
+    a, b = match_by_id(gpu.particles(0), orc.particles(0))
+    for k in ("x", "y", "z", "px", "py", "pz", "w"):
+        assert np.array_equal(getattr(a, k), getattr(b, k)), k
+    _cmp_fields(gpu, orc, ["jxm", "jrm", "jtm"])
+
+
+def test_cell_indices_after_push(gpu_lib):
+    deck = cg.thermal_plasma(nx=40, ny=20, ppc=5)
+    flds = random_fields(deck, 2)
+    gpu, orc = _pair(deck, fields=flds, initialise=False)
+    gpu.push_only()
+    orc.stage("push")
+    ga = gpu.particles(0)
+    gx, gy = gpu.cell_indices(0)
+    ox, oy = orc.cell_indices(0)
+    ob = orc.particles(0)
+    og = np.argsort(ga.id)
+    oo = np.argsort(ob.id)
+    assert np.array_equal(gx[og], ox[oo])
+    assert np.array_equal(gy[og], oy[oo])
+
+
+def test_thermal_steps_parity(gpu_lib):
+    deck = cg.thermal_plasma(nx=64, ny=32, ppc=8)
+    gpu, orc = _pair(deck)
+    gpu.step(1)
+    orc.step(1)
+    a, b = match_by_id(gpu.particles(0), orc.particles(0))
+    for k in ("x", "y", "z", "px", "py", "pz"):
+        assert np.array_equal(getattr(a, k), getattr(b, k)), f"step 1 {k}"
+    gpu.step(9)
+    orc.step(9)
+    sg, so = gpu.state(), orc.state()
+    assert sg.n_live[0] == so.n_live[0]
+    a, b = match_by_id(gpu.particles(0), orc.particles(0))
+    for k in ("x", "y", "z"):
+        assert rel_l2(getattr(a, k), getattr(b, k)) < 1e-12
+    _cmp_fields(gpu, orc, ["exm", "erm", "etm", "bxm", "brm", "btm", "jxm", "jrm", "jtm"])
+
+
+def _small_wake(nsteps=80):
+    deck = cg.wakefield(nx=128, ny=32, ppc=4, density=3.0e24, ramp=2.0e-6)
+    # start the window early so that shifts happen inside a short test
+    deck.window_start_time = 20 * 5.0e-17
+    return deck
+
+
+def test_wakefield_window_parity(gpu_lib):
+    deck = _small_wake()
+    gpu, orc = _pair(deck)
+    for chunk in (1, 15, 24, 40):
+        gpu.step(chunk)
+        orc.step(chunk)
+        sg, so = gpu.state(), orc.state()
+        assert sg.step == so.step
+        assert sg.n_shifts == so.n_shifts
+        assert sg.x_grid_min == so.x_grid_min
+        assert sg.n_live[0] == so.n_live[0], (sg.n_live[0], so.n_live[0])
+    assert so.n_shifts > 10
+    a, b = match_by_id(gpu.particles(0), orc.particles(0))
+    for k in ("x", "y", "z"):
+        assert rel_l2(getattr(a, k), getattr(b, k)) < 1e-12
+    _cmp_fields(gpu, orc, ["exm", "erm", "etm", "bxm", "brm", "btm", "jxm", "jrm", "jtm"])
+
+
+def test_graph_matches_eager(gpu_lib):
+    deck = _small_wake()
+    parts, rng = cg.host_load(deck)
+    a = cg.Run(deck, particles=parts, rng=rng)
+    b = cg.Run(deck, particles=parts, rng=rng)
+    a.step(48, graph=False)
+    b.step(48, graph=True)
+    assert a.state().n_live[0] == b.state().n_live[0]
+    for n in ("exm", "btm", "jxm"):
+        assert rel_l2(b.field(n), a.field(n)) < 1e-10
