@@ -10,6 +10,7 @@
 // adds are FP64 atomics, whose order is the only source of difference in J.
 #include "cyl_common.cuh"
 #include "cyl_kernels.cuh"
+#include "../../include/cyl_math.h"
 
 namespace cyl {
 
@@ -131,7 +132,7 @@ __global__ void __launch_bounds__(256) k_push_fp64(FieldSet F, GeomTables g, Spe
     double part_r = sqrt(part_y * part_y + part_z * part_z);
     double part_r_local = part_r - y_grid_min_local;
     const cplx exp_min_itheta = mk(part_y / part_r, (-part_z) / part_r);
-    const double theta_05 = atan2(part_z, part_y);
+    const double theta_05 = cyl_atan2(part_z, part_y);
     const cplx exp_itheta_05 = crecip(exp_min_itheta);
 
     double gx[5] = {0, 0, 0, 0, 0}, gy[5] = {0, 0, 0, 0, 0};
@@ -241,7 +242,7 @@ __global__ void __launch_bounds__(256) k_push_fp64(FieldSet F, GeomTables g, Spe
     part_r = sqrt(part_y * part_y + part_z * part_z);
     part_r_local = part_r - y_grid_min_local;
     const cplx exp_itheta_15 = mk(part_y / part_r, part_z / part_r);
-    const double theta_15 = atan2(part_z, part_y);
+    const double theta_15 = cyl_atan2(part_z, part_y);
     const cplx exp_idtheta = exp_itheta_15 * exp_min_itheta;
     const double dtheta = theta_15 - theta_05;
 #pragma unroll

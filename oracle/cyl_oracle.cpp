@@ -17,6 +17,7 @@
 // path:line inside the reference project (epoch_axial/src/...).
 
 #include "../include/cylpic.h"
+#include "../include/cyl_math.h"
 
 #include <cmath>
 #include <cstdint>
@@ -924,7 +925,7 @@ void push_one(Sim& s, const Geom& g, Species& spc, size_t i, double part_q, doub
   double part_r = std::sqrt(part_y * part_y + part_z * part_z);
   double part_r_local = part_r - y_grid_min_local;
   cplx exp_min_itheta = mk(part_y / part_r, (-part_z) / part_r);
-  double theta_05 = std::atan2(part_z, part_y);
+  double theta_05 = cyl_atan2(part_z, part_y);
   cplx exp_min_itheta_05 = exp_min_itheta;
   cplx exp_itheta_05 = crecip(exp_min_itheta_05);
 
@@ -1039,7 +1040,7 @@ void push_one(Sim& s, const Geom& g, Species& spc, size_t i, double part_q, doub
   part_r = std::sqrt(part_y * part_y + part_z * part_z);
   part_r_local = part_r - y_grid_min_local;
   cplx exp_itheta_15 = mk(part_y / part_r, part_z / part_r);
-  double theta_15 = std::atan2(part_z, part_y);
+  double theta_15 = cyl_atan2(part_z, part_y);
   cplx exp_idtheta = exp_itheta_15 * exp_min_itheta_05;
   double dtheta = theta_15 - theta_05;
   for (int k = 0; k < 5; ++k) { gx[k] = hx[k]; gy[k] = hy[k]; }
@@ -1824,6 +1825,8 @@ int orc_cell_indices(orc_handle h, int32_t isp, int32_t* cx, int32_t* cy) {
   }
   return CYL_OK;
 }
+
+double orc_atan2(double y, double x) { return cyl_atan2(y, x); }
 
 double orc_dx(orc_handle h) { return ((Sim*)h)->dx; }
 double orc_dy(orc_handle h) { return ((Sim*)h)->dy; }

@@ -26,7 +26,8 @@ def build(force=False):
     the reference's default gfortran build on x86 and the product's FP64
     kernels)."""
     os.makedirs(BUILD, exist_ok=True)
-    deps = [SRC, os.path.join(HERE, "..", "include", "cylpic.h")]
+    deps = [SRC, os.path.join(HERE, "..", "include", "cylpic.h"),
+            os.path.join(HERE, "..", "include", "cyl_math.h")]
     if not force and os.path.exists(LIB) and all(os.path.getmtime(d) <= os.path.getmtime(LIB) for d in deps):
         return LIB
     tmp = LIB + ".tmp"
@@ -68,6 +69,7 @@ def load():
         "orc_get_run_state": (C.c_int, [H, C.POINTER(abi.RunState)]),
         "orc_diagnostics": (C.c_int, [H, C.POINTER(abi.Diag)]),
         "orc_cell_indices": (C.c_int, [H, C.c_int32, PI32, PI32]),
+        "orc_atan2": (C.c_double, [C.c_double, C.c_double]),
         "orc_dx": (C.c_double, [H]),
         "orc_dy": (C.c_double, [H]),
         "orc_time": (C.c_double, [H]),
