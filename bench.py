@@ -1,0 +1,356 @@
+"""Benchmark of the quasi-3D PIC step on one GB300 (and N replicas).
+
+Metric: particle-steps/s = mobile particles pushed x steps / wall time of
+the full step (fields + boundaries + push/deposit + moving window), on the
+laser-wakefield deck (2048 x 256 cells, modes m = 0..1, 8 particles per cell,
+moving window at c).  A step is one iteration of the reference's driver loop
+(epoch2d.F90:213-265).  The timed steps are steps [W, W+K) of the deck run
+from t = 0 (the default K = 2000 is the whole deck run).
+
+Arms:
+  default             this package, CUDA graphs, device-resident state
+  --impl reference    the CPU restatement of the reference's step (oracle/)
+                      on all host threads, on a bounded sample of the deck
+
+Prints one JSON line (rank 0).
+"""
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _profile_traffic(form):
+    """DRAM bytes per push launch from the committed ncu summary, scaled to
+    the benchmark workload (profiles/push_<form>_traffic.json)."""
+    p = os.path.join(ROOT, "profiles", f"push_{form}_traffic.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return d
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for k, n in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(deck, parts, rng, seconds=12.0, threads=None):
+    """The oracle (CPU restatement of the reference step) on all host threads,
+    on a bounded sample of the same deck: as many steps from the loaded state
+    as fit in about `seconds`."""
+    from oracle.oracle import Oracle, load
+    lib = load()
+    nt = threads or os.cpu_count() or 1
+    lib.orc_set_threads(nt)
+    orc = Oracle(deck, particles=parts, rng=rng)
+    orc.initialise()
+    n0 = sum(p.n for p in parts)
+    t0 = time.perf_counter()
+    steps = 0
+    while True:
+        orc.step(1)
+        steps += 1
+        if time.perf_counter() - t0 >= seconds or steps >= 400:
+            break
+    dt = time.perf_counter() - t0
+    n1 = sum(orc.state().n_live[i] for i in range(len(deck.species)))
+    lib.orc_set_threads(1)
+    return {"value": 0.5 * (n0 + n1) * steps / dt, "unit": "particle-steps/s", "cores": nt,
+            "kind": "port", "sample": f"{steps} oracle steps of the deck from t=0 ({n0} particles), "
+                                      f"{dt:.1f} s, {nt} OpenMP threads"}
+
+
+def build_deck(name, form):
+    import cylindrical_epoch_gb300 as cg
+    from cylindrical_epoch_gb300 import abi
+    prec = abi.PREC_MIXED if form == "mixed" else abi.PREC_FP64
+    if name == "wakefield":
+        return cg.wakefield(precision=prec)
+    if name == "thermal":
+        return cg.thermal_plasma(precision=prec)
+    if name == "large":
+        return cg.large_wakefield(precision=prec)
+    raise ValueError(name)
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return 0
+    import cylindrical_epoch_gb300 as cg
+    form = "fp64"
+    deck = build_deck(args.deck, form)
+    parts, rng = cg.host_load(deck)
+    base = cpu_baseline(deck, parts, rng, seconds=min(60.0, 5.0 + 0.02 * args.steps))
+    line = {
+        "impl": "reference", "metric": "particle-steps/s", "value": base["value"],
+        "unit": "particle-steps/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": _config(args, deck, form),
+        "cpu_baseline": base,
+        "e2e": {"value": base["value"], "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def _config(args, deck, form):
+    return {"workload": f"{deck.name} {deck.nx}x{deck.ny} m=0..{deck.n_mode - 1} "
+                        f"{deck.species[0].npart_per_cell:g} ppc, steps [W, W+K) of the deck from t=0",
+            "form": form, "nx": deck.nx, "ny": deck.ny, "n_mode": deck.n_mode,
+            "ppc": deck.species[0].npart_per_cell, "moving_window": deck.move_window,
+            "l2": "state larger than L2 (fields 15 x (nx+10)(ny+10) M complex + particles)",
+            "parallelism": f"replicas x{args.gpus}"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--form", default="auto", choices=["auto", "fp64", "mixed"])
+    ap.add_argument("--deck", default="wakefield", choices=["wakefield", "thermal", "large"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--eager", action="store_true", help="no CUDA graphs")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        return run_reference(args, rank)
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    import cylindrical_epoch_gb300 as cg
+    from cylindrical_epoch_gb300 import abi, build
+    build.build()
+    lib = cg.load()
+    form = args.form
+    if form == "auto":
+        form = "fp64"
+        probe = build_deck("thermal", "mixed")
+        g = probe.grid_desc()
+        sp = probe.species_descs()
+        h = C.c_void_p()
+        rc = lib.cyl_create(C.byref(g), sp, 1, None, 0, None, C.byref(h))
+        if rc == abi.CYL_OK:
+            lib.cyl_destroy(h)
+            form = "mixed"
+    deck = build_deck(args.deck, form)
+    parts, rng = cg.host_load(deck)
+    run = cg.Run(deck, particles=parts, rng=rng)
+    graph = not args.eager
+
+    run.step(args.warmup, graph=False)
+    run.kernel_timing()  # reset counters
+    s0 = run.state()
+    n_start = sum(s0.n_live[i] for i in range(len(deck.species)) if not deck.species[i].immobile)
+    clocks = ClockSampler(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    t0 = time.perf_counter()
+    run.step(args.steps, graph=graph)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    elapsed = t1 - t0
+    push_ms, launches = run.kernel_timing()
+    s1 = run.state()
+    n_end = sum(s1.n_live[i] for i in range(len(deck.species)) if not deck.species[i].immobile)
+    psteps = 0.5 * (n_start + n_end) * args.steps
+    if dist:
+        t = torch.tensor([elapsed, psteps], dtype=torch.float64, device="cuda")
+        tm = t.clone()
+        dist.all_reduce(tm[:1], op=dist.ReduceOp.MAX)
+        dist.all_reduce(t[1:], op=dist.ReduceOp.SUM)
+        elapsed, psteps = float(tm[0]), float(t[1])
+    value = psteps / elapsed
+
+    # roofline of the dominant kernel (push + deposit): algorithmic bytes per
+    # particle-step = particle state in + out + amortised field read and
+    # current read-modify-write
+    M = deck.n_mode
+    ppc = deck.species[0].npart_per_cell
+    per_particle = (104.0 if form == "fp64" else 60.0) + 192.0 * M / ppc
+    nparts = 0.5 * (n_start + n_end)
+    peak, peak_kind = _peaks()
+    achieved = per_particle * nparts / (push_ms * 1e-3) / 1e9 if push_ms > 0 else None
+    prof = _profile_traffic(form)
+    traffic = None
+    if prof and prof.get("bytes_per_particle"):
+        traffic = prof["bytes_per_particle"] * nparts
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                "peak_kind": peak_kind, "kernel": f"k_push_{form}",
+                "kernel_ms": push_ms, "algorithmic_bytes_per_particle_step": per_particle}
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = e2e_run(deck, parts, rng, args.steps, graph)
+        if dist:
+            t = torch.tensor([e2e["seconds"], e2e["psteps"]], dtype=torch.float64, device="cuda")
+            tm = t.clone()
+            dist.all_reduce(tm[:1], op=dist.ReduceOp.MAX)
+            dist.all_reduce(t[1:], op=dist.ReduceOp.SUM)
+            e2e["value"] = float(t[1]) / float(tm[0])
+    base = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        base = cpu_baseline(build_deck(args.deck, "fp64"), parts, rng)
+
+    if rank == 0:
+        line = {
+            "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if form == "fp64" else "f32+f64",
+            "data": "synthetic", "config": _config(args, deck, form),
+            "roofline": roofline, "clocks": clk, "gpu_launches": launches,
+            "particles": nparts,
+        }
+        if e2e:
+            line["e2e"] = {"value": e2e["value"], "unit": "particle-steps/s",
+                           "h2d_bytes_per_step": e2e["h2d"] / args.steps,
+                           "d2h_bytes_per_step": e2e["d2h"] / args.steps}
+        if base:
+            line["cpu_baseline"] = base
+        print(json.dumps(line))
+    run.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def e2e_run(deck, parts, rng, steps, graph):
+    """The same run through the C ABI with host buffers: the initial state
+    is copied from pinned host memory, every 16 steps the diagnostics are
+    read back, and the final particles and fields are copied to the host,
+    all inside the timed region."""
+    import numpy as np
+    import torch
+    import cylindrical_epoch_gb300 as cg
+    from cylindrical_epoch_gb300 import abi
+    pinned = []
+    for p in parts:
+        q = cg.Particles(0)
+        for k in q.__slots__:
+            src = getattr(p, k)
+            t = torch.empty(src.shape[0], dtype=torch.float64 if src.dtype == np.float64 else torch.int64,
+                            pin_memory=True)
+            a = t.numpy()
+            a[:] = src
+            setattr(q, k, a)
+        pinned.append(q)
+    h2d = sum(sum(getattr(p, k).nbytes for k in p.__slots__) for p in pinned)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    run = cg.Run(deck, particles=pinned, rng=rng)
+    d2h = 0
+    left = steps
+    while left > 0:
+        k = min(16, left)
+        run.step(k, graph=graph)
+        run.diagnostics()
+        d2h += C.sizeof(abi.Diag)
+        left -= k
+    outp = [run.particles(i) for i in range(len(deck.species))]
+    fields = [run.field(n) for n in ("exm", "erm", "etm", "bxm", "brm", "btm")]
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    s = run.state()
+    d2h += sum(sum(getattr(p, k).nbytes for k in p.__slots__) for p in outp)
+    d2h += sum(f.nbytes for f in fields)
+    n0 = sum(p.n for p in parts)
+    n1 = sum(s.n_live[i] for i in range(len(deck.species)))
+    run.close()
+    # per-step host inputs (step records, laser sources, injected particles)
+    # are copied inside cyl_step; count their bytes
+    h2d += steps * (512 + 4 * 8 * (deck.ny + 1))
+    return {"seconds": t1 - t0, "psteps": 0.5 * (n0 + n1) * steps, "value": 0.5 * (n0 + n1) * steps / (t1 - t0),
+            "h2d": h2d, "d2h": d2h}
+
+
+if __name__ == "__main__":
+    sys.exit(main())

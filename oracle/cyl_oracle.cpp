@@ -193,6 +193,7 @@ struct Sim {
   std::vector<Laser> lasers;
   Rng rng;
   int smooth, smooth_its, smooth_comp_its, smooth_stride;
+  std::vector<Field> thread_j;  // per-thread currents of the multi-threaded timing form
 
   Field* field(int which) {
     Field* t[15] = {&ex, &er, &et, &bx, &br, &bt, &jx, &jr, &jt,
@@ -867,6 +868,8 @@ void smooth_mode_array(Sim& s, Field& f) {
 
 // ------------------------------------------------------------ particles
 
+int g_threads = 1;
+
 struct Geom {
   std::vector<double> inv_area_rt, inv_area_xt, inv_volume, ratio_area_xt;
   int lo;  // index offset: arrays start at 1-jng (inv_area_xt at 0-jng)
@@ -901,7 +904,7 @@ inline int fdiv2(int v) { return v / 2; }
 
 // The body of push_particles for one particle (particles.F90:270-665).
 void push_one(Sim& s, const Geom& g, Species& spc, size_t i, double part_q, double part_mc,
-              double ipart_mc, double cmratio, double ccmratio) {
+              double ipart_mc, double cmratio, double ccmratio, Field& JX, Field& JR, Field& JT) {
   const double fac = 0.25;  // (0.5)**c_ndims
   const double idx = 1.0 / s.dx, idy = 1.0 / s.dy, idt = 1.0 / s.dt;
   const double dto2 = s.dt / 2.0, dtco2 = C * dto2;
@@ -1126,9 +1129,9 @@ void push_one(Sim& s, const Geom& g, Species& spc, size_t i, double part_q, doub
         jxh = jxh - (fjx * hx[ix + 2]) * w_rt;
         jyh[ix + 2] = jyh[ix + 2] * rat - fjy * w_xt;
         cplx jzh = fjz * w_xr;
-        s.jx(cx + 1, cy, im) = s.jx(cx + 1, cy, im) + jxh;
-        s.jr(cx, cy + 1, im) = s.jr(cx, cy + 1, im) + jyh[ix + 2];
-        s.jt(cx, cy, im) = s.jt(cx, cy, im) + jzh;
+        JX(cx + 1, cy, im) = JX(cx + 1, cy, im) + jxh;
+        JR(cx, cy + 1, im) = JR(cx, cy + 1, im) + jyh[ix + 2];
+        JT(cx, cy, im) = JT(cx, cy, im) + jzh;
       }
     }
   }
@@ -1151,7 +1154,34 @@ void push_particles_core(Sim& s) {
     double ipart_mc = 1.0 / part_mc;
     double cmratio = (part_q * dtfac) * ipart_mc;
     double ccmratio = C * cmratio;
-    for (size_t i = 0; i < spc.n(); ++i) push_one(s, g, spc, i, part_q, part_mc, ipart_mc, cmratio, ccmratio);
+    if (g_threads <= 1) {
+      for (size_t i = 0; i < spc.n(); ++i)
+        push_one(s, g, spc, i, part_q, part_mc, ipart_mc, cmratio, ccmratio, s.jx, s.jr, s.jt);
+      continue;
+    }
+    // Multi-threaded timing form (CPU baseline only): private current
+    // arrays per thread, summed afterwards; positions are unaffected.
+    const int nt = g_threads;
+    std::vector<Field>& pj = s.thread_j;
+    if ((int)pj.size() != 3 * nt) {
+      pj.assign(3 * nt, Field());
+      for (auto& f : pj) f.init(s.nx, s.ny, s.M);
+    }
+    const long long n = (long long)spc.n();
+#pragma omp parallel for num_threads(nt) schedule(static)
+    for (int t = 0; t < nt; ++t) {
+      for (int c = 0; c < 3; ++c) std::fill(pj[3 * t + c].a.begin(), pj[3 * t + c].a.end(), mk(0, 0));
+      const long long a = n * t / nt, b = n * (t + 1) / nt;
+      for (long long i = a; i < b; ++i)
+        push_one(s, g, spc, (size_t)i, part_q, part_mc, ipart_mc, cmratio, ccmratio, pj[3 * t], pj[3 * t + 1],
+                 pj[3 * t + 2]);
+    }
+    Field* dst[3] = {&s.jx, &s.jr, &s.jt};
+    const size_t ne = s.jx.a.size();
+#pragma omp parallel for num_threads(nt) schedule(static)
+    for (long long e = 0; e < (long long)ne; ++e)
+      for (int t = 0; t < nt; ++t)
+        for (int c = 0; c < 3; ++c) dst[c]->a[e] = dst[c]->a[e] + pj[3 * t + c].a[e];
   }
 }
 
@@ -1825,6 +1855,8 @@ int orc_cell_indices(orc_handle h, int32_t isp, int32_t* cx, int32_t* cy) {
   }
   return CYL_OK;
 }
+
+void orc_set_threads(int32_t n) { g_threads = n < 1 ? 1 : n; }
 
 double orc_atan2(double y, double x) { return cyl_atan2(y, x); }
 

@@ -70,6 +70,7 @@ def load():
         "orc_diagnostics": (C.c_int, [H, C.POINTER(abi.Diag)]),
         "orc_cell_indices": (C.c_int, [H, C.c_int32, PI32, PI32]),
         "orc_atan2": (C.c_double, [C.c_double, C.c_double]),
+        "orc_set_threads": (None, [C.c_int32]),
         "orc_dx": (C.c_double, [H]),
         "orc_dy": (C.c_double, [H]),
         "orc_time": (C.c_double, [H]),
