@@ -27,6 +27,8 @@ SOURCES = [
     ("fields.cu", ["--fmad=false"]),
     ("push_fp64.cu", ["--fmad=false"]),
     ("particles.cu", ["--fmad=false"]),
+    ("push_mixed.cu", ["--fmad=true"]),
+    ("mixed_particles.cu", ["--fmad=true"]),
     ("host_deck.cpp", []),
 ]
 

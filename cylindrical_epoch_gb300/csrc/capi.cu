@@ -16,6 +16,7 @@
 #include "cyl_common.cuh"
 #include "cyl_kernels.cuh"
 #include "host_deck.h"
+#include "push_mixed.cuh"
 
 namespace cyl {
 
@@ -36,10 +37,6 @@ struct HostLaser {
   double current_integral_phase = 0.0;
 };
 
-// push-mixed.cu (mixed precision form)
-void launch_push_mixed(cudaStream_t s, const FieldSet& F, const GeomTables& g, const SpeciesPtrs& sp,
-                       SpeciesCounters* cnt, const StepRec* rec, const RunConst& rc, int apply_bcs,
-                       int* err, int nblocks);
 
 struct Handle {
   int device = 0;
@@ -95,6 +92,12 @@ struct Handle {
   double push_ms_sum = 0.0;
   int64_t push_launches = 0;
   int nblocks = 152 * 8;
+  int nblocks_mixed = 152 * 4;
+  double xg0 = 0.0;  // x_grid_min at creation: origin of the mixed form's cell index
+  MixedParams mp[MAX_SPECIES];
+  TileTable* d_tiles = nullptr;     // one per species
+  int64_t* d_tile_start = nullptr;  // (ntiles_max + 1) per species
+  int ntiles_max = 0;
   int64_t kernel_launches = 0;
   int64_t graph_launches = 0;
 };
@@ -190,6 +193,7 @@ static void prepare_step(Handle* h, int k, int64_t& inj_used) {
   StepRec& r = h->h_rec[k];
   std::memset(&r, 0, sizeof(r));
   r.time_half = h->time;
+  r.nshift_total = (int32_t)h->n_shifts;
   fill_grid(r, h->g, false);
   for (int i = 0; i < 4; ++i) {
     r.bc_field[i] = h->bc_field[i];
@@ -248,6 +252,7 @@ static void prepare_step(Handle* h, int k, int64_t& inj_used) {
     }
   }
   r.nshift = nshift;
+  r.nshift_total_after = (int32_t)h->n_shifts;
   for (int i = 0; i < 4; ++i) r.bc_field_after[i] = h->bc_field[i];
   fill_grid(r, h->g, true);
 }
@@ -256,12 +261,11 @@ static void count_launch(Handle* h, int n) { h->kernel_launches += n; }
 
 static void push_species(Handle* h, cudaStream_t s, const FieldSet& F, int i, const StepRec* rec,
                          int apply_bcs) {
-#ifdef CYL_WITH_MIXED
   if (h->prec == CYL_PREC_MIXED) {
-    launch_push_mixed(s, F, h->geom, h->sp[i], h->d_cnt + i, rec, h->rc, apply_bcs, h->d_err, h->nblocks);
+    launch_push_mixed(s, F, h->geom, h->sp[i], h->d_cnt + i, rec, h->rc, apply_bcs, h->d_err,
+                      h->nblocks_mixed, h->mp[i], h->d_tiles + i);
     return;
   }
-#endif
   launch_push_fp64(s, F, h->geom, h->sp[i], h->d_cnt + i, rec, h->rc, apply_bcs, h->d_err, h->nblocks);
 }
 
@@ -306,7 +310,10 @@ static void enqueue_step(Handle* h, const StepRec* rec, const double* src, int k
   // moving_window
   if (h->move_window) {
     for (int i = 0; i < h->nsp; ++i) {
-      launch_window_particles(s, h->sp[i], h->d_cnt + i, h->d_inj, rec, i, rc, h->d_err, h->nblocks);
+      if (h->prec == CYL_PREC_MIXED)
+        mixed_window_particles(s, h->sp[i], h->d_cnt + i, h->d_inj, rec, i, h->xg0, rc, h->d_err, h->nblocks);
+      else
+        launch_window_particles(s, h->sp[i], h->d_cnt + i, h->d_inj, rec, i, rc, h->d_err, h->nblocks);
       count_launch(h, 3);
     }
     launch_shift_fields(s, F, h->cols, rec, 0, rc);
@@ -317,10 +324,17 @@ static void enqueue_step(Handle* h, const StepRec* rec, const double* src, int k
 
 // Counting sort of every species by cell; xgm points at the device copy of
 // the current x_grid_min (the grid moves with the window).
-static void enqueue_sort(Handle* h, const double* xgm) {
+static void enqueue_sort(Handle* h, const StepRec* rec) {
   for (int i = 0; i < h->nsp; ++i) {
-    sort_species(h->st, h->sp[i], h->d_cnt + i, h->sc, xgm, h->rc, h->nblocks);
-    count_launch(h, 7);
+    if (h->sp[i].immobile) continue;
+    if (h->prec == CYL_PREC_MIXED) {
+      mixed_sort(h->st, h->sp[i], h->d_cnt + i, h->sc, h->d_tiles + i,
+                 h->d_tile_start + (size_t)i * (h->ntiles_max + 1), rec, h->rc, h->nblocks);
+      count_launch(h, 9);
+    } else {
+      sort_species(h->st, h->sp[i], h->d_cnt + i, h->sc, &rec->x_grid_min_after, h->rc, h->nblocks);
+      count_launch(h, 7);
+    }
   }
 }
 
@@ -337,6 +351,15 @@ static int alloc_species(Handle* h, int i, const cyl_species_desc& d) {
   p.pz = buf + 5 * cap;
   p.w = buf + 6 * cap;
   p.id = (int64_t*)(buf + 7 * cap);
+  p.kx = (int32_t*)buf;
+  float* fb = (float*)buf + cap;
+  p.fx = fb;
+  p.fy = fb + cap;
+  p.fz = fb + 2 * cap;
+  p.ux = fb + 3 * cap;
+  p.uy = fb + 4 * cap;
+  p.uz = fb + 5 * cap;
+  p.fw = fb + 6 * cap;
   p.cap = cap;
   p.charge = d.charge;
   p.mass = d.mass;
@@ -399,7 +422,7 @@ static int run_chunk(Handle* h, int k, bool use_graph) {
     CK(cudaMemcpyAsync(h->d_inj, h->h_inj, sizeof(double) * 8 * inj_used, cudaMemcpyHostToDevice, h->st));
   CK(cudaEventRecord(h->ev_copy, h->st));
   h->copy_pending = true;
-  const double* xgm = &h->d_rec[k - 1].x_grid_min_after;
+  const StepRec* last = h->d_rec + (k - 1);
   if (use_graph && k == CHUNK) {
     const int par0 = h->jpar;
     if (!h->gexec || h->graph_parity != par0) {
@@ -412,7 +435,7 @@ static int run_chunk(Handle* h, int k, bool use_graph) {
       CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
       for (int i = 0; i < k; ++i)
         enqueue_step(h, h->d_rec + i, h->d_src + h->src_per_step * i, i, true, true);
-      enqueue_sort(h, xgm);
+      enqueue_sort(h, last);
       CK(cudaStreamEndCapture(h->st, &graph));
       CK(cudaGraphInstantiate(&h->gexec, graph, 0));
       cudaGraphDestroy(graph);
@@ -428,7 +451,7 @@ static int run_chunk(Handle* h, int k, bool use_graph) {
   } else {
     for (int i = 0; i < k; ++i)
       enqueue_step(h, h->d_rec + i, h->d_src + h->src_per_step * i, i, true, false);
-    enqueue_sort(h, xgm);
+    enqueue_sort(h, last);
   }
   CK(cudaEventSynchronize(h->ev_push[k - 1][1]));
   collect_push_timing(h, k);
@@ -452,9 +475,7 @@ int cyl_create(const cyl_grid_desc* gd, const cyl_species_desc* spd, int32_t nsp
   if (nsp < 0 || nsp > MAX_SPECIES || nlas < 0 || nlas > MAX_LASERS) return CYL_ERR_BAD_ARG;
   if (!(gd->dt > 0.0) || !(gd->x_max > gd->x_min) || !(gd->y_max > 0.0)) return CYL_ERR_BAD_ARG;
   if (gd->precision != CYL_PREC_FP64 && gd->precision != CYL_PREC_MIXED) return CYL_ERR_BAD_ARG;
-#ifndef CYL_WITH_MIXED
-  if (gd->precision == CYL_PREC_MIXED) return CYL_ERR_UNSUPPORTED;
-#endif
+
   for (int i = 0; i < nlas; ++i) {
     if (las[i].boundary != CYL_BD_X_MIN && las[i].boundary != CYL_BD_X_MAX) return CYL_ERR_UNSUPPORTED;
     if (!las[i].profile || !las[i].phase) return CYL_ERR_BAD_ARG;
@@ -565,6 +586,14 @@ int cyl_create(const cyl_grid_desc* gd, const cyl_species_desc* spd, int32_t nsp
     }
     if (h->sp[i].cap > maxcap) maxcap = h->sp[i].cap;
   }
+  h->xg0 = h->g.x_grid_min;
+  h->ntiles_max = (rc.nx / TILE_X + 3) * (rc.ny / TILE_Y + 2);
+  cudaMalloc(&h->d_tiles, sizeof(TileTable) * MAX_SPECIES);
+  cudaMemset(h->d_tiles, 0, sizeof(TileTable) * MAX_SPECIES);
+  cudaMalloc(&h->d_tile_start, sizeof(int64_t) * (h->ntiles_max + 1) * MAX_SPECIES);
+  cudaMemset(h->d_tile_start, 0, sizeof(int64_t) * (h->ntiles_max + 1) * MAX_SPECIES);
+  for (int i = 0; i < nsp; ++i) h->mp[i] = mixed_params(h->sp[i], rc);
+  h->nblocks_mixed = nsm * push_mixed_blocks_per_sm(rc.M);
   cudaMalloc(&h->d_cnt, sizeof(SpeciesCounters) * MAX_SPECIES);
   cudaMemset(h->d_cnt, 0, sizeof(SpeciesCounters) * MAX_SPECIES);
   // sort scratch: keys, histogram, block sums, 7 doubles + id per particle
@@ -628,6 +657,8 @@ int cyl_destroy(cyl_handle hh) {
   cudaFree(h->cols);
   cudaFree(h->geom_buf);
   cudaFree(h->d_cnt);
+  cudaFree(h->d_tiles);
+  cudaFree(h->d_tile_start);
   cudaFree(h->sort_buf);
   cudaFree(h->d_err);
   cudaFree(h->d_red);
@@ -658,7 +689,15 @@ int cyl_upload_particles(cyl_handle hh, int32_t isp, const double* x, const doub
   if (n > p.cap) return CYL_ERR_CAPACITY;
   cudaStream_t s = h->st;
   const size_t b = (size_t)n * 8;
-  if (n > 0) {
+  if (n > 0 && h->prec == CYL_PREC_MIXED) {
+    // stage the FP64 arrays in the sort scratch, convert on the device
+    double* st = h->sc.tmp;
+    const int64_t cap = h->sc.cap;
+    const double* srcs[7] = {x, y, z, px, py, pz, w};
+    for (int k = 0; k < 7; ++k) CK(cudaMemcpyAsync(st + (size_t)k * cap, srcs[k], b, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(st + (size_t)7 * cap, id, b, cudaMemcpyHostToDevice, s));
+    mixed_from_double(s, p, st, n, cap, h->xg0, h->rc);
+  } else if (n > 0) {
     CK(cudaMemcpyAsync(p.x, x, b, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(p.y, y, b, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(p.z, z, b, cudaMemcpyHostToDevice, s));
@@ -687,10 +726,20 @@ int cyl_download_particles(cyl_handle hh, int32_t isp, double* x, double* y, dou
   const int64_t n = c.n_used;
   std::vector<double> buf((size_t)n * 8);
   SpeciesPtrs& p = h->sp[isp];
-  double* srcs[7] = {p.x, p.y, p.z, p.px, p.py, p.pz, p.w};
-  for (int k = 0; k < 7; ++k)
-    CK(cudaMemcpy(buf.data() + (size_t)k * n, srcs[k], (size_t)n * 8, cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(buf.data() + (size_t)7 * n, p.id, (size_t)n * 8, cudaMemcpyDeviceToHost));
+  if (h->prec == CYL_PREC_MIXED) {
+    double* st = h->sc.tmp;
+    const int64_t cap = h->sc.cap;
+    mixed_to_double(h->st, p, st, n, cap, h->xg0, h->rc);
+    for (int k = 0; k < 8; ++k)
+      CK(cudaMemcpyAsync(buf.data() + (size_t)k * n, st + (size_t)k * cap, (size_t)n * 8, cudaMemcpyDeviceToHost,
+                         h->st));
+    CK(cudaStreamSynchronize(h->st));
+  } else {
+    double* srcs[7] = {p.x, p.y, p.z, p.px, p.py, p.pz, p.w};
+    for (int k = 0; k < 7; ++k)
+      CK(cudaMemcpy(buf.data() + (size_t)k * n, srcs[k], (size_t)n * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(buf.data() + (size_t)7 * n, p.id, (size_t)n * 8, cudaMemcpyDeviceToHost));
+  }
   int64_t live = 0;
   for (int64_t i = 0; i < n; ++i)
     if (!std::isnan(buf[i])) live++;
@@ -746,6 +795,7 @@ int cyl_initialise(cyl_handle hh) {
     r.add_laser[i] = h->add_laser[i];
     r.bc_field_after[i] = h->bc_field[i];
   }
+  r.nshift_total = r.nshift_total_after = (int32_t)h->n_shifts;
   // epoch2d.F90:157-161: dt halved, time advanced by it, bfield_final_bcs
   const double dt_half = h->g.dt / 2.0;
   h->time = h->time + dt_half;
@@ -753,10 +803,18 @@ int cyl_initialise(cyl_handle hh) {
   laser_sources(h, h->h_src);
   CK(cudaMemcpyAsync(h->d_rec, h->h_rec, sizeof(StepRec), cudaMemcpyHostToDevice, h->st));
   CK(cudaMemcpyAsync(h->d_src, h->h_src, sizeof(double) * h->src_per_step, cudaMemcpyHostToDevice, h->st));
-  for (int i = 0; i < h->nsp; ++i) launch_particle_bcs(h->st, h->sp[i], h->d_cnt + i, h->d_rec, 0, h->rc, h->nblocks);
+  for (int i = 0; i < h->nsp; ++i) {
+    if (h->prec == CYL_PREC_MIXED)
+      mixed_particle_bcs(h->st, h->sp[i], h->d_cnt + i, h->d_rec, h->rc, h->nblocks);
+    else
+      launch_particle_bcs(h->st, h->sp[i], h->d_cnt + i, h->d_rec, 0, h->rc, h->nblocks);
+  }
   FieldSet F = fieldset(h, h->jpar);
   launch_efield_bcs(h->st, F, h->d_rec, h->rc);
   launch_b_final_bcs(h->st, F, h->d_rec, h->d_src, h->cols, 0, dt_half, h->rc);
+  if (h->prec == CYL_PREC_MIXED) enqueue_sort(h, h->d_rec);
+  CK(cudaEventRecord(h->ev_copy, h->st));
+  h->copy_pending = true;
   return sync_and_check(h);
 }
 
@@ -838,7 +896,10 @@ int cyl_diagnostics(cyl_handle hh, cyl_diag* out) {
   if (!hh || !out) return CYL_ERR_BAD_ARG;
   Handle* h = &hh->h;
   CK(cudaMemsetAsync(h->d_red, 0, 8 * sizeof(double), h->st));
-  for (int i = 0; i < h->nsp; ++i) launch_energy(h->st, h->sp[i], h->d_cnt + i, h->d_red, h->nblocks);
+  for (int i = 0; i < h->nsp; ++i) {
+    if (h->prec == CYL_PREC_MIXED) mixed_energy(h->st, h->sp[i], h->d_cnt + i, h->d_red, h->nblocks);
+    else launch_energy(h->st, h->sp[i], h->d_cnt + i, h->d_red, h->nblocks);
+  }
   launch_field_energy(h->st, fieldset(h, h->jpar), h->rc, h->d_red + 2);
   double red[8];
   CK(cudaMemcpyAsync(red, h->d_red, sizeof(red), cudaMemcpyDeviceToHost, h->st));
@@ -863,8 +924,16 @@ int cyl_get_rng_state(cyl_handle hh, cyl_rng_state* out) {
 int cyl_sort_particles(cyl_handle hh) {
   if (!hh) return CYL_ERR_BAD_ARG;
   Handle* h = &hh->h;
-  CK(cudaMemcpyAsync(h->d_red + 7, &h->g.x_grid_min, sizeof(double), cudaMemcpyHostToDevice, h->st));
-  enqueue_sort(h, h->d_red + 7);
+  if (h->copy_pending) CK(cudaEventSynchronize(h->ev_copy));
+  StepRec& r = h->h_rec[0];
+  std::memset(&r, 0, sizeof(r));
+  fill_grid(r, h->g, false);
+  fill_grid(r, h->g, true);
+  r.nshift_total = r.nshift_total_after = (int32_t)h->n_shifts;
+  CK(cudaMemcpyAsync(h->d_rec + CHUNK, h->h_rec, sizeof(StepRec), cudaMemcpyHostToDevice, h->st));
+  CK(cudaEventRecord(h->ev_copy, h->st));
+  h->copy_pending = true;
+  enqueue_sort(h, h->d_rec + CHUNK);
   return sync_and_check(h);
 }
 
@@ -882,8 +951,12 @@ int cyl_cell_indices(cyl_handle hh, int32_t isp, int32_t* cx, int32_t* cy, int64
   }
   int32_t* d = nullptr;
   CK(cudaMalloc(&d, (size_t)n * 12 + 16));
-  launch_cell_indices(h->st, h->sp[isp], h->d_cnt + isp, h->g.x_grid_min, h->rc, d, d + n, d + 2 * n,
-                      h->nblocks);
+  if (h->prec == CYL_PREC_MIXED)
+    mixed_cell_indices(h->st, h->sp[isp], h->d_cnt + isp, h->xg0, h->g.x_grid_min, h->rc, d, d + n, d + 2 * n,
+                       h->nblocks);
+  else
+    launch_cell_indices(h->st, h->sp[isp], h->d_cnt + isp, h->g.x_grid_min, h->rc, d, d + n, d + 2 * n,
+                        h->nblocks);
   std::vector<int32_t> b((size_t)n * 3);
   cudaError_t e = cudaMemcpyAsync(b.data(), d, (size_t)n * 12, cudaMemcpyDeviceToHost, h->st);
   cudaStreamSynchronize(h->st);

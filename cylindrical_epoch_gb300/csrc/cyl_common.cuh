@@ -94,6 +94,8 @@ struct StepRec {
   int64_t inject_off[MAX_SPECIES];  // offsets into the injection batch
   int64_t inject_cnt[MAX_SPECIES];
   int64_t src_off;           // offset of this step's laser source vectors
+  int32_t nshift_total;      // window shifts before this step (mixed-form cell origin)
+  int32_t nshift_total_after;
 };
 
 // Run-constant geometry and physics parameters (pushed by value).
@@ -106,12 +108,18 @@ struct RunConst {
 };
 
 struct SpeciesPtrs {
+  // FP64 form: Cartesian position (m), momentum (kg m/s), weight
   double *x, *y, *z, *px, *py, *pz, *w;
   int64_t* id;
   int64_t cap;
   double charge, mass;
   int immobile;
   int bc[4];
+  // mixed form, in the same allocation: absolute axial cell index and FP32
+  // offset in [0,1) (x = x_grid_min0 + (kx + fx) dx), y and z in units of
+  // dy, normalised momentum u = p/(m c), weight
+  int32_t* kx;
+  float *fx, *fy, *fz, *ux, *uy, *uz, *fw;
 };
 
 // Device error word bits.

@@ -335,6 +335,14 @@ __global__ void k_scan_add(int* data, int n, const int* block_sums) {
     if (base + k < n) data[base + k] += add;
 }
 
+void scan_exclusive(cudaStream_t s, int32_t* data, int n, int32_t* block_sums) {
+  const int per = SCAN_BLOCK * SCAN_ITEMS;
+  const int nb = (n + per - 1) / per;
+  k_scan_local<<<nb, SCAN_BLOCK, 0, s>>>(data, n, block_sums);
+  k_scan_sums<<<1, SCAN_BLOCK, 0, s>>>(block_sums, nb);
+  k_scan_add<<<nb, SCAN_BLOCK, 0, s>>>(data, n, block_sums);
+}
+
 __global__ void k_sort_copy_out(SpeciesPtrs sp, const SpeciesCounters* cnt, double* tmp,
                                 int64_t* tmp_id, int64_t cap) {
   const int64_t n = cnt->n_used;

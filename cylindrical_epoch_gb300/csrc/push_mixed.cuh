@@ -1,0 +1,59 @@
+// push_mixed.cuh -- mixed-precision form: tile table, push parameters and
+// the particle kernels that know the mixed particle layout.
+#pragma once
+
+#include "cyl_common.cuh"
+#include "cyl_kernels.cuh"
+
+namespace cyl {
+
+constexpr int TILE_X = 16;  // cells per tile along x
+constexpr int TILE_Y = 8;   // cells per tile along r
+
+// Particles sorted by tile: tile t owns slots [start[t], start[t+1]);
+// slots [n_sorted, n_used) were appended after the sort.
+struct TileTable {
+  int next;       // persistent-kernel work counter
+  int ntiles;
+  int ntx, nty;
+  int tx_min;     // absolute tile column of tile 0
+  int pad;
+  int64_t n_sorted;
+  int64_t* start;  // ntiles + 1
+};
+
+struct MixedParams {
+  float cdt2_dx, cdt2_dy;   // c dt / 2 in cells along x and r
+  float cmratio, ccmratio;  // q dt fac / (2 m c) and c times it
+  float q_fac, idt, c;
+  // particle boundaries in cell units of the step's grid (set per launch)
+  float x_lo, x_hi, x_sys_lo, x_sys_hi, x_out_lo, x_out_hi;
+  float r_hi, r_sys, r_out;
+  int* err;
+};
+
+MixedParams mixed_params(const SpeciesPtrs& sp, const RunConst& rc);
+size_t push_mixed_smem(int M);
+int push_mixed_blocks_per_sm(int M);
+
+void launch_push_mixed(cudaStream_t s, const FieldSet& F, const GeomTables& g, const SpeciesPtrs& sp,
+                       SpeciesCounters* cnt, const StepRec* rec, const RunConst& rc, int apply_bcs,
+                       int* err, int nblocks, const MixedParams& P, TileTable* tt);
+
+// mixed_particles.cu
+void mixed_from_double(cudaStream_t s, const SpeciesPtrs& sp, const double* stage, int64_t n, int64_t cap,
+                       double xg0, const RunConst& rc);
+void mixed_to_double(cudaStream_t s, const SpeciesPtrs& sp, double* stage, int64_t n, int64_t cap,
+                     double xg0, const RunConst& rc);
+void mixed_window_particles(cudaStream_t s, const SpeciesPtrs& sp, SpeciesCounters* cnt, const double* inject,
+                            const StepRec* rec, int isp, double xg0, const RunConst& rc, int* err, int nblocks);
+void mixed_particle_bcs(cudaStream_t s, const SpeciesPtrs& sp, SpeciesCounters* cnt, const StepRec* rec,
+                        const RunConst& rc, int nblocks);
+void mixed_energy(cudaStream_t s, const SpeciesPtrs& sp, const SpeciesCounters* cnt, double* out, int nblocks);
+void mixed_sort(cudaStream_t s, const SpeciesPtrs& sp, SpeciesCounters* cnt, SortScratch& sc, TileTable* tt,
+                int64_t* tile_start, const StepRec* rec, const RunConst& rc, int nblocks);
+void mixed_cell_indices(cudaStream_t s, const SpeciesPtrs& sp, const SpeciesCounters* cnt, double xg0,
+                        double x_grid_min, const RunConst& rc, int32_t* cx, int32_t* cy, int32_t* live,
+                        int nblocks);
+
+}  // namespace cyl

@@ -1,0 +1,73 @@
+"""Mixed-precision form (int cell + FP32 offset, FP32 push/deposit into FP64
+currents) against the FP64 form and the oracle.
+
+Error bar (the benchmark spec): per-mode Ez (exm) relative L2 <= 1e-3 against the
+FP64 result on the same deck; the other stated results (wake amplitude,
+electron energy moments, particle count) are compared with the same
+tolerance here.
+"""
+import numpy as np
+import pytest
+
+import cylindrical_epoch_gb300 as cg
+from cylindrical_epoch_gb300 import abi
+from tests.helpers import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL_EZ = 1.0e-3
+
+
+def _wake(prec, nx=256, ny=64, ppc=4):
+    deck = cg.wakefield(nx=nx, ny=ny, ppc=ppc, density=3.0e24, ramp=4.0e-6, precision=prec)
+    deck.window_start_time = 60 * 5.0e-17
+    return deck
+
+
+def test_mixed_roundtrip_conversion(gpu_lib):
+    deck = _wake(abi.PREC_MIXED)
+    parts, rng = cg.host_load(deck)
+    run = cg.Run(deck, particles=parts, rng=rng, initialise=False)
+    p = run.particles(0).sorted_by_id()
+    q = parts[0].sorted_by_id()
+    assert np.array_equal(p.id, q.id)
+    assert np.max(np.abs(p.x - q.x)) < 1e-6 * deck.dx
+    assert np.max(np.abs(p.y - q.y)) < 1e-6 * deck.y_max
+    assert rel_l2(p.w, q.w) < 1e-7
+
+
+def test_mixed_vs_fp64_wakefield(gpu_lib):
+    d64 = _wake(abi.PREC_FP64)
+    d32 = _wake(abi.PREC_MIXED)
+    parts, rng = cg.host_load(d64)
+    a = cg.Run(d64, particles=parts, rng=rng)
+    b = cg.Run(d32, particles=parts, rng=rng)
+    for k in (16, 16, 32, 32):
+        a.step(k)
+        b.step(k)
+    sa, sb = a.state(), b.state()
+    assert sa.n_shifts == sb.n_shifts and sa.n_shifts > 0
+    assert abs(sa.n_live[0] - sb.n_live[0]) <= max(2, 1e-4 * sa.n_live[0])
+    ea, eb = a.field("exm"), b.field("exm")
+    for m in range(d64.n_mode):
+        e = rel_l2(eb[m], ea[m])
+        assert e < TOL_EZ, (m, e)
+    da, db = a.diagnostics(), b.diagnostics()
+    assert abs(db.kinetic_energy - da.kinetic_energy) <= TOL_EZ * da.kinetic_energy
+    assert db.device_error == 0
+
+
+def test_mixed_thermal_energy(gpu_lib):
+    d64 = cg.thermal_plasma(nx=64, ny=32, ppc=8)
+    d32 = cg.thermal_plasma(nx=64, ny=32, ppc=8, precision=abi.PREC_MIXED)
+    parts, rng = cg.host_load(d64)
+    a = cg.Run(d64, particles=parts, rng=rng)
+    b = cg.Run(d32, particles=parts, rng=rng)
+    a.step(40)
+    b.step(40)
+    da, db = a.diagnostics(), b.diagnostics()
+    assert da.n_live == db.n_live
+    assert abs(db.kinetic_energy - da.kinetic_energy) < 1e-3 * da.kinetic_energy
+    for n in ("exm", "erm"):
+        x, y = a.field(n), b.field(n)
+        assert rel_l2(y[0], x[0]) < 5e-3, n
