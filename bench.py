@@ -183,6 +183,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--eager", action="store_true", help="no CUDA graphs")
+    ap.add_argument("--fp64-steps", type=int, default=200,
+                    help="steps of the plain FP64 form timed beside the mixed form (0: skip)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -267,6 +269,23 @@ def main():
                 "peak_kind": peak_kind, "kernel": f"k_push_{form}",
                 "kernel_ms": push_ms, "algorithmic_bytes_per_particle_step": per_particle}
 
+    fp64 = None
+    if form == "mixed" and args.fp64_steps > 0:
+        d64 = build_deck(args.deck, "fp64")
+        r64 = cg.Run(d64, particles=parts, rng=rng)
+        r64.step(args.warmup, graph=False)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r64.step(args.fp64_steps, graph=graph)
+        torch.cuda.synchronize()
+        dt64 = time.perf_counter() - t0
+        s64 = r64.state()
+        n64 = sum(s64.n_live[i] for i in range(len(d64.species)))
+        fp64 = {"value": n64 * args.fp64_steps / dt64, "steps": args.fp64_steps,
+                "ms_per_step": 1e3 * dt64 / args.fp64_steps,
+                "note": "plain FP64 form, steps [W, W+K64) of the same deck"}
+        r64.close()
+
     e2e = None
     if not args.no_e2e:
         e2e = e2e_run(deck, parts, rng, args.steps, graph)
@@ -296,6 +315,9 @@ def main():
                            "d2h_bytes_per_step": e2e["d2h"] / args.steps}
         if base:
             line["cpu_baseline"] = base
+        if fp64:
+            line["fp64_form"] = fp64
+            line["mixed_over_fp64"] = value / fp64["value"]
         print(json.dumps(line))
     run.close()
     if dist:

@@ -28,6 +28,7 @@ SOURCES = [
     ("push_fp64.cu", ["--fmad=false"]),
     ("particles.cu", ["--fmad=false"]),
     ("push_mixed.cu", ["--fmad=true"]),
+    ("fields_fp32.cu", ["--fmad=true"]),
     ("mixed_particles.cu", ["--fmad=true"]),
     ("host_deck.cpp", []),
 ]

@@ -49,6 +49,11 @@ struct Handle {
   size_t fcount = 0;  // complex elements per mode array
   cplx* fbuf = nullptr;
   cplx* F[16] = {};   // 15 arrays + smoothing work array
+  cplxf* ffbuf = nullptr;  // mixed form: E, B, B_old in FP32
+  cplxf* Ff[9] = {};
+  float4* rowtab = nullptr;   // per-row FP32 Yee coefficients of the mixed form
+  float* gtab_f = nullptr;    // FP32 geometric factors of the mixed deposit
+  int* fb_buf = nullptr;      // mixed form: deferred-particle lists + counters
   int jpar = 0;       // 0: J in slots 6..8, J_old in 12..14; 1: swapped
   cplx* cols = nullptr;
   double* geom_buf = nullptr;
@@ -122,6 +127,9 @@ static int map_particle_bc(int b) {
   return b;
 }
 
+template <typename T>
+static FieldSetT<T> fieldset_t(const Handle* h, int jpar);
+
 static FieldSet fieldset(const Handle* h, int jpar) {
   auto v = [&](int k) { return FView{h->F[k], h->rc.nxg, h->rc.nyg}; };
   FieldSet F;
@@ -133,6 +141,25 @@ static FieldSet fieldset(const Handle* h, int jpar) {
   F.jxo = v(jo); F.jro = v(jo + 1); F.jto = v(jo + 2);
   return F;
 }
+
+// Mixed form: E, B and B_old live in the FP32 buffer, J and J_old in the
+// FP64 one (same parity rule).
+static FieldSetF fieldset_f(const Handle* h, int jpar) {
+  auto v = [&](int k) { return FViewF{h->Ff[k], h->rc.nxg, h->rc.nyg}; };
+  auto d = [&](int k) { return FView{h->F[k], h->rc.nxg, h->rc.nyg}; };
+  FieldSetF F;
+  F.ex = v(0); F.er = v(1); F.et = v(2);
+  F.bx = v(3); F.br = v(4); F.bt = v(5);
+  F.bxo = v(6); F.bro = v(7); F.bto = v(8);
+  const int j0 = jpar ? 12 : 6, jo = jpar ? 6 : 12;
+  F.jx = d(j0); F.jr = d(j0 + 1); F.jt = d(j0 + 2);
+  F.jxo = d(jo); F.jro = d(jo + 1); F.jto = d(jo + 2);
+  return F;
+}
+template <>
+FieldSet fieldset_t<cplx>(const Handle* h, int jpar) { return fieldset(h, jpar); }
+template <>
+FieldSetF fieldset_t<cplxf>(const Handle* h, int jpar) { return fieldset_f(h, jpar); }
 
 // Slot of a public field index under the current J parity.
 static int field_slot(const Handle* h, int which) {
@@ -259,54 +286,70 @@ static void prepare_step(Handle* h, int k, int64_t& inj_used) {
 
 static void count_launch(Handle* h, int n) { h->kernel_launches += n; }
 
-static void push_species(Handle* h, cudaStream_t s, const FieldSet& F, int i, const StepRec* rec,
-                         int apply_bcs) {
-  if (h->prec == CYL_PREC_MIXED) {
-    launch_push_mixed(s, F, h->geom, h->sp[i], h->d_cnt + i, rec, h->rc, apply_bcs, h->d_err,
-                      h->nblocks_mixed, h->mp[i], h->d_tiles + i);
-    return;
+
+// Enqueue the kernels of one step; rec/src point at this step's records.
+// Bulk Yee updates: exact FP64 kernels for the plain form, FP32 for the mixed form.
+static void bulk_e(Handle* h, cudaStream_t s, const FieldSet& F) { launch_update_e(s, F, h->rc); }
+static void bulk_e(Handle* h, cudaStream_t s, const FieldSetF& F) {
+  launch_update_e_f32(s, F, (const double*)h->rowtab, h->rc);
+}
+static void bulk_b(Handle* h, cudaStream_t s, const FieldSet& F, int save_old) {
+  launch_update_b(s, F, save_old, h->rc);
+}
+static void bulk_b(Handle* h, cudaStream_t s, const FieldSetF& F, int save_old) {
+  launch_update_b_f32(s, F, save_old, (const double*)h->rowtab, h->rc);
+}
+static void push_all(Handle* h, cudaStream_t s, const FieldSet& F, const StepRec* rec, int apply_bcs) {
+  for (int i = 0; i < h->nsp; ++i) {
+    if (h->sp[i].immobile) continue;
+    launch_push_fp64(s, F, h->geom, h->sp[i], h->d_cnt + i, rec, h->rc, apply_bcs, h->d_err, h->nblocks);
+    count_launch(h, 1);
   }
-  launch_push_fp64(s, F, h->geom, h->sp[i], h->d_cnt + i, rec, h->rc, apply_bcs, h->d_err, h->nblocks);
+}
+static void push_all(Handle* h, cudaStream_t s, const FieldSetF& F, const StepRec* rec, int apply_bcs) {
+  for (int i = 0; i < h->nsp; ++i) {
+    if (h->sp[i].immobile) continue;
+    launch_push_mixed(s, F, h->sp[i], h->d_cnt + i, rec, h->rc, apply_bcs, h->nblocks_mixed, h->nblocks,
+                      h->mp[i], h->d_tiles + i);
+    count_launch(h, 2);
+  }
 }
 
 // Enqueue the kernels of one step; rec/src point at this step's records.
-static void enqueue_step(Handle* h, const StepRec* rec, const double* src, int k_in_chunk,
-                         bool timing, bool capturing) {
+template <typename T>
+static void enqueue_step_t(Handle* h, const StepRec* rec, const double* src, int k_in_chunk, bool timing,
+                           bool capturing) {
   const unsigned evflag = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
   cudaStream_t s = h->st;
   const RunConst& rc = h->rc;
-  FieldSet F = fieldset(h, h->jpar);
+  FieldSetT<T> F = fieldset_t<T>(h, h->jpar);
   // update_eb_fields_half (fields.f90:316-337)
-  launch_update_e(s, F, rc);
+  bulk_e(h, s, F);
   launch_e_axis_bcs(s, F, rec, rc);
-  launch_update_b(s, F, 1, rc);
+  bulk_b(h, s, F, 1);
   launch_b_axis_bcs(s, F, rec, rc);
-  count_launch(h, 4);
+  count_launch(h, 6);
   // push_particles: J_old = J, J = 0 (particles.F90:163-169) by buffer swap
   h->jpar ^= 1;
-  F = fieldset(h, h->jpar);
+  F = fieldset_t<T>(h, h->jpar);
   const size_t bytes = h->fcount * sizeof(cplx);
   cudaMemsetAsync(F.jx.p, 0, bytes, s);
   cudaMemsetAsync(F.jr.p, 0, bytes, s);
   cudaMemsetAsync(F.jt.p, 0, bytes, s);
   if (timing) cudaEventRecordWithFlags(h->ev_push[k_in_chunk][0], s, evflag);
-  for (int i = 0; i < h->nsp; ++i) {
-    if (h->sp[i].immobile) continue;
-    push_species(h, s, F, i, rec, 1);
-    count_launch(h, 1);
-  }
+  push_all(h, s, F, rec, 1);
   if (timing) cudaEventRecordWithFlags(h->ev_push[k_in_chunk][1], s, evflag);
   // current_bcs_r_min_final + current_finish
   FView wk{h->F[15], rc.nxg, rc.nyg};
   launch_current_finish(s, F, rec, rc, h->gd.smooth_currents, h->gd.smooth_its, h->gd.smooth_comp_its,
                         h->gd.smooth_stride > 0 ? h->gd.smooth_stride : 1, wk);
-  count_launch(h, 1);
+  count_launch(h, 2);
   // update_eb_fields_final (fields.f90:341-353)
-  launch_update_b(s, F, 0, rc);
+  bulk_b(h, s, F, 0);
   launch_b_final_bcs(s, F, rec, src, h->cols, 1, rc.dt, rc);
-  launch_update_e(s, F, rc);
+  bulk_e(h, s, F);
   launch_e_axis_bcs(s, F, rec, rc);
-  count_launch(h, 4);
+  count_launch(h, 6);
   // moving_window
   if (h->move_window) {
     for (int i = 0; i < h->nsp; ++i) {
@@ -320,6 +363,12 @@ static void enqueue_step(Handle* h, const StepRec* rec, const double* src, int k
     launch_shift_fields(s, F, h->cols, rec, 1, rc);
     count_launch(h, 2);
   }
+}
+
+static void enqueue_step(Handle* h, const StepRec* rec, const double* src, int k_in_chunk, bool timing,
+                         bool capturing) {
+  if (h->prec == CYL_PREC_MIXED) enqueue_step_t<cplxf>(h, rec, src, k_in_chunk, timing, capturing);
+  else enqueue_step_t<cplx>(h, rec, src, k_in_chunk, timing, capturing);
 }
 
 // Counting sort of every species by cell; xgm points at the device copy of
@@ -556,6 +605,8 @@ int cyl_create(const cyl_grid_desc* gd, const cyl_species_desc* spd, int32_t nsp
   int nsm = 152;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device);
   h->nblocks = nsm * 8;
+  cudaMalloc(&h->d_err, sizeof(int));
+  cudaMemset(h->d_err, 0, sizeof(int));
   // fields: 15 arrays + one work array, one allocation
   h->fcount = (size_t)rc.nxg * rc.nyg * rc.M;
   if (cudaMalloc(&h->fbuf, h->fcount * 16 * sizeof(cplx)) != cudaSuccess) {
@@ -578,6 +629,29 @@ int cyl_create(const cyl_grid_desc* gd, const cyl_species_desc* spd, int32_t nsp
     h->geom.inv_volume = h->geom_buf + n1 + n0;
     h->geom.ratio_area_xt = h->geom_buf + 2 * n1 + n0;
   }
+  if (h->prec == CYL_PREC_MIXED) {
+    // FP32 E, B, B_old
+    if (cudaMalloc(&h->ffbuf, h->fcount * 9 * sizeof(cplxf)) != cudaSuccess) {
+      cyl_destroy((cyl_handle)hs);
+      return CYL_ERR_OUT_OF_MEMORY;
+    }
+    cudaMemset(h->ffbuf, 0, h->fcount * 9 * sizeof(cplxf));
+    for (int k = 0; k < 9; ++k) h->Ff[k] = h->ffbuf + h->fcount * k;
+    // per-row Yee coefficients: c^2/r_p dt/2, c^2/r_d dt/2, dt/2/r_d, dt/2/r_p
+    std::vector<float4> rt(rc.ny + 2);
+    for (int ir = 0; ir <= rc.ny + 1; ++ir) {
+      const double r_d = std::fabs((double)(ir - 1) * rc.dy + rc.y_grid_min);
+      const double r_p = r_d + 0.5 * rc.dy;
+      const double hh2 = 0.5 * rc.dt, c2 = CLIGHT * CLIGHT;
+      rt[ir] = make_float4((float)(c2 / r_p * hh2), (float)(c2 / r_d * hh2), (float)(hh2 / r_d), (float)(hh2 / r_p));
+    }
+    cudaMalloc(&h->rowtab, rt.size() * sizeof(float4));
+    cudaMemcpy(h->rowtab, rt.data(), rt.size() * sizeof(float4), cudaMemcpyHostToDevice);
+    std::vector<float> gf(geo.size());
+    for (size_t k = 0; k < geo.size(); ++k) gf[k] = (float)geo[k];
+    cudaMalloc(&h->gtab_f, gf.size() * sizeof(float));
+    cudaMemcpy(h->gtab_f, gf.data(), gf.size() * sizeof(float), cudaMemcpyHostToDevice);
+  }
   int64_t maxcap = 1;
   for (int i = 0; i < nsp; ++i) {
     if (alloc_species(h, i, spd[i]) != CYL_OK) {
@@ -592,7 +666,26 @@ int cyl_create(const cyl_grid_desc* gd, const cyl_species_desc* spd, int32_t nsp
   cudaMemset(h->d_tiles, 0, sizeof(TileTable) * MAX_SPECIES);
   cudaMalloc(&h->d_tile_start, sizeof(int64_t) * (h->ntiles_max + 1) * MAX_SPECIES);
   cudaMemset(h->d_tile_start, 0, sizeof(int64_t) * (h->ntiles_max + 1) * MAX_SPECIES);
-  for (int i = 0; i < nsp; ++i) h->mp[i] = mixed_params(h->sp[i], rc);
+  if (h->prec == CYL_PREC_MIXED) {
+    int64_t fbtot = 0;
+    for (int i = 0; i < nsp; ++i) fbtot += h->sp[i].cap + 1;
+    if (cudaMalloc(&h->fb_buf, sizeof(int) * (size_t)fbtot) != cudaSuccess) {
+      cyl_destroy((cyl_handle)hs);
+      return CYL_ERR_OUT_OF_MEMORY;
+    }
+    int64_t off = 0;
+    const int n1 = rc.ny + 2 * JNG, n0 = n1 + 1;
+    for (int i = 0; i < nsp; ++i) {
+      h->mp[i] = mixed_params(h->sp[i], rc);
+      h->mp[i].err = h->d_err;
+      h->mp[i].g_rt = h->gtab_f;
+      h->mp[i].g_xt = h->gtab_f + n1;
+      h->mp[i].g_vol = h->gtab_f + n1 + n0;
+      h->mp[i].fb_count = h->fb_buf + off;
+      h->mp[i].fb_list = h->fb_buf + off + 1;
+      off += h->sp[i].cap + 1;
+    }
+  }
   h->nblocks_mixed = nsm * push_mixed_blocks_per_sm(rc.M);
   cudaMalloc(&h->d_cnt, sizeof(SpeciesCounters) * MAX_SPECIES);
   cudaMemset(h->d_cnt, 0, sizeof(SpeciesCounters) * MAX_SPECIES);
@@ -617,8 +710,6 @@ int cyl_create(const cyl_grid_desc* gd, const cyl_species_desc* spd, int32_t nsp
     p += (size_t)maxcap * 4;
     h->sc.hist = (int32_t*)p;
   }
-  cudaMalloc(&h->d_err, sizeof(int));
-  cudaMemset(h->d_err, 0, sizeof(int));
   cudaMalloc(&h->d_red, 8 * sizeof(double));
   // staging for CHUNK steps
   h->src_per_step = (size_t)4 * (rc.ny + 1);
@@ -658,6 +749,10 @@ int cyl_destroy(cyl_handle hh) {
   cudaFree(h->geom_buf);
   cudaFree(h->d_cnt);
   cudaFree(h->d_tiles);
+  cudaFree(h->ffbuf);
+  cudaFree(h->rowtab);
+  cudaFree(h->gtab_f);
+  cudaFree(h->fb_buf);
   cudaFree(h->d_tile_start);
   cudaFree(h->sort_buf);
   cudaFree(h->d_err);
@@ -765,9 +860,24 @@ int cyl_download_particles(cyl_handle hh, int32_t isp, double* x, double* y, dou
   return CYL_OK;
 }
 
+// Mixed form: slot of an E / B / B_old array in the FP32 buffer, else -1.
+static int f32_slot(const Handle* h, int which) {
+  if (h->prec != CYL_PREC_MIXED) return -1;
+  if (which >= 0 && which <= 5) return which;
+  if (which >= 9 && which <= 11) return which - 3;
+  return -1;
+}
+
 int cyl_upload_field(cyl_handle hh, int32_t which, const double* data) {
   if (!hh || !data || which < 0 || which >= CYL_NFIELDS) return CYL_ERR_BAD_ARG;
   Handle* h = &hh->h;
+  const int fs = f32_slot(h, which);
+  if (fs >= 0) {
+    std::vector<float> tmp(h->fcount * 2);
+    for (size_t i = 0; i < tmp.size(); ++i) tmp[i] = (float)data[i];
+    CK(cudaMemcpy(h->Ff[fs], tmp.data(), tmp.size() * sizeof(float), cudaMemcpyHostToDevice));
+    return CYL_OK;
+  }
   CK(cudaMemcpyAsync(h->F[field_slot(h, which)], data, h->fcount * sizeof(cplx), cudaMemcpyHostToDevice,
                      h->st));
   CK(cudaStreamSynchronize(h->st));
@@ -778,6 +888,13 @@ int cyl_download_field(cyl_handle hh, int32_t which, double* data) {
   if (!hh || !data || which < 0 || which >= CYL_NFIELDS) return CYL_ERR_BAD_ARG;
   Handle* h = &hh->h;
   CK(cudaStreamSynchronize(h->st));
+  const int fs = f32_slot(h, which);
+  if (fs >= 0) {
+    std::vector<float> tmp(h->fcount * 2);
+    CK(cudaMemcpy(tmp.data(), h->Ff[fs], tmp.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < tmp.size(); ++i) data[i] = (double)tmp[i];
+    return CYL_OK;
+  }
   CK(cudaMemcpy(data, h->F[field_slot(h, which)], h->fcount * sizeof(cplx), cudaMemcpyDeviceToHost));
   return CYL_OK;
 }
@@ -809,10 +926,16 @@ int cyl_initialise(cyl_handle hh) {
     else
       launch_particle_bcs(h->st, h->sp[i], h->d_cnt + i, h->d_rec, 0, h->rc, h->nblocks);
   }
-  FieldSet F = fieldset(h, h->jpar);
-  launch_efield_bcs(h->st, F, h->d_rec, h->rc);
-  launch_b_final_bcs(h->st, F, h->d_rec, h->d_src, h->cols, 0, dt_half, h->rc);
-  if (h->prec == CYL_PREC_MIXED) enqueue_sort(h, h->d_rec);
+  if (h->prec == CYL_PREC_MIXED) {
+    FieldSetF F = fieldset_f(h, h->jpar);
+    launch_efield_bcs(h->st, F, h->d_rec, h->rc);
+    launch_b_final_bcs(h->st, F, h->d_rec, h->d_src, h->cols, 0, dt_half, h->rc);
+    enqueue_sort(h, h->d_rec);
+  } else {
+    FieldSet F = fieldset(h, h->jpar);
+    launch_efield_bcs(h->st, F, h->d_rec, h->rc);
+    launch_b_final_bcs(h->st, F, h->d_rec, h->d_src, h->cols, 0, dt_half, h->rc);
+  }
   CK(cudaEventRecord(h->ev_copy, h->st));
   h->copy_pending = true;
   return sync_and_check(h);
@@ -850,10 +973,8 @@ int cyl_push_only(cyl_handle hh) {
   cudaMemsetAsync(F.jr.p, 0, bytes, h->st);
   cudaMemsetAsync(F.jt.p, 0, bytes, h->st);
   CK(cudaEventRecord(h->ev_push[0][0], h->st));
-  for (int i = 0; i < h->nsp; ++i) {
-    if (h->sp[i].immobile) continue;
-    push_species(h, h->st, F, i, h->d_rec, 0);
-  }
+  if (h->prec == CYL_PREC_MIXED) push_all(h, h->st, fieldset_f(h, h->jpar), h->d_rec, 0);
+  else push_all(h, h->st, F, h->d_rec, 0);
   CK(cudaEventRecord(h->ev_push[0][1], h->st));
   CK(cudaEventSynchronize(h->ev_push[0][1]));
   collect_push_timing(h, 1);
@@ -900,7 +1021,8 @@ int cyl_diagnostics(cyl_handle hh, cyl_diag* out) {
     if (h->prec == CYL_PREC_MIXED) mixed_energy(h->st, h->sp[i], h->d_cnt + i, h->d_red, h->nblocks);
     else launch_energy(h->st, h->sp[i], h->d_cnt + i, h->d_red, h->nblocks);
   }
-  launch_field_energy(h->st, fieldset(h, h->jpar), h->rc, h->d_red + 2);
+  if (h->prec == CYL_PREC_MIXED) launch_field_energy(h->st, fieldset_f(h, h->jpar), h->rc, h->d_red + 2);
+  else launch_field_energy(h->st, fieldset(h, h->jpar), h->rc, h->d_red + 2);
   double red[8];
   CK(cudaMemcpyAsync(red, h->d_red, sizeof(red), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));

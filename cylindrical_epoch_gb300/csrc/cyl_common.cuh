@@ -60,15 +60,47 @@ CYL_HD cplx crecip(cplx z) {
 }
 constexpr cplx IMAGI = {0.0, 1.0};
 
-// Layout of one complex mode array in HBM: Fortran order with ghosts,
-// F(1-ng:nx+ng, 1-ng:ny+ng, 0:M-1), element (re, im) as 16 bytes.
-struct FView {
-  cplx* p;
-  int nxg, nyg;
-  CYL_HD cplx& operator()(int ix, int iy, int m) const {
-    return p[(int64_t)(ix + NG - 1) + (int64_t)nxg * ((int64_t)(iy + NG - 1) + (int64_t)nyg * m)];
+// FP32 complex, the storage of E and B in the mixed-precision form.
+struct cplxf {
+  float re, im;
+};
+CYL_HD cplx to_c(const cplx& v) { return v; }
+CYL_HD cplx to_c(const cplxf& v) { return {(double)v.re, (double)v.im}; }
+CYL_HD void from_c(cplx& d, const cplx& v) { d = v; }
+CYL_HD void from_c(cplxf& d, const cplx& v) {
+  d.re = (float)v.re;
+  d.im = (float)v.im;
+}
+
+// Reference to one element of a mode array: reads convert to FP64 complex,
+// writes convert back to the storage type (exact for FP64 storage).
+template <typename T>
+struct FRef {
+  T* q;
+  CYL_HD operator cplx() const { return to_c(*q); }
+  CYL_HD FRef& operator=(const cplx& v) {
+    from_c(*q, v);
+    return *this;
+  }
+  CYL_HD FRef& operator=(const FRef& o) {
+    from_c(*q, to_c(*o.q));
+    return *this;
   }
 };
+
+// Layout of one complex mode array in HBM: Fortran order with ghosts,
+// F(1-ng:nx+ng, 1-ng:ny+ng, 0:M-1), x fastest.
+template <typename T>
+struct FViewT {
+  T* p;
+  int nxg, nyg;
+  CYL_HD T* ptr(int ix, int iy, int m) const {
+    return p + ((int64_t)(ix + NG - 1) + (int64_t)nxg * ((int64_t)(iy + NG - 1) + (int64_t)nyg * m));
+  }
+  CYL_HD FRef<T> operator()(int ix, int iy, int m) const { return FRef<T>{ptr(ix, iy, m)}; }
+};
+using FView = FViewT<cplx>;
+using FViewF = FViewT<cplxf>;
 
 // Stagger table (setup.F90:126-136 with constants.F90:291-296).
 // which: 0 exm, 1 erm, 2 etm, 3 bxm, 4 brm, 5 btm

@@ -5,9 +5,18 @@
 
 namespace cyl {
 
-struct FieldSet {
-  FView ex, er, et, bx, br, bt, jx, jr, jt, bxo, bro, bto, jxo, jro, jto;
+// The mode arrays of one step: E, B and B_old in the form's storage type T
+// (FP64 for the plain form, FP32 for the mixed form); J and J_old are FP64
+// in both forms.
+template <typename T>
+struct FieldSetT {
+  FViewT<T> ex, er, et, bx, br, bt;
+  FView jx, jr, jt;
+  FViewT<T> bxo, bro, bto;
+  FView jxo, jro, jto;
 };
+using FieldSet = FieldSetT<cplx>;
+using FieldSetF = FieldSetT<cplxf>;
 
 // Geometry tables of push_particles (particles.F90:189-217), run constant.
 struct GeomTables {
@@ -23,18 +32,29 @@ struct SpeciesCounters {
   int64_t n_dead;  // removed particles still occupying a slot
 };
 
-// fields.cu
+// fields.cu (E/B boundary and axis kernels for either storage type)
 void launch_update_e(cudaStream_t s, const FieldSet& F, const RunConst& rc);
 void launch_update_b(cudaStream_t s, const FieldSet& F, int save_old, const RunConst& rc);
-void launch_e_axis_bcs(cudaStream_t s, const FieldSet& F, const StepRec* rec, const RunConst& rc);
-void launch_efield_bcs(cudaStream_t s, const FieldSet& F, const StepRec* rec, const RunConst& rc);
-void launch_b_axis_bcs(cudaStream_t s, const FieldSet& F, const StepRec* rec, const RunConst& rc);
-void launch_b_final_bcs(cudaStream_t s, const FieldSet& F, const StepRec* rec, const double* src,
+template <typename T>
+void launch_e_axis_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc);
+template <typename T>
+void launch_efield_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc);
+template <typename T>
+void launch_b_axis_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc);
+template <typename T>
+void launch_b_final_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const double* src,
                         const cplx* cols, int do_axis, double dt, const RunConst& rc);
-void launch_current_finish(cudaStream_t s, const FieldSet& F, const StepRec* rec, const RunConst& rc,
+template <typename T>
+void launch_current_finish(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc,
                            int smooth, int its, int comp_its, int stride, FView wk);
-void launch_shift_fields(cudaStream_t s, const FieldSet& F, const cplx* cols, const StepRec* rec,
+template <typename T>
+void launch_shift_fields(cudaStream_t s, const FieldSetT<T>& F, const cplx* cols, const StepRec* rec,
                          int which, const RunConst& rc);
+
+// fields_fp32.cu (bulk Yee updates of the mixed form, FP32 storage)
+void launch_update_e_f32(cudaStream_t s, const FieldSetF& F, const double* rowtab, const RunConst& rc);
+void launch_update_b_f32(cudaStream_t s, const FieldSetF& F, int save_old, const double* rowtab,
+                         const RunConst& rc);
 
 // push_fp64.cu
 void launch_push_fp64(cudaStream_t s, const FieldSet& F, const GeomTables& g, const SpeciesPtrs& sp,
@@ -52,7 +72,8 @@ void launch_cell_indices(cudaStream_t s, const SpeciesPtrs& sp, const SpeciesCou
                          int32_t* live, int nblocks);
 void launch_energy(cudaStream_t s, const SpeciesPtrs& sp, const SpeciesCounters* cnt, double* out,
                    int nblocks);
-void launch_field_energy(cudaStream_t s, const FieldSet& F, const RunConst& rc, double* out);
+template <typename T>
+void launch_field_energy(cudaStream_t s, const FieldSetT<T>& F, const RunConst& rc, double* out);
 // Counting sort of one species by cell; scratch holds the keys, histogram and
 // a second copy of the particle arrays.  Removes dead slots.
 struct SortScratch {

@@ -77,7 +77,8 @@ constexpr int CTA_THREADS = 512;
 #define CTA_FOR(var, n) for (int var = threadIdx.x; var < (n); var += blockDim.x)
 
 // halo_x: periodic-x self wrap of rows [j0, j1] (boundary.F90:500-593 on one rank)
-__device__ void halo_x(FView f, int j0, int j1, const int* bcf, const RunConst& rc) {
+template <typename T>
+__device__ void halo_x(FViewT<T> f, int j0, int j1, const int* bcf, const RunConst& rc) {
   const int nrow = j1 - j0 + 1;
   if (bcf[CYL_BD_X_MAX] == CYL_BC_PERIODIC) {
     CTA_FOR(t, nrow * rc.M * NG) {
@@ -98,7 +99,8 @@ __device__ void halo_x(FView f, int j0, int j1, const int* bcf, const RunConst& 
 }
 
 // field_mode_zero_gradient (boundary.F90:654-707) on one boundary
-__device__ void zero_gradient(FView f, int st, int bd, const int* bcf, const RunConst& rc) {
+template <typename T>
+__device__ void zero_gradient(FViewT<T> f, int st, int bd, const int* bcf, const RunConst& rc) {
   if (bcf[bd] == CYL_BC_PERIODIC) return;
   const int nx = rc.nx, ny = rc.ny, M = rc.M;
   if (bd == CYL_BD_X_MIN || bd == CYL_BD_X_MAX) {
@@ -124,7 +126,8 @@ __device__ void zero_gradient(FView f, int st, int bd, const int* bcf, const Run
 }
 
 // field_mode_clamp_zero (boundary.F90:772-829) on one boundary
-__device__ void clamp_zero(FView f, int st, int bd, const int* bcf, const RunConst& rc) {
+template <typename T>
+__device__ void clamp_zero(FViewT<T> f, int st, int bd, const int* bcf, const RunConst& rc) {
   if (bcf[bd] == CYL_BC_PERIODIC) return;
   const int nx = rc.nx, ny = rc.ny, M = rc.M;
   const cplx Z = mk(0.0, 0.0);
@@ -163,7 +166,8 @@ __device__ void clamp_zero(FView f, int st, int bd, const int* bcf, const RunCon
 }
 
 // efield_bcs (boundary.F90:1355-1413)
-__device__ void efield_bcs_dev(FView ex, FView er, FView et, const int* bcf, const RunConst& rc) {
+template <typename T>
+__device__ void efield_bcs_dev(FViewT<T> ex, FViewT<T> er, FViewT<T> et, const int* bcf, const RunConst& rc) {
   __syncthreads();
   halo_x(ex, 1 - NG, rc.ny + NG - 1, bcf, rc);
   halo_x(er, 1 - NG, rc.ny + NG, bcf, rc);
@@ -200,7 +204,8 @@ __device__ void efield_bcs_dev(FView ex, FView er, FView et, const int* bcf, con
 }
 
 // bfield_bcs (boundary.F90:1417-1476)
-__device__ void bfield_bcs_dev(FView bx, FView br, FView bt, bool mpi_only, const int* bcf,
+template <typename T>
+__device__ void bfield_bcs_dev(FViewT<T> bx, FViewT<T> br, FViewT<T> bt, bool mpi_only, const int* bcf,
                                const RunConst& rc) {
   __syncthreads();
   halo_x(bx, 1 - NG, rc.ny + NG, bcf, rc);
@@ -239,11 +244,13 @@ __device__ void bfield_bcs_dev(FView bx, FView br, FView bt, bool mpi_only, cons
 }
 
 // Axis rules of update_e_field (fields.f90:116-180), one column per thread.
-__device__ void e_axis_dev(FView ex, FView er, FView et, FView jx, FView bt, const RunConst& rc) {
+template <typename T>
+__device__ void e_axis_dev(FViewT<T> ex, FViewT<T> er, FViewT<T> et, FView jx, FViewT<T> bt, const RunConst& rc, int t0,
+                           int tstride) {
   const int M = rc.M;
   const double dy = rc.dy, dt = rc.dt, c2 = CLIGHT * CLIGHT;
   const int ncol = rc.nx + 2 * NG;
-  CTA_FOR(t, ncol) {
+  for (int t = t0; t < ncol; t += tstride) {
     const int ix = 1 - NG + t;
     ex(ix, 0, 0) = ex(ix, 0, 0) + ((4.0 * c2 / dy) * bt(ix, 1, 0) - jx(ix, 0, 0) / EPS0) * 0.5 * dt;
     et(ix, 0, 0) = mk(0.0, 0.0);
@@ -280,11 +287,13 @@ __device__ void e_axis_dev(FView ex, FView er, FView et, FView jx, FView bt, con
 }
 
 // Axis rules of update_b_field (fields.f90:249-310).
-__device__ void b_axis_dev(FView bx, FView br, FView bt, FView ex, FView et, const RunConst& rc) {
+template <typename T>
+__device__ void b_axis_dev(FViewT<T> bx, FViewT<T> br, FViewT<T> bt, FViewT<T> ex, FViewT<T> et, const RunConst& rc, int t0,
+                           int tstride) {
   const int M = rc.M;
   const double dx = rc.dx, dy = rc.dy, dt = rc.dt;
   const int ncol = rc.nx + 2 * NG;
-  CTA_FOR(t, ncol) {
+  for (int t = t0; t < ncol; t += tstride) {
     const int ix = 1 - NG + t;
     br(ix, 0, 0) = mk(0.0, 0.0);
     bx(ix, 0, 0) = bx(ix, 1, 0);
@@ -322,27 +331,28 @@ __device__ void b_axis_dev(FView bx, FView br, FView bt, FView ex, FView et, con
 }
 
 // update_e_field axis rules + efield_bcs (one CTA)
-__global__ void __launch_bounds__(CTA_THREADS) k_e_axis_bcs(FView ex, FView er, FView et, FView jx, FView bt,
+template <typename T>
+__global__ void __launch_bounds__(CTA_THREADS) k_e_axis_bcs(FViewT<T> ex, FViewT<T> er, FViewT<T> et, FView jx, FViewT<T> bt,
                              const StepRec* rec, RunConst rc) {
   __shared__ int bcf[4];
   if (threadIdx.x < 4) bcf[threadIdx.x] = rec->bc_field[threadIdx.x];
   __syncthreads();
-  e_axis_dev(ex, er, et, jx, bt, rc);
   efield_bcs_dev(ex, er, et, bcf, rc);
 }
 
 // update_b_field axis rules + bfield_bcs(.TRUE.) (one CTA)
-__global__ void __launch_bounds__(CTA_THREADS) k_b_axis_bcs(FView bx, FView br, FView bt, FView ex, FView et,
+template <typename T>
+__global__ void __launch_bounds__(CTA_THREADS) k_b_axis_bcs(FViewT<T> bx, FViewT<T> br, FViewT<T> bt, FViewT<T> ex, FViewT<T> et,
                              const StepRec* rec, RunConst rc) {
   __shared__ int bcf[4];
   if (threadIdx.x < 4) bcf[threadIdx.x] = rec->bc_field[threadIdx.x];
   __syncthreads();
-  b_axis_dev(bx, br, bt, ex, et, rc);
   bfield_bcs_dev(bx, br, bt, true, bcf, rc);
 }
 
 // efield_bcs alone (start-up, epoch2d.F90:144)
-__global__ void __launch_bounds__(CTA_THREADS) k_efield_bcs(FView ex, FView er, FView et, const StepRec* rec, RunConst rc) {
+template <typename T>
+__global__ void __launch_bounds__(CTA_THREADS) k_efield_bcs(FViewT<T> ex, FViewT<T> er, FViewT<T> et, const StepRec* rec, RunConst rc) {
   __shared__ int bcf[4];
   if (threadIdx.x < 4) bcf[threadIdx.x] = rec->bc_field[threadIdx.x];
   __syncthreads();
@@ -354,7 +364,8 @@ __global__ void __launch_bounds__(CTA_THREADS) k_efield_bcs(FView ex, FView er, 
 // outflow (laser.f90:637-690).  src holds this step's Cartesian laser
 // sources (source1, source2 for x_min then x_max, each ny+1 values), which
 // the host evaluates from the deck's time and transverse profiles.
-__global__ void __launch_bounds__(CTA_THREADS) k_b_axis_final_bcs(FieldSet F, const StepRec* rec, const double* src,
+template <typename T>
+__global__ void __launch_bounds__(CTA_THREADS) k_b_axis_final_bcs(FieldSetT<T> F, const StepRec* rec, const double* src,
                                    const cplx* cols, int do_axis, double dt, RunConst rc) {
   __shared__ int bcf[4];
   __shared__ int addl[4];
@@ -365,7 +376,6 @@ __global__ void __launch_bounds__(CTA_THREADS) k_b_axis_final_bcs(FieldSet F, co
   __syncthreads();
   rc.dt = dt;
   const int nx = rc.nx, ny = rc.ny, M = rc.M;
-  if (do_axis) b_axis_dev(F.bx, F.br, F.bt, F.ex, F.et, rc);
   bfield_bcs_dev(F.bx, F.br, F.bt, false, bcf, rc);
   __syncthreads();
   const double c2 = CLIGHT * CLIGHT;
@@ -544,9 +554,9 @@ __device__ void reflect_side(FView f, int flip, int bd, const RunConst& rc) {
 }
 
 // current_bcs_r_min_final (boundary.F90:1909-1959), per column
-__device__ void j_rmin_dev(FView jx, FView jr, FView jt, const RunConst& rc) {
+__device__ void j_rmin_dev(FView jx, FView jr, FView jt, const RunConst& rc, int t0, int tstride) {
   const int ncol = rc.nx + 2 * NG;
-  CTA_FOR(t, ncol) {
+  for (int t = t0; t < ncol; t += tstride) {
     const int ix = 1 - NG + t;
     double mode_sign = 1.0;
     for (int im = 0; im < rc.M; ++im) {
@@ -599,8 +609,6 @@ __global__ void __launch_bounds__(CTA_THREADS) k_current_finish(FView jx, FView 
   __shared__ int bcf[4];
   if (threadIdx.x < 4) bcf[threadIdx.x] = rec->bc_field[threadIdx.x];
   __syncthreads();
-  j_rmin_dev(jx, jr, jt, rc);
-  __syncthreads();
   const int bds[3] = {CYL_BD_X_MIN, CYL_BD_X_MAX, CYL_BD_Y_MAX};
   for (int k = 0; k < 3; ++k) {
     if (rc.bc_allspecies[bds[k]] == CYL_BC_REFLECT) {
@@ -649,29 +657,40 @@ __global__ void __launch_bounds__(CTA_THREADS) k_halo_rows(FView f, const StepRe
 // staged in shared memory so the in-place left shift is race free.  The
 // periodic self-wrap of shift_field_modes and the x_max column fix-ups act
 // within the same row.
-__global__ void k_shift_fields(FieldSet F, const cplx* cols, const StepRec* rec, int which, RunConst rc) {
+template <typename U>
+__device__ void shift_row(FViewT<U> f, cplx* row, int j, int m, const int* bcf, const RunConst& rc) {
+  const int nxg = rc.nxg, nx = rc.nx;
+  __syncthreads();
+  for (int i = threadIdx.x; i < nxg; i += blockDim.x) row[i] = f(1 - NG + i, j, m);
+  __syncthreads();
+  for (int i = threadIdx.x; i < nxg - 1; i += blockDim.x) f(1 - NG + i, j, m) = row[i + 1];
+  __syncthreads();
+  // periodic self-wrap (field_mode_bc) within this row
+  if (bcf[CYL_BD_X_MAX] == CYL_BC_PERIODIC)
+    for (int i = 1 + threadIdx.x; i <= NG; i += blockDim.x) f(nx + i, j, m) = f(i, j, m);
+  __syncthreads();
+  if (bcf[CYL_BD_X_MIN] == CYL_BC_PERIODIC)
+    for (int i = 1 - NG + threadIdx.x; i <= 0; i += blockDim.x) f(i, j, m) = f(nx + i, j, m);
+}
+
+template <typename T>
+__global__ void k_shift_fields(FieldSetT<T> F, const cplx* cols, const StepRec* rec, int which, RunConst rc) {
   extern __shared__ cplx row[];
   const int j = 1 - NG + (int)blockIdx.x;
   const int m = blockIdx.y;
-  const int nxg = rc.nxg, nx = rc.nx;
+  const int nx = rc.nx;
   __shared__ int bcf[4];
   if (threadIdx.x < 4) bcf[threadIdx.x] = rec->bc_field_after[threadIdx.x];
   if (rec->nshift <= which) return;
-  FView arr[9] = {F.ex, F.er, F.et, F.bx, F.br, F.bt, F.jx, F.jr, F.jt};
-  for (int a = 0; a < 9; ++a) {
-    FView f = arr[a];
-    __syncthreads();
-    for (int i = threadIdx.x; i < nxg; i += blockDim.x) row[i] = f(1 - NG + i, j, m);
-    __syncthreads();
-    for (int i = threadIdx.x; i < nxg - 1; i += blockDim.x) f(1 - NG + i, j, m) = row[i + 1];
-    __syncthreads();
-    // periodic self-wrap (field_mode_bc) within this row
-    if (bcf[CYL_BD_X_MAX] == CYL_BC_PERIODIC)
-      for (int i = 1 + threadIdx.x; i <= NG; i += blockDim.x) f(nx + i, j, m) = f(i, j, m);
-    __syncthreads();
-    if (bcf[CYL_BD_X_MIN] == CYL_BC_PERIODIC)
-      for (int i = 1 - NG + threadIdx.x; i <= 0; i += blockDim.x) f(i, j, m) = f(nx + i, j, m);
-  }
+  shift_row(F.ex, row, j, m, bcf, rc);
+  shift_row(F.er, row, j, m, bcf, rc);
+  shift_row(F.et, row, j, m, bcf, rc);
+  shift_row(F.bx, row, j, m, bcf, rc);
+  shift_row(F.br, row, j, m, bcf, rc);
+  shift_row(F.bt, row, j, m, bcf, rc);
+  shift_row(F.jx, row, j, m, bcf, rc);
+  shift_row(F.jr, row, j, m, bcf, rc);
+  shift_row(F.jt, row, j, m, bcf, rc);
   __syncthreads();
   if (threadIdx.x == 0) {
     const int ncolv = rc.ny + 2 * NG;
@@ -691,6 +710,21 @@ __global__ void k_shift_fields(FieldSet F, const cplx* cols, const StepRec* rec,
   }
 }
 
+// Axis rules act column by column, so they run on many CTAs (one thread per
+// column); the boundary phases that follow stay in the single-CTA kernels.
+template <typename T>
+__global__ void k_e_axis(FViewT<T> ex, FViewT<T> er, FViewT<T> et, FView jx, FViewT<T> bt, RunConst rc) {
+  e_axis_dev(ex, er, et, jx, bt, rc, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+template <typename T>
+__global__ void k_b_axis(FViewT<T> bx, FViewT<T> br, FViewT<T> bt, FViewT<T> ex, FViewT<T> et, RunConst rc) {
+  b_axis_dev(bx, br, bt, ex, et, rc, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+__global__ void k_j_rmin(FView jx, FView jr, FView jt, RunConst rc) {
+  j_rmin_dev(jx, jr, jt, rc, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+static int axis_blocks(const RunConst& rc) { return (rc.nx + 2 * NG + 63) / 64; }
+
 // ------------------------------------------------------------ launchers
 
 void launch_update_e(cudaStream_t s, const FieldSet& F, const RunConst& rc) {
@@ -701,21 +735,30 @@ void launch_update_b(cudaStream_t s, const FieldSet& F, int save_old, const RunC
   dim3 blk(128), grd((rc.nxg + 127) / 128, rc.nyg, rc.M);
   k_update_b<<<grd, blk, 0, s>>>(F.ex, F.er, F.et, F.bx, F.br, F.bt, F.bxo, F.bro, F.bto, save_old, rc);
 }
-void launch_e_axis_bcs(cudaStream_t s, const FieldSet& F, const StepRec* rec, const RunConst& rc) {
-  k_e_axis_bcs<<<1, CTA_THREADS, 0, s>>>(F.ex, F.er, F.et, F.jx, F.bt, rec, rc);
+template <typename T>
+void launch_e_axis_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc) {
+  k_e_axis<T><<<axis_blocks(rc), 64, 0, s>>>(F.ex, F.er, F.et, F.jx, F.bt, rc);
+  k_e_axis_bcs<T><<<1, CTA_THREADS, 0, s>>>(F.ex, F.er, F.et, F.jx, F.bt, rec, rc);
 }
-void launch_efield_bcs(cudaStream_t s, const FieldSet& F, const StepRec* rec, const RunConst& rc) {
-  k_efield_bcs<<<1, CTA_THREADS, 0, s>>>(F.ex, F.er, F.et, rec, rc);
+template <typename T>
+void launch_efield_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc) {
+  k_efield_bcs<T><<<1, CTA_THREADS, 0, s>>>(F.ex, F.er, F.et, rec, rc);
 }
-void launch_b_axis_bcs(cudaStream_t s, const FieldSet& F, const StepRec* rec, const RunConst& rc) {
-  k_b_axis_bcs<<<1, CTA_THREADS, 0, s>>>(F.bx, F.br, F.bt, F.ex, F.et, rec, rc);
+template <typename T>
+void launch_b_axis_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc) {
+  k_b_axis<T><<<axis_blocks(rc), 64, 0, s>>>(F.bx, F.br, F.bt, F.ex, F.et, rc);
+  k_b_axis_bcs<T><<<1, CTA_THREADS, 0, s>>>(F.bx, F.br, F.bt, F.ex, F.et, rec, rc);
 }
-void launch_b_final_bcs(cudaStream_t s, const FieldSet& F, const StepRec* rec, const double* src,
+template <typename T>
+void launch_b_final_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const double* src,
                         const cplx* cols, int do_axis, double dt, const RunConst& rc) {
-  k_b_axis_final_bcs<<<1, CTA_THREADS, 0, s>>>(F, rec, src, cols, do_axis, dt, rc);
+  if (do_axis) k_b_axis<T><<<axis_blocks(rc), 64, 0, s>>>(F.bx, F.br, F.bt, F.ex, F.et, rc);
+  k_b_axis_final_bcs<T><<<1, CTA_THREADS, 0, s>>>(F, rec, src, cols, do_axis, dt, rc);
 }
-void launch_current_finish(cudaStream_t s, const FieldSet& F, const StepRec* rec, const RunConst& rc,
+template <typename T>
+void launch_current_finish(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc,
                            int smooth, int its, int comp_its, int stride, FView wk) {
+  k_j_rmin<<<axis_blocks(rc), 64, 0, s>>>(F.jx, F.jr, F.jt, rc);
   k_current_finish<<<1, CTA_THREADS, 0, s>>>(F.jx, F.jr, F.jt, rec, rc);
   if (!smooth) return;
   FView js[3] = {F.jx, F.jr, F.jt};
@@ -733,10 +776,25 @@ void launch_current_finish(cudaStream_t s, const FieldSet& F, const StepRec* rec
     k_copy_interior<<<grd, blk, 0, s>>>(js[a], wk, rc);
   }
 }
-void launch_shift_fields(cudaStream_t s, const FieldSet& F, const cplx* cols, const StepRec* rec,
+template <typename T>
+void launch_shift_fields(cudaStream_t s, const FieldSetT<T>& F, const cplx* cols, const StepRec* rec,
                          int which, const RunConst& rc) {
   dim3 grd(rc.nyg, rc.M);
-  k_shift_fields<<<grd, 256, (size_t)rc.nxg * sizeof(cplx), s>>>(F, cols, rec, which, rc);
+  k_shift_fields<T><<<grd, 256, (size_t)rc.nxg * sizeof(cplx), s>>>(F, cols, rec, which, rc);
 }
+
+#define INST(T)                                                                                          \
+  template void launch_e_axis_bcs<T>(cudaStream_t, const FieldSetT<T>&, const StepRec*, const RunConst&);  \
+  template void launch_efield_bcs<T>(cudaStream_t, const FieldSetT<T>&, const StepRec*, const RunConst&);  \
+  template void launch_b_axis_bcs<T>(cudaStream_t, const FieldSetT<T>&, const StepRec*, const RunConst&);  \
+  template void launch_b_final_bcs<T>(cudaStream_t, const FieldSetT<T>&, const StepRec*, const double*,    \
+                                      const cplx*, int, double, const RunConst&);                          \
+  template void launch_current_finish<T>(cudaStream_t, const FieldSetT<T>&, const StepRec*, const RunConst&, \
+                                         int, int, int, int, FView);                                       \
+  template void launch_shift_fields<T>(cudaStream_t, const FieldSetT<T>&, const cplx*, const StepRec*, int,  \
+                                       const RunConst&);
+INST(cplx)
+INST(cplxf)
+#undef INST
 
 }  // namespace cyl

@@ -1,0 +1,139 @@
+// fields_fp32.cu -- bulk per-mode Yee updates of the mixed-precision form.
+//
+// Same equations as update_e_field / update_b_field (fields.f90:67-108,
+// 203-241) with E and B stored as FP32 complex and the currents FP64.  The
+// bulk rows run in FP32 with the per-row coefficients (c^2/r, dt/r, ...)
+// precomputed; the first radial cell (ir = 1, where the 1/r terms are
+// largest) is updated in FP64 arithmetic.  The FP64 -> FP32 conversion of
+// the currents is done with integer operations (GB300's FP64 pipe is narrow).
+#include "cyl_common.cuh"
+#include "cyl_kernels.cuh"
+#include "cyl_convert.cuh"
+
+namespace cyl {
+
+// rowtab (per ir = 0 .. ny+1, float4): x = c^2/r_p * dt/2, y = c^2/r_d * dt/2,
+// z = dt/2 / r_d, w = dt/2 / r_p
+__device__ __forceinline__ float2 ld2(const cplxf* p) { return *reinterpret_cast<const float2*>(p); }
+__device__ __forceinline__ void st2(cplxf* p, float2 v) { *reinterpret_cast<float2*>(p) = v; }
+__device__ __forceinline__ float2 ldj(const cplx* p) {
+  const double2 v = *reinterpret_cast<const double2*>(p);
+  return make_float2(d2f_bits(v.x), d2f_bits(v.y));
+}
+
+__global__ void k_update_e_f32(FieldSetF F, const float4* rowtab, float cdx, float cdy, float cj, RunConst rc) {
+  const int ix = blockIdx.x * blockDim.x + threadIdx.x;  // 0..nx
+  const int ir = 1 + blockIdx.y;
+  const int im = blockIdx.z;
+  if (ix > rc.nx) return;
+  if (ir == 1) {
+    // first radial cell in FP64 arithmetic (same equations as update_e_field)
+    const double dx = rc.dx, dy = rc.dy, dt = rc.dt, c2 = CLIGHT * CLIGHT;
+    const double r_d = fabs((double)(ir - 1) * dy + rc.y_grid_min);
+    const double r_p = r_d + 0.5 * dy;
+    const double fac_x = c2 / r_p;
+    const cplx im_fac_x = (IMAGI * (double)im) * fac_x;
+    const cplx im_fac_r = ((IMAGI * (double)im) * c2) / r_d;
+    const cplx bt0 = F.bt(ix, ir, im), bt1 = F.bt(ix, ir + 1, im), btx = F.bt(ix + 1, ir, im);
+    const cplx br0 = F.br(ix, ir, im), brx = F.br(ix + 1, ir, im);
+    const cplx bx0 = F.bx(ix, ir, im), bx1 = F.bx(ix, ir + 1, im);
+    F.ex(ix, ir, im) = (cplx)F.ex(ix, ir, im) +
+        ((((fac_x * 0.5) * (bt1 + bt0) + im_fac_x * br0) + (c2 * (bt1 - bt0)) / dy) -
+         (cplx)F.jx(ix, ir, im) / EPS0) * 0.5 * dt;
+    F.er(ix, ir, im) = (cplx)F.er(ix, ir, im) +
+        ((-(im_fac_r * bx0) - (c2 * (btx - bt0)) / dx) - (cplx)F.jr(ix, ir, im) / EPS0) * 0.5 * dt;
+    F.et(ix, ir, im) = (cplx)F.et(ix, ir, im) +
+        (((c2 * (brx - br0)) / dx - (c2 * (bx1 - bx0)) / dy) - (cplx)F.jt(ix, ir, im) / EPS0) * 0.5 * dt;
+    return;
+  }
+  const float4 rt = rowtab[ir];
+  const float m = (float)im;
+  const float2 bt0 = ld2(F.bt.ptr(ix, ir, im)), bt1 = ld2(F.bt.ptr(ix, ir + 1, im)), btx = ld2(F.bt.ptr(ix + 1, ir, im));
+  const float2 br0 = ld2(F.br.ptr(ix, ir, im)), brx = ld2(F.br.ptr(ix + 1, ir, im));
+  const float2 bx0 = ld2(F.bx.ptr(ix, ir, im)), bx1 = ld2(F.bx.ptr(ix, ir + 1, im));
+  const float2 jx = ldj(F.jx.ptr(ix, ir, im)), jr = ldj(F.jr.ptr(ix, ir, im)), jt = ldj(F.jt.ptr(ix, ir, im));
+  // ex += c^2/r_p*dt/2 * (0.5 (bt1 + bt0) + i m br0) + c^2 dt/(2 dy) (bt1 - bt0) - dt/(2 eps0) jx
+  float2 e = ld2(F.ex.ptr(ix, ir, im));
+  const float a = rt.x, am = rt.x * m, b = rt.y * m;
+  e.x += a * 0.5f * (bt1.x + bt0.x) - am * br0.y + cdy * (bt1.x - bt0.x) - cj * jx.x;
+  e.y += a * 0.5f * (bt1.y + bt0.y) + am * br0.x + cdy * (bt1.y - bt0.y) - cj * jx.y;
+  st2(F.ex.ptr(ix, ir, im), e);
+  // er += -i m c^2/r_d dt/2 bx0 - c^2 dt/(2 dx) (btx - bt0) - dt/(2 eps0) jr
+  e = ld2(F.er.ptr(ix, ir, im));
+  e.x += b * bx0.y - cdx * (btx.x - bt0.x) - cj * jr.x;
+  e.y += -b * bx0.x - cdx * (btx.y - bt0.y) - cj * jr.y;
+  st2(F.er.ptr(ix, ir, im), e);
+  // et += c^2 dt/(2 dx) (brx - br0) - c^2 dt/(2 dy) (bx1 - bx0) - dt/(2 eps0) jt
+  e = ld2(F.et.ptr(ix, ir, im));
+  e.x += cdx * (brx.x - br0.x) - cdy * (bx1.x - bx0.x) - cj * jt.x;
+  e.y += cdx * (brx.y - br0.y) - cdy * (bx1.y - bx0.y) - cj * jt.y;
+  st2(F.et.ptr(ix, ir, im), e);
+}
+
+__global__ void k_update_b_f32(FieldSetF F, int save_old, const float4* rowtab, float hdx, float hdy,
+                               RunConst rc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  const int im = blockIdx.z;
+  if (i >= rc.nxg) return;
+  const int ix = i + 1 - NG, ir = j + 1 - NG;
+  if (save_old) {
+    st2(F.bxo.ptr(ix, ir, im), ld2(F.bx.ptr(ix, ir, im)));
+    st2(F.bro.ptr(ix, ir, im), ld2(F.br.ptr(ix, ir, im)));
+    st2(F.bto.ptr(ix, ir, im), ld2(F.bt.ptr(ix, ir, im)));
+  }
+  if (ix < 0 || ix > rc.nx || ir < 1 || ir > rc.ny - 1) return;
+  if (ir == 1) {
+    const double dx = rc.dx, dy = rc.dy, dt = rc.dt;
+    const double r_d = fabs((double)(ir - 1) * dy + rc.y_grid_min);
+    const double r_p = r_d + 0.5 * dy;
+    const cplx im_fac_x = (IMAGI * (double)im) / r_d;
+    const cplx im_fac_r = (IMAGI * (double)im) / r_p;
+    const cplx et0 = F.et(ix, ir, im), etm1 = F.et(ix, ir - 1, im), etxm = F.et(ix - 1, ir, im);
+    const cplx er0 = F.er(ix, ir, im), erxm = F.er(ix - 1, ir, im);
+    const cplx ex0 = F.ex(ix, ir, im), exm1 = F.ex(ix, ir - 1, im);
+    F.bx(ix, ir, im) = (cplx)F.bx(ix, ir, im) -
+        ((im_fac_x * er0 + (0.5 * (et0 + etm1)) / r_d) + (et0 - etm1) / dy) * 0.5 * dt;
+    F.br(ix, ir, im) = (cplx)F.br(ix, ir, im) + (im_fac_r * ex0 + (et0 - etxm) / dx) * 0.5 * dt;
+    F.bt(ix, ir, im) = (cplx)F.bt(ix, ir, im) + (-((er0 - erxm) / dx) + (ex0 - exm1) / dy) * 0.5 * dt;
+    return;
+  }
+  const float4 rt = rowtab[ir];
+  const float m = (float)im;
+  const float2 et0 = ld2(F.et.ptr(ix, ir, im)), etm1 = ld2(F.et.ptr(ix, ir - 1, im)), etxm = ld2(F.et.ptr(ix - 1, ir, im));
+  const float2 er0 = ld2(F.er.ptr(ix, ir, im)), erxm = ld2(F.er.ptr(ix - 1, ir, im));
+  const float2 ex0 = ld2(F.ex.ptr(ix, ir, im)), exm1 = ld2(F.ex.ptr(ix, ir - 1, im));
+  // bx -= dt/2 (i m/r_d er0 + 0.5 (et0 + etm1)/r_d + (et0 - etm1)/dy)
+  const float c1 = rt.z * m, c2 = rt.z * 0.5f, c3 = rt.w * m;
+  float2 b = ld2(F.bx.ptr(ix, ir, im));
+  b.x -= -c1 * er0.y + c2 * (et0.x + etm1.x) + hdy * (et0.x - etm1.x);
+  b.y -= c1 * er0.x + c2 * (et0.y + etm1.y) + hdy * (et0.y - etm1.y);
+  st2(F.bx.ptr(ix, ir, im), b);
+  // br += dt/2 (i m/r_p ex0 + (et0 - etxm)/dx)
+  b = ld2(F.br.ptr(ix, ir, im));
+  b.x += -c3 * ex0.y + hdx * (et0.x - etxm.x);
+  b.y += c3 * ex0.x + hdx * (et0.y - etxm.y);
+  st2(F.br.ptr(ix, ir, im), b);
+  // bt += dt/2 (-(er0 - erxm)/dx + (ex0 - exm1)/dy)
+  b = ld2(F.bt.ptr(ix, ir, im));
+  b.x += -hdx * (er0.x - erxm.x) + hdy * (ex0.x - exm1.x);
+  b.y += -hdx * (er0.y - erxm.y) + hdy * (ex0.y - exm1.y);
+  st2(F.bt.ptr(ix, ir, im), b);
+}
+
+void launch_update_e_f32(cudaStream_t s, const FieldSetF& F, const double* rowtab, const RunConst& rc) {
+  const double c2 = CLIGHT * CLIGHT, h = 0.5 * rc.dt;
+  dim3 blk(128), grd((rc.nx + 1 + 127) / 128, rc.ny, rc.M);
+  k_update_e_f32<<<grd, blk, 0, s>>>(F, reinterpret_cast<const float4*>(rowtab), (float)(c2 / rc.dx * h),
+                                     (float)(c2 / rc.dy * h), (float)(h / EPS0), rc);
+}
+
+void launch_update_b_f32(cudaStream_t s, const FieldSetF& F, int save_old, const double* rowtab,
+                         const RunConst& rc) {
+  const double h = 0.5 * rc.dt;
+  dim3 blk(128), grd((rc.nxg + 127) / 128, rc.nyg, rc.M);
+  k_update_b_f32<<<grd, blk, 0, s>>>(F, save_old, reinterpret_cast<const float4*>(rowtab), (float)(h / rc.dx),
+                                     (float)(h / rc.dy), rc);
+}
+
+}  // namespace cyl

@@ -207,7 +207,8 @@ void launch_energy(cudaStream_t s, const SpeciesPtrs& sp, const SpeciesCounters*
 
 // Per-mode field energy over the interior: m = 0 contributes |F_0|^2, m >= 1
 // contributes |F_m|^2 / 2 (F = Re sum F_m e^{-im theta}), cell volume 2 pi r dx dr.
-__global__ void k_field_energy(FieldSet F, RunConst rc, double* out) {
+template <typename T>
+__global__ void k_field_energy(FieldSetT<T> F, RunConst rc, double* out) {
   const int ix = 1 + blockIdx.x * blockDim.x + threadIdx.x;
   const int iy = 1 + blockIdx.y;
   const int m = blockIdx.z;
@@ -233,10 +234,13 @@ __global__ void k_field_energy(FieldSet F, RunConst rc, double* out) {
   }
 }
 
-void launch_field_energy(cudaStream_t s, const FieldSet& F, const RunConst& rc, double* out) {
+template <typename T>
+void launch_field_energy(cudaStream_t s, const FieldSetT<T>& F, const RunConst& rc, double* out) {
   dim3 blk(128), grd((rc.nx + 127) / 128, rc.ny, rc.M);
-  k_field_energy<<<grd, blk, 0, s>>>(F, rc, out);
+  k_field_energy<T><<<grd, blk, 0, s>>>(F, rc, out);
 }
+template void launch_field_energy<cplx>(cudaStream_t, const FieldSet&, const RunConst&, double*);
+template void launch_field_energy<cplxf>(cudaStream_t, const FieldSetF&, const RunConst&, double*);
 
 // ------------------------------------------------------------- sorting
 

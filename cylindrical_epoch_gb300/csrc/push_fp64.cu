@@ -332,9 +332,9 @@ __global__ void __launch_bounds__(256) k_push_fp64(FieldSet F, GeomTables g, Spe
           jxh = jxh - (fjx * hx[ix + 2]) * w_rt;
           jyh[ix + 2] = jyh[ix + 2] * rat - fjy * w_xt;
           const cplx jzh = fjz * w_xr;
-          catomic_add(&F.jx(cx + 1, cy, im), jxh);
-          catomic_add(&F.jr(cx, cy + 1, im), jyh[ix + 2]);
-          catomic_add(&F.jt(cx, cy, im), jzh);
+          catomic_add(F.jx.ptr(cx + 1, cy, im), jxh);
+          catomic_add(F.jr.ptr(cx, cy + 1, im), jyh[ix + 2]);
+          catomic_add(F.jt.ptr(cx, cy, im), jzh);
         }
       }
     }

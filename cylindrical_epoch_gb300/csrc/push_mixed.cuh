@@ -30,15 +30,20 @@ struct MixedParams {
   float x_lo, x_hi, x_sys_lo, x_sys_hi, x_out_lo, x_out_hi;
   float r_hi, r_sys, r_out;
   int* err;
+  // FP32 copies of the geometric factors (rows 1-jng.., 0-jng.., 1-jng..)
+  const float *g_rt, *g_xt, *g_vol;
+  // particles deferred to the global-memory pass
+  int* fb_list;
+  int* fb_count;
 };
 
 MixedParams mixed_params(const SpeciesPtrs& sp, const RunConst& rc);
 size_t push_mixed_smem(int M);
 int push_mixed_blocks_per_sm(int M);
 
-void launch_push_mixed(cudaStream_t s, const FieldSet& F, const GeomTables& g, const SpeciesPtrs& sp,
-                       SpeciesCounters* cnt, const StepRec* rec, const RunConst& rc, int apply_bcs,
-                       int* err, int nblocks, const MixedParams& P, TileTable* tt);
+void launch_push_mixed(cudaStream_t s, const FieldSetF& F, const SpeciesPtrs& sp, SpeciesCounters* cnt,
+                       const StepRec* rec, const RunConst& rc, int apply_bcs, int nblocks_tiles,
+                       int nblocks_global, const MixedParams& P, TileTable* tt);
 
 // mixed_particles.cu
 void mixed_from_double(cudaStream_t s, const SpeciesPtrs& sp, const double* stage, int64_t n, int64_t cap,
