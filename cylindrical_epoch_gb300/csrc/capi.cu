@@ -10,6 +10,7 @@
 // once into a CUDA graph and replayed.
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -54,6 +55,7 @@ struct Handle {
   float4* rowtab = nullptr;   // per-row FP32 Yee coefficients of the mixed form
   float* gtab_f = nullptr;    // FP32 geometric factors of the mixed deposit
   int* fb_buf = nullptr;      // mixed form: deferred-particle lists + counters
+  float* d_dbg = nullptr;     // diagnostic record of the first flagged particle
   int jpar = 0;       // 0: J in slots 6..8, J_old in 12..14; 1: swapped
   cplx* cols = nullptr;
   double* geom_buf = nullptr;
@@ -607,6 +609,8 @@ int cyl_create(const cyl_grid_desc* gd, const cyl_species_desc* spd, int32_t nsp
   h->nblocks = nsm * 8;
   cudaMalloc(&h->d_err, sizeof(int));
   cudaMemset(h->d_err, 0, sizeof(int));
+  cudaMalloc(&h->d_dbg, 16 * sizeof(float));
+  cudaMemset(h->d_dbg, 0, 16 * sizeof(float));
   // fields: 15 arrays + one work array, one allocation
   h->fcount = (size_t)rc.nxg * rc.nyg * rc.M;
   if (cudaMalloc(&h->fbuf, h->fcount * 16 * sizeof(cplx)) != cudaSuccess) {
@@ -683,6 +687,7 @@ int cyl_create(const cyl_grid_desc* gd, const cyl_species_desc* spd, int32_t nsp
       h->mp[i].g_vol = h->gtab_f + n1 + n0;
       h->mp[i].fb_count = h->fb_buf + off;
       h->mp[i].fb_list = h->fb_buf + off + 1;
+      h->mp[i].dbg = h->d_dbg;
       off += h->sp[i].cap + 1;
     }
   }
@@ -753,6 +758,7 @@ int cyl_destroy(cyl_handle hh) {
   cudaFree(h->rowtab);
   cudaFree(h->gtab_f);
   cudaFree(h->fb_buf);
+  cudaFree(h->d_dbg);
   cudaFree(h->d_tile_start);
   cudaFree(h->sort_buf);
   cudaFree(h->d_err);
@@ -1034,6 +1040,14 @@ int cyl_diagnostics(cyl_handle hh, cyl_diag* out) {
   out->field_energy_b = 0.5 / (4.0e-7 * PI) * red[3];
   out->jsum_abs = red[4];
   out->device_error = err;
+  return CYL_OK;
+}
+
+int cyl_debug_record(cyl_handle hh, float* out16) {
+  if (!hh || !out16) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  CK(cudaStreamSynchronize(h->st));
+  CK(cudaMemcpy(out16, h->d_dbg, 16 * sizeof(float), cudaMemcpyDeviceToHost));
   return CYL_OK;
 }
 

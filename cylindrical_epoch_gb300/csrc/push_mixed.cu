@@ -104,6 +104,16 @@ struct Gather {
   }
 };
 
+__device__ __forceinline__ void record(const MixedParams& P, int reason, int64_t i, float a, float b, float c,
+                                       float d, float e, float f, float g, float h) {
+  if (!P.dbg) return;
+  int* flag = reinterpret_cast<int*>(P.dbg);
+  if (atomicCAS(flag, 0, reason) != 0) return;
+  P.dbg[1] = (float)i;
+  P.dbg[2] = a; P.dbg[3] = b; P.dbg[4] = c; P.dbg[5] = d;
+  P.dbg[6] = e; P.dbg[7] = f; P.dbg[8] = g; P.dbg[9] = h;
+}
+
 __device__ __forceinline__ void gadd_f(cplx* p, float re, float im) {
   atomicAdd(&p->re, f2d_bits(re));
   if (im != 0.f) atomicAdd(&p->im, f2d_bits(im));
@@ -150,6 +160,7 @@ __device__ __forceinline__ bool push_one(int64_t i, const SpeciesPtrs& sp, Speci
     if (cx2 - 2 < 1 - NG || cx2 + 3 > rc.nx + NG || cy2 - 2 < 1 - NG || cy2 + 3 > rc.ny + NG ||
         cx1 - 1 < 1 - NG || cx1 + 1 > rc.nx + NG || cy1 - 1 < 1 - NG || cy1 + 1 > rc.ny + NG) {
       atomicOr(P.err, ERR_CELL_RANGE);
+      record(P, 1, i, (float)k, fx, y, z, (float)cx2, (float)cy2, (float)cx1, (float)cy1);
       return true;
     }
   }
@@ -203,6 +214,11 @@ __device__ __forceinline__ bool push_one(int64_t i, const SpeciesPtrs& sp, Speci
       emi = emi * e1;
     }
   }
+  if (!isfinite(exr + er_ + etr + bxr + brr + btr)) {
+    atomicOr(P.err, ERR_NONFINITE);
+    record(P, 20 + (SHARED ? 10 : 0), i, exr, er_, etr, bxr, brr, btr, (float)cx2, (float)cy2);
+    return true;
+  }
   const float eyr = er_ * ct - etr * st;
   const float ezr = er_ * st + etr * ct;
   const float byr = brr * ct - btr * st;
@@ -222,6 +238,11 @@ __device__ __forceinline__ bool push_one(int64_t i, const SpeciesPtrs& sp, Speci
   ux = uxp + cm * exr;
   uy = uyp + cm * eyr;
   uz = uzp + cm * ezr;
+  if (!isfinite(ux + uy + uz)) {
+    atomicOr(P.err, ERR_NONFINITE);
+    record(P, 40 + (SHARED ? 10 : 0), i, exr, er_, etr, bxr, brr, btr, (float)cx1, (float)cy2);
+    return true;
+  }
   gam = sqrtf(ux * ux + uy * uy + uz * uz + 1.0f);
   igm = 1.0f / gam;
   const float dxs = ux * (P.cdt2_dx * igm), dys = uy * (P.cdt2_dy * igm), dzs = uz * (P.cdt2_dy * igm);
@@ -244,6 +265,7 @@ __device__ __forceinline__ bool push_one(int64_t i, const SpeciesPtrs& sp, Speci
   const int dcx = a3 - a2, dcy = b3 - b2;
   if (dcx < -1 || dcx > 1 || dcy < -1 || dcy > 1) {
     atomicOr(P.err, ERR_CELL_RANGE);
+    record(P, 2 + (SHARED ? 10 : 0), i, (float)k, fx, fx3, cyr, cyr3, (float)dcx, (float)dcy, ux);
     return true;
   }
   // old (t+dt/2) staggered weights on offsets -2..2 and their change
@@ -412,19 +434,14 @@ __global__ void __launch_bounds__(PUSH_THREADS) k_push_tiles(FieldSetF F, Specie
   extern __shared__ float4 smem4[];
   float2* sf = reinterpret_cast<float2*>(smem4);        // 6 * M * RCELLS float2
   float* sj = reinterpret_cast<float*>(sf + 6 * M * RCELLS);  // 3 * M * 2 * RCELLS float
-  __shared__ int s_tile;
   const int nsh = rec->nshift_total;
   set_bounds(P, rec, rc);
   const int ntiles = tt->ntiles;
   const int ntx = tt->ntx;
-  for (;;) {
-    if (threadIdx.x == 0) s_tile = atomicAdd(&tt->next, 1);
-    __syncthreads();
-    const int t = s_tile;
-    __syncthreads();
-    if (t >= ntiles) break;
+  // static round-robin over tiles; every thread evaluates the same tile
+  // conditions, so all threads meet the same barriers
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const int64_t p0 = tt->start[t], p1 = tt->start[t + 1];
-    if (p1 <= p0) continue;
     Tile tile;
     tile.sf = sf;
     tile.sj = sj;
@@ -432,6 +449,7 @@ __global__ void __launch_bounds__(PUSH_THREADS) k_push_tiles(FieldSetF F, Specie
     tile.y0 = (t / ntx) * TILE_Y + 1 - DRIFT - 2;
     const bool inside = tile.x0 >= 1 - NG && tile.x0 + RW - 1 <= rc.nx + NG && tile.y0 >= 1 - NG &&
                         tile.y0 + RH - 1 <= rc.ny + NG;
+    if (p1 <= p0) continue;
     if (!inside) {
       // tile partly outside the ghosted grid: every particle takes the global path
       for (int64_t i = p0 + threadIdx.x; i < p1; i += PUSH_THREADS) P.fb_list[atomicAdd(P.fb_count, 1)] = (int)i;

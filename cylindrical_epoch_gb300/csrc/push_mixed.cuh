@@ -35,6 +35,9 @@ struct MixedParams {
   // particles deferred to the global-memory pass
   int* fb_list;
   int* fb_count;
+  // first particle that raised the device error word: reason, index and
+  // state (diagnostic record read by cyl_debug_record)
+  float* dbg;
 };
 
 MixedParams mixed_params(const SpeciesPtrs& sp, const RunConst& rc);

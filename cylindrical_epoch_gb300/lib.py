@@ -38,6 +38,7 @@ SIGNATURES = {
     "cyl_get_run_state": (C.c_int, [H, P(abi.RunState)]),
     "cyl_diagnostics": (C.c_int, [H, P(abi.Diag)]),
     "cyl_get_rng_state": (C.c_int, [H, P(abi.RngState)]),
+    "cyl_debug_record": (C.c_int, [H, P(C.c_float)]),
     "cyl_sort_particles": (C.c_int, [H]),
     "cyl_cell_indices": (C.c_int, [H, I32, PI32, PI32, PI64]),
     "cyl_push_only": (C.c_int, [H]),

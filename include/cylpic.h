@@ -222,6 +222,12 @@ int cyl_get_run_state(cyl_handle h, cyl_run_state* out);
 int cyl_diagnostics(cyl_handle h, cyl_diag* out);
 int cyl_get_rng_state(cyl_handle h, cyl_rng_state* out);
 
+/* The first particle that raised the device error word in the mixed form:
+ * out16[0] holds the reason as an int bit pattern (0 = none), out16[1] the
+ * particle slot, out16[2..9] its state at the failing check.  No
+ * counterpart in the reference (its debug builds trap instead). */
+int cyl_debug_record(cyl_handle h, float* out16);
+
 /* Sort each species' particles by cell tile and drop removed particles
  * (the device analogue of reorder_particles_to_grid, split_particle.F90:29-73). */
 int cyl_sort_particles(cyl_handle h);
