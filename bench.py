@@ -227,18 +227,25 @@ def main():
     s0 = run.state()
     n_start = sum(s0.n_live[i] for i in range(len(deck.species)) if not deck.species[i].immobile)
     clocks = ClockSampler(local)
+    # CUDA events on the handle's own stream bracket the timed steps
+    ext = torch.cuda.ExternalStream(run.stream())
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     clocks.start()
     t0 = time.perf_counter()
+    ev0.record(ext)
     run.step(args.steps, graph=graph)
+    ev1.record(ext)
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     if dist:
         dist.barrier()
     clk = clocks.stop()
-    elapsed = t1 - t0
+    elapsed = ev0.elapsed_time(ev1) * 1e-3
+    wall = t1 - t0
     push_ms, launches = run.kernel_timing()
     s1 = run.state()
     n_end = sum(s1.n_live[i] for i in range(len(deck.species)) if not deck.species[i].immobile)
@@ -252,11 +259,17 @@ def main():
     value = psteps / elapsed
 
     # roofline of the dominant kernel (push + deposit): algorithmic bytes per
-    # particle-step = particle state in + out + amortised field read and
-    # current read-modify-write
+    # particle-step = particle state in + out + amortised field read (6 E/B
+    # mode arrays) and current read-modify-write (3 FP64 J mode arrays) per
+    # cell.  FP64 form: 7 x 8 B read + 6 x 8 B written, E/B 16 B per complex.
+    # Mixed form: 32 B read (int32 cell, FP32 offset, y, z, u(3), w) + 28 B
+    # written, E/B 8 B per complex (FP32 storage), J 16 B.
     M = deck.n_mode
     ppc = deck.species[0].npart_per_cell
-    per_particle = (104.0 if form == "fp64" else 60.0) + 192.0 * M / ppc
+    if form == "fp64":
+        per_particle = 104.0 + (6 * 16 + 3 * 16 * 2) * M / ppc
+    else:
+        per_particle = 60.0 + (6 * 8 + 3 * 16 * 2) * M / ppc
     nparts = 0.5 * (n_start + n_end)
     peak, peak_kind = _peaks()
     achieved = per_particle * nparts / (push_ms * 1e-3) / 1e9 if push_ms > 0 else None
@@ -266,7 +279,7 @@ def main():
         traffic = prof["bytes_per_particle"] * nparts
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                "peak_kind": peak_kind, "kernel": f"k_push_{form}",
+                "peak_kind": peak_kind, "kernel": "k_push_tiles" if form == "mixed" else "k_push_fp64",
                 "kernel_ms": push_ms, "algorithmic_bytes_per_particle_step": per_particle}
 
     fp64 = None
@@ -307,7 +320,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if form == "fp64" else "f32+f64",
             "data": "synthetic", "config": _config(args, deck, form),
             "roofline": roofline, "clocks": clk, "gpu_launches": launches,
-            "particles": nparts,
+            "particles": nparts, "host_wall_s": wall, "timing": "CUDA events on the handle's stream",
         }
         if e2e:
             line["e2e"] = {"value": e2e["value"], "unit": "particle-steps/s",

@@ -8,6 +8,7 @@
 // injects.  All array state (fields, currents, particles) stays resident in
 // HBM.  Steps are enqueued in chunks; a chunk of CHUNK steps can be captured
 // once into a CUDA graph and replayed.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -98,6 +99,7 @@ struct Handle {
   int push_events_used = 0;
   double push_ms_sum = 0.0;
   int64_t push_launches = 0;
+  int timing_pending = 0;  // steps of the last chunk whose push events are not yet read
   int nblocks = 152 * 8;
   int nblocks_mixed = 152 * 4;
   double xg0 = 0.0;  // x_grid_min at creation: origin of the mixed form's cell index
@@ -109,17 +111,37 @@ struct Handle {
   int64_t graph_launches = 0;
 };
 
-static void setup_boundaries(Handle* h) {
+static int map_field_bc(int b) {
   // boundary.F90:30-75
+  if (b == CYL_BC_OTHER) b = CYL_BC_CLAMP;
+  if (b == CYL_BC_REFLECT) b = CYL_BC_CLAMP;
+  if (b == CYL_BC_OPEN) b = CYL_BC_SIMPLE_OUTFLOW;
+  return b;
+}
+
+static void setup_boundaries(Handle* h) {
   for (int i = 0; i < 4; ++i) {
-    int b = h->bc_deck[i];
-    h->add_laser[i] = 0;
-    if (b == CYL_BC_OTHER) b = CYL_BC_CLAMP;
-    if (b == CYL_BC_SIMPLE_LASER) h->add_laser[i] = 1;
-    if (b == CYL_BC_REFLECT) b = CYL_BC_CLAMP;
-    if (b == CYL_BC_OPEN) b = CYL_BC_SIMPLE_OUTFLOW;
-    h->bc_field[i] = b;
+    h->add_laser[i] = h->bc_deck[i] == CYL_BC_SIMPLE_LASER;
+    h->bc_field[i] = map_field_bc(h->bc_deck[i]);
   }
+}
+
+// Field bc kinds a run can meet: the deck's bcs and, with a moving window,
+// the bcs after it starts.
+static int bc_mask_of(const int* deck, const int* after, bool window) {
+  int mask = 0;
+  for (int pass = 0; pass < (window ? 2 : 1); ++pass) {
+    for (int i = 0; i < 4; ++i) {
+      if (i == CYL_BD_Y_MIN) continue;
+      const int b = map_field_bc(pass == 0 ? deck[i] : after[i]);
+      if (b == CYL_BC_PERIODIC && i != CYL_BD_Y_MAX) mask |= BCM_PERIODIC_X;
+      if (b == CYL_BC_CONDUCT) mask |= BCM_CONDUCT;
+      if (b == CYL_BC_CLAMP || b == CYL_BC_SIMPLE_LASER || b == CYL_BC_SIMPLE_OUTFLOW ||
+          b == CYL_BC_ZERO_GRADIENT)
+        mask |= BCM_OTHER;
+    }
+  }
+  return mask;
 }
 
 static int map_particle_bc(int b) {
@@ -444,8 +466,11 @@ static void make_geom(const HostGrid& g, std::vector<double>& out) {
   }
 }
 
+static int flush_push_timing(Handle* h);
+
 static int sync_and_check(Handle* h) {
   CK(cudaStreamSynchronize(h->st));
+  if (int r = flush_push_timing(h)) return r;
   int err = 0;
   CK(cudaMemcpy(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost));
   if (err) return CYL_ERR_DEVICE_FLAG;
@@ -462,11 +487,23 @@ static void collect_push_timing(Handle* h, int nsteps) {
   }
 }
 
+// Read the push events of the last chunk (they are re-recorded by the next).
+static int flush_push_timing(Handle* h) {
+  if (h->timing_pending > 0) {
+    CK(cudaEventSynchronize(h->ev_push[h->timing_pending - 1][1]));
+    collect_push_timing(h, h->timing_pending);
+    h->timing_pending = 0;
+  }
+  return CYL_OK;
+}
+
 static int run_chunk(Handle* h, int k, bool use_graph) {
   // staging buffers are reused: wait until the previous chunk's copies are done
   if (h->copy_pending) CK(cudaEventSynchronize(h->ev_copy));
+  // the host work of this chunk overlaps the device work of the previous one
   int64_t inj_used = 0;
   for (int i = 0; i < k; ++i) prepare_step(h, i, inj_used);
+  if (int r = flush_push_timing(h)) return r;
   CK(cudaMemcpyAsync(h->d_rec, h->h_rec, sizeof(StepRec) * k, cudaMemcpyHostToDevice, h->st));
   CK(cudaMemcpyAsync(h->d_src, h->h_src, sizeof(double) * h->src_per_step * k, cudaMemcpyHostToDevice, h->st));
   if (inj_used > 0)
@@ -504,8 +541,7 @@ static int run_chunk(Handle* h, int k, bool use_graph) {
       enqueue_step(h, h->d_rec + i, h->d_src + h->src_per_step * i, i, true, false);
     enqueue_sort(h, last);
   }
-  CK(cudaEventSynchronize(h->ev_push[k - 1][1]));
-  collect_push_timing(h, k);
+  h->timing_pending = k;
   return CYL_OK;
 }
 
@@ -559,6 +595,7 @@ int cyl_create(const cyl_grid_desc* gd, const cyl_species_desc* spd, int32_t nsp
   }
   setup_boundaries(h);
   h->move_window = gd->move_window != 0;
+  rc.bc_mask = bc_mask_of(gd->bc_field, gd->bc_after_move, h->move_window);
   h->window_v_x = gd->window_v_x;
   h->window_start_time = gd->window_start_time;
   h->window_stop_time = gd->window_stop_time;
@@ -808,10 +845,14 @@ int cyl_upload_particles(cyl_handle hh, int32_t isp, const double* x, const doub
     CK(cudaMemcpyAsync(p.w, w, b, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(p.id, id, b, cudaMemcpyHostToDevice, s));
   }
-  SpeciesCounters c{n, 0};
-  CK(cudaMemcpyAsync(h->d_cnt + isp, &c, sizeof(c), cudaMemcpyHostToDevice, s));
-  for (int64_t i = 0; i < n; ++i)
+  SpeciesCounters c{n, 0, 0u, 0u};
+  float wmax = 0.f;  // largest FP32 weight, for the mixed form's fixed-point deposit scale
+  for (int64_t i = 0; i < n; ++i) {
     if (id[i] >= h->next_id) h->next_id = id[i] + 1;
+    wmax = std::max(wmax, std::fabs((float)w[i]));
+  }
+  std::memcpy(&c.wmax_bits, &wmax, sizeof(float));
+  CK(cudaMemcpyAsync(h->d_cnt + isp, &c, sizeof(c), cudaMemcpyHostToDevice, s));
   CK(cudaStreamSynchronize(s));
   return CYL_OK;
 }
@@ -966,6 +1007,7 @@ int cyl_push_only(cyl_handle hh) {
   if (!hh) return CYL_ERR_BAD_ARG;
   Handle* h = &hh->h;
   if (h->copy_pending) CK(cudaEventSynchronize(h->ev_copy));
+  if (int r = flush_push_timing(h)) return r;
   StepRec& r = h->h_rec[0];
   std::memset(&r, 0, sizeof(r));
   fill_grid(r, h->g, false);
@@ -985,6 +1027,12 @@ int cyl_push_only(cyl_handle hh) {
   CK(cudaEventSynchronize(h->ev_push[0][1]));
   collect_push_timing(h, 1);
   return sync_and_check(h);
+}
+
+int cyl_get_stream(cyl_handle hh, void** stream_out) {
+  if (!hh || !stream_out) return CYL_ERR_BAD_ARG;
+  *stream_out = (void*)hh->h.st;
+  return CYL_OK;
 }
 
 int cyl_kernel_timing(cyl_handle hh, double* push_ms_avg, int64_t* launches) {

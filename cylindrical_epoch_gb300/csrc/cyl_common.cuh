@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/cylpic.h"
+#include "cyl_convert.cuh"
 
 #define CYL_HD __host__ __device__ __forceinline__
 
@@ -64,12 +65,25 @@ constexpr cplx IMAGI = {0.0, 1.0};
 struct cplxf {
   float re, im;
 };
+// On the device the FP32 <-> FP64 conversions use the integer routines of
+// cyl_convert.cuh (the conversion instructions run on the narrow FP64 pipe).
 CYL_HD cplx to_c(const cplx& v) { return v; }
-CYL_HD cplx to_c(const cplxf& v) { return {(double)v.re, (double)v.im}; }
+CYL_HD cplx to_c(const cplxf& v) {
+#ifdef __CUDA_ARCH__
+  return {f2d_bits(v.re), f2d_bits(v.im)};
+#else
+  return {(double)v.re, (double)v.im};
+#endif
+}
 CYL_HD void from_c(cplx& d, const cplx& v) { d = v; }
 CYL_HD void from_c(cplxf& d, const cplx& v) {
+#ifdef __CUDA_ARCH__
+  d.re = d2f_bits(v.re);
+  d.im = d2f_bits(v.im);
+#else
   d.re = (float)v.re;
   d.im = (float)v.im;
+#endif
 }
 
 // Reference to one element of a mode array: reads convert to FP64 complex,
@@ -137,7 +151,14 @@ struct RunConst {
   double y_grid_min, y_max, y_max_local;
   double length_x, length_y;
   int bc_allspecies[4];
+  int bc_mask;  // BCM_* bits: field bc kinds this run can meet (before and after the window starts)
 };
+
+// Field bc kinds present in a run, so that ghost-cell phases with nothing to
+// do are not launched.
+constexpr int BCM_PERIODIC_X = 1;
+constexpr int BCM_CONDUCT = 2;
+constexpr int BCM_OTHER = 4;  // clamp, simple_laser, simple_outflow, zero_gradient
 
 struct SpeciesPtrs {
   // FP64 form: Cartesian position (m), momentum (kg m/s), weight

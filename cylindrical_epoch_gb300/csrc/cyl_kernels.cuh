@@ -30,6 +30,8 @@ struct GeomTables {
 struct SpeciesCounters {
   int64_t n_used;  // slots in use (live + removed holes)
   int64_t n_dead;  // removed particles still occupying a slot
+  uint32_t wmax_bits;  // mixed form: FP32 bits of the largest weight uploaded or injected
+  uint32_t pad;
 };
 
 // fields.cu (E/B boundary and axis kernels for either storage type)

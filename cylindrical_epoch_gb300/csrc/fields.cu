@@ -3,14 +3,17 @@
 //
 // Bulk updates (update_e_field / update_b_field bulk loops,
 // fields.f90:67-108, 203-241) are grid-wide elementwise kernels over
-// (ix, ir, m), coalesced along x.  Everything that touches only ghost slabs,
-// the axis rows or one boundary column (axis rules fields.f90:116-180,
-// 249-310; efield_bcs / bfield_bcs / bfield_final_bcs boundary.F90:1355-1537;
-// laser.f90:411-690; current_bcs_r_min_final boundary.F90:1909-1959;
-// current_finish current_smooth.F90:29-45) is O(perimeter) work whose
-// sub-steps depend on each other at the domain corners; each such call is one
-// single-CTA kernel whose phases are separated by __syncthreads, in the
-// reference's order.
+// (ix, ir, m), coalesced along x.  The O(perimeter) work -- axis rules
+// (fields.f90:116-180, 249-310), efield_bcs / bfield_bcs / bfield_final_bcs
+// (boundary.F90:1355-1537), the x boundary laser and outflow and the r_max
+// outflow (laser.f90:411-690), current_bcs_r_min_final (boundary.F90:
+// 1909-1959) -- runs as a sequence of multi-CTA launches, one per phase whose
+// work items are independent, in the reference's order (the phases depend on
+// each other at the domain corners).  current_finish (current_smooth.F90:
+// 29-45), which is cheap and only active for periodic or reflecting
+// particle boundaries, stays one single-CTA kernel.
+#include <cstddef>
+
 #include "cyl_common.cuh"
 #include "cyl_kernels.cuh"
 
@@ -71,7 +74,7 @@ __global__ void k_update_b(FView ex, FView er, FView et, FView bx, FView br, FVi
   bt(ix, ir, im) = bt(ix, ir, im) + (-((er0 - erxm) / dx) + (ex0 - exm1) / dy) * 0.5 * dt;
 }
 
-// --------------------------------------------------- single-CTA helpers
+// ----------------------------------------------------- halo (one CTA)
 
 constexpr int CTA_THREADS = 512;
 #define CTA_FOR(var, n) for (int var = threadIdx.x; var < (n); var += blockDim.x)
@@ -98,151 +101,154 @@ __device__ void halo_x(FViewT<T> f, int j0, int j1, const int* bcf, const RunCon
   __syncthreads();
 }
 
-// field_mode_zero_gradient (boundary.F90:654-707) on one boundary
+// ---------------------------------------------------- ghost-cell phases
+//
+// efield_bcs (boundary.F90:1355-1413) and bfield_bcs (boundary.F90:1417-1476)
+// in five phases, each one launch over many CTAs:
+//   PH_HALO       periodic self-wrap in x (boundary.F90:500-593 on one rank)
+//   PH_CONDUCT_X  conducting x boundaries      PH_CONDUCT_Y  conducting r_max
+//   PH_OTHER_X    clamp / laser / outflow / zero-gradient x boundaries
+//   PH_OTHER_Y    the same at r_max
+// with the ghost mirrors of field_mode_clamp_zero (boundary.F90:772-829) and
+// field_mode_zero_gradient (boundary.F90:654-707).  Within a phase every work
+// item writes ghost or boundary cells and reads only cells that no item of
+// the phase writes (nx, ny >= 8), so the items are independent; the phases
+// run in the reference's order.  Copies and sign flips act on the storage
+// type, so they are exact in both forms.
+enum GhostPhase { PH_HALO = 0, PH_CONDUCT_X = 1, PH_CONDUCT_Y = 2, PH_OTHER_X = 3, PH_OTHER_Y = 4 };
+enum GhostKind { GK_NONE = 0, GK_CLAMP = 1, GK_ZERO_GRADIENT = 2 };
+
 template <typename T>
-__device__ void zero_gradient(FViewT<T> f, int st, int bd, const int* bcf, const RunConst& rc) {
-  if (bcf[bd] == CYL_BC_PERIODIC) return;
+__device__ __forceinline__ void gset(FViewT<T> f, int ix, int iy, int m, int kind, int sx, int sy) {
+  T v = *f.ptr(sx, sy, m);
+  if (kind == GK_CLAMP) {
+    v.re = -v.re;
+    v.im = -v.im;
+  }
+  *f.ptr(ix, iy, m) = v;
+}
+template <typename T>
+__device__ __forceinline__ void gzero(FViewT<T> f, int ix, int iy, int m) {
+  T v;
+  v.re = 0;
+  v.im = 0;
+  *f.ptr(ix, iy, m) = v;
+}
+
+// Kind of ghost rule for field st (0..5 = ex er et bx br bt) on boundary bd
+// in phase ph, from the mapped field bc codes.
+__device__ __forceinline__ int ghost_kind(int ph, int st, int bd, const int32_t* bcf) {
+  const int b = bcf[bd];
+  if (b == CYL_BC_PERIODIC) return GK_NONE;
+  if (ph == PH_CONDUCT_X || ph == PH_CONDUCT_Y) {
+    if (b != CYL_BC_CONDUCT) return GK_NONE;
+    // x: ex clamp, er et zero-gradient; bx zero-gradient, br bt clamp.
+    // r_max: ex et zero-gradient, er clamp; bx bt clamp, br zero-gradient.
+    static constexpr int kx[6] = {GK_CLAMP, GK_ZERO_GRADIENT, GK_ZERO_GRADIENT, GK_ZERO_GRADIENT, GK_CLAMP, GK_CLAMP};
+    static constexpr int ky[6] = {GK_ZERO_GRADIENT, GK_CLAMP, GK_ZERO_GRADIENT, GK_CLAMP, GK_ZERO_GRADIENT, GK_CLAMP};
+    return ph == PH_CONDUCT_X ? kx[st] : ky[st];
+  }
+  if (b == CYL_BC_CLAMP || b == CYL_BC_SIMPLE_LASER || b == CYL_BC_SIMPLE_OUTFLOW) return GK_CLAMP;
+  if (b == CYL_BC_ZERO_GRADIENT) return GK_ZERO_GRADIENT;
+  return GK_NONE;
+}
+
+template <typename T>
+struct Triplet {
+  FViewT<T> f[3];
+};
+
+// st0 = 0 for (ex, er, et), 3 for (bx, br, bt)
+template <typename T>
+__global__ void k_ghost_phase(Triplet<T> tr, int st0, int ph, const int32_t* bcp, RunConst rc) {
   const int nx = rc.nx, ny = rc.ny, M = rc.M;
-  if (bd == CYL_BD_X_MIN || bd == CYL_BD_X_MAX) {
-    const int nrow = ny + 2 * NG;
-    CTA_FOR(t, nrow * M) {
-      int j = 1 - NG + t % nrow, m = t / nrow;
-      if (bd == CYL_BD_X_MIN) {
-        if (stag_x(st)) for (int i = 1; i <= NG - 1; ++i) f(i - NG, j, m) = f(NG - i, j, m);
-        else for (int i = 1; i <= NG; ++i) f(i - NG, j, m) = f(NG + 1 - i, j, m);
-      } else {
-        if (stag_x(st)) for (int i = 1; i <= NG - 1; ++i) f(nx + i, j, m) = f(nx - i, j, m);
-        else for (int i = 1; i <= NG; ++i) f(nx + i, j, m) = f(nx + 1 - i, j, m);
-      }
-    }
-  } else if (bd == CYL_BD_Y_MAX) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (ph == PH_CONDUCT_Y || ph == PH_OTHER_Y) {
+    // r_max: items (ix fastest, i = 1..NG, m, q)
     const int ncol = nx + 2 * NG;
-    CTA_FOR(t, ncol * M) {
-      int ix = 1 - NG + t % ncol, m = t / ncol;
-      if (stag_y(st)) for (int i = 1; i <= NG - 1; ++i) f(ix, ny + i, m) = f(ix, ny - i, m);
-      else for (int i = 1; i <= NG; ++i) f(ix, ny + i, m) = f(ix, ny + 1 - i, m);
+    if (t >= (int64_t)ncol * NG * M * 3) return;
+    const int ix = 1 - NG + (int)(t % ncol);
+    int r = (int)(t / ncol);
+    const int i = 1 + r % NG;
+    r /= NG;
+    const int m = r % M, q = r / M;
+    const int st = st0 + q;
+    const int kind = ghost_kind(ph, st, CYL_BD_Y_MAX, bcp);
+    if (kind == GK_NONE) return;
+    const FViewT<T> f = tr.f[q];
+    if (stag_y(st)) {
+      if (i < NG) gset(f, ix, ny + i, m, kind, ix, ny - i);
+      else if (kind == GK_CLAMP) gzero(f, ix, ny, m);
+    } else {
+      gset(f, ix, ny + i, m, kind, ix, ny + 1 - i);
+    }
+    return;
+  }
+  // x boundaries: items (i = 1..NG fastest, row j, m, q, side)
+  const int nrow = ny + 2 * NG;
+  if (t >= (int64_t)2 * 3 * M * nrow * NG) return;
+  const int i = 1 + (int)(t % NG);
+  int r = (int)(t / NG);
+  const int j = 1 - NG + r % nrow;
+  r /= nrow;
+  const int m = r % M;
+  r /= M;
+  const int q = r % 3, side = r / 3;
+  const int st = st0 + q;
+  const int bd = side == 0 ? CYL_BD_X_MIN : CYL_BD_X_MAX;
+  const FViewT<T> f = tr.f[q];
+  if (ph == PH_HALO) {
+    if (bcp[bd] != CYL_BC_PERIODIC) return;
+    // rows 1-ng .. ny+ng, one fewer for r-staggered arrays (boundary.F90:1362-1371)
+    if (j > ny + NG - (stag_y(st) ? 1 : 0)) return;
+    if (side == 1) gset(f, nx + i, j, m, GK_ZERO_GRADIENT, i, j);
+    else gset(f, i - NG, j, m, GK_ZERO_GRADIENT, nx + i - NG, j);
+    return;
+  }
+  const int kind = ghost_kind(ph, st, bd, bcp);
+  if (kind == GK_NONE) return;
+  if (side == 0) {
+    if (stag_x(st)) {
+      if (i < NG) gset(f, i - NG, j, m, kind, NG - i, j);
+      else if (kind == GK_CLAMP) gzero(f, 0, j, m);
+    } else {
+      gset(f, i - NG, j, m, kind, NG + 1 - i, j);
+    }
+  } else {
+    if (stag_x(st)) {
+      if (i < NG) gset(f, nx + i, j, m, kind, nx - i, j);
+      else if (kind == GK_CLAMP) gzero(f, nx, j, m);
+    } else {
+      gset(f, nx + i, j, m, kind, nx + 1 - i, j);
     }
   }
 }
 
-// field_mode_clamp_zero (boundary.F90:772-829) on one boundary
+// Device address of a step record's field bc codes (no host dereference).
+static const int32_t* bc_ptr(const StepRec* rec) {
+  return reinterpret_cast<const int32_t*>(reinterpret_cast<const char*>(rec) + offsetof(StepRec, bc_field));
+}
+
+// Launch the phases of efield_bcs / bfield_bcs (halo_only: bfield_bcs(.TRUE.),
+// the halo exchange alone) that this run's bc kinds can need.
 template <typename T>
-__device__ void clamp_zero(FViewT<T> f, int st, int bd, const int* bcf, const RunConst& rc) {
-  if (bcf[bd] == CYL_BC_PERIODIC) return;
-  const int nx = rc.nx, ny = rc.ny, M = rc.M;
-  const cplx Z = mk(0.0, 0.0);
-  if (bd == CYL_BD_X_MIN || bd == CYL_BD_X_MAX) {
-    const int nrow = ny + 2 * NG;
-    CTA_FOR(t, nrow * M) {
-      int j = 1 - NG + t % nrow, m = t / nrow;
-      if (bd == CYL_BD_X_MIN) {
-        if (stag_x(st)) {
-          for (int i = 1; i <= NG - 1; ++i) f(i - NG, j, m) = -f(NG - i, j, m);
-          f(0, j, m) = Z;
-        } else {
-          for (int i = 1; i <= NG; ++i) f(i - NG, j, m) = -f(NG + 1 - i, j, m);
-        }
-      } else {
-        if (stag_x(st)) {
-          f(nx, j, m) = Z;
-          for (int i = 1; i <= NG - 1; ++i) f(nx + i, j, m) = -f(nx - i, j, m);
-        } else {
-          for (int i = 1; i <= NG; ++i) f(nx + i, j, m) = -f(nx + 1 - i, j, m);
-        }
-      }
-    }
-  } else if (bd == CYL_BD_Y_MAX) {
-    const int ncol = nx + 2 * NG;
-    CTA_FOR(t, ncol * M) {
-      int ix = 1 - NG + t % ncol, m = t / ncol;
-      if (stag_y(st)) {
-        f(ix, ny, m) = Z;
-        for (int i = 1; i <= NG - 1; ++i) f(ix, ny + i, m) = -f(ix, ny - i, m);
-      } else {
-        for (int i = 1; i <= NG; ++i) f(ix, ny + i, m) = -f(ix, ny + 1 - i, m);
-      }
-    }
+static void launch_ghost_bcs(cudaStream_t s, FViewT<T> a, FViewT<T> b, FViewT<T> c, int st0, bool halo_only,
+                             const int32_t* bcp, const RunConst& rc) {
+  const Triplet<T> tr{{a, b, c}};
+  const int nx_items = 2 * 3 * rc.M * (rc.ny + 2 * NG) * NG;
+  const int ny_items = (rc.nx + 2 * NG) * NG * rc.M * 3;
+  const int bx = (nx_items + 255) / 256, by = (ny_items + 255) / 256;
+  if (rc.bc_mask & BCM_PERIODIC_X) k_ghost_phase<T><<<bx, 256, 0, s>>>(tr, st0, PH_HALO, bcp, rc);
+  if (halo_only) return;
+  if (rc.bc_mask & BCM_CONDUCT) {
+    k_ghost_phase<T><<<bx, 256, 0, s>>>(tr, st0, PH_CONDUCT_X, bcp, rc);
+    k_ghost_phase<T><<<by, 256, 0, s>>>(tr, st0, PH_CONDUCT_Y, bcp, rc);
+  }
+  if (rc.bc_mask & BCM_OTHER) {
+    k_ghost_phase<T><<<bx, 256, 0, s>>>(tr, st0, PH_OTHER_X, bcp, rc);
+    k_ghost_phase<T><<<by, 256, 0, s>>>(tr, st0, PH_OTHER_Y, bcp, rc);
   }
 }
-
-// efield_bcs (boundary.F90:1355-1413)
-template <typename T>
-__device__ void efield_bcs_dev(FViewT<T> ex, FViewT<T> er, FViewT<T> et, const int* bcf, const RunConst& rc) {
-  __syncthreads();
-  halo_x(ex, 1 - NG, rc.ny + NG - 1, bcf, rc);
-  halo_x(er, 1 - NG, rc.ny + NG, bcf, rc);
-  halo_x(et, 1 - NG, rc.ny + NG - 1, bcf, rc);
-  for (int i = CYL_BD_X_MIN; i <= CYL_BD_X_MAX; ++i) {
-    if (bcf[i] == CYL_BC_CONDUCT) {
-      clamp_zero(ex, 0, i, bcf, rc);
-      zero_gradient(er, 1, i, bcf, rc);
-      zero_gradient(et, 2, i, bcf, rc);
-    }
-    __syncthreads();
-  }
-  if (bcf[CYL_BD_Y_MAX] == CYL_BC_CONDUCT) {
-    zero_gradient(ex, 0, CYL_BD_Y_MAX, bcf, rc);
-    clamp_zero(er, 1, CYL_BD_Y_MAX, bcf, rc);
-    zero_gradient(et, 2, CYL_BD_Y_MAX, bcf, rc);
-  }
-  __syncthreads();
-  for (int i = 0; i < 4; ++i) {
-    if (i == CYL_BD_Y_MIN) continue;
-    int b = bcf[i];
-    if (b == CYL_BC_CLAMP || b == CYL_BC_SIMPLE_LASER || b == CYL_BC_SIMPLE_OUTFLOW) {
-      clamp_zero(ex, 0, i, bcf, rc);
-      clamp_zero(er, 1, i, bcf, rc);
-      clamp_zero(et, 2, i, bcf, rc);
-    }
-    if (b == CYL_BC_ZERO_GRADIENT) {
-      zero_gradient(ex, 0, i, bcf, rc);
-      zero_gradient(er, 1, i, bcf, rc);
-      zero_gradient(et, 2, i, bcf, rc);
-    }
-    __syncthreads();
-  }
-}
-
-// bfield_bcs (boundary.F90:1417-1476)
-template <typename T>
-__device__ void bfield_bcs_dev(FViewT<T> bx, FViewT<T> br, FViewT<T> bt, bool mpi_only, const int* bcf,
-                               const RunConst& rc) {
-  __syncthreads();
-  halo_x(bx, 1 - NG, rc.ny + NG, bcf, rc);
-  halo_x(br, 1 - NG, rc.ny + NG - 1, bcf, rc);
-  halo_x(bt, 1 - NG, rc.ny + NG, bcf, rc);
-  if (mpi_only) return;
-  for (int i = CYL_BD_X_MIN; i <= CYL_BD_X_MAX; ++i) {
-    if (bcf[i] == CYL_BC_CONDUCT) {
-      zero_gradient(bx, 3, i, bcf, rc);
-      clamp_zero(br, 4, i, bcf, rc);
-      clamp_zero(bt, 5, i, bcf, rc);
-    }
-    __syncthreads();
-  }
-  if (bcf[CYL_BD_Y_MAX] == CYL_BC_CONDUCT) {
-    clamp_zero(bx, 3, CYL_BD_Y_MAX, bcf, rc);
-    zero_gradient(br, 4, CYL_BD_Y_MAX, bcf, rc);
-    clamp_zero(bt, 5, CYL_BD_Y_MAX, bcf, rc);
-  }
-  __syncthreads();
-  for (int i = 0; i < 4; ++i) {
-    if (i == CYL_BD_Y_MIN) continue;
-    int b = bcf[i];
-    if (b == CYL_BC_CLAMP || b == CYL_BC_SIMPLE_LASER || b == CYL_BC_SIMPLE_OUTFLOW) {
-      clamp_zero(bx, 3, i, bcf, rc);
-      clamp_zero(br, 4, i, bcf, rc);
-      clamp_zero(bt, 5, i, bcf, rc);
-    }
-    if (b == CYL_BC_ZERO_GRADIENT) {
-      zero_gradient(bx, 3, i, bcf, rc);
-      zero_gradient(br, 4, i, bcf, rc);
-      zero_gradient(bt, 5, i, bcf, rc);
-    }
-    __syncthreads();
-  }
-}
-
 // Axis rules of update_e_field (fields.f90:116-180), one column per thread.
 template <typename T>
 __device__ void e_axis_dev(FViewT<T> ex, FViewT<T> er, FViewT<T> et, FView jx, FViewT<T> bt, const RunConst& rc, int t0,
@@ -330,184 +336,131 @@ __device__ void b_axis_dev(FViewT<T> bx, FViewT<T> br, FViewT<T> bt, FViewT<T> e
   }
 }
 
-// update_e_field axis rules + efield_bcs (one CTA)
+// Laser source and Mur outflow at the x boundaries (outflow_bcs_x_min /
+// outflow_bcs_x_max, laser.f90:411-633), one thread per (side, ir, m).  src
+// holds this step's Cartesian laser sources (source1, source2 for x_min then
+// x_max, each ny+1 values), which the host evaluates from the deck's time and
+// transverse profiles.  cols: the boundary column arrays, 12 arrays
+// [ex,er,et,bx,br,bt]_x_min then _x_max, each (1-ng:ny+ng, M).  Every read
+// is of a column other than the ones written (columns 0, 1 at x_min and nx
+// at x_max; nx >= 8).
 template <typename T>
-__global__ void __launch_bounds__(CTA_THREADS) k_e_axis_bcs(FViewT<T> ex, FViewT<T> er, FViewT<T> et, FView jx, FViewT<T> bt,
-                             const StepRec* rec, RunConst rc) {
-  __shared__ int bcf[4];
-  if (threadIdx.x < 4) bcf[threadIdx.x] = rec->bc_field[threadIdx.x];
-  __syncthreads();
-  efield_bcs_dev(ex, er, et, bcf, rc);
-}
-
-// update_b_field axis rules + bfield_bcs(.TRUE.) (one CTA)
-template <typename T>
-__global__ void __launch_bounds__(CTA_THREADS) k_b_axis_bcs(FViewT<T> bx, FViewT<T> br, FViewT<T> bt, FViewT<T> ex, FViewT<T> et,
-                             const StepRec* rec, RunConst rc) {
-  __shared__ int bcf[4];
-  if (threadIdx.x < 4) bcf[threadIdx.x] = rec->bc_field[threadIdx.x];
-  __syncthreads();
-  bfield_bcs_dev(bx, br, bt, true, bcf, rc);
-}
-
-// efield_bcs alone (start-up, epoch2d.F90:144)
-template <typename T>
-__global__ void __launch_bounds__(CTA_THREADS) k_efield_bcs(FViewT<T> ex, FViewT<T> er, FViewT<T> et, const StepRec* rec, RunConst rc) {
-  __shared__ int bcf[4];
-  if (threadIdx.x < 4) bcf[threadIdx.x] = rec->bc_field[threadIdx.x];
-  __syncthreads();
-  efield_bcs_dev(ex, er, et, bcf, rc);
-}
-
-// update_b_field axis rules + bfield_final_bcs (boundary.F90:1505-1537),
-// with the x boundary laser / outflow (laser.f90:411-633) and r_max
-// outflow (laser.f90:637-690).  src holds this step's Cartesian laser
-// sources (source1, source2 for x_min then x_max, each ny+1 values), which
-// the host evaluates from the deck's time and transverse profiles.
-template <typename T>
-__global__ void __launch_bounds__(CTA_THREADS) k_b_axis_final_bcs(FieldSetT<T> F, const StepRec* rec, const double* src,
-                                   const cplx* cols, int do_axis, double dt, RunConst rc) {
-  __shared__ int bcf[4];
-  __shared__ int addl[4];
-  if (threadIdx.x < 4) {
-    bcf[threadIdx.x] = rec->bc_field[threadIdx.x];
-    addl[threadIdx.x] = rec->add_laser[threadIdx.x];
-  }
-  __syncthreads();
-  rc.dt = dt;
+__global__ void k_laser_x(FieldSetT<T> F, const StepRec* rec, const double* src, const cplx* cols, double dt,
+                          RunConst rc) {
   const int nx = rc.nx, ny = rc.ny, M = rc.M;
-  bfield_bcs_dev(F.bx, F.br, F.bt, false, bcf, rc);
-  __syncthreads();
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 2 * (ny + 1) * M) return;
+  const int side = t / ((ny + 1) * M);
+  const int ir = t % (ny + 1), m = (t / (ny + 1)) % M;
+  const int bd = side == 0 ? CYL_BD_X_MIN : CYL_BD_X_MAX;
+  if (!(rec->add_laser[bd] || rec->bc_field[bd] == CYL_BC_SIMPLE_OUTFLOW)) return;
   const double c2 = CLIGHT * CLIGHT;
   const double dtc2 = dt * c2, lx = dtc2 / rc.dx, lr = dtc2 / rc.dy;
   const double sum = 1.0 / (lx + CLIGHT), diff = lx - CLIGHT, dt_eps = dt / EPS0;
-  const int ncolv = ny + 2 * NG;  // boundary column arrays are (1-ng:ny+ng, M)
-  for (int side = 0; side < 2; ++side) {
-    const int bd = side == 0 ? CYL_BD_X_MIN : CYL_BD_X_MAX;
-    if (!(addl[bd] || bcf[bd] == CYL_BC_SIMPLE_OUTFLOW)) continue;
-    // cols: 12 arrays [ex,er,et,bx,br,bt]_x_min then _x_max, each ncolv*M
-    const cplx* bxb = cols + (size_t)(side * 6 + 3) * ncolv * M;
-    const cplx* erb = cols + (size_t)(side * 6 + 1) * ncolv * M;
-    const cplx* etb = cols + (size_t)(side * 6 + 2) * ncolv * M;
-    const cplx* brb = cols + (size_t)(side * 6 + 4) * ncolv * M;
-    const cplx* btb = cols + (size_t)(side * 6 + 5) * ncolv * M;
-    const int xc = side == 0 ? 0 : nx;
-    CTA_FOR(t, (ny + 1) * M) {
-      int ir = t % (ny + 1), m = t / (ny + 1);
-      F.bx(xc, ir, m) = bxb[(ir + NG - 1) + ncolv * m];
-    }
-    __syncthreads();
-    const double* s1 = src + (size_t)side * 2 * (ny + 1);
-    const double* s2 = s1 + (ny + 1);
-    CTA_FOR(t, ny * M) {
-      const int ir = 1 + t % ny, m = t / ny;
-      const cplx imc = ((IMAGI * (double)m) * c2) * dt;
-      // Bt row: ir pairs with r_d_vals(ir-1) (whole array inside a 1:ny section)
-      const double rdv = fabs((double)(ir - 2) * rc.dy + rc.y_grid_min);
-      cplx nbt;
-      if (side == 0) {
-        cplx st = mk(0.0, 0.0);
-        if (m == 1) st = s1[ir] + IMAGI * s2[ir];
-        nbt = sum * (((((4.0 * st + 2.0 * (erb[(ir + NG - 1) + ncolv * m] + CLIGHT * btb[(ir + NG - 1) + ncolv * m])) -
-                        2.0 * F.er(1, ir, m)) +
-                       (imc * F.bx(1, ir, m)) / rdv) +
-                      dt_eps * F.jr(1, ir, m)) +
-                     diff * F.bt(2, ir, m));
-      } else {
-        // source_t whole array (0:ny) inside the 1:ny section: index ir-1
-        cplx st = mk(0.0, 0.0);
-        if (m == 1) st = s1[ir - 1] + IMAGI * s2[ir - 1];
-        nbt = sum * ((((((-4.0) * st - 2.0 * (erb[(ir + NG - 1) + ncolv * m] + CLIGHT * btb[(ir + NG - 1) + ncolv * m])) +
-                        2.0 * F.er(nx - 1, ir, m)) -
-                       (imc * F.bx(nx - 1, ir, m)) / rdv) -
-                      dt_eps * F.jr(nx - 1, ir, m)) +
-                     diff * F.bt(nx - 1, ir, m));
-      }
-      cplx nbr = mk(0.0, 0.0);
-      const bool do_br = ir <= ny - 1;
-      if (do_br) {
-        cplx sr = mk(0.0, 0.0);
-        if (m == 1) sr = (-IMAGI) * s1[ir] + s2[ir];
-        if (side == 0) {
-          nbr = sum * (((((((-4.0) * sr - 2.0 * (etb[(ir + NG - 1) + ncolv * m] + CLIGHT * brb[(ir + NG - 1) + ncolv * m])) +
-                           2.0 * F.et(1, ir, m)) -
-                          lr * (F.bx(1, ir + 1, m) - F.bx(1, ir, m))) -
-                         dt_eps * F.jt(1, ir, m)) +
-                        diff * F.br(2, ir, m)));
-        } else {
-          nbr = sum * (((((4.0 * sr + 2.0 * (etb[(ir + NG - 1) + ncolv * m] + CLIGHT * brb[(ir + NG - 1) + ncolv * m])) -
-                          2.0 * F.et(nx - 1, ir, m)) +
-                         lr * (F.bx(nx - 1, ir + 1, m) - F.bx(nx - 1, ir, m))) +
-                        dt_eps * F.jt(nx - 1, ir, m)) +
-                       diff * F.br(nx - 1, ir, m));
-        }
-      }
-      // every read above is of columns other than the one written below
-      if (side == 0) {
-        F.bt(1, ir, m) = nbt;
-        if (do_br) F.br(1, ir, m) = nbr;
-      } else {
-        F.bt(nx, ir, m) = nbt;
-        if (do_br) F.br(nx, ir, m) = nbr;
-      }
-    }
-    __syncthreads();
+  const int ncolv = ny + 2 * NG;
+  const size_t cs = (size_t)ncolv * M;
+  const cplx* erb = cols + (size_t)(side * 6 + 1) * cs;
+  const cplx* etb = cols + (size_t)(side * 6 + 2) * cs;
+  const cplx* bxb = cols + (size_t)(side * 6 + 3) * cs;
+  const cplx* brb = cols + (size_t)(side * 6 + 4) * cs;
+  const cplx* btb = cols + (size_t)(side * 6 + 5) * cs;
+  const size_t cj = (size_t)(ir + NG - 1) + (size_t)ncolv * m;
+  F.bx(side == 0 ? 0 : nx, ir, m) = bxb[cj];
+  if (ir == 0) return;
+  const double* s1 = src + (size_t)side * 2 * (ny + 1);
+  const double* s2 = s1 + (ny + 1);
+  const cplx imc = ((IMAGI * (double)m) * c2) * dt;
+  // Bt row: ir pairs with r_d_vals(ir-1) (whole array inside a 1:ny section)
+  const double rdv = fabs((double)(ir - 2) * rc.dy + rc.y_grid_min);
+  cplx nbt;
+  if (side == 0) {
+    cplx st = mk(0.0, 0.0);
+    if (m == 1) st = s1[ir] + IMAGI * s2[ir];
+    nbt = sum * (((((4.0 * st + 2.0 * (erb[cj] + CLIGHT * btb[cj])) - 2.0 * F.er(1, ir, m)) +
+                   (imc * F.bx(1, ir, m)) / rdv) +
+                  dt_eps * F.jr(1, ir, m)) +
+                 diff * F.bt(2, ir, m));
+  } else {
+    // source_t whole array (0:ny) inside the 1:ny section: index ir-1
+    cplx st = mk(0.0, 0.0);
+    if (m == 1) st = s1[ir - 1] + IMAGI * s2[ir - 1];
+    nbt = sum * ((((((-4.0) * st - 2.0 * (erb[cj] + CLIGHT * btb[cj])) + 2.0 * F.er(nx - 1, ir, m)) -
+                   (imc * F.bx(nx - 1, ir, m)) / rdv) -
+                  dt_eps * F.jr(nx - 1, ir, m)) +
+                 diff * F.bt(nx - 1, ir, m));
   }
-  if (bcf[CYL_BD_Y_MAX] == CYL_BC_SIMPLE_OUTFLOW) {
-    // outflow_bcs_r_max (laser.f90:637-690)
-    const double inv_r = 1.0 / ((double)((float)ny - 1.5f) * rc.dy + rc.y_grid_min);
-    const double dtc2_4r = 0.25 * dtc2 * inv_r;
-    const cplx icdt_2r = ((0.5 * IMAGI) * CLIGHT) * dt * inv_r;
-    const double ly = dtc2 / rc.dy;
-    const double sum_x = 1.0 / (ly + CLIGHT), sum_t = 1.0 / ((ly + CLIGHT) + dtc2_4r);
-    const double dt_2eps = 0.5 * dt / EPS0;
-    // new values depend on row ny-1 and the old arrays only: compute, sync, store
-    const int n = nx * M;
-    for (int base = 0; base < n; base += blockDim.x) {
-      const int t = base + threadIdx.x;
-      cplx nbx = mk(0, 0), nbt = mk(0, 0);
-      int ix = 0, m = 0;
-      if (t < n) {
-        ix = 1 + t % nx;
-        m = t / nx;
-        const cplx icm = icdt_2r * (double)m;
-        if (ix <= nx - 1) {
-          cplx v = (-F.bx(ix, ny - 1, m)) * (CLIGHT - ly);
-          v = v - F.bxo(ix, ny, m) * ((-CLIGHT) + ly);
-          v = v - F.bxo(ix, ny - 1, m) * ((-CLIGHT) - ly);
-          v = v - ((CLIGHT * dt) * inv_r) * F.et(ix, ny - 1, m);
-          v = v + (0.5 * lx) * (((F.br(ix + 1, ny - 1, m) - F.br(ix, ny - 1, m)) + F.bro(ix + 1, ny - 1, m)) -
-                                F.bro(ix, ny - 1, m));
-          v = v - icm * (F.er(ix, ny, m) + F.er(ix, ny - 1, m));
-          v = v - dt_2eps * (F.jt(ix, ny - 1, m) + F.jto(ix, ny - 1, m));
-          nbx = sum_x * v;
-        }
-        cplx v = (-F.bt(ix, ny - 1, m)) * ((CLIGHT - ly) + dtc2_4r);
-        v = v - F.bto(ix, ny, m) * (((-CLIGHT) + ly) + dtc2_4r);
-        v = v - F.bto(ix, ny - 1, m) * (((-CLIGHT) - ly) + dtc2_4r);
-        v = v - ((0.5 * lx) / CLIGHT) * (((F.er(ix, ny, m) + F.er(ix, ny - 1, m)) - F.er(ix - 1, ny, m)) -
-                                         F.er(ix - 1, ny - 1, m));
-        v = v - (icm * CLIGHT) * (F.br(ix, ny - 1, m) + F.bro(ix, ny - 1, m));
-        v = v + dt_2eps * (F.jx(ix, ny - 1, m) + F.jxo(ix, ny - 1, m));
-        nbt = sum_t * v;
-      }
-      if (t < n) {
-        if (ix <= nx - 1) F.bx(ix, ny, m) = nbx;
-        F.bt(ix, ny, m) = nbt;
-      }
-    }
-  } else if (bcf[CYL_BD_Y_MAX] == CYL_BC_ZERO_B) {
-    CTA_FOR(t, (nx + 2 * NG) * M) {
-      int ix = 1 - NG + t % (nx + 2 * NG), m = t / (nx + 2 * NG);
-      F.bx(ix, ny, m) = mk(0, 0);
-      F.br(ix, ny, m) = mk(0, 0);
-      F.bt(ix, ny, m) = mk(0, 0);
+  cplx nbr = mk(0.0, 0.0);
+  const bool do_br = ir <= ny - 1;
+  if (do_br) {
+    cplx sr = mk(0.0, 0.0);
+    if (m == 1) sr = (-IMAGI) * s1[ir] + s2[ir];
+    if (side == 0) {
+      nbr = sum * (((((((-4.0) * sr - 2.0 * (etb[cj] + CLIGHT * brb[cj])) + 2.0 * F.et(1, ir, m)) -
+                      lr * (F.bx(1, ir + 1, m) - F.bx(1, ir, m))) -
+                     dt_eps * F.jt(1, ir, m)) +
+                    diff * F.br(2, ir, m)));
+    } else {
+      nbr = sum * (((((4.0 * sr + 2.0 * (etb[cj] + CLIGHT * brb[cj])) - 2.0 * F.et(nx - 1, ir, m)) +
+                     lr * (F.bx(nx - 1, ir + 1, m) - F.bx(nx - 1, ir, m))) +
+                    dt_eps * F.jt(nx - 1, ir, m)) +
+                   diff * F.br(nx - 1, ir, m));
     }
   }
-  __syncthreads();
-  bfield_bcs_dev(F.bx, F.br, F.bt, true, bcf, rc);
+  if (side == 0) {
+    F.bt(1, ir, m) = nbt;
+    if (do_br) F.br(1, ir, m) = nbr;
+  } else {
+    F.bt(nx, ir, m) = nbt;
+    if (do_br) F.br(nx, ir, m) = nbr;
+  }
 }
 
+// outflow_bcs_r_max (laser.f90:637-690) or zero_b (boundary.F90:1528-1531),
+// one thread per (ix, m).  The new Bx, Bt of row ny depend on row ny-1, row
+// ny of the other arrays and the B_old / J_old arrays only.
+template <typename T>
+__global__ void k_rmax_b(FieldSetT<T> F, const StepRec* rec, double dt, RunConst rc) {
+  const int nx = rc.nx, ny = rc.ny, M = rc.M;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = rec->bc_field[CYL_BD_Y_MAX];
+  if (b == CYL_BC_ZERO_B) {
+    if (t >= (nx + 2 * NG) * M) return;
+    const int ix = 1 - NG + t % (nx + 2 * NG), m = t / (nx + 2 * NG);
+    F.bx(ix, ny, m) = mk(0, 0);
+    F.br(ix, ny, m) = mk(0, 0);
+    F.bt(ix, ny, m) = mk(0, 0);
+    return;
+  }
+  if (b != CYL_BC_SIMPLE_OUTFLOW || t >= nx * M) return;
+  const int ix = 1 + t % nx, m = t / nx;
+  const double dtc2 = dt * CLIGHT * CLIGHT, lx = dtc2 / rc.dx;
+  const double inv_r = 1.0 / ((double)((float)ny - 1.5f) * rc.dy + rc.y_grid_min);
+  const double dtc2_4r = 0.25 * dtc2 * inv_r;
+  const cplx icdt_2r = ((0.5 * IMAGI) * CLIGHT) * dt * inv_r;
+  const double ly = dtc2 / rc.dy;
+  const double sum_x = 1.0 / (ly + CLIGHT), sum_t = 1.0 / ((ly + CLIGHT) + dtc2_4r);
+  const double dt_2eps = 0.5 * dt / EPS0;
+  const cplx icm = icdt_2r * (double)m;
+  if (ix <= nx - 1) {
+    cplx v = (-F.bx(ix, ny - 1, m)) * (CLIGHT - ly);
+    v = v - F.bxo(ix, ny, m) * ((-CLIGHT) + ly);
+    v = v - F.bxo(ix, ny - 1, m) * ((-CLIGHT) - ly);
+    v = v - ((CLIGHT * dt) * inv_r) * F.et(ix, ny - 1, m);
+    v = v + (0.5 * lx) * (((F.br(ix + 1, ny - 1, m) - F.br(ix, ny - 1, m)) + F.bro(ix + 1, ny - 1, m)) -
+                          F.bro(ix, ny - 1, m));
+    v = v - icm * (F.er(ix, ny, m) + F.er(ix, ny - 1, m));
+    v = v - dt_2eps * (F.jt(ix, ny - 1, m) + F.jto(ix, ny - 1, m));
+    F.bx(ix, ny, m) = sum_x * v;
+  }
+  cplx v = (-F.bt(ix, ny - 1, m)) * ((CLIGHT - ly) + dtc2_4r);
+  v = v - F.bto(ix, ny, m) * (((-CLIGHT) + ly) + dtc2_4r);
+  v = v - F.bto(ix, ny - 1, m) * (((-CLIGHT) - ly) + dtc2_4r);
+  v = v - ((0.5 * lx) / CLIGHT) * (((F.er(ix, ny, m) + F.er(ix, ny - 1, m)) - F.er(ix - 1, ny, m)) -
+                                   F.er(ix - 1, ny - 1, m));
+  v = v - (icm * CLIGHT) * (F.br(ix, ny - 1, m) + F.bro(ix, ny - 1, m));
+  v = v + dt_2eps * (F.jx(ix, ny - 1, m) + F.jxo(ix, ny - 1, m));
+  F.bt(ix, ny, m) = sum_t * v;
+}
 // ------------------------------------------------------------- currents
 
 // particle_reflection_bcs_complex (boundary.F90:918-1015) for one side
@@ -711,7 +664,7 @@ __global__ void k_shift_fields(FieldSetT<T> F, const cplx* cols, const StepRec* 
 }
 
 // Axis rules act column by column, so they run on many CTAs (one thread per
-// column); the boundary phases that follow stay in the single-CTA kernels.
+// column).
 template <typename T>
 __global__ void k_e_axis(FViewT<T> ex, FViewT<T> er, FViewT<T> et, FView jx, FViewT<T> bt, RunConst rc) {
   e_axis_dev(ex, er, et, jx, bt, rc, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
@@ -738,22 +691,28 @@ void launch_update_b(cudaStream_t s, const FieldSet& F, int save_old, const RunC
 template <typename T>
 void launch_e_axis_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc) {
   k_e_axis<T><<<axis_blocks(rc), 64, 0, s>>>(F.ex, F.er, F.et, F.jx, F.bt, rc);
-  k_e_axis_bcs<T><<<1, CTA_THREADS, 0, s>>>(F.ex, F.er, F.et, F.jx, F.bt, rec, rc);
+  launch_ghost_bcs<T>(s, F.ex, F.er, F.et, 0, false, bc_ptr(rec), rc);
 }
 template <typename T>
 void launch_efield_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc) {
-  k_efield_bcs<T><<<1, CTA_THREADS, 0, s>>>(F.ex, F.er, F.et, rec, rc);
+  launch_ghost_bcs<T>(s, F.ex, F.er, F.et, 0, false, bc_ptr(rec), rc);
 }
 template <typename T>
 void launch_b_axis_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc) {
   k_b_axis<T><<<axis_blocks(rc), 64, 0, s>>>(F.bx, F.br, F.bt, F.ex, F.et, rc);
-  k_b_axis_bcs<T><<<1, CTA_THREADS, 0, s>>>(F.bx, F.br, F.bt, F.ex, F.et, rec, rc);
+  launch_ghost_bcs<T>(s, F.bx, F.br, F.bt, 3, true, bc_ptr(rec), rc);
 }
+// update_b_field axis rules, then bfield_final_bcs (boundary.F90:1505-1537):
+// bfield_bcs, the x boundary laser / outflow, the r_max outflow or zero_b,
+// and the closing halo exchange (bfield_bcs(.TRUE.)).
 template <typename T>
 void launch_b_final_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const double* src,
                         const cplx* cols, int do_axis, double dt, const RunConst& rc) {
   if (do_axis) k_b_axis<T><<<axis_blocks(rc), 64, 0, s>>>(F.bx, F.br, F.bt, F.ex, F.et, rc);
-  k_b_axis_final_bcs<T><<<1, CTA_THREADS, 0, s>>>(F, rec, src, cols, do_axis, dt, rc);
+  launch_ghost_bcs<T>(s, F.bx, F.br, F.bt, 3, false, bc_ptr(rec), rc);
+  k_laser_x<T><<<(2 * (rc.ny + 1) * rc.M + 127) / 128, 128, 0, s>>>(F, rec, src, cols, dt, rc);
+  k_rmax_b<T><<<((rc.nx + 2 * NG) * rc.M + 127) / 128, 128, 0, s>>>(F, rec, dt, rc);
+  launch_ghost_bcs<T>(s, F.bx, F.br, F.bt, 3, true, bc_ptr(rec), rc);
 }
 template <typename T>
 void launch_current_finish(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc,

@@ -180,11 +180,15 @@ __global__ void k_mixed_append(SpeciesPtrs sp, SpeciesCounters* cnt, const doubl
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err, ERR_CAPACITY);
     return;
   }
+  unsigned wb = 0u;  // bits of the largest |FP32 weight| (positive floats order as integers)
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < k; i += (int64_t)gridDim.x * blockDim.x) {
     const double* q = inject + (off + i) * 8;
     to_mixed(sp, base + i, q[0], q[1], q[2], q[3], q[4], q[5], q[6], xg0, rc);
     sp.id[base + i] = __double_as_longlong(q[7]);
+    wb = max(wb, __float_as_uint(fabsf(sp.fw[base + i])));
   }
+  wb = __reduce_max_sync(0xffffffffu, wb);
+  if ((threadIdx.x & 31) == 0 && wb != 0u) atomicMax(&cnt->wmax_bits, wb);
 }
 __global__ void k_mixed_append_commit(SpeciesPtrs sp, SpeciesCounters* cnt, const StepRec* rec, int isp) {
   const int64_t k = rec->inject_cnt[isp];

@@ -5,18 +5,18 @@
 // Particles: absolute axial cell index (int32) + FP32 offset, y and z in units
 // of dy (FP32), normalised momentum u = p/(m c) (FP32), FP32 weight; E and B
 // are FP32, the currents FP64.  Particles are kept sorted by cell tile
-// (TILE_X x TILE_Y cells).  One CTA works on one tile at a time (persistent
-// loop over a work counter):
+// (TILE_X x TILE_Y cells).  One CTA works on one tile at a time (static
+// round-robin over the tiles):
 //   1. the tile's E and B modes plus a halo are staged in shared memory;
 //   2. each particle is pushed in FP32, gathers from shared memory and adds
-//      its charge fluxes to FP32 shared-memory accumulators;
+//      its charge fluxes to fixed-point (int32) shared-memory accumulators;
 //   3. the accumulators are flushed once into the FP64 global currents; the
 //      per-row geometric factors of the reference (inv_area_rt, inv_area_xt,
 //      inv_volume, particles.F90:189-217) are applied there.
 // The deposit uses the flux form of the reference's recursion: with
 // F = jyh / inv_area_xt(cy) the radial recursion jyh = jyh*ratio - fjy*w_xt
 // (particles.F90:658) becomes F(cy) = F(cy-1) - fc*hy*w_xt, so no geometric
-// factor enters the FP32 sums.  A particle whose stencil leaves the staged
+// factor enters the tile sums.  A particle whose stencil leaves the staged
 // region (it drifted since the last sort) is deferred to a second kernel that
 // gathers from global memory and adds each contribution with an FP64 atomic;
 // so are the particles the moving window appended since the last sort.
@@ -32,6 +32,9 @@ constexpr int RW = TILE_X + 2 * DRIFT + 5;  // staged region width (x)
 constexpr int RH = TILE_Y + 2 * DRIFT + 5;  // staged region height (r)
 constexpr int RCELLS = RW * RH;
 constexpr int PUSH_THREADS = 256;
+#ifndef PUSH_MIN_BLOCKS
+#define PUSH_MIN_BLOCKS 3  // resident CTAs per SM the register budget is sized for
+#endif
 
 struct f2 {
   float re, im;
@@ -80,12 +83,25 @@ __device__ __forceinline__ void mode_factors(float phi, f2 eip, f2& F2, f2& F3, 
 }
 
 // Shared-memory layout: fields [6][M][RCELLS] float2; current accumulators
-// [3][M][re, im][RCELLS] float.
+// [3][M][re, im][hi, lo][RCELLS] int32 (fixed point, see deposit_tile).
 struct Tile {
   const float2* sf;
-  float* sj;
-  int x0, y0;  // Fortran indices of the staged region's first cell
+  int* sj;
+  int x0, y0;       // Fortran indices of the staged region's first cell
+  float s_xr, s_t;  // accumulator units per unit of jx / jr and of jtheta flux
 };
+
+// Fixed-point scales of a tile's current accumulators.  One particle adds at
+// most 16 |q fac| w_max / dt (jx, jr) or 16 |q fac| w_max c (jtheta) to one
+// accumulator value (|partial sums of the weight changes| <= 2, |mode
+// factors| <= 2, 1, 2/3 with the 2 e^{i m theta} prefactor).  That bound is
+// scaled to 2^30 / k, k = max(1, n / 2^16) for a tile of n particles.
+__device__ __forceinline__ void tile_scales(Tile& t, int64_t n, float qw_max, float idt, float c) {
+  const float k = fmaxf(1.0f, (float)n * (1.0f / 65536.0f));
+  const float bxr = 16.0f * qw_max * idt * k, bt = 16.0f * qw_max * c * k;
+  t.s_xr = bxr > 0.f ? 1073741824.0f / bxr : 0.f;
+  t.s_t = bt > 0.f ? 1073741824.0f / bt : 0.f;
+}
 
 template <int M, bool SHARED>
 struct Gather {
@@ -117,6 +133,170 @@ __device__ __forceinline__ void record(const MixedParams& P, int reason, int64_t
 __device__ __forceinline__ void gadd_f(cplx* p, float re, float im) {
   atomicAdd(&p->re, f2d_bits(re));
   if (im != 0.f) atomicAdd(&p->im, f2d_bits(im));
+}
+
+// Per-mode deposit weights of particles.F90:589-665 for one particle: mode
+// factors F2, F3, F4 (with the 2 e^{i m theta0} prefactor for m > 0).
+template <int M>
+struct ModeWalk {
+  f2 eimt = {1.f, 0.f}, eimd = {1.f, 0.f};
+  __device__ __forceinline__ void next(int m, f2 e05, f2 edt, float dth, f2& F2, f2& F3, f2& F4) {
+    F2 = fm(1.f, 0.f);
+    F3 = fm(0.5f, 0.f);
+    F4 = fm(1.0f / 3.0f, 0.f);
+    if (m > 0) {
+      eimt = eimt * e05;
+      eimd = eimd * edt;
+      mode_factors((float)m * dth, eimd, F2, F3, F4);
+      const f2 pre = 2.0f * eimt;
+      F2 = pre * F2;
+      F3 = pre * F3;
+      F4 = pre * F4;
+    }
+  }
+};
+
+// Add one FP32 value v (in accumulator units, |v| <= 2^30) to a hi/lo pair
+// of int32 accumulators: v = hi 2^15 + lo with |hi| <= 2^15, |lo| <= 2^14
+// + 1/2, each rounded to an integer with the 1.5 * 2^23 offset trick (the
+// split itself is exact).  The sums are exact integer sums -- independent of
+// the order of the adds -- and, with at most 2^16 adds per accumulator,
+// cannot overflow.  The error of one add is that of rounding v to FP32 plus
+// at most 1/2 unit.  Integer shared-memory adds are single native
+// instructions (FP32 shared-memory adds are not).
+constexpr float FXP_MAGIC = 12582912.0f;  // 1.5 * 2^23
+constexpr int FXP_MAGIC_BITS = 0x4B400000;
+__device__ __forceinline__ void sadd(int* hi_p, int* lo_p, float v) {
+  const float t = fmaf(v, 1.0f / 32768.0f, FXP_MAGIC);
+  const int hi = __float_as_int(t) - FXP_MAGIC_BITS;
+  const float lo = fmaf(-(t - FXP_MAGIC), 32768.0f, v);
+  const int lo_i = __float_as_int(lo + FXP_MAGIC) - FXP_MAGIC_BITS;
+  if (hi != 0) atomicAdd(hi_p, hi);
+  if (lo_i != 0) atomicAdd(lo_p, lo_i);
+}
+
+// Deposit into the tile accumulators over a W x W window whose first cell is
+// (cx2 + x0, cy2 + y0); x0, y0 in {-2, -1} select the offsets -2..2 of the
+// weight arrays.  The accumulators are fixed-point integers (scale
+// tile.s_xr for jx and jr, tile.s_t for jtheta): integer shared-memory adds
+// are single instructions and their sums do not depend on the order of the
+// adds.
+template <int M, int W>
+__device__ __forceinline__ void deposit_tile(const Tile& tile, const float* og, const float* oh, const float* dgx,
+                                             const float* dgy, int x0, int y0, int cx2, int cy2, float fc,
+                                             float fcz, f2 e05, f2 edt, float dth) {
+  float gxw[W], hxw[W], gyw[W], hyw[W];
+#pragma unroll
+  for (int c = 0; c < W; ++c) {
+    gxw[c] = (x0 == -2) ? og[c] : og[c + 1];
+    hxw[c] = (x0 == -2) ? dgx[c] : dgx[c + 1];
+    gyw[c] = (y0 == -2) ? oh[c] : oh[c + 1];
+    hyw[c] = (y0 == -2) ? dgy[c] : dgy[c + 1];
+  }
+  const float fcs = fc * tile.s_xr, fczs = fcz * tile.s_t;
+  const float third = 1.0f / 3.0f;
+  int* const sj = tile.sj;
+  const int b0 = (cy2 + y0 - tile.y0) * RW + (cx2 + x0 - tile.x0);
+  ModeWalk<M> mw;
+#pragma unroll
+  for (int m = 0; m < M; ++m) {
+    f2 F2, F3, F4;
+    mw.next(m, e05, edt, dth, F2, F3, F4);
+    // [comp][m][re, im][hi, lo][RCELLS]
+    int* const ax = sj + ((0 * M + m) * 4) * RCELLS;
+    int* const ar = sj + ((1 * M + m) * 4) * RCELLS;
+    int* const at = sj + ((2 * M + m) * 4) * RCELLS;
+    f2 qr[W];
+#pragma unroll
+    for (int c = 0; c < W; ++c) qr[c] = fm(0.f, 0.f);
+#pragma unroll
+    for (int r = 0; r < W; ++r) {
+      const float gyv = gyw[r], hyv = hyw[r];
+      f2 w_rt, ym1;
+      if (m == 0) {
+        w_rt = fm(gyv + 0.5f * hyv, 0.f);
+        ym1 = fm(0.5f * gyv + third * hyv, 0.f);
+      } else {
+        w_rt = gyv * F2 + hyv * F3;
+        ym1 = gyv * F3 + hyv * F4;
+      }
+      f2 qx = fm(0.f, 0.f);
+#pragma unroll
+      for (int c = 0; c < W; ++c) {
+        const float gxv = gxw[c], hxv = hxw[c];
+        const f2 w_xt = (m == 0) ? fm(gxv + 0.5f * hxv, 0.f) : (gxv * F2 + hxv * F3);
+        const f2 w_xr = gxv * w_rt + hxv * ym1;
+        qx = qx - (fcs * hxv) * w_rt;
+        qr[c] = qr[c] - (fcs * hyv) * w_xt;
+        const f2 qt = fczs * w_xr;
+        const int cell = b0 + r * RW + c;
+        // The window's last column (jx) and last row (jr) carry the running
+        // flux sum after every weight change of the row (column), which is
+        // zero up to FP32 round-off (old and new weights both sum to 2):
+        // those adds are left out.
+        if (c < W - 1) sadd(ax + cell + 1, ax + RCELLS + cell + 1, qx.re);       // jx at (cx + 1, cy)
+        if (r < W - 1) sadd(ar + cell + RW, ar + RCELLS + cell + RW, qr[c].re);  // jr at (cx, cy + 1)
+        sadd(at + cell, at + RCELLS + cell, qt.re);                              // jtheta at (cx, cy)
+        if (m > 0) {
+          if (c < W - 1) sadd(ax + 2 * RCELLS + cell + 1, ax + 3 * RCELLS + cell + 1, qx.im);
+          if (r < W - 1) sadd(ar + 2 * RCELLS + cell + RW, ar + 3 * RCELLS + cell + RW, qr[c].im);
+          sadd(at + 2 * RCELLS + cell, at + 3 * RCELLS + cell, qt.im);
+        }
+      }
+    }
+  }
+}
+
+// Deposit of a particle on the global path: FP64 atomics into the global
+// currents with the geometric factor of each row, over the reference's
+// xmin..xmax, ymin..ymax range.
+template <int M>
+__device__ __forceinline__ void deposit_global(const FieldSetF& F, const MixedParams& P, const float* og,
+                                               const float* oh, const float* dgx, const float* dgy, int dcx,
+                                               int dcy, int cx2, int cy2, float fc, float fcz, f2 e05, f2 edt,
+                                               float dth) {
+  const int xmin = -1 + (dcx - 1) / 2, xmax = 1 + (dcx + 1) / 2;
+  const int ymin = -1 + (dcy - 1) / 2, ymax = 1 + (dcy + 1) / 2;
+  const float third = 1.0f / 3.0f;
+  ModeWalk<M> mw;
+#pragma unroll
+  for (int m = 0; m < M; ++m) {
+    f2 F2, F3, F4;
+    mw.next(m, e05, edt, dth, F2, F3, F4);
+    f2 qr[5];
+#pragma unroll
+    for (int q = 0; q < 5; ++q) qr[q] = fm(0.f, 0.f);
+    for (int iy = ymin; iy <= ymax; ++iy) {
+      const float gyv = oh[iy + 2], hyv = dgy[iy + 2];
+      f2 w_rt, ym1;
+      if (m == 0) {
+        w_rt = fm(gyv + 0.5f * hyv, 0.f);
+        ym1 = fm(0.5f * gyv + third * hyv, 0.f);
+      } else {
+        w_rt = gyv * F2 + hyv * F3;
+        ym1 = gyv * F3 + hyv * F4;
+      }
+      const int cy = cy2 + iy;
+      const float gx_ = P.g_rt[cy - (1 - JNG)];
+      const float gr_ = P.g_xt[cy - (0 - JNG)];
+      const float gt_ = P.g_vol[cy - (1 - JNG)];
+      f2 qx = fm(0.f, 0.f);
+#pragma unroll
+      for (int ix = -2; ix <= 2; ++ix) {
+        if (ix < xmin || ix > xmax) continue;
+        const float gxv = og[ix + 2], hxv = dgx[ix + 2];
+        const f2 w_xt = (m == 0) ? fm(gxv + 0.5f * hxv, 0.f) : (gxv * F2 + hxv * F3);
+        const f2 w_xr = gxv * w_rt + hxv * ym1;
+        qx = qx - (fc * hxv) * w_rt;
+        qr[ix + 2] = qr[ix + 2] - (fc * hyv) * w_xt;
+        const f2 qt = fcz * w_xr;
+        const int cx = cx2 + ix;
+        gadd_f(F.jx.ptr(cx + 1, cy, m), qx.re * gx_, qx.im * gx_);
+        gadd_f(F.jr.ptr(cx, cy + 1, m), qr[ix + 2].re * gr_, qr[ix + 2].im * gr_);
+        gadd_f(F.jt.ptr(cx, cy, m), qt.re * gt_, qt.im * gt_);
+      }
+    }
+  }
 }
 
 // Push one particle.  Returns false (and leaves the particle untouched) when
@@ -285,80 +465,24 @@ __device__ __forceinline__ bool push_one(int64_t i, const SpeciesPtrs& sp, Speci
       dgy[q] = hny - oh[q];
     }
   }
-  const int xmin = -1 + (dcx - 1) / 2, xmax = 1 + (dcx + 1) / 2;
-  const int ymin = -1 + (dcy - 1) / 2, ymax = 1 + (dcy + 1) / 2;
   const float qwf = P.q_fac * w;  // q w fac
   const float fc = qwf * P.idt;   // fcx = fcy
   const float fcz = qwf * vt;
-  const float third = 1.0f / 3.0f;
   const f2 e05 = fm(ct, st);
   const f2 edt = fm(c3, s3) * fm(ct, -st);
   const float dth = atan2f(z3, y3) - atan2f(z, y);
-  f2 eimt = fm(1.f, 0.f), eimd = fm(1.f, 0.f);
-#pragma unroll
-  for (int m = 0; m < M; ++m) {
-    f2 F2 = fm(1.f, 0.f), F3 = fm(0.5f, 0.f), F4 = fm(third, 0.f);
-    if (m > 0) {
-      eimt = eimt * e05;
-      eimd = eimd * edt;
-      mode_factors((float)m * dth, eimd, F2, F3, F4);
-      const f2 pre = 2.0f * eimt;
-      F2 = pre * F2;
-      F3 = pre * F3;
-      F4 = pre * F4;
-    }
-    f2 qr[5];
-#pragma unroll
-    for (int q = 0; q < 5; ++q) qr[q] = fm(0.f, 0.f);
-#pragma unroll
-    for (int iy = -2; iy <= 2; ++iy) {
-      if (iy < ymin || iy > ymax) continue;
-      const float gyv = oh[iy + 2], hyv = dgy[iy + 2];
-      f2 w_rt, ym1;
-      if (m == 0) {
-        w_rt = fm(gyv + 0.5f * hyv, 0.f);
-        ym1 = fm(0.5f * gyv + third * hyv, 0.f);
-      } else {
-        w_rt = gyv * F2 + hyv * F3;
-        ym1 = gyv * F3 + hyv * F4;
-      }
-      const int cy = cy2 + iy;
-      f2 qx = fm(0.f, 0.f);
-#pragma unroll
-      for (int ix = -2; ix <= 2; ++ix) {
-        if (ix < xmin || ix > xmax) continue;
-        const float gxv = og[ix + 2], hxv = dgx[ix + 2];
-        const f2 w_xt = (m == 0) ? fm(gxv + 0.5f * hxv, 0.f) : (gxv * F2 + hxv * F3);
-        const f2 w_xr = gxv * w_rt + hxv * ym1;
-        qx = qx - (fc * hxv) * w_rt;
-        qr[ix + 2] = qr[ix + 2] - (fc * hyv) * w_xt;
-        const f2 qt = fcz * w_xr;
-        const int cx = cx2 + ix;
-        if (SHARED) {
-          float* base = tile.sj;
-          const int cjx = (cy - tile.y0) * RW + (cx + 1 - tile.x0);
-          const int cjr = (cy + 1 - tile.y0) * RW + (cx - tile.x0);
-          const int cjt = (cy - tile.y0) * RW + (cx - tile.x0);
-          atomicAdd(base + ((0 * M + m) * 2 + 0) * RCELLS + cjx, qx.re);
-          atomicAdd(base + ((1 * M + m) * 2 + 0) * RCELLS + cjr, qr[ix + 2].re);
-          atomicAdd(base + ((2 * M + m) * 2 + 0) * RCELLS + cjt, qt.re);
-          if (m > 0) {
-            atomicAdd(base + ((0 * M + m) * 2 + 1) * RCELLS + cjx, qx.im);
-            atomicAdd(base + ((1 * M + m) * 2 + 1) * RCELLS + cjr, qr[ix + 2].im);
-            atomicAdd(base + ((2 * M + m) * 2 + 1) * RCELLS + cjt, qt.im);
-          }
-        } else {
-          const float gx_ = P.g_rt[cy - (1 - JNG)];
-          const float gr_ = P.g_xt[cy - (0 - JNG)];
-          const float gt_ = P.g_vol[cy - (1 - JNG)];
-          gadd_f(F.jx.ptr(cx + 1, cy, m), qx.re * gx_, qx.im * gx_);
-          gadd_f(F.jr.ptr(cx, cy + 1, m), qr[ix + 2].re * gr_, qr[ix + 2].im * gr_);
-          gadd_f(F.jt.ptr(cx, cy, m), qt.re * gt_, qt.im * gt_);
-        }
-      }
-    }
+  if (SHARED) {
+    // 3 x 3 cells when no lane of the warp changes cell, else a 4 x 4 window
+    // that holds the reference's xmin..xmax, ymin..ymax range (the extra row
+    // or column carries zero flux)
+    if (__all_sync(__activemask(), dcx == 0 && dcy == 0))
+      deposit_tile<M, 3>(tile, og, oh, dgx, dgy, -1, -1, cx2, cy2, fc, fcz, e05, edt, dth);
+    else
+      deposit_tile<M, 4>(tile, og, oh, dgx, dgy, dcx < 0 ? -2 : -1, dcy < 0 ? -2 : -1, cx2, cy2, fc, fcz, e05,
+                         edt, dth);
+  } else {
+    deposit_global<M>(F, P, og, oh, dgx, dgy, dcx, dcy, cx2, cy2, fc, fcz, e05, edt, dth);
   }
-
   // position at t + dt, then particle_bcs in the cell units of this grid
   const int kk = (int)floorf(fxn);
   int knew = k + kk;
@@ -428,13 +552,14 @@ __device__ __forceinline__ void set_bounds(MixedParams& P, const StepRec* rec, c
 }
 
 template <int M>
-__global__ void __launch_bounds__(PUSH_THREADS) k_push_tiles(FieldSetF F, SpeciesPtrs sp, SpeciesCounters* cnt,
+__global__ void __launch_bounds__(PUSH_THREADS, PUSH_MIN_BLOCKS) k_push_tiles(FieldSetF F, SpeciesPtrs sp, SpeciesCounters* cnt,
                                                              const StepRec* rec, RunConst rc, MixedParams P,
                                                              TileTable* tt, int apply_bcs) {
   extern __shared__ float4 smem4[];
   float2* sf = reinterpret_cast<float2*>(smem4);        // 6 * M * RCELLS float2
-  float* sj = reinterpret_cast<float*>(sf + 6 * M * RCELLS);  // 3 * M * 2 * RCELLS float
+  int* sj = reinterpret_cast<int*>(sf + 6 * M * RCELLS);  // 3 * M * 4 * RCELLS int32
   const int nsh = rec->nshift_total;
+  const float qw_max = fabsf(P.q_fac) * __uint_as_float(cnt->wmax_bits);
   set_bounds(P, rec, rc);
   const int ntiles = tt->ntiles;
   const int ntx = tt->ntx;
@@ -447,6 +572,7 @@ __global__ void __launch_bounds__(PUSH_THREADS) k_push_tiles(FieldSetF F, Specie
     tile.sj = sj;
     tile.x0 = (tt->tx_min + t % ntx) * TILE_X - nsh + 1 - DRIFT - 2;
     tile.y0 = (t / ntx) * TILE_Y + 1 - DRIFT - 2;
+    tile_scales(tile, p1 - p0, qw_max, P.idt, P.c);
     const bool inside = tile.x0 >= 1 - NG && tile.x0 + RW - 1 <= rc.nx + NG && tile.y0 >= 1 - NG &&
                         tile.y0 + RH - 1 <= rc.ny + NG;
     if (p1 <= p0) continue;
@@ -467,25 +593,30 @@ __global__ void __launch_bounds__(PUSH_THREADS) k_push_tiles(FieldSetF F, Specie
           sf[(q * M + m) * RCELLS + c] =
               *reinterpret_cast<const float2*>(v.ptr(tile.x0 + c % RW, tile.y0 + c / RW, m));
     }
-    for (int e = threadIdx.x; e < 3 * M * 2 * RCELLS; e += PUSH_THREADS) sj[e] = 0.f;
+    for (int e = threadIdx.x; e < 3 * M * 4 * RCELLS; e += PUSH_THREADS) sj[e] = 0;
     __syncthreads();
     for (int64_t i = p0 + threadIdx.x; i < p1; i += PUSH_THREADS) {
       if (!push_one<M, true>(i, sp, cnt, F, P, rc, tile, nsh, apply_bcs))
         P.fb_list[atomicAdd(P.fb_count, 1)] = (int)i;
     }
     __syncthreads();
-    // flush: one FP64 add per non-zero accumulator, geometric factor per row
+    // flush: one FP64 add per non-zero accumulator, with the geometric
+    // factor of the row and the inverse fixed-point scale
+    const float inv_xr = tile.s_xr > 0.f ? 1.0f / tile.s_xr : 0.f;
+    const float inv_t = tile.s_t > 0.f ? 1.0f / tile.s_t : 0.f;
     for (int e = threadIdx.x; e < 3 * M * RCELLS; e += PUSH_THREADS) {
       const int cell = e % RCELLS, cm = e / RCELLS;
       const int comp = cm / M, m = cm % M;
-      const float vr = sj[(cm * 2 + 0) * RCELLS + cell], vi = sj[(cm * 2 + 1) * RCELLS + cell];
-      if (vr == 0.f && vi == 0.f) continue;
+      const int* a = sj + cm * 4 * RCELLS + cell;
+      const int rh = a[0], rl = a[RCELLS], ih = a[2 * RCELLS], il = a[3 * RCELLS];
+      if ((rh | rl | ih | il) == 0) continue;
+      const float vr = fmaf((float)rh, 32768.0f, (float)rl), vi = fmaf((float)ih, 32768.0f, (float)il);
       const int cx = tile.x0 + cell % RW, cy = tile.y0 + cell / RW;
       float f;
       cplx* dst;
-      if (comp == 0) { f = P.g_rt[cy - (1 - JNG)]; dst = F.jx.ptr(cx, cy, m); }
-      else if (comp == 1) { f = P.g_xt[cy - 1 - (0 - JNG)]; dst = F.jr.ptr(cx, cy, m); }
-      else { f = P.g_vol[cy - (1 - JNG)]; dst = F.jt.ptr(cx, cy, m); }
+      if (comp == 0) { f = P.g_rt[cy - (1 - JNG)] * inv_xr; dst = F.jx.ptr(cx, cy, m); }
+      else if (comp == 1) { f = P.g_xt[cy - 1 - (0 - JNG)] * inv_xr; dst = F.jr.ptr(cx, cy, m); }
+      else { f = P.g_vol[cy - (1 - JNG)] * inv_t; dst = F.jt.ptr(cx, cy, m); }
       gadd_f(dst, vr * f, vi * f);
     }
     __syncthreads();
@@ -503,7 +634,7 @@ __global__ void __launch_bounds__(PUSH_THREADS) k_push_global(FieldSetF F, Speci
   const int64_t nlist = *P.fb_count;
   const int64_t n_sorted = tt->n_sorted, n_used = cnt->n_used;
   const int64_t ntail = n_used > n_sorted ? n_used - n_sorted : 0;
-  Tile none{nullptr, nullptr, 0, 0};
+  Tile none{nullptr, nullptr, 0, 0, 0.f, 0.f};
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nlist + ntail;
        t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = (t < nlist) ? (int64_t)P.fb_list[t] : n_sorted + (t - nlist);
@@ -511,7 +642,7 @@ __global__ void __launch_bounds__(PUSH_THREADS) k_push_global(FieldSetF F, Speci
   }
 }
 
-size_t push_mixed_smem(int M) { return (size_t)6 * M * RCELLS * sizeof(float2) + (size_t)6 * M * RCELLS * sizeof(float); }
+size_t push_mixed_smem(int M) { return (size_t)6 * M * RCELLS * sizeof(float2) + (size_t)12 * M * RCELLS * sizeof(int); }
 
 int push_mixed_blocks_per_sm(int M) {
   const size_t smem = push_mixed_smem(M);

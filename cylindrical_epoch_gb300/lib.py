@@ -43,6 +43,7 @@ SIGNATURES = {
     "cyl_cell_indices": (C.c_int, [H, I32, PI32, PI32, PI64]),
     "cyl_push_only": (C.c_int, [H]),
     "cyl_kernel_timing": (C.c_int, [H, PD, PI64]),
+    "cyl_get_stream": (C.c_int, [H, P(C.c_void_p)]),
     "cyl_rng_init": (None, [P(abi.RngState), I32]),
     "cyl_rng_random": (C.c_double, [P(abi.RngState)]),
     "cyl_rng_box_muller": (C.c_double, [P(abi.RngState), D, D]),

@@ -165,6 +165,12 @@ class Run:
         fn = self.lib.cyl_step_graph if graph else self.lib.cyl_step
         abi.check("cyl_step", fn(self.h, n))
 
+    def stream(self):
+        """The handle's CUDA stream (cudaStream_t as an int)."""
+        st = C.c_void_p()
+        abi.check("cyl_get_stream", self.lib.cyl_get_stream(self.h, C.byref(st)))
+        return st.value or 0
+
     def push_only(self):
         abi.check("cyl_push_only", self.lib.cyl_push_only(self.h))
 

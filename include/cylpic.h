@@ -247,6 +247,11 @@ int cyl_push_only(cyl_handle h);
  * the last call, measured with CUDA events on the launching stream. */
 int cyl_kernel_timing(cyl_handle h, double* push_ms_avg, int64_t* launches);
 
+/* The CUDA stream (a cudaStream_t) every kernel and copy of the handle is
+ * enqueued on, so that a caller can time the steps with its own CUDA events
+ * on that stream.  No counterpart in the reference. */
+int cyl_get_stream(cyl_handle h, void** stream_out);
+
 /* ---- host-side deck helpers (stand in for the Fortran loader) ---------- */
 
 /* KISS generator and polar Box-Muller of random_generator.f90:45-173. */

@@ -49,8 +49,9 @@ def test_mixed_vs_fp64_wakefield(gpu_lib):
     assert sa.n_shifts == sb.n_shifts and sa.n_shifts > 0
     assert abs(sa.n_live[0] - sb.n_live[0]) <= max(2, 1e-4 * sa.n_live[0])
     ea, eb = a.field("exm"), b.field("exm")
-    for m in range(d64.n_mode):
-        e = rel_l2(eb[m], ea[m])
+    errs = [rel_l2(eb[m], ea[m]) for m in range(d64.n_mode)]
+    print("mixed vs fp64 Ez rel L2 per mode:", errs)
+    for m, e in enumerate(errs):
         assert e < TOL_EZ, (m, e)
     da, db = a.diagnostics(), b.diagnostics()
     assert abs(db.kinetic_energy - da.kinetic_energy) <= TOL_EZ * da.kinetic_energy

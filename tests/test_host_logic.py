@@ -1,0 +1,65 @@
+"""Host-side logic of the product library against the oracle (CPU only).
+
+The loader and the KISS stream of libcylpic.so (host code, no GPU needed)
+must reproduce the oracle's loader bit for bit; the decks' time steps follow
+set_dt (setup.F90:629-670) and the values quoted for the benchmark decks.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import cylindrical_epoch_gb300 as cg
+from cylindrical_epoch_gb300 import abi
+
+oracle = pytest.importorskip("oracle.oracle")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from cylindrical_epoch_gb300 import build
+    build.build()
+    return cg.load()
+
+
+@pytest.mark.parametrize("name", ["thermal", "wakefield"])
+def test_product_loader_bit_exact_vs_oracle(lib, name):
+    if name == "thermal":
+        deck = cg.thermal_plasma(nx=32, ny=16, ppc=6)
+    else:
+        deck = cg.wakefield(nx=64, ny=24, ppc=3, density=3.0e24, ramp=1.0e-6)
+    parts, rng = cg.host_load(deck)
+    orc = oracle.Oracle(deck, load_species=True)
+    for i in range(len(deck.species)):
+        a = parts[i].sorted_by_id()
+        b = orc.particles(i).sorted_by_id()
+        assert np.array_equal(a.id, b.id)
+        for k in ("x", "y", "z", "px", "py", "pz", "w"):
+            assert np.array_equal(getattr(a, k), getattr(b, k)), k
+    r = orc.rng_state()
+    for k in ("x", "y", "z", "w", "box_muller_cached"):
+        assert getattr(rng, k) == getattr(r, k), k
+
+
+def test_kiss_stream_matches_oracle(lib):
+    s = abi.RngState()
+    lib.cyl_rng_init(C.byref(s), 7842432)
+    deck = cg.thermal_plasma(nx=16, ny=8, ppc=1)
+    orc = oracle.Oracle(deck)
+    r = orc.rng_state()
+    for k in ("x", "y", "z", "w"):
+        assert getattr(s, k) == getattr(r, k), k
+    v = [lib.cyl_rng_random(C.byref(s)) for _ in range(1000)]
+    assert all(0.0 <= x < 1.0 for x in v)
+    assert abs(np.mean(v) - 0.5) < 0.03
+
+
+def test_deck_time_steps():
+    # thermal plasma: dz = dr = 50 nm, CFL 0.95 -> dt = 0.95 * 0.9 * 50 nm / sqrt(2) / c
+    d1 = cg.thermal_plasma()
+    assert cg.deck.set_dt(d1) == pytest.approx(1.008e-16, rel=2e-3)
+    # wakefield: dz = lambda/32 = 25 nm -> dt ~ 5.04e-17 s
+    d2 = cg.wakefield()
+    assert cg.deck.set_dt(d2) == pytest.approx(5.04e-17, rel=2e-3)
+    # the grid descriptor carries the same value
+    assert d2.grid_desc().dt == cg.deck.set_dt(d2)

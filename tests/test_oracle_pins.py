@@ -1,0 +1,110 @@
+"""Pins of the CPU oracle (test infrastructure) against known answers.
+
+The reference's own test suite holds no golden vectors for this path, and
+the reference (Fortran + MPI) cannot be built here, so the oracle is pinned
+by results that do not come from the oracle itself:
+
+* the analytic current of the reference's documentation, section 7.2 (the
+  example deck example_decks/current_density_test.deck): a uniform electron
+  plasma drifting with p = (-1.23e20, +1.23e20, 0) kg m/s carries
+  J = -e n v, i.e. Jx = +3.40e-6 A/m^2 and Jy = -3.40e-6 A/m^2; in modes,
+  Jx lives on even m only and Jr, Jtheta on odd m only (the documentation's
+  selection rule), with Jr(theta = 0) = Jy;
+* energy conservation of the thermal plasma deck (physics, not a reference
+  output): kinetic + field energy over 200 steps;
+* energy conservation of the vacuum Yee update with conducting walls.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from cylindrical_epoch_gb300 import abi
+from cylindrical_epoch_gb300.deck import CL, M0, Q0, Deck, Species, thermal_plasma
+
+oracle = pytest.importorskip("oracle.oracle")
+
+NG = abi.NG
+
+
+def _current_density_deck(nx=40, ny=24, ppc=64):
+    # the documentation deck's cell sizes (20 um / 500, 5 um / 100), a smaller box
+    dx, dy = 0.04e-6, 0.05e-6
+    e = Species("electron", -Q0, M0, ppc, 1.0e5, drift=(-1.23e20, 1.23e20, 0.0),
+                bc=(abi.BC_SIMPLE_LASER, abi.BC_OPEN, abi.BC_OTHER, abi.BC_OPEN))
+    e.capacity = nx * ny * ppc * 2
+    return Deck("current_density_test", nx, ny, 2, 0.0, nx * dx, ny * dy,
+                (abi.BC_SIMPLE_LASER, abi.BC_OPEN, abi.BC_OTHER, abi.BC_OPEN), [e])
+
+
+def test_documented_current_density_and_mode_selection():
+    deck = _current_density_deck()
+    orc = oracle.Oracle(deck, load_species=True)
+    orc.initialise()
+    orc.step(1)
+    jx, jr, jt = orc.field("jxm"), orc.field("jrm"), orc.field("jtm")
+    # interior: away from the axis, r_max and the x boundaries the plasma streams through
+    sl = (slice(NG + 4, NG + deck.ny - 3), slice(NG + 6, NG + deck.nx - 6))
+    mean = lambda a, m: complex(np.mean(a[m][sl]))
+    p = 1.23e20
+    v = CL * p / math.sqrt(2.0 * p * p + (M0 * CL) ** 2)  # |vx| = |vy|
+    j_ana = Q0 * 1.0e5 * v                                  # 3.40e-6 A/m^2
+    assert abs(j_ana - 3.40e-6) < 0.01e-6
+    # Jx = -e n vx = +j_ana on mode 0
+    assert abs(mean(jx, 0).real - j_ana) < 2e-3 * j_ana
+    # Jr(theta=0) = Jy = -j_ana and Jtheta(theta=pi/2) = -Jy on mode 1
+    # (field = Re sum_m F_m e^{-i m theta})
+    assert abs(mean(jr, 1).real + j_ana) < 2e-2 * j_ana
+    assert abs(mean(jr, 1).imag) < 2e-2 * j_ana
+    assert abs(mean(jt, 1).imag - j_ana) < 2e-2 * j_ana
+    assert abs(mean(jt, 1).real) < 2e-2 * j_ana
+    # selection rule: Jx odd modes and Jr, Jtheta even modes vanish
+    assert abs(mean(jx, 1)) < 5e-2 * j_ana
+    assert abs(mean(jr, 0)) < 5e-2 * j_ana
+    assert abs(mean(jt, 0)) < 5e-2 * j_ana
+
+
+def _total_energy(orc):
+    d = orc.diagnostics()
+    return d.kinetic_energy + d.field_energy_e + d.field_energy_b
+
+
+def test_thermal_plasma_energy_conservation():
+    lib = oracle.load()
+    lib.orc_set_threads(4)
+    try:
+        deck = thermal_plasma(nx=64, ny=32, ppc=16)
+        orc = oracle.Oracle(deck, load_species=True)
+        orc.initialise()
+        e0 = _total_energy(orc)
+        orc.step(200)
+        e1 = _total_energy(orc)
+    finally:
+        lib.orc_set_threads(1)
+    # measured 8.3e-4 for this deck and seed
+    assert abs(e1 - e0) / e0 < 5e-3
+
+
+def test_vacuum_yee_energy():
+    deck = thermal_plasma(nx=64, ny=32, ppc=1)
+    deck.species = []
+    orc = oracle.Oracle(deck)
+    # a smooth pulse in Er/Etheta of mode 1 and Bt of mode 0, zero on the walls
+    x = np.arange(deck.nx + 2 * NG) - NG + 0.5
+    r = np.arange(deck.ny + 2 * NG) - NG + 0.5
+    X, R = np.meshgrid(x, r)
+    env = np.exp(-((X - 32.0) / 6.0) ** 2 - ((R - 12.0) / 4.0) ** 2)
+    f = np.zeros((deck.n_mode, deck.ny + 2 * NG, deck.nx + 2 * NG), dtype=np.complex128)
+    er, et, bt = f.copy(), f.copy(), f.copy()
+    er[1] = 1.0e9 * env
+    et[1] = 1.0e9j * env
+    bt[0] = 2.0 * env
+    orc.set_field("erm", er)
+    orc.set_field("etm", et)
+    orc.set_field("btm", bt)
+    orc.initialise()
+    e0 = _total_energy(orc)
+    orc.step(150)
+    e1 = _total_energy(orc)
+    assert e0 > 0
+    assert abs(e1 - e0) / e0 < 2e-2, (e0, e1)
