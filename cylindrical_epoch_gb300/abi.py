@@ -18,6 +18,8 @@ CYL_ERR_UNSUPPORTED = 5
 CYL_ERR_DEVICE_FLAG = 6
 CYL_ERR_TIMEOUT = 7
 CYL_ERR_OUT_OF_MEMORY = 8
+CYL_ERR_SCRATCH = 9
+NOALLOC_MAX_PARTICLES = 262144  # CYL_NOALLOC_MAX_PARTICLES
 
 ERROR_NAMES = {
     CYL_ERR_BAD_ARG: "bad argument",
@@ -28,6 +30,7 @@ ERROR_NAMES = {
     CYL_ERR_DEVICE_FLAG: "device error flag raised",
     CYL_ERR_TIMEOUT: "timed out waiting for the GPU",
     CYL_ERR_OUT_OF_MEMORY: "device out of memory",
+    CYL_ERR_SCRATCH: "input larger than the fixed scratch (CYL_NOALLOC_MAX_PARTICLES slots)",
 }
 
 BC_PERIODIC = 1

@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "cyl_common.cuh"
@@ -543,6 +544,91 @@ static int run_chunk(Handle* h, int k, bool use_graph) {
   }
   h->timing_pending = k;
   return CYL_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Cell-sort indices without allocation (cyl_cell_indices_noalloc).
+//
+// cyl_cell_indices takes a device scratch of 12 bytes per particle slot from
+// cudaMalloc on every call.  Callers that cannot allocate per call -- a
+// diagnostics hook run between queued steps, where cudaMalloc/cudaFree would
+// synchronise the device and stall the steps behind it, and runs admitted
+// against a fully committed HBM budget, where the allocation could fail --
+// use this fixed scratch instead: a file-scope device array reserved when the
+// library is loaded, 5 int32 words per slot:
+//   [0, N)   cell_x of every slot      [N, 2N)  cell_y      [2N, 3N) live flag
+//   [3N, 4N) compacted cell_x          [4N, 5N) compacted cell_y
+//   [5N]     number of live slots
+// with N = CYL_NOALLOC_MAX_PARTICLES.  Nothing in it needs to start at zero:
+// every word a call reads was written earlier in the same call.  The scratch
+// is shared by every handle of the process, so calls that overlap in time
+// race on it.
+static __device__ __align__(256) int32_t g_cell_scratch[5 * (size_t)CYL_NOALLOC_MAX_PARTICLES + 64];
+
+constexpr int MAX_SCRATCH_DEVICES = 64;
+static int32_t* g_cell_scratch_ptr[MAX_SCRATCH_DEVICES] = {};
+static std::mutex g_cell_scratch_mu;
+
+// Device address of the scratch on the current device, looked up by the first
+// call on each device (the lookup can load the module, so that first call
+// should come before any stream capture).
+static int cell_scratch(int32_t** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return CYL_ERR_CUDA;
+  if (dev < 0 || dev >= MAX_SCRATCH_DEVICES) return CYL_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lock(g_cell_scratch_mu);
+  if (!g_cell_scratch_ptr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_cell_scratch);
+    if (e != cudaSuccess || !p) return CYL_ERR_CUDA;
+    g_cell_scratch_ptr[dev] = static_cast<int32_t*>(p);
+  }
+  *out = g_cell_scratch_ptr[dev];
+  return CYL_OK;
+}
+
+// Order-preserving compaction of the live slots' (cell_x, cell_y) by one CTA
+// of 1024 threads: a block-wide exclusive scan of the live flags per chunk of
+// 1024 slots.  Writes the live count to *count.
+__global__ void __launch_bounds__(1024) k_compact_cells(const int32_t* cx, const int32_t* cy, const int32_t* live,
+                                                        int64_t n, int32_t* ocx, int32_t* ocy, int32_t* count) {
+  __shared__ int warp_sums[32];
+  __shared__ int base_s;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (threadIdx.x == 0) base_s = 0;
+  __syncthreads();
+  for (int64_t c0 = 0; c0 < n; c0 += 1024) {
+    const int64_t i = c0 + threadIdx.x;
+    const int f = (i < n && live[i]) ? 1 : 0;
+    int v = f;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, v, d);
+      if (lane >= d) v += t;
+    }
+    if (lane == 31) warp_sums[w] = v;
+    __syncthreads();
+    if (w == 0) {
+      int s = warp_sums[lane];
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, s, d);
+        if (lane >= d) s += t;
+      }
+      warp_sums[lane] = s;
+    }
+    __syncthreads();
+    const int base = base_s;
+    const int excl = base + (v - f) + (w > 0 ? warp_sums[w - 1] : 0);
+    if (f) {
+      ocx[excl] = cx[i];
+      ocy[excl] = cy[i];
+    }
+    __syncthreads();
+    if (threadIdx.x == 1023) base_s = excl + f;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *count = base_s;
 }
 
 }  // namespace cyl
@@ -1119,6 +1205,47 @@ int cyl_sort_particles(cyl_handle hh) {
   h->copy_pending = true;
   enqueue_sort(h, h->d_rec + CHUNK);
   return sync_and_check(h);
+}
+
+int cyl_cell_indices_noalloc(cyl_handle hh, int32_t isp, int32_t* cx, int32_t* cy, int64_t* n_inout) {
+  if (!hh || !n_inout) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  if (isp < 0 || isp >= h->nsp) return CYL_ERR_BAD_ARG;
+  int32_t* sc = nullptr;
+  if (int r = cell_scratch(&sc)) return r;
+  CK(cudaStreamSynchronize(h->st));
+  SpeciesCounters c;
+  CK(cudaMemcpy(&c, h->d_cnt + isp, sizeof(c), cudaMemcpyDeviceToHost));
+  const int64_t n = c.n_used;
+  if (!cx) {
+    *n_inout = n - c.n_dead;
+    return CYL_OK;
+  }
+  if (n > CYL_NOALLOC_MAX_PARTICLES) return CYL_ERR_SCRATCH;
+  if (n == 0) {
+    *n_inout = 0;
+    return CYL_OK;
+  }
+  const int64_t N = CYL_NOALLOC_MAX_PARTICLES;
+  if (h->prec == CYL_PREC_MIXED)
+    mixed_cell_indices(h->st, h->sp[isp], h->d_cnt + isp, h->xg0, h->g.x_grid_min, h->rc, sc, sc + N, sc + 2 * N,
+                       h->nblocks);
+  else
+    launch_cell_indices(h->st, h->sp[isp], h->d_cnt + isp, h->g.x_grid_min, h->rc, sc, sc + N, sc + 2 * N,
+                        h->nblocks);
+  k_compact_cells<<<1, 1024, 0, h->st>>>(sc, sc + N, sc + 2 * N, n, sc + 3 * N, sc + 4 * N, sc + 5 * N);
+  CK(cudaGetLastError());
+  int32_t k = 0;
+  CK(cudaMemcpyAsync(&k, sc + 5 * N, sizeof(int32_t), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if (k > *n_inout) return CYL_ERR_CAPACITY;
+  if (k > 0) {
+    CK(cudaMemcpyAsync(cx, sc + 3 * N, (size_t)k * sizeof(int32_t), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaMemcpyAsync(cy, sc + 4 * N, (size_t)k * sizeof(int32_t), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  }
+  *n_inout = k;
+  return CYL_OK;
 }
 
 int cyl_cell_indices(cyl_handle hh, int32_t isp, int32_t* cx, int32_t* cy, int64_t* n_inout) {

@@ -48,6 +48,7 @@ extern "C" {
 #define CYL_ERR_DEVICE_FLAG 6    /* a kernel raised its device error word    */
 #define CYL_ERR_TIMEOUT 7        /* a bounded host wait on the GPU ran out   */
 #define CYL_ERR_OUT_OF_MEMORY 8  /* device allocation failed                 */
+#define CYL_ERR_SCRATCH 9        /* input larger than a fixed scratch buffer */
 
 /* ---- boundary codes: the values of constants.F90:56-72 ------------------- */
 #define CYL_BC_PERIODIC 1
@@ -237,6 +238,24 @@ int cyl_sort_particles(cyl_handle h);
  * cell_y = FLOOR((r - y_grid_min_local)/dy + 1.5)  (split_particle.F90:61-62). */
 int cyl_cell_indices(cyl_handle h, int32_t ispecies, int32_t* cell_x,
                      int32_t* cell_y, int64_t* n_inout);
+
+/* Same result and arguments as cyl_cell_indices, computed without any
+ * allocation: no cudaMalloc/cudaFree and no allocating library call, host or
+ * device.  No counterpart in the reference.  It serves callers that cannot
+ * allocate per call -- a diagnostics hook run between queued steps (cudaMalloc
+ * and cudaFree synchronise the device and would stall them) and runs admitted
+ * against a fully committed HBM budget (an allocation could fail).
+ *
+ * The scratch is one fixed device array of CYL_NOALLOC_MAX_PARTICLES slots
+ * (5 int32 words per slot, 5 MiB) reserved when the library is loaded; a
+ * species with more particle slots (live + removed since the last sort) is
+ * rejected with CYL_ERR_SCRATCH.  The first call on a device looks the scratch
+ * up (cudaGetSymbolAddress) and should come before any stream capture.  The
+ * scratch is shared by every handle of the process: calls that overlap in
+ * time race on it. */
+#define CYL_NOALLOC_MAX_PARTICLES 262144
+int cyl_cell_indices_noalloc(cyl_handle h, int32_t ispecies, int32_t* cell_x,
+                             int32_t* cell_y, int64_t* n_inout);
 
 /* Push-and-deposit only (the body of push_particles, particles.F90:163-734,
  * without current_bcs_r_min_final and particle_bcs): used by the parity tests
