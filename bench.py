@@ -163,6 +163,97 @@ def run_reference(args, rank):
     return 0
 
 
+def scan_decks(n, seed=20261204):
+    """The parameter-scan stream: n wakefield decks with nz in {512, 1024, 2048},
+    nr in {64, 128, 256}, modes m = 0..1 or 0..2, a0 ~ U[0.5, 3], density
+    log-uniform in [5e23, 5e24] m^-3, 4-16 particles per cell, 500-2000 steps,
+    mixed precision, and Poisson arrival gaps."""
+    import numpy as np
+    import cylindrical_epoch_gb300 as cg
+    from cylindrical_epoch_gb300 import abi
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        nx = int(rng.choice([512, 1024, 2048]))
+        ny = int(rng.choice([64, 128, 256]))
+        nm = int(rng.choice([2, 3]))
+        a0 = float(rng.uniform(0.5, 3.0))
+        dens = float(10 ** rng.uniform(math.log10(5e23), math.log10(5e24)))
+        ppc = int(rng.integers(4, 17))
+        steps = int(rng.integers(500, 2001))
+        deck = cg.wakefield(nx=nx, ny=ny, n_mode=nm, ppc=ppc, a0=a0, density=dens, precision=abi.PREC_MIXED)
+        deck.seed = 7842432 + k
+        out.append((deck, steps))
+    return out
+
+
+def run_serve(args):
+    """Serving benchmark: a stream of scan decks with Poisson arrivals through
+    the request loop; p50/p99 completion latency and aggregate particle-steps/s,
+    beside the plain FP64 form run one deck at a time on a sample of the decks."""
+    import numpy as np
+    import torch
+    import cylindrical_epoch_gb300 as cg
+    from cylindrical_epoch_gb300 import abi, build, serve
+    build.build()
+    torch.cuda.set_device(0)
+    decks = scan_decks(args.jobs)
+    gaps = np.random.default_rng(7).exponential(args.arrival, size=len(decks))
+    clocks = ClockSampler(0)
+    clocks.start()
+    with serve.Server(0, args.workers) as srv:
+        ids = []
+        t_sub = time.perf_counter()
+        for (deck, steps), gap in zip(decks, gaps):
+            ids.append(srv.submit(deck, steps))
+            time.sleep(float(gap))
+        res = [srv.wait(i, 3600.0) for i in ids]
+    clk = clocks.stop()
+    bad = [r.error for r in res if r.status != abi.JOB_DONE]
+    st = serve.latency_stats(res)
+    # plain FP64 form, one deck at a time, on a sample of the decks (bounded steps)
+    fp64 = []
+    for deck, steps in decks[:args.fp64_sample]:
+        d64 = cg.wakefield(nx=deck.nx, ny=deck.ny, n_mode=deck.n_mode, ppc=int(deck.species[0].npart_per_cell),
+                           density=deck.species[0].density, precision=abi.PREC_FP64)
+        parts, rng = cg.host_load(d64)
+        run = cg.Run(d64, particles=parts, rng=rng)
+        k = min(steps, args.fp64_steps_max)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        run.step(k, graph=True)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        s = run.state()
+        fp64.append(0.5 * (sum(p.n for p in parts) + s.n_live[0]) * k / dt)
+        run.close()
+    fp64_rate = float(np.mean(fp64)) if fp64 else None
+    line = {
+        "metric": "scan p50/p99 completion latency and aggregate particle-steps/s",
+        "value": st["aggregate"], "unit": "particle-steps/s", "n_gpus": 1,
+        "steps": int(sum(s for _, s in decks)), "warmup": 0, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": f"{len(decks)} wakefield scan decks, Poisson arrivals mean {args.arrival} s, "
+                               "nz {512,1024,2048}, nr {64,128,256}, m 0..1|0..2, a0 U[0.5,3], "
+                               "n logU[5e23,5e24], 4-16 ppc, 500-2000 steps, mixed form",
+                   "workers": args.workers, "hbm_budget": "free memory - 2 GiB"},
+        "latency": {"p50_s": st["p50_s"], "p99_s": st["p99_s"], "mean_s": st["mean_s"],
+                    "makespan_s": st["makespan_s"]},
+        "failed_jobs": len(bad),
+        "failed": [{"job": k, "error": int(r.error), "nx": decks[k][0].nx, "ny": decks[k][0].ny,
+                    "n_mode": decks[k][0].n_mode, "ppc": decks[k][0].species[0].npart_per_cell,
+                    "steps_done": int(r.steps_done)}
+                   for k, r in enumerate(res) if r.status != abi.JOB_DONE],
+        "particle_steps": st["particle_steps"],
+        "fp64_one_at_a_time": {"value": fp64_rate, "unit": "particle-steps/s", "sample": len(fp64),
+                               "steps_per_deck_max": args.fp64_steps_max,
+                               "estimated_makespan_s": (st["particle_steps"] / fp64_rate) if fp64_rate else None},
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def _config(args, deck, form):
     return {"workload": f"{deck.name} {deck.nx}x{deck.ny} m=0..{deck.n_mode - 1} "
                         f"{deck.species[0].npart_per_cell:g} ppc, steps [W, W+K) of the deck from t=0",
@@ -185,8 +276,16 @@ def main():
     ap.add_argument("--eager", action="store_true", help="no CUDA graphs")
     ap.add_argument("--fp64-steps", type=int, default=200,
                     help="steps of the plain FP64 form timed beside the mixed form (0: skip)")
+    ap.add_argument("--serve", action="store_true", help="parameter-scan serving benchmark")
+    ap.add_argument("--jobs", type=int, default=64)
+    ap.add_argument("--arrival", type=float, default=0.5, help="mean Poisson arrival gap (s)")
+    ap.add_argument("--workers", type=int, default=4)
+    ap.add_argument("--fp64-sample", type=int, default=3)
+    ap.add_argument("--fp64-steps-max", type=int, default=100)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.serve:
+        return run_serve(args)
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -128,6 +128,33 @@ class Diag(C.Structure):
     ]
 
 
+JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED = 0, 1, 2, 3
+
+
+class JobDesc(C.Structure):
+    _fields_ = [
+        ("grid", GridDesc),
+        ("nspecies", C.c_int32),
+        ("species", SpeciesDesc * 8),
+        ("nlasers", C.c_int32),
+        ("lasers", LaserDesc * 8),
+        ("nsteps", C.c_int64),
+        ("seed", C.c_int32),
+    ]
+
+
+class JobResult(C.Structure):
+    _fields_ = [
+        ("status", C.c_int32), ("error", C.c_int32),
+        ("t_submit", C.c_double), ("t_start", C.c_double), ("t_end", C.c_double),
+        ("steps_done", C.c_int64),
+        ("particle_steps", C.c_double),
+        ("device_bytes", C.c_int64),
+        ("diag", Diag),
+        ("state", RunState),
+    ]
+
+
 class CylError(RuntimeError):
     """Raised when an entry point returns a non-zero status."""
 

@@ -31,6 +31,7 @@ SOURCES = [
     ("fields_fp32.cu", ["--fmad=true"]),
     ("mixed_particles.cu", ["--fmad=true"]),
     ("host_deck.cpp", []),
+    ("server.cpp", []),
 ]
 
 
@@ -45,7 +46,7 @@ def _compile(src, extra, verbose):
     obj = os.path.join(OUT_DIR, src + ".o")
     path = os.path.join(CSRC, src)
     if src.endswith(".cpp"):
-        cmd = [nvcc(), "-x", "c++", "-O2", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
+        cmd = [nvcc(), "-x", "c++", "-O2", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-pthread",
                "-c", path, "-o", obj]
     else:
         cmd = [nvcc()] + ARCH + COMMON + extra + ["-c", path, "-o", obj]
@@ -80,7 +81,7 @@ def build(force=False, verbose=False):
         for (src, _), (_, log) in zip(SOURCES, results):
             sys.stderr.write(f"== {src}\n{log}")
     tmp = LIB + ".tmp"
-    cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
+    cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-Xcompiler", "-pthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

@@ -641,6 +641,39 @@ struct cyl_handle_s {
 
 extern "C" {
 
+int cyl_estimate_device_bytes(const cyl_grid_desc* gd, const cyl_species_desc* spd, int32_t nsp,
+                              int64_t* out) {
+  // the allocations of cyl_create below, from the descriptors alone
+  if (!gd || !out || (nsp > 0 && !spd) || nsp < 0 || nsp > MAX_SPECIES) return CYL_ERR_BAD_ARG;
+  if (gd->nx < 8 || gd->ny < 8 || gd->n_mode < 1 || gd->n_mode > MAX_MODES) return CYL_ERR_BAD_ARG;
+  const int64_t nxg = gd->nx + 2 * NG, nyg = gd->ny + 2 * NG, M = gd->n_mode;
+  const int64_t fcount = nxg * nyg * M;
+  int64_t b = fcount * 16 * (int64_t)sizeof(cplx);                 // 15 mode arrays + work array
+  if (gd->precision == CYL_PREC_MIXED) b += fcount * 9 * (int64_t)sizeof(cplxf);  // FP32 E, B, B_old
+  b += (gd->ny + 2 * NG) * M * 12 * (int64_t)sizeof(cplx);         // boundary columns
+  int64_t maxcap = 1, fbtot = 0, per_step_inj = 0;
+  const double dx = (gd->x_max - gd->x_min) / (double)gd->nx;
+  const double shifts_max = std::floor(gd->dt * std::fabs(gd->window_v_x) / dx) + 1.0;
+  for (int i = 0; i < nsp; ++i) {
+    const int64_t cap = spd[i].capacity > 0 ? spd[i].capacity : 1;
+    b += cap * 8 * (int64_t)sizeof(double);                        // particle SoA
+    maxcap = std::max(maxcap, cap);
+    fbtot += cap + 1;
+    per_step_inj += (int64_t)(shifts_max * (double)gd->ny * (std::floor(spd[i].npart_per_cell) + 1.0));
+  }
+  if (gd->precision == CYL_PREC_MIXED) b += fbtot * (int64_t)sizeof(int);  // deferred lists
+  const int64_t ntiles_max = (gd->nx / TILE_X + 3) * (gd->ny / TILE_Y + 2);
+  b += (ntiles_max + 1) * MAX_SPECIES * 8;
+  const int64_t ncells = nxg * nyg;
+  b += maxcap * (4 + 8 * 8) + (ncells + 2) * 4 + ((ncells + 4096) / 4096 + 64) * 8;  // sort scratch
+  const int64_t inj_cap = gd->move_window ? per_step_inj * CHUNK + 1 : 1;
+  b += inj_cap * 8 * (int64_t)sizeof(double) + (int64_t)4 * (gd->ny + 1) * CHUNK * 8 +
+       (int64_t)sizeof(StepRec) * (CHUNK + 1);
+  b += 1 << 20;  // small tables, counters, allocation granularity
+  *out = b;
+  return CYL_OK;
+}
+
 int cyl_create(const cyl_grid_desc* gd, const cyl_species_desc* spd, int32_t nsp,
                const cyl_laser_desc* las, int32_t nlas, const cyl_rng_state* rng, cyl_handle* out) {
   if (!gd || !out || (nsp > 0 && !spd) || (nlas > 0 && !las)) return CYL_ERR_BAD_ARG;

@@ -249,90 +249,90 @@ static void launch_ghost_bcs(cudaStream_t s, FViewT<T> a, FViewT<T> b, FViewT<T>
     k_ghost_phase<T><<<by, 256, 0, s>>>(tr, st0, PH_OTHER_Y, bcp, rc);
   }
 }
-// Axis rules of update_e_field (fields.f90:116-180), one column per thread.
+// Axis rules of update_e_field (fields.f90:116-180) and update_b_field
+// (fields.f90:249-310).  Per column and mode they are one short sequence on
+// the axis row (task 0) and the r < 0 ghost-row mirrors by mode parity
+// (tasks 1 .. ng-1, ghost row ir = -task).  The mirrors read rows >= 1 (E)
+// or >= 1 (B) that the axis sequence does not write (it writes row 0, and
+// row 1 of Er only for m > 1, which no mirror reads), so every
+// (column, mode, task) is an independent work item.
+// mode_sign of the reference for m >= 2: +1 at m = 2, alternating.
+__device__ __forceinline__ double mode_sign_of(int im) { return ((im - 2) & 1) ? -1.0 : 1.0; }
+
 template <typename T>
-__device__ void e_axis_dev(FViewT<T> ex, FViewT<T> er, FViewT<T> et, FView jx, FViewT<T> bt, const RunConst& rc, int t0,
-                           int tstride) {
-  const int M = rc.M;
+__device__ __forceinline__ void e_axis_item(FViewT<T> ex, FViewT<T> er, FViewT<T> et, FView jx, FViewT<T> bt,
+                                            const RunConst& rc, int ix, int im, int task) {
   const double dy = rc.dy, dt = rc.dt, c2 = CLIGHT * CLIGHT;
-  const int ncol = rc.nx + 2 * NG;
-  for (int t = t0; t < ncol; t += tstride) {
-    const int ix = 1 - NG + t;
-    ex(ix, 0, 0) = ex(ix, 0, 0) + ((4.0 * c2 / dy) * bt(ix, 1, 0) - jx(ix, 0, 0) / EPS0) * 0.5 * dt;
-    et(ix, 0, 0) = mk(0.0, 0.0);
-    er(ix, 0, 0) = -er(ix, 1, 0);
-    for (int ir = 1 - NG; ir <= -1; ++ir) {
-      et(ix, ir, 0) = -et(ix, -ir, 0);
-      er(ix, ir, 0) = -er(ix, -ir + 1, 0);
-      ex(ix, ir, 0) = ex(ix, -ir, 0);
-    }
-    if (M > 1) {
+  if (task == 0) {
+    if (im == 0) {
+      ex(ix, 0, 0) = ex(ix, 0, 0) + ((4.0 * c2 / dy) * bt(ix, 1, 0) - jx(ix, 0, 0) / EPS0) * 0.5 * dt;
+      et(ix, 0, 0) = mk(0.0, 0.0);
+      er(ix, 0, 0) = -er(ix, 1, 0);
+    } else if (im == 1) {
       ex(ix, 0, 1) = mk(0.0, 0.0);
       er(ix, 0, 1) = (2.0 * IMAGI) * et(ix, 0, 1) - er(ix, 1, 1);
       et(ix, 0, 1) = (-IMAGI / 8.0) * (9.0 * er(ix, 1, 1) - er(ix, 2, 1));
-      for (int ir = 1 - NG; ir <= -1; ++ir) {
-        et(ix, ir, 1) = et(ix, -ir, 1);
-        er(ix, ir, 1) = er(ix, -ir + 1, 1);
-        ex(ix, ir, 1) = -ex(ix, -ir, 1);
-      }
-    }
-    double mode_sign = 1.0;
-    for (int im = 2; im < M; ++im) {
+    } else {
       ex(ix, 0, im) = mk(0.0, 0.0);
       et(ix, 0, im) = mk(0.0, 0.0);
       er(ix, 0, im) = -er(ix, 1, im);
       er(ix, 1, im) = er(ix, 2, im) / 9.0;
-      for (int ir = 1 - NG; ir <= -1; ++ir) {
-        et(ix, ir, im) = (-mode_sign) * et(ix, -ir, im);
-        er(ix, ir, im) = (-mode_sign) * er(ix, -ir + 1, im);
-        ex(ix, ir, im) = mode_sign * ex(ix, -ir, im);
-      }
-      mode_sign = -mode_sign;
     }
+    return;
+  }
+  const int ir = -task;
+  if (im == 0) {
+    et(ix, ir, 0) = -et(ix, -ir, 0);
+    er(ix, ir, 0) = -er(ix, -ir + 1, 0);
+    ex(ix, ir, 0) = ex(ix, -ir, 0);
+  } else if (im == 1) {
+    et(ix, ir, 1) = et(ix, -ir, 1);
+    er(ix, ir, 1) = er(ix, -ir + 1, 1);
+    ex(ix, ir, 1) = -ex(ix, -ir, 1);
+  } else {
+    const double ms = mode_sign_of(im);
+    et(ix, ir, im) = (-ms) * et(ix, -ir, im);
+    er(ix, ir, im) = (-ms) * er(ix, -ir + 1, im);
+    ex(ix, ir, im) = ms * ex(ix, -ir, im);
   }
 }
 
-// Axis rules of update_b_field (fields.f90:249-310).
 template <typename T>
-__device__ void b_axis_dev(FViewT<T> bx, FViewT<T> br, FViewT<T> bt, FViewT<T> ex, FViewT<T> et, const RunConst& rc, int t0,
-                           int tstride) {
-  const int M = rc.M;
+__device__ __forceinline__ void b_axis_item(FViewT<T> bx, FViewT<T> br, FViewT<T> bt, FViewT<T> ex, FViewT<T> et,
+                                            const RunConst& rc, int ix, int im, int task) {
   const double dx = rc.dx, dy = rc.dy, dt = rc.dt;
-  const int ncol = rc.nx + 2 * NG;
-  for (int t = t0; t < ncol; t += tstride) {
-    const int ix = 1 - NG + t;
-    br(ix, 0, 0) = mk(0.0, 0.0);
-    bx(ix, 0, 0) = bx(ix, 1, 0);
-    bt(ix, 0, 0) = -bt(ix, 1, 0);
-    for (int ir = 1 - NG; ir <= -1; ++ir) {
-      bt(ix, ir, 0) = -bt(ix, -ir + 1, 0);
-      br(ix, ir, 0) = -br(ix, -ir, 0);
-      bx(ix, ir, 0) = bx(ix, -ir + 1, 0);
-    }
-    if (M > 1) {
+  if (task == 0) {
+    if (im == 0) {
+      br(ix, 0, 0) = mk(0.0, 0.0);
+      bx(ix, 0, 0) = bx(ix, 1, 0);
+      bt(ix, 0, 0) = -bt(ix, 1, 0);
+    } else if (im == 1) {
       bx(ix, 0, 1) = -bx(ix, 1, 1);
       if (ix >= 2 - NG)
         br(ix, 0, 1) = br(ix, 0, 1) +
             ((IMAGI / dy) * ex(ix, 0, 1) + (et(ix, 0, 1) - et(ix - 1, 0, 1)) / dx) * 0.5 * dt;
       bt(ix, 0, 1) = (-2.0 * IMAGI) * br(ix, 0, 1) - bt(ix, 1, 1);
-      for (int ir = 1 - NG; ir <= -1; ++ir) {
-        bt(ix, ir, 1) = bt(ix, -ir + 1, 1);
-        br(ix, ir, 1) = br(ix, -ir, 1);
-        bx(ix, ir, 1) = -bx(ix, -ir + 1, 1);
-      }
-    }
-    double mode_sign = 1.0;
-    for (int im = 2; im < M; ++im) {
+    } else {
       bx(ix, 0, im) = -bx(ix, 1, im);
       br(ix, 0, im) = mk(0.0, 0.0);
       bt(ix, 0, im) = -bt(ix, 1, im);
-      for (int ir = 1 - NG; ir <= -1; ++ir) {
-        bt(ix, ir, im) = (-mode_sign) * bt(ix, -ir + 1, im);
-        br(ix, ir, im) = (-mode_sign) * br(ix, -ir, im);
-        bx(ix, ir, im) = mode_sign * bx(ix, -ir + 1, im);
-      }
-      mode_sign = -mode_sign;
     }
+    return;
+  }
+  const int ir = -task;
+  if (im == 0) {
+    bt(ix, ir, 0) = -bt(ix, -ir + 1, 0);
+    br(ix, ir, 0) = -br(ix, -ir, 0);
+    bx(ix, ir, 0) = bx(ix, -ir + 1, 0);
+  } else if (im == 1) {
+    bt(ix, ir, 1) = bt(ix, -ir + 1, 1);
+    br(ix, ir, 1) = br(ix, -ir, 1);
+    bx(ix, ir, 1) = -bx(ix, -ir + 1, 1);
+  } else {
+    const double ms = mode_sign_of(im);
+    bt(ix, ir, im) = (-ms) * bt(ix, -ir + 1, im);
+    br(ix, ir, im) = (-ms) * br(ix, -ir, im);
+    bx(ix, ir, im) = ms * bx(ix, -ir + 1, im);
   }
 }
 
@@ -506,35 +506,48 @@ __device__ void reflect_side(FView f, int flip, int bd, const RunConst& rc) {
   }
 }
 
-// current_bcs_r_min_final (boundary.F90:1909-1959), per column
-__device__ void j_rmin_dev(FView jx, FView jr, FView jt, const RunConst& rc, int t0, int tstride) {
-  const int ncol = rc.nx + 2 * NG;
-  for (int t = t0; t < ncol; t += tstride) {
-    const int ix = 1 - NG + t;
-    double mode_sign = 1.0;
-    for (int im = 0; im < rc.M; ++im) {
-      for (int j = 2; j <= JNG; ++j) {
-        jx(ix, j - 1, im) = jx(ix, j - 1, im) + mode_sign * jx(ix, 1 - j, im);
-        jr(ix, j, im) = jr(ix, j, im) - mode_sign * jr(ix, 1 - j, im);
-        jt(ix, j - 1, im) = jt(ix, j - 1, im) - mode_sign * jt(ix, 1 - j, im);
-        jx(ix, 1 - j, im) = mk(0, 0);
-        jr(ix, 1 - j, im) = mk(0, 0);
-        jt(ix, 1 - j, im) = mk(0, 0);
-      }
-      jr(ix, 1, im) = jr(ix, 1, im) - mode_sign * jr(ix, 0, im);
-      mode_sign = -mode_sign;
-    }
-    for (int im = 0; im < rc.M; ++im) {
-      if (im > 0) jx(ix, 0, im) = mk(0, 0);
-      else jx(ix, 0, im) = (4.0 * jx(ix, 1, im) - jx(ix, 2, im)) / 3.0;
-      if (im == 1) {
-        jt(ix, 0, im) = ((-IMAGI) * (9.0 * jr(ix, 1, im) - jr(ix, 2, im))) / 8.0;
-        jr(ix, 0, im) = (2.0 * IMAGI) * jt(ix, 0, im) - jr(ix, 1, im);
-      } else {
-        jt(ix, 0, im) = mk(0, 0);
-        jr(ix, 0, im) = -jr(ix, 1, im);
-      }
-    }
+// current_bcs_r_min_final (boundary.F90:1909-1959) for one (column, mode):
+// fold the r < 0 ghost rows of J into rows 1 .. jng-1 with the mode-parity
+// signs, then set the axis row.  The ghost and target rows are read before
+// any is written, so their loads overlap.
+__device__ __forceinline__ void j_rmin_item(FView jx, FView jr, FView jt, int ix, int im) {
+  const double mode_sign = (im & 1) ? -1.0 : 1.0;
+  const cplx Z = mk(0, 0);
+  cplx gx[JNG - 1], gr[JNG - 1], gt[JNG - 1], tx[JNG - 1], tr[JNG - 1], tt[JNG - 1];
+#pragma unroll
+  for (int j = 2; j <= JNG; ++j) {
+    gx[j - 2] = jx(ix, 1 - j, im);
+    gr[j - 2] = jr(ix, 1 - j, im);
+    gt[j - 2] = jt(ix, 1 - j, im);
+    tx[j - 2] = jx(ix, j - 1, im);
+    tr[j - 2] = jr(ix, j, im);
+    tt[j - 2] = jt(ix, j - 1, im);
+  }
+  const cplx r0 = jr(ix, 0, im), r1 = jr(ix, 1, im);
+#pragma unroll
+  for (int j = 2; j <= JNG; ++j) {
+    tx[j - 2] = tx[j - 2] + mode_sign * gx[j - 2];
+    tr[j - 2] = tr[j - 2] - mode_sign * gr[j - 2];
+    tt[j - 2] = tt[j - 2] - mode_sign * gt[j - 2];
+    jx(ix, j - 1, im) = tx[j - 2];
+    jr(ix, j, im) = tr[j - 2];
+    jt(ix, j - 1, im) = tt[j - 2];
+    jx(ix, 1 - j, im) = Z;
+    jr(ix, 1 - j, im) = Z;
+    jt(ix, 1 - j, im) = Z;
+  }
+  const cplx r1n = r1 - mode_sign * r0;
+  jr(ix, 1, im) = r1n;
+  // rows 1 and 2 after the fold: jx(1) = tx[0], jx(2) = tx[1], jr(2) = tr[0]
+  if (im > 0) jx(ix, 0, im) = Z;
+  else jx(ix, 0, im) = (4.0 * tx[0] - tx[1]) / 3.0;
+  if (im == 1) {
+    const cplx t0 = ((-IMAGI) * (9.0 * r1n - tr[0])) / 8.0;
+    jt(ix, 0, im) = t0;
+    jr(ix, 0, im) = (2.0 * IMAGI) * t0 - r1n;
+  } else {
+    jt(ix, 0, im) = Z;
+    jr(ix, 0, im) = -r1n;
   }
 }
 
@@ -663,20 +676,31 @@ __global__ void k_shift_fields(FieldSetT<T> F, const cplx* cols, const StepRec* 
   }
 }
 
-// Axis rules act column by column, so they run on many CTAs (one thread per
-// column).
+// Axis rules and J folding: one thread per independent work item.
 template <typename T>
 __global__ void k_e_axis(FViewT<T> ex, FViewT<T> er, FViewT<T> et, FView jx, FViewT<T> bt, RunConst rc) {
-  e_axis_dev(ex, er, et, jx, bt, rc, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+  const int ncol = rc.nx + 2 * NG;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ncol * rc.M * NG) return;
+  const int ix = 1 - NG + t % ncol, r = t / ncol;
+  e_axis_item(ex, er, et, jx, bt, rc, ix, r % rc.M, r / rc.M);
 }
 template <typename T>
 __global__ void k_b_axis(FViewT<T> bx, FViewT<T> br, FViewT<T> bt, FViewT<T> ex, FViewT<T> et, RunConst rc) {
-  b_axis_dev(bx, br, bt, ex, et, rc, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+  const int ncol = rc.nx + 2 * NG;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ncol * rc.M * NG) return;
+  const int ix = 1 - NG + t % ncol, r = t / ncol;
+  b_axis_item(bx, br, bt, ex, et, rc, ix, r % rc.M, r / rc.M);
 }
 __global__ void k_j_rmin(FView jx, FView jr, FView jt, RunConst rc) {
-  j_rmin_dev(jx, jr, jt, rc, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+  const int ncol = rc.nx + 2 * NG;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ncol * rc.M) return;
+  j_rmin_item(jx, jr, jt, 1 - NG + t % ncol, t / ncol);
 }
-static int axis_blocks(const RunConst& rc) { return (rc.nx + 2 * NG + 63) / 64; }
+static int axis_blocks(const RunConst& rc) { return ((rc.nx + 2 * NG) * rc.M * NG + 127) / 128; }
+static int jrmin_blocks(const RunConst& rc) { return ((rc.nx + 2 * NG) * rc.M + 127) / 128; }
 
 // ------------------------------------------------------------ launchers
 
@@ -690,7 +714,7 @@ void launch_update_b(cudaStream_t s, const FieldSet& F, int save_old, const RunC
 }
 template <typename T>
 void launch_e_axis_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc) {
-  k_e_axis<T><<<axis_blocks(rc), 64, 0, s>>>(F.ex, F.er, F.et, F.jx, F.bt, rc);
+  k_e_axis<T><<<axis_blocks(rc), 128, 0, s>>>(F.ex, F.er, F.et, F.jx, F.bt, rc);
   launch_ghost_bcs<T>(s, F.ex, F.er, F.et, 0, false, bc_ptr(rec), rc);
 }
 template <typename T>
@@ -699,7 +723,7 @@ void launch_efield_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec
 }
 template <typename T>
 void launch_b_axis_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc) {
-  k_b_axis<T><<<axis_blocks(rc), 64, 0, s>>>(F.bx, F.br, F.bt, F.ex, F.et, rc);
+  k_b_axis<T><<<axis_blocks(rc), 128, 0, s>>>(F.bx, F.br, F.bt, F.ex, F.et, rc);
   launch_ghost_bcs<T>(s, F.bx, F.br, F.bt, 3, true, bc_ptr(rec), rc);
 }
 // update_b_field axis rules, then bfield_final_bcs (boundary.F90:1505-1537):
@@ -708,7 +732,7 @@ void launch_b_axis_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec
 template <typename T>
 void launch_b_final_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const double* src,
                         const cplx* cols, int do_axis, double dt, const RunConst& rc) {
-  if (do_axis) k_b_axis<T><<<axis_blocks(rc), 64, 0, s>>>(F.bx, F.br, F.bt, F.ex, F.et, rc);
+  if (do_axis) k_b_axis<T><<<axis_blocks(rc), 128, 0, s>>>(F.bx, F.br, F.bt, F.ex, F.et, rc);
   launch_ghost_bcs<T>(s, F.bx, F.br, F.bt, 3, false, bc_ptr(rec), rc);
   k_laser_x<T><<<(2 * (rc.ny + 1) * rc.M + 127) / 128, 128, 0, s>>>(F, rec, src, cols, dt, rc);
   k_rmax_b<T><<<((rc.nx + 2 * NG) * rc.M + 127) / 128, 128, 0, s>>>(F, rec, dt, rc);
@@ -717,7 +741,7 @@ void launch_b_final_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* re
 template <typename T>
 void launch_current_finish(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc,
                            int smooth, int its, int comp_its, int stride, FView wk) {
-  k_j_rmin<<<axis_blocks(rc), 64, 0, s>>>(F.jx, F.jr, F.jt, rc);
+  k_j_rmin<<<jrmin_blocks(rc), 128, 0, s>>>(F.jx, F.jr, F.jt, rc);
   k_current_finish<<<1, CTA_THREADS, 0, s>>>(F.jx, F.jr, F.jt, rec, rc);
   if (!smooth) return;
   FView js[3] = {F.jx, F.jr, F.jt};

@@ -1,0 +1,273 @@
+// server.cpp -- request loop for parameter scans (cyl_server_* in cylpic.h).
+//
+// A queue of jobs and a pool of worker threads on one GPU.  The head of the
+// queue is admitted when its estimated device memory fits the HBM budget
+// (strict arrival order, so a large job cannot be starved by small ones); a
+// worker then loads the job's species on the host with the reference's
+// loader and KISS stream, creates a handle (its own non-blocking CUDA
+// stream), runs the steps as CUDA graphs of 16 steps, reads the diagnostics
+// and destroys the handle, which returns the job's memory to the budget.
+// Workers run their jobs at the same time, so the kernels of several runs
+// overlap on the device; a new job is admitted as soon as a worker and
+// memory are free (continuous batching of independent runs).
+//
+// The server is host code on top of the public C ABI; it has no counterpart
+// in the reference, which runs one deck per MPI job.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstdint>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/cylpic.h"
+
+namespace {
+
+constexpr int CHUNK_STEPS = 16;
+
+struct Job {
+  int64_t id = 0;
+  cyl_job_desc desc{};
+  std::vector<std::vector<double>> profile, phase;  // owned copies of the laser vectors
+  cyl_job_result res{};
+};
+
+double now_since(const std::chrono::steady_clock::time_point& t0) {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+}  // namespace
+
+struct cyl_server_s {
+  int device = 0;
+  int64_t budget = 0, in_use = 0;
+  int running = 0;
+  bool stop = false;
+  int64_t next_id = 1;
+  std::chrono::steady_clock::time_point t0;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<Job*> queue;
+  std::map<int64_t, std::unique_ptr<Job>> jobs;
+  std::vector<std::thread> workers;
+};
+
+namespace {
+
+// Load, create, initialise, step, read back, destroy.  Returns CYL_OK or the
+// status of the failing call; fills res.diag, res.state, res.steps_done.
+int run_job(cyl_server_s* srv, Job* job) {
+  if (cudaSetDevice(srv->device) != cudaSuccess) return CYL_ERR_CUDA;
+  const cyl_job_desc& d = job->desc;
+  cyl_rng_state rng;
+  cyl_rng_init(&rng, d.seed);
+  // host load of every mobile species (auto_load order, ids continue across species)
+  struct Host {
+    std::vector<double> x, y, z, px, py, pz, w;
+    std::vector<int64_t> id;
+  };
+  std::vector<Host> hp((size_t)d.nspecies);
+  int64_t id_base = 0, n0 = 0;
+  for (int i = 0; i < d.nspecies; ++i) {
+    if (d.species[i].immobile) continue;
+    int64_t n = 0;
+    int r = cyl_host_load_species(&d.grid, &d.species[i], &rng, id_base, nullptr, nullptr, nullptr, nullptr,
+                                  nullptr, nullptr, nullptr, nullptr, &n);
+    if (r != CYL_OK) return r;
+    Host& h = hp[(size_t)i];
+    h.x.resize((size_t)n); h.y.resize((size_t)n); h.z.resize((size_t)n);
+    h.px.resize((size_t)n); h.py.resize((size_t)n); h.pz.resize((size_t)n);
+    h.w.resize((size_t)n); h.id.resize((size_t)n);
+    r = cyl_host_load_species(&d.grid, &d.species[i], &rng, id_base, h.x.data(), h.y.data(), h.z.data(),
+                              h.px.data(), h.py.data(), h.pz.data(), h.w.data(), h.id.data(), &n);
+    if (r != CYL_OK) return r;
+    id_base += n;
+    n0 += n;
+  }
+  cyl_laser_desc las[8];
+  for (int k = 0; k < d.nlasers; ++k) {
+    las[k] = d.lasers[k];
+    las[k].profile = job->profile[(size_t)k].data();
+    las[k].phase = job->phase[(size_t)k].data();
+  }
+  cyl_handle h = nullptr;
+  int r = cyl_create(&d.grid, d.species, d.nspecies, las, d.nlasers, &rng, &h);
+  if (r != CYL_OK) return r;
+  for (int i = 0; i < d.nspecies && r == CYL_OK; ++i) {
+    Host& p = hp[(size_t)i];
+    const int64_t n = (int64_t)p.x.size();
+    if (n == 0) continue;
+    r = cyl_upload_particles(h, i, p.x.data(), p.y.data(), p.z.data(), p.px.data(), p.py.data(), p.pz.data(),
+                             p.w.data(), p.id.data(), n);
+  }
+  hp.clear();
+  if (r == CYL_OK) r = cyl_initialise(h);
+  {
+    std::lock_guard<std::mutex> lock(srv->mu);
+    job->res.t_start = now_since(srv->t0);
+  }
+  int64_t done = 0;
+  while (r == CYL_OK && done < d.nsteps) {
+    const int k = (int)std::min<int64_t>(CHUNK_STEPS, d.nsteps - done);
+    r = cyl_step_graph(h, k);
+    if (r == CYL_OK) done += k;
+    std::lock_guard<std::mutex> lock(srv->mu);
+    job->res.steps_done = done;
+  }
+  if (r == CYL_OK) r = cyl_diagnostics(h, &job->res.diag);
+  if (r == CYL_OK) r = cyl_get_run_state(h, &job->res.state);
+  if (r == CYL_OK) {
+    int64_t n1 = 0;
+    for (int i = 0; i < d.nspecies; ++i)
+      if (!d.species[i].immobile) n1 += job->res.state.n_live[i];
+    job->res.particle_steps = 0.5 * (double)(n0 + n1) * (double)done;
+  }
+  cyl_destroy(h);
+  return r;
+}
+
+void worker_main(cyl_server_s* srv) {
+  for (;;) {
+    Job* job = nullptr;
+    {
+      std::unique_lock<std::mutex> lock(srv->mu);
+      // admit the head of the queue when it fits (or when nothing else holds memory)
+      srv->cv_work.wait(lock, [&] {
+        if (srv->queue.empty()) return srv->stop;
+        const int64_t need = srv->queue.front()->res.device_bytes;
+        return srv->in_use + need <= srv->budget || srv->in_use == 0;
+      });
+      if (srv->queue.empty()) return;
+      job = srv->queue.front();
+      srv->queue.pop_front();
+      srv->in_use += job->res.device_bytes;
+      srv->running += 1;
+      job->res.status = CYL_JOB_RUNNING;
+    }
+    const int r = run_job(srv, job);
+    {
+      std::lock_guard<std::mutex> lock(srv->mu);
+      srv->in_use -= job->res.device_bytes;
+      srv->running -= 1;
+      job->res.error = r;
+      job->res.t_end = now_since(srv->t0);
+      job->res.status = (r == CYL_OK) ? CYL_JOB_DONE : CYL_JOB_FAILED;
+    }
+    srv->cv_work.notify_all();
+    srv->cv_done.notify_all();
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int cyl_server_create(int64_t hbm_budget_bytes, int32_t workers, cyl_server* out) {
+  if (!out || workers < 1 || workers > 64 || hbm_budget_bytes < 0) return CYL_ERR_BAD_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return CYL_ERR_NO_DEVICE;
+  auto* srv = new cyl_server_s();
+  if (cudaGetDevice(&srv->device) != cudaSuccess) {
+    delete srv;
+    return CYL_ERR_CUDA;
+  }
+  if (hbm_budget_bytes == 0) {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+      delete srv;
+      return CYL_ERR_CUDA;
+    }
+    const int64_t reserve = (int64_t)2 << 30;
+    hbm_budget_bytes = std::max<int64_t>((int64_t)free_b - reserve, (int64_t)free_b / 2);
+  }
+  srv->budget = hbm_budget_bytes;
+  srv->t0 = std::chrono::steady_clock::now();
+  for (int i = 0; i < workers; ++i) srv->workers.emplace_back(worker_main, srv);
+  *out = srv;
+  return CYL_OK;
+}
+
+int cyl_server_submit(cyl_server s, const cyl_job_desc* job, int64_t* job_id) {
+  if (!s || !job || !job_id) return CYL_ERR_BAD_ARG;
+  if (job->nspecies < 0 || job->nspecies > 8 || job->nlasers < 0 || job->nlasers > 8 || job->nsteps < 0)
+    return CYL_ERR_BAD_ARG;
+  int64_t bytes = 0;
+  int r = cyl_estimate_device_bytes(&job->grid, job->species, job->nspecies, &bytes);
+  if (r != CYL_OK) return r;
+  auto j = std::make_unique<Job>();
+  j->desc = *job;
+  const size_t nprof = (size_t)job->grid.ny + 1;
+  for (int k = 0; k < job->nlasers; ++k) {
+    if (!job->lasers[k].profile || !job->lasers[k].phase) return CYL_ERR_BAD_ARG;
+    j->profile.emplace_back(job->lasers[k].profile, job->lasers[k].profile + nprof);
+    j->phase.emplace_back(job->lasers[k].phase, job->lasers[k].phase + nprof);
+    j->desc.lasers[k].profile = nullptr;
+    j->desc.lasers[k].phase = nullptr;
+  }
+  std::lock_guard<std::mutex> lock(s->mu);
+  if (s->stop) return CYL_ERR_BAD_ARG;
+  if (bytes > s->budget) return CYL_ERR_OUT_OF_MEMORY;
+  j->id = s->next_id++;
+  j->res.status = CYL_JOB_QUEUED;
+  j->res.error = CYL_OK;
+  j->res.device_bytes = bytes;
+  j->res.t_submit = now_since(s->t0);
+  *job_id = j->id;
+  s->queue.push_back(j.get());
+  s->jobs.emplace(j->id, std::move(j));
+  s->cv_work.notify_all();
+  return CYL_OK;
+}
+
+int cyl_server_poll(cyl_server s, int64_t job_id, cyl_job_result* out) {
+  if (!s || !out) return CYL_ERR_BAD_ARG;
+  std::lock_guard<std::mutex> lock(s->mu);
+  auto it = s->jobs.find(job_id);
+  if (it == s->jobs.end()) return CYL_ERR_BAD_ARG;
+  *out = it->second->res;
+  return CYL_OK;
+}
+
+int cyl_server_wait(cyl_server s, int64_t job_id, double timeout_s, cyl_job_result* out) {
+  if (!s || !out || !(timeout_s >= 0.0)) return CYL_ERR_BAD_ARG;
+  std::unique_lock<std::mutex> lock(s->mu);
+  auto it = s->jobs.find(job_id);
+  if (it == s->jobs.end()) return CYL_ERR_BAD_ARG;
+  Job* j = it->second.get();
+  const bool ok = s->cv_done.wait_for(lock, std::chrono::duration<double>(timeout_s), [&] {
+    return j->res.status == CYL_JOB_DONE || j->res.status == CYL_JOB_FAILED;
+  });
+  *out = j->res;
+  return ok ? CYL_OK : CYL_ERR_TIMEOUT;
+}
+
+int cyl_server_stats(cyl_server s, int32_t* queued, int32_t* running, int64_t* bytes_in_use) {
+  if (!s) return CYL_ERR_BAD_ARG;
+  std::lock_guard<std::mutex> lock(s->mu);
+  if (queued) *queued = (int32_t)s->queue.size();
+  if (running) *running = s->running;
+  if (bytes_in_use) *bytes_in_use = s->in_use;
+  return CYL_OK;
+}
+
+int cyl_server_destroy(cyl_server s) {
+  if (!s) return CYL_ERR_BAD_ARG;
+  {
+    std::lock_guard<std::mutex> lock(s->mu);
+    s->stop = true;
+  }
+  s->cv_work.notify_all();
+  for (auto& t : s->workers) t.join();
+  delete s;
+  return CYL_OK;
+}
+
+}  // extern "C"

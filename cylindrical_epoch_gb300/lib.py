@@ -45,6 +45,13 @@ SIGNATURES = {
     "cyl_push_only": (C.c_int, [H]),
     "cyl_kernel_timing": (C.c_int, [H, PD, PI64]),
     "cyl_get_stream": (C.c_int, [H, P(C.c_void_p)]),
+    "cyl_estimate_device_bytes": (C.c_int, [P(abi.GridDesc), P(abi.SpeciesDesc), I32, PI64]),
+    "cyl_server_create": (C.c_int, [I64, I32, P(H)]),
+    "cyl_server_submit": (C.c_int, [H, P(abi.JobDesc), PI64]),
+    "cyl_server_poll": (C.c_int, [H, I64, P(abi.JobResult)]),
+    "cyl_server_wait": (C.c_int, [H, I64, D, P(abi.JobResult)]),
+    "cyl_server_stats": (C.c_int, [H, PI32, PI32, PI64]),
+    "cyl_server_destroy": (C.c_int, [H]),
     "cyl_rng_init": (None, [P(abi.RngState), I32]),
     "cyl_rng_random": (C.c_double, [P(abi.RngState)]),
     "cyl_rng_box_muller": (C.c_double, [P(abi.RngState), D, D]),

@@ -271,6 +271,65 @@ int cyl_kernel_timing(cyl_handle h, double* push_ms_avg, int64_t* launches);
  * on that stream.  No counterpart in the reference. */
 int cyl_get_stream(cyl_handle h, void** stream_out);
 
+/* Device bytes cyl_create would allocate for these descriptors (an upper
+ * bound; used for admission against an HBM budget).  Host only. */
+int cyl_estimate_device_bytes(const cyl_grid_desc* grid, const cyl_species_desc* species,
+                              int32_t nspecies, int64_t* out);
+
+/* ---- serving: a request loop for parameter scans ----------------------
+ * No counterpart in the reference (one deck per MPI job there).  A server
+ * owns a queue of runs (jobs) and a pool of worker threads on one GPU.  Jobs
+ * are admitted in arrival order while their estimated device memory fits the
+ * HBM budget; each admitted job loads its species on the host (the
+ * reference's loader and KISS stream, seeded per job), creates a handle on
+ * its own CUDA stream, runs its steps as CUDA graphs of 16 steps and is
+ * retired (its device memory freed) when done, so runs of uneven size
+ * overlap on the device.  Results stay readable until the server is
+ * destroyed. */
+#define CYL_JOB_QUEUED 0
+#define CYL_JOB_RUNNING 1
+#define CYL_JOB_DONE 2
+#define CYL_JOB_FAILED 3
+
+typedef struct cyl_job_desc {
+  cyl_grid_desc grid;
+  int32_t nspecies;
+  cyl_species_desc species[8];
+  int32_t nlasers;
+  cyl_laser_desc lasers[8];      /* profile / phase are copied at submit   */
+  int64_t nsteps;
+  int32_t seed;                  /* KISS seed of the loader (7842432 + rank in the reference) */
+} cyl_job_desc;
+
+typedef struct cyl_job_result {
+  int32_t status;                /* CYL_JOB_*                               */
+  int32_t error;                 /* CYL_OK or the failing call's status     */
+  double t_submit, t_start, t_end;  /* seconds since the server was created */
+  int64_t steps_done;
+  double particle_steps;         /* mean live mobile particles x steps      */
+  int64_t device_bytes;          /* estimate charged to the budget          */
+  cyl_diag diag;                 /* diagnostics after the last step         */
+  cyl_run_state state;
+} cyl_job_result;
+
+typedef struct cyl_server_s* cyl_server;
+
+/* hbm_budget_bytes: device memory the jobs may hold together (0: the free
+ * memory of the device at creation, minus 2 GiB); workers: jobs run at the
+ * same time (>= 1). */
+int cyl_server_create(int64_t hbm_budget_bytes, int32_t workers, cyl_server* out);
+/* Queue a job; CYL_ERR_OUT_OF_MEMORY if it alone exceeds the budget. */
+int cyl_server_submit(cyl_server s, const cyl_job_desc* job, int64_t* job_id);
+/* Current state of a job (non-blocking). */
+int cyl_server_poll(cyl_server s, int64_t job_id, cyl_job_result* out);
+/* Wait until the job is done or failed, at most timeout_s seconds
+ * (CYL_ERR_TIMEOUT when the wait runs out). */
+int cyl_server_wait(cyl_server s, int64_t job_id, double timeout_s, cyl_job_result* out);
+/* Jobs queued, running, and device bytes currently charged. */
+int cyl_server_stats(cyl_server s, int32_t* queued, int32_t* running, int64_t* bytes_in_use);
+/* Finish the running and queued jobs, join the workers, free everything. */
+int cyl_server_destroy(cyl_server s);
+
 /* ---- host-side deck helpers (stand in for the Fortran loader) ---------- */
 
 /* KISS generator and polar Box-Muller of random_generator.f90:45-173. */

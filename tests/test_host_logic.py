@@ -63,3 +63,25 @@ def test_deck_time_steps():
     assert cg.deck.set_dt(d2) == pytest.approx(5.04e-17, rel=2e-3)
     # the grid descriptor carries the same value
     assert d2.grid_desc().dt == cg.deck.set_dt(d2)
+
+
+def test_device_estimate_grows_with_the_run(lib):
+    from cylindrical_epoch_gb300 import serve
+    small = serve.estimate_bytes(cg.wakefield(nx=256, ny=64, ppc=2))
+    wide = serve.estimate_bytes(cg.wakefield(nx=512, ny=64, ppc=2))
+    dense = serve.estimate_bytes(cg.wakefield(nx=256, ny=64, ppc=8))
+    mixed = serve.estimate_bytes(cg.wakefield(nx=256, ny=64, ppc=2, precision=abi.PREC_MIXED))
+    assert small < wide and small < dense and small < mixed
+    # C2: 15 FP64 mode arrays of 2058 x 266 x 2 complex plus 4.6 M particle slots
+    c2 = serve.estimate_bytes(cg.wakefield())
+    assert 0.6e9 < c2 < 1.5e9
+
+
+def test_server_without_device_reports_status(lib):
+    from cylindrical_epoch_gb300 import serve
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(abi.CylError) as e:
+        serve.Server(0, 2)
+    assert e.value.code == abi.CYL_ERR_NO_DEVICE
