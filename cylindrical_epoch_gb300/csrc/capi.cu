@@ -760,28 +760,36 @@ int cyl_create(const cyl_grid_desc* gd, const cyl_species_desc* spd, int32_t nsp
     delete hs;
     return CYL_ERR_CUDA;
   }
+  // first failing CUDA call of the set-up (its code is checked at the end)
+  cudaError_t first_err = cudaSuccess;
+  auto ok = [&first_err](cudaError_t e) {
+    if (e != cudaSuccess && first_err == cudaSuccess) first_err = e;
+  };
   int nsm = 152;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device);
   h->nblocks = nsm * 8;
-  cudaMalloc(&h->d_err, sizeof(int));
-  cudaMemset(h->d_err, 0, sizeof(int));
-  cudaMalloc(&h->d_dbg, 16 * sizeof(float));
-  cudaMemset(h->d_dbg, 0, 16 * sizeof(float));
+  ok(cudaMalloc(&h->d_err, sizeof(int)));
+  ok(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->st));
+  ok(cudaMalloc(&h->d_dbg, 16 * sizeof(float)));
+  ok(cudaMemsetAsync(h->d_dbg, 0, 16 * sizeof(float), h->st));
   // fields: 15 arrays + one work array, one allocation
   h->fcount = (size_t)rc.nxg * rc.nyg * rc.M;
   if (cudaMalloc(&h->fbuf, h->fcount * 16 * sizeof(cplx)) != cudaSuccess) {
     cyl_destroy((cyl_handle)hs);
     return CYL_ERR_OUT_OF_MEMORY;
   }
-  cudaMemset(h->fbuf, 0, h->fcount * 16 * sizeof(cplx));
+  ok(cudaMemsetAsync(h->fbuf, 0, h->fcount * 16 * sizeof(cplx), h->st));
   for (int k = 0; k < 16; ++k) h->F[k] = h->fbuf + h->fcount * k;
   const size_t ncolv = (size_t)(rc.ny + 2 * NG) * rc.M;
-  cudaMalloc(&h->cols, ncolv * 12 * sizeof(cplx));
-  cudaMemset(h->cols, 0, ncolv * 12 * sizeof(cplx));
+  ok(cudaMalloc(&h->cols, ncolv * 12 * sizeof(cplx)));
+  ok(cudaMemsetAsync(h->cols, 0, ncolv * 12 * sizeof(cplx), h->st));
+  // host sources of the set-up copies, alive until the stream is synchronised
   std::vector<double> geo;
+  std::vector<float4> rt;
+  std::vector<float> gf;
   make_geom(h->g, geo);
-  cudaMalloc(&h->geom_buf, geo.size() * sizeof(double));
-  cudaMemcpy(h->geom_buf, geo.data(), geo.size() * sizeof(double), cudaMemcpyHostToDevice);
+  ok(cudaMalloc(&h->geom_buf, geo.size() * sizeof(double)));
+  ok(cudaMemcpyAsync(h->geom_buf, geo.data(), geo.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));
   {
     const int n1 = rc.ny + 2 * JNG, n0 = n1 + 1;
     h->geom.inv_area_rt = h->geom_buf;
@@ -795,22 +803,22 @@ int cyl_create(const cyl_grid_desc* gd, const cyl_species_desc* spd, int32_t nsp
       cyl_destroy((cyl_handle)hs);
       return CYL_ERR_OUT_OF_MEMORY;
     }
-    cudaMemset(h->ffbuf, 0, h->fcount * 9 * sizeof(cplxf));
+    ok(cudaMemsetAsync(h->ffbuf, 0, h->fcount * 9 * sizeof(cplxf), h->st));
     for (int k = 0; k < 9; ++k) h->Ff[k] = h->ffbuf + h->fcount * k;
     // per-row Yee coefficients: c^2/r_p dt/2, c^2/r_d dt/2, dt/2/r_d, dt/2/r_p
-    std::vector<float4> rt(rc.ny + 2);
+    rt.resize(rc.ny + 2);
     for (int ir = 0; ir <= rc.ny + 1; ++ir) {
       const double r_d = std::fabs((double)(ir - 1) * rc.dy + rc.y_grid_min);
       const double r_p = r_d + 0.5 * rc.dy;
       const double hh2 = 0.5 * rc.dt, c2 = CLIGHT * CLIGHT;
       rt[ir] = make_float4((float)(c2 / r_p * hh2), (float)(c2 / r_d * hh2), (float)(hh2 / r_d), (float)(hh2 / r_p));
     }
-    cudaMalloc(&h->rowtab, rt.size() * sizeof(float4));
-    cudaMemcpy(h->rowtab, rt.data(), rt.size() * sizeof(float4), cudaMemcpyHostToDevice);
-    std::vector<float> gf(geo.size());
+    ok(cudaMalloc(&h->rowtab, rt.size() * sizeof(float4)));
+    ok(cudaMemcpyAsync(h->rowtab, rt.data(), rt.size() * sizeof(float4), cudaMemcpyHostToDevice, h->st));
+    gf.resize(geo.size());
     for (size_t k = 0; k < geo.size(); ++k) gf[k] = (float)geo[k];
-    cudaMalloc(&h->gtab_f, gf.size() * sizeof(float));
-    cudaMemcpy(h->gtab_f, gf.data(), gf.size() * sizeof(float), cudaMemcpyHostToDevice);
+    ok(cudaMalloc(&h->gtab_f, gf.size() * sizeof(float)));
+    ok(cudaMemcpyAsync(h->gtab_f, gf.data(), gf.size() * sizeof(float), cudaMemcpyHostToDevice, h->st));
   }
   int64_t maxcap = 1;
   for (int i = 0; i < nsp; ++i) {
@@ -822,10 +830,10 @@ int cyl_create(const cyl_grid_desc* gd, const cyl_species_desc* spd, int32_t nsp
   }
   h->xg0 = h->g.x_grid_min;
   h->ntiles_max = (rc.nx / TILE_X + 3) * (rc.ny / TILE_Y + 2);
-  cudaMalloc(&h->d_tiles, sizeof(TileTable) * MAX_SPECIES);
-  cudaMemset(h->d_tiles, 0, sizeof(TileTable) * MAX_SPECIES);
-  cudaMalloc(&h->d_tile_start, sizeof(int64_t) * (h->ntiles_max + 1) * MAX_SPECIES);
-  cudaMemset(h->d_tile_start, 0, sizeof(int64_t) * (h->ntiles_max + 1) * MAX_SPECIES);
+  ok(cudaMalloc(&h->d_tiles, sizeof(TileTable) * MAX_SPECIES));
+  ok(cudaMemsetAsync(h->d_tiles, 0, sizeof(TileTable) * MAX_SPECIES, h->st));
+  ok(cudaMalloc(&h->d_tile_start, sizeof(int64_t) * (h->ntiles_max + 1) * MAX_SPECIES));
+  ok(cudaMemsetAsync(h->d_tile_start, 0, sizeof(int64_t) * (h->ntiles_max + 1) * MAX_SPECIES, h->st));
   if (h->prec == CYL_PREC_MIXED) {
     int64_t fbtot = 0;
     for (int i = 0; i < nsp; ++i) fbtot += h->sp[i].cap + 1;
@@ -848,8 +856,8 @@ int cyl_create(const cyl_grid_desc* gd, const cyl_species_desc* spd, int32_t nsp
     }
   }
   h->nblocks_mixed = nsm * push_mixed_blocks_per_sm(rc.M);
-  cudaMalloc(&h->d_cnt, sizeof(SpeciesCounters) * MAX_SPECIES);
-  cudaMemset(h->d_cnt, 0, sizeof(SpeciesCounters) * MAX_SPECIES);
+  ok(cudaMalloc(&h->d_cnt, sizeof(SpeciesCounters) * MAX_SPECIES));
+  ok(cudaMemsetAsync(h->d_cnt, 0, sizeof(SpeciesCounters) * MAX_SPECIES, h->st));
   // sort scratch: keys, histogram, block sums, 7 doubles + id per particle
   h->sc.ncells = rc.nxg * rc.nyg;
   h->sc.cap = maxcap;
@@ -871,7 +879,7 @@ int cyl_create(const cyl_grid_desc* gd, const cyl_species_desc* spd, int32_t nsp
     p += (size_t)maxcap * 4;
     h->sc.hist = (int32_t*)p;
   }
-  cudaMalloc(&h->d_red, 8 * sizeof(double));
+  ok(cudaMalloc(&h->d_red, 8 * sizeof(double)));
   // staging for CHUNK steps
   h->src_per_step = (size_t)4 * (rc.ny + 1);
   int64_t per_step_inj = 0;
@@ -879,20 +887,24 @@ int cyl_create(const cyl_grid_desc* gd, const cyl_species_desc* spd, int32_t nsp
   for (int i = 0; i < nsp; ++i)
     per_step_inj += (int64_t)(shifts_max * (double)rc.ny * (std::floor(spd[i].npart_per_cell) + 1.0));
   h->inj_cap = h->move_window ? per_step_inj * CHUNK + 1 : 1;
-  cudaMallocHost(&h->h_rec, sizeof(StepRec) * CHUNK);
-  cudaMalloc(&h->d_rec, sizeof(StepRec) * (CHUNK + 1));
-  cudaMallocHost(&h->h_src, sizeof(double) * h->src_per_step * CHUNK);
-  cudaMalloc(&h->d_src, sizeof(double) * h->src_per_step * CHUNK);
-  cudaMallocHost(&h->h_inj, sizeof(double) * 8 * h->inj_cap);
-  cudaMalloc(&h->d_inj, sizeof(double) * 8 * h->inj_cap);
-  cudaEventCreateWithFlags(&h->ev_copy, cudaEventDisableTiming);
+  ok(cudaMallocHost(&h->h_rec, sizeof(StepRec) * CHUNK));
+  ok(cudaMalloc(&h->d_rec, sizeof(StepRec) * (CHUNK + 1)));
+  ok(cudaMallocHost(&h->h_src, sizeof(double) * h->src_per_step * CHUNK));
+  ok(cudaMalloc(&h->d_src, sizeof(double) * h->src_per_step * CHUNK));
+  ok(cudaMallocHost(&h->h_inj, sizeof(double) * 8 * h->inj_cap));
+  ok(cudaMalloc(&h->d_inj, sizeof(double) * 8 * h->inj_cap));
+  ok(cudaEventCreateWithFlags(&h->ev_copy, cudaEventDisableTiming));
   for (int k = 0; k < CHUNK; ++k) {
-    cudaEventCreate(&h->ev_push[k][0]);
-    cudaEventCreate(&h->ev_push[k][1]);
+    ok(cudaEventCreate(&h->ev_push[k][0]));
+    ok(cudaEventCreate(&h->ev_push[k][1]));
   }
-  if (cudaDeviceSynchronize() != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+  // Only this handle's stream is synchronised: a device-wide synchronisation
+  // is invalid while another thread's stream is being captured into a graph
+  // (the request loop creates handles while other runs capture their steps).
+  ok(cudaStreamSynchronize(h->st));
+  if (first_err != cudaSuccess) {
     cyl_destroy((cyl_handle)hs);
-    return CYL_ERR_OUT_OF_MEMORY;
+    return first_err == cudaErrorMemoryAllocation ? CYL_ERR_OUT_OF_MEMORY : CYL_ERR_CUDA;
   }
   *out = (cyl_handle)hs;
   return CYL_OK;
