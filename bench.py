@@ -274,8 +274,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--eager", action="store_true", help="no CUDA graphs")
-    ap.add_argument("--fp64-steps", type=int, default=200,
-                    help="steps of the plain FP64 form timed beside the mixed form (0: skip)")
+    ap.add_argument("--fp64-steps", type=int, default=-1,
+                    help="steps of the plain FP64 form timed beside the mixed form "
+                         "(-1: the same K steps, compared with the mixed result; 0: skip)")
     ap.add_argument("--serve", action="store_true", help="parameter-scan serving benchmark")
     ap.add_argument("--jobs", type=int, default=64)
     ap.add_argument("--arrival", type=float, default=0.5, help="mean Poisson arrival gap (s)")
@@ -382,20 +383,31 @@ def main():
                 "kernel_ms": push_ms, "algorithmic_bytes_per_particle_step": per_particle}
 
     fp64 = None
-    if form == "mixed" and args.fp64_steps > 0:
+    accuracy = None
+    if form == "mixed" and args.fp64_steps != 0:
+        # the plain FP64 form on the same deck, seed and steps; with the whole
+        # K steps (the default) its final state is compared with the mixed run
+        k64 = args.steps if args.fp64_steps < 0 else args.fp64_steps
         d64 = build_deck(args.deck, "fp64")
         r64 = cg.Run(d64, particles=parts, rng=rng)
         r64.step(args.warmup, graph=False)
+        s64a = r64.state()
+        n64a = sum(s64a.n_live[i] for i in range(len(d64.species)) if not d64.species[i].immobile)
+        ext64 = torch.cuda.ExternalStream(r64.stream())
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        r64.step(args.fp64_steps, graph=graph)
+        e0.record(ext64)
+        r64.step(k64, graph=graph)
+        e1.record(ext64)
         torch.cuda.synchronize()
-        dt64 = time.perf_counter() - t0
+        dt64 = e0.elapsed_time(e1) * 1e-3
         s64 = r64.state()
-        n64 = sum(s64.n_live[i] for i in range(len(d64.species)))
-        fp64 = {"value": n64 * args.fp64_steps / dt64, "steps": args.fp64_steps,
-                "ms_per_step": 1e3 * dt64 / args.fp64_steps,
-                "note": "plain FP64 form, steps [W, W+K64) of the same deck"}
+        n64 = sum(s64.n_live[i] for i in range(len(d64.species)) if not d64.species[i].immobile)
+        fp64 = {"value": 0.5 * (n64a + n64) * k64 / dt64, "steps": k64, "ms_per_step": 1e3 * dt64 / k64,
+                "note": "plain FP64 form, the same steps [W, W+K) of the same deck, CUDA events"}
+        if k64 == args.steps:
+            accuracy = compare_forms(run, r64, deck)
         r64.close()
 
     e2e = None
@@ -430,11 +442,71 @@ def main():
         if fp64:
             line["fp64_form"] = fp64
             line["mixed_over_fp64"] = value / fp64["value"]
+        if accuracy:
+            line["accuracy"] = accuracy
         print(json.dumps(line))
     run.close()
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def _spectrum(p, mass):
+    """Weighted moments of the kinetic energy (MeV) of one species."""
+    import numpy as np
+    mc = mass * 2.99792458e8
+    u2 = (p.px ** 2 + p.py ** 2 + p.pz ** 2) / mc ** 2
+    ke = mc * 2.99792458e8 * u2 / (np.sqrt(u2 + 1.0) + 1.0) / 1.602176565e-13
+    w = p.w / np.sum(p.w)
+    return {"mean_mev": float(np.sum(w * ke)), "rms_mev": float(np.sqrt(np.sum(w * ke ** 2))),
+            "m3_mev": float(np.cbrt(np.sum(w * ke ** 3))), "max_mev": float(np.max(ke))}
+
+
+def _residual_step(run, deck, tries=8):
+    """Continuity residual of the next step of `run` that does not shift the
+    window (the charge densities must be on one grid)."""
+    from cylindrical_epoch_gb300.diagnostics import continuity_residual
+    for _ in range(tries):
+        s0 = run.state().n_shifts
+        r0 = run.charge_density()
+        run.step(1)
+        if run.state().n_shifts != s0:
+            continue
+        r1 = run.charge_density()
+        return continuity_residual(deck, r0, r1, run.field("jxm"), run.field("jrm"), run.field("jtm"),
+                                   deck.grid_desc().dt)[0]
+    return None
+
+
+def compare_forms(mixed, fp64, deck):
+    """Error of the mixed form against the plain FP64 form after the same
+    steps: per-mode Ez relative L2, on-axis wake amplitude, electron
+    kinetic-energy moments, and the continuity residual of one further step."""
+    import numpy as np
+    rel = lambda a, b: float(np.sqrt(np.sum(np.abs(a - b) ** 2) / max(np.sum(np.abs(b) ** 2), 1e-300)))
+    ea, eb = mixed.field("exm"), fp64.field("exm")
+    ez = [rel(ea[m], eb[m]) for m in range(deck.n_mode)]
+    from cylindrical_epoch_gb300 import abi
+    ax = abi.NG - 1  # exm row ir = 0 (r = 0) is array row ng - 1
+    lo, hi = abi.NG, abi.NG + deck.nx  # ix = 1 .. nx
+    wa = float(np.max(np.abs(ea[0, ax, lo:hi].real)))
+    wb = float(np.max(np.abs(eb[0, ax, lo:hi].real)))
+    spa = _spectrum(mixed.particles(0), deck.species[0].mass)
+    spb = _spectrum(fp64.particles(0), deck.species[0].mass)
+    sa, sb = mixed.state(), fp64.state()
+    res_m = _residual_step(mixed, deck)
+    res_f = _residual_step(fp64, deck)
+    return {
+        "against": "plain FP64 GPU form, same deck, seed and steps (the FP64 form matches the oracle "
+                   "to 1e-10 in tests/)",
+        "ez_rel_l2_per_mode": ez,
+        "wake_amplitude_v_per_m": {"mixed": wa, "fp64": wb, "rel_err": abs(wa - wb) / max(wb, 1e-300)},
+        "electron_spectrum": {"mixed": spa, "fp64": spb,
+                              "rel_err": {k: abs(spa[k] - spb[k]) / max(abs(spb[k]), 1e-300) for k in spa}},
+        "continuity_residual_per_mode": {"mixed": res_m, "fp64": res_f},
+        "n_live": {"mixed": int(sa.n_live[0]), "fp64": int(sb.n_live[0])},
+        "n_shifts": {"mixed": int(sa.n_shifts), "fp64": int(sb.n_shifts)},
+    }
 
 
 def e2e_run(deck, parts, rng, steps, graph):

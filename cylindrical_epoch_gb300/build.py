@@ -27,6 +27,7 @@ SOURCES = [
     ("fields.cu", ["--fmad=false"]),
     ("push_fp64.cu", ["--fmad=false"]),
     ("particles.cu", ["--fmad=false"]),
+    ("charge.cu", ["--fmad=false"]),
     ("push_mixed.cu", ["--fmad=true"]),
     ("fields_fp32.cu", ["--fmad=true"]),
     ("mixed_particles.cu", ["--fmad=true"]),

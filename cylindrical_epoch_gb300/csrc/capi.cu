@@ -1252,6 +1252,23 @@ int cyl_sort_particles(cyl_handle hh) {
   return sync_and_check(h);
 }
 
+int cyl_charge_density(cyl_handle hh, double* rho) {
+  if (!hh || !rho) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  // the work array is free between steps
+  cplx* dst = h->F[15];
+  const FView v{dst, h->rc.nxg, h->rc.nyg};
+  CK(cudaMemsetAsync(dst, 0, h->fcount * sizeof(cplx), h->st));
+  for (int i = 0; i < h->nsp; ++i) {
+    if (h->sp[i].immobile) continue;
+    launch_charge_density(h->st, h->sp[i], h->d_cnt + i, h->geom.inv_volume, h->rc, h->g.x_grid_min,
+                          (int)h->n_shifts, h->prec == CYL_PREC_MIXED, v, h->nblocks);
+  }
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(rho, dst, h->fcount * sizeof(cplx), cudaMemcpyDeviceToHost, h->st));
+  return sync_and_check(h);
+}
+
 int cyl_cell_indices_noalloc(cyl_handle hh, int32_t isp, int32_t* cx, int32_t* cy, int64_t* n_inout) {
   if (!hh || !n_inout) return CYL_ERR_BAD_ARG;
   Handle* h = &hh->h;

@@ -63,6 +63,11 @@ void launch_push_fp64(cudaStream_t s, const FieldSet& F, const GeomTables& g, co
                       SpeciesCounters* cnt, const StepRec* rec, const RunConst& rc, int apply_bcs,
                       int* err, int nblocks);
 
+// charge.cu (continuity-residual diagnostic)
+void launch_charge_density(cudaStream_t s, const SpeciesPtrs& sp, const SpeciesCounters* cnt,
+                           const double* inv_volume, const RunConst& rc, double x_grid_min, int nsh,
+                           bool mixed, const FView& rho, int nblocks);
+
 // particles.cu
 void launch_particle_bcs(cudaStream_t s, const SpeciesPtrs& sp, SpeciesCounters* cnt,
                          const StepRec* rec, int after_shift, const RunConst& rc, int nblocks);

@@ -42,6 +42,7 @@ SIGNATURES = {
     "cyl_sort_particles": (C.c_int, [H]),
     "cyl_cell_indices": (C.c_int, [H, I32, PI32, PI32, PI64]),
     "cyl_cell_indices_noalloc": (C.c_int, [H, I32, PI32, PI32, PI64]),
+    "cyl_charge_density": (C.c_int, [H, PD]),
     "cyl_push_only": (C.c_int, [H]),
     "cyl_kernel_timing": (C.c_int, [H, PD, PI64]),
     "cyl_get_stream": (C.c_int, [H, P(C.c_void_p)]),

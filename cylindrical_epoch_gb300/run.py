@@ -155,6 +155,13 @@ class Run:
         abi.check("cyl_download_field", self.lib.cyl_download_field(self.h, which, _p(a.view(np.float64))))
         return a
 
+    def charge_density(self):
+        """Per-mode charge density of the deposit's staggered shape for the
+        current state (cyl_charge_density), shaped like field()."""
+        a = np.zeros((self.deck.n_mode, self.nyg, self.nxg), dtype=np.complex128)
+        abi.check("cyl_charge_density", self.lib.cyl_charge_density(self.h, _p(a.view(np.float64))))
+        return a
+
     def upload_field(self, name, arr):
         which = abi.FIELD_INDEX[name] if isinstance(name, str) else name
         a = np.ascontiguousarray(arr, dtype=np.complex128)

@@ -257,6 +257,17 @@ int cyl_cell_indices(cyl_handle h, int32_t ispecies, int32_t* cell_x,
 int cyl_cell_indices_noalloc(cyl_handle h, int32_t ispecies, int32_t* cell_x,
                              int32_t* cell_y, int64_t* n_inout);
 
+/* Per-mode charge density of the mobile species, complex FP64 in the field
+ * layout (like cyl_download_field), computed from the current particle state
+ * with the current deposit's own staggered shape at t + dt/2 (the half-drift
+ * of particles.F90:304-312, cell_x2 and the h weights of :369-388, the
+ * 2 e^{i m theta} mode factor of :595-611 and inv_volume of :661).  Between
+ * two calls around one step, (rho' - rho)/dt + div J is the discrete
+ * continuity residual of that step's deposit; the reference has no such
+ * diagnostic (its Gauss-law consistency rests on the same identity).  The
+ * mixed form evaluates it in FP64 from its stored state. */
+int cyl_charge_density(cyl_handle h, double* rho);
+
 /* Push-and-deposit only (the body of push_particles, particles.F90:163-734,
  * without current_bcs_r_min_final and particle_bcs): used by the parity tests
  * and by the kernel benchmark to time the dominant kernel alone. */

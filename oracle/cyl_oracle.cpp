@@ -1137,6 +1137,68 @@ void push_one(Sim& s, const Geom& g, Species& spc, size_t i, double part_q, doub
   }
 }
 
+// Per-mode charge density of the mobile species with the deposit's own
+// staggered (h) shape, at the half-drifted position x + u c dt/2 / gamma: the
+// t + dt/2 shape of the next push (particles.F90:304-312 for the drift,
+// :369-388 for cell_x2 and the h weights, :548-571 for the same shape at
+// t + 3 dt/2).  Mode m > 0 carries the 2 e^{i m theta} factor of m_fac_1
+// (:595-611) and every cell the inv_volume of its row (:661), so that the
+// deposit satisfies, per particle,
+//   (rho' - rho)/dt + div_x J + div_r J - (i m / r_p) J_theta = 0
+// exactly in its x and r parts (the theta part uses v_theta, :587).
+void charge_density(Sim& s, Field& rho) {
+  std::fill(rho.a.begin(), rho.a.end(), mk(0, 0));
+  Geom g;
+  make_geom(s, g);
+  const double fac = 0.25;
+  const double idx = 1.0 / s.dx, idy = 1.0 / s.dy;
+  const double dtco2 = C * (s.dt / 2.0);
+  for (auto& spc : s.sp) {
+    if (spc.d.immobile) continue;
+    const double part_q = spc.d.charge;
+    const double ipart_mc = 1.0 / (C * spc.d.mass);
+    for (size_t i = 0; i < spc.n(); ++i) {
+      const double part_ux = spc.px[i] * ipart_mc, part_uy = spc.py[i] * ipart_mc, part_uz = spc.pz[i] * ipart_mc;
+      const double gamma_rel = std::sqrt(((part_ux * part_ux + part_uy * part_uy) + part_uz * part_uz) + 1.0);
+      const double root = dtco2 / gamma_rel;
+      const double part_x = spc.x[i] + part_ux * root;
+      const double part_y = spc.y[i] + part_uy * root;
+      const double part_z = spc.z[i] + part_uz * root;
+      const double part_r = std::sqrt(part_y * part_y + part_z * part_z);
+      const cplx exp_itheta = crecip(mk(part_y / part_r, (-part_z) / part_r));
+      const double cell_x_r = (part_x - s.x_grid_min) * idx;
+      const double cell_y_r = (part_r - s.y_grid_min) * idy;
+      int cell_x2 = ffloor(cell_x_r);
+      const double fx = ((double)cell_x2 - cell_x_r) + 0.5;
+      cell_x2 = cell_x2 + 1;
+      int cell_y2 = ffloor(cell_y_r);
+      const double fy = ((double)cell_y2 - cell_y_r) + 0.5;
+      cell_y2 = cell_y2 + 1;
+      double hx[3], hy[3];
+      double cf2 = fx * fx;
+      hx[0] = (0.25 + cf2) + fx; hx[1] = 1.5 - 2.0 * cf2; hx[2] = (0.25 + cf2) - fx;
+      cf2 = fy * fy;
+      hy[0] = (0.25 + cf2) + fy; hy[1] = 1.5 - 2.0 * cf2; hy[2] = (0.25 + cf2) - fy;
+      const double qwf = part_q * spc.w[i] * fac;
+      cplx mf = mk(1.0, 0.0), e_m = mk(1.0, 0.0);
+      for (int im = 0; im < s.M; ++im) {
+        if (im > 0) {
+          e_m = e_m * exp_itheta;
+          mf = 2.0 * e_m;
+        }
+        for (int iy = -1; iy <= 1; ++iy) {
+          const int cy = cell_y2 + iy;
+          const double fr = qwf * hy[iy + 1] * g.inv_volume[cy - (1 - JNG)];
+          for (int ix = -1; ix <= 1; ++ix) {
+            cplx& d = rho(cell_x2 + ix, cy, im);
+            d = d + (fr * hx[ix + 1]) * mf;
+          }
+        }
+      }
+    }
+  }
+}
+
 // push_particles without the trailing current_bcs_r_min_final / particle_bcs
 void push_particles_core(Sim& s) {
   s.jx_old = s.jx; s.jr_old = s.jr; s.jt_old = s.jt;
@@ -1854,6 +1916,16 @@ int orc_cell_indices(orc_handle h, int32_t isp, int32_t* cx, int32_t* cy) {
     cy[i] = ffloor((part_r - s->y_grid_min) / s->dy + 1.5);
   }
   return CYL_OK;
+}
+
+// Per-mode charge density (complex FP64, field layout) of the current state.
+int orc_charge_density(orc_handle h, double* data) {
+  Sim& s = *(Sim*)h;
+  Field rho;
+  rho.init(s.nx, s.ny, s.M);
+  charge_density(s, rho);
+  std::memcpy(data, rho.a.data(), rho.a.size() * sizeof(cplx));
+  return 0;
 }
 
 void orc_set_threads(int32_t n) { g_threads = n < 1 ? 1 : n; }

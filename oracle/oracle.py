@@ -69,6 +69,7 @@ def load():
         "orc_get_run_state": (C.c_int, [H, C.POINTER(abi.RunState)]),
         "orc_diagnostics": (C.c_int, [H, C.POINTER(abi.Diag)]),
         "orc_cell_indices": (C.c_int, [H, C.c_int32, PI32, PI32]),
+        "orc_charge_density": (C.c_int, [H, PD]),
         "orc_atan2": (C.c_double, [C.c_double, C.c_double]),
         "orc_set_threads": (None, [C.c_int32]),
         "orc_dx": (C.c_double, [H]),
@@ -180,6 +181,13 @@ class Oracle:
         d = self.abi.Diag()
         self.lib.orc_diagnostics(self.h, C.byref(d))
         return d
+
+    def charge_density(self):
+        """Per-mode charge density of the deposit's staggered shape (the
+        t + dt/2 shape of the next push), complex (M, ny+2ng, nx+2ng)."""
+        a = np.zeros((self.deck.n_mode, self.nyg, self.nxg), dtype=np.complex128)
+        self.lib.orc_charge_density(self.h, a.view(np.float64).ctypes.data_as(C.POINTER(C.c_double)))
+        return a
 
     def cell_indices(self, isp=0):
         n = self.lib.orc_count(self.h, isp)

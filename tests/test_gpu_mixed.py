@@ -72,3 +72,27 @@ def test_mixed_thermal_energy(gpu_lib):
     for n in ("exm", "erm"):
         x, y = a.field(n), b.field(n)
         assert rel_l2(y[0], x[0]) < 5e-3, n
+
+
+def test_mixed_continuity_residual(gpu_lib):
+    """Discrete continuity residual of one mixed-form step, evaluated in FP64
+    from the stored state: m = 0 within the form's 1e-3 error bar (the FP64
+    form is at round-off), m = 1 within 1e-3 of the FP64 form's value."""
+    from cylindrical_epoch_gb300.diagnostics import continuity_residual
+    d64 = cg.thermal_plasma(nx=64, ny=32, ppc=8)
+    d32 = cg.thermal_plasma(nx=64, ny=32, ppc=8, precision=abi.PREC_MIXED)
+    parts, rng = cg.host_load(d64)
+    res = []
+    for d in (d64, d32):
+        run = cg.Run(d, particles=parts, rng=rng)
+        run.step(2)
+        r0 = run.charge_density()
+        run.step(1)
+        r1 = run.charge_density()
+        res.append(continuity_residual(d, r0, r1, run.field("jxm"), run.field("jrm"), run.field("jtm"),
+                                       d.grid_desc().dt)[0])
+        run.close()
+    print("continuity residual per mode: fp64", res[0], "mixed", res[1])
+    assert res[0][0] < 1e-12
+    assert res[1][0] < TOL_EZ
+    assert abs(res[1][1] - res[0][1]) < TOL_EZ

@@ -125,3 +125,26 @@ def test_graph_matches_eager(gpu_lib):
     assert a.state().n_live[0] == b.state().n_live[0]
     for n in ("exm", "btm", "jxm"):
         assert rel_l2(b.field(n), a.field(n)) < 1e-10
+
+
+def test_charge_density_and_continuity(gpu_lib):
+    """cyl_charge_density against the oracle, and the discrete continuity
+    residual of one step of the FP64 form: m = 0 at round-off, m = 1 equal
+    to the oracle's (its theta current is not exactly conservative)."""
+    from cylindrical_epoch_gb300.diagnostics import continuity_residual
+    deck = cg.thermal_plasma(nx=64, ny=32, ppc=8)
+    gpu, orc = _pair(deck)
+    gpu.step(2)
+    orc.step(2)
+    r0g, r0o = gpu.charge_density(), orc.charge_density()
+    for m in range(deck.n_mode):
+        assert rel_l2(r0g[m], r0o[m]) < TOL_FIELD, m
+    gpu.step(1)
+    orc.step(1)
+    r1g, r1o = gpu.charge_density(), orc.charge_density()
+    dt = deck.grid_desc().dt
+    rg = continuity_residual(deck, r0g, r1g, gpu.field("jxm"), gpu.field("jrm"), gpu.field("jtm"), dt)[0]
+    ro = continuity_residual(deck, r0o, r1o, orc.field("jxm"), orc.field("jrm"), orc.field("jtm"), dt)[0]
+    print("continuity residual per mode: gpu", rg, "oracle", ro)
+    assert rg[0] < 1e-12
+    assert abs(rg[1] - ro[1]) < 1e-8
