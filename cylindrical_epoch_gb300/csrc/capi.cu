@@ -107,6 +107,7 @@ struct Handle {
   MixedParams mp[MAX_SPECIES];
   TileTable* d_tiles = nullptr;     // one per species
   int64_t* d_tile_start = nullptr;  // (ntiles_max + 1) per species
+  int32_t* d_tile_order = nullptr;  // ntiles_max per species (push schedule)
   int ntiles_max = 0;
   int64_t kernel_launches = 0;
   int64_t graph_launches = 0;
@@ -403,7 +404,8 @@ static void enqueue_sort(Handle* h, const StepRec* rec) {
     if (h->sp[i].immobile) continue;
     if (h->prec == CYL_PREC_MIXED) {
       mixed_sort(h->st, h->sp[i], h->d_cnt + i, h->sc, h->d_tiles + i,
-                 h->d_tile_start + (size_t)i * (h->ntiles_max + 1), rec, h->rc, h->nblocks);
+                 h->d_tile_start + (size_t)i * (h->ntiles_max + 1), h->d_tile_order + (size_t)i * h->ntiles_max,
+                 rec, h->rc, h->nblocks);
       count_launch(h, 9);
     } else {
       sort_species(h->st, h->sp[i], h->d_cnt + i, h->sc, &rec->x_grid_min_after, h->rc, h->nblocks);
@@ -663,7 +665,7 @@ int cyl_estimate_device_bytes(const cyl_grid_desc* gd, const cyl_species_desc* s
   }
   if (gd->precision == CYL_PREC_MIXED) b += fbtot * (int64_t)sizeof(int);  // deferred lists
   const int64_t ntiles_max = (gd->nx / TILE_X + 3) * (gd->ny / TILE_Y + 2);
-  b += (ntiles_max + 1) * MAX_SPECIES * 8;
+  b += (ntiles_max + 1) * MAX_SPECIES * 8 + ntiles_max * MAX_SPECIES * 4;
   const int64_t ncells = nxg * nyg;
   b += maxcap * (4 + 8 * 8) + (ncells + 2) * 4 + ((ncells + 4096) / 4096 + 64) * 8;  // sort scratch
   const int64_t inj_cap = gd->move_window ? per_step_inj * CHUNK + 1 : 1;
@@ -834,6 +836,7 @@ int cyl_create(const cyl_grid_desc* gd, const cyl_species_desc* spd, int32_t nsp
   ok(cudaMemsetAsync(h->d_tiles, 0, sizeof(TileTable) * MAX_SPECIES, h->st));
   ok(cudaMalloc(&h->d_tile_start, sizeof(int64_t) * (h->ntiles_max + 1) * MAX_SPECIES));
   ok(cudaMemsetAsync(h->d_tile_start, 0, sizeof(int64_t) * (h->ntiles_max + 1) * MAX_SPECIES, h->st));
+  ok(cudaMalloc(&h->d_tile_order, sizeof(int32_t) * h->ntiles_max * MAX_SPECIES));
   if (h->prec == CYL_PREC_MIXED) {
     int64_t fbtot = 0;
     for (int i = 0; i < nsp; ++i) fbtot += h->sp[i].cap + 1;
@@ -928,6 +931,7 @@ int cyl_destroy(cyl_handle hh) {
   cudaFree(h->fb_buf);
   cudaFree(h->d_dbg);
   cudaFree(h->d_tile_start);
+  cudaFree(h->d_tile_order);
   cudaFree(h->sort_buf);
   cudaFree(h->d_err);
   cudaFree(h->d_red);

@@ -257,13 +257,14 @@ void mixed_cell_indices(cudaStream_t s, const SpeciesPtrs& sp, const SpeciesCoun
 
 __device__ __forceinline__ int floordiv(int a, int b) { return (a >= 0) ? a / b : -((-a + b - 1) / b); }
 
-__global__ void k_tile_layout(TileTable* tt, const StepRec* rec, RunConst rc, int64_t* start) {
+__global__ void k_tile_layout(TileTable* tt, const StepRec* rec, RunConst rc, int64_t* start, int32_t* order) {
   const int nsh = rec->nshift_total_after;
   tt->tx_min = floordiv(nsh, TILE_X) - 1;
   tt->ntx = rc.nx / TILE_X + 3;
   tt->nty = rc.ny / TILE_Y + 2;
   tt->ntiles = tt->ntx * tt->nty;
   tt->start = start;
+  tt->order = order;
 }
 
 __global__ void k_tile_keys(SpeciesPtrs sp, const SpeciesCounters* cnt, const TileTable* tt, int32_t* keys,
@@ -352,21 +353,68 @@ __global__ void k_tile_scatter(SpeciesPtrs sp, const SpeciesCounters* cnt, const
   }
 }
 
+// The push's tile schedule: tiles by decreasing particle count, bucketed by
+// count / 8 (counts of 8 * (ORDER_BUCKETS - 1) and more share the top
+// bucket).  One CTA: a histogram of the buckets, an exclusive scan from the
+// top bucket down, and a scatter of the tile indices.  Every tile appears
+// exactly once; the order inside a bucket follows the shared-memory atomics.
+constexpr int ORDER_BUCKETS = 1024;
+__global__ void __launch_bounds__(ORDER_BUCKETS) k_tile_order(const TileTable* tt, const int64_t* start,
+                                                               int32_t* order) {
+  __shared__ int hist[ORDER_BUCKETS];
+  __shared__ int warp_tot[ORDER_BUCKETS / 32];
+  const int nt = tt->ntiles;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  hist[tid] = 0;
+  __syncthreads();
+  auto bucket = [&](int t) {
+    const int64_t c = (start[t + 1] - start[t]) >> 3;
+    // descending: the fullest tiles get the lowest bucket index
+    return ORDER_BUCKETS - 1 - (int)(c < ORDER_BUCKETS - 1 ? c : ORDER_BUCKETS - 1);
+  };
+  for (int t = tid; t < nt; t += ORDER_BUCKETS) atomicAdd(&hist[bucket(t)], 1);
+  __syncthreads();
+  // exclusive scan of hist over the 1024 buckets (thread = bucket)
+  const int v = hist[tid];
+  int x = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, d);
+    if (lane >= d) x += y;
+  }
+  if (lane == 31) warp_tot[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    int s = warp_tot[lane];
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, s, d);
+      if (lane >= d) s += y;
+    }
+    warp_tot[lane] = s;  // inclusive sums of the warp totals
+  }
+  __syncthreads();
+  hist[tid] = x - v + (w > 0 ? warp_tot[w - 1] : 0);  // first slot of this bucket
+  __syncthreads();
+  for (int t = tid; t < nt; t += ORDER_BUCKETS) order[atomicAdd(&hist[bucket(t)], 1)] = t;
+}
+
 __global__ void k_tile_commit(SpeciesCounters* cnt, const TileTable* tt) {
   cnt->n_used = tt->n_sorted;
   cnt->n_dead = 0;
 }
 
 void mixed_sort(cudaStream_t s, const SpeciesPtrs& sp, SpeciesCounters* cnt, SortScratch& sc, TileTable* tt,
-                int64_t* tile_start, const StepRec* rec, const RunConst& rc, int nblocks) {
+                int64_t* tile_start, int32_t* tile_order, const StepRec* rec, const RunConst& rc, int nblocks) {
   const int ntiles_max = (rc.nx / TILE_X + 3) * (rc.ny / TILE_Y + 2);
-  k_tile_layout<<<1, 1, 0, s>>>(tt, rec, rc, tile_start);
+  k_tile_layout<<<1, 1, 0, s>>>(tt, rec, rc, tile_start, tile_order);
   cudaMemsetAsync(sc.hist, 0, sizeof(int32_t) * (ntiles_max + 1), s);
   k_tile_keys<<<nblocks, 256, 0, s>>>(sp, cnt, tt, sc.keys, sc.hist);
   scan_exclusive(s, sc.hist, ntiles_max + 1, (int32_t*)sc.perm);
   k_tile_starts<<<64, 256, 0, s>>>(sc.hist, tile_start, tt, ntiles_max);
   k_tile_copy_out<<<nblocks, 256, 0, s>>>(sp, cnt, sc.tmp, sc.tmp_id, sc.cap);
   k_tile_scatter<<<nblocks, 256, 0, s>>>(sp, cnt, sc.tmp, sc.tmp_id, sc.cap, sc.keys, sc.hist, tt);
+  k_tile_order<<<1, ORDER_BUCKETS, 0, s>>>(tt, tile_start, tile_order);
   k_tile_commit<<<1, 1, 0, s>>>(cnt, tt);
 }
 

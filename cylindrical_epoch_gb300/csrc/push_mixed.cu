@@ -49,27 +49,25 @@ __device__ __forceinline__ f2 operator*(float s, f2 a) { return {s * a.re, s * a
 // f4 = i (e^{i phi}(2 - 2 i phi - phi^2) - 2)/phi^3: the per-mode deposit
 // factors of particles.F90:603-625 without the 2 e^{i m theta0} prefactor.
 // Their Taylor series sum_k c_k (i phi)^k have c_k = 1/(k+1)!,
-// (k+1)/(k+2)! and (k+1)(k+2)/(k+3)!; FP32 sums the series below
-// |phi| = 0.5 (the closed forms cancel there) and uses the closed forms above.
+// (k+1)/(k+2)! and (k+1)(k+2)/(k+3)!.  Below |phi| = 0.5 (where the closed
+// forms cancel) FP32 sums the series to k = 7 (the first omitted term is
+// below 1e-8 of the sum) as two real polynomials in phi^2: the even terms
+// give the real part, the odd terms the imaginary part.
+__device__ __forceinline__ f2 series(float p2, float phi, float c0, float c1, float c2, float c3, float c4, float c5,
+                                     float c6, float c7) {
+  const float re = fmaf(fmaf(fmaf(-c6, p2, c4), p2, -c2), p2, c0);
+  const float im = phi * fmaf(fmaf(fmaf(-c7, p2, c5), p2, -c3), p2, c1);
+  return fm(re, im);
+}
 __device__ __forceinline__ void mode_factors(float phi, f2 eip, f2& F2, f2& F3, f2& F4) {
   if (fabsf(phi) < 0.5f) {
-    const f2 z = fm(0.0f, phi);
-    f2 a = fm(1.0f / 3628800.0f, 0.f), b = fm(10.0f / 39916800.0f, 0.f), c = fm(110.0f / 479001600.0f, 0.f);
-    const float c2[9] = {1.0f / 362880.0f, 1.0f / 40320.0f, 1.0f / 5040.0f, 1.0f / 720.0f, 1.0f / 120.0f,
-                         1.0f / 24.0f, 1.0f / 6.0f, 1.0f / 2.0f, 1.0f};
-    const float c3[9] = {9.0f / 3628800.0f, 8.0f / 362880.0f, 7.0f / 40320.0f, 6.0f / 5040.0f, 5.0f / 720.0f,
-                         4.0f / 120.0f, 3.0f / 24.0f, 2.0f / 6.0f, 1.0f / 2.0f};
-    const float c4[9] = {90.0f / 39916800.0f, 72.0f / 3628800.0f, 56.0f / 362880.0f, 42.0f / 40320.0f,
-                         30.0f / 5040.0f, 20.0f / 720.0f, 12.0f / 120.0f, 6.0f / 24.0f, 2.0f / 6.0f};
-#pragma unroll
-    for (int k = 0; k < 9; ++k) {
-      a = a * z + fm(c2[k], 0.f);
-      b = b * z + fm(c3[k], 0.f);
-      c = c * z + fm(c4[k], 0.f);
-    }
-    F2 = a;
-    F3 = b;
-    F4 = c;
+    const float p2 = phi * phi;
+    F2 = series(p2, phi, 1.0f, 1.0f / 2.0f, 1.0f / 6.0f, 1.0f / 24.0f, 1.0f / 120.0f, 1.0f / 720.0f,
+                1.0f / 5040.0f, 1.0f / 40320.0f);
+    F3 = series(p2, phi, 1.0f / 2.0f, 2.0f / 6.0f, 3.0f / 24.0f, 4.0f / 120.0f, 5.0f / 720.0f, 6.0f / 5040.0f,
+                7.0f / 40320.0f, 8.0f / 362880.0f);
+    F4 = series(p2, phi, 2.0f / 6.0f, 6.0f / 24.0f, 12.0f / 120.0f, 20.0f / 720.0f, 30.0f / 5040.0f,
+                42.0f / 40320.0f, 56.0f / 362880.0f, 72.0f / 3628800.0f);
   } else {
     const float ip = 1.0f / phi, ip2 = ip * ip;
     const f2 em1 = fm(eip.re - 1.0f, eip.im);
@@ -83,7 +81,7 @@ __device__ __forceinline__ void mode_factors(float phi, f2 eip, f2& F2, f2& F3, 
 }
 
 // Shared-memory layout: fields [6][M][RCELLS] float2; current accumulators
-// [3][M][re, im][hi, lo][RCELLS] int32 (fixed point, see deposit_tile).
+// [3][M][re, im][hi, lo][RCELLS] int32 (fixed point, see sadd).
 struct Tile {
   const float2* sf;
   int* sj;
@@ -95,7 +93,11 @@ struct Tile {
 // most 16 |q fac| w_max / dt (jx, jr) or 16 |q fac| w_max c (jtheta) to one
 // accumulator value (|partial sums of the weight changes| <= 2, |mode
 // factors| <= 2, 1, 2/3 with the 2 e^{i m theta} prefactor).  That bound is
-// scaled to 2^30 / k, k = max(1, n / 2^16) for a tile of n particles.
+// scaled to 2^30 / k, k = max(1, n / 2^16) for a tile of n particles.  The
+// bound is a worst case (a particle crossing a whole cell in one step): the
+// currents of slowly moving particles are 1e-3 of it and smaller, which is
+// why the accumulators are exact hi/lo pairs with a 2^-30 quantum rather
+// than single words (whose range would cap the quantum at n / 2^30).
 __device__ __forceinline__ void tile_scales(Tile& t, int64_t n, float qw_max, float idt, float c) {
   const float k = fmaxf(1.0f, (float)n * (1.0f / 65536.0f));
   const float bxr = 16.0f * qw_max * idt * k, bt = 16.0f * qw_max * c * k;
@@ -156,40 +158,44 @@ struct ModeWalk {
   }
 };
 
-// Add one FP32 value v (in accumulator units, |v| <= 2^30) to a hi/lo pair
-// of int32 accumulators: v = hi 2^15 + lo with |hi| <= 2^15, |lo| <= 2^14
-// + 1/2, each rounded to an integer with the 1.5 * 2^23 offset trick (the
-// split itself is exact).  The sums are exact integer sums -- independent of
-// the order of the adds -- and, with at most 2^16 adds per accumulator,
-// cannot overflow.  The error of one add is that of rounding v to FP32 plus
-// at most 1/2 unit.  Integer shared-memory adds are single native
-// instructions (FP32 shared-memory adds are not).
+// Add one FP32 value v (in accumulator units, |v| <= 2^30) to the hi/lo pair
+// of int32 accumulators at p (hi word p[0], lo word p[RCELLS]):
+// v = hi 2^15 + lo with |hi| <= 2^15, |lo| <= 2^14 + 1/2, each rounded to an
+// integer with the 1.5 * 2^23 offset trick (the split itself is exact).  The
+// sums are exact integer sums -- independent of the order of the adds -- and,
+// with at most 2^16 adds per accumulator, cannot overflow.  The error of one
+// add is that of rounding v to FP32 plus at most 1/2 unit.  Integer
+// shared-memory adds are single native instructions (FP32 shared-memory
+// adds are not).
 constexpr float FXP_MAGIC = 12582912.0f;  // 1.5 * 2^23
 constexpr int FXP_MAGIC_BITS = 0x4B400000;
-__device__ __forceinline__ void sadd(int* hi_p, int* lo_p, float v) {
+__device__ __forceinline__ void sadd(int* p, float v) {
   const float t = fmaf(v, 1.0f / 32768.0f, FXP_MAGIC);
   const int hi = __float_as_int(t) - FXP_MAGIC_BITS;
   const float lo = fmaf(-(t - FXP_MAGIC), 32768.0f, v);
   const int lo_i = __float_as_int(lo + FXP_MAGIC) - FXP_MAGIC_BITS;
-  if (hi != 0) atomicAdd(hi_p, hi);
-  if (lo_i != 0) atomicAdd(lo_p, lo_i);
+  if (hi != 0) atomicAdd(p, hi);
+  if (lo_i != 0) atomicAdd(p + RCELLS, lo_i);
 }
 
-// Deposit into the tile accumulators over a W x W window whose first cell is
-// (cx2 + x0, cy2 + y0); x0, y0 in {-2, -1} select the offsets -2..2 of the
-// weight arrays.  The accumulators are fixed-point integers (scale
-// tile.s_xr for jx and jr, tile.s_t for jtheta): integer shared-memory adds
-// are single instructions and their sums do not depend on the order of the
-// adds.
-template <int M, int W>
+// Deposit into the tile accumulators over a WX x WY window whose first cell
+// is (cx2 + x0, cy2 + y0); x0, y0 in {-2, -1} select the offsets -2..2 of the
+// weight arrays (a 3-cell extent always starts at -1).  The accumulators are
+// fixed-point integers (scale tile.s_xr for jx and jr, tile.s_t for jtheta):
+// integer shared-memory adds are single instructions and their sums do not
+// depend on the order of the adds.
+template <int M, int WX, int WY>
 __device__ __forceinline__ void deposit_tile(const Tile& tile, const float* og, const float* oh, const float* dgx,
                                              const float* dgy, int x0, int y0, int cx2, int cy2, float fc,
                                              float fcz, f2 e05, f2 edt, float dth) {
-  float gxw[W], hxw[W], gyw[W], hyw[W];
+  float gxw[WX], hxw[WX], gyw[WY], hyw[WY];
 #pragma unroll
-  for (int c = 0; c < W; ++c) {
+  for (int c = 0; c < WX; ++c) {
     gxw[c] = (x0 == -2) ? og[c] : og[c + 1];
     hxw[c] = (x0 == -2) ? dgx[c] : dgx[c + 1];
+  }
+#pragma unroll
+  for (int c = 0; c < WY; ++c) {
     gyw[c] = (y0 == -2) ? oh[c] : oh[c + 1];
     hyw[c] = (y0 == -2) ? dgy[c] : dgy[c + 1];
   }
@@ -206,11 +212,11 @@ __device__ __forceinline__ void deposit_tile(const Tile& tile, const float* og, 
     int* const ax = sj + ((0 * M + m) * 4) * RCELLS;
     int* const ar = sj + ((1 * M + m) * 4) * RCELLS;
     int* const at = sj + ((2 * M + m) * 4) * RCELLS;
-    f2 qr[W];
+    f2 qr[WX];
 #pragma unroll
-    for (int c = 0; c < W; ++c) qr[c] = fm(0.f, 0.f);
+    for (int c = 0; c < WX; ++c) qr[c] = fm(0.f, 0.f);
 #pragma unroll
-    for (int r = 0; r < W; ++r) {
+    for (int r = 0; r < WY; ++r) {
       const float gyv = gyw[r], hyv = hyw[r];
       f2 w_rt, ym1;
       if (m == 0) {
@@ -222,29 +228,57 @@ __device__ __forceinline__ void deposit_tile(const Tile& tile, const float* og, 
       }
       f2 qx = fm(0.f, 0.f);
 #pragma unroll
-      for (int c = 0; c < W; ++c) {
+      for (int c = 0; c < WX; ++c) {
         const float gxv = gxw[c], hxv = hxw[c];
-        const f2 w_xt = (m == 0) ? fm(gxv + 0.5f * hxv, 0.f) : (gxv * F2 + hxv * F3);
-        const f2 w_xr = gxv * w_rt + hxv * ym1;
-        qx = qx - (fcs * hxv) * w_rt;
-        qr[c] = qr[c] - (fcs * hyv) * w_xt;
-        const f2 qt = fczs * w_xr;
         const int cell = b0 + r * RW + c;
         // The window's last column (jx) and last row (jr) carry the running
         // flux sum after every weight change of the row (column), which is
         // zero up to FP32 round-off (old and new weights both sum to 2):
         // those adds are left out.
-        if (c < W - 1) sadd(ax + cell + 1, ax + RCELLS + cell + 1, qx.re);       // jx at (cx + 1, cy)
-        if (r < W - 1) sadd(ar + cell + RW, ar + RCELLS + cell + RW, qr[c].re);  // jr at (cx, cy + 1)
-        sadd(at + cell, at + RCELLS + cell, qt.re);                              // jtheta at (cx, cy)
-        if (m > 0) {
-          if (c < W - 1) sadd(ax + 2 * RCELLS + cell + 1, ax + 3 * RCELLS + cell + 1, qx.im);
-          if (r < W - 1) sadd(ar + 2 * RCELLS + cell + RW, ar + 3 * RCELLS + cell + RW, qr[c].im);
-          sadd(at + 2 * RCELLS + cell, at + 3 * RCELLS + cell, qt.im);
+        if (m == 0) {
+          const float w_xt = gxv + 0.5f * hxv;
+          const float w_xr = gxv * w_rt.re + hxv * ym1.re;
+          qx.re = qx.re - (fcs * hxv) * w_rt.re;
+          qr[c].re = qr[c].re - (fcs * hyv) * w_xt;
+          if (c < WX - 1) sadd(ax + cell + 1, qx.re);       // jx at (cx + 1, cy)
+          if (r < WY - 1) sadd(ar + cell + RW, qr[c].re);  // jr at (cx, cy + 1)
+          sadd(at + cell, fczs * w_xr);                     // jtheta at (cx, cy)
+        } else {
+          const f2 w_xt = gxv * F2 + hxv * F3;
+          const f2 w_xr = gxv * w_rt + hxv * ym1;
+          qx = qx - (fcs * hxv) * w_rt;
+          qr[c] = qr[c] - (fcs * hyv) * w_xt;
+          const f2 qt = fczs * w_xr;
+          if (c < WX - 1) {
+            sadd(ax + cell + 1, qx.re);
+            sadd(ax + 2 * RCELLS + cell + 1, qx.im);
+          }
+          if (r < WY - 1) {
+            sadd(ar + cell + RW, qr[c].re);
+            sadd(ar + 2 * RCELLS + cell + RW, qr[c].im);
+          }
+          sadd(at + cell, qt.re);
+          sadd(at + 2 * RCELLS + cell, qt.im);
         }
       }
     }
   }
+}
+
+// The window shape of a warp: 3 cells along a direction when no lane of the
+// warp changes cell along it, else 4 (holding the reference's xmin..xmax or
+// ymin..ymax range; the extra row or column carries zero flux).
+template <int M>
+__device__ __forceinline__ void deposit_tile_warp(const Tile& tile, const float* og, const float* oh,
+                                                  const float* dgx, const float* dgy, int dcx, int dcy, int cx2,
+                                                  int cy2, float fc, float fcz, f2 e05, f2 edt, float dth) {
+  const unsigned am = __activemask();
+  const bool wx = __any_sync(am, dcx != 0), wy = __any_sync(am, dcy != 0);
+  const int x0 = dcx < 0 ? -2 : -1, y0 = dcy < 0 ? -2 : -1;
+  if (!wx && !wy)
+    deposit_tile<M, 3, 3>(tile, og, oh, dgx, dgy, -1, -1, cx2, cy2, fc, fcz, e05, edt, dth);
+  else
+    deposit_tile<M, 4, 4>(tile, og, oh, dgx, dgy, x0, y0, cx2, cy2, fc, fcz, e05, edt, dth);
 }
 
 // Deposit of a particle on the global path: FP64 atomics into the global
@@ -357,42 +391,65 @@ __device__ __forceinline__ bool push_one(int64_t i, const SpeciesPtrs& sp, Speci
     hy[0] = 0.25f + c2 + fry2; hy[1] = 1.5f - 2.0f * c2; hy[2] = 0.25f + c2 - fry2;
   }
 
-  // gather (e_part.inc / b_part.inc): field = Re sum_m e^{-i m theta} F_m
+  // gather (e_part.inc / b_part.inc): field = Re sum_m e^{-i m theta} F_m;
+  // mode 0 contributes Re F_0 alone, so its sums are real
   float exr = 0.f, er_ = 0.f, etr = 0.f, bxr = 0.f, brr = 0.f, btr = 0.f;
   {
+#define GET(q, m, x, y) Gather<M, SHARED>::get(F, tile, q, m, x, y)
+#pragma unroll
+    for (int jj = 0; jj < 3; ++jj) {
+      float rex = 0.f, rer = 0.f, ret = 0.f, rbr = 0.f, rbt = 0.f, rbx = 0.f;
+#pragma unroll
+      for (int ii = 0; ii < 3; ++ii) {
+        // Ex, Br at (cx1, cy2); Er, Bx at (cx2, cy1); Et at (cx2, cy2); Bt at (cx1, cy1)
+        rex = fmaf(gx[ii], GET(0, 0, cx1 - 1 + ii, cy2 - 1 + jj).re, rex);
+        rbr = fmaf(gx[ii], GET(4, 0, cx1 - 1 + ii, cy2 - 1 + jj).re, rbr);
+        rer = fmaf(hx[ii], GET(1, 0, cx2 - 1 + ii, cy1 - 1 + jj).re, rer);
+        rbx = fmaf(hx[ii], GET(3, 0, cx2 - 1 + ii, cy1 - 1 + jj).re, rbx);
+        ret = fmaf(hx[ii], GET(2, 0, cx2 - 1 + ii, cy2 - 1 + jj).re, ret);
+        rbt = fmaf(gx[ii], GET(5, 0, cx1 - 1 + ii, cy1 - 1 + jj).re, rbt);
+      }
+      exr = fmaf(hy[jj], rex, exr);
+      brr = fmaf(hy[jj], rbr, brr);
+      er_ = fmaf(gy[jj], rer, er_);
+      bxr = fmaf(gy[jj], rbx, bxr);
+      etr = fmaf(hy[jj], ret, etr);
+      btr = fmaf(gy[jj], rbt, btr);
+    }
     f2 emi = fm(1.f, 0.f);
     const f2 e1 = fm(ct, -st);
 #pragma unroll
-    for (int m = 0; m < M; ++m) {
+    for (int m = 1; m < M; ++m) {
+      emi = emi * e1;
       f2 aex = fm(0, 0), aer = fm(0, 0), aet = fm(0, 0), abx = fm(0, 0), abr = fm(0, 0), abt = fm(0, 0);
 #pragma unroll
       for (int jj = 0; jj < 3; ++jj) {
-        f2 rex = fm(0, 0), rer = fm(0, 0), ret = fm(0, 0), rbr = fm(0, 0), rbt = fm(0, 0);
+        f2 rex = fm(0, 0), rer = fm(0, 0), ret = fm(0, 0), rbr = fm(0, 0), rbt = fm(0, 0), rbx = fm(0, 0);
 #pragma unroll
         for (int ii = 0; ii < 3; ++ii) {
-          // Ex, Br at (cx1, cy2); Er, Bx at (cx2, cy1); Et at (cx2, cy2); Bt at (cx1, cy1)
-          rex = rex + gx[ii] * Gather<M, SHARED>::get(F, tile, 0, m, cx1 - 1 + ii, cy2 - 1 + jj);
-          rbr = rbr + gx[ii] * Gather<M, SHARED>::get(F, tile, 4, m, cx1 - 1 + ii, cy2 - 1 + jj);
-          rer = rer + hx[ii] * Gather<M, SHARED>::get(F, tile, 1, m, cx2 - 1 + ii, cy1 - 1 + jj);
-          const f2 vbx = Gather<M, SHARED>::get(F, tile, 3, m, cx2 - 1 + ii, cy1 - 1 + jj);
-          abx = abx + (gy[jj] * hx[ii]) * vbx;
-          ret = ret + hx[ii] * Gather<M, SHARED>::get(F, tile, 2, m, cx2 - 1 + ii, cy2 - 1 + jj);
-          rbt = rbt + gx[ii] * Gather<M, SHARED>::get(F, tile, 5, m, cx1 - 1 + ii, cy1 - 1 + jj);
+          rex = rex + gx[ii] * GET(0, m, cx1 - 1 + ii, cy2 - 1 + jj);
+          rbr = rbr + gx[ii] * GET(4, m, cx1 - 1 + ii, cy2 - 1 + jj);
+          rer = rer + hx[ii] * GET(1, m, cx2 - 1 + ii, cy1 - 1 + jj);
+          rbx = rbx + hx[ii] * GET(3, m, cx2 - 1 + ii, cy1 - 1 + jj);
+          ret = ret + hx[ii] * GET(2, m, cx2 - 1 + ii, cy2 - 1 + jj);
+          rbt = rbt + gx[ii] * GET(5, m, cx1 - 1 + ii, cy1 - 1 + jj);
         }
         aex = aex + hy[jj] * rex;
         abr = abr + hy[jj] * rbr;
         aer = aer + gy[jj] * rer;
+        abx = abx + gy[jj] * rbx;
         aet = aet + hy[jj] * ret;
         abt = abt + gy[jj] * rbt;
       }
-      exr += (emi * aex).re;
-      er_ += (emi * aer).re;
-      etr += (emi * aet).re;
-      bxr += (emi * abx).re;
-      brr += (emi * abr).re;
-      btr += (emi * abt).re;
-      emi = emi * e1;
+      // Re(emi * a) = emi.re a.re - emi.im a.im
+      exr += emi.re * aex.re - emi.im * aex.im;
+      er_ += emi.re * aer.re - emi.im * aer.im;
+      etr += emi.re * aet.re - emi.im * aet.im;
+      bxr += emi.re * abx.re - emi.im * abx.im;
+      brr += emi.re * abr.re - emi.im * abr.im;
+      btr += emi.re * abt.re - emi.im * abt.im;
     }
+#undef GET
   }
   if (!isfinite(exr + er_ + etr + bxr + brr + btr)) {
     atomicOr(P.err, ERR_NONFINITE);
@@ -472,14 +529,7 @@ __device__ __forceinline__ bool push_one(int64_t i, const SpeciesPtrs& sp, Speci
   const f2 edt = fm(c3, s3) * fm(ct, -st);
   const float dth = atan2f(z3, y3) - atan2f(z, y);
   if (SHARED) {
-    // 3 x 3 cells when no lane of the warp changes cell, else a 4 x 4 window
-    // that holds the reference's xmin..xmax, ymin..ymax range (the extra row
-    // or column carries zero flux)
-    if (__all_sync(__activemask(), dcx == 0 && dcy == 0))
-      deposit_tile<M, 3>(tile, og, oh, dgx, dgy, -1, -1, cx2, cy2, fc, fcz, e05, edt, dth);
-    else
-      deposit_tile<M, 4>(tile, og, oh, dgx, dgy, dcx < 0 ? -2 : -1, dcy < 0 ? -2 : -1, cx2, cy2, fc, fcz, e05,
-                         edt, dth);
+    deposit_tile_warp<M>(tile, og, oh, dgx, dgy, dcx, dcy, cx2, cy2, fc, fcz, e05, edt, dth);
   } else {
     deposit_global<M>(F, P, og, oh, dgx, dgy, dcx, dcy, cx2, cy2, fc, fcz, e05, edt, dth);
   }
@@ -563,16 +613,17 @@ __global__ void __launch_bounds__(PUSH_THREADS, PUSH_MIN_BLOCKS) k_push_tiles(Fi
   set_bounds(P, rec, rc);
   const int ntiles = tt->ntiles;
   const int ntx = tt->ntx;
-  // static round-robin over tiles; every thread evaluates the same tile
-  // conditions, so all threads meet the same barriers
-  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+  // static round-robin over the tiles in decreasing order of particle count
+  // (longest first); every thread evaluates the same tile conditions, so all
+  // threads meet the same barriers
+  for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x) {
+    const int t = tt->order[ti];
     const int64_t p0 = tt->start[t], p1 = tt->start[t + 1];
     Tile tile;
     tile.sf = sf;
     tile.sj = sj;
     tile.x0 = (tt->tx_min + t % ntx) * TILE_X - nsh + 1 - DRIFT - 2;
     tile.y0 = (t / ntx) * TILE_Y + 1 - DRIFT - 2;
-    tile_scales(tile, p1 - p0, qw_max, P.idt, P.c);
     const bool inside = tile.x0 >= 1 - NG && tile.x0 + RW - 1 <= rc.nx + NG && tile.y0 >= 1 - NG &&
                         tile.y0 + RH - 1 <= rc.ny + NG;
     if (p1 <= p0) continue;
@@ -594,6 +645,7 @@ __global__ void __launch_bounds__(PUSH_THREADS, PUSH_MIN_BLOCKS) k_push_tiles(Fi
               *reinterpret_cast<const float2*>(v.ptr(tile.x0 + c % RW, tile.y0 + c / RW, m));
     }
     for (int e = threadIdx.x; e < 3 * M * 4 * RCELLS; e += PUSH_THREADS) sj[e] = 0;
+    tile_scales(tile, p1 - p0, qw_max, P.idt, P.c);
     __syncthreads();
     for (int64_t i = p0 + threadIdx.x; i < p1; i += PUSH_THREADS) {
       if (!push_one<M, true>(i, sp, cnt, F, P, rc, tile, nsh, apply_bcs))
@@ -666,7 +718,6 @@ void launch_push_mixed(cudaStream_t s, const FieldSetF& F, const SpeciesPtrs& sp
                        const StepRec* rec, const RunConst& rc, int apply_bcs, int nblocks_tiles,
                        int nblocks_global, const MixedParams& P, TileTable* tt) {
   const size_t smem = push_mixed_smem(rc.M);
-  cudaMemsetAsync(&tt->next, 0, sizeof(int), s);
   cudaMemsetAsync(P.fb_count, 0, sizeof(int), s);
   switch (rc.M) {
 #define CASE(MM)                                                                                    \

@@ -11,15 +11,16 @@ constexpr int TILE_X = 16;  // cells per tile along x
 constexpr int TILE_Y = 8;   // cells per tile along r
 
 // Particles sorted by tile: tile t owns slots [start[t], start[t+1]);
-// slots [n_sorted, n_used) were appended after the sort.
+// slots [n_sorted, n_used) were appended after the sort.  order[] lists the
+// tiles by decreasing particle count (the push deals them to its CTAs
+// round-robin in that order, a longest-first static schedule).
 struct TileTable {
-  int next;       // persistent-kernel work counter
   int ntiles;
   int ntx, nty;
   int tx_min;     // absolute tile column of tile 0
-  int pad;
   int64_t n_sorted;
   int64_t* start;  // ntiles + 1
+  int32_t* order;  // ntiles
 };
 
 struct MixedParams {
@@ -59,7 +60,7 @@ void mixed_particle_bcs(cudaStream_t s, const SpeciesPtrs& sp, SpeciesCounters* 
                         const RunConst& rc, int nblocks);
 void mixed_energy(cudaStream_t s, const SpeciesPtrs& sp, const SpeciesCounters* cnt, double* out, int nblocks);
 void mixed_sort(cudaStream_t s, const SpeciesPtrs& sp, SpeciesCounters* cnt, SortScratch& sc, TileTable* tt,
-                int64_t* tile_start, const StepRec* rec, const RunConst& rc, int nblocks);
+                int64_t* tile_start, int32_t* tile_order, const StepRec* rec, const RunConst& rc, int nblocks);
 void mixed_cell_indices(cudaStream_t s, const SpeciesPtrs& sp, const SpeciesCounters* cnt, double xg0,
                         double x_grid_min, const RunConst& rc, int32_t* cx, int32_t* cy, int32_t* live,
                         int nblocks);
