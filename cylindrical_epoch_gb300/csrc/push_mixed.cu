@@ -45,6 +45,14 @@ __device__ __forceinline__ f2 operator+(f2 a, f2 b) { return {a.re + b.re, a.im 
 __device__ __forceinline__ f2 operator-(f2 a, f2 b) { return {a.re - b.re, a.im - b.im}; }
 __device__ __forceinline__ f2 operator*(float s, f2 a) { return {s * a.re, s * a.im}; }
 
+// Paired FP32 arithmetic (one FFMA2 / FMUL2 instruction for two lanes of
+// FP32 work): acc + s v and s v for a scalar s and a pair v.
+__device__ __forceinline__ float2 pfma(float s, float2 v, float2 acc) { return __ffma2_rn(make_float2(s, s), v, acc); }
+__device__ __forceinline__ float2 pfma(float2 s, float2 v, float2 acc) { return __ffma2_rn(s, v, acc); }
+__device__ __forceinline__ float2 pmul(float s, float2 v) { return __fmul2_rn(make_float2(s, s), v); }
+__device__ __forceinline__ float2 P2(f2 a) { return make_float2(a.re, a.im); }
+__device__ __forceinline__ f2 U2(float2 a) { return {a.x, a.y}; }
+
 // f2(phi) = -i (e^{i phi} - 1)/phi, f3 = (e^{i phi}(1 - i phi) - 1)/phi^2,
 // f4 = i (e^{i phi}(2 - 2 i phi - phi^2) - 2)/phi^3: the per-mode deposit
 // factors of particles.F90:603-625 without the 2 e^{i m theta0} prefactor.
@@ -80,8 +88,9 @@ __device__ __forceinline__ void mode_factors(float phi, f2 eip, f2& F2, f2& F3, 
   }
 }
 
-// Shared-memory layout: fields [6][M][RCELLS] float2; current accumulators
-// [3][M][re, im][hi, lo][RCELLS] int32 (fixed point, see sadd).
+// Shared-memory layout: staged fields (planes of RCELLS cells, see Gather);
+// current accumulators [3][M][re, im][hi, lo][RCELLS] int32 (fixed point,
+// see sadd).
 struct Tile {
   const float2* sf;
   int* sj;
@@ -105,20 +114,52 @@ __device__ __forceinline__ void tile_scales(Tile& t, int64_t n, float qw_max, fl
   t.s_t = bt > 0.f ? 1073741824.0f / bt : 0.f;
 }
 
+// Staged fields of a tile, in shared memory (RCELLS cells per plane):
+//   plane 0: float2 {Re Ex_0, Re Br_0}   plane 1: float2 {Re Er_0, Re Bx_0}
+//   plane 2: float {Re Et_0} then float {Re Bt_0} (one float2 plane)
+//   planes 3..: float2 complex F_m of field q, m >= 1, at 3 + q (M-1) + m - 1
+// Mode 0 contributes Re F_0 alone; Ex and Br share their stencil (gx along
+// x at cell_x1, hy along r at cell_y2), and so do Er and Bx (hx at cell_x2,
+// gy at cell_y1), so each pair is gathered by one 64-bit load and one
+// paired FMA.
+constexpr int PLANES_M0 = 3;
+template <int M>
+constexpr int staged_planes() { return PLANES_M0 + 6 * (M - 1); }
+
 template <int M, bool SHARED>
 struct Gather {
   // SHARED: read from the staged tile; else from the FP32 global arrays
-  __device__ __forceinline__ static f2 get(const FieldSetF& F, const Tile& t, int q, int m, int x, int y) {
-    if (SHARED) {
-      const float2 v = t.sf[(q * M + m) * RCELLS + (y - t.y0) * RW + (x - t.x0)];
-      return fm(v.x, v.y);
-    } else {
-      const cplxf* base = (q == 0) ? F.ex.p : (q == 1) ? F.er.p : (q == 2) ? F.et.p : (q == 3) ? F.bx.p
-                        : (q == 4) ? F.br.p : F.bt.p;
-      const FViewF fv{const_cast<cplxf*>(base), F.ex.nxg, F.ex.nyg};
-      const float2 v = *reinterpret_cast<const float2*>(fv.ptr(x, y, m));
-      return fm(v.x, v.y);
-    }
+  __device__ __forceinline__ static FViewF view(const FieldSetF& F, int q) {
+    const cplxf* base = (q == 0) ? F.ex.p : (q == 1) ? F.er.p : (q == 2) ? F.et.p : (q == 3) ? F.bx.p
+                      : (q == 4) ? F.br.p : F.bt.p;
+    return FViewF{const_cast<cplxf*>(base), F.ex.nxg, F.ex.nyg};
+  }
+  __device__ __forceinline__ static float re0(const FieldSetF& F, int q, int x, int y) {
+    return view(F, q).ptr(x, y, 0)->re;
+  }
+  __device__ __forceinline__ static int cell(const Tile& t, int x, int y) { return (y - t.y0) * RW + (x - t.x0); }
+  // {Re Ex_0, Re Br_0} at (x, y)
+  __device__ __forceinline__ static float2 eb0(const FieldSetF& F, const Tile& t, int x, int y) {
+    if (SHARED) return t.sf[cell(t, x, y)];
+    return make_float2(re0(F, 0, x, y), re0(F, 4, x, y));
+  }
+  // {Re Er_0, Re Bx_0} at (x, y)
+  __device__ __forceinline__ static float2 rx0(const FieldSetF& F, const Tile& t, int x, int y) {
+    if (SHARED) return t.sf[RCELLS + cell(t, x, y)];
+    return make_float2(re0(F, 1, x, y), re0(F, 3, x, y));
+  }
+  __device__ __forceinline__ static float et0(const FieldSetF& F, const Tile& t, int x, int y) {
+    if (SHARED) return reinterpret_cast<const float*>(t.sf + 2 * RCELLS)[cell(t, x, y)];
+    return re0(F, 2, x, y);
+  }
+  __device__ __forceinline__ static float bt0(const FieldSetF& F, const Tile& t, int x, int y) {
+    if (SHARED) return reinterpret_cast<const float*>(t.sf + 2 * RCELLS)[RCELLS + cell(t, x, y)];
+    return re0(F, 5, x, y);
+  }
+  // complex F_m of field q (m >= 1)
+  __device__ __forceinline__ static float2 get(const FieldSetF& F, const Tile& t, int q, int m, int x, int y) {
+    if (SHARED) return t.sf[(PLANES_M0 + q * (M - 1) + m - 1) * RCELLS + cell(t, x, y)];
+    return *reinterpret_cast<const float2*>(view(F, q).ptr(x, y, m));
   }
 };
 
@@ -178,6 +219,20 @@ __device__ __forceinline__ void sadd(int* p, float v) {
   if (lo_i != 0) atomicAdd(p + RCELLS, lo_i);
 }
 
+// sadd for the real and imaginary parts of one complex value at once (the
+// same split, computed with paired FP32 instructions).
+__device__ __forceinline__ void sadd2(int* pr, int* pi, float2 v) {
+  const float2 t = __ffma2_rn(v, make_float2(1.0f / 32768.0f, 1.0f / 32768.0f), make_float2(FXP_MAGIC, FXP_MAGIC));
+  const int hr = __float_as_int(t.x) - FXP_MAGIC_BITS, hi = __float_as_int(t.y) - FXP_MAGIC_BITS;
+  const float2 d = __fadd2_rn(t, make_float2(-FXP_MAGIC, -FXP_MAGIC));
+  const float2 lo = __fadd2_rn(__ffma2_rn(d, make_float2(-32768.0f, -32768.0f), v), make_float2(FXP_MAGIC, FXP_MAGIC));
+  const int lr = __float_as_int(lo.x) - FXP_MAGIC_BITS, li = __float_as_int(lo.y) - FXP_MAGIC_BITS;
+  if (hr != 0) atomicAdd(pr, hr);
+  if (lr != 0) atomicAdd(pr + RCELLS, lr);
+  if (hi != 0) atomicAdd(pi, hi);
+  if (li != 0) atomicAdd(pi + RCELLS, li);
+}
+
 // Deposit into the tile accumulators over a WX x WY window whose first cell
 // is (cx2 + x0, cy2 + y0); x0, y0 in {-2, -1} select the offsets -2..2 of the
 // weight arrays (a 3-cell extent always starts at -1).  The accumulators are
@@ -212,21 +267,23 @@ __device__ __forceinline__ void deposit_tile(const Tile& tile, const float* og, 
     int* const ax = sj + ((0 * M + m) * 4) * RCELLS;
     int* const ar = sj + ((1 * M + m) * 4) * RCELLS;
     int* const at = sj + ((2 * M + m) * 4) * RCELLS;
-    f2 qr[WX];
+    const float2 F2p = P2(F2), F3p = P2(F3), F4p = P2(F4);
+    float2 qr[WX];
 #pragma unroll
-    for (int c = 0; c < WX; ++c) qr[c] = fm(0.f, 0.f);
+    for (int c = 0; c < WX; ++c) qr[c] = make_float2(0.f, 0.f);
 #pragma unroll
     for (int r = 0; r < WY; ++r) {
       const float gyv = gyw[r], hyv = hyw[r];
-      f2 w_rt, ym1;
+      const float nfy = -(fcs * hyv);
+      float2 w_rt, ym1;
       if (m == 0) {
-        w_rt = fm(gyv + 0.5f * hyv, 0.f);
-        ym1 = fm(0.5f * gyv + third * hyv, 0.f);
+        w_rt = make_float2(gyv + 0.5f * hyv, 0.f);
+        ym1 = make_float2(0.5f * gyv + third * hyv, 0.f);
       } else {
-        w_rt = gyv * F2 + hyv * F3;
-        ym1 = gyv * F3 + hyv * F4;
+        w_rt = pfma(gyv, F2p, pmul(hyv, F3p));
+        ym1 = pfma(gyv, F3p, pmul(hyv, F4p));
       }
-      f2 qx = fm(0.f, 0.f);
+      float2 qx = make_float2(0.f, 0.f);
 #pragma unroll
       for (int c = 0; c < WX; ++c) {
         const float gxv = gxw[c], hxv = hxw[c];
@@ -237,28 +294,20 @@ __device__ __forceinline__ void deposit_tile(const Tile& tile, const float* og, 
         // those adds are left out.
         if (m == 0) {
           const float w_xt = gxv + 0.5f * hxv;
-          const float w_xr = gxv * w_rt.re + hxv * ym1.re;
-          qx.re = qx.re - (fcs * hxv) * w_rt.re;
-          qr[c].re = qr[c].re - (fcs * hyv) * w_xt;
-          if (c < WX - 1) sadd(ax + cell + 1, qx.re);       // jx at (cx + 1, cy)
-          if (r < WY - 1) sadd(ar + cell + RW, qr[c].re);  // jr at (cx, cy + 1)
-          sadd(at + cell, fczs * w_xr);                     // jtheta at (cx, cy)
+          const float w_xr = gxv * w_rt.x + hxv * ym1.x;
+          qx.x = qx.x - (fcs * hxv) * w_rt.x;
+          qr[c].x = qr[c].x + nfy * w_xt;
+          if (c < WX - 1) sadd(ax + cell + 1, qx.x);       // jx at (cx + 1, cy)
+          if (r < WY - 1) sadd(ar + cell + RW, qr[c].x);  // jr at (cx, cy + 1)
+          sadd(at + cell, fczs * w_xr);                    // jtheta at (cx, cy)
         } else {
-          const f2 w_xt = gxv * F2 + hxv * F3;
-          const f2 w_xr = gxv * w_rt + hxv * ym1;
-          qx = qx - (fcs * hxv) * w_rt;
-          qr[c] = qr[c] - (fcs * hyv) * w_xt;
-          const f2 qt = fczs * w_xr;
-          if (c < WX - 1) {
-            sadd(ax + cell + 1, qx.re);
-            sadd(ax + 2 * RCELLS + cell + 1, qx.im);
-          }
-          if (r < WY - 1) {
-            sadd(ar + cell + RW, qr[c].re);
-            sadd(ar + 2 * RCELLS + cell + RW, qr[c].im);
-          }
-          sadd(at + cell, qt.re);
-          sadd(at + 2 * RCELLS + cell, qt.im);
+          const float2 w_xt = pfma(gxv, F2p, pmul(hxv, F3p));
+          const float2 w_xr = pfma(gxv, w_rt, pmul(hxv, ym1));
+          qx = pfma(-(fcs * hxv), w_rt, qx);
+          qr[c] = pfma(nfy, w_xt, qr[c]);
+          if (c < WX - 1) sadd2(ax + cell + 1, ax + 2 * RCELLS + cell + 1, qx);
+          if (r < WY - 1) sadd2(ar + cell + RW, ar + 2 * RCELLS + cell + RW, qr[c]);
+          sadd2(at + cell, at + 2 * RCELLS + cell, pmul(fczs, w_xr));
         }
       }
     }
@@ -391,65 +440,63 @@ __device__ __forceinline__ bool push_one(int64_t i, const SpeciesPtrs& sp, Speci
     hy[0] = 0.25f + c2 + fry2; hy[1] = 1.5f - 2.0f * c2; hy[2] = 0.25f + c2 - fry2;
   }
 
-  // gather (e_part.inc / b_part.inc): field = Re sum_m e^{-i m theta} F_m;
-  // mode 0 contributes Re F_0 alone, so its sums are real
-  float exr = 0.f, er_ = 0.f, etr = 0.f, bxr = 0.f, brr = 0.f, btr = 0.f;
+  // gather (e_part.inc / b_part.inc): field = Re sum_m e^{-i m theta} F_m
+  float exr, er_, etr, bxr, brr, btr;
   {
-#define GET(q, m, x, y) Gather<M, SHARED>::get(F, tile, q, m, x, y)
+    using G = Gather<M, SHARED>;
+    // mode 0: (Ex, Br), (Er, Bx) and (Et, Bt) as pairs
+    float2 aEB = make_float2(0.f, 0.f), aRX = aEB, aTB = aEB;
 #pragma unroll
     for (int jj = 0; jj < 3; ++jj) {
-      float rex = 0.f, rer = 0.f, ret = 0.f, rbr = 0.f, rbt = 0.f, rbx = 0.f;
+      float2 rEB = make_float2(0.f, 0.f), rRX = rEB, rTB = rEB;
 #pragma unroll
       for (int ii = 0; ii < 3; ++ii) {
         // Ex, Br at (cx1, cy2); Er, Bx at (cx2, cy1); Et at (cx2, cy2); Bt at (cx1, cy1)
-        rex = fmaf(gx[ii], GET(0, 0, cx1 - 1 + ii, cy2 - 1 + jj).re, rex);
-        rbr = fmaf(gx[ii], GET(4, 0, cx1 - 1 + ii, cy2 - 1 + jj).re, rbr);
-        rer = fmaf(hx[ii], GET(1, 0, cx2 - 1 + ii, cy1 - 1 + jj).re, rer);
-        rbx = fmaf(hx[ii], GET(3, 0, cx2 - 1 + ii, cy1 - 1 + jj).re, rbx);
-        ret = fmaf(hx[ii], GET(2, 0, cx2 - 1 + ii, cy2 - 1 + jj).re, ret);
-        rbt = fmaf(gx[ii], GET(5, 0, cx1 - 1 + ii, cy1 - 1 + jj).re, rbt);
+        rEB = pfma(gx[ii], G::eb0(F, tile, cx1 - 1 + ii, cy2 - 1 + jj), rEB);
+        rRX = pfma(hx[ii], G::rx0(F, tile, cx2 - 1 + ii, cy1 - 1 + jj), rRX);
+        rTB = pfma(make_float2(hx[ii], gx[ii]),
+                   make_float2(G::et0(F, tile, cx2 - 1 + ii, cy2 - 1 + jj), G::bt0(F, tile, cx1 - 1 + ii, cy1 - 1 + jj)),
+                   rTB);
       }
-      exr = fmaf(hy[jj], rex, exr);
-      brr = fmaf(hy[jj], rbr, brr);
-      er_ = fmaf(gy[jj], rer, er_);
-      bxr = fmaf(gy[jj], rbx, bxr);
-      etr = fmaf(hy[jj], ret, etr);
-      btr = fmaf(gy[jj], rbt, btr);
+      aEB = pfma(hy[jj], rEB, aEB);
+      aRX = pfma(gy[jj], rRX, aRX);
+      aTB = pfma(make_float2(hy[jj], gy[jj]), rTB, aTB);
     }
+    exr = aEB.x; brr = aEB.y; er_ = aRX.x; bxr = aRX.y; etr = aTB.x; btr = aTB.y;
+    // modes m >= 1: complex sums, then Re(e^{-i m theta} F_m)
     f2 emi = fm(1.f, 0.f);
     const f2 e1 = fm(ct, -st);
 #pragma unroll
     for (int m = 1; m < M; ++m) {
       emi = emi * e1;
-      f2 aex = fm(0, 0), aer = fm(0, 0), aet = fm(0, 0), abx = fm(0, 0), abr = fm(0, 0), abt = fm(0, 0);
+      float2 aex = make_float2(0.f, 0.f), aer = aex, aet = aex, abx = aex, abr = aex, abt = aex;
 #pragma unroll
       for (int jj = 0; jj < 3; ++jj) {
-        f2 rex = fm(0, 0), rer = fm(0, 0), ret = fm(0, 0), rbr = fm(0, 0), rbt = fm(0, 0), rbx = fm(0, 0);
+        float2 rex = make_float2(0.f, 0.f), rer = rex, ret = rex, rbr = rex, rbt = rex, rbx = rex;
 #pragma unroll
         for (int ii = 0; ii < 3; ++ii) {
-          rex = rex + gx[ii] * GET(0, m, cx1 - 1 + ii, cy2 - 1 + jj);
-          rbr = rbr + gx[ii] * GET(4, m, cx1 - 1 + ii, cy2 - 1 + jj);
-          rer = rer + hx[ii] * GET(1, m, cx2 - 1 + ii, cy1 - 1 + jj);
-          rbx = rbx + hx[ii] * GET(3, m, cx2 - 1 + ii, cy1 - 1 + jj);
-          ret = ret + hx[ii] * GET(2, m, cx2 - 1 + ii, cy2 - 1 + jj);
-          rbt = rbt + gx[ii] * GET(5, m, cx1 - 1 + ii, cy1 - 1 + jj);
+          rex = pfma(gx[ii], G::get(F, tile, 0, m, cx1 - 1 + ii, cy2 - 1 + jj), rex);
+          rbr = pfma(gx[ii], G::get(F, tile, 4, m, cx1 - 1 + ii, cy2 - 1 + jj), rbr);
+          rer = pfma(hx[ii], G::get(F, tile, 1, m, cx2 - 1 + ii, cy1 - 1 + jj), rer);
+          rbx = pfma(hx[ii], G::get(F, tile, 3, m, cx2 - 1 + ii, cy1 - 1 + jj), rbx);
+          ret = pfma(hx[ii], G::get(F, tile, 2, m, cx2 - 1 + ii, cy2 - 1 + jj), ret);
+          rbt = pfma(gx[ii], G::get(F, tile, 5, m, cx1 - 1 + ii, cy1 - 1 + jj), rbt);
         }
-        aex = aex + hy[jj] * rex;
-        abr = abr + hy[jj] * rbr;
-        aer = aer + gy[jj] * rer;
-        abx = abx + gy[jj] * rbx;
-        aet = aet + hy[jj] * ret;
-        abt = abt + gy[jj] * rbt;
+        aex = pfma(hy[jj], rex, aex);
+        abr = pfma(hy[jj], rbr, abr);
+        aer = pfma(gy[jj], rer, aer);
+        abx = pfma(gy[jj], rbx, abx);
+        aet = pfma(hy[jj], ret, aet);
+        abt = pfma(gy[jj], rbt, abt);
       }
       // Re(emi * a) = emi.re a.re - emi.im a.im
-      exr += emi.re * aex.re - emi.im * aex.im;
-      er_ += emi.re * aer.re - emi.im * aer.im;
-      etr += emi.re * aet.re - emi.im * aet.im;
-      bxr += emi.re * abx.re - emi.im * abx.im;
-      brr += emi.re * abr.re - emi.im * abr.im;
-      btr += emi.re * abt.re - emi.im * abt.im;
+      exr += emi.re * aex.x - emi.im * aex.y;
+      er_ += emi.re * aer.x - emi.im * aer.y;
+      etr += emi.re * aet.x - emi.im * aet.y;
+      bxr += emi.re * abx.x - emi.im * abx.y;
+      brr += emi.re * abr.x - emi.im * abr.y;
+      btr += emi.re * abt.x - emi.im * abt.y;
     }
-#undef GET
   }
   if (!isfinite(exr + er_ + etr + bxr + brr + btr)) {
     atomicOr(P.err, ERR_NONFINITE);
@@ -606,8 +653,8 @@ __global__ void __launch_bounds__(PUSH_THREADS, PUSH_MIN_BLOCKS) k_push_tiles(Fi
                                                              const StepRec* rec, RunConst rc, MixedParams P,
                                                              TileTable* tt, int apply_bcs) {
   extern __shared__ float4 smem4[];
-  float2* sf = reinterpret_cast<float2*>(smem4);        // 6 * M * RCELLS float2
-  int* sj = reinterpret_cast<int*>(sf + 6 * M * RCELLS);  // 3 * M * 4 * RCELLS int32
+  float2* sf = reinterpret_cast<float2*>(smem4);                       // staged_planes<M>() * RCELLS float2
+  int* sj = reinterpret_cast<int*>(sf + staged_planes<M>() * RCELLS);  // 3 * M * 4 * RCELLS int32
   const int nsh = rec->nshift_total;
   const float qw_max = fabsf(P.q_fac) * __uint_as_float(cnt->wmax_bits);
   set_bounds(P, rec, rc);
@@ -632,17 +679,27 @@ __global__ void __launch_bounds__(PUSH_THREADS, PUSH_MIN_BLOCKS) k_push_tiles(Fi
       for (int64_t i = p0 + threadIdx.x; i < p1; i += PUSH_THREADS) P.fb_list[atomicAdd(P.fb_count, 1)] = (int)i;
       continue;
     }
-    // stage E and B (FP32) and clear the accumulators
+    // stage E and B (FP32; mode 0 as real pairs, see Gather) and clear the
+    // accumulators
+    {
+      using G = Gather<M, false>;
+      float* s_t = reinterpret_cast<float*>(sf + 2 * RCELLS);
+      for (int c = threadIdx.x; c < RCELLS; c += PUSH_THREADS) {
+        const int x = tile.x0 + c % RW, y = tile.y0 + c / RW;
+        sf[c] = make_float2(G::re0(F, 0, x, y), G::re0(F, 4, x, y));
+        sf[RCELLS + c] = make_float2(G::re0(F, 1, x, y), G::re0(F, 3, x, y));
+        s_t[c] = G::re0(F, 2, x, y);
+        s_t[RCELLS + c] = G::re0(F, 5, x, y);
+      }
 #pragma unroll 1
-    for (int q = 0; q < 6; ++q) {
-      const cplxf* base = (q == 0) ? F.ex.p : (q == 1) ? F.er.p : (q == 2) ? F.et.p
-                        : (q == 3) ? F.bx.p : (q == 4) ? F.br.p : F.bt.p;
-      const FViewF v{const_cast<cplxf*>(base), F.ex.nxg, F.ex.nyg};
+      for (int q = 0; q < 6; ++q) {
+        const FViewF v = G::view(F, q);
 #pragma unroll 1
-      for (int m = 0; m < M; ++m)
-        for (int c = threadIdx.x; c < RCELLS; c += PUSH_THREADS)
-          sf[(q * M + m) * RCELLS + c] =
-              *reinterpret_cast<const float2*>(v.ptr(tile.x0 + c % RW, tile.y0 + c / RW, m));
+        for (int m = 1; m < M; ++m)
+          for (int c = threadIdx.x; c < RCELLS; c += PUSH_THREADS)
+            sf[(PLANES_M0 + q * (M - 1) + m - 1) * RCELLS + c] =
+                *reinterpret_cast<const float2*>(v.ptr(tile.x0 + c % RW, tile.y0 + c / RW, m));
+      }
     }
     for (int e = threadIdx.x; e < 3 * M * 4 * RCELLS; e += PUSH_THREADS) sj[e] = 0;
     tile_scales(tile, p1 - p0, qw_max, P.idt, P.c);
@@ -694,7 +751,9 @@ __global__ void __launch_bounds__(PUSH_THREADS) k_push_global(FieldSetF F, Speci
   }
 }
 
-size_t push_mixed_smem(int M) { return (size_t)6 * M * RCELLS * sizeof(float2) + (size_t)12 * M * RCELLS * sizeof(int); }
+size_t push_mixed_smem(int M) {
+  return (size_t)(PLANES_M0 + 6 * (M - 1)) * RCELLS * sizeof(float2) + (size_t)12 * M * RCELLS * sizeof(int);
+}
 
 int push_mixed_blocks_per_sm(int M) {
   const size_t smem = push_mixed_smem(M);
