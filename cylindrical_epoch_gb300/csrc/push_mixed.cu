@@ -208,6 +208,13 @@ struct ModeWalk {
 // add is that of rounding v to FP32 plus at most 1/2 unit.  Integer
 // shared-memory adds are single native instructions (FP32 shared-memory
 // adds are not).
+__device__ __forceinline__ void red_hi(int* p, int v) {
+  asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.s32 q, %1, 0;\n\t@q red.shared.add.s32 [%0], %1;\n\t}" ::"r"(
+                   (unsigned)__cvta_generic_to_shared(p)), "r"(v));
+}
+__device__ __forceinline__ void red_lo(int* p, int v) {
+  asm volatile("red.shared.add.s32 [%0], %1;" ::"r"((unsigned)__cvta_generic_to_shared(p)), "r"(v));
+}
 constexpr float FXP_MAGIC = 12582912.0f;  // 1.5 * 2^23
 constexpr int FXP_MAGIC_BITS = 0x4B400000;
 __device__ __forceinline__ void sadd(int* p, float v) {
@@ -215,8 +222,8 @@ __device__ __forceinline__ void sadd(int* p, float v) {
   const int hi = __float_as_int(t) - FXP_MAGIC_BITS;
   const float lo = fmaf(-(t - FXP_MAGIC), 32768.0f, v);
   const int lo_i = __float_as_int(lo + FXP_MAGIC) - FXP_MAGIC_BITS;
-  if (hi != 0) atomicAdd(p, hi);
-  if (lo_i != 0) atomicAdd(p + RCELLS, lo_i);
+  red_hi(p, hi);
+  red_lo(p + RCELLS, lo_i);
 }
 
 // sadd for the real and imaginary parts of one complex value at once (the
@@ -227,10 +234,10 @@ __device__ __forceinline__ void sadd2(int* pr, int* pi, float2 v) {
   const float2 d = __fadd2_rn(t, make_float2(-FXP_MAGIC, -FXP_MAGIC));
   const float2 lo = __fadd2_rn(__ffma2_rn(d, make_float2(-32768.0f, -32768.0f), v), make_float2(FXP_MAGIC, FXP_MAGIC));
   const int lr = __float_as_int(lo.x) - FXP_MAGIC_BITS, li = __float_as_int(lo.y) - FXP_MAGIC_BITS;
-  if (hr != 0) atomicAdd(pr, hr);
-  if (lr != 0) atomicAdd(pr + RCELLS, lr);
-  if (hi != 0) atomicAdd(pi, hi);
-  if (li != 0) atomicAdd(pi + RCELLS, li);
+  red_hi(pr, hr);
+  red_lo(pr + RCELLS, lr);
+  red_hi(pi, hi);
+  red_lo(pi + RCELLS, li);
 }
 
 // Deposit into the tile accumulators over a WX x WY window whose first cell
