@@ -321,6 +321,9 @@ def main():
     parts, rng = cg.host_load(deck)
     run = cg.Run(deck, particles=parts, rng=rng)
     graph = not args.eager
+    tile = None
+    if form == "mixed":
+        tile = run.tune_tiles()  # the push tile shape, timed on the initial state
 
     run.step(args.warmup, graph=False)
     run.kernel_timing()  # reset counters
@@ -429,7 +432,7 @@ def main():
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if form == "fp64" else "f32+f64",
-            "data": "synthetic", "config": _config(args, deck, form),
+            "data": "synthetic", "config": dict(_config(args, deck, form), tile_shape=tile[1] if tile else None),
             "roofline": roofline, "clocks": clk, "gpu_launches": launches,
             "particles": nparts, "host_wall_s": wall, "timing": "CUDA events on the handle's stream",
         }
@@ -533,6 +536,8 @@ def e2e_run(deck, parts, rng, steps, graph):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     run = cg.Run(deck, particles=pinned, rng=rng)
+    if deck.precision == abi.PREC_MIXED:
+        run.tune_tiles()
     d2h = 0
     left = steps
     while left > 0:

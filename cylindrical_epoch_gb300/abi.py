@@ -20,6 +20,9 @@ CYL_ERR_TIMEOUT = 7
 CYL_ERR_OUT_OF_MEMORY = 8
 CYL_ERR_SCRATCH = 9
 NOALLOC_MAX_PARTICLES = 262144  # CYL_NOALLOC_MAX_PARTICLES
+N_TILE_SHAPES = 5  # CYL_N_TILE_SHAPES
+TUNE_SET = 0       # CYL_TUNE_SET
+TUNE_TIME = 1      # CYL_TUNE_TIME
 
 ERROR_NAMES = {
     CYL_ERR_BAD_ARG: "bad argument",

@@ -21,18 +21,26 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
           "--expt-relaxed-constexpr"]
 
-# (source, extra flags)
+# Tile shapes of the mixed push (the order of TILE_SHAPES in push_mixed.cuh):
+# push_mixed.cu is compiled once per shape.
+TILE_SHAPES = ((16, 8), (8, 16), (8, 8), (16, 4), (8, 4))
+
+# (source, extra flags, object name)
 SOURCES = [
-    ("capi.cu", ["--fmad=false"]),
-    ("fields.cu", ["--fmad=false"]),
-    ("push_fp64.cu", ["--fmad=false"]),
-    ("particles.cu", ["--fmad=false"]),
-    ("charge.cu", ["--fmad=false"]),
-    ("push_mixed.cu", ["--fmad=true"]),
-    ("fields_fp32.cu", ["--fmad=true"]),
-    ("mixed_particles.cu", ["--fmad=true"]),
-    ("host_deck.cpp", []),
-    ("server.cpp", []),
+    ("capi.cu", ["--fmad=false"], "capi"),
+    ("fields.cu", ["--fmad=false"], "fields"),
+    ("push_fp64.cu", ["--fmad=false"], "push_fp64"),
+    ("particles.cu", ["--fmad=false"], "particles"),
+    ("charge.cu", ["--fmad=false"], "charge"),
+] + [
+    ("push_mixed.cu", ["--fmad=true", f"-DCYL_TILE_X={tx}", f"-DCYL_TILE_Y={ty}", f"-DCYL_TILE_NS=t{tx}x{ty}",
+                       f"-DCYL_TILE_FNS=push_mixed_fns_{tx}x{ty}"], f"push_mixed_{tx}x{ty}")
+    for tx, ty in TILE_SHAPES
+] + [
+    ("fields_fp32.cu", ["--fmad=true"], "fields_fp32"),
+    ("mixed_particles.cu", ["--fmad=true"], "mixed_particles"),
+    ("host_deck.cpp", [], "host_deck"),
+    ("server.cpp", [], "server"),
 ]
 
 
@@ -43,8 +51,8 @@ def nvcc():
     raise RuntimeError("nvcc not found")
 
 
-def _compile(src, extra, verbose):
-    obj = os.path.join(OUT_DIR, src + ".o")
+def _compile(src, extra, name, verbose):
+    obj = os.path.join(OUT_DIR, name + ".o")
     path = os.path.join(CSRC, src)
     if src.endswith(".cpp"):
         cmd = [nvcc(), "-x", "c++", "-O2", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-pthread",
@@ -76,11 +84,11 @@ def build(force=False, verbose=False):
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        results = list(ex.map(lambda a: _compile(a[0], a[1], verbose), SOURCES))
+        results = list(ex.map(lambda a: _compile(a[0], a[1], a[2], verbose), SOURCES))
     objs = [o for o, _ in results]
     if verbose:
-        for (src, _), (_, log) in zip(SOURCES, results):
-            sys.stderr.write(f"== {src}\n{log}")
+        for (_, _, name), (_, log) in zip(SOURCES, results):
+            sys.stderr.write(f"== {name}\n{log}")
     tmp = LIB + ".tmp"
     cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-Xcompiler", "-pthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)

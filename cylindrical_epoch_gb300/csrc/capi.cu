@@ -102,7 +102,9 @@ struct Handle {
   int64_t push_launches = 0;
   int timing_pending = 0;  // steps of the last chunk whose push events are not yet read
   int nblocks = 152 * 8;
-  int nblocks_mixed = 152 * 4;
+  int nblocks_mixed = 152 * 4;               // push CTAs of the current tile shape
+  int tile_shape = 0;                         // index into TILE_SHAPES (mixed form)
+  int nblocks_by_shape[N_TILE_SHAPES] = {};   // resident push CTAs per shape
   double xg0 = 0.0;  // x_grid_min at creation: origin of the mixed form's cell index
   MixedParams mp[MAX_SPECIES];
   TileTable* d_tiles = nullptr;     // one per species
@@ -335,8 +337,9 @@ static void push_all(Handle* h, cudaStream_t s, const FieldSet& F, const StepRec
 static void push_all(Handle* h, cudaStream_t s, const FieldSetF& F, const StepRec* rec, int apply_bcs) {
   for (int i = 0; i < h->nsp; ++i) {
     if (h->sp[i].immobile) continue;
-    launch_push_mixed(s, F, h->sp[i], h->d_cnt + i, rec, h->rc, apply_bcs, h->nblocks_mixed, h->nblocks,
-                      h->mp[i], h->d_tiles + i);
+    push_mixed_fns(h->tile_shape)
+        .launch(s, F, h->sp[i], h->d_cnt + i, rec, h->rc, apply_bcs, h->nblocks_mixed, h->nblocks, h->mp[i],
+                h->d_tiles + i);
     count_launch(h, 2);
   }
 }
@@ -405,7 +408,7 @@ static void enqueue_sort(Handle* h, const StepRec* rec) {
     if (h->prec == CYL_PREC_MIXED) {
       mixed_sort(h->st, h->sp[i], h->d_cnt + i, h->sc, h->d_tiles + i,
                  h->d_tile_start + (size_t)i * (h->ntiles_max + 1), h->d_tile_order + (size_t)i * h->ntiles_max,
-                 rec, h->rc, h->nblocks);
+                 TILE_SHAPES[h->tile_shape][0], TILE_SHAPES[h->tile_shape][1], rec, h->rc, h->nblocks);
       count_launch(h, 9);
     } else {
       sort_species(h->st, h->sp[i], h->d_cnt + i, h->sc, &rec->x_grid_min_after, h->rc, h->nblocks);
@@ -540,9 +543,13 @@ static int run_chunk(Handle* h, int k, bool use_graph) {
     // a chunk swaps J and J_old an even number of times
     h->jpar = h->graph_parity ^ (CHUNK & 1);
   } else {
+    // a launch that cannot start (a bad configuration) reports only through
+    // the thread's last error: clear it before the launches, read it after
+    (void)cudaGetLastError();
     for (int i = 0; i < k; ++i)
       enqueue_step(h, h->d_rec + i, h->d_src + h->src_per_step * i, i, true, false);
     enqueue_sort(h, last);
+    CK(cudaGetLastError());
   }
   h->timing_pending = k;
   return CYL_OK;
@@ -664,7 +671,7 @@ int cyl_estimate_device_bytes(const cyl_grid_desc* gd, const cyl_species_desc* s
     per_step_inj += (int64_t)(shifts_max * (double)gd->ny * (std::floor(spd[i].npart_per_cell) + 1.0));
   }
   if (gd->precision == CYL_PREC_MIXED) b += fbtot * (int64_t)sizeof(int);  // deferred lists
-  const int64_t ntiles_max = (gd->nx / TILE_X + 3) * (gd->ny / TILE_Y + 2);
+  const int64_t ntiles_max = ntiles_max_of(gd->nx, gd->ny);
   b += (ntiles_max + 1) * MAX_SPECIES * 8 + ntiles_max * MAX_SPECIES * 4;
   const int64_t ncells = nxg * nyg;
   b += maxcap * (4 + 8 * 8) + (ncells + 2) * 4 + ((ncells + 4096) / 4096 + 64) * 8;  // sort scratch
@@ -831,7 +838,7 @@ int cyl_create(const cyl_grid_desc* gd, const cyl_species_desc* spd, int32_t nsp
     if (h->sp[i].cap > maxcap) maxcap = h->sp[i].cap;
   }
   h->xg0 = h->g.x_grid_min;
-  h->ntiles_max = (rc.nx / TILE_X + 3) * (rc.ny / TILE_Y + 2);
+  h->ntiles_max = ntiles_max_of(rc.nx, rc.ny);
   ok(cudaMalloc(&h->d_tiles, sizeof(TileTable) * MAX_SPECIES));
   ok(cudaMemsetAsync(h->d_tiles, 0, sizeof(TileTable) * MAX_SPECIES, h->st));
   ok(cudaMalloc(&h->d_tile_start, sizeof(int64_t) * (h->ntiles_max + 1) * MAX_SPECIES));
@@ -858,7 +865,10 @@ int cyl_create(const cyl_grid_desc* gd, const cyl_species_desc* spd, int32_t nsp
       off += h->sp[i].cap + 1;
     }
   }
-  h->nblocks_mixed = nsm * push_mixed_blocks_per_sm(rc.M);
+  if (h->prec == CYL_PREC_MIXED) {
+    for (int k = 0; k < N_TILE_SHAPES; ++k) h->nblocks_by_shape[k] = nsm * push_mixed_fns(k).blocks_per_sm(rc.M);
+    h->nblocks_mixed = h->nblocks_by_shape[h->tile_shape];
+  }
   ok(cudaMalloc(&h->d_cnt, sizeof(SpeciesCounters) * MAX_SPECIES));
   ok(cudaMemsetAsync(h->d_cnt, 0, sizeof(SpeciesCounters) * MAX_SPECIES, h->st));
   // sort scratch: keys, histogram, block sums, 7 doubles + id per particle
@@ -1253,6 +1263,126 @@ int cyl_sort_particles(cyl_handle hh) {
   CK(cudaEventRecord(h->ev_copy, h->st));
   h->copy_pending = true;
   enqueue_sort(h, h->d_rec + CHUNK);
+  return sync_and_check(h);
+}
+
+int cyl_tile_shape(int32_t shape, int32_t* tx, int32_t* ty) {
+  if (shape < 0 || shape >= N_TILE_SHAPES || !tx || !ty) return CYL_ERR_BAD_ARG;
+  *tx = TILE_SHAPES[shape][0];
+  *ty = TILE_SHAPES[shape][1];
+  return CYL_OK;
+}
+
+// Use tile shape k for the mixed push from the next sort on; a captured step
+// graph holds the old shape's launches and is rebuilt.
+static void set_tile_shape(Handle* h, int k) {
+  h->tile_shape = k;
+  h->nblocks_mixed = h->nblocks_by_shape[k];
+  if (h->gexec) {
+    cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+  }
+}
+
+// The step record of the current grid (no step in progress) at d_rec + CHUNK.
+static int current_rec(Handle* h) {
+  if (h->copy_pending) CK(cudaEventSynchronize(h->ev_copy));
+  StepRec& r = h->h_rec[0];
+  std::memset(&r, 0, sizeof(r));
+  fill_grid(r, h->g, false);
+  fill_grid(r, h->g, true);
+  for (int i = 0; i < 4; ++i) r.bc_field[i] = r.bc_field_after[i] = h->bc_field[i];
+  r.nshift_total = r.nshift_total_after = (int32_t)h->n_shifts;
+  CK(cudaMemcpyAsync(h->d_rec + CHUNK, h->h_rec, sizeof(StepRec), cudaMemcpyHostToDevice, h->st));
+  CK(cudaEventRecord(h->ev_copy, h->st));
+  h->copy_pending = true;
+  return CYL_OK;
+}
+
+int cyl_tune_tiles(cyl_handle hh, int32_t mode, int32_t* shape) {
+  if (!hh || !shape) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  if (h->prec != CYL_PREC_MIXED) return CYL_ERR_UNSUPPORTED;
+  if (mode == CYL_TUNE_SET) {
+    if (*shape < 0 || *shape >= N_TILE_SHAPES) return CYL_ERR_BAD_ARG;
+    set_tile_shape(h, *shape);
+    return cyl_sort_particles(hh);
+  }
+  if (mode != CYL_TUNE_TIME) return CYL_ERR_BAD_ARG;
+  if (int r = flush_push_timing(h)) return r;
+  if (int r = current_rec(h)) return r;
+  const StepRec* rec = h->d_rec + CHUNK;
+  CK(cudaStreamSynchronize(h->st));
+  // Copy of the state a push changes: the mixed particle words of every
+  // species (kx, fx, fy, fz, ux, uy, uz, fw: bytes [0, 32 cap) of the species
+  // buffer; id: bytes [56 cap, 64 cap)) and the counters.  The trial pushes
+  // deposit into three scratch current arrays behind the copy.
+  size_t bytes = 0;
+  for (int i = 0; i < h->nsp; ++i) bytes += (size_t)h->sp[i].cap * 40;
+  const size_t jbytes = h->fcount * sizeof(cplx);
+  char* snap = nullptr;
+  if (cudaMalloc(&snap, bytes + 3 * jbytes) != cudaSuccess) return CYL_ERR_OUT_OF_MEMORY;
+  std::vector<SpeciesCounters> cnt0(MAX_SPECIES);
+  int rcode = CYL_OK;
+  auto run = [&](cudaError_t e) {
+    if (e != cudaSuccess && rcode == CYL_OK) {
+      h->last_cuda_error = e;
+      rcode = CYL_ERR_CUDA;
+    }
+  };
+  auto copy_state = [&](bool save) {
+    size_t off = 0;
+    for (int i = 0; i < h->nsp; ++i) {
+      char* buf = reinterpret_cast<char*>(h->sp[i].x);
+      const size_t cap = (size_t)h->sp[i].cap;
+      char* a = save ? snap + off : buf;
+      const char* b = save ? buf : snap + off;
+      run(cudaMemcpyAsync(a, b, 32 * cap, cudaMemcpyDeviceToDevice, h->st));
+      a = save ? snap + off + 32 * cap : buf + 56 * cap;
+      b = save ? buf + 56 * cap : snap + off + 32 * cap;
+      run(cudaMemcpyAsync(a, b, 8 * cap, cudaMemcpyDeviceToDevice, h->st));
+      off += 40 * cap;
+    }
+    if (save)
+      run(cudaMemcpyAsync(cnt0.data(), h->d_cnt, sizeof(SpeciesCounters) * MAX_SPECIES, cudaMemcpyDeviceToHost,
+                          h->st));
+    else
+      run(cudaMemcpyAsync(h->d_cnt, cnt0.data(), sizeof(SpeciesCounters) * MAX_SPECIES, cudaMemcpyHostToDevice,
+                          h->st));
+    run(cudaStreamSynchronize(h->st));
+  };
+  copy_state(true);
+  FieldSetF F = fieldset_f(h, h->jpar);
+  cplx* jscr = reinterpret_cast<cplx*>(snap + bytes);
+  F.jx.p = jscr;
+  F.jr.p = jscr + h->fcount;
+  F.jt.p = jscr + 2 * h->fcount;
+  float best_ms[N_TILE_SHAPES];
+  for (int k = 0; k < N_TILE_SHAPES; ++k) best_ms[k] = 1e30f;
+  for (int rep = 0; rep < 2 && rcode == CYL_OK; ++rep) {
+    for (int k = 0; k < N_TILE_SHAPES && rcode == CYL_OK; ++k) {
+      copy_state(false);
+      set_tile_shape(h, k);
+      enqueue_sort(h, rec);
+      run(cudaMemsetAsync(jscr, 0, 3 * jbytes, h->st));
+      run(cudaEventRecord(h->ev_push[0][0], h->st));
+      push_all(h, h->st, F, rec, 0);
+      run(cudaEventRecord(h->ev_push[0][1], h->st));
+      run(cudaEventSynchronize(h->ev_push[0][1]));
+      float ms = 0.f;
+      run(cudaEventElapsedTime(&ms, h->ev_push[0][0], h->ev_push[0][1]));
+      if (ms < best_ms[k]) best_ms[k] = ms;
+    }
+  }
+  int best = 0;
+  for (int k = 1; k < N_TILE_SHAPES; ++k)
+    if (best_ms[k] < best_ms[best]) best = k;
+  copy_state(false);
+  cudaFree(snap);
+  set_tile_shape(h, best);
+  if (rcode != CYL_OK) return rcode;
+  enqueue_sort(h, rec);
+  *shape = best;
   return sync_and_check(h);
 }
 

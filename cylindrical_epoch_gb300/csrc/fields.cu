@@ -619,18 +619,24 @@ __global__ void __launch_bounds__(CTA_THREADS) k_halo_rows(FView f, const StepRe
 
 // -------------------------------------------------------- moving window
 
-// shift_fields (window.F90:98-132): one block per (row j, mode m); the row is
-// staged in shared memory so the in-place left shift is race free.  The
-// periodic self-wrap of shift_field_modes and the x_max column fix-ups act
-// within the same row.
+// shift_fields (window.F90:98-132): one block per (row j, mode m).  The
+// in-place left shift f(i) = f(i+1) runs in chunks of blockDim.x elements
+// from the left: a chunk reads its sources into registers before any of its
+// writes, and the next chunk reads only beyond what this one wrote, so no
+// row staging is needed whatever the row length.  The periodic self-wrap of
+// shift_field_modes and the x_max column fix-ups act within the same row.
 template <typename U>
-__device__ void shift_row(FViewT<U> f, cplx* row, int j, int m, const int* bcf, const RunConst& rc) {
+__device__ void shift_row(FViewT<U> f, int j, int m, const int* bcf, const RunConst& rc) {
   const int nxg = rc.nxg, nx = rc.nx;
   __syncthreads();
-  for (int i = threadIdx.x; i < nxg; i += blockDim.x) row[i] = f(1 - NG + i, j, m);
-  __syncthreads();
-  for (int i = threadIdx.x; i < nxg - 1; i += blockDim.x) f(1 - NG + i, j, m) = row[i + 1];
-  __syncthreads();
+  for (int c = 0; c < nxg - 1; c += blockDim.x) {
+    const int i = c + threadIdx.x;
+    U v;
+    if (i < nxg - 1) v = *f.ptr(1 - NG + i + 1, j, m);
+    __syncthreads();
+    if (i < nxg - 1) *f.ptr(1 - NG + i, j, m) = v;
+    __syncthreads();
+  }
   // periodic self-wrap (field_mode_bc) within this row
   if (bcf[CYL_BD_X_MAX] == CYL_BC_PERIODIC)
     for (int i = 1 + threadIdx.x; i <= NG; i += blockDim.x) f(nx + i, j, m) = f(i, j, m);
@@ -641,22 +647,21 @@ __device__ void shift_row(FViewT<U> f, cplx* row, int j, int m, const int* bcf, 
 
 template <typename T>
 __global__ void k_shift_fields(FieldSetT<T> F, const cplx* cols, const StepRec* rec, int which, RunConst rc) {
-  extern __shared__ cplx row[];
   const int j = 1 - NG + (int)blockIdx.x;
   const int m = blockIdx.y;
   const int nx = rc.nx;
   __shared__ int bcf[4];
   if (threadIdx.x < 4) bcf[threadIdx.x] = rec->bc_field_after[threadIdx.x];
   if (rec->nshift <= which) return;
-  shift_row(F.ex, row, j, m, bcf, rc);
-  shift_row(F.er, row, j, m, bcf, rc);
-  shift_row(F.et, row, j, m, bcf, rc);
-  shift_row(F.bx, row, j, m, bcf, rc);
-  shift_row(F.br, row, j, m, bcf, rc);
-  shift_row(F.bt, row, j, m, bcf, rc);
-  shift_row(F.jx, row, j, m, bcf, rc);
-  shift_row(F.jr, row, j, m, bcf, rc);
-  shift_row(F.jt, row, j, m, bcf, rc);
+  shift_row(F.ex, j, m, bcf, rc);
+  shift_row(F.er, j, m, bcf, rc);
+  shift_row(F.et, j, m, bcf, rc);
+  shift_row(F.bx, j, m, bcf, rc);
+  shift_row(F.br, j, m, bcf, rc);
+  shift_row(F.bt, j, m, bcf, rc);
+  shift_row(F.jx, j, m, bcf, rc);
+  shift_row(F.jr, j, m, bcf, rc);
+  shift_row(F.jt, j, m, bcf, rc);
   __syncthreads();
   if (threadIdx.x == 0) {
     const int ncolv = rc.ny + 2 * NG;
@@ -763,7 +768,7 @@ template <typename T>
 void launch_shift_fields(cudaStream_t s, const FieldSetT<T>& F, const cplx* cols, const StepRec* rec,
                          int which, const RunConst& rc) {
   dim3 grd(rc.nyg, rc.M);
-  k_shift_fields<T><<<grd, 256, (size_t)rc.nxg * sizeof(cplx), s>>>(F, cols, rec, which, rc);
+  k_shift_fields<T><<<grd, 256, 0, s>>>(F, cols, rec, which, rc);
 }
 
 #define INST(T)                                                                                          \

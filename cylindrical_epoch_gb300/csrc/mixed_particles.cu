@@ -257,11 +257,14 @@ void mixed_cell_indices(cudaStream_t s, const SpeciesPtrs& sp, const SpeciesCoun
 
 __device__ __forceinline__ int floordiv(int a, int b) { return (a >= 0) ? a / b : -((-a + b - 1) / b); }
 
-__global__ void k_tile_layout(TileTable* tt, const StepRec* rec, RunConst rc, int64_t* start, int32_t* order) {
+__global__ void k_tile_layout(TileTable* tt, const StepRec* rec, RunConst rc, int64_t* start, int32_t* order,
+                              int tile_x, int tile_y) {
   const int nsh = rec->nshift_total_after;
-  tt->tx_min = floordiv(nsh, TILE_X) - 1;
-  tt->ntx = rc.nx / TILE_X + 3;
-  tt->nty = rc.ny / TILE_Y + 2;
+  tt->tile_x = tile_x;
+  tt->tile_y = tile_y;
+  tt->tx_min = floordiv(nsh, tile_x) - 1;
+  tt->ntx = rc.nx / tile_x + 3;
+  tt->nty = rc.ny / tile_y + 2;
   tt->ntiles = tt->ntx * tt->nty;
   tt->start = start;
   tt->order = order;
@@ -271,16 +274,17 @@ __global__ void k_tile_keys(SpeciesPtrs sp, const SpeciesCounters* cnt, const Ti
                             int32_t* hist) {
   const int64_t n = cnt->n_used;
   const int ntiles = tt->ntiles, ntx = tt->ntx, nty = tt->nty, txm = tt->tx_min;
+  const int tile_x = tt->tile_x, tile_y = tt->tile_y;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i - threadIdx.x < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     int key = ntiles;  // holes sort last and are dropped
     if (i < n) {
       const int32_t k = sp.kx[i];
       if (k != INT32_MIN) {
-        int tx = floordiv(k, TILE_X) - txm;
+        int tx = floordiv(k, tile_x) - txm;
         const float y = sp.fy[i], z = sp.fz[i];
         int ky = (int)floorf(sqrtf(y * y + z * z) - 0.5f);
-        int ty = ky < 0 ? 0 : ky / TILE_Y;
+        int ty = ky < 0 ? 0 : ky / tile_y;
         tx = tx < 0 ? 0 : (tx >= ntx ? ntx - 1 : tx);
         ty = ty >= nty ? nty - 1 : ty;
         key = ty * ntx + tx;
@@ -405,9 +409,10 @@ __global__ void k_tile_commit(SpeciesCounters* cnt, const TileTable* tt) {
 }
 
 void mixed_sort(cudaStream_t s, const SpeciesPtrs& sp, SpeciesCounters* cnt, SortScratch& sc, TileTable* tt,
-                int64_t* tile_start, int32_t* tile_order, const StepRec* rec, const RunConst& rc, int nblocks) {
-  const int ntiles_max = (rc.nx / TILE_X + 3) * (rc.ny / TILE_Y + 2);
-  k_tile_layout<<<1, 1, 0, s>>>(tt, rec, rc, tile_start, tile_order);
+                int64_t* tile_start, int32_t* tile_order, int tile_x, int tile_y, const StepRec* rec,
+                const RunConst& rc, int nblocks) {
+  const int ntiles_max = ntiles_max_of(rc.nx, rc.ny);
+  k_tile_layout<<<1, 1, 0, s>>>(tt, rec, rc, tile_start, tile_order, tile_x, tile_y);
   cudaMemsetAsync(sc.hist, 0, sizeof(int32_t) * (ntiles_max + 1), s);
   k_tile_keys<<<nblocks, 256, 0, s>>>(sp, cnt, tt, sc.keys, sc.hist);
   scan_exclusive(s, sc.hist, ntiles_max + 1, (int32_t*)sc.perm);
@@ -416,6 +421,21 @@ void mixed_sort(cudaStream_t s, const SpeciesPtrs& sp, SpeciesCounters* cnt, Sor
   k_tile_scatter<<<nblocks, 256, 0, s>>>(sp, cnt, sc.tmp, sc.tmp_id, sc.cap, sc.keys, sc.hist, tt);
   k_tile_order<<<1, ORDER_BUCKETS, 0, s>>>(tt, tile_start, tile_order);
   k_tile_commit<<<1, 1, 0, s>>>(cnt, tt);
+}
+
+// ------------------------------------------------- push tile shapes
+
+PushMixedFns push_mixed_fns_16x8();
+PushMixedFns push_mixed_fns_8x16();
+PushMixedFns push_mixed_fns_8x8();
+PushMixedFns push_mixed_fns_16x4();
+PushMixedFns push_mixed_fns_8x4();
+
+const PushMixedFns& push_mixed_fns(int shape) {
+  static const PushMixedFns table[N_TILE_SHAPES] = {push_mixed_fns_16x8(), push_mixed_fns_8x16(),
+                                                    push_mixed_fns_8x8(), push_mixed_fns_16x4(),
+                                                    push_mixed_fns_8x4()};
+  return table[shape < 0 || shape >= N_TILE_SHAPES ? 0 : shape];
 }
 
 }  // namespace cyl

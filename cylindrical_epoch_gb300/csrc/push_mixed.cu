@@ -25,8 +25,18 @@
 #include "cyl_kernels.cuh"
 #include "push_mixed.cuh"
 
-namespace cyl {
+// This file is compiled once per tile shape with -DCYL_TILE_X, -DCYL_TILE_Y,
+// -DCYL_TILE_NS (the namespace of that build) and -DCYL_TILE_FNS (the name
+// of its PushMixedFns accessor).
+#if !defined(CYL_TILE_X) || !defined(CYL_TILE_Y) || !defined(CYL_TILE_NS) || !defined(CYL_TILE_FNS)
+#error "push_mixed.cu is built per tile shape: define CYL_TILE_X, CYL_TILE_Y, CYL_TILE_NS, CYL_TILE_FNS"
+#endif
 
+namespace cyl {
+namespace CYL_TILE_NS {
+
+constexpr int TILE_X = CYL_TILE_X;          // cells per tile along x
+constexpr int TILE_Y = CYL_TILE_Y;          // cells per tile along r
 constexpr int DRIFT = 1;                    // cells a particle may drift from its tile
 constexpr int RW = TILE_X + 2 * DRIFT + 5;  // staged region width (x)
 constexpr int RH = TILE_Y + 2 * DRIFT + 5;  // staged region height (r)
@@ -796,6 +806,12 @@ void launch_push_mixed(cudaStream_t s, const FieldSetF& F, const SpeciesPtrs& sp
     default:
       break;
   }
+}
+
+}  // namespace CYL_TILE_NS
+
+PushMixedFns CYL_TILE_FNS() {
+  return {&CYL_TILE_NS::push_mixed_smem, &CYL_TILE_NS::push_mixed_blocks_per_sm, &CYL_TILE_NS::launch_push_mixed};
 }
 
 }  // namespace cyl

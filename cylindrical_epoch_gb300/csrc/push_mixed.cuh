@@ -7,14 +7,20 @@
 
 namespace cyl {
 
-constexpr int TILE_X = 16;  // cells per tile along x
-constexpr int TILE_Y = 8;   // cells per tile along r
+// Tile shapes (cells along x, cells along r) the mixed push is built for;
+// push_mixed.cu is compiled once per shape.  Shape 0 is the default;
+// cyl_tune_tiles picks another per run.
+constexpr int N_TILE_SHAPES = CYL_N_TILE_SHAPES;
+constexpr int TILE_SHAPES[N_TILE_SHAPES][2] = {{16, 8}, {8, 16}, {8, 8}, {16, 4}, {8, 4}};
+constexpr int TILE_MIN_X = 8, TILE_MIN_Y = 4;  // the smallest extents: tile-table sizes
+inline int ntiles_max_of(int nx, int ny) { return (nx / TILE_MIN_X + 3) * (ny / TILE_MIN_Y + 2); }
 
 // Particles sorted by tile: tile t owns slots [start[t], start[t+1]);
 // slots [n_sorted, n_used) were appended after the sort.  order[] lists the
 // tiles by decreasing particle count (the push deals them to its CTAs
 // round-robin in that order, a longest-first static schedule).
 struct TileTable {
+  int tile_x, tile_y;  // the tile shape of the last sort
   int ntiles;
   int ntx, nty;
   int tx_min;     // absolute tile column of tile 0
@@ -42,12 +48,19 @@ struct MixedParams {
 };
 
 MixedParams mixed_params(const SpeciesPtrs& sp, const RunConst& rc);
-size_t push_mixed_smem(int M);
-int push_mixed_blocks_per_sm(int M);
 
-void launch_push_mixed(cudaStream_t s, const FieldSetF& F, const SpeciesPtrs& sp, SpeciesCounters* cnt,
-                       const StepRec* rec, const RunConst& rc, int apply_bcs, int nblocks_tiles,
-                       int nblocks_global, const MixedParams& P, TileTable* tt);
+// The push of one tile shape (push_mixed.cu built for that shape):
+// shared memory per CTA, resident CTAs per SM (also sets the kernel's
+// shared-memory attributes; call before the first launch), and the launch
+// of the tile kernel and the global-path kernel.
+struct PushMixedFns {
+  size_t (*smem)(int M);
+  int (*blocks_per_sm)(int M);
+  void (*launch)(cudaStream_t s, const FieldSetF& F, const SpeciesPtrs& sp, SpeciesCounters* cnt,
+                 const StepRec* rec, const RunConst& rc, int apply_bcs, int nblocks_tiles, int nblocks_global,
+                 const MixedParams& P, TileTable* tt);
+};
+const PushMixedFns& push_mixed_fns(int shape);
 
 // mixed_particles.cu
 void mixed_from_double(cudaStream_t s, const SpeciesPtrs& sp, const double* stage, int64_t n, int64_t cap,
@@ -60,7 +73,8 @@ void mixed_particle_bcs(cudaStream_t s, const SpeciesPtrs& sp, SpeciesCounters* 
                         const RunConst& rc, int nblocks);
 void mixed_energy(cudaStream_t s, const SpeciesPtrs& sp, const SpeciesCounters* cnt, double* out, int nblocks);
 void mixed_sort(cudaStream_t s, const SpeciesPtrs& sp, SpeciesCounters* cnt, SortScratch& sc, TileTable* tt,
-                int64_t* tile_start, int32_t* tile_order, const StepRec* rec, const RunConst& rc, int nblocks);
+                int64_t* tile_start, int32_t* tile_order, int tile_x, int tile_y, const StepRec* rec,
+                const RunConst& rc, int nblocks);
 void mixed_cell_indices(cudaStream_t s, const SpeciesPtrs& sp, const SpeciesCounters* cnt, double xg0,
                         double x_grid_min, const RunConst& rc, int32_t* cx, int32_t* cy, int32_t* live,
                         int nblocks);

@@ -5,8 +5,10 @@
 // (strict arrival order, so a large job cannot be starved by small ones); a
 // worker then loads the job's species on the host with the reference's
 // loader and KISS stream, creates a handle (its own non-blocking CUDA
-// stream), runs the steps as CUDA graphs of 16 steps, reads the diagnostics
-// and destroys the handle, which returns the job's memory to the budget.
+// stream), picks the push tile shape of a mixed-form run (timed once per
+// deck shape, see g_tile_choice), runs the steps as CUDA graphs of 16 steps,
+// reads the diagnostics and destroys the handle, which returns the job's
+// memory to the budget.
 // Workers run their jobs at the same time, so the kernels of several runs
 // overlap on the device; a new job is admitted as soon as a worker and
 // memory are free (continuous batching of independent runs).
@@ -39,6 +41,14 @@ struct Job {
   std::vector<std::vector<double>> profile, phase;  // owned copies of the laser vectors
   cyl_job_result res{};
 };
+
+// Mixed-form tile shape chosen for each deck shape (device, nx, ny, modes,
+// particles per cell of the first species), shared by every server of the
+// process: the first run of a deck shape times the shapes (cyl_tune_tiles),
+// later runs reuse the choice, so a deck runs the same kernels alone and in
+// a mix, whatever else is on the device.
+std::mutex g_tile_mu;
+std::map<std::vector<int64_t>, int> g_tile_choice;
 
 double now_since(const std::chrono::steady_clock::time_point& t0) {
   return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -110,6 +120,25 @@ int run_job(cyl_server_s* srv, Job* job) {
   }
   hp.clear();
   if (r == CYL_OK) r = cyl_initialise(h);
+  if (r == CYL_OK && d.grid.precision == CYL_PREC_MIXED) {
+    const std::vector<int64_t> key = {srv->device, d.grid.nx, d.grid.ny, d.grid.n_mode,
+                                      d.nspecies > 0 ? (int64_t)(d.species[0].npart_per_cell * 1000.0) : 0};
+    int shape = -1;
+    {
+      std::lock_guard<std::mutex> lock(g_tile_mu);
+      auto it = g_tile_choice.find(key);
+      if (it != g_tile_choice.end()) shape = it->second;
+    }
+    if (shape >= 0) {
+      r = cyl_tune_tiles(h, CYL_TUNE_SET, &shape);
+    } else {
+      r = cyl_tune_tiles(h, CYL_TUNE_TIME, &shape);
+      if (r == CYL_OK) {
+        std::lock_guard<std::mutex> lock(g_tile_mu);
+        g_tile_choice.emplace(key, shape);
+      }
+    }
+  }
   {
     std::lock_guard<std::mutex> lock(srv->mu);
     job->res.t_start = now_since(srv->t0);

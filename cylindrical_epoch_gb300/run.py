@@ -181,6 +181,17 @@ class Run:
     def push_only(self):
         abi.check("cyl_push_only", self.lib.cyl_push_only(self.h))
 
+    def tune_tiles(self, shape=None):
+        """Mixed form: with shape=None time one push of the current state with
+        every tile shape and keep the fastest, else use tile shape `shape`
+        (cyl_tune_tiles).  Returns (index, (cells x, cells r))."""
+        k = C.c_int32(-1 if shape is None else int(shape))
+        mode = abi.TUNE_TIME if shape is None else abi.TUNE_SET
+        abi.check("cyl_tune_tiles", self.lib.cyl_tune_tiles(self.h, mode, C.byref(k)))
+        tx, ty = C.c_int32(0), C.c_int32(0)
+        abi.check("cyl_tile_shape", self.lib.cyl_tile_shape(k.value, C.byref(tx), C.byref(ty)))
+        return k.value, (tx.value, ty.value)
+
     def sort(self):
         abi.check("cyl_sort_particles", self.lib.cyl_sort_particles(self.h))
 

@@ -268,6 +268,29 @@ int cyl_cell_indices_noalloc(cyl_handle h, int32_t ispecies, int32_t* cell_x,
  * mixed form evaluates it in FP64 from its stored state. */
 int cyl_charge_density(cyl_handle h, double* rho);
 
+/* ---- tile shape of the mixed form's push ------------------------------
+ * The mixed form keeps particles sorted by tiles of tx x ty cells and pushes
+ * one tile per CTA with the tile's fields staged in shared memory.  The push
+ * is built for CYL_N_TILE_SHAPES shapes; shape 0 (16 x 8) is the default.
+ * No counterpart in the reference (its push walks linked lists).
+ *
+ * cyl_tile_shape: the cells (x, r) of shape `shape`.  Host only.
+ *
+ * cyl_tune_tiles (mixed form only; CYL_ERR_UNSUPPORTED for the FP64 form):
+ *   mode CYL_TUNE_SET:  use shape *shape (re-sorts the particles);
+ *   mode CYL_TUNE_TIME: time one push of the current state with every shape
+ *     (each on a copy of the state that is restored afterwards: the run's
+ *     particles and currents are unchanged) and keep the fastest; its index
+ *     is returned in *shape.  The copy is a temporary device allocation of
+ *     40 bytes per particle slot plus three current arrays.
+ * The shape changes the order of the per-tile FP32 partial sums only; the
+ * results of two shapes agree to FP32 round-off. */
+#define CYL_N_TILE_SHAPES 5
+#define CYL_TUNE_SET 0
+#define CYL_TUNE_TIME 1
+int cyl_tile_shape(int32_t shape, int32_t* tx, int32_t* ty);
+int cyl_tune_tiles(cyl_handle h, int32_t mode, int32_t* shape);
+
 /* Push-and-deposit only (the body of push_particles, particles.F90:163-734,
  * without current_bcs_r_min_final and particle_bcs): used by the parity tests
  * and by the kernel benchmark to time the dominant kernel alone. */

@@ -96,3 +96,60 @@ def test_mixed_continuity_residual(gpu_lib):
     assert res[0][0] < 1e-12
     assert res[1][0] < TOL_EZ
     assert abs(res[1][1] - res[0][1]) < TOL_EZ
+
+
+def test_tile_shapes_agree(gpu_lib):
+    """Every tile shape of the mixed push gives the same run: the shape only
+    changes how particles are grouped into the exact per-tile sums, whose
+    FP32 flush rounds differently.  After 96 steps of a laser wakefield with
+    the window moving: particle count within 2, Ez per mode and kinetic
+    energy within 1e-4 relative of shape 0 (the form's error bar against
+    FP64 is 1e-3)."""
+    deck = _wake(abi.PREC_MIXED)
+    parts, rng = cg.host_load(deck)
+    ref = None
+    for k in range(abi.N_TILE_SHAPES):
+        run = cg.Run(deck, particles=parts, rng=rng)
+        idx, (tx, ty) = run.tune_tiles(k)
+        assert idx == k and tx * ty > 0
+        run.step(48)
+        run.step(48, graph=True)
+        s, d, ez = run.state(), run.diagnostics(), run.field("exm")
+        assert d.device_error == 0
+        run.close()
+        if ref is None:
+            ref = (s, d, ez)
+            assert s.n_shifts > 0
+            continue
+        assert s.n_shifts == ref[0].n_shifts
+        assert abs(s.n_live[0] - ref[0].n_live[0]) <= 2
+        assert abs(d.kinetic_energy - ref[1].kinetic_energy) <= 1e-4 * ref[1].kinetic_energy, k
+        for m in range(deck.n_mode):
+            assert rel_l2(ez[m], ref[2][m]) < 1e-4, (k, m)
+
+
+def test_tune_tiles_keeps_state(gpu_lib):
+    """cyl_tune_tiles in timing mode pushes copies of the state: the run's
+    particles are the same set afterwards (same ids, positions, momenta),
+    and its currents and later steps are those of a run set to the chosen
+    shape.  The FP64 form has no tiles and refuses."""
+    deck = _wake(abi.PREC_MIXED)
+    parts, rng = cg.host_load(deck)
+    a = cg.Run(deck, particles=parts, rng=rng)
+    a.step(20)
+    before = a.particles(0).sorted_by_id()
+    j0 = a.field("jxm")
+    k, _ = a.tune_tiles()
+    assert 0 <= k < abi.N_TILE_SHAPES
+    after = a.particles(0).sorted_by_id()
+    for name in ("id", "x", "y", "z", "px", "py", "pz", "w"):
+        assert np.array_equal(getattr(before, name), getattr(after, name)), name
+    assert np.array_equal(j0, a.field("jxm"))
+    a.step(20)
+    assert a.diagnostics().device_error == 0
+    a.close()
+    d64 = _wake(abi.PREC_FP64)
+    b = cg.Run(d64, particles=parts, rng=rng)
+    with pytest.raises(abi.CylError):
+        b.tune_tiles()
+    b.close()

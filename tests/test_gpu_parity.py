@@ -148,3 +148,18 @@ def test_charge_density_and_continuity(gpu_lib):
     print("continuity residual per mode: gpu", rg, "oracle", ro)
     assert rg[0] < 1e-12
     assert abs(rg[1] - ro[1]) < 1e-8
+
+
+def test_wide_window_shift(gpu_lib):
+    """Window shifts on a grid 3200 cells long (a 3210-cell row of complex
+    FP64 is 51 KB): counts, shifts and fields against the oracle."""
+    deck = cg.wakefield(nx=3200, ny=16, ppc=1, density=3.0e24, ramp=2.0e-6)
+    deck.window_start_time = 10 * 5.0e-17
+    gpu, orc = _pair(deck)
+    for chunk in (16, 24):
+        gpu.step(chunk)
+        orc.step(chunk)
+        sg, so = gpu.state(), orc.state()
+        assert sg.n_shifts == so.n_shifts and sg.n_live[0] == so.n_live[0]
+    assert so.n_shifts > 10
+    _cmp_fields(gpu, orc, ["exm", "erm", "btm", "jxm"])
