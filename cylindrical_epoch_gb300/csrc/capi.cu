@@ -1266,6 +1266,25 @@ int cyl_sort_particles(cyl_handle hh) {
   return sync_and_check(h);
 }
 
+int cyl_number_density(cyl_handle hh, int32_t isp, double* out) {
+  if (!hh || !out) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  if (isp >= h->nsp) return CYL_ERR_BAD_ARG;
+  // the work array is free between steps
+  cplx* dst = h->F[15];
+  const FView v{dst, h->rc.nxg, h->rc.nyg};
+  CK(cudaMemsetAsync(dst, 0, h->fcount * sizeof(cplx), h->st));
+  for (int i = 0; i < h->nsp; ++i) {
+    if (isp >= 0 && i != isp) continue;
+    launch_number_density(h->st, h->sp[i], h->d_cnt + i, h->rc, h->g.x_grid_min, (int)h->n_shifts,
+                          h->prec == CYL_PREC_MIXED, v, h->nblocks);
+  }
+  launch_number_density_bcs(h->st, v, h->rc, h->bc_field);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out, dst, h->fcount * sizeof(cplx), cudaMemcpyDeviceToHost, h->st));
+  return sync_and_check(h);
+}
+
 int cyl_tile_shape(int32_t shape, int32_t* tx, int32_t* ty) {
   if (shape < 0 || shape >= N_TILE_SHAPES || !tx || !ty) return CYL_ERR_BAD_ARG;
   *tx = TILE_SHAPES[shape][0];

@@ -92,6 +92,147 @@ __global__ void __launch_bounds__(256) k_charge_density(SpeciesPtrs sp, const Sp
   }
 }
 
+// calc_number_density_modes (calc_df.F90:588-661): cell-centred weights
+// (particle_to_grid.inc, triangle/gxfac.inc with gy folded for r < dy), the
+// macro particle volume 2 pi dx dy r (partlist.F90:999-1013), mode factor
+// 2 e^{i m theta}; FP64 atomics into the output.  Same operation order as
+// the reference on the FP64 layout.
+template <bool MIXED>
+__global__ void __launch_bounds__(256) k_number_density(SpeciesPtrs sp, const SpeciesCounters* cnt, RunConst rc,
+                                                        double x_grid_min, int nsh, FView out) {
+  const int64_t n = cnt->n_used;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double cell_x_r, y, z, wdata;
+    if (MIXED) {
+      const int32_t kx = sp.kx[i];
+      if (kx == INT32_MIN) continue;
+      cell_x_r = (double)(kx - nsh) + f2d_bits(sp.fx[i]);
+      y = f2d_bits(sp.fy[i]) * rc.dy;
+      z = f2d_bits(sp.fz[i]) * rc.dy;
+      wdata = f2d_bits(sp.fw[i]);
+    } else {
+      const double x = sp.x[i];
+      if (isnan(x)) continue;
+      cell_x_r = (x - x_grid_min) / rc.dx;
+      y = sp.y[i];
+      z = sp.z[i];
+      wdata = sp.w[i];
+    }
+    const double part_r = sqrt(y * y + z * z);
+    const double cell_y_r = (part_r - rc.y_grid_min) / rc.dy;
+    int cell_x = (int)floor(cell_x_r + 0.5), cell_y = (int)floor(cell_y_r + 0.5);
+    const double fx = (double)cell_x - cell_x_r, fy = (double)cell_y - cell_y_r;
+    cell_x = cell_x + 1;
+    cell_y = cell_y + 1;
+    if (cell_x - 1 < 1 - NG || cell_x + 1 > rc.nx + NG || cell_y - 1 < 1 - NG || cell_y + 1 > rc.ny + NG) continue;
+    double gx[3], gy[3];
+    double c2 = fx * fx;
+    gx[0] = 0.5 * ((0.25 + c2) + fx);
+    gx[1] = 0.75 - c2;
+    gx[2] = 0.5 * ((0.25 + c2) - fx);
+    c2 = fy * fy;
+    gy[0] = 0.5 * ((0.25 + c2) + fy);
+    gy[1] = 0.75 - c2;
+    gy[2] = 0.5 * ((0.25 + c2) - fy);
+    if (part_r < rc.dy) {
+      gy[1] = gy[1] + gy[0];
+      gy[0] = 0.0;
+    }
+    const double macro_part_volume = ((2.0 * PI) * rc.dx) * rc.dy * part_r;
+    const double part_num_dens = wdata / macro_part_volume;
+    const cplx exp_itheta = mk(y / part_r, z / part_r);
+    cplx exp_imtheta = mk(1.0, 0.0), mode_fac = mk(1.0, 0.0);
+    for (int im = 0; im < rc.M; ++im) {
+      if (im > 0) {
+        exp_imtheta = exp_imtheta * exp_itheta;
+        mode_fac = 2.0 * exp_imtheta;
+      }
+      for (int iy = -1; iy <= 1; ++iy)
+        for (int ix = -1; ix <= 1; ++ix) {
+          const cplx v = ((gx[ix + 1] * gy[iy + 1]) * part_num_dens) * mode_fac;
+          cplx* d = out.ptr(cell_x + ix, cell_y + iy, im);
+          atomicAdd(&d->re, v.re);
+          if (im > 0) atomicAdd(&d->im, v.im);
+        }
+    }
+  }
+}
+
+// calc_boundary_modes (calc_df.F90:35-55) and field_mode_zero_gradient on the
+// four boundaries, centre stagger (boundary.F90:654-707): reflecting folds
+// (particle_reflection_bcs without flip, boundary.F90:833-915), periodic
+// sums (particle_periodic_bcs, boundary.F90:1019-1100), then the
+// zero-gradient ghost fill.  One CTA, the reference's phase order.
+__global__ void k_number_density_bcs(FView f, RunConst rc, int4 bcf) {
+  const int nx = rc.nx, ny = rc.ny, M = rc.M, nxg = rc.nxg, nyg = rc.nyg;
+  const int bcx0 = rc.bc_allspecies[CYL_BD_X_MIN], bcx1 = rc.bc_allspecies[CYL_BD_X_MAX];
+  const int bcy1 = rc.bc_allspecies[CYL_BD_Y_MAX];
+  const cplx Z = mk(0.0, 0.0);
+  if (bcx0 == CYL_BC_REFLECT)
+    for (int t = threadIdx.x; t < (NG - 1) * nyg * M; t += blockDim.x) {
+      const int i = 1 + t % (NG - 1), j = 1 - NG + (t / (NG - 1)) % nyg, m = t / ((NG - 1) * nyg);
+      f(i, j, m) = (cplx)f(i, j, m) + (cplx)f(1 - i, j, m);
+      f(1 - i, j, m) = Z;
+    }
+  __syncthreads();
+  if (bcx1 == CYL_BC_REFLECT)
+    for (int t = threadIdx.x; t < NG * nyg * M; t += blockDim.x) {
+      const int i = 1 + t % NG, j = 1 - NG + (t / NG) % nyg, m = t / (NG * nyg);
+      f(nx + 1 - i, j, m) = (cplx)f(nx + 1 - i, j, m) + (cplx)f(nx + i, j, m);
+      f(nx + i, j, m) = Z;
+    }
+  __syncthreads();
+  if (bcy1 == CYL_BC_REFLECT)
+    for (int t = threadIdx.x; t < NG * nxg * M; t += blockDim.x) {
+      const int i = 1 + t % NG, ix = 1 - NG + (t / NG) % nxg, m = t / (NG * nxg);
+      f(ix, ny + 1 - i, m) = (cplx)f(ix, ny + 1 - i, m) + (cplx)f(ix, ny + i, m);
+      f(ix, ny + i, m) = Z;
+    }
+  __syncthreads();
+  if (bcx0 == CYL_BC_PERIODIC) {
+    for (int t = threadIdx.x; t < NG * nyg * M; t += blockDim.x) {
+      const int i = 1 + t % NG, j = 1 - NG + (t / NG) % nyg, m = t / (NG * nyg);
+      f(i, j, m) = (cplx)f(i, j, m) + (cplx)f(nx + i, j, m);
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < NG * nyg * M; t += blockDim.x) {
+      const int i = 1 + t % NG, j = 1 - NG + (t / NG) % nyg, m = t / (NG * nyg);
+      f(nx - NG + i, j, m) = (cplx)f(nx - NG + i, j, m) + (cplx)f(i - NG, j, m);
+    }
+  }
+  __syncthreads();
+  // zero gradient, centre stagger: ghosts copy the mirrored interior cells
+  if (bcf.x != CYL_BC_PERIODIC)
+    for (int t = threadIdx.x; t < NG * nyg * M; t += blockDim.x) {
+      const int i = 1 + t % NG, j = 1 - NG + (t / NG) % nyg, m = t / (NG * nyg);
+      f(i - NG, j, m) = (cplx)f(NG + 1 - i, j, m);
+    }
+  __syncthreads();
+  if (bcf.y != CYL_BC_PERIODIC)
+    for (int t = threadIdx.x; t < NG * nyg * M; t += blockDim.x) {
+      const int i = 1 + t % NG, j = 1 - NG + (t / NG) % nyg, m = t / (NG * nyg);
+      f(nx + i, j, m) = (cplx)f(nx + 1 - i, j, m);
+    }
+  __syncthreads();
+  if (bcf.w != CYL_BC_PERIODIC)
+    for (int t = threadIdx.x; t < NG * nxg * M; t += blockDim.x) {
+      const int i = 1 + t % NG, ix = 1 - NG + (t / NG) % nxg, m = t / (NG * nxg);
+      f(ix, ny + i, m) = (cplx)f(ix, ny + 1 - i, m);
+    }
+}
+
+void launch_number_density(cudaStream_t s, const SpeciesPtrs& sp, const SpeciesCounters* cnt, const RunConst& rc,
+                           double x_grid_min, int nsh, bool mixed, const FView& out, int nblocks) {
+  if (mixed)
+    k_number_density<true><<<nblocks, 256, 0, s>>>(sp, cnt, rc, x_grid_min, nsh, out);
+  else
+    k_number_density<false><<<nblocks, 256, 0, s>>>(sp, cnt, rc, x_grid_min, nsh, out);
+}
+
+void launch_number_density_bcs(cudaStream_t s, const FView& out, const RunConst& rc, const int* bc_field) {
+  k_number_density_bcs<<<1, 1024, 0, s>>>(out, rc, make_int4(bc_field[0], bc_field[1], bc_field[2], bc_field[3]));
+}
+
 void launch_charge_density(cudaStream_t s, const SpeciesPtrs& sp, const SpeciesCounters* cnt,
                            const double* inv_volume, const RunConst& rc, double x_grid_min, int nsh,
                            bool mixed, const FView& rho, int nblocks) {

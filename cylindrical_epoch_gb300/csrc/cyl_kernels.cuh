@@ -63,7 +63,10 @@ void launch_push_fp64(cudaStream_t s, const FieldSet& F, const GeomTables& g, co
                       SpeciesCounters* cnt, const StepRec* rec, const RunConst& rc, int apply_bcs,
                       int* err, int nblocks);
 
-// charge.cu (continuity-residual diagnostic)
+// charge.cu (continuity-residual and number-density diagnostics)
+void launch_number_density(cudaStream_t s, const SpeciesPtrs& sp, const SpeciesCounters* cnt, const RunConst& rc,
+                           double x_grid_min, int nsh, bool mixed, const FView& out, int nblocks);
+void launch_number_density_bcs(cudaStream_t s, const FView& out, const RunConst& rc, const int* bc_field);
 void launch_charge_density(cudaStream_t s, const SpeciesPtrs& sp, const SpeciesCounters* cnt,
                            const double* inv_volume, const RunConst& rc, double x_grid_min, int nsh,
                            bool mixed, const FView& rho, int nblocks);

@@ -75,3 +75,58 @@ def continuity_residual(deck, rho0, rho1, jx, jr, jt, dt, margin=3):
         rel.append(nR / nD if nD > 0 else nR)
         ab.append(nR)
     return rel, ab
+
+
+def spectrum(p, mass):
+    """Weighted moments of the kinetic energy (MeV) of one species."""
+    mc = mass * 2.99792458e8
+    u2 = (p.px ** 2 + p.py ** 2 + p.pz ** 2) / mc ** 2
+    ke = mc * 2.99792458e8 * u2 / (np.sqrt(u2 + 1.0) + 1.0) / 1.602176565e-13
+    w = p.w / np.sum(p.w)
+    return {"mean_mev": float(np.sum(w * ke)), "rms_mev": float(np.sqrt(np.sum(w * ke ** 2))),
+            "m3_mev": float(np.cbrt(np.sum(w * ke ** 3))), "max_mev": float(np.max(ke))}
+
+
+def residual_step(run, deck, tries=8):
+    """Continuity residual of the next step of `run` that does not shift the
+    window (the charge densities must be on one grid)."""
+    for _ in range(tries):
+        s0 = run.state().n_shifts
+        r0 = run.charge_density()
+        run.step(1)
+        if run.state().n_shifts != s0:
+            continue
+        r1 = run.charge_density()
+        return continuity_residual(deck, r0, r1, run.field("jxm"), run.field("jrm"), run.field("jtm"),
+                                   deck.grid_desc().dt)[0]
+    return None
+
+
+def compare_runs(a, b, deck, residual=True):
+    """Error of run `a` against run `b` of the same deck after the same steps
+    (any objects with field, particles, state, charge_density and step, e.g.
+    a GPU run and the oracle): per-mode Ez relative L2, on-axis wake
+    amplitude (max |Re Ez_0| on r = 0), electron kinetic-energy moments,
+    particle counts and window shifts, and the continuity residual of one
+    further step of each (which advances both)."""
+    rel = lambda x, y: float(np.sqrt(np.sum(np.abs(x - y) ** 2) / max(np.sum(np.abs(y) ** 2), 1e-300)))
+    ea, eb = a.field("exm"), b.field("exm")
+    ez = [rel(ea[m], eb[m]) for m in range(deck.n_mode)]
+    ax = NG - 1  # exm row ir = 0 (r = 0) is array row ng - 1
+    lo, hi = abi.NG, abi.NG + deck.nx  # ix = 1 .. nx
+    wa = float(np.max(np.abs(ea[0, ax, lo:hi].real)))
+    wb = float(np.max(np.abs(eb[0, ax, lo:hi].real)))
+    spa = spectrum(a.particles(0), deck.species[0].mass)
+    spb = spectrum(b.particles(0), deck.species[0].mass)
+    sa, sb = a.state(), b.state()
+    out = {
+        "ez_rel_l2_per_mode": ez,
+        "wake_amplitude_v_per_m": {"run": wa, "against": wb, "rel_err": abs(wa - wb) / max(wb, 1e-300)},
+        "electron_spectrum": {"run": spa, "against": spb,
+                              "rel_err": {k: abs(spa[k] - spb[k]) / max(abs(spb[k]), 1e-300) for k in spa}},
+        "n_live": {"run": int(sa.n_live[0]), "against": int(sb.n_live[0])},
+        "n_shifts": {"run": int(sa.n_shifts), "against": int(sb.n_shifts)},
+    }
+    if residual:
+        out["continuity_residual_per_mode"] = {"run": residual_step(a, deck), "against": residual_step(b, deck)}
+    return out

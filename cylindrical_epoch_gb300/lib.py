@@ -43,6 +43,7 @@ SIGNATURES = {
     "cyl_cell_indices": (C.c_int, [H, I32, PI32, PI32, PI64]),
     "cyl_cell_indices_noalloc": (C.c_int, [H, I32, PI32, PI32, PI64]),
     "cyl_charge_density": (C.c_int, [H, PD]),
+    "cyl_number_density": (C.c_int, [H, I32, PD]),
     "cyl_tile_shape": (C.c_int, [I32, PI32, PI32]),
     "cyl_tune_tiles": (C.c_int, [H, I32, PI32]),
     "cyl_push_only": (C.c_int, [H]),

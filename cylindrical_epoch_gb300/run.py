@@ -162,6 +162,13 @@ class Run:
         abi.check("cyl_charge_density", self.lib.cyl_charge_density(self.h, _p(a.view(np.float64))))
         return a
 
+    def number_density(self, isp=-1):
+        """Per-mode number density of species isp, or of every species with
+        isp < 0 (cyl_number_density), shaped like field()."""
+        a = np.zeros((self.deck.n_mode, self.nyg, self.nxg), dtype=np.complex128)
+        abi.check("cyl_number_density", self.lib.cyl_number_density(self.h, int(isp), _p(a.view(np.float64))))
+        return a
+
     def upload_field(self, name, arr):
         which = abi.FIELD_INDEX[name] if isinstance(name, str) else name
         a = np.ascontiguousarray(arr, dtype=np.complex128)

@@ -268,6 +268,16 @@ int cyl_cell_indices_noalloc(cyl_handle h, int32_t ispecies, int32_t* cell_x,
  * mixed form evaluates it in FP64 from its stored state. */
 int cyl_charge_density(cyl_handle h, double* rho);
 
+/* Per-mode number density of species `ispecies` (every species when
+ * ispecies < 0), complex FP64 in the field layout: the reference's
+ * calc_number_density_modes (io/calc_df.F90:588-661) -- cell-centred triangle
+ * weights with the r < dy fold (include/triangle/gxfac.inc), each particle's
+ * weight over its macro-particle volume 2 pi dx dy r
+ * (housekeeping/partlist.F90:999-1013), mode factor 2 e^{i m theta} for
+ * m > 0, boundary sums (calc_df.F90:35-55) and zero-gradient ghosts.  The
+ * mixed form evaluates it in FP64 from its stored state. */
+int cyl_number_density(cyl_handle h, int32_t ispecies, double* out);
+
 /* ---- tile shape of the mixed form's push ------------------------------
  * The mixed form keeps particles sorted by tiles of tx x ty cells and pushes
  * one tile per CTA with the tile's fields staged in shared memory.  The push

@@ -1199,6 +1199,91 @@ void charge_density(Sim& s, Field& rho) {
   }
 }
 
+// particle_reflection_bcs for a real array, no flip (boundary.F90:833-915):
+// the centre-staggered number density folds its ghost rows back at
+// reflecting walls (applied to the real and imaginary parts alike).
+void density_reflection(Sim& s, Field& f) {
+  const int nx = s.nx, ny = s.ny, M = s.M;
+  const cplx Z = mk(0.0, 0.0);
+  for (int m = 0; m < M; ++m) {
+    if (s.bc_allspecies[CYL_BD_X_MIN] == CYL_BC_REFLECT)
+      for (int i = 1; i <= NG - 1; ++i)
+        for (int j = 1 - NG; j <= ny + NG; ++j) {
+          f(i, j, m) = f(i, j, m) + f(1 - i, j, m);
+          f(1 - i, j, m) = Z;
+        }
+    if (s.bc_allspecies[CYL_BD_X_MAX] == CYL_BC_REFLECT)
+      for (int i = 1; i <= NG; ++i)
+        for (int j = 1 - NG; j <= ny + NG; ++j) {
+          f(nx + 1 - i, j, m) = f(nx + 1 - i, j, m) + f(nx + i, j, m);
+          f(nx + i, j, m) = Z;
+        }
+    if (s.bc_allspecies[CYL_BD_Y_MAX] == CYL_BC_REFLECT)
+      for (int i = 1; i <= NG; ++i)
+        for (int ix = 1 - NG; ix <= nx + NG; ++ix) {
+          f(ix, ny + 1 - i, m) = f(ix, ny + 1 - i, m) + f(ix, ny + i, m);
+          f(ix, ny + i, m) = Z;
+        }
+  }
+}
+
+// calc_number_density_modes (calc_df.F90:588-661) for species isp, or every
+// species with particles when isp < 0: particle_to_grid.inc with
+// triangle/gxfac.inc (cell-centred weights; gy folded for r < dy), the macro
+// particle volume 2 pi dx dy r (partlist.F90:999-1013), the mode factor
+// 2 e^{i m theta} for m > 0, then calc_boundary_modes (calc_df.F90:35-55:
+// reflecting folds and periodic sums, no per-species bcs here) and
+// field_mode_zero_gradient on every boundary with the centre stagger (not
+// staggered along x or r, the stagger of btm).
+void number_density_modes(Sim& s, Field& out, int isp) {
+  std::fill(out.a.begin(), out.a.end(), mk(0, 0));
+  for (size_t k = 0; k < s.sp.size(); ++k) {
+    if (isp >= 0 && (int)k != isp) continue;
+    const Species& spc = s.sp[k];
+    for (size_t i = 0; i < spc.n(); ++i) {
+      const double wdata = spc.w[i];
+      const double part_r = std::sqrt(spc.y[i] * spc.y[i] + spc.z[i] * spc.z[i]);
+      const double cell_x_r = (spc.x[i] - s.x_grid_min) / s.dx;
+      const double cell_y_r = (part_r - s.y_grid_min) / s.dy;
+      int cell_x = ffloor(cell_x_r + 0.5), cell_y = ffloor(cell_y_r + 0.5);
+      const double fx = (double)cell_x - cell_x_r, fy = (double)cell_y - cell_y_r;
+      cell_x = cell_x + 1;
+      cell_y = cell_y + 1;
+      double gx[3], gy[3];
+      double c2 = fx * fx;
+      gx[0] = 0.5 * ((0.25 + c2) + fx);
+      gx[1] = 0.75 - c2;
+      gx[2] = 0.5 * ((0.25 + c2) - fx);
+      c2 = fy * fy;
+      gy[0] = 0.5 * ((0.25 + c2) + fy);
+      gy[1] = 0.75 - c2;
+      gy[2] = 0.5 * ((0.25 + c2) - fy);
+      if (part_r < s.dy) {
+        gy[1] = gy[1] + gy[0];
+        gy[0] = 0.0;
+      }
+      const double macro_part_volume = ((2.0 * PI) * s.dx) * s.dy * part_r;
+      const double part_num_dens = wdata / macro_part_volume;
+      const cplx exp_itheta = mk(spc.y[i] / part_r, spc.z[i] / part_r);
+      cplx exp_imtheta = mk(1.0, 0.0), mode_fac = mk(1.0, 0.0);
+      for (int im = 0; im < s.M; ++im) {
+        if (im > 0) {
+          exp_imtheta = exp_imtheta * exp_itheta;
+          mode_fac = 2.0 * exp_imtheta;
+        }
+        for (int iy = -1; iy <= 1; ++iy)
+          for (int ix = -1; ix <= 1; ++ix) {
+            cplx& d = out(cell_x + ix, cell_y + iy, im);
+            d = d + ((gx[ix + 1] * gy[iy + 1]) * part_num_dens) * mode_fac;
+          }
+      }
+    }
+  }
+  density_reflection(s, out);
+  periodic_sum(s, out);
+  for (int bd = 0; bd < 4; ++bd) zero_gradient(s, out, 5, bd);
+}
+
 // push_particles without the trailing current_bcs_r_min_final / particle_bcs
 void push_particles_core(Sim& s) {
   s.jx_old = s.jx; s.jr_old = s.jr; s.jt_old = s.jt;
@@ -1925,6 +2010,17 @@ int orc_charge_density(orc_handle h, double* data) {
   rho.init(s.nx, s.ny, s.M);
   charge_density(s, rho);
   std::memcpy(data, rho.a.data(), rho.a.size() * sizeof(cplx));
+  return 0;
+}
+
+// Per-mode number density (complex FP64, field layout) of species isp (< 0:
+// every species with particles).
+int orc_number_density(orc_handle h, int32_t isp, double* data) {
+  Sim& s = *(Sim*)h;
+  Field nd;
+  nd.init(s.nx, s.ny, s.M);
+  number_density_modes(s, nd, isp);
+  std::memcpy(data, nd.a.data(), nd.a.size() * sizeof(cplx));
   return 0;
 }
 

@@ -70,6 +70,7 @@ def load():
         "orc_diagnostics": (C.c_int, [H, C.POINTER(abi.Diag)]),
         "orc_cell_indices": (C.c_int, [H, C.c_int32, PI32, PI32]),
         "orc_charge_density": (C.c_int, [H, PD]),
+        "orc_number_density": (C.c_int, [H, C.c_int32, PD]),
         "orc_atan2": (C.c_double, [C.c_double, C.c_double]),
         "orc_set_threads": (None, [C.c_int32]),
         "orc_dx": (C.c_double, [H]),
@@ -187,6 +188,13 @@ class Oracle:
         t + dt/2 shape of the next push), complex (M, ny+2ng, nx+2ng)."""
         a = np.zeros((self.deck.n_mode, self.nyg, self.nxg), dtype=np.complex128)
         self.lib.orc_charge_density(self.h, a.view(np.float64).ctypes.data_as(C.POINTER(C.c_double)))
+        return a
+
+    def number_density(self, isp=-1):
+        """Per-mode number density (calc_number_density_modes) of species isp,
+        or of every species with isp < 0; complex (M, ny+2ng, nx+2ng)."""
+        a = np.zeros((self.deck.n_mode, self.nyg, self.nxg), dtype=np.complex128)
+        self.lib.orc_number_density(self.h, isp, a.view(np.float64).ctypes.data_as(C.POINTER(C.c_double)))
         return a
 
     def cell_indices(self, isp=0):

@@ -1,7 +1,7 @@
 """Mixed-precision form (int cell + FP32 offset, FP32 push/deposit into FP64
 currents) against the FP64 form and the oracle.
 
-Error bar (the benchmark spec): per-mode Ez (exm) relative L2 <= 1e-3 against the
+Error bar: per-mode Ez (exm) relative L2 <= 1e-3 against the
 FP64 result on the same deck; the other stated results (wake amplitude,
 electron energy moments, particle count) are compared with the same
 tolerance here.
@@ -153,3 +153,19 @@ def test_tune_tiles_keeps_state(gpu_lib):
     with pytest.raises(abi.CylError):
         b.tune_tiles()
     b.close()
+
+
+def test_mixed_number_density(gpu_lib):
+    """The mixed form's number density (evaluated in FP64 from its stored
+    state) against the FP64 form's after a windowed wakefield run."""
+    d64 = _wake(abi.PREC_FP64)
+    d32 = _wake(abi.PREC_MIXED)
+    parts, rng = cg.host_load(d64)
+    a = cg.Run(d64, particles=parts, rng=rng)
+    b = cg.Run(d32, particles=parts, rng=rng)
+    a.step(96)
+    b.step(96)
+    na, nb = a.number_density(), b.number_density()
+    for m in range(d64.n_mode):
+        e = rel_l2(nb[m], na[m])
+        assert e < TOL_EZ, (m, e)

@@ -1,6 +1,6 @@
 """Parity of the CUDA FP64 path against the CPU oracle (through the C ABI).
 
-Tolerances (the benchmark spec): particle counts and cell-sort indices bit-exact;
+Tolerances: particle counts and cell-sort indices bit-exact;
 positions and momenta bit-exact after a push from identical state (the FP64
 kernels are built without FMA contraction); per-mode fields and currents
 within 1e-10 relative L2, the slack being the order of the FP64 atomic
@@ -163,3 +163,18 @@ def test_wide_window_shift(gpu_lib):
         assert sg.n_shifts == so.n_shifts and sg.n_live[0] == so.n_live[0]
     assert so.n_shifts > 10
     _cmp_fields(gpu, orc, ["exm", "erm", "btm", "jxm"])
+
+
+def test_number_density_parity(gpu_lib):
+    """cyl_number_density (calc_number_density_modes) against the oracle
+    after a windowed laser-wakefield run, per mode, all species and one
+    species."""
+    deck = _small_wake()
+    gpu, orc = _pair(deck)
+    gpu.step(48)
+    orc.step(48)
+    assert orc.state().n_shifts > 0
+    for isp in (-1, 0):
+        a, b = gpu.number_density(isp), orc.number_density(isp)
+        for m in range(deck.n_mode):
+            assert rel_l2(a[m], b[m]) < TOL_FIELD, (isp, m)

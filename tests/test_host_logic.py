@@ -85,3 +85,23 @@ def test_server_without_device_reports_status(lib):
     with pytest.raises(abi.CylError) as e:
         serve.Server(0, 2)
     assert e.value.code == abi.CYL_ERR_NO_DEVICE
+
+
+def test_compare_runs_of_identical_runs():
+    """The run comparison used by the bench and the full-size oracle check:
+    two oracle runs of the same deck compare with zero error."""
+    oracle = pytest.importorskip("oracle.oracle")
+    import cylindrical_epoch_gb300 as cg
+    from cylindrical_epoch_gb300.diagnostics import compare_runs
+    deck = cg.wakefield(nx=64, ny=16, ppc=2, density=3.0e24, ramp=2.0e-6)
+    a = oracle.Oracle(deck, load_species=True)
+    b = oracle.Oracle(deck, load_species=True)
+    for o in (a, b):
+        o.initialise()
+        o.step(6)
+    r = compare_runs(a, b, deck)
+    assert r["ez_rel_l2_per_mode"] == [0.0] * deck.n_mode
+    assert r["n_live"]["run"] == r["n_live"]["against"] > 0
+    assert r["electron_spectrum"]["rel_err"]["mean_mev"] == 0.0
+    assert r["continuity_residual_per_mode"]["run"] == r["continuity_residual_per_mode"]["against"]
+    assert r["continuity_residual_per_mode"]["run"][0] < 1e-10  # round-off; the charge barely moves in 6 steps

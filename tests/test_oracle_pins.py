@@ -149,3 +149,20 @@ def test_charge_conservation_wakefield():
     assert orc.state().n_shifts == 0
     assert res[0] < 1e-12, res
     assert res[1] < 5e-2, res
+
+
+def test_number_density_of_loaded_plasma():
+    """calc_number_density_modes (calc_df.F90:588-661) of the loaded thermal
+    plasma against the deck's density (a physical input, not an oracle
+    output): mode 0 averages to 1e25 m^-3 over the interior within the
+    sampling noise, row by row down to the axis row (where the loader's and
+    the diagnostic's r < dy folds meet), and mode 1 has no mean."""
+    deck = thermal_plasma(nx=64, ny=32, ppc=16)
+    orc = oracle.Oracle(deck, load_species=True)
+    nd = orc.number_density()
+    n0 = nd[0][NG:NG + deck.ny, NG:NG + deck.nx].real
+    n_deck = deck.species[0].density
+    assert abs(n0[1:-1].mean() / n_deck - 1.0) < 0.01
+    for row in range(deck.ny - 1):
+        assert abs(n0[row].mean() / n_deck - 1.0) < 0.04, row
+    assert abs(nd[1][NG:NG + deck.ny, NG:NG + deck.nx].mean()) < 0.02 * n_deck
