@@ -179,5 +179,6 @@ struct SpeciesPtrs {
 constexpr int ERR_CAPACITY = 1;
 constexpr int ERR_CELL_RANGE = 2;    // particle stencil left the ghosted grid
 constexpr int ERR_NONFINITE = 4;
+constexpr int ERR_TMA_TIMEOUT = 8;  // a TMA tile copy did not complete within its bounded wait
 
 }  // namespace cyl

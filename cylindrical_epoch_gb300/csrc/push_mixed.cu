@@ -20,6 +20,12 @@
 // region (it drifted since the last sort) is deferred to a second kernel that
 // gathers from global memory and adds each contribution with an FP64 atomic;
 // so are the particles the moving window appended since the last sort.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <cstring>
+#include <mutex>
+
 #include "cyl_common.cuh"
 #include "cyl_convert.cuh"
 #include "cyl_kernels.cuh"
@@ -41,6 +47,14 @@ constexpr int DRIFT = 1;                    // cells a particle may drift from i
 constexpr int RW = TILE_X + 2 * DRIFT + 5;  // staged region width (x)
 constexpr int RH = TILE_Y + 2 * DRIFT + 5;  // staged region height (r)
 constexpr int RCELLS = RW * RH;
+// Modes m >= 1 are staged by TMA (cp.async.bulk.tensor) as boxes of TW x RH
+// complex values: the box's first column is the staged region's first column
+// rounded down to an even index (a TMA copy starts on a 16-byte boundary, two
+// 8-byte complex values), so TW = RW + 1 covers the region; each plane starts
+// on a 128-byte boundary.
+constexpr int TW = RW + 1;
+static_assert((TW * 8) % 16 == 0, "TMA box rows must be whole 16-byte units");
+constexpr int TPLANE = ((TW * RH * 8 + 127) / 128) * 128 / 8;  // float2 per TMA plane
 constexpr int PUSH_THREADS = 256;
 #ifndef PUSH_MIN_BLOCKS
 #define PUSH_MIN_BLOCKS 3  // resident CTAs per SM the register budget is sized for
@@ -102,8 +116,10 @@ __device__ __forceinline__ void mode_factors(float phi, f2 eip, f2& F2, f2& F3, 
 // current accumulators [3][M][re, im][hi, lo][RCELLS] int32 (fixed point,
 // see sadd).
 struct Tile {
-  const float2* sf;
+  const float2* sf;  // mode-0 planes (RCELLS cells each)
+  const float2* tm;  // modes m >= 1: TMA planes (TPLANE float2 each, row pitch TW)
   int* sj;
+  int xs;           // Fortran x index of the TMA boxes' first column
   int x0, y0;       // Fortran indices of the staged region's first cell
   float s_xr, s_t;  // accumulator units per unit of jx / jr and of jtheta flux
 };
@@ -124,17 +140,17 @@ __device__ __forceinline__ void tile_scales(Tile& t, int64_t n, float qw_max, fl
   t.s_t = bt > 0.f ? 1073741824.0f / bt : 0.f;
 }
 
-// Staged fields of a tile, in shared memory (RCELLS cells per plane):
-//   plane 0: float2 {Re Ex_0, Re Br_0}   plane 1: float2 {Re Er_0, Re Bx_0}
-//   plane 2: float {Re Et_0} then float {Re Bt_0} (one float2 plane)
-//   planes 3..: float2 complex F_m of field q, m >= 1, at 3 + q (M-1) + m - 1
+// Staged fields of a tile, in shared memory:
+//   mode 0 (RCELLS cells per plane, row pitch RW):
+//     plane 0: float2 {Re Ex_0, Re Br_0}   plane 1: float2 {Re Er_0, Re Bx_0}
+//     plane 2: float {Re Et_0} then float {Re Bt_0} (one float2 plane)
+//   modes m >= 1: float2 complex F_m of field q in TMA plane q (M-1) + m - 1
+//     (TPLANE float2 each, row pitch TW, first column at Fortran x = xs)
 // Mode 0 contributes Re F_0 alone; Ex and Br share their stencil (gx along
 // x at cell_x1, hy along r at cell_y2), and so do Er and Bx (hx at cell_x2,
 // gy at cell_y1), so each pair is gathered by one 64-bit load and one
 // paired FMA.
 constexpr int PLANES_M0 = 3;
-template <int M>
-constexpr int staged_planes() { return PLANES_M0 + 6 * (M - 1); }
 
 template <int M, bool SHARED>
 struct Gather {
@@ -168,7 +184,7 @@ struct Gather {
   }
   // complex F_m of field q (m >= 1)
   __device__ __forceinline__ static float2 get(const FieldSetF& F, const Tile& t, int q, int m, int x, int y) {
-    if (SHARED) return t.sf[(PLANES_M0 + q * (M - 1) + m - 1) * RCELLS + cell(t, x, y)];
+    if (SHARED) return t.tm[(q * (M - 1) + m - 1) * TPLANE + (y - t.y0) * TW + (x - t.xs)];
     return *reinterpret_cast<const float2*>(view(F, q).ptr(x, y, m));
   }
 };
@@ -665,13 +681,67 @@ __device__ __forceinline__ void set_bounds(MixedParams& P, const StepRec* rec, c
   P.x_out_hi = P.x_sys_hi + 2.0f;
 }
 
+// Tensor maps of the six FP32 E/B arrays (8-byte complex elements, dims
+// nxg x nyg x M, box TW x RH x 1), one set per launch.
+struct TmaSet {
+  CUtensorMap map[6];
+};
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Wait for phase `parity` of the barrier, at most `limit` polls.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, int limit) {
+  for (int k = 0; k < limit; ++k) {
+    if (mbar_try_wait(bar, parity)) return true;
+    __nanosleep(64);
+  }
+  return false;
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Polls of the TMA barrier before a tile gives up (with 64 ns sleeps: about
+// a second).
+constexpr int TMA_WAIT_POLLS = 1 << 24;
+
 template <int M>
-__global__ void __launch_bounds__(PUSH_THREADS, PUSH_MIN_BLOCKS) k_push_tiles(FieldSetF F, SpeciesPtrs sp, SpeciesCounters* cnt,
-                                                             const StepRec* rec, RunConst rc, MixedParams P,
-                                                             TileTable* tt, int apply_bcs) {
+__global__ void __launch_bounds__(PUSH_THREADS, PUSH_MIN_BLOCKS) k_push_tiles(
+    FieldSetF F, SpeciesPtrs sp, SpeciesCounters* cnt, const StepRec* rec, RunConst rc, MixedParams P, TileTable* tt,
+    int apply_bcs, const __grid_constant__ TmaSet tma, int use_tma) {
   extern __shared__ float4 smem4[];
-  float2* sf = reinterpret_cast<float2*>(smem4);                       // staged_planes<M>() * RCELLS float2
-  int* sj = reinterpret_cast<int*>(sf + staged_planes<M>() * RCELLS);  // 3 * M * 4 * RCELLS int32
+  __shared__ uint64_t tma_bar;
+  __shared__ int tma_failed;
+  // dynamic shared memory: 128-byte aligned TMA planes, mode-0 planes, accumulators
+  char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(smem4) + 127) & ~(uintptr_t)127);
+  float2* tm = reinterpret_cast<float2*>(base);                             // 6 (M-1) TPLANE float2
+  float2* sf = tm + 6 * (M - 1) * TPLANE;                                   // PLANES_M0 RCELLS float2
+  int* sj = reinterpret_cast<int*>(sf + PLANES_M0 * RCELLS);                // 3 M 4 RCELLS int32
+  if (threadIdx.x == 0) {
+    tma_failed = 0;
+    if (use_tma) mbar_init(&tma_bar);
+  }
+  __syncthreads();
+  unsigned tma_phase = 0;
   const int nsh = rec->nshift_total;
   const float qw_max = fabsf(P.q_fac) * __uint_as_float(cnt->wmax_bits);
   set_bounds(P, rec, rc);
@@ -685,9 +755,11 @@ __global__ void __launch_bounds__(PUSH_THREADS, PUSH_MIN_BLOCKS) k_push_tiles(Fi
     const int64_t p0 = tt->start[t], p1 = tt->start[t + 1];
     Tile tile;
     tile.sf = sf;
+    tile.tm = tm;
     tile.sj = sj;
     tile.x0 = (tt->tx_min + t % ntx) * TILE_X - nsh + 1 - DRIFT - 2;
     tile.y0 = (t / ntx) * TILE_Y + 1 - DRIFT - 2;
+    tile.xs = tile.x0 - (((tile.x0 % 2) + 2) % 2);  // rounded down to even
     const bool inside = tile.x0 >= 1 - NG && tile.x0 + RW - 1 <= rc.nx + NG && tile.y0 >= 1 - NG &&
                         tile.y0 + RH - 1 <= rc.ny + NG;
     if (p1 <= p0) continue;
@@ -696,8 +768,15 @@ __global__ void __launch_bounds__(PUSH_THREADS, PUSH_MIN_BLOCKS) k_push_tiles(Fi
       for (int64_t i = p0 + threadIdx.x; i < p1; i += PUSH_THREADS) P.fb_list[atomicAdd(P.fb_count, 1)] = (int)i;
       continue;
     }
-    // stage E and B (FP32; mode 0 as real pairs, see Gather) and clear the
-    // accumulators
+    // stage E and B (FP32): modes m >= 1 by TMA boxes (issued first, they
+    // arrive while mode 0 is staged by plain loads as real pairs, see Gather)
+    if (M > 1 && use_tma && threadIdx.x == 0) {
+      mbar_expect_tx(&tma_bar, (unsigned)(6 * (M - 1) * TW * RH * 8));
+      for (int q = 0; q < 6; ++q)
+        for (int m = 1; m < M; ++m)
+          tma_load_3d(tm + (q * (M - 1) + m - 1) * TPLANE, &tma.map[q], tile.xs + NG - 1, tile.y0 + NG - 1, m,
+                      &tma_bar);
+    }
     {
       using G = Gather<M, false>;
       float* s_t = reinterpret_cast<float*>(sf + 2 * RCELLS);
@@ -708,19 +787,37 @@ __global__ void __launch_bounds__(PUSH_THREADS, PUSH_MIN_BLOCKS) k_push_tiles(Fi
         s_t[c] = G::re0(F, 2, x, y);
         s_t[RCELLS + c] = G::re0(F, 5, x, y);
       }
+      if (M > 1 && !use_tma) {
+        // the same boxes by plain loads (row pitches that TMA cannot take)
 #pragma unroll 1
-      for (int q = 0; q < 6; ++q) {
-        const FViewF v = G::view(F, q);
+        for (int q = 0; q < 6; ++q) {
+          const FViewF v = G::view(F, q);
 #pragma unroll 1
-        for (int m = 1; m < M; ++m)
-          for (int c = threadIdx.x; c < RCELLS; c += PUSH_THREADS)
-            sf[(PLANES_M0 + q * (M - 1) + m - 1) * RCELLS + c] =
-                *reinterpret_cast<const float2*>(v.ptr(tile.x0 + c % RW, tile.y0 + c / RW, m));
+          for (int m = 1; m < M; ++m)
+            for (int c = threadIdx.x; c < TW * RH; c += PUSH_THREADS) {
+              const int x = tile.xs + c % TW, y = tile.y0 + c / TW;
+              tm[(q * (M - 1) + m - 1) * TPLANE + c] =
+                  x <= rc.nx + NG ? *reinterpret_cast<const float2*>(v.ptr(x, y, m)) : make_float2(0.f, 0.f);
+            }
+        }
       }
+    }
+    if (M > 1 && use_tma) {
+      // every thread waits for the boxes (the barrier's completion makes the
+      // copies visible to the waiting thread); a wait that runs out flags the
+      // run, waits once more for copies in flight, and the CTA leaves at the
+      // next barrier
+      if (!mbar_wait_bounded(&tma_bar, tma_phase, TMA_WAIT_POLLS)) {
+        atomicOr(P.err, ERR_TMA_TIMEOUT);
+        mbar_wait_bounded(&tma_bar, tma_phase, TMA_WAIT_POLLS);
+        tma_failed = 1;
+      }
+      tma_phase ^= 1u;
     }
     for (int e = threadIdx.x; e < 3 * M * 4 * RCELLS; e += PUSH_THREADS) sj[e] = 0;
     tile_scales(tile, p1 - p0, qw_max, P.idt, P.c);
     __syncthreads();
+    if (tma_failed) return;  // uniform: read by every thread after the barrier
     for (int64_t i = p0 + threadIdx.x; i < p1; i += PUSH_THREADS) {
       if (!push_one<M, true>(i, sp, cnt, F, P, rc, tile, nsh, apply_bcs))
         P.fb_list[atomicAdd(P.fb_count, 1)] = (int)i;
@@ -760,7 +857,7 @@ __global__ void __launch_bounds__(PUSH_THREADS) k_push_global(FieldSetF F, Speci
   const int64_t nlist = *P.fb_count;
   const int64_t n_sorted = tt->n_sorted, n_used = cnt->n_used;
   const int64_t ntail = n_used > n_sorted ? n_used - n_sorted : 0;
-  Tile none{nullptr, nullptr, 0, 0, 0.f, 0.f};
+  Tile none{nullptr, nullptr, nullptr, 0, 0, 0, 0.f, 0.f};
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nlist + ntail;
        t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = (t < nlist) ? (int64_t)P.fb_list[t] : n_sorted + (t - nlist);
@@ -769,7 +866,44 @@ __global__ void __launch_bounds__(PUSH_THREADS) k_push_global(FieldSetF F, Speci
 }
 
 size_t push_mixed_smem(int M) {
-  return (size_t)(PLANES_M0 + 6 * (M - 1)) * RCELLS * sizeof(float2) + (size_t)12 * M * RCELLS * sizeof(int);
+  return 128 + (size_t)6 * (M - 1) * TPLANE * sizeof(float2) + (size_t)PLANES_M0 * RCELLS * sizeof(float2) +
+         (size_t)12 * M * RCELLS * sizeof(int);
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (null if
+// the driver does not provide it: the push then stages by plain loads).
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+// Tensor maps of the six FP32 E/B arrays for the TMA staging.  Returns false
+// (plain-load staging) when the rows cannot be described: a row pitch or base
+// that is not a multiple of 16 bytes, or no encoder.
+static bool make_tma_set(const FieldSetF& F, const RunConst& rc, TmaSet* out) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc || rc.M < 2 || ((size_t)rc.nxg * 8) % 16 != 0) return false;
+  const cplxf* bases[6] = {F.ex.p, F.er.p, F.et.p, F.bx.p, F.br.p, F.bt.p};
+  const cuuint64_t dims[3] = {(cuuint64_t)rc.nxg, (cuuint64_t)rc.nyg, (cuuint64_t)rc.M};
+  const cuuint64_t strides[2] = {(cuuint64_t)rc.nxg * 8, (cuuint64_t)rc.nxg * rc.nyg * 8};
+  const cuuint32_t box[3] = {(cuuint32_t)TW, (cuuint32_t)RH, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  for (int q = 0; q < 6; ++q) {
+    if ((reinterpret_cast<uintptr_t>(bases[q]) & 15) != 0) return false;
+    if (enc(&out->map[q], CU_TENSOR_MAP_DATA_TYPE_INT64, 3, const_cast<cplxf*>(bases[q]), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return false;
+  }
+  return true;
 }
 
 int push_mixed_blocks_per_sm(int M) {
@@ -794,11 +928,14 @@ void launch_push_mixed(cudaStream_t s, const FieldSetF& F, const SpeciesPtrs& sp
                        const StepRec* rec, const RunConst& rc, int apply_bcs, int nblocks_tiles,
                        int nblocks_global, const MixedParams& P, TileTable* tt) {
   const size_t smem = push_mixed_smem(rc.M);
+  TmaSet tma;
+  std::memset(&tma, 0, sizeof(tma));
+  const int use_tma = make_tma_set(F, rc, &tma) ? 1 : 0;
   cudaMemsetAsync(P.fb_count, 0, sizeof(int), s);
   switch (rc.M) {
 #define CASE(MM)                                                                                    \
   case MM:                                                                                          \
-    k_push_tiles<MM><<<nblocks_tiles, PUSH_THREADS, smem, s>>>(F, sp, cnt, rec, rc, P, tt, apply_bcs); \
+    k_push_tiles<MM><<<nblocks_tiles, PUSH_THREADS, smem, s>>>(F, sp, cnt, rec, rc, P, tt, apply_bcs, tma, use_tma); \
     k_push_global<MM><<<nblocks_global, PUSH_THREADS, 0, s>>>(F, sp, cnt, rec, rc, P, tt, apply_bcs);  \
     break;
     CASE(1) CASE(2) CASE(3) CASE(4)
