@@ -362,13 +362,8 @@ def main():
     s1 = run.state()
     n_end = sum(s1.n_live[i] for i in range(len(deck.species)) if not deck.species[i].immobile)
     psteps = 0.5 * (n_start + n_end) * args.steps
-    if dist:
-        t = torch.tensor([elapsed, psteps], dtype=torch.float64, device="cuda")
-        tm = t.clone()
-        dist.all_reduce(tm[:1], op=dist.ReduceOp.MAX)
-        dist.all_reduce(t[1:], op=dist.ReduceOp.SUM)
-        elapsed, psteps = float(tm[0]), float(t[1])
-    value = psteps / elapsed
+    from cylindrical_epoch_gb300.replicas import reduce_replicas
+    elapsed, psteps, value = reduce_replicas(elapsed, psteps, dist, "cuda")
 
     # roofline of the dominant kernel (push + deposit): algorithmic bytes per
     # particle-step = particle state in + out + amortised field read (6 E/B
@@ -428,11 +423,7 @@ def main():
     if not args.no_e2e:
         e2e = e2e_run(deck, parts, rng, args.steps, graph)
         if dist:
-            t = torch.tensor([e2e["seconds"], e2e["psteps"]], dtype=torch.float64, device="cuda")
-            tm = t.clone()
-            dist.all_reduce(tm[:1], op=dist.ReduceOp.MAX)
-            dist.all_reduce(t[1:], op=dist.ReduceOp.SUM)
-            e2e["value"] = float(t[1]) / float(tm[0])
+            e2e["value"] = reduce_replicas(e2e["seconds"], e2e["psteps"], dist, "cuda")[2]
     base = None
     if rank == 0 and world == 1 and not args.no_cpu:
         base = cpu_baseline(build_deck(args.deck, "fp64"), parts, rng)
