@@ -10,6 +10,7 @@ import numpy as np
 import pytest
 
 import cylindrical_epoch_gb300 as cg
+from cylindrical_epoch_gb300 import abi
 from tests.helpers import match_by_id, random_fields, rel_l2
 
 pytestmark = pytest.mark.gpu
@@ -178,3 +179,60 @@ def test_number_density_parity(gpu_lib):
         a, b = gpu.number_density(isp), orc.number_density(isp)
         for m in range(deck.n_mode):
             assert rel_l2(a[m], b[m]) < TOL_FIELD, (isp, m)
+
+
+def _steps_parity(deck, nsteps=10, fields=("exm", "erm", "etm", "bxm", "brm", "btm", "jxm", "jrm", "jtm")):
+    gpu, orc = _pair(deck)
+    gpu.step(1)
+    orc.step(1)
+    for isp in range(len(deck.species)):
+        a, b = match_by_id(gpu.particles(isp), orc.particles(isp))
+        for k in ("x", "y", "z", "px", "py", "pz"):
+            assert np.array_equal(getattr(a, k), getattr(b, k)), (isp, k)
+    gpu.step(nsteps - 1)
+    orc.step(nsteps - 1)
+    sg, so = gpu.state(), orc.state()
+    for isp in range(len(deck.species)):
+        assert sg.n_live[isp] == so.n_live[isp], isp
+    _cmp_fields(gpu, orc, list(fields))
+    return gpu, orc
+
+
+@pytest.mark.parametrize("n_mode", [3, 4])
+def test_more_modes_parity(gpu_lib, n_mode):
+    """Modes m = 0..2 and 0..3 (the scan decks and the large deck)."""
+    _steps_parity(cg.thermal_plasma(nx=48, ny=24, ppc=4, n_mode=n_mode))
+
+
+def test_two_mobile_species_parity(gpu_lib):
+    """Electrons and mobile thermal protons: both pushed, both deposit."""
+    from cylindrical_epoch_gb300.deck import EV, KB, M0, Q0, Species
+    deck = cg.thermal_plasma(nx=48, ny=24, ppc=4)
+    t_k = 100.0 * EV / KB
+    p = Species("proton", Q0, 1836.15267245 * M0, 2, 1.0e25, temp_k=(t_k, t_k, t_k), bc=deck.species[0].bc)
+    p.capacity = 2 * deck.nx * deck.ny * 2 + 1024
+    deck.species.append(p)
+    _steps_parity(deck)
+
+
+def test_reflecting_walls_parity(gpu_lib):
+    """Reflecting particle walls and conducting field walls at both x ends
+    (boundary.F90:1561-1569, the reflection folding of current_finish)."""
+    deck = cg.thermal_plasma(nx=40, ny=20, ppc=6)
+    walls = (abi.BC_REFLECT, abi.BC_REFLECT, abi.BC_OTHER, abi.BC_CONDUCT)
+    deck.species[0].bc = walls
+    deck.bc_field = (abi.BC_CONDUCT, abi.BC_CONDUCT, abi.BC_OTHER, abi.BC_CONDUCT)
+    _steps_parity(deck, nsteps=30)
+
+
+def test_current_smoothing_parity(gpu_lib):
+    """smooth_mode_array (current_smooth.F90:145-196): two binomial passes and
+    one compensation pass on a windowed laser wakefield."""
+    deck = _small_wake()
+    deck.smooth_currents, deck.smooth_its, deck.smooth_comp_its, deck.smooth_stride = 1, 2, 1, 1
+    gpu, orc = _pair(deck)
+    gpu.step(40)
+    orc.step(40)
+    assert gpu.state().n_live[0] == orc.state().n_live[0]
+    assert orc.state().n_shifts > 0
+    _cmp_fields(gpu, orc, ["exm", "erm", "btm", "jxm", "jrm", "jtm"])
