@@ -344,42 +344,42 @@ static void push_all(Handle* h, cudaStream_t s, const FieldSetF& F, const StepRe
   }
 }
 
-// Enqueue the kernels of one step; rec/src point at this step's records.
+// The kernels of one step before the push: update_eb_fields_half
+// (fields.f90:316-337), then J_old = J, J = 0 (particles.F90:163-169) by
+// buffer swap.  Returns the field set of the push.
 template <typename T>
-static void enqueue_step_t(Handle* h, const StepRec* rec, const double* src, int k_in_chunk, bool timing,
-                           bool capturing) {
-  const unsigned evflag = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
-  cudaStream_t s = h->st;
+static FieldSetT<T> enqueue_step_pre(Handle* h, cudaStream_t s, const StepRec* rec) {
   const RunConst& rc = h->rc;
   FieldSetT<T> F = fieldset_t<T>(h, h->jpar);
-  // update_eb_fields_half (fields.f90:316-337)
   bulk_e(h, s, F);
   launch_e_axis_bcs(s, F, rec, rc);
   bulk_b(h, s, F, 1);
   launch_b_axis_bcs(s, F, rec, rc);
   count_launch(h, 6);
-  // push_particles: J_old = J, J = 0 (particles.F90:163-169) by buffer swap
   h->jpar ^= 1;
   F = fieldset_t<T>(h, h->jpar);
   const size_t bytes = h->fcount * sizeof(cplx);
   cudaMemsetAsync(F.jx.p, 0, bytes, s);
   cudaMemsetAsync(F.jr.p, 0, bytes, s);
   cudaMemsetAsync(F.jt.p, 0, bytes, s);
-  if (timing) cudaEventRecordWithFlags(h->ev_push[k_in_chunk][0], s, evflag);
-  push_all(h, s, F, rec, 1);
-  if (timing) cudaEventRecordWithFlags(h->ev_push[k_in_chunk][1], s, evflag);
-  // current_bcs_r_min_final + current_finish
+  return F;
+}
+
+// The kernels of one step after the push: current_bcs_r_min_final and
+// current_finish, update_eb_fields_final (fields.f90:341-353), moving_window.
+template <typename T>
+static void enqueue_step_post(Handle* h, cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec,
+                              const double* src) {
+  const RunConst& rc = h->rc;
   FView wk{h->F[15], rc.nxg, rc.nyg};
   launch_current_finish(s, F, rec, rc, h->gd.smooth_currents, h->gd.smooth_its, h->gd.smooth_comp_its,
                         h->gd.smooth_stride > 0 ? h->gd.smooth_stride : 1, wk);
   count_launch(h, 2);
-  // update_eb_fields_final (fields.f90:341-353)
   bulk_b(h, s, F, 0);
   launch_b_final_bcs(s, F, rec, src, h->cols, 1, rc.dt, rc);
   bulk_e(h, s, F);
   launch_e_axis_bcs(s, F, rec, rc);
   count_launch(h, 6);
-  // moving_window
   if (h->move_window) {
     for (int i = 0; i < h->nsp; ++i) {
       if (h->prec == CYL_PREC_MIXED)
@@ -392,6 +392,19 @@ static void enqueue_step_t(Handle* h, const StepRec* rec, const double* src, int
     launch_shift_fields(s, F, h->cols, rec, 1, rc);
     count_launch(h, 2);
   }
+}
+
+// Enqueue the kernels of one step; rec/src point at this step's records.
+template <typename T>
+static void enqueue_step_t(Handle* h, const StepRec* rec, const double* src, int k_in_chunk, bool timing,
+                           bool capturing) {
+  const unsigned evflag = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+  cudaStream_t s = h->st;
+  const FieldSetT<T> F = enqueue_step_pre<T>(h, s, rec);
+  if (timing) cudaEventRecordWithFlags(h->ev_push[k_in_chunk][0], s, evflag);
+  push_all(h, s, F, rec, 1);
+  if (timing) cudaEventRecordWithFlags(h->ev_push[k_in_chunk][1], s, evflag);
+  enqueue_step_post<T>(h, s, F, rec, src);
 }
 
 static void enqueue_step(Handle* h, const StepRec* rec, const double* src, int k_in_chunk, bool timing,
@@ -647,6 +660,74 @@ using namespace cyl;
 struct cyl_handle_s {
   Handle h;
 };
+
+// A batch: mixed-form runs with the same number of modes stepped together,
+// their pushes one launch per step over a shared (job, tile) work table (a
+// job is one mobile species of one run).  The stages before and after the
+// push stay per run, on each run's own stream, forked from and joined to the
+// batch stream around the push; a chunk of 16 steps is one CUDA graph,
+// captured again when the membership or a run's current parity changes.
+struct cyl_batch_s {
+  int device = 0;
+  int cap_runs = 0, cap_jobs = 0;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev_sched = nullptr, ev_push = nullptr, ev_done = nullptr, ev_jobs = nullptr;
+  std::vector<cudaEvent_t> ev_run;  // one per run slot
+  BatchJob* h_jobs = nullptr;       // pinned, CHUNK x cap_jobs (step-major)
+  BatchJob* d_jobs = nullptr;
+  int2* d_work = nullptr;
+  int* d_nwork = nullptr;
+  int64_t work_cap = 0;
+  bool jobs_pending = false;
+  cudaGraphExec_t gexec = nullptr;
+  std::vector<Handle*> g_runs;  // membership and parities of the captured graph
+  std::vector<int> g_par;
+  int g_jobs = 0;
+};
+
+namespace cyl {
+
+struct JobRef {
+  Handle* h;
+  int isp;
+};
+
+// The kernels of k steps of a batch, on b->st with each run's stream forked
+// and joined around every push; the chunk's (job, tile) table first, every
+// run's sort last.
+static void enqueue_batch_chunk(cyl_batch_s* b, const std::vector<Handle*>& runs, int njobs, int k, int M) {
+  const PushMixedFns& fns = push_mixed_fns(0);
+  const int nbt = runs[0]->nblocks_by_shape[0], nbg = runs[0]->nblocks;
+  batch_schedule(b->st, b->d_jobs, njobs, b->d_work, b->d_nwork);
+  cudaEventRecord(b->ev_sched, b->st);
+  std::vector<FieldSetF> F(runs.size());
+  for (int i = 0; i < k; ++i) {
+    for (size_t r = 0; r < runs.size(); ++r) {
+      Handle* h = runs[r];
+      cudaStreamWaitEvent(h->st, i == 0 ? b->ev_sched : b->ev_push, 0);
+      F[r] = enqueue_step_pre<cplxf>(h, h->st, h->d_rec + i);
+      cudaEventRecord(b->ev_run[r], h->st);
+      cudaStreamWaitEvent(b->st, b->ev_run[r], 0);
+    }
+    const BatchJob* tab = b->d_jobs + (size_t)i * b->cap_jobs;
+    batch_reset(b->st, tab, njobs);
+    fns.launch_batch(b->st, M, tab, njobs, b->d_work, b->d_nwork, nbt, nbg);
+    cudaEventRecord(b->ev_push, b->st);
+    for (size_t r = 0; r < runs.size(); ++r) {
+      Handle* h = runs[r];
+      cudaStreamWaitEvent(h->st, b->ev_push, 0);
+      enqueue_step_post<cplxf>(h, h->st, F[r], h->d_rec + i, h->d_src + h->src_per_step * i);
+    }
+  }
+  for (size_t r = 0; r < runs.size(); ++r) {
+    Handle* h = runs[r];
+    enqueue_sort(h, h->d_rec + (k - 1));
+    cudaEventRecord(b->ev_run[r], h->st);
+    cudaStreamWaitEvent(b->st, b->ev_run[r], 0);
+  }
+}
+
+}  // namespace cyl
 
 extern "C" {
 
@@ -1497,6 +1578,176 @@ int cyl_cell_indices(cyl_handle hh, int32_t isp, int32_t* cx, int32_t* cy, int64
     ++k;
   }
   *n_inout = k;
+  return CYL_OK;
+}
+
+int cyl_batch_create(int32_t max_runs, cyl_batch* out) {
+  if (!out || max_runs < 1 || max_runs > 1024) return CYL_ERR_BAD_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return CYL_ERR_NO_DEVICE;
+  auto* b = new cyl_batch_s();
+  cudaError_t e = cudaGetDevice(&b->device);
+  b->cap_runs = max_runs;
+  b->cap_jobs = max_runs * MAX_SPECIES;
+  auto ok = [&e](cudaError_t r) {
+    if (r != cudaSuccess && e == cudaSuccess) e = r;
+  };
+  ok(cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking));
+  for (cudaEvent_t* ev : {&b->ev_sched, &b->ev_push, &b->ev_done, &b->ev_jobs})
+    ok(cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
+  b->ev_run.assign((size_t)max_runs, nullptr);
+  for (auto& ev : b->ev_run) ok(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  const size_t tab = sizeof(BatchJob) * (size_t)CHUNK * b->cap_jobs;
+  ok(cudaMallocHost(&b->h_jobs, tab));
+  ok(cudaMalloc(&b->d_jobs, tab));
+  ok(cudaMalloc(&b->d_nwork, sizeof(int)));
+  if (e != cudaSuccess) {
+    cyl_batch_destroy(b);
+    return e == cudaErrorMemoryAllocation ? CYL_ERR_OUT_OF_MEMORY : CYL_ERR_CUDA;
+  }
+  *out = b;
+  return CYL_OK;
+}
+
+int cyl_batch_step(cyl_batch b, const cyl_handle* hs, int32_t n, int32_t nsteps) {
+  if (!b || !hs || n < 1 || n > b->cap_runs || nsteps < 0) return CYL_ERR_BAD_ARG;
+  std::vector<Handle*> runs;
+  std::vector<JobRef> jobs;
+  int M = -1;
+  int64_t need = 0;
+  for (int r = 0; r < n; ++r) {
+    if (!hs[r]) return CYL_ERR_BAD_ARG;
+    Handle* h = &hs[r]->h;
+    if (h->prec != CYL_PREC_MIXED) return CYL_ERR_UNSUPPORTED;
+    if (h->device != b->device) return CYL_ERR_BAD_ARG;
+    if (M < 0) M = h->rc.M;
+    if (h->rc.M != M) return CYL_ERR_UNSUPPORTED;
+    for (Handle* q : runs)
+      if (q == h) return CYL_ERR_BAD_ARG;
+    runs.push_back(h);
+    for (int i = 0; i < h->nsp; ++i)
+      if (!h->sp[i].immobile) {
+        jobs.push_back({h, i});
+        need += h->ntiles_max;
+      }
+  }
+  const int nj = (int)jobs.size();
+  if (nj > b->cap_jobs) return CYL_ERR_BAD_ARG;
+  // every run on the batch kernel's tile shape (shape 0), sorted for it
+  for (int r = 0; r < n; ++r)
+    if (runs[r]->tile_shape != 0) {
+      int32_t shape = 0;
+      if (int rc = cyl_tune_tiles(hs[r], CYL_TUNE_SET, &shape)) return rc;
+    }
+  if (need > b->work_cap) {
+    cudaStreamSynchronize(b->st);
+    cudaFree(b->d_work);
+    b->d_work = nullptr;
+    if (cudaMalloc(&b->d_work, sizeof(int2) * (size_t)need) != cudaSuccess) return CYL_ERR_OUT_OF_MEMORY;
+    b->work_cap = need;
+    if (b->gexec) {
+      cudaGraphExecDestroy(b->gexec);
+      b->gexec = nullptr;
+    }
+  }
+  int32_t done = 0;
+  while (done < nsteps) {
+    const int k = nsteps - done < CHUNK ? nsteps - done : CHUNK;
+    // each run's step records and host inputs (as run_chunk), copied on its stream
+    for (Handle* h : runs) {
+      if (h->copy_pending && cudaEventSynchronize(h->ev_copy) != cudaSuccess) return CYL_ERR_CUDA;
+      if (int r = flush_push_timing(h)) return r;
+      int64_t inj_used = 0;
+      for (int i = 0; i < k; ++i) prepare_step(h, i, inj_used);
+      cudaError_t e = cudaMemcpyAsync(h->d_rec, h->h_rec, sizeof(StepRec) * k, cudaMemcpyHostToDevice, h->st);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h->d_src, h->h_src, sizeof(double) * h->src_per_step * k, cudaMemcpyHostToDevice,
+                            h->st);
+      if (e == cudaSuccess && inj_used > 0)
+        e = cudaMemcpyAsync(h->d_inj, h->h_inj, sizeof(double) * 8 * inj_used, cudaMemcpyHostToDevice, h->st);
+      if (e == cudaSuccess) e = cudaEventRecord(h->ev_copy, h->st);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(b->st, h->ev_copy, 0);
+      if (e != cudaSuccess) return CYL_ERR_CUDA;
+      h->copy_pending = true;
+      h->timing_pending = 0;
+    }
+    // the job table of the chunk: per step, the fields of the J parity after
+    // that step's swap
+    if (b->jobs_pending && cudaEventSynchronize(b->ev_jobs) != cudaSuccess) return CYL_ERR_CUDA;
+    std::vector<int> par0(runs.size());
+    for (size_t r = 0; r < runs.size(); ++r) par0[r] = runs[r]->jpar;
+    for (int i = 0; i < k; ++i)
+      for (int j = 0; j < nj; ++j) {
+        Handle* h = jobs[j].h;
+        const int isp = jobs[j].isp;
+        BatchJob& J = b->h_jobs[(size_t)i * b->cap_jobs + j];
+        J.F = fieldset_f(h, h->jpar ^ ((i + 1) & 1));
+        J.sp = h->sp[isp];
+        J.cnt = h->d_cnt + isp;
+        J.rec = h->d_rec + i;
+        J.rc = h->rc;
+        J.P = h->mp[isp];
+        J.tt = h->d_tiles + isp;
+        J.apply_bcs = 1;
+      }
+    if (cudaMemcpyAsync(b->d_jobs, b->h_jobs, sizeof(BatchJob) * (size_t)k * b->cap_jobs, cudaMemcpyHostToDevice,
+                        b->st) != cudaSuccess ||
+        cudaEventRecord(b->ev_jobs, b->st) != cudaSuccess)
+      return CYL_ERR_CUDA;
+    b->jobs_pending = true;
+    if (k == CHUNK) {
+      const bool same = b->gexec && b->g_runs == runs && b->g_par == par0 && b->g_jobs == nj;
+      if (!same) {
+        if (b->gexec) {
+          cudaGraphExecDestroy(b->gexec);
+          b->gexec = nullptr;
+        }
+        cudaGraph_t graph;
+        if (cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return CYL_ERR_CUDA;
+        enqueue_batch_chunk(b, runs, nj, k, M);
+        if (cudaStreamEndCapture(b->st, &graph) != cudaSuccess) return CYL_ERR_CUDA;
+        const cudaError_t e = cudaGraphInstantiate(&b->gexec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return CYL_ERR_CUDA;
+        b->g_runs = runs;
+        b->g_par = par0;
+        b->g_jobs = nj;
+        // the capture advanced each run's J parity by k (even): unchanged
+      } else {
+        for (Handle* h : runs) h->jpar ^= (k & 1);
+      }
+      if (cudaGraphLaunch(b->gexec, b->st) != cudaSuccess) return CYL_ERR_CUDA;
+    } else {
+      (void)cudaGetLastError();
+      enqueue_batch_chunk(b, runs, nj, k, M);
+      if (cudaGetLastError() != cudaSuccess) return CYL_ERR_CUDA;
+    }
+    // each run's later work (its next copies, reads) comes after the chunk
+    if (cudaEventRecord(b->ev_done, b->st) != cudaSuccess) return CYL_ERR_CUDA;
+    for (Handle* h : runs)
+      if (cudaStreamWaitEvent(h->st, b->ev_done, 0) != cudaSuccess) return CYL_ERR_CUDA;
+    done += k;
+  }
+  if (cudaStreamSynchronize(b->st) != cudaSuccess) return CYL_ERR_CUDA;
+  for (Handle* h : runs)
+    if (int r = sync_and_check(h)) return r;
+  return CYL_OK;
+}
+
+int cyl_batch_destroy(cyl_batch b) {
+  if (!b) return CYL_ERR_BAD_ARG;
+  if (b->st) cudaStreamSynchronize(b->st);
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  cudaFreeHost(b->h_jobs);
+  cudaFree(b->d_jobs);
+  cudaFree(b->d_work);
+  cudaFree(b->d_nwork);
+  for (cudaEvent_t ev : {b->ev_sched, b->ev_push, b->ev_done, b->ev_jobs})
+    if (ev) cudaEventDestroy(ev);
+  for (cudaEvent_t ev : b->ev_run)
+    if (ev) cudaEventDestroy(ev);
+  if (b->st) cudaStreamDestroy(b->st);
+  delete b;
   return CYL_OK;
 }
 

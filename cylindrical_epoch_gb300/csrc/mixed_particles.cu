@@ -423,6 +423,74 @@ void mixed_sort(cudaStream_t s, const SpeciesPtrs& sp, SpeciesCounters* cnt, Sor
   k_tile_commit<<<1, 1, 0, s>>>(cnt, tt);
 }
 
+// ------------------------------------------------- batched push
+
+// The work table of a batched push: every non-empty tile of every job as a
+// (job, tile) item, in decreasing order of particle count (the bucketing of
+// k_tile_order, over all jobs).  One CTA.
+__global__ void __launch_bounds__(ORDER_BUCKETS) k_batch_schedule(const BatchJob* jobs, int njobs, int2* work,
+                                                                   int* nwork) {
+  __shared__ int hist[ORDER_BUCKETS];
+  __shared__ int warp_tot[ORDER_BUCKETS / 32];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  hist[tid] = 0;
+  __syncthreads();
+  auto bucket = [&](const int64_t* start, int t) {
+    const int64_t c = (start[t + 1] - start[t]) >> 3;
+    return ORDER_BUCKETS - 1 - (int)(c < ORDER_BUCKETS - 1 ? c : ORDER_BUCKETS - 1);
+  };
+  for (int j = 0; j < njobs; ++j) {
+    const TileTable* tt = jobs[j].tt;
+    const int nt = tt->ntiles;
+    const int64_t* start = tt->start;
+    for (int t = tid; t < nt; t += ORDER_BUCKETS)
+      if (start[t + 1] > start[t]) atomicAdd(&hist[bucket(start, t)], 1);
+  }
+  __syncthreads();
+  const int v = hist[tid];
+  int x = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, d);
+    if (lane >= d) x += y;
+  }
+  if (lane == 31) warp_tot[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    int s = warp_tot[lane];
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, s, d);
+      if (lane >= d) s += y;
+    }
+    warp_tot[lane] = s;
+  }
+  __syncthreads();
+  hist[tid] = x - v + (w > 0 ? warp_tot[w - 1] : 0);
+  if (tid == ORDER_BUCKETS - 1) *nwork = x + (w > 0 ? warp_tot[w - 1] : 0);
+  __syncthreads();
+  for (int j = 0; j < njobs; ++j) {
+    const TileTable* tt = jobs[j].tt;
+    const int nt = tt->ntiles;
+    const int64_t* start = tt->start;
+    for (int t = tid; t < nt; t += ORDER_BUCKETS)
+      if (start[t + 1] > start[t]) work[atomicAdd(&hist[bucket(start, t)], 1)] = make_int2(j, t);
+  }
+}
+
+// Clear the deferred-list counters of a batch's jobs (one step's table).
+__global__ void k_batch_reset(const BatchJob* jobs, int njobs) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < njobs) *jobs[j].P.fb_count = 0;
+}
+
+void batch_schedule(cudaStream_t s, const BatchJob* jobs, int njobs, int2* work, int* nwork) {
+  k_batch_schedule<<<1, ORDER_BUCKETS, 0, s>>>(jobs, njobs, work, nwork);
+}
+void batch_reset(cudaStream_t s, const BatchJob* jobs, int njobs) {
+  k_batch_reset<<<(njobs + 127) / 128, 128, 0, s>>>(jobs, njobs);
+}
+
 // ------------------------------------------------- push tile shapes
 
 PushMixedFns push_mixed_fns_16x8();

@@ -724,34 +724,35 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
 // a second).
 constexpr int TMA_WAIT_POLLS = 1 << 24;
 
+// Shared memory of one push CTA: 128-byte aligned TMA planes, mode-0
+// planes, accumulators.
 template <int M>
-__global__ void __launch_bounds__(PUSH_THREADS, PUSH_MIN_BLOCKS) k_push_tiles(
-    FieldSetF F, SpeciesPtrs sp, SpeciesCounters* cnt, const StepRec* rec, RunConst rc, MixedParams P, TileTable* tt,
-    int apply_bcs, const __grid_constant__ TmaSet tma, int use_tma) {
-  extern __shared__ float4 smem4[];
-  __shared__ uint64_t tma_bar;
-  __shared__ int tma_failed;
-  // dynamic shared memory: 128-byte aligned TMA planes, mode-0 planes, accumulators
-  char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(smem4) + 127) & ~(uintptr_t)127);
-  float2* tm = reinterpret_cast<float2*>(base);                             // 6 (M-1) TPLANE float2
-  float2* sf = tm + 6 * (M - 1) * TPLANE;                                   // PLANES_M0 RCELLS float2
-  int* sj = reinterpret_cast<int*>(sf + PLANES_M0 * RCELLS);                // 3 M 4 RCELLS int32
-  if (threadIdx.x == 0) {
-    tma_failed = 0;
-    if (use_tma) mbar_init(&tma_bar);
+struct TileSmem {
+  float2* tm;  // 6 (M-1) TPLANE float2
+  float2* sf;  // PLANES_M0 RCELLS float2
+  int* sj;     // 3 M 4 RCELLS int32
+  __device__ __forceinline__ explicit TileSmem(float4* smem4) {
+    char* base = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(smem4) + 127) & ~(uintptr_t)127);
+    tm = reinterpret_cast<float2*>(base);
+    sf = tm + 6 * (M - 1) * TPLANE;
+    sj = reinterpret_cast<int*>(sf + PLANES_M0 * RCELLS);
   }
-  __syncthreads();
-  unsigned tma_phase = 0;
-  const int nsh = rec->nshift_total;
-  const float qw_max = fabsf(P.q_fac) * __uint_as_float(cnt->wmax_bits);
-  set_bounds(P, rec, rc);
-  const int ntiles = tt->ntiles;
+};
+
+// One tile of one run: stage its fields, push and deposit its particles, and
+// flush its current accumulators.  Every thread of the CTA calls it with the
+// same tile, so all meet the same barriers.  Returns false when the TMA
+// staging timed out (the CTA must leave).
+template <int M>
+__device__ __forceinline__ bool process_tile(const FieldSetF& F, const SpeciesPtrs& sp, SpeciesCounters* cnt,
+                                             const RunConst& rc, const MixedParams& P, const TileTable* tt, int t,
+                                             int nsh, float qw_max, int apply_bcs, const TmaSet* tma, int use_tma,
+                                             const TileSmem<M>& sm, uint64_t* tma_bar, int* tma_failed,
+                                             unsigned& tma_phase) {
+  float2* const tm = sm.tm;
+  float2* const sf = sm.sf;
+  int* const sj = sm.sj;
   const int ntx = tt->ntx;
-  // static round-robin over the tiles in decreasing order of particle count
-  // (longest first); every thread evaluates the same tile conditions, so all
-  // threads meet the same barriers
-  for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x) {
-    const int t = tt->order[ti];
     const int64_t p0 = tt->start[t], p1 = tt->start[t + 1];
     Tile tile;
     tile.sf = sf;
@@ -762,20 +763,20 @@ __global__ void __launch_bounds__(PUSH_THREADS, PUSH_MIN_BLOCKS) k_push_tiles(
     tile.xs = tile.x0 - (((tile.x0 % 2) + 2) % 2);  // rounded down to even
     const bool inside = tile.x0 >= 1 - NG && tile.x0 + RW - 1 <= rc.nx + NG && tile.y0 >= 1 - NG &&
                         tile.y0 + RH - 1 <= rc.ny + NG;
-    if (p1 <= p0) continue;
+    if (p1 <= p0) return true;
     if (!inside) {
       // tile partly outside the ghosted grid: every particle takes the global path
       for (int64_t i = p0 + threadIdx.x; i < p1; i += PUSH_THREADS) P.fb_list[atomicAdd(P.fb_count, 1)] = (int)i;
-      continue;
+      return true;
     }
     // stage E and B (FP32): modes m >= 1 by TMA boxes (issued first, they
     // arrive while mode 0 is staged by plain loads as real pairs, see Gather)
     if (M > 1 && use_tma && threadIdx.x == 0) {
-      mbar_expect_tx(&tma_bar, (unsigned)(6 * (M - 1) * TW * RH * 8));
+      mbar_expect_tx(tma_bar, (unsigned)(6 * (M - 1) * TW * RH * 8));
       for (int q = 0; q < 6; ++q)
         for (int m = 1; m < M; ++m)
-          tma_load_3d(tm + (q * (M - 1) + m - 1) * TPLANE, &tma.map[q], tile.xs + NG - 1, tile.y0 + NG - 1, m,
-                      &tma_bar);
+          tma_load_3d(tm + (q * (M - 1) + m - 1) * TPLANE, &tma->map[q], tile.xs + NG - 1, tile.y0 + NG - 1, m,
+                      tma_bar);
     }
     {
       using G = Gather<M, false>;
@@ -807,17 +808,17 @@ __global__ void __launch_bounds__(PUSH_THREADS, PUSH_MIN_BLOCKS) k_push_tiles(
       // copies visible to the waiting thread); a wait that runs out flags the
       // run, waits once more for copies in flight, and the CTA leaves at the
       // next barrier
-      if (!mbar_wait_bounded(&tma_bar, tma_phase, TMA_WAIT_POLLS)) {
+      if (!mbar_wait_bounded(tma_bar, tma_phase, TMA_WAIT_POLLS)) {
         atomicOr(P.err, ERR_TMA_TIMEOUT);
-        mbar_wait_bounded(&tma_bar, tma_phase, TMA_WAIT_POLLS);
-        tma_failed = 1;
+        mbar_wait_bounded(tma_bar, tma_phase, TMA_WAIT_POLLS);
+        *tma_failed = 1;
       }
       tma_phase ^= 1u;
     }
     for (int e = threadIdx.x; e < 3 * M * 4 * RCELLS; e += PUSH_THREADS) sj[e] = 0;
     tile_scales(tile, p1 - p0, qw_max, P.idt, P.c);
     __syncthreads();
-    if (tma_failed) return;  // uniform: read by every thread after the barrier
+    if (*tma_failed) return false;  // uniform: read by every thread after the barrier
     for (int64_t i = p0 + threadIdx.x; i < p1; i += PUSH_THREADS) {
       if (!push_one<M, true>(i, sp, cnt, F, P, rc, tile, nsh, apply_bcs))
         P.fb_list[atomicAdd(P.fb_count, 1)] = (int)i;
@@ -843,6 +844,78 @@ __global__ void __launch_bounds__(PUSH_THREADS, PUSH_MIN_BLOCKS) k_push_tiles(
       gadd_f(dst, vr * f, vi * f);
     }
     __syncthreads();
+  return true;
+}
+
+template <int M>
+__global__ void __launch_bounds__(PUSH_THREADS, PUSH_MIN_BLOCKS) k_push_tiles(
+    FieldSetF F, SpeciesPtrs sp, SpeciesCounters* cnt, const StepRec* rec, RunConst rc, MixedParams P, TileTable* tt,
+    int apply_bcs, const __grid_constant__ TmaSet tma, int use_tma) {
+  extern __shared__ float4 smem4[];
+  __shared__ uint64_t tma_bar;
+  __shared__ int tma_failed;
+  const TileSmem<M> sm(smem4);
+  if (threadIdx.x == 0) {
+    tma_failed = 0;
+    if (use_tma) mbar_init(&tma_bar);
+  }
+  __syncthreads();
+  unsigned tma_phase = 0;
+  const int nsh = rec->nshift_total;
+  const float qw_max = fabsf(P.q_fac) * __uint_as_float(cnt->wmax_bits);
+  set_bounds(P, rec, rc);
+  const int ntiles = tt->ntiles;
+  // static round-robin over the tiles in decreasing order of particle count
+  // (longest first)
+  for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x) {
+    if (!process_tile<M>(F, sp, cnt, rc, P, tt, tt->order[ti], nsh, qw_max, apply_bcs, &tma, use_tma, sm, &tma_bar,
+                         &tma_failed, tma_phase))
+      return;
+  }
+}
+
+// The push of several runs (a batch) in one launch: the runs' tiles form one
+// table of (run, tile) items in decreasing order of particle count, dealt to
+// the CTAs round-robin.  Each item reads its run's parameters from the job
+// table (one entry per run and step of the chunk).  Fields are staged by
+// plain loads.
+template <int M>
+__global__ void __launch_bounds__(PUSH_THREADS, PUSH_MIN_BLOCKS) k_push_tiles_batch(const BatchJob* jobs,
+                                                                                   const int2* work,
+                                                                                   const int* nwork) {
+  extern __shared__ float4 smem4[];
+  __shared__ int tma_failed;
+  if (threadIdx.x == 0) tma_failed = 0;
+  __syncthreads();
+  const TileSmem<M> sm(smem4);
+  unsigned tma_phase = 0;
+  const int n = *nwork;
+  for (int w = blockIdx.x; w < n; w += gridDim.x) {
+    const int2 jt = work[w];
+    const BatchJob& J = jobs[jt.x];
+    MixedParams P = J.P;
+    set_bounds(P, J.rec, J.rc);
+    const float qw_max = fabsf(P.q_fac) * __uint_as_float(J.cnt->wmax_bits);
+    process_tile<M>(J.F, J.sp, J.cnt, J.rc, P, J.tt, jt.y, J.rec->nshift_total, qw_max, J.apply_bcs, nullptr, 0, sm,
+                    nullptr, &tma_failed, tma_phase);
+  }
+}
+
+// The deferred particles of every run of a batch (blockIdx.y = run).
+template <int M>
+__global__ void __launch_bounds__(PUSH_THREADS) k_push_global_batch(const BatchJob* jobs) {
+  const BatchJob& J = jobs[blockIdx.y];
+  MixedParams P = J.P;
+  set_bounds(P, J.rec, J.rc);
+  const int nsh = J.rec->nshift_total;
+  const int64_t nlist = *P.fb_count;
+  const int64_t n_sorted = J.tt->n_sorted, n_used = J.cnt->n_used;
+  const int64_t ntail = n_used > n_sorted ? n_used - n_sorted : 0;
+  Tile none{nullptr, nullptr, nullptr, 0, 0, 0, 0.f, 0.f};
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nlist + ntail;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = (t < nlist) ? (int64_t)P.fb_list[t] : n_sorted + (t - nlist);
+    push_one<M, false>(i, J.sp, J.cnt, J.F, P, J.rc, none, nsh, J.apply_bcs);
   }
 }
 
@@ -914,6 +987,10 @@ int push_mixed_blocks_per_sm(int M) {
   case MM:                                                                                          \
     cudaFuncSetAttribute(k_push_tiles<MM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
     cudaFuncSetAttribute(k_push_tiles<MM>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);    \
+    cudaFuncSetAttribute(k_push_tiles_batch<MM>, cudaFuncAttributeMaxDynamicSharedMemorySize,       \
+                         (int)smem);                                                                 \
+    cudaFuncSetAttribute(k_push_tiles_batch<MM>, cudaFuncAttributePreferredSharedMemoryCarveout,    \
+                         100);                                                                       \
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_push_tiles<MM>, PUSH_THREADS, smem);       \
     break;
     OCC(1) OCC(2) OCC(3) OCC(4)
@@ -945,10 +1022,29 @@ void launch_push_mixed(cudaStream_t s, const FieldSetF& F, const SpeciesPtrs& sp
   }
 }
 
+// The push of a batch of runs with the same number of modes: the tile
+// kernel over the (run, tile) table, then the deferred particles of each run.
+void launch_push_mixed_batch(cudaStream_t s, int M, const BatchJob* jobs, int njobs, const int2* work,
+                             const int* nwork, int nblocks_tiles, int nblocks_global) {
+  const size_t smem = push_mixed_smem(M);
+  switch (M) {
+#define CASE(MM)                                                                                      \
+  case MM:                                                                                            \
+    k_push_tiles_batch<MM><<<nblocks_tiles, PUSH_THREADS, smem, s>>>(jobs, work, nwork);                \
+    k_push_global_batch<MM><<<dim3(nblocks_global, njobs), PUSH_THREADS, 0, s>>>(jobs);                 \
+    break;
+    CASE(1) CASE(2) CASE(3) CASE(4)
+#undef CASE
+    default:
+      break;
+  }
+}
+
 }  // namespace CYL_TILE_NS
 
 PushMixedFns CYL_TILE_FNS() {
-  return {&CYL_TILE_NS::push_mixed_smem, &CYL_TILE_NS::push_mixed_blocks_per_sm, &CYL_TILE_NS::launch_push_mixed};
+  return {&CYL_TILE_NS::push_mixed_smem, &CYL_TILE_NS::push_mixed_blocks_per_sm, &CYL_TILE_NS::launch_push_mixed,
+          &CYL_TILE_NS::launch_push_mixed_batch};
 }
 
 }  // namespace cyl

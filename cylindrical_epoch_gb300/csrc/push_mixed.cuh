@@ -49,6 +49,20 @@ struct MixedParams {
 
 MixedParams mixed_params(const SpeciesPtrs& sp, const RunConst& rc);
 
+// One run of a batched push (one entry per run and step of a chunk): the
+// run's fields (J of the step's parity), particles, counters, step record,
+// constants, push parameters and tile table.
+struct BatchJob {
+  FieldSetF F;
+  SpeciesPtrs sp;
+  SpeciesCounters* cnt;
+  const StepRec* rec;
+  RunConst rc;
+  MixedParams P;
+  TileTable* tt;
+  int apply_bcs;
+};
+
 // The push of one tile shape (push_mixed.cu built for that shape):
 // shared memory per CTA, resident CTAs per SM (also sets the kernel's
 // shared-memory attributes; call before the first launch), and the launch
@@ -59,8 +73,16 @@ struct PushMixedFns {
   void (*launch)(cudaStream_t s, const FieldSetF& F, const SpeciesPtrs& sp, SpeciesCounters* cnt,
                  const StepRec* rec, const RunConst& rc, int apply_bcs, int nblocks_tiles, int nblocks_global,
                  const MixedParams& P, TileTable* tt);
+  // the batched push: jobs[0, njobs) of one step, work = (job, tile) items
+  void (*launch_batch)(cudaStream_t s, int M, const BatchJob* jobs, int njobs, const int2* work, const int* nwork,
+                       int nblocks_tiles, int nblocks_global);
 };
 const PushMixedFns& push_mixed_fns(int shape);
+
+// mixed_particles.cu: the (job, tile) work table of a batched push, and the
+// per-step reset of the jobs' deferred-list counters.
+void batch_schedule(cudaStream_t s, const BatchJob* jobs, int njobs, int2* work, int* nwork);
+void batch_reset(cudaStream_t s, const BatchJob* jobs, int njobs);
 
 // mixed_particles.cu
 void mixed_from_double(cudaStream_t s, const SpeciesPtrs& sp, const double* stage, int64_t n, int64_t cap,

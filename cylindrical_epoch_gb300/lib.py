@@ -50,6 +50,9 @@ SIGNATURES = {
     "cyl_kernel_timing": (C.c_int, [H, PD, PI64]),
     "cyl_get_stream": (C.c_int, [H, P(C.c_void_p)]),
     "cyl_estimate_device_bytes": (C.c_int, [P(abi.GridDesc), P(abi.SpeciesDesc), I32, PI64]),
+    "cyl_batch_create": (C.c_int, [I32, P(H)]),
+    "cyl_batch_step": (C.c_int, [H, P(H), I32, I32]),
+    "cyl_batch_destroy": (C.c_int, [H]),
     "cyl_server_create": (C.c_int, [I64, I32, P(H)]),
     "cyl_server_submit": (C.c_int, [H, P(abi.JobDesc), PI64]),
     "cyl_server_poll": (C.c_int, [H, I64, P(abi.JobResult)]),

@@ -231,3 +231,36 @@ class Run:
         abi.check("cyl_cell_indices", self.lib.cyl_cell_indices(self.h, isp, _p(cx, PI32), _p(cy, PI32),
                                                                 C.byref(n)))
         return cx[:n.value], cy[:n.value]
+
+
+class Batch:
+    """Mixed-form runs stepped together (cyl_batch_*): one push launch per
+    step over all runs' tiles; the other stages per run, in one graph per
+    chunk of 16 steps."""
+
+    def __init__(self, max_runs=16):
+        self.lib = load()
+        self.b = C.c_void_p()
+        abi.check("cyl_batch_create", self.lib.cyl_batch_create(int(max_runs), C.byref(self.b)))
+
+    def step(self, runs, nsteps):
+        hs = (C.c_void_p * len(runs))(*[r.h for r in runs])
+        abi.check("cyl_batch_step", self.lib.cyl_batch_step(self.b, hs, len(runs), int(nsteps)))
+
+    def close(self):
+        if getattr(self, "b", None):
+            self.lib.cyl_batch_destroy(self.b)
+            self.b = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+

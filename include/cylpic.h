@@ -320,6 +320,23 @@ int cyl_get_stream(cyl_handle h, void** stream_out);
 int cyl_estimate_device_bytes(const cyl_grid_desc* grid, const cyl_species_desc* species,
                               int32_t nspecies, int64_t* out);
 
+/* ---- batches: several mixed-form runs stepped together ------------------
+ * No counterpart in the reference (one deck per MPI job there).  A batch
+ * steps n handles (mixed form, the same number of modes, any grids and
+ * particle counts) through the same steps in lockstep: the push of all of
+ * them is one persistent kernel per step over a shared table of (run,
+ * species, tile) items in decreasing order of particle count; the field,
+ * boundary and window stages stay per run, on each run's own stream, forked
+ * and joined around the push, and a chunk of 16 steps is one CUDA graph
+ * (captured again when the membership changes).  Membership may change from
+ * one call to the next (runs join and leave between calls).  The runs use
+ * tile shape 0 while batched.  Each run's results are those of stepping it
+ * alone, up to the order of its FP64 current additions. */
+typedef struct cyl_batch_s* cyl_batch;
+int cyl_batch_create(int32_t max_runs, cyl_batch* out);
+int cyl_batch_step(cyl_batch b, const cyl_handle* handles, int32_t n, int32_t nsteps);
+int cyl_batch_destroy(cyl_batch b);
+
 /* ---- serving: a request loop for parameter scans ----------------------
  * No counterpart in the reference (one deck per MPI job there).  A server
  * owns a queue of runs (jobs) and a pool of worker threads on one GPU.  Jobs
