@@ -213,10 +213,22 @@ def run_serve(args):
     with serve.Server(0, args.workers) as srv:
         ids = [srv.submit(deck, steps) for deck, steps in decks]
         res_sat = [srv.wait(i, 3600.0) for i in ids]
+    # the same stream and the same burst through the continuous-batching loop
+    with serve.Server(0, args.workers, batched=True, max_batch=args.max_batch) as srv:
+        ids = []
+        for (deck, steps), gap in zip(decks, gaps):
+            ids.append(srv.submit(deck, steps))
+            time.sleep(float(gap))
+        res_b = [srv.wait(i, 3600.0) for i in ids]
+    with serve.Server(0, args.workers, batched=True, max_batch=args.max_batch) as srv:
+        ids = [srv.submit(deck, steps) for deck, steps in decks]
+        res_bsat = [srv.wait(i, 3600.0) for i in ids]
     clk = clocks.stop()
     bad = [r.error for r in res if r.status != abi.JOB_DONE]
     st = serve.latency_stats(res)
     st_sat = serve.latency_stats(res_sat)
+    st_b = serve.latency_stats(res_b)
+    st_bsat = serve.latency_stats(res_bsat)
     # plain FP64 form, one deck at a time, on a sample of the decks (bounded steps)
     fp64 = []
     for deck, steps in decks[:args.fp64_sample]:
@@ -248,7 +260,14 @@ def run_serve(args):
         "saturated": {"value": st_sat["aggregate"], "unit": "particle-steps/s",
                       "makespan_s": st_sat["makespan_s"], "p50_s": st_sat["p50_s"], "p99_s": st_sat["p99_s"],
                       "note": "the same decks submitted at once"},
-        "failed_jobs": len(bad) + sum(1 for r in res_sat if r.status != abi.JOB_DONE),
+        "batched": {"value": st_b["aggregate"], "unit": "particle-steps/s",
+                    "latency": {"p50_s": st_b["p50_s"], "p99_s": st_b["p99_s"], "mean_s": st_b["mean_s"],
+                                "makespan_s": st_b["makespan_s"]},
+                    "saturated": {"value": st_bsat["aggregate"], "makespan_s": st_bsat["makespan_s"],
+                                  "p50_s": st_bsat["p50_s"], "p99_s": st_bsat["p99_s"]},
+                    "note": "continuous batching: mixed-form jobs with the same modes step together, "
+                            f"at most {args.max_batch} per batch, {args.workers} loader threads"},
+        "failed_jobs": len(bad) + sum(1 for r in res_sat + res_b + res_bsat if r.status != abi.JOB_DONE),
         "failed": [{"job": k, "error": int(r.error), "nx": decks[k][0].nx, "ny": decks[k][0].ny,
                     "n_mode": decks[k][0].n_mode, "ppc": decks[k][0].species[0].npart_per_cell,
                     "steps_done": int(r.steps_done)}
@@ -290,6 +309,7 @@ def main():
     ap.add_argument("--jobs", type=int, default=64)
     ap.add_argument("--arrival", type=float, default=0.5, help="mean Poisson arrival gap (s)")
     ap.add_argument("--workers", type=int, default=4)
+    ap.add_argument("--max-batch", type=int, default=16)
     ap.add_argument("--fp64-sample", type=int, default=3)
     ap.add_argument("--fp64-steps-max", type=int, default=100)
     args = ap.parse_args()

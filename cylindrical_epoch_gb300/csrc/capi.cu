@@ -9,6 +9,7 @@
 // HBM.  Steps are enqueued in chunks; a chunk of CHUNK steps can be captured
 // once into a CUDA graph and replayed.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -42,6 +43,7 @@ struct HostLaser {
 
 
 struct Handle {
+  uint64_t serial = 0;  // unique per handle in the process (never reused, unlike the address)
   int device = 0;
   cudaStream_t st = nullptr;
   cudaError_t last_cuda_error = cudaSuccess;
@@ -680,7 +682,7 @@ struct cyl_batch_s {
   int64_t work_cap = 0;
   bool jobs_pending = false;
   cudaGraphExec_t gexec = nullptr;
-  std::vector<Handle*> g_runs;  // membership and parities of the captured graph
+  std::vector<uint64_t> g_runs;  // membership (handle serials) and parities of the captured graph
   std::vector<int> g_par;
   int g_jobs = 0;
 };
@@ -778,8 +780,10 @@ int cyl_create(const cyl_grid_desc* gd, const cyl_species_desc* spd, int32_t nsp
   }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return CYL_ERR_NO_DEVICE;
+  static std::atomic<uint64_t> next_serial{1};
   cyl_handle_s* hs = new cyl_handle_s();
   Handle* h = &hs->h;
+  h->serial = next_serial.fetch_add(1);
   cudaGetDevice(&h->device);
   h->gd = *gd;
   h->prec = gd->precision;
@@ -1696,7 +1700,9 @@ int cyl_batch_step(cyl_batch b, const cyl_handle* hs, int32_t n, int32_t nsteps)
       return CYL_ERR_CUDA;
     b->jobs_pending = true;
     if (k == CHUNK) {
-      const bool same = b->gexec && b->g_runs == runs && b->g_par == par0 && b->g_jobs == nj;
+      std::vector<uint64_t> serials(runs.size());
+      for (size_t r = 0; r < runs.size(); ++r) serials[r] = runs[r]->serial;
+      const bool same = b->gexec && b->g_runs == serials && b->g_par == par0 && b->g_jobs == nj;
       if (!same) {
         if (b->gexec) {
           cudaGraphExecDestroy(b->gexec);
@@ -1709,7 +1715,7 @@ int cyl_batch_step(cyl_batch b, const cyl_handle* hs, int32_t n, int32_t nsteps)
         const cudaError_t e = cudaGraphInstantiate(&b->gexec, graph, 0);
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) return CYL_ERR_CUDA;
-        b->g_runs = runs;
+        b->g_runs = serials;
         b->g_par = par0;
         b->g_jobs = nj;
         // the capture advanced each run's J parity by k (even): unchanged

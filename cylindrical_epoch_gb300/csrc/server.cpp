@@ -68,13 +68,28 @@ struct cyl_server_s {
   std::deque<Job*> queue;
   std::map<int64_t, std::unique_ptr<Job>> jobs;
   std::vector<std::thread> workers;
+  // batched mode: the workers only open jobs; one stepper thread advances
+  // every open job, the mixed-form ones in batches (cyl_batch_step)
+  bool batched = false;
+  int max_batch = 16;
+  int loading = 0;  // jobs being opened by workers
+  struct Active {
+    Job* job;
+    cyl_handle h;
+    int64_t done, n0;
+  };
+  std::vector<Active> active;
+  std::condition_variable cv_active;
+  std::thread stepper;
 };
 
 namespace {
 
-// Load, create, initialise, step, read back, destroy.  Returns CYL_OK or the
-// status of the failing call; fills res.diag, res.state, res.steps_done.
-int run_job(cyl_server_s* srv, Job* job) {
+// Load the job's species on the host (the reference's loader and KISS
+// stream), create its handle and initialise it; a mixed-form run then gets
+// its push tile shape (timed once per deck shape, see g_tile_choice) unless
+// it is to be batched.  Returns CYL_OK or the failing call's status.
+int open_job(cyl_server_s* srv, Job* job, cyl_handle* out, int64_t* n0_out) {
   if (cudaSetDevice(srv->device) != cudaSuccess) return CYL_ERR_CUDA;
   const cyl_job_desc& d = job->desc;
   cyl_rng_state rng;
@@ -120,7 +135,7 @@ int run_job(cyl_server_s* srv, Job* job) {
   }
   hp.clear();
   if (r == CYL_OK) r = cyl_initialise(h);
-  if (r == CYL_OK && d.grid.precision == CYL_PREC_MIXED) {
+  if (r == CYL_OK && d.grid.precision == CYL_PREC_MIXED && !srv->batched) {
     const std::vector<int64_t> key = {srv->device, d.grid.nx, d.grid.ny, d.grid.n_mode,
                                       d.nspecies > 0 ? (int64_t)(d.species[0].npart_per_cell * 1000.0) : 0};
     int shape = -1;
@@ -139,18 +154,18 @@ int run_job(cyl_server_s* srv, Job* job) {
       }
     }
   }
-  {
-    std::lock_guard<std::mutex> lock(srv->mu);
-    job->res.t_start = now_since(srv->t0);
+  if (r != CYL_OK) {
+    cyl_destroy(h);
+    return r;
   }
-  int64_t done = 0;
-  while (r == CYL_OK && done < d.nsteps) {
-    const int k = (int)std::min<int64_t>(CHUNK_STEPS, d.nsteps - done);
-    r = cyl_step_graph(h, k);
-    if (r == CYL_OK) done += k;
-    std::lock_guard<std::mutex> lock(srv->mu);
-    job->res.steps_done = done;
-  }
+  *out = h;
+  *n0_out = n0;
+  return CYL_OK;
+}
+
+// Read the results of a finished (or failed) run and destroy its handle.
+int close_job(Job* job, cyl_handle h, int64_t done, int64_t n0, int r) {
+  const cyl_job_desc& d = job->desc;
   if (r == CYL_OK) r = cyl_diagnostics(h, &job->res.diag);
   if (r == CYL_OK) r = cyl_get_run_state(h, &job->res.state);
   if (r == CYL_OK) {
@@ -161,6 +176,131 @@ int run_job(cyl_server_s* srv, Job* job) {
   }
   cyl_destroy(h);
   return r;
+}
+
+// Open, step (graphs of 16 steps on the run's own stream), close.
+int run_job(cyl_server_s* srv, Job* job) {
+  cyl_handle h = nullptr;
+  int64_t n0 = 0;
+  int r = open_job(srv, job, &h, &n0);
+  if (r != CYL_OK) return r;
+  {
+    std::lock_guard<std::mutex> lock(srv->mu);
+    job->res.t_start = now_since(srv->t0);
+  }
+  int64_t done = 0;
+  while (r == CYL_OK && done < job->desc.nsteps) {
+    const int k = (int)std::min<int64_t>(CHUNK_STEPS, job->desc.nsteps - done);
+    r = cyl_step_graph(h, k);
+    if (r == CYL_OK) done += k;
+    std::lock_guard<std::mutex> lock(srv->mu);
+    job->res.steps_done = done;
+  }
+  return close_job(job, h, done, n0, r);
+}
+
+// Record a finished job and return its memory to the budget.
+void retire(cyl_server_s* srv, Job* job, int r) {
+  {
+    std::lock_guard<std::mutex> lock(srv->mu);
+    srv->in_use -= job->res.device_bytes;
+    srv->running -= 1;
+    job->res.error = r;
+    job->res.t_end = now_since(srv->t0);
+    job->res.status = (r == CYL_OK) ? CYL_JOB_DONE : CYL_JOB_FAILED;
+  }
+  srv->cv_work.notify_all();
+  srv->cv_done.notify_all();
+}
+
+// Batched mode: advance every open job by up to CHUNK_STEPS steps per pass,
+// mixed-form runs with the same number of modes together (cyl_batch_step,
+// at most max_batch per call), FP64-form runs one at a time; retire the
+// finished ones.  A pass steps each group by the smallest number of steps
+// any member has left, so members finish at chunk boundaries and new jobs
+// join at the next pass.
+void stepper_main(cyl_server_s* srv) {
+  cudaSetDevice(srv->device);
+  std::map<int, cyl_batch> batches;
+  for (;;) {
+    std::vector<cyl_server_s::Active> act;
+    {
+      std::unique_lock<std::mutex> lock(srv->mu);
+      srv->cv_active.wait(lock, [&] {
+        return !srv->active.empty() || (srv->stop && srv->queue.empty() && srv->loading == 0);
+      });
+      if (srv->active.empty()) break;
+      act = srv->active;
+    }
+    std::map<int, std::vector<size_t>> groups;  // mixed runs by modes
+    std::vector<size_t> singles;
+    for (size_t a = 0; a < act.size(); ++a) {
+      const cyl_job_desc& d = act[a].job->desc;
+      if (d.grid.precision == CYL_PREC_MIXED) groups[d.grid.n_mode].push_back(a);
+      else singles.push_back(a);
+    }
+    std::vector<int> err(act.size(), CYL_OK);
+    std::vector<int64_t> stepped(act.size(), 0);
+    for (auto& g : groups) {
+      const int M = g.first;
+      if (!batches.count(M)) {
+        cyl_batch b = nullptr;
+        const int rc = cyl_batch_create(srv->max_batch, &b);
+        if (rc != CYL_OK) {
+          for (size_t a : g.second) err[a] = rc;
+          continue;
+        }
+        batches[M] = b;
+      }
+      for (size_t s0 = 0; s0 < g.second.size(); s0 += (size_t)srv->max_batch) {
+        const size_t s1 = std::min(g.second.size(), s0 + (size_t)srv->max_batch);
+        int64_t k = CHUNK_STEPS;
+        std::vector<cyl_handle> hs;
+        for (size_t q = s0; q < s1; ++q) {
+          const size_t a = g.second[q];
+          k = std::min<int64_t>(k, act[a].job->desc.nsteps - act[a].done);
+          hs.push_back(act[a].h);
+        }
+        const int rc = cyl_batch_step(batches[M], hs.data(), (int32_t)hs.size(), (int32_t)k);
+        for (size_t q = s0; q < s1; ++q) {
+          const size_t a = g.second[q];
+          err[a] = rc;
+          stepped[a] = rc == CYL_OK ? k : 0;
+        }
+      }
+    }
+    for (size_t a : singles) {
+      const int64_t k = std::min<int64_t>(CHUNK_STEPS, act[a].job->desc.nsteps - act[a].done);
+      err[a] = cyl_step_graph(act[a].h, (int32_t)k);
+      stepped[a] = err[a] == CYL_OK ? k : 0;
+    }
+    // bookkeeping; finished or failed jobs leave the active set
+    std::vector<cyl_server_s::Active> leaving;
+    std::vector<int> leaving_err;
+    {
+      std::lock_guard<std::mutex> lock(srv->mu);
+      for (size_t a = 0; a < act.size(); ++a) {
+        for (auto& x : srv->active)
+          if (x.job == act[a].job) {
+            x.done += stepped[a];
+            x.job->res.steps_done = x.done;
+            if (err[a] != CYL_OK || x.done >= x.job->desc.nsteps) {
+              leaving.push_back(x);
+              leaving_err.push_back(err[a]);
+            }
+          }
+      }
+      for (auto& l : leaving)
+        srv->active.erase(std::remove_if(srv->active.begin(), srv->active.end(),
+                                         [&](const cyl_server_s::Active& x) { return x.job == l.job; }),
+                          srv->active.end());
+    }
+    for (size_t q = 0; q < leaving.size(); ++q) {
+      const int r = close_job(leaving[q].job, leaving[q].h, leaving[q].done, leaving[q].n0, leaving_err[q]);
+      retire(srv, leaving[q].job, r);
+    }
+  }
+  for (auto& b : batches) cyl_batch_destroy(b.second);
 }
 
 void worker_main(cyl_server_s* srv) {
@@ -180,18 +320,25 @@ void worker_main(cyl_server_s* srv) {
       srv->in_use += job->res.device_bytes;
       srv->running += 1;
       job->res.status = CYL_JOB_RUNNING;
+      if (srv->batched) srv->loading += 1;  // with the pop, so the stepper never misses it
     }
-    const int r = run_job(srv, job);
+    if (!srv->batched) {
+      retire(srv, job, run_job(srv, job));
+      continue;
+    }
+    cyl_handle h = nullptr;
+    int64_t n0 = 0;
+    const int r = open_job(srv, job, &h, &n0);
     {
       std::lock_guard<std::mutex> lock(srv->mu);
-      srv->in_use -= job->res.device_bytes;
-      srv->running -= 1;
-      job->res.error = r;
-      job->res.t_end = now_since(srv->t0);
-      job->res.status = (r == CYL_OK) ? CYL_JOB_DONE : CYL_JOB_FAILED;
+      srv->loading -= 1;
+      if (r == CYL_OK) {
+        job->res.t_start = now_since(srv->t0);
+        srv->active.push_back({job, h, 0, n0});
+      }
     }
-    srv->cv_work.notify_all();
-    srv->cv_done.notify_all();
+    if (r != CYL_OK) retire(srv, job, r);
+    srv->cv_active.notify_all();
   }
 }
 
@@ -199,8 +346,10 @@ void worker_main(cyl_server_s* srv) {
 
 extern "C" {
 
-int cyl_server_create(int64_t hbm_budget_bytes, int32_t workers, cyl_server* out) {
+static int server_create(int64_t hbm_budget_bytes, int32_t workers, bool batched, int32_t max_batch,
+                         cyl_server* out) {
   if (!out || workers < 1 || workers > 64 || hbm_budget_bytes < 0) return CYL_ERR_BAD_ARG;
+  if (batched && (max_batch < 1 || max_batch > 1024)) return CYL_ERR_BAD_ARG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return CYL_ERR_NO_DEVICE;
   auto* srv = new cyl_server_s();
@@ -218,10 +367,21 @@ int cyl_server_create(int64_t hbm_budget_bytes, int32_t workers, cyl_server* out
     hbm_budget_bytes = std::max<int64_t>((int64_t)free_b - reserve, (int64_t)free_b / 2);
   }
   srv->budget = hbm_budget_bytes;
+  srv->batched = batched;
+  srv->max_batch = max_batch;
   srv->t0 = std::chrono::steady_clock::now();
   for (int i = 0; i < workers; ++i) srv->workers.emplace_back(worker_main, srv);
+  if (batched) srv->stepper = std::thread(stepper_main, srv);
   *out = srv;
   return CYL_OK;
+}
+
+int cyl_server_create(int64_t hbm_budget_bytes, int32_t workers, cyl_server* out) {
+  return server_create(hbm_budget_bytes, workers, false, 0, out);
+}
+
+int cyl_server_create_batched(int64_t hbm_budget_bytes, int32_t loaders, int32_t max_batch, cyl_server* out) {
+  return server_create(hbm_budget_bytes, loaders, true, max_batch, out);
 }
 
 int cyl_server_submit(cyl_server s, const cyl_job_desc* job, int64_t* job_id) {
@@ -295,6 +455,8 @@ int cyl_server_destroy(cyl_server s) {
   }
   s->cv_work.notify_all();
   for (auto& t : s->workers) t.join();
+  s->cv_active.notify_all();
+  if (s->stepper.joinable()) s->stepper.join();
   delete s;
   return CYL_OK;
 }

@@ -54,6 +54,7 @@ SIGNATURES = {
     "cyl_batch_step": (C.c_int, [H, P(H), I32, I32]),
     "cyl_batch_destroy": (C.c_int, [H]),
     "cyl_server_create": (C.c_int, [I64, I32, P(H)]),
+    "cyl_server_create_batched": (C.c_int, [I64, I32, I32, P(H)]),
     "cyl_server_submit": (C.c_int, [H, P(abi.JobDesc), PI64]),
     "cyl_server_poll": (C.c_int, [H, I64, P(abi.JobResult)]),
     "cyl_server_wait": (C.c_int, [H, I64, D, P(abi.JobResult)]),

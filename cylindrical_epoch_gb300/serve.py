@@ -40,11 +40,21 @@ def estimate_bytes(deck):
 
 
 class Server:
-    def __init__(self, hbm_budget_bytes=0, workers=4):
+    """The request loop.  batched=False: each worker runs its jobs on their
+    own streams, start to end.  batched=True: workers only open jobs; one
+    stepper advances all open mixed-form jobs of the same mode count
+    together as a batch (cyl_server_create_batched)."""
+
+    def __init__(self, hbm_budget_bytes=0, workers=4, batched=False, max_batch=16):
         self.lib = load()
         self.h = C.c_void_p()
-        abi.check("cyl_server_create", self.lib.cyl_server_create(int(hbm_budget_bytes), int(workers),
-                                                                  C.byref(self.h)))
+        if batched:
+            abi.check("cyl_server_create_batched",
+                      self.lib.cyl_server_create_batched(int(hbm_budget_bytes), int(workers), int(max_batch),
+                                                         C.byref(self.h)))
+        else:
+            abi.check("cyl_server_create", self.lib.cyl_server_create(int(hbm_budget_bytes), int(workers),
+                                                                      C.byref(self.h)))
 
     def submit(self, deck, nsteps, seed=None):
         d, keep = job_desc(deck, nsteps, seed)

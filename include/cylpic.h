@@ -380,6 +380,13 @@ typedef struct cyl_server_s* cyl_server;
  * same time (>= 1). */
 int cyl_server_create(int64_t hbm_budget_bytes, int32_t workers, cyl_server* out);
 /* Queue a job; CYL_ERR_OUT_OF_MEMORY if it alone exceeds the budget. */
+/* The request loop with continuous batching: `loaders` threads admit jobs
+ * against the budget, load them and create their handles; one stepper
+ * thread advances every open job, the mixed-form ones with the same number
+ * of modes together through one cyl_batch (at most max_batch runs per
+ * call), FP64-form ones one at a time, by up to 16 steps per pass; new jobs
+ * join at the next pass, finished ones are retired and their memory freed. */
+int cyl_server_create_batched(int64_t hbm_budget_bytes, int32_t loaders, int32_t max_batch, cyl_server* out);
 int cyl_server_submit(cyl_server s, const cyl_job_desc* job, int64_t* job_id);
 /* Current state of a job (non-blocking). */
 int cyl_server_poll(cyl_server s, int64_t job_id, cyl_job_result* out);

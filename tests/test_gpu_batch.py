@@ -85,3 +85,24 @@ def test_batch_rejects_mixed_modes_and_forms(gpu_lib):
             b.step(runs[:2], 16)
         with pytest.raises(abi.CylError):
             b.step([runs[0], runs[2]], 16)
+
+
+def test_batch_run_replaced_by_new_run(gpu_lib):
+    """A run that leaves and is destroyed, then a new run of the same deck in
+    its place (which may get the same handle address): the batch rebuilds its
+    graph for the new member instead of reusing the old one."""
+    decks = _decks()[:2]
+    loads = [cg.host_load(d) for d in decks]
+    alone = _runs(decks, loads)
+    for r in alone:
+        r.step(32, graph=True)
+    first = cg.Run(decks[0], particles=loads[0][0], rng=loads[0][1])
+    gone = cg.Run(decks[1], particles=loads[1][0], rng=loads[1][1])
+    with cg.Batch(4) as b:
+        b.step([first, gone], 16)
+        gone.close()
+        fresh = cg.Run(decks[1], particles=loads[1][0], rng=loads[1][1])
+        fresh.step(16, graph=True)
+        b.step([first, fresh], 16)
+    _same(alone[0], first)
+    _same(alone[1], fresh)

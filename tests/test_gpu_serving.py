@@ -68,3 +68,29 @@ def test_admission_respects_budget(gpu_lib):
     for q in res:
         if q is not big:
             assert q.t_end <= big.t_start or q.t_start >= big.t_end
+
+
+def test_batched_server_matches_runs_alone(gpu_lib):
+    """The request loop with continuous batching (cyl_server_create_batched):
+    the two mixed-form jobs step together in one batch (with the FP64 job
+    beside them); each result matches the same deck stepped alone on its own
+    handle, within the same tolerances."""
+    jobs = _jobs()
+    alone = []
+    for deck, n, _ in jobs:
+        run = cg.Run(deck)
+        run.step(n, graph=True)
+        alone.append((run.state(), run.diagnostics()))
+        run.close()
+    with serve.Server(0, 2, batched=True, max_batch=4) as srv:
+        ids = [srv.submit(deck, n) for deck, n, _ in jobs]
+        res = [srv.wait(i, 300.0) for i in ids]
+    for (deck, n, tol), (sa, da), b in zip(jobs, alone, res):
+        assert b.status == abi.JOB_DONE, b.error
+        assert b.steps_done == n
+        assert b.state.n_live[0] == sa.n_live[0]
+        assert b.state.n_shifts == sa.n_shifts
+        assert b.diag.device_error == 0
+        assert _rel(b.diag.kinetic_energy, da.kinetic_energy) < tol
+        assert _rel(b.diag.field_energy_e, da.field_energy_e) < tol
+        assert _rel(b.diag.field_energy_b, da.field_energy_b) < tol
