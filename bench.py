@@ -163,19 +163,19 @@ def run_reference(args, rank):
     return 0
 
 
-def scan_decks(n, seed=20261204):
+def scan_decks(n, seed=20261204, nzs=(512, 1024, 2048), nrs=(64, 128, 256)):
     """The parameter-scan stream: n wakefield decks with nz in {512, 1024, 2048},
     nr in {64, 128, 256}, modes m = 0..1 or 0..2, a0 ~ U[0.5, 3], density
     log-uniform in [5e23, 5e24] m^-3, 4-16 particles per cell, 500-2000 steps,
-    mixed precision, and Poisson arrival gaps."""
+    mixed precision (other grid sizes through nzs, nrs)."""
     import numpy as np
     import cylindrical_epoch_gb300 as cg
     from cylindrical_epoch_gb300 import abi
     rng = np.random.default_rng(seed)
     out = []
     for k in range(n):
-        nx = int(rng.choice([512, 1024, 2048]))
-        ny = int(rng.choice([64, 128, 256]))
+        nx = int(rng.choice(list(nzs)))
+        ny = int(rng.choice(list(nrs)))
         nm = int(rng.choice([2, 3]))
         a0 = float(rng.uniform(0.5, 3.0))
         dens = float(10 ** rng.uniform(math.log10(5e23), math.log10(5e24)))
@@ -223,6 +223,14 @@ def run_serve(args):
     with serve.Server(0, args.workers, batched=True, max_batch=args.max_batch) as srv:
         ids = [srv.submit(deck, steps) for deck, steps in decks]
         res_bsat = [srv.wait(i, 3600.0) for i in ids]
+    # a scan of small decks (at most one push tile per SM: the ones the
+    # batched loop steps together), all submitted at once, through both loops
+    small = scan_decks(args.jobs, seed=20261205, nzs=(128, 256), nrs=(32, 64))
+    small_res = {}
+    for mode in ("streams", "batched"):
+        with serve.Server(0, args.workers, batched=(mode == "batched"), max_batch=args.max_batch) as srv:
+            ids = [srv.submit(deck, steps) for deck, steps in small]
+            small_res[mode] = [srv.wait(i, 3600.0) for i in ids]
     clk = clocks.stop()
     bad = [r.error for r in res if r.status != abi.JOB_DONE]
     st = serve.latency_stats(res)
@@ -265,9 +273,19 @@ def run_serve(args):
                                 "makespan_s": st_b["makespan_s"]},
                     "saturated": {"value": st_bsat["aggregate"], "makespan_s": st_bsat["makespan_s"],
                                   "p50_s": st_bsat["p50_s"], "p99_s": st_bsat["p99_s"]},
-                    "note": "continuous batching: mixed-form jobs with the same modes step together, "
-                            f"at most {args.max_batch} per batch, {args.workers} loader threads"},
-        "failed_jobs": len(bad) + sum(1 for r in res_sat + res_b + res_bsat if r.status != abi.JOB_DONE),
+                    "note": "continuous batching: mixed-form jobs of at most one push tile per SM "
+                            "step together (none in this scan: its decks fill the device alone and run "
+                            f"on their loader's stream), at most {args.max_batch} open jobs, "
+                            f"{args.workers} loader threads"},
+        "small_scan": {"workload": f"{len(small)} wakefield decks as above but nz {{128,256}}, nr {{32,64}} "
+                                   "(at most 128 tiles of 16x8 cells), all submitted at once",
+                       **{mode: {"value": serve.latency_stats(r)["aggregate"], "unit": "particle-steps/s",
+                                 "makespan_s": serve.latency_stats(r)["makespan_s"],
+                                 "p50_s": serve.latency_stats(r)["p50_s"],
+                                 "p99_s": serve.latency_stats(r)["p99_s"]}
+                          for mode, r in small_res.items()}},
+        "failed_jobs": len(bad) + sum(1 for r in res_sat + res_b + res_bsat + small_res["streams"]
+                                      + small_res["batched"] if r.status != abi.JOB_DONE),
         "failed": [{"job": k, "error": int(r.error), "nx": decks[k][0].nx, "ny": decks[k][0].ny,
                     "n_mode": decks[k][0].n_mode, "ppc": decks[k][0].species[0].npart_per_cell,
                     "steps_done": int(r.steps_done)}

@@ -14,11 +14,14 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "cyl_common.cuh"
 #include "cyl_kernels.cuh"
+#include "host_pool.h"
 #include "host_deck.h"
 #include "push_mixed.cuh"
 
@@ -685,6 +688,7 @@ struct cyl_batch_s {
   std::vector<uint64_t> g_runs;  // membership (handle serials) and parities of the captured graph
   std::vector<int> g_par;
   int g_jobs = 0;
+  std::unique_ptr<HostPool> pool;  // per-run host preparation of a chunk
 };
 
 namespace cyl {
@@ -1605,6 +1609,8 @@ int cyl_batch_create(int32_t max_runs, cyl_batch* out) {
   ok(cudaMallocHost(&b->h_jobs, tab));
   ok(cudaMalloc(&b->d_jobs, tab));
   ok(cudaMalloc(&b->d_nwork, sizeof(int)));
+  const int hw = (int)std::thread::hardware_concurrency();
+  b->pool.reset(new HostPool(std::max(0, std::min({max_runs - 1, hw / 2, 8}))));
   if (e != cudaSuccess) {
     cyl_batch_destroy(b);
     return e == cudaErrorMemoryAllocation ? CYL_ERR_OUT_OF_MEMORY : CYL_ERR_CUDA;
@@ -1657,10 +1663,20 @@ int cyl_batch_step(cyl_batch b, const cyl_handle* hs, int32_t n, int32_t nsteps)
   int32_t done = 0;
   while (done < nsteps) {
     const int k = nsteps - done < CHUNK ? nsteps - done : CHUNK;
-    // each run's step records and host inputs (as run_chunk), copied on its stream
-    for (Handle* h : runs) {
-      if (h->copy_pending && cudaEventSynchronize(h->ev_copy) != cudaSuccess) return CYL_ERR_CUDA;
-      if (int r = flush_push_timing(h)) return r;
+    // each run's step records and host inputs (as run_chunk), copied on its
+    // stream; runs share no host state, so the pool prepares them in parallel
+    std::vector<int> prep_err(runs.size(), CYL_OK);
+    b->pool->run((int)runs.size(), [&](int r) {
+      Handle* h = runs[(size_t)r];
+      cudaSetDevice(h->device);
+      if (h->copy_pending && cudaEventSynchronize(h->ev_copy) != cudaSuccess) {
+        prep_err[(size_t)r] = CYL_ERR_CUDA;
+        return;
+      }
+      if (int rc = flush_push_timing(h)) {
+        prep_err[(size_t)r] = rc;
+        return;
+      }
       int64_t inj_used = 0;
       for (int i = 0; i < k; ++i) prepare_step(h, i, inj_used);
       cudaError_t e = cudaMemcpyAsync(h->d_rec, h->h_rec, sizeof(StepRec) * k, cudaMemcpyHostToDevice, h->st);
@@ -1671,10 +1687,15 @@ int cyl_batch_step(cyl_batch b, const cyl_handle* hs, int32_t n, int32_t nsteps)
         e = cudaMemcpyAsync(h->d_inj, h->h_inj, sizeof(double) * 8 * inj_used, cudaMemcpyHostToDevice, h->st);
       if (e == cudaSuccess) e = cudaEventRecord(h->ev_copy, h->st);
       if (e == cudaSuccess) e = cudaStreamWaitEvent(b->st, h->ev_copy, 0);
-      if (e != cudaSuccess) return CYL_ERR_CUDA;
+      if (e != cudaSuccess) {
+        prep_err[(size_t)r] = CYL_ERR_CUDA;
+        return;
+      }
       h->copy_pending = true;
       h->timing_pending = 0;
-    }
+    });
+    for (int rc : prep_err)
+      if (rc != CYL_OK) return rc;
     // the job table of the chunk: per step, the fields of the J parity after
     // that step's swap
     if (b->jobs_pending && cudaEventSynchronize(b->ev_jobs) != cudaSuccess) return CYL_ERR_CUDA;

@@ -11,7 +11,14 @@
 // memory to the budget.
 // Workers run their jobs at the same time, so the kernels of several runs
 // overlap on the device; a new job is admitted as soon as a worker and
-// memory are free (continuous batching of independent runs).
+// memory are free.
+// In batched mode (cyl_server_create_batched) a worker only loads a small
+// mixed-form job (at most one push tile per SM) and creates its handle; one
+// stepper thread advances all such open jobs, those with the same number of
+// modes together as one cyl_batch (one push launch per step over all their
+// tiles), and jobs join and leave the batch at 16-step boundaries
+// (continuous batching).  Larger and FP64-form jobs fill the device alone
+// and run on their worker's stream as above.
 //
 // The server is host code on top of the public C ABI; it has no counterpart
 // in the reference, which runs one deck per MPI job.
@@ -72,6 +79,7 @@ struct cyl_server_s {
   // every open job, the mixed-form ones in batches (cyl_batch_step)
   bool batched = false;
   int max_batch = 16;
+  int64_t batch_tiles = 0;  // a mixed-form run joins the batches when its tiles (16 x 8 cells) are at most this
   int loading = 0;  // jobs being opened by workers
   struct Active {
     Job* job;
@@ -87,9 +95,10 @@ namespace {
 
 // Load the job's species on the host (the reference's loader and KISS
 // stream), create its handle and initialise it; a mixed-form run then gets
-// its push tile shape (timed once per deck shape, see g_tile_choice) unless
-// it is to be batched.  Returns CYL_OK or the failing call's status.
-int open_job(cyl_server_s* srv, Job* job, cyl_handle* out, int64_t* n0_out) {
+// its push tile shape (timed once per deck shape, see g_tile_choice) when
+// `tune`, i.e. unless it is to be batched.  Returns CYL_OK or the failing
+// call's status.
+int open_job(cyl_server_s* srv, Job* job, bool tune, cyl_handle* out, int64_t* n0_out) {
   if (cudaSetDevice(srv->device) != cudaSuccess) return CYL_ERR_CUDA;
   const cyl_job_desc& d = job->desc;
   cyl_rng_state rng;
@@ -135,7 +144,7 @@ int open_job(cyl_server_s* srv, Job* job, cyl_handle* out, int64_t* n0_out) {
   }
   hp.clear();
   if (r == CYL_OK) r = cyl_initialise(h);
-  if (r == CYL_OK && d.grid.precision == CYL_PREC_MIXED && !srv->batched) {
+  if (r == CYL_OK && d.grid.precision == CYL_PREC_MIXED && tune) {
     const std::vector<int64_t> key = {srv->device, d.grid.nx, d.grid.ny, d.grid.n_mode,
                                       d.nspecies > 0 ? (int64_t)(d.species[0].npart_per_cell * 1000.0) : 0};
     int shape = -1;
@@ -182,7 +191,7 @@ int close_job(Job* job, cyl_handle h, int64_t done, int64_t n0, int r) {
 int run_job(cyl_server_s* srv, Job* job) {
   cyl_handle h = nullptr;
   int64_t n0 = 0;
-  int r = open_job(srv, job, &h, &n0);
+  int r = open_job(srv, job, true, &h, &n0);
   if (r != CYL_OK) return r;
   {
     std::lock_guard<std::mutex> lock(srv->mu);
@@ -213,12 +222,27 @@ void retire(cyl_server_s* srv, Job* job, int r) {
   srv->cv_done.notify_all();
 }
 
-// Batched mode: advance every open job by up to CHUNK_STEPS steps per pass,
-// mixed-form runs with the same number of modes together (cyl_batch_step,
-// at most max_batch per call), FP64-form runs one at a time; retire the
-// finished ones.  A pass steps each group by the smallest number of steps
-// any member has left, so members finish at chunk boundaries and new jobs
-// join at the next pass.
+// Is the job one for the batches?  A mixed-form run whose push has at most
+// one 16 x 8-cell tile per SM cannot fill the device alone, and many such
+// runs stepped as separate streams lose to one launch over all their tiles;
+// a larger run fills the device by itself, and a batch's per-step join of
+// all members would only cost it the overlap of one run's field stages with
+// another's push, so it runs alone on its own stream like an FP64-form run.
+bool batchable(const cyl_server_s* srv, const cyl_job_desc& d) {
+  if (d.grid.precision != CYL_PREC_MIXED) return false;
+  int32_t tx = 0, ty = 0;
+  if (cyl_tile_shape(0, &tx, &ty) != CYL_OK || tx < 1 || ty < 1) return false;
+  const int64_t tiles = (((int64_t)d.grid.nx + tx - 1) / tx) * (((int64_t)d.grid.ny + ty - 1) / ty);
+  return tiles <= srv->batch_tiles;
+}
+
+// Batched mode (at most max_batch jobs open at once, counting those being
+// loaded and those run alone): advance every batched job by up to
+// CHUNK_STEPS steps per pass, those with the same number of modes together
+// (cyl_batch_step, at most max_batch per call); retire the finished ones.
+// A pass steps each group by the smallest number of steps any member has
+// left, so members finish at chunk boundaries and new jobs join at the next
+// pass.
 void stepper_main(cyl_server_s* srv) {
   cudaSetDevice(srv->device);
   std::map<int, cyl_batch> batches;
@@ -232,13 +256,8 @@ void stepper_main(cyl_server_s* srv) {
       if (srv->active.empty()) break;
       act = srv->active;
     }
-    std::map<int, std::vector<size_t>> groups;  // mixed runs by modes
-    std::vector<size_t> singles;
-    for (size_t a = 0; a < act.size(); ++a) {
-      const cyl_job_desc& d = act[a].job->desc;
-      if (d.grid.precision == CYL_PREC_MIXED) groups[d.grid.n_mode].push_back(a);
-      else singles.push_back(a);
-    }
+    std::map<int, std::vector<size_t>> groups;  // runs by modes
+    for (size_t a = 0; a < act.size(); ++a) groups[act[a].job->desc.grid.n_mode].push_back(a);
     std::vector<int> err(act.size(), CYL_OK);
     std::vector<int64_t> stepped(act.size(), 0);
     for (auto& g : groups) {
@@ -268,11 +287,6 @@ void stepper_main(cyl_server_s* srv) {
           stepped[a] = rc == CYL_OK ? k : 0;
         }
       }
-    }
-    for (size_t a : singles) {
-      const int64_t k = std::min<int64_t>(CHUNK_STEPS, act[a].job->desc.nsteps - act[a].done);
-      err[a] = cyl_step_graph(act[a].h, (int32_t)k);
-      stepped[a] = err[a] == CYL_OK ? k : 0;
     }
     // bookkeeping; finished or failed jobs leave the active set
     std::vector<cyl_server_s::Active> leaving;
@@ -306,11 +320,15 @@ void stepper_main(cyl_server_s* srv) {
 void worker_main(cyl_server_s* srv) {
   for (;;) {
     Job* job = nullptr;
+    bool to_stepper = false;
     {
       std::unique_lock<std::mutex> lock(srv->mu);
-      // admit the head of the queue when it fits (or when nothing else holds memory)
+      // admit the head of the queue when it fits (or when nothing else holds
+      // memory); in batched mode also while fewer than max_batch jobs are open,
+      // so that queued jobs wait for a place instead of slowing every open one
       srv->cv_work.wait(lock, [&] {
         if (srv->queue.empty()) return srv->stop;
+        if (srv->batched && srv->running >= srv->max_batch) return false;
         const int64_t need = srv->queue.front()->res.device_bytes;
         return srv->in_use + need <= srv->budget || srv->in_use == 0;
       });
@@ -320,15 +338,16 @@ void worker_main(cyl_server_s* srv) {
       srv->in_use += job->res.device_bytes;
       srv->running += 1;
       job->res.status = CYL_JOB_RUNNING;
-      if (srv->batched) srv->loading += 1;  // with the pop, so the stepper never misses it
+      to_stepper = srv->batched && batchable(srv, job->desc);
+      if (to_stepper) srv->loading += 1;  // with the pop, so the stepper never misses it
     }
-    if (!srv->batched) {
+    if (!to_stepper) {
       retire(srv, job, run_job(srv, job));
       continue;
     }
     cyl_handle h = nullptr;
     int64_t n0 = 0;
-    const int r = open_job(srv, job, &h, &n0);
+    const int r = open_job(srv, job, false, &h, &n0);
     {
       std::lock_guard<std::mutex> lock(srv->mu);
       srv->loading -= 1;
@@ -369,6 +388,12 @@ static int server_create(int64_t hbm_budget_bytes, int32_t workers, bool batched
   srv->budget = hbm_budget_bytes;
   srv->batched = batched;
   srv->max_batch = max_batch;
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, srv->device) != cudaSuccess) {
+    delete srv;
+    return CYL_ERR_CUDA;
+  }
+  srv->batch_tiles = sms;
   srv->t0 = std::chrono::steady_clock::now();
   for (int i = 0; i < workers; ++i) srv->workers.emplace_back(worker_main, srv);
   if (batched) srv->stepper = std::thread(stepper_main, srv);

@@ -41,9 +41,10 @@ def estimate_bytes(deck):
 
 class Server:
     """The request loop.  batched=False: each worker runs its jobs on their
-    own streams, start to end.  batched=True: workers only open jobs; one
-    stepper advances all open mixed-form jobs of the same mode count
-    together as a batch (cyl_server_create_batched)."""
+    own streams, start to end.  batched=True: workers only open the small
+    mixed-form jobs (at most one push tile per SM); one stepper advances all
+    of them with the same mode count together as a batch, and larger or
+    FP64-form jobs run as with batched=False (cyl_server_create_batched)."""
 
     def __init__(self, hbm_budget_bytes=0, workers=4, batched=False, max_batch=16):
         self.lib = load()

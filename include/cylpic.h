@@ -379,14 +379,16 @@ typedef struct cyl_server_s* cyl_server;
  * memory of the device at creation, minus 2 GiB); workers: jobs run at the
  * same time (>= 1). */
 int cyl_server_create(int64_t hbm_budget_bytes, int32_t workers, cyl_server* out);
-/* Queue a job; CYL_ERR_OUT_OF_MEMORY if it alone exceeds the budget. */
 /* The request loop with continuous batching: `loaders` threads admit jobs
- * against the budget, load them and create their handles; one stepper
- * thread advances every open job, the mixed-form ones with the same number
- * of modes together through one cyl_batch (at most max_batch runs per
- * call), FP64-form ones one at a time, by up to 16 steps per pass; new jobs
- * join at the next pass, finished ones are retired and their memory freed. */
+ * against the budget (and while fewer than max_batch jobs are open).  A
+ * mixed-form job with at most one push tile (16 x 8 cells) per SM is loaded
+ * and handed to one stepper thread, which advances all such jobs with the
+ * same number of modes together through one cyl_batch, by up to 16 steps
+ * per pass; new jobs join at the next pass, finished ones are retired and
+ * their memory freed.  Larger and FP64-form jobs fill the device alone and
+ * run start to end on their loader's stream, as in cyl_server_create. */
 int cyl_server_create_batched(int64_t hbm_budget_bytes, int32_t loaders, int32_t max_batch, cyl_server* out);
+/* Queue a job; CYL_ERR_OUT_OF_MEMORY if it alone exceeds the budget. */
 int cyl_server_submit(cyl_server s, const cyl_job_desc* job, int64_t* job_id);
 /* Current state of a job (non-blocking). */
 int cyl_server_poll(cyl_server s, int64_t job_id, cyl_job_result* out);
