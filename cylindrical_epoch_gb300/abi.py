@@ -23,6 +23,8 @@ NOALLOC_MAX_PARTICLES = 262144  # CYL_NOALLOC_MAX_PARTICLES
 N_TILE_SHAPES = 5  # CYL_N_TILE_SHAPES
 TUNE_SET = 0       # CYL_TUNE_SET
 TUNE_TIME = 1      # CYL_TUNE_TIME
+RNG_KISS = 0       # CYL_RNG_KISS: host KISS stream, the reference's order
+RNG_COUNTER = 1    # CYL_RNG_COUNTER: device counter stream (Philox4x32-10)
 
 ERROR_NAMES = {
     CYL_ERR_BAD_ARG: "bad argument",

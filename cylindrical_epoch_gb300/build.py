@@ -32,6 +32,7 @@ SOURCES = [
     ("push_fp64.cu", ["--fmad=false"], "push_fp64"),
     ("particles.cu", ["--fmad=false"], "particles"),
     ("charge.cu", ["--fmad=false"], "charge"),
+    ("loader.cu", ["--fmad=false"], "loader"),
 ] + [
     ("push_mixed.cu", ["--fmad=true", f"-DCYL_TILE_X={tx}", f"-DCYL_TILE_Y={ty}", f"-DCYL_TILE_NS=t{tx}x{ty}",
                        f"-DCYL_TILE_FNS=push_mixed_fns_{tx}x{ty}"], f"push_mixed_{tx}x{ty}")

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "cyl_common.cuh"
+#include "counter_rng.cuh"
 #include "cyl_kernels.cuh"
 #include "host_pool.h"
 #include "host_deck.h"
@@ -47,6 +48,7 @@ struct HostLaser {
 
 struct Handle {
   uint64_t serial = 0;  // unique per handle in the process (never reused, unlike the address)
+  uint64_t topo_epoch = 0;  // bumped when the kernels of a step change (captured graphs are stale)
   int device = 0;
   cudaStream_t st = nullptr;
   cudaError_t last_cuda_error = cudaSuccess;
@@ -74,6 +76,11 @@ struct Handle {
   SortScratch sc;
   double* sort_buf = nullptr;
   int64_t next_id = 0;
+  // window injection: 0 = the host KISS stream (reference order), 1 = the
+  // device counter stream keyed by inj_seed (cyl_set_injection_stream)
+  int inj_counter = 0;
+  uint64_t inj_seed = 0;
+  InjSpecies* d_injsp = nullptr;
   // host bookkeeping (module globals)
   double time = 0.0;
   int64_t step = 0;
@@ -249,6 +256,62 @@ static void fill_grid(StepRec& r, const HostGrid& g, bool after) {
 
 // Advance the host scalars through one driver-loop iteration and describe it
 // (epoch2d.F90:213-265 with moving_window, window.F90:330-376).
+// The window shifts of one step with the injection drawn on the device
+// (k_inject_counter): per shift the column's left edge x_grid_max + dx/2
+// and global shift index, per species the clamped column density
+// (insert_particles evaluates the profile at pack_ix = nx) and the count --
+// floor(ppc) per row plus the rows' fraction bits, recomputed here from the
+// same counter stream -- then the grid shift.  Ids are handed out shift by
+// shift, species by species, and the batch holds each species' particles
+// together, as in the host path.  At most MAX_INJ_SHIFTS shifts per step
+// (cyl_set_injection_stream checks the deck allows no more).
+static void inject_counter_step(Handle* h, StepRec& r, int cells, int64_t& inj_used) {
+  r.inj_counter = 1;
+  r.inj_nshift = cells;
+  int64_t cnt[MAX_INJ_SHIFTS][MAX_SPECIES] = {};
+  for (int c = 0; c < cells && c < MAX_INJ_SHIFTS; ++c) {
+    r.inj_x0[c] = h->g.x_grid_max + 0.5 * h->g.dx;
+    r.inj_shift[c] = h->n_shifts;
+    for (int s = 0; s < h->nsp; ++s) {
+      const cyl_species_desc& d = h->sd[s];
+      double dens = species_density(d, h->g.xg(h->g.nx));
+      if (dens > d.density_max) dens = d.density_max;
+      if (dens < d.density_min) dens = 0.0;
+      int64_t n = 0;
+      if (!d.immobile && dens >= d.density_min) {
+        const int64_t nppc = (int64_t)std::floor(d.npart_per_cell);
+        const double frac = d.npart_per_cell - (double)nppc;
+        for (int iy = 1; iy <= h->g.ny; ++iy) {
+          n += nppc;
+          if (frac > 0.0 &&
+              u01(philox4x32_10((uint32_t)iy, (uint32_t)h->n_shifts, (uint32_t)s, TAG_INJ_COUNT, h->inj_seed)
+                      .v[0]) < frac)
+            n += 1;
+        }
+      }
+      r.inj_dens[c][s] = dens;
+      r.inj_id0[c][s] = h->next_id;
+      r.inj_n[c][s] = n;
+      cnt[c][s] = n;
+      h->next_id += n;
+    }
+    h->g.x_grid_min = h->g.xg(1) + h->g.dx;
+    h->g.xb_min = h->g.xb_min + h->g.dx;
+    h->g.x_min = h->g.xb_min + h->g.dx * 0.0;
+    h->g.x_max = (h->g.xb_min + (double)(h->g.nx + 1 - 1) * h->g.dx) - h->g.dx * 0.0;
+    h->g.setup_grid_x();
+    h->n_shifts++;
+  }
+  for (int s = 0; s < h->nsp; ++s) {
+    r.inject_off[s] = inj_used;
+    for (int c = 0; c < cells && c < MAX_INJ_SHIFTS; ++c) {
+      r.inj_base[c][s] = inj_used;
+      inj_used += cnt[c][s];
+    }
+    r.inject_cnt[s] = inj_used - r.inject_off[s];
+  }
+}
+
 static void prepare_step(Handle* h, int k, int64_t& inj_used) {
   StepRec& r = h->h_rec[k];
   std::memset(&r, 0, sizeof(r));
@@ -282,7 +345,11 @@ static void prepare_step(Handle* h, int k, int64_t& inj_used) {
     if (h->window_started && !(h->time >= h->window_stop_time) && h->window_v_x > 0.0) {
       h->wsf = h->wsf + h->g.dt * h->window_v_x / h->g.dx;
       const int cells = (int)std::floor(h->wsf);
-      if (cells > 0) {
+      if (cells > 0 && h->inj_counter) {
+        inject_counter_step(h, r, cells, inj_used);
+        nshift = cells;
+        h->wsf = h->wsf - (double)cells;
+      } else if (cells > 0) {
         std::vector<HostParticle> batch;
         // one buffer region per species: inject all species for every shift
         std::vector<std::vector<HostParticle>> per(h->nsp);
@@ -386,6 +453,10 @@ static void enqueue_step_post(Handle* h, cudaStream_t s, const FieldSetT<T>& F, 
   launch_e_axis_bcs(s, F, rec, rc);
   count_launch(h, 6);
   if (h->move_window) {
+    if (h->inj_counter) {
+      launch_inject_counter(s, rec, h->d_injsp, h->nsp, rc, h->inj_seed, h->d_inj);
+      count_launch(h, 1);
+    }
     for (int i = 0; i < h->nsp; ++i) {
       if (h->prec == CYL_PREC_MIXED)
         mixed_window_particles(s, h->sp[i], h->d_cnt + i, h->d_inj, rec, i, h->xg0, rc, h->d_err, h->nblocks);
@@ -530,7 +601,7 @@ static int run_chunk(Handle* h, int k, bool use_graph) {
   if (int r = flush_push_timing(h)) return r;
   CK(cudaMemcpyAsync(h->d_rec, h->h_rec, sizeof(StepRec) * k, cudaMemcpyHostToDevice, h->st));
   CK(cudaMemcpyAsync(h->d_src, h->h_src, sizeof(double) * h->src_per_step * k, cudaMemcpyHostToDevice, h->st));
-  if (inj_used > 0)
+  if (inj_used > 0 && !h->inj_counter)
     CK(cudaMemcpyAsync(h->d_inj, h->h_inj, sizeof(double) * 8 * inj_used, cudaMemcpyHostToDevice, h->st));
   CK(cudaEventRecord(h->ev_copy, h->st));
   h->copy_pending = true;
@@ -685,7 +756,7 @@ struct cyl_batch_s {
   int64_t work_cap = 0;
   bool jobs_pending = false;
   cudaGraphExec_t gexec = nullptr;
-  std::vector<uint64_t> g_runs;  // membership (handle serials) and parities of the captured graph
+  std::vector<uint64_t> g_runs;  // membership (handle serials, step epochs) and parities of the captured graph
   std::vector<int> g_par;
   int g_jobs = 0;
   std::unique_ptr<HostPool> pool;  // per-run host preparation of a chunk
@@ -1017,6 +1088,7 @@ int cyl_destroy(cyl_handle hh) {
   Handle* h = &hh->h;
   if (h->st) cudaStreamSynchronize(h->st);
   if (h->gexec) cudaGraphExecDestroy(h->gexec);
+  cudaFree(h->d_injsp);
   for (int i = 0; i < h->nsp; ++i)
     if (h->sp[i].x) cudaFree(h->sp[i].x);
   cudaFree(h->fbuf);
@@ -1088,6 +1160,141 @@ int cyl_upload_particles(cyl_handle hh, int32_t isp, const double* x, const doub
   std::memcpy(&c.wmax_bits, &wmax, sizeof(float));
   CK(cudaMemcpyAsync(h->d_cnt + isp, &c, sizeof(c), cudaMemcpyHostToDevice, s));
   CK(cudaStreamSynchronize(s));
+  return CYL_OK;
+}
+
+int cyl_load_species_device(cyl_handle hh, int32_t isp, uint64_t seed, int64_t id_base, int64_t* n_out) {
+  if (!hh || !n_out) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  if (isp < 0 || isp >= h->nsp || id_base < 0) return CYL_ERR_BAD_ARG;
+  const cyl_species_desc& d = h->sd[isp];
+  if (d.immobile) return CYL_ERR_BAD_ARG;
+  SpeciesPtrs& p = h->sp[isp];
+  std::vector<double> dens;
+  std::vector<char> dmap;
+  std::vector<int32_t> valid;
+  host_density_map(h->g, h->gd, d, dens, dmap, valid);
+  const int64_t nvalid = (int64_t)valid.size();
+  const int64_t n = (int64_t)std::floor(d.npart_per_cell * (double)nvalid);
+  if (n > p.cap) return CYL_ERR_CAPACITY;
+  cudaStream_t s = h->st;
+  CK(cudaStreamSynchronize(s));
+  SpeciesCounters c{n, 0, 0u, 0u};
+  CK(cudaMemcpy(h->d_cnt + isp, &c, sizeof(c), cudaMemcpyHostToDevice));
+  if (n > 0) {
+    double* d_dens = nullptr;
+    int8_t* d_dmap = nullptr;
+    int32_t* d_valid = nullptr;
+    int* d_npic = nullptr;
+    const size_t cells = dens.size();
+    auto release = [&]() {
+      cudaFree(d_dens);
+      cudaFree(d_dmap);
+      cudaFree(d_valid);
+      cudaFree(d_npic);
+    };
+    if (cudaMalloc(&d_dens, cells * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&d_dmap, cells) != cudaSuccess ||
+        cudaMalloc(&d_valid, (size_t)nvalid * sizeof(int32_t)) != cudaSuccess ||
+        cudaMalloc(&d_npic, cells * sizeof(int)) != cudaSuccess) {
+      release();
+      return CYL_ERR_OUT_OF_MEMORY;
+    }
+    std::vector<int8_t> dm(cells);
+    for (size_t k = 0; k < cells; ++k) dm[k] = (int8_t)dmap[k];
+    cudaError_t e = cudaMemcpy(d_dens, dens.data(), cells * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_dmap, dm.data(), cells, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(d_valid, valid.data(), (size_t)nvalid * sizeof(int32_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_npic, 0, cells * sizeof(int), s);
+    LoadParams P{};
+    P.nx = h->g.nx;
+    P.ny = h->g.ny;
+    P.W = h->g.nx + 2 * NG;
+    P.dx = h->g.dx;
+    P.dy = h->g.dy;
+    P.x_grid_min = h->g.x_grid_min;
+    P.y_grid_min = h->g.y_grid_min;
+    P.nppc = (int64_t)std::floor(d.npart_per_cell);
+    P.nvalid = nvalid;
+    P.n = n;
+    P.id_base = id_base;
+    P.seed = seed;
+    P.species = isp;
+    for (int k = 0; k < 3; ++k) {
+      P.temp[k] = d.temp[k];
+      P.drift[k] = d.drift[k];
+    }
+    P.mass = d.mass;
+    // the FP64 form loads into the particle arrays, the mixed form into the
+    // FP64 staging of cyl_upload_particles, converted on the device after
+    LoadOut o;
+    double* st = h->sc.tmp;
+    const int64_t cap = h->sc.cap;
+    if (h->prec == CYL_PREC_MIXED)
+      o = LoadOut{st, st + cap, st + 2 * cap, st + 3 * cap, st + 4 * cap, st + 5 * cap, st + 6 * cap,
+                  (int64_t*)(st + 7 * cap)};
+    else
+      o = LoadOut{p.x, p.y, p.z, p.px, p.py, p.pz, p.w, p.id};
+    if (e == cudaSuccess) {
+      launch_load_particles(s, P, d_valid, d_dens, d_dmap, d_npic, o, &h->d_cnt[isp].wmax_bits);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && h->prec == CYL_PREC_MIXED) {
+      mixed_from_double(s, p, st, n, cap, h->xg0, h->rc);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    release();
+    if (e != cudaSuccess) {
+      h->last_cuda_error = e;
+      return e == cudaErrorMemoryAllocation ? CYL_ERR_OUT_OF_MEMORY : CYL_ERR_CUDA;
+    }
+  }
+  if (id_base + n > h->next_id) h->next_id = id_base + n;
+  *n_out = n;
+  return CYL_OK;
+}
+
+int cyl_counter_block(uint64_t seed, const uint32_t* ctr4, uint32_t* out4) {
+  if (!ctr4 || !out4) return CYL_ERR_BAD_ARG;
+  const U4 r = philox4x32_10(ctr4[0], ctr4[1], ctr4[2], ctr4[3], seed);
+  for (int k = 0; k < 4; ++k) out4[k] = r.v[k];
+  return CYL_OK;
+}
+
+int cyl_set_injection_stream(cyl_handle hh, int32_t mode, uint64_t seed) {
+  if (!hh) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  if (mode != CYL_RNG_KISS && mode != CYL_RNG_COUNTER) return CYL_ERR_BAD_ARG;
+  if (mode == CYL_RNG_COUNTER && h->move_window) {
+    const double shifts_max = std::floor(h->g.dt * std::fabs(h->window_v_x) / h->g.dx) + 1.0;
+    if (shifts_max > (double)MAX_INJ_SHIFTS) return CYL_ERR_UNSUPPORTED;
+  }
+  if (mode == CYL_RNG_COUNTER && !h->d_injsp) {
+    InjSpecies tab[MAX_SPECIES] = {};
+    for (int s = 0; s < h->nsp; ++s) {
+      const cyl_species_desc& d = h->sd[s];
+      tab[s].nppc = (int64_t)std::floor(d.npart_per_cell);
+      tab[s].frac = d.npart_per_cell - (double)tab[s].nppc;
+      for (int k = 0; k < 3; ++k) {
+        tab[s].temp[k] = d.temp[k];
+        tab[s].drift[k] = d.drift[k];
+      }
+      tab[s].mass = d.mass;
+    }
+    CK(cudaStreamSynchronize(h->st));
+    if (cudaMalloc(&h->d_injsp, sizeof(tab)) != cudaSuccess) return CYL_ERR_OUT_OF_MEMORY;
+    CK(cudaMemcpy(h->d_injsp, tab, sizeof(tab), cudaMemcpyHostToDevice));
+  }
+  h->inj_counter = mode == CYL_RNG_COUNTER;
+  h->inj_seed = seed;
+  // the step's kernels change: a captured step graph is rebuilt
+  if (h->gexec) {
+    cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+  }
+  h->topo_epoch++;
   return CYL_OK;
 }
 
@@ -1386,6 +1593,7 @@ int cyl_tile_shape(int32_t shape, int32_t* tx, int32_t* ty) {
 static void set_tile_shape(Handle* h, int k) {
   h->tile_shape = k;
   h->nblocks_mixed = h->nblocks_by_shape[k];
+  h->topo_epoch++;
   if (h->gexec) {
     cudaGraphExecDestroy(h->gexec);
     h->gexec = nullptr;
@@ -1683,7 +1891,7 @@ int cyl_batch_step(cyl_batch b, const cyl_handle* hs, int32_t n, int32_t nsteps)
       if (e == cudaSuccess)
         e = cudaMemcpyAsync(h->d_src, h->h_src, sizeof(double) * h->src_per_step * k, cudaMemcpyHostToDevice,
                             h->st);
-      if (e == cudaSuccess && inj_used > 0)
+      if (e == cudaSuccess && inj_used > 0 && !h->inj_counter)
         e = cudaMemcpyAsync(h->d_inj, h->h_inj, sizeof(double) * 8 * inj_used, cudaMemcpyHostToDevice, h->st);
       if (e == cudaSuccess) e = cudaEventRecord(h->ev_copy, h->st);
       if (e == cudaSuccess) e = cudaStreamWaitEvent(b->st, h->ev_copy, 0);
@@ -1721,8 +1929,11 @@ int cyl_batch_step(cyl_batch b, const cyl_handle* hs, int32_t n, int32_t nsteps)
       return CYL_ERR_CUDA;
     b->jobs_pending = true;
     if (k == CHUNK) {
-      std::vector<uint64_t> serials(runs.size());
-      for (size_t r = 0; r < runs.size(); ++r) serials[r] = runs[r]->serial;
+      std::vector<uint64_t> serials(2 * runs.size());
+      for (size_t r = 0; r < runs.size(); ++r) {
+        serials[2 * r] = runs[r]->serial;
+        serials[2 * r + 1] = runs[r]->topo_epoch;
+      }
       const bool same = b->gexec && b->g_runs == serials && b->g_par == par0 && b->g_jobs == nj;
       if (!same) {
         if (b->gexec) {

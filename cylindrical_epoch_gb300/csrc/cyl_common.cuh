@@ -20,6 +20,7 @@ constexpr int NG = CYL_NG;  // ghost width of every mode array
 constexpr int JNG = CYL_NG;
 constexpr int PNG = 3;
 constexpr int MAX_SPECIES = 8;
+constexpr int MAX_INJ_SHIFTS = 2;  // window shifts per step the device injector handles
 constexpr int MAX_LASERS = 8;
 constexpr int MAX_MODES = 8;
 
@@ -142,6 +143,18 @@ struct StepRec {
   int64_t src_off;           // offset of this step's laser source vectors
   int32_t nshift_total;      // window shifts before this step (mixed-form cell origin)
   int32_t nshift_total_after;
+  // window injection drawn on the device from the counter stream (counter_rng.cuh):
+  // per shift c of this step and species s, the column's left edge, the
+  // global shift index, the clamped column density, and where its particles
+  // go in the injection batch (inject_off[s] + ...) with their first id
+  int32_t inj_counter;       // 1: the kernel k_inject_counter makes this step's batch
+  int32_t inj_nshift;
+  double inj_x0[MAX_INJ_SHIFTS];
+  int64_t inj_shift[MAX_INJ_SHIFTS];
+  double inj_dens[MAX_INJ_SHIFTS][MAX_SPECIES];
+  int64_t inj_base[MAX_INJ_SHIFTS][MAX_SPECIES];
+  int64_t inj_id0[MAX_INJ_SHIFTS][MAX_SPECIES];
+  int64_t inj_n[MAX_INJ_SHIFTS][MAX_SPECIES];
 };
 
 // Run-constant geometry and physics parameters (pushed by value).

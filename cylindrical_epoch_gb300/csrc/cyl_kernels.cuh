@@ -34,6 +34,32 @@ struct SpeciesCounters {
   uint32_t pad;
 };
 
+// loader.cu: particle loading and window injection from the counter stream
+// (counter_rng.cuh).  The density map is the (nx + 2ng) x (ny + 2ng) grid of
+// setup_particle_density with row length W; valid lists the valid interior
+// cells as (ix - 1) + nx (iy - 1), iy outer.
+struct LoadParams {
+  int nx, ny, W;
+  double dx, dy, x_grid_min, y_grid_min;
+  int64_t nppc, nvalid, n, id_base;
+  uint64_t seed;
+  int species;
+  double temp[3], drift[3], mass;
+};
+struct LoadOut {
+  double *x, *y, *z, *px, *py, *pz, *w;
+  int64_t* id;
+};
+struct InjSpecies {  // per species: what insert_particles needs besides the column density
+  int64_t nppc;
+  double frac;
+  double temp[3], drift[3], mass;
+};
+void launch_load_particles(cudaStream_t s, const LoadParams& P, const int32_t* valid, const double* dens,
+                           const int8_t* dmap, int* npic, LoadOut o, uint32_t* wmax_bits);
+void launch_inject_counter(cudaStream_t s, const StepRec* rec, const InjSpecies* isp, int nsp, const RunConst& rc,
+                           uint64_t seed, double* inj);
+
 // fields.cu (E/B boundary and axis kernels for either storage type)
 void launch_update_e(cudaStream_t s, const FieldSet& F, const RunConst& rc);
 void launch_update_b(cudaStream_t s, const FieldSet& F, int save_old, const RunConst& rc);

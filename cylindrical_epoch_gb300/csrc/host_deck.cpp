@@ -112,6 +112,32 @@ double species_density(const cyl_species_desc& d, double x) {
   return d.density;
 }
 
+void host_density_map(const HostGrid& g, const cyl_grid_desc& gd, const cyl_species_desc& sp,
+                      std::vector<double>& dens, std::vector<char>& dmap, std::vector<int32_t>& valid) {
+  const int nx = g.nx, ny = g.ny;
+  const int W = nx + 2 * NG_H;
+  auto at = [&](int ix, int iy) { return (size_t)(ix + NG_H - 1) + (size_t)W * (size_t)(iy + NG_H - 1); };
+  dens.assign((size_t)W * (ny + 2 * NG_H), 0.0);
+  dmap.assign(dens.size(), 0);
+  for (int iy = 1 - NG_H; iy <= ny + NG_H; ++iy)
+    for (int ix = 1 - NG_H; ix <= nx + NG_H; ++ix) dens[at(ix, iy)] = species_density(sp, g.xg(ix));
+  if (gd.bc_field[CYL_BD_X_MAX] == CYL_BC_PERIODIC)
+    for (int iy = 1 - NG_H; iy <= ny + NG_H; ++iy)
+      for (int i = 1; i <= NG_H; ++i) dens[at(nx + i, iy)] = dens[at(i, iy)];
+  if (gd.bc_field[CYL_BD_X_MIN] == CYL_BC_PERIODIC)
+    for (int iy = 1 - NG_H; iy <= ny + NG_H; ++iy)
+      for (int i = 1 - NG_H; i <= 0; ++i) dens[at(i, iy)] = dens[at(nx + i, iy)];
+  for (size_t k = 0; k < dens.size(); ++k) {
+    if (dens[k] > sp.density_max) dens[k] = sp.density_max;
+    if (dens[k] >= sp.density_min) dmap[k] = 1;
+    else dens[k] = 0.0;
+  }
+  valid.clear();
+  for (int iy = 1; iy <= ny; ++iy)
+    for (int ix = 1; ix <= nx; ++ix)
+      if (dmap[at(ix, iy)]) valid.push_back((int32_t)((ix - 1) + nx * (iy - 1)));
+}
+
 // ------------------------------------------------------------ injection
 
 void host_insert_particles(const HostGrid& g, const cyl_species_desc& d, KissRng& rng,
@@ -202,29 +228,14 @@ int cyl_host_load_species(const cyl_grid_desc* gd, const cyl_species_desc* sp, c
   if (!gd || !sp || !n_inout) return CYL_ERR_BAD_ARG;
   HostGrid g;
   g.init(*gd);
-  const int nx = g.nx, ny = g.ny;
+  const int nx = g.nx;
   const int W = nx + 2 * NG_H;
   auto at = [&](int ix, int iy) { return (size_t)(ix + NG_H - 1) + (size_t)W * (size_t)(iy + NG_H - 1); };
-  std::vector<double> dens((size_t)W * (ny + 2 * NG_H));
-  std::vector<char> dmap(dens.size(), 0);
-  for (int iy = 1 - NG_H; iy <= ny + NG_H; ++iy)
-    for (int ix = 1 - NG_H; ix <= nx + NG_H; ++ix) dens[at(ix, iy)] = species_density(*sp, g.xg(ix));
-  const bool per = gd->bc_field[CYL_BD_X_MIN] == CYL_BC_PERIODIC;
-  if (gd->bc_field[CYL_BD_X_MAX] == CYL_BC_PERIODIC)
-    for (int iy = 1 - NG_H; iy <= ny + NG_H; ++iy)
-      for (int i = 1; i <= NG_H; ++i) dens[at(nx + i, iy)] = dens[at(i, iy)];
-  if (per)
-    for (int iy = 1 - NG_H; iy <= ny + NG_H; ++iy)
-      for (int i = 1 - NG_H; i <= 0; ++i) dens[at(i, iy)] = dens[at(nx + i, iy)];
-  for (size_t k = 0; k < dens.size(); ++k) {
-    if (dens[k] > sp->density_max) dens[k] = sp->density_max;
-    if (dens[k] >= sp->density_min) dmap[k] = 1;
-    else dens[k] = 0.0;
-  }
-  int64_t nvalid = 0;
-  for (int iy = 1; iy <= ny; ++iy)
-    for (int ix = 1; ix <= nx; ++ix)
-      if (dmap[at(ix, iy)]) nvalid++;
+  std::vector<double> dens;
+  std::vector<char> dmap;
+  std::vector<int32_t> valid_cells;
+  host_density_map(g, *gd, *sp, dens, dmap, valid_cells);
+  const int64_t nvalid = (int64_t)valid_cells.size();
   const int64_t nppc = (int64_t)std::floor(sp->npart_per_cell);
   const int64_t nnew = (int64_t)std::floor(sp->npart_per_cell * (double)nvalid);
   if (!x) {
@@ -236,27 +247,22 @@ int cyl_host_load_species(const cyl_grid_desc* gd, const cyl_species_desc* sp, c
   rng.from_state(rs);
   int64_t n = 0;
   if (nppc > 0) {
-    for (int iy = 1; iy <= ny; ++iy)
-      for (int ix = 1; ix <= nx; ++ix) {
-        if (!dmap[at(ix, iy)]) continue;
-        for (int64_t ip = 0; ip < nppc && n < nnew; ++ip) {
-          x[n] = g.xg(ix) + (rng.random() - 0.5) * g.dx;
-          const double pr = g.yg(iy) + (rng.random() - 0.5) * g.dy;
-          const double th = 2.0 * PI_H * rng.random();
-          y[n] = pr * std::cos(th);
-          z[n] = pr * std::sin(th);
-          ++n;
-        }
+    for (const int32_t cell : valid_cells) {
+      const int iy = cell / nx + 1, ix = cell % nx + 1;
+      for (int64_t ip = 0; ip < nppc && n < nnew; ++ip) {
+        x[n] = g.xg(ix) + (rng.random() - 0.5) * g.dx;
+        const double pr = g.yg(iy) + (rng.random() - 0.5) * g.dy;
+        const double th = 2.0 * PI_H * rng.random();
+        y[n] = pr * std::cos(th);
+        z[n] = pr * std::sin(th);
+        ++n;
       }
+    }
   }
   if (n < nnew) {
-    std::vector<int64_t> valid;
-    for (int iy = 1; iy <= ny; ++iy)
-      for (int ix = 1; ix <= nx; ++ix)
-        if (dmap[at(ix, iy)]) valid.push_back((int64_t)(ix - 1) + (int64_t)nx * (iy - 1));
     while (n < nnew) {
       int64_t ipos = (int64_t)(rng.random() * (double)(nvalid - 1)) + 1;
-      ipos = valid[ipos - 1];
+      ipos = valid_cells[ipos - 1];
       const int64_t cyy = ipos / nx;
       ipos = ipos - nx * cyy;
       const int cy = (int)cyy + 1, cx = (int)ipos + 1;

@@ -49,6 +49,14 @@ struct HostParticle {
 
 double species_density(const cyl_species_desc& d, double x);
 
+// setup_particle_density for one species (helper.F90:373-663): the density
+// on the (nx + 2ng) x (ny + 2ng) grid (index (ix + ng - 1) + W (iy + ng - 1),
+// W = nx + 2ng), with the periodic x self-wrap, clamped to density_max and
+// zeroed below density_min; dmap marks the cells at or above density_min.
+// valid lists the valid interior cells as (ix - 1) + nx (iy - 1), iy outer.
+void host_density_map(const HostGrid& g, const cyl_grid_desc& gd, const cyl_species_desc& sp,
+                      std::vector<double>& dens, std::vector<char>& dmap, std::vector<int32_t>& valid);
+
 // insert_particles (window.F90:157-300) for one species at the current grid
 // (before the shift): appends to out, advances rng and next_id.
 void host_insert_particles(const HostGrid& g, const cyl_species_desc& d, KissRng& rng,

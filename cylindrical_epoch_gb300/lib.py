@@ -29,6 +29,9 @@ SIGNATURES = {
                              P(abi.RngState), P(H)]),
     "cyl_destroy": (C.c_int, [H]),
     "cyl_upload_particles": (C.c_int, [H, I32, PD, PD, PD, PD, PD, PD, PD, PI64, I64]),
+    "cyl_load_species_device": (C.c_int, [H, I32, C.c_uint64, I64, PI64]),
+    "cyl_set_injection_stream": (C.c_int, [H, I32, C.c_uint64]),
+    "cyl_counter_block": (C.c_int, [C.c_uint64, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     "cyl_download_particles": (C.c_int, [H, I32, PD, PD, PD, PD, PD, PD, PD, PI64, PI64]),
     "cyl_upload_field": (C.c_int, [H, I32, PD]),
     "cyl_download_field": (C.c_int, [H, I32, PD]),

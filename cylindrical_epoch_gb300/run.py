@@ -81,19 +81,52 @@ def host_load(deck: Deck, rng=None):
     return out, rng
 
 
-class Run:
-    """One simulation resident on the GPU, driven through the C ABI."""
+def load_counts(deck: Deck):
+    """Particles the loader makes per species (floor(ppc x valid cells); 0
+    for immobile species), without loading them."""
+    lib = load()
+    g = deck.grid_desc()
+    out = []
+    for s in deck.species:
+        n = C.c_int64(0)
+        if not s.immobile:
+            d = s.desc()
+            abi.check("cyl_host_load_species",
+                      lib.cyl_host_load_species(C.byref(g), C.byref(d), None, 0, None, None, None, None, None,
+                                                None, None, None, C.byref(n)))
+        out.append(n.value)
+    return out
 
-    def __init__(self, deck: Deck, particles=None, rng=None, fields=None, initialise=True):
+
+class Run:
+    """One simulation resident on the GPU, driven through the C ABI.
+
+    rng_mode=abi.RNG_KISS (default): particles come from the host loader (the
+    reference's KISS stream, or `particles`) and window injection replays
+    the same stream.  rng_mode=abi.RNG_COUNTER: the species are loaded on the
+    device and the window injects on the device, both from the counter
+    stream keyed by `counter_seed` (default: the deck's seed)."""
+
+    def __init__(self, deck: Deck, particles=None, rng=None, fields=None, initialise=True,
+                 rng_mode=abi.RNG_KISS, counter_seed=None):
         self.lib = load()
         self.deck = deck
-        if particles is None:
+        counter = rng_mode == abi.RNG_COUNTER
+        if counter:
+            counts = load_counts(deck)
+            if rng is None:
+                rng = abi.RngState()
+                self.lib.cyl_rng_init(C.byref(rng), deck.seed)
+        elif particles is None:
             particles, rng = host_load(deck, rng)
         g = deck.grid_desc()
         self.dt = g.dt
         sp = deck.species_descs()
         for i, s in enumerate(deck.species):
-            need = particles[i].n if i < len(particles) else 0
+            if counter:
+                need = counts[i]
+            else:
+                need = particles[i].n if i < len(particles) else 0
             if sp[i].capacity < need + 1024:
                 sp[i].capacity = int(need * 1.1) + 4096
         las, self._keep = deck.laser_descs()
@@ -104,8 +137,20 @@ class Run:
         self.h = h
         self.nxg = deck.nx + 2 * abi.NG
         self.nyg = deck.ny + 2 * abi.NG
-        for i, p in enumerate(particles):
-            self.upload_particles(i, p)
+        if counter:
+            seed = deck.seed if counter_seed is None else int(counter_seed)
+            id_base = 0
+            for i, s in enumerate(deck.species):
+                if s.immobile:
+                    continue
+                n = C.c_int64(0)
+                abi.check("cyl_load_species_device",
+                          self.lib.cyl_load_species_device(self.h, i, seed, id_base, C.byref(n)))
+                id_base += n.value
+            abi.check("cyl_set_injection_stream", self.lib.cyl_set_injection_stream(self.h, abi.RNG_COUNTER, seed))
+        else:
+            for i, p in enumerate(particles):
+                self.upload_particles(i, p)
         if fields:
             for name, arr in fields.items():
                 self.upload_field(name, arr)

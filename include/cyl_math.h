@@ -98,4 +98,61 @@ CYLM_FN double cyl_atan2(double y, double x) {
   return signbit(y) ? -a : a;
 }
 
+/*
+ * cyl_sincos_turn: sin and cos of 2 pi u for u in [0, 1) (u in turns), for
+ * the angles of the counter-stream loader and injector, whose particles'
+ * theta = atan2(z, y) enters the same (m dtheta)^-2 deposit factors: the CUDA
+ * kernels and the CPU restatement must place them bit-identically.
+ * Method: the quadrant k = floor(4u) is split off in turns, where
+ * f = u - k/4 is exact for the stream's u = (r + 1/2) 2^-32; x = 2 pi f lies
+ * in [0, pi/2), and sin x, cos x are their Taylor series to x^23 and x^22
+ * (truncation below 2e-18 at pi/2) in Horner form with the reciprocal
+ * factorial ratios as compile-time constants; the quadrant rotates the pair.
+ * About one ulp from the correctly rounded values (tests/test_cyl_math.py).
+ */
+CYLM_FN void cyl_sincos_turn(double u, double* s, double* c) {
+  int k = (int)(u * 4.0);
+  if (k < 0) k = 0;
+  if (k > 3) k = 3;
+  const double f = u - 0.25 * (double)k;
+  const double x = f * 6.283185307179586;
+  const double x2 = x * x;
+  double ps = 1.0 - x2 * (1.0 / 506.0);  /* 22 * 23 */
+  ps = 1.0 - x2 * (1.0 / 420.0) * ps;    /* 20 * 21 */
+  ps = 1.0 - x2 * (1.0 / 342.0) * ps;
+  ps = 1.0 - x2 * (1.0 / 272.0) * ps;
+  ps = 1.0 - x2 * (1.0 / 210.0) * ps;
+  ps = 1.0 - x2 * (1.0 / 156.0) * ps;
+  ps = 1.0 - x2 * (1.0 / 110.0) * ps;
+  ps = 1.0 - x2 * (1.0 / 72.0) * ps;
+  ps = 1.0 - x2 * (1.0 / 42.0) * ps;
+  ps = 1.0 - x2 * (1.0 / 20.0) * ps;
+  ps = 1.0 - x2 * (1.0 / 6.0) * ps;      /* 2 * 3 */
+  double pc = 1.0 - x2 * (1.0 / 462.0);  /* 21 * 22 */
+  pc = 1.0 - x2 * (1.0 / 380.0) * pc;    /* 19 * 20 */
+  pc = 1.0 - x2 * (1.0 / 306.0) * pc;
+  pc = 1.0 - x2 * (1.0 / 240.0) * pc;
+  pc = 1.0 - x2 * (1.0 / 182.0) * pc;
+  pc = 1.0 - x2 * (1.0 / 132.0) * pc;
+  pc = 1.0 - x2 * (1.0 / 90.0) * pc;
+  pc = 1.0 - x2 * (1.0 / 56.0) * pc;
+  pc = 1.0 - x2 * (1.0 / 30.0) * pc;
+  pc = 1.0 - x2 * (1.0 / 12.0) * pc;
+  pc = 1.0 - x2 * (1.0 / 2.0) * pc;      /* 1 * 2 */
+  const double sx = x * ps, cx = pc;
+  if (k == 0) {
+    *s = sx;
+    *c = cx;
+  } else if (k == 1) {
+    *s = cx;
+    *c = -sx;
+  } else if (k == 2) {
+    *s = -sx;
+    *c = -cx;
+  } else {
+    *s = -cx;
+    *c = sx;
+  }
+}
+
 #endif /* CYL_MATH_H */

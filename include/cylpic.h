@@ -193,6 +193,27 @@ int cyl_upload_particles(cyl_handle h, int32_t ispecies, const double* x,
                          const double* y, const double* z, const double* px,
                          const double* py, const double* pz, const double* w,
                          const int64_t* id, int64_t n);
+/* Device loading and window injection from a counter-based stream
+ * (Philox4x32-10 keyed by seed, one counter per particle) instead of the
+ * reference's serial KISS stream: the loader and injector of the reference
+ * (helper.F90:669-811, window.F90:157-300) with each particle made by its
+ * own thread; the particles differ from the KISS-stream ones but follow the
+ * same distributions, counts, weights and id order.
+ * cyl_load_species_device: fill species ispecies (replacing its particles)
+ * on the current grid; ids id_base .. id_base + n - 1; n_out = particles
+ * (floor(npart_per_cell * valid cells), as the reference loads).  Immobile
+ * species: CYL_ERR_BAD_ARG.
+ * cyl_set_injection_stream: window injection from the next step on comes
+ * from the host KISS stream (CYL_RNG_KISS, the default, reference order) or
+ * is drawn on the device (CYL_RNG_COUNTER, keyed by seed); the counter mode
+ * handles at most 2 window shifts per step (CYL_ERR_UNSUPPORTED beyond). */
+#define CYL_RNG_KISS 0
+#define CYL_RNG_COUNTER 1
+int cyl_load_species_device(cyl_handle h, int32_t ispecies, uint64_t seed, int64_t id_base, int64_t* n_out);
+int cyl_set_injection_stream(cyl_handle h, int32_t mode, uint64_t seed);
+/* One block of the counter stream: Philox4x32-10 of counter ctr under key
+ * seed (host only; for reproducing the stream outside the library). */
+int cyl_counter_block(uint64_t seed, const uint32_t* ctr4, uint32_t* out4);
 /* Download the live particles of one species, in device order.  n_inout in:
  * capacity of the host arrays; out: particles written. */
 int cyl_download_particles(cyl_handle h, int32_t ispecies, double* x, double* y,

@@ -138,6 +138,48 @@ struct Rng {
   }
 };
 
+// The counter stream of device loading and device window injection, restated
+// from the published algorithm: Philox4x32-10 (Salmon, Moraes, Dror, Shaw,
+// SC'11).  A round multiplies words 0 and 2 by 0xD2511F53 and 0xCD9E8D57,
+// takes the high halves xor the other two words and the round key as the new
+// words 0 and 2, the low halves as the new 3 and 1; the key advances by
+// 0x9E3779B9 / 0xBB67AE85 between rounds.  Counters and tags as the product
+// documents them: (p, p >> 32, species, 1|2) for loading positions/momenta,
+// (row, shift, species, 3) for the injected row's fraction bit,
+// (j, shift, species, 4|5) for injected positions/momenta.
+struct Ctr4 {
+  uint32_t w[4];
+};
+Ctr4 philox10(Ctr4 c, uint64_t seed) {
+  uint32_t key[2] = {(uint32_t)(seed & 0xffffffffu), (uint32_t)(seed >> 32)};
+  for (int round = 0; round < 10; ++round) {
+    const uint64_t m0 = (uint64_t)0xD2511F53u * c.w[0];
+    const uint64_t m1 = (uint64_t)0xCD9E8D57u * c.w[2];
+    Ctr4 n;
+    n.w[0] = (uint32_t)(m1 >> 32) ^ c.w[1] ^ key[0];
+    n.w[1] = (uint32_t)m1;
+    n.w[2] = (uint32_t)(m0 >> 32) ^ c.w[3] ^ key[1];
+    n.w[3] = (uint32_t)m0;
+    c = n;
+    key[0] += 0x9E3779B9u;
+    key[1] += 0xBB67AE85u;
+  }
+  return c;
+}
+inline double ctr_u01(uint32_t r) { return ((double)r + 0.5) * 2.3283064365386963e-10; }
+// three normal deviates: Box-Muller of words (0, 1) -> cos, sin; (2, 3) ->
+// cos; angles in turns through cyl_sincos_turn (shared with the kernels)
+void ctr_normals(const Ctr4& r, double out[3]) {
+  const double rho1 = std::sqrt(-2.0 * std::log(ctr_u01(r.w[0])));
+  double s1, c1, s2, c2;
+  cyl_sincos_turn(ctr_u01(r.w[1]), &s1, &c1);
+  const double rho2 = std::sqrt(-2.0 * std::log(ctr_u01(r.w[2])));
+  cyl_sincos_turn(ctr_u01(r.w[3]), &s2, &c2);
+  out[0] = rho1 * c1;
+  out[1] = rho1 * s1;
+  out[2] = rho2 * c2;
+}
+
 struct Species {
   cyl_species_desc d;
   int bc[4];  // particle bcs after setup_particle_boundary
@@ -186,6 +228,8 @@ struct Sim {
   int bc_after_move[4];
   int64_t n_shifts;
   int64_t next_id;
+  bool inj_counter = false;  // window injection from the counter stream
+  uint64_t inj_seed = 0;
   Field ex, er, et, bx, br, bt, jx, jr, jt, bx_old, br_old, bt_old, jx_old, jr_old, jt_old;
   Col ex_xmin, er_xmin, et_xmin, bx_xmin, br_xmin, bt_xmin;
   Col ex_xmax, er_xmax, et_xmax, bx_xmax, br_xmax, bt_xmax;
@@ -1424,8 +1468,65 @@ double density_at(const cyl_species_desc& d, double x) {
   return d.density;
 }
 
+// insert_particles with the counter stream: the same rows, weights,
+// temperatures and drifts, the random numbers from Philox counters instead
+// of the KISS sequence; immobile species get none.
+void insert_particles_counter(Sim& s) {
+  const int ny = s.ny;
+  const uint32_t shift = (uint32_t)s.n_shifts;
+  for (size_t isp = 0; isp < s.sp.size(); ++isp) {
+    Species& spc = s.sp[isp];
+    const cyl_species_desc& d = spc.d;
+    if (d.immobile) continue;
+    const int64_t nppc = (int64_t)std::floor(d.npart_per_cell);
+    const double npart_frac = d.npart_per_cell - (double)nppc;
+    double dens = density_at(d, s.xg(s.nx));
+    if (dens > d.density_max) dens = d.density_max;
+    if (dens < d.density_min) dens = 0.0;
+    if (dens < d.density_min) continue;
+    const double x0 = s.x_grid_max + 0.5 * s.dx;
+    int64_t j = 0;
+    for (int iy = 1; iy <= ny; ++iy) {
+      int64_t n_frac = 0;
+      if (npart_frac > 0.0 &&
+          ctr_u01(philox10(Ctr4{{(uint32_t)iy, shift, (uint32_t)isp, 3u}}, s.inj_seed).w[0]) < npart_frac)
+        n_frac = 1;
+      for (int64_t ip = 0; ip < nppc + n_frac; ++ip, ++j) {
+        const Ctr4 r = philox10(Ctr4{{(uint32_t)j, shift, (uint32_t)isp, 4u}}, s.inj_seed);
+        const double cell_frac_y = 0.5 - ctr_u01(r.w[0]);
+        const double part_r = s.yg(iy) - cell_frac_y * s.dy;
+        double sn, cs;
+        cyl_sincos_turn(ctr_u01(r.w[1]), &sn, &cs);  // theta = 2 pi U
+        const double px0 = x0 + ctr_u01(r.w[2]) * s.dx;
+        const double wdata = (2.0 * PI * s.dx * s.dy * part_r) / (double)(nppc + n_frac);
+        const double cy2 = cell_frac_y * cell_frac_y;
+        const double gyv[3] = {0.5 * ((0.25 + cy2) + cell_frac_y), 0.75 - cy2,
+                               0.5 * ((0.25 + cy2) - cell_frac_y)};
+        double nrm[3];
+        ctr_normals(philox10(Ctr4{{(uint32_t)j, shift, (uint32_t)isp, 5u}}, s.inj_seed), nrm);
+        double pm[3];
+        for (int i = 0; i < 3; ++i) {
+          double tl = 0.0, dl = 0.0;
+          for (int k = 0; k < 3; ++k) {
+            tl = tl + gyv[k] * d.temp[i];
+            dl = dl + gyv[k] * d.drift[i];
+          }
+          pm[i] = nrm[i] * std::sqrt(tl * KB * d.mass) + dl;
+        }
+        double wl = 0.0;
+        for (int k = 0; k < 3; ++k) wl = wl + gyv[k] * dens;
+        spc.push_back(px0, part_r * cs, part_r * sn, pm[0], pm[1], pm[2], wl * wdata, s.next_id++);
+      }
+    }
+  }
+}
+
 // insert_particles (window.F90:157-300), thermal species
 void insert_particles(Sim& s) {
+  if (s.inj_counter) {
+    insert_particles_counter(s);
+    return;
+  }
   const int ny = s.ny;
   for (auto& spc : s.sp) {
     const cyl_species_desc& d = spc.d;
@@ -1757,6 +1858,90 @@ void load_species(Sim& s, Species& spc) {
   }
 }
 
+// load_particles with the counter stream: the valid cells, counts, extra
+// particles' cell rule, weights and temperatures of load_species, the random
+// numbers from Philox counters (positions (p, species, 1), momenta
+// (p, species, 2)); ids id_base + p.
+void load_species_counter(Sim& s, Species& spc, int isp, uint64_t seed, int64_t id_base) {
+  const cyl_species_desc& d = spc.d;
+  const int nx = s.nx, ny = s.ny;
+  const int W = nx + 2 * NG;
+  auto at = [&](int ix, int iy) { return (size_t)(ix + NG - 1) + (size_t)W * (size_t)(iy + NG - 1); };
+  std::vector<double> density((size_t)W * (ny + 2 * NG));
+  std::vector<char> dmap(density.size(), 0);
+  for (int iy = 1 - NG; iy <= ny + NG; ++iy)
+    for (int ix = 1 - NG; ix <= nx + NG; ++ix) density[at(ix, iy)] = density_at(d, s.xg(ix));
+  if (s.bc_field[CYL_BD_X_MAX] == CYL_BC_PERIODIC)
+    for (int iy = 1 - NG; iy <= ny + NG; ++iy)
+      for (int i = 1; i <= NG; ++i) density[at(nx + i, iy)] = density[at(i, iy)];
+  if (s.bc_field[CYL_BD_X_MIN] == CYL_BC_PERIODIC)
+    for (int iy = 1 - NG; iy <= ny + NG; ++iy)
+      for (int i = 1 - NG; i <= 0; ++i) density[at(i, iy)] = density[at(nx + i, iy)];
+  for (size_t k = 0; k < density.size(); ++k) {
+    if (density[k] > d.density_max) density[k] = d.density_max;
+    if (density[k] >= d.density_min) dmap[k] = 1;
+    else density[k] = 0.0;
+  }
+  std::vector<std::pair<int, int>> valid;
+  for (int iy = 1; iy <= ny; ++iy)
+    for (int ix = 1; ix <= nx; ++ix)
+      if (dmap[at(ix, iy)]) valid.push_back({ix, iy});
+  const int64_t nvalid = (int64_t)valid.size();
+  const int64_t nppc = (int64_t)std::floor(d.npart_per_cell);
+  const int64_t nnew = (int64_t)std::floor(d.npart_per_cell * (double)nvalid);
+  spc.x.clear(); spc.y.clear(); spc.z.clear(); spc.px.clear(); spc.py.clear(); spc.pz.clear();
+  spc.w.clear(); spc.id.clear();
+  for (int64_t p = 0; p < nnew; ++p) {
+    const Ctr4 r = philox10(Ctr4{{(uint32_t)p, (uint32_t)((uint64_t)p >> 32), (uint32_t)isp, 1u}}, seed);
+    const int64_t v = p < nppc * nvalid ? p / nppc : (int64_t)(ctr_u01(r.w[3]) * (double)(nvalid - 1));
+    const int ix = valid[(size_t)v].first, iy = valid[(size_t)v].second;
+    const double px0 = s.xg(ix) + (ctr_u01(r.w[0]) - 0.5) * s.dx;
+    const double pr = s.yg(iy) + (ctr_u01(r.w[1]) - 0.5) * s.dy;
+    double sn, cs;
+    cyl_sincos_turn(ctr_u01(r.w[2]), &sn, &cs);  // theta = 2 pi U
+    spc.push_back(px0, pr * cs, pr * sn, 0, 0, 0, 0, id_base + p);
+  }
+  std::vector<int> npic(density.size(), 0);
+  for (size_t p = 0; p < spc.n(); ++p) {
+    Shape sh = shape_at(s, spc.x[p], spc.y[p], spc.z[p]);
+    npic[at(sh.cell_x, sh.cell_y)]++;
+  }
+  for (size_t p = 0; p < spc.n(); ++p) {
+    Shape sh = shape_at(s, spc.x[p], spc.y[p], spc.z[p]);
+    double wdata = 0.0;
+    for (int isuby = SF_MIN; isuby <= SF_MAX; ++isuby) {
+      int i = sh.cell_x;
+      int j = sh.cell_y + isuby;
+      if (!dmap[at(i, j)]) j = sh.cell_y + isuby / 2;
+      for (int isubx = SF_MIN; isubx <= SF_MAX; ++isubx) {
+        i = sh.cell_x + isubx;
+        if (!dmap[at(i, j)]) i = sh.cell_x + isubx / 2;
+        wdata = wdata + (sh.gx[isubx + 1] * sh.gy[isuby + 1]) * density[at(i, j)];
+      }
+    }
+    const double part_r = std::sqrt(spc.y[p] * spc.y[p] + spc.z[p] * spc.z[p]);
+    const int cx = ffloor((spc.x[p] - s.x_grid_min) / s.dx + 1.5);
+    const int cy = ffloor((part_r - s.y_grid_min) / s.dy + 1.5);
+    const double vol = 2.0 * PI * s.dx * s.dy * part_r;
+    spc.w[p] = wdata * vol / (double)npic[at(cx, cy)];
+    double nrm[3];
+    ctr_normals(philox10(Ctr4{{(uint32_t)p, (uint32_t)((uint64_t)p >> 32), (uint32_t)isp, 2u}}, seed), nrm);
+    for (int dir = 0; dir < 3; ++dir) {
+      double tl = 0.0, dl = 0.0;
+      for (int iy = SF_MIN; iy <= SF_MAX; ++iy)
+        for (int ix = SF_MIN; ix <= SF_MAX; ++ix) {
+          tl = tl + (sh.gx[ix + 1] * sh.gy[iy + 1]) * d.temp[dir];
+          dl = dl + (sh.gx[ix + 1] * sh.gy[iy + 1]) * d.drift[dir];
+        }
+      const double v = nrm[dir] * std::sqrt(tl * KB * d.mass) + dl;
+      if (dir == 0) spc.px[p] = v;
+      else if (dir == 1) spc.py[p] = v;
+      else spc.pz[p] = v;
+    }
+  }
+  if (id_base + (int64_t)spc.n() > s.next_id) s.next_id = id_base + (int64_t)spc.n();
+}
+
 // kinetic energy (calc_df.F90:1246-1291) and per-mode field energy
 void diagnostics(Sim& s, cyl_diag* out) {
   double ke = 0.0;
@@ -1871,6 +2056,27 @@ int orc_load_species(orc_handle h, int32_t isp) {
   Sim* s = (Sim*)h;
   if (isp < 0 || isp >= (int)s->sp.size()) return CYL_ERR_BAD_ARG;
   load_species(*s, s->sp[isp]);
+  return CYL_OK;
+}
+
+int orc_load_species_counter(orc_handle h, int32_t isp, uint64_t seed, int64_t id_base) {
+  Sim* s = (Sim*)h;
+  if (isp < 0 || isp >= (int)s->sp.size() || s->sp[isp].d.immobile) return CYL_ERR_BAD_ARG;
+  load_species_counter(*s, s->sp[isp], isp, seed, id_base);
+  return CYL_OK;
+}
+
+int orc_counter_block(uint64_t seed, const uint32_t* ctr4, uint32_t* out4) {
+  const Ctr4 r = philox10(Ctr4{{ctr4[0], ctr4[1], ctr4[2], ctr4[3]}}, seed);
+  for (int k = 0; k < 4; ++k) out4[k] = r.w[k];
+  return CYL_OK;
+}
+
+int orc_set_injection_stream(orc_handle h, int32_t mode, uint64_t seed) {
+  Sim* s = (Sim*)h;
+  if (mode != CYL_RNG_KISS && mode != CYL_RNG_COUNTER) return CYL_ERR_BAD_ARG;
+  s->inj_counter = mode == CYL_RNG_COUNTER;
+  s->inj_seed = seed;
   return CYL_OK;
 }
 
@@ -2027,6 +2233,7 @@ int orc_number_density(orc_handle h, int32_t isp, double* data) {
 void orc_set_threads(int32_t n) { g_threads = n < 1 ? 1 : n; }
 
 double orc_atan2(double y, double x) { return cyl_atan2(y, x); }
+void orc_sincos_turn(double u, double* s, double* c) { cyl_sincos_turn(u, s, c); }
 
 double orc_dx(orc_handle h) { return ((Sim*)h)->dx; }
 double orc_dy(orc_handle h) { return ((Sim*)h)->dy; }

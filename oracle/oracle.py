@@ -56,6 +56,9 @@ def load():
                                  C.POINTER(abi.LaserDesc), C.c_int32, C.c_int32, C.POINTER(H)]),
         "orc_destroy": (C.c_int, [H]),
         "orc_load_species": (C.c_int, [H, C.c_int32]),
+        "orc_load_species_counter": (C.c_int, [H, C.c_int32, C.c_uint64, C.c_int64]),
+        "orc_set_injection_stream": (C.c_int, [H, C.c_int32, C.c_uint64]),
+        "orc_counter_block": (C.c_int, [C.c_uint64, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
         "orc_set_particles": (C.c_int, [H, C.c_int32, PD, PD, PD, PD, PD, PD, PD, PI64, C.c_int64]),
         "orc_count": (C.c_int64, [H, C.c_int32]),
         "orc_get_particles": (C.c_int, [H, C.c_int32, PD, PD, PD, PD, PD, PD, PD, PI64]),
@@ -72,6 +75,7 @@ def load():
         "orc_charge_density": (C.c_int, [H, PD]),
         "orc_number_density": (C.c_int, [H, C.c_int32, PD]),
         "orc_atan2": (C.c_double, [C.c_double, C.c_double]),
+        "orc_sincos_turn": (None, [C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
         "orc_set_threads": (None, [C.c_int32]),
         "orc_dx": (C.c_double, [H]),
         "orc_dy": (C.c_double, [H]),
@@ -93,7 +97,7 @@ STAGE = {"update_e": 0, "efield_bcs": 1, "update_b": 2, "bfield_bcs_mpi": 3, "pu
 class Oracle:
     """One run of the CPU restatement, fed the same inputs as the GPU run."""
 
-    def __init__(self, deck, particles=None, rng=None, load_species=False):
+    def __init__(self, deck, particles=None, rng=None, load_species=False, counter_seed=None):
         from cylindrical_epoch_gb300 import abi
         self.abi = abi
         self.lib = load()
@@ -109,7 +113,16 @@ class Oracle:
         self.h = h
         self.nxg = deck.nx + 2 * abi.NG
         self.nyg = deck.ny + 2 * abi.NG
-        if load_species:
+        if counter_seed is not None:
+            # the counter stream for loading and window injection (ids
+            # continue across the mobile species, as the host loader's)
+            id_base = 0
+            for i in range(len(deck.species)):
+                if not deck.species[i].immobile:
+                    self.lib.orc_load_species_counter(self.h, i, int(counter_seed), id_base)
+                    id_base += self.lib.orc_count(self.h, i)
+            self.lib.orc_set_injection_stream(self.h, abi.RNG_COUNTER, int(counter_seed))
+        elif load_species:
             for i in range(len(deck.species)):
                 if not deck.species[i].immobile:
                     self.lib.orc_load_species(self.h, i)
