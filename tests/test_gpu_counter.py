@@ -6,9 +6,9 @@ loaded positions and weights bit-exact (the same operations, no FMA
 contraction on either side, angles through the shared cyl_sincos_turn);
 momenta within 1e-13 relative (the device's log against the host libm, a
 few ulp); after steps, positions within 1e-12 and fields within 1e-10
-relative L2 (the other parity tests' bar).  Mixed form: the FP32 particle state
-within 1e-6,
-and the run within the mixed form's 1e-3 bar on Ez against FP64.
+relative L2 (the other parity tests' bar).  Mixed form: the FP32 particle
+state within 1e-6, and the run within the mixed form's 1e-3 bar on Ez
+against FP64.
 """
 import numpy as np
 import pytest
