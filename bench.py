@@ -223,6 +223,17 @@ def run_serve(args):
     with serve.Server(0, args.workers, batched=True, max_batch=args.max_batch) as srv:
         ids = [srv.submit(deck, steps) for deck, steps in decks]
         res_bsat = [srv.wait(i, 3600.0) for i in ids]
+    # the same stream and burst with each job loaded and injected on the
+    # device (counter stream) instead of the host KISS load and upload
+    with serve.Server(0, args.workers) as srv:
+        ids = []
+        for (deck, steps), gap in zip(decks, gaps):
+            ids.append(srv.submit(deck, steps, rng_mode=abi.RNG_COUNTER))
+            time.sleep(float(gap))
+        res_c = [srv.wait(i, 3600.0) for i in ids]
+    with serve.Server(0, args.workers) as srv:
+        ids = [srv.submit(deck, steps, rng_mode=abi.RNG_COUNTER) for deck, steps in decks]
+        res_csat = [srv.wait(i, 3600.0) for i in ids]
     # a scan of small decks (at most one push tile per SM: the ones the
     # batched loop steps together), all submitted at once, through both loops
     small = scan_decks(args.jobs, seed=20261205, nzs=(128, 256), nrs=(32, 64))
@@ -277,6 +288,13 @@ def run_serve(args):
                             "step together (none in this scan: its decks fill the device alone and run "
                             f"on their loader's stream), at most {args.max_batch} open jobs, "
                             f"{args.workers} loader threads"},
+        "device_loading": {"value": serve.latency_stats(res_c)["aggregate"], "unit": "particle-steps/s",
+                           "latency": {k: serve.latency_stats(res_c)[k] for k in ("p50_s", "p99_s", "mean_s",
+                                                                                   "makespan_s")},
+                           "saturated": {k: serve.latency_stats(res_csat)[k]
+                                         for k in ("aggregate", "makespan_s", "p50_s", "p99_s")},
+                           "note": "jobs loaded and window-injected on the device from the counter stream "
+                                   "(cyl_load_species_device) instead of the host KISS load and upload"},
         "small_scan": {"workload": f"{len(small)} wakefield decks as above but nz {{128,256}}, nr {{32,64}} "
                                    "(at most 128 tiles of 16x8 cells), all submitted at once",
                        **{mode: {"value": serve.latency_stats(r)["aggregate"], "unit": "particle-steps/s",
@@ -284,8 +302,8 @@ def run_serve(args):
                                  "p50_s": serve.latency_stats(r)["p50_s"],
                                  "p99_s": serve.latency_stats(r)["p99_s"]}
                           for mode, r in small_res.items()}},
-        "failed_jobs": len(bad) + sum(1 for r in res_sat + res_b + res_bsat + small_res["streams"]
-                                      + small_res["batched"] if r.status != abi.JOB_DONE),
+        "failed_jobs": len(bad) + sum(1 for r in res_sat + res_b + res_bsat + res_c + res_csat
+                                      + small_res["streams"] + small_res["batched"] if r.status != abi.JOB_DONE),
         "failed": [{"job": k, "error": int(r.error), "nx": decks[k][0].nx, "ny": decks[k][0].ny,
                     "n_mode": decks[k][0].n_mode, "ppc": decks[k][0].species[0].npart_per_cell,
                     "steps_done": int(r.steps_done)}

@@ -145,6 +145,7 @@ class JobDesc(C.Structure):
         ("lasers", LaserDesc * 8),
         ("nsteps", C.c_int64),
         ("seed", C.c_int32),
+        ("rng_mode", C.c_int32),
     ]
 
 

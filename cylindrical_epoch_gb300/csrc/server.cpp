@@ -103,6 +103,7 @@ int open_job(cyl_server_s* srv, Job* job, bool tune, cyl_handle* out, int64_t* n
   const cyl_job_desc& d = job->desc;
   cyl_rng_state rng;
   cyl_rng_init(&rng, d.seed);
+  const bool counter = d.rng_mode == CYL_RNG_COUNTER;
   // host load of every mobile species (auto_load order, ids continue across species)
   struct Host {
     std::vector<double> x, y, z, px, py, pz, w;
@@ -110,7 +111,7 @@ int open_job(cyl_server_s* srv, Job* job, bool tune, cyl_handle* out, int64_t* n
   };
   std::vector<Host> hp((size_t)d.nspecies);
   int64_t id_base = 0, n0 = 0;
-  for (int i = 0; i < d.nspecies; ++i) {
+  for (int i = 0; i < d.nspecies && !counter; ++i) {
     if (d.species[i].immobile) continue;
     int64_t n = 0;
     int r = cyl_host_load_species(&d.grid, &d.species[i], &rng, id_base, nullptr, nullptr, nullptr, nullptr,
@@ -135,7 +136,7 @@ int open_job(cyl_server_s* srv, Job* job, bool tune, cyl_handle* out, int64_t* n
   cyl_handle h = nullptr;
   int r = cyl_create(&d.grid, d.species, d.nspecies, las, d.nlasers, &rng, &h);
   if (r != CYL_OK) return r;
-  for (int i = 0; i < d.nspecies && r == CYL_OK; ++i) {
+  for (int i = 0; i < d.nspecies && r == CYL_OK && !counter; ++i) {
     Host& p = hp[(size_t)i];
     const int64_t n = (int64_t)p.x.size();
     if (n == 0) continue;
@@ -143,6 +144,16 @@ int open_job(cyl_server_s* srv, Job* job, bool tune, cyl_handle* out, int64_t* n
                              p.w.data(), p.id.data(), n);
   }
   hp.clear();
+  // counter mode: every mobile species loaded on the device (ids continue
+  // across species as in the host load), window injection on the device
+  for (int i = 0; i < d.nspecies && r == CYL_OK && counter; ++i) {
+    if (d.species[i].immobile) continue;
+    int64_t n = 0;
+    r = cyl_load_species_device(h, i, (uint64_t)(uint32_t)d.seed, id_base, &n);
+    id_base += n;
+    n0 += n;
+  }
+  if (r == CYL_OK && counter) r = cyl_set_injection_stream(h, CYL_RNG_COUNTER, (uint64_t)(uint32_t)d.seed);
   if (r == CYL_OK) r = cyl_initialise(h);
   if (r == CYL_OK && d.grid.precision == CYL_PREC_MIXED && tune) {
     const std::vector<int64_t> key = {srv->device, d.grid.nx, d.grid.ny, d.grid.n_mode,
@@ -413,6 +424,7 @@ int cyl_server_submit(cyl_server s, const cyl_job_desc* job, int64_t* job_id) {
   if (!s || !job || !job_id) return CYL_ERR_BAD_ARG;
   if (job->nspecies < 0 || job->nspecies > 8 || job->nlasers < 0 || job->nlasers > 8 || job->nsteps < 0)
     return CYL_ERR_BAD_ARG;
+  if (job->rng_mode != CYL_RNG_KISS && job->rng_mode != CYL_RNG_COUNTER) return CYL_ERR_BAD_ARG;
   int64_t bytes = 0;
   int r = cyl_estimate_device_bytes(&job->grid, job->species, job->nspecies, &bytes);
   if (r != CYL_OK) return r;

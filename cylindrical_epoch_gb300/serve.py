@@ -13,8 +13,10 @@ from . import abi
 from .lib import load
 
 
-def job_desc(deck, nsteps, seed=None):
-    """cyl_job_desc for a deck; returns (desc, buffers to keep alive until submitted)."""
+def job_desc(deck, nsteps, seed=None, rng_mode=abi.RNG_KISS):
+    """cyl_job_desc for a deck; returns (desc, buffers to keep alive until submitted).
+    rng_mode=abi.RNG_COUNTER loads and injects on the device (counter stream
+    keyed by the seed) instead of the host KISS stream."""
     d = abi.JobDesc()
     d.grid = deck.grid_desc()
     d.nspecies = len(deck.species)
@@ -26,6 +28,7 @@ def job_desc(deck, nsteps, seed=None):
         d.lasers[i] = las[i]
     d.nsteps = int(nsteps)
     d.seed = int(deck.seed if seed is None else seed)
+    d.rng_mode = int(rng_mode)
     return d, (las, keep)
 
 
@@ -57,8 +60,8 @@ class Server:
             abi.check("cyl_server_create", self.lib.cyl_server_create(int(hbm_budget_bytes), int(workers),
                                                                       C.byref(self.h)))
 
-    def submit(self, deck, nsteps, seed=None):
-        d, keep = job_desc(deck, nsteps, seed)
+    def submit(self, deck, nsteps, seed=None, rng_mode=abi.RNG_KISS):
+        d, keep = job_desc(deck, nsteps, seed, rng_mode)
         jid = C.c_int64(0)
         abi.check("cyl_server_submit", self.lib.cyl_server_submit(self.h, C.byref(d), C.byref(jid)))
         return jid.value

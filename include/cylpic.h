@@ -381,6 +381,8 @@ typedef struct cyl_job_desc {
   cyl_laser_desc lasers[8];      /* profile / phase are copied at submit   */
   int64_t nsteps;
   int32_t seed;                  /* KISS seed of the loader (7842432 + rank in the reference) */
+  int32_t rng_mode;              /* CYL_RNG_KISS: host load and injection from the KISS stream;
+                                    CYL_RNG_COUNTER: device load and injection, counter stream keyed by seed */
 } cyl_job_desc;
 
 typedef struct cyl_job_result {

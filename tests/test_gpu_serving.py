@@ -94,3 +94,28 @@ def test_batched_server_matches_runs_alone(gpu_lib):
         assert _rel(b.diag.kinetic_energy, da.kinetic_energy) < tol
         assert _rel(b.diag.field_energy_e, da.field_energy_e) < tol
         assert _rel(b.diag.field_energy_b, da.field_energy_b) < tol
+
+
+def test_counter_jobs_in_server(gpu_lib):
+    """Jobs loaded and injected on the device (rng_mode = counter): the FP64
+    job's result equals the same deck run alone in the counter mode, and
+    every job's result is the same alone and in the mix."""
+    jobs = _jobs()
+    with serve.Server(0, 1) as srv:
+        alone = [srv.wait(srv.submit(d, n, rng_mode=abi.RNG_COUNTER), 300.0) for d, n, _ in jobs]
+    with serve.Server(0, len(jobs)) as srv:
+        ids = [srv.submit(d, n, rng_mode=abi.RNG_COUNTER) for d, n, _ in jobs]
+        mixed = [srv.wait(i, 300.0) for i in ids]
+    for (deck, n, tol), a, b in zip(jobs, alone, mixed):
+        assert a.status == abi.JOB_DONE and b.status == abi.JOB_DONE, (a.error, b.error)
+        assert a.state.n_live[0] == b.state.n_live[0]
+        assert a.state.n_shifts == b.state.n_shifts
+        assert _rel(b.diag.kinetic_energy, a.diag.kinetic_energy) < tol
+        assert _rel(b.diag.field_energy_e, a.diag.field_energy_e) < tol
+    deck, n, tol = jobs[1]
+    run = cg.Run(deck, rng_mode=abi.RNG_COUNTER)
+    run.step(n, graph=True)
+    s, d = run.state(), run.diagnostics()
+    assert s.n_live[0] == alone[1].state.n_live[0]
+    assert _rel(alone[1].diag.kinetic_energy, d.kinetic_energy) < tol
+    assert _rel(alone[1].diag.field_energy_e, d.field_energy_e) < tol
