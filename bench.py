@@ -516,7 +516,11 @@ def e2e_run(deck, parts, rng, steps, graph):
     """The same run through the C ABI with host buffers: the initial state
     is copied from pinned host memory, every 16 steps the diagnostics are
     read back, and the final particles and fields are copied to the host,
-    all inside the timed region."""
+    all inside the timed region.  The steps are enqueued without a sync
+    (cyl_step_async) and each chunk's diagnostics are read one chunk later
+    (cyl_diagnostics_async / _read), so the host's preparation of a chunk
+    overlaps the device's work on the one before; every read's device
+    error word is checked."""
     import numpy as np
     import torch
     import cylindrical_epoch_gb300 as cg
@@ -540,12 +544,23 @@ def e2e_run(deck, parts, rng, steps, graph):
         run.tune_tiles()
     d2h = 0
     left = steps
+    pending = 0
     while left > 0:
         k = min(16, left)
-        run.step(k, graph=graph)
-        run.diagnostics()
-        d2h += C.sizeof(abi.Diag)
+        if graph:
+            run.step_async(k)
+        else:
+            run.step(k, graph=False)
+        if pending:
+            assert run.diagnostics_read().device_error == 0
+            pending -= 1
+        run.diagnostics_async()
+        pending += 1
+        d2h += 8 * 8 + 4
         left -= k
+    while pending:
+        assert run.diagnostics_read().device_error == 0
+        pending -= 1
     outp = [run.particles(i) for i in range(len(deck.species))]
     fields = [run.field(n) for n in ("exm", "erm", "etm", "bxm", "brm", "btm")]
     torch.cuda.synchronize()

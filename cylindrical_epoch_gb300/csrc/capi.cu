@@ -81,6 +81,14 @@ struct Handle {
   int inj_counter = 0;
   uint64_t inj_seed = 0;
   InjSpecies* d_injsp = nullptr;
+  // diagnostics read without a stream sync: a ring of two pinned slots, each
+  // the 8 reductions plus the device error word, with an event
+  struct DiagSlot {
+    double* h = nullptr;  // pinned: 8 doubles, then the error word
+    cudaEvent_t ev = nullptr;
+    bool pending = false;
+  } diag_slot[2];
+  int diag_head = 0, diag_count = 0;  // oldest pending slot, slots pending
   // host bookkeeping (module globals)
   double time = 0.0;
   int64_t step = 0;
@@ -1089,6 +1097,10 @@ int cyl_destroy(cyl_handle hh) {
   if (h->st) cudaStreamSynchronize(h->st);
   if (h->gexec) cudaGraphExecDestroy(h->gexec);
   cudaFree(h->d_injsp);
+  for (auto& d : h->diag_slot) {
+    if (d.h) cudaFreeHost(d.h);
+    if (d.ev) cudaEventDestroy(d.ev);
+  }
   for (int i = 0; i < h->nsp; ++i)
     if (h->sp[i].x) cudaFree(h->sp[i].x);
   cudaFree(h->fbuf);
@@ -1429,7 +1441,7 @@ int cyl_initialise(cyl_handle hh) {
   return sync_and_check(h);
 }
 
-static int step_impl(cyl_handle hh, int32_t nsteps, bool graph) {
+static int step_impl(cyl_handle hh, int32_t nsteps, bool graph, bool sync = true) {
   if (!hh || nsteps < 0) return CYL_ERR_BAD_ARG;
   Handle* h = &hh->h;
   while (nsteps > 0) {
@@ -1438,11 +1450,20 @@ static int step_impl(cyl_handle hh, int32_t nsteps, bool graph) {
     if (r != CYL_OK) return r;
     nsteps -= k;
   }
+  if (!sync) {
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      h->last_cuda_error = e;
+      return CYL_ERR_CUDA;
+    }
+    return CYL_OK;
+  }
   return sync_and_check(h);
 }
 
 int cyl_step(cyl_handle hh, int32_t nsteps) { return step_impl(hh, nsteps, false); }
 int cyl_step_graph(cyl_handle hh, int32_t nsteps) { return step_impl(hh, nsteps, true); }
+int cyl_step_async(cyl_handle hh, int32_t nsteps) { return step_impl(hh, nsteps, true, false); }
 
 int cyl_push_only(cyl_handle hh) {
   if (!hh) return CYL_ERR_BAD_ARG;
@@ -1508,27 +1529,69 @@ int cyl_get_run_state(cyl_handle hh, cyl_run_state* out) {
   return CYL_OK;
 }
 
-int cyl_diagnostics(cyl_handle hh, cyl_diag* out) {
-  if (!hh || !out) return CYL_ERR_BAD_ARG;
-  Handle* h = &hh->h;
-  CK(cudaMemsetAsync(h->d_red, 0, 8 * sizeof(double), h->st));
+// The diagnostic reductions of the current state into d_red (8 doubles).
+static void enqueue_diag_reductions(Handle* h) {
+  cudaMemsetAsync(h->d_red, 0, 8 * sizeof(double), h->st);
   for (int i = 0; i < h->nsp; ++i) {
     if (h->prec == CYL_PREC_MIXED) mixed_energy(h->st, h->sp[i], h->d_cnt + i, h->d_red, h->nblocks);
     else launch_energy(h->st, h->sp[i], h->d_cnt + i, h->d_red, h->nblocks);
   }
   if (h->prec == CYL_PREC_MIXED) launch_field_energy(h->st, fieldset_f(h, h->jpar), h->rc, h->d_red + 2);
   else launch_field_energy(h->st, fieldset(h, h->jpar), h->rc, h->d_red + 2);
-  double red[8];
-  CK(cudaMemcpyAsync(red, h->d_red, sizeof(red), cudaMemcpyDeviceToHost, h->st));
-  CK(cudaStreamSynchronize(h->st));
-  int err = 0;
-  CK(cudaMemcpy(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+}
+
+static void fill_diag(const double* red, int err, cyl_diag* out) {
   out->kinetic_energy = red[0];
   out->n_live = (int64_t)(red[1] + 0.5);
   out->field_energy_e = 0.5 * EPS0 * red[2];
   out->field_energy_b = 0.5 / (4.0e-7 * PI) * red[3];
   out->jsum_abs = red[4];
   out->device_error = err;
+}
+
+int cyl_diagnostics(cyl_handle hh, cyl_diag* out) {
+  if (!hh || !out) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  enqueue_diag_reductions(h);
+  double red[8];
+  CK(cudaMemcpyAsync(red, h->d_red, sizeof(red), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  int err = 0;
+  CK(cudaMemcpy(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  fill_diag(red, err, out);
+  return CYL_OK;
+}
+
+int cyl_diagnostics_async(cyl_handle hh) {
+  if (!hh) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  if (h->diag_count >= 2) return CYL_ERR_BAD_ARG;  // read one first
+  Handle::DiagSlot& d = h->diag_slot[(h->diag_head + h->diag_count) % 2];
+  if (!d.h) {
+    CK(cudaMallocHost(&d.h, 9 * sizeof(double)));
+    CK(cudaEventCreateWithFlags(&d.ev, cudaEventDisableTiming));
+  }
+  enqueue_diag_reductions(h);
+  CK(cudaMemcpyAsync(d.h, h->d_red, 8 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(d.h + 8, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaEventRecord(d.ev, h->st));
+  d.pending = true;
+  h->diag_count++;
+  return CYL_OK;
+}
+
+int cyl_diagnostics_read(cyl_handle hh, cyl_diag* out) {
+  if (!hh || !out) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  if (h->diag_count == 0) return CYL_ERR_BAD_ARG;
+  Handle::DiagSlot& d = h->diag_slot[h->diag_head];
+  CK(cudaEventSynchronize(d.ev));
+  int err = 0;
+  std::memcpy(&err, d.h + 8, sizeof(int));
+  fill_diag(d.h, err, out);
+  d.pending = false;
+  h->diag_head = (h->diag_head + 1) % 2;
+  h->diag_count--;
   return CYL_OK;
 }
 

@@ -38,6 +38,9 @@ SIGNATURES = {
     "cyl_initialise": (C.c_int, [H]),
     "cyl_step": (C.c_int, [H, I32]),
     "cyl_step_graph": (C.c_int, [H, I32]),
+    "cyl_step_async": (C.c_int, [H, I32]),
+    "cyl_diagnostics_async": (C.c_int, [H]),
+    "cyl_diagnostics_read": (C.c_int, [H, P(abi.Diag)]),
     "cyl_get_run_state": (C.c_int, [H, P(abi.RunState)]),
     "cyl_diagnostics": (C.c_int, [H, P(abi.Diag)]),
     "cyl_get_rng_state": (C.c_int, [H, P(abi.RngState)]),

@@ -224,6 +224,20 @@ class Run:
         fn = self.lib.cyl_step_graph if graph else self.lib.cyl_step
         abi.check("cyl_step", fn(self.h, n))
 
+    def step_async(self, n=1):
+        """Enqueue n steps (graphs) and return without waiting (cyl_step_async)."""
+        abi.check("cyl_step_async", self.lib.cyl_step_async(self.h, n))
+
+    def diagnostics_async(self):
+        """Enqueue a diagnostics read of the state after the enqueued steps."""
+        abi.check("cyl_diagnostics_async", self.lib.cyl_diagnostics_async(self.h))
+
+    def diagnostics_read(self):
+        """Wait for the oldest enqueued diagnostics read and return it."""
+        d = abi.Diag()
+        abi.check("cyl_diagnostics_read", self.lib.cyl_diagnostics_read(self.h, C.byref(d)))
+        return d
+
     def stream(self):
         """The handle's CUDA stream (cudaStream_t as an int)."""
         st = C.c_void_p()

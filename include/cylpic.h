@@ -239,9 +239,21 @@ int cyl_step(cyl_handle h, int32_t nsteps);
 /* Same as cyl_step but the steps are captured once into a CUDA graph and
  * replayed (one graph launch per call after the first). */
 int cyl_step_graph(cyl_handle h, int32_t nsteps);
+/* As cyl_step_graph without the final stream sync: the call returns once
+ * the steps are enqueued (the host work of a chunk overlaps the device work
+ * of the one before, also across calls).  A device error flag raised by
+ * these steps is reported by the next call that syncs (cyl_diagnostics,
+ * cyl_diagnostics_read's device_error, cyl_get_run_state, downloads). */
+int cyl_step_async(cyl_handle h, int32_t nsteps);
 
 int cyl_get_run_state(cyl_handle h, cyl_run_state* out);
 int cyl_diagnostics(cyl_handle h, cyl_diag* out);
+/* Diagnostics without a stream sync: cyl_diagnostics_async enqueues the
+ * reductions of the state after the steps enqueued so far, with their copy
+ * to pinned host memory (at most two pending, else CYL_ERR_BAD_ARG);
+ * cyl_diagnostics_read waits for the oldest pending one and returns it. */
+int cyl_diagnostics_async(cyl_handle h);
+int cyl_diagnostics_read(cyl_handle h, cyl_diag* out);
 int cyl_get_rng_state(cyl_handle h, cyl_rng_state* out);
 
 /* The first particle that raised the device error word in the mixed form:

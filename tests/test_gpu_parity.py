@@ -239,3 +239,36 @@ def test_current_smoothing_parity(gpu_lib):
     assert gpu.state().n_live[0] == orc.state().n_live[0]
     assert orc.state().n_shifts > 0
     _cmp_fields(gpu, orc, ["exm", "erm", "btm", "jxm", "jrm", "jtm"])
+
+
+@pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_MIXED])
+def test_async_steps_and_pipelined_diagnostics(gpu_lib, precision):
+    """cyl_step_async with each chunk's diagnostics read one chunk later
+    (cyl_diagnostics_async / _read) gives, chunk by chunk, the diagnostics of
+    synchronous steps and reads, and the same final state.  Energies within
+    1e-10 relative in the FP64 form (the order of the FP64 atomic adds) and
+    1e-6 in the mixed form, where that order also flips FP32 roundings of
+    the stored fields (two identical mixed runs differ by about 1e-9)."""
+    tol = 1e-10 if precision == abi.PREC_FP64 else 1e-6
+    deck = cg.wakefield(nx=128, ny=32, ppc=4, density=3.0e24, ramp=2.0e-6, precision=precision)
+    deck.window_start_time = 20 * 5.0e-17
+    parts, rng = cg.host_load(deck)
+    a = cg.Run(deck, particles=parts, rng=rng)
+    b = cg.Run(deck, particles=parts, rng=rng)
+    da, db = [], []
+    for _ in range(5):
+        a.step(16, graph=True)
+        da.append(a.diagnostics())
+    for i in range(5):
+        b.step_async(16)
+        if i:
+            db.append(b.diagnostics_read())
+        b.diagnostics_async()
+    db.append(b.diagnostics_read())
+    with pytest.raises(abi.CylError):
+        b.diagnostics_read()  # nothing pending
+    for x, y in zip(da, db):
+        assert y.device_error == 0 and x.n_live == y.n_live
+        for k in ("kinetic_energy", "field_energy_e", "field_energy_b"):
+            assert abs(getattr(y, k) - getattr(x, k)) <= tol * abs(getattr(x, k)), k
+    assert a.state().n_shifts == b.state().n_shifts > 10
