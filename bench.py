@@ -497,7 +497,8 @@ def main():
         if e2e:
             line["e2e"] = {"value": e2e["value"], "unit": "particle-steps/s",
                            "h2d_bytes_per_step": e2e["h2d"] / args.steps,
-                           "d2h_bytes_per_step": e2e["d2h"] / args.steps}
+                           "d2h_bytes_per_step": e2e["d2h"] / args.steps,
+                           "phases_s": e2e["phases_s"]}
         if base:
             line["cpu_baseline"] = base
         if fp64:
@@ -537,11 +538,24 @@ def e2e_run(deck, parts, rng, steps, graph):
             setattr(q, k, a)
         pinned.append(q)
     h2d = sum(sum(getattr(p, k).nbytes for k in p.__slots__) for p in pinned)
+    # pinned destinations of the final download, sized for the capacity
+    caps = [int(sd.capacity) for sd in deck.species_descs()]
+    outs = []
+    for cap in caps:
+        q = cg.Particles(0)
+        for k in q.__slots__:
+            t = torch.empty(max(cap, 1), dtype=torch.int64 if k == "id" else torch.float64, pin_memory=True)
+            setattr(q, k, t.numpy())
+        outs.append(q)
+    shape = (deck.n_mode, deck.ny + 2 * abi.NG, deck.nx + 2 * abi.NG)
+    fouts = [torch.empty(shape, dtype=torch.complex128, pin_memory=True).numpy() for _ in range(6)]
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     run = cg.Run(deck, particles=pinned, rng=rng)
+    t_up = time.perf_counter()
     if deck.precision == abi.PREC_MIXED:
         run.tune_tiles()
+    t_tune = time.perf_counter()
     d2h = 0
     left = steps
     pending = 0
@@ -561,8 +575,9 @@ def e2e_run(deck, parts, rng, steps, graph):
     while pending:
         assert run.diagnostics_read().device_error == 0
         pending -= 1
-    outp = [run.particles(i) for i in range(len(deck.species))]
-    fields = [run.field(n) for n in ("exm", "erm", "etm", "bxm", "brm", "btm")]
+    t_steps = time.perf_counter()
+    outp = [run.particles(i, out=outs[i]) for i in range(len(deck.species))]
+    fields = [run.field(n, out=fouts[j]) for j, n in enumerate(("exm", "erm", "etm", "bxm", "brm", "btm"))]
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     s = run.state()
@@ -575,7 +590,9 @@ def e2e_run(deck, parts, rng, steps, graph):
     # are copied inside cyl_step; count their bytes
     h2d += steps * (512 + 4 * 8 * (deck.ny + 1))
     return {"seconds": t1 - t0, "psteps": 0.5 * (n0 + n1) * steps, "value": 0.5 * (n0 + n1) * steps / (t1 - t0),
-            "h2d": h2d, "d2h": d2h}
+            "h2d": h2d, "d2h": d2h,
+            "phases_s": {"create_and_upload": t_up - t0, "tune_tiles": t_tune - t_up, "steps": t_steps - t_tune,
+                         "download": t1 - t_steps}}
 
 
 if __name__ == "__main__":

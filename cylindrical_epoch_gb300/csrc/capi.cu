@@ -1319,29 +1319,53 @@ int cyl_download_particles(cyl_handle hh, int32_t isp, double* x, double* y, dou
   SpeciesCounters c;
   CK(cudaMemcpy(&c, h->d_cnt + isp, sizeof(c), cudaMemcpyDeviceToHost));
   const int64_t n = c.n_used;
-  std::vector<double> buf((size_t)n * 8);
   SpeciesPtrs& p = h->sp[isp];
+  // the count alone: live = slots in use - removed holes (the counters the
+  // push, the window and the sort keep)
+  if (!x) {
+    *n_inout = n - c.n_dead;
+    return CYL_OK;
+  }
+  if (!y || !z || !px || !py || !pz || !w || !id) return CYL_ERR_BAD_ARG;
+  if (c.n_dead == 0) {
+    // no holes (as after every chunk's sort): straight into the caller's arrays
+    if (*n_inout < n) return CYL_ERR_CAPACITY;
+    double* dst[7] = {x, y, z, px, py, pz, w};
+    const size_t b = (size_t)n * 8;
+    if (h->prec == CYL_PREC_MIXED) {
+      double* st = h->sc.tmp;
+      const int64_t cap = h->sc.cap;
+      mixed_to_double(h->st, p, st, n, cap, h->xg0, h->rc);
+      for (int k = 0; k < 7 && n > 0; ++k)
+        CK(cudaMemcpyAsync(dst[k], st + (size_t)k * cap, b, cudaMemcpyDeviceToHost, h->st));
+      if (n > 0) CK(cudaMemcpyAsync(id, st + (size_t)7 * cap, b, cudaMemcpyDeviceToHost, h->st));
+    } else {
+      const double* srcs[7] = {p.x, p.y, p.z, p.px, p.py, p.pz, p.w};
+      for (int k = 0; k < 7 && n > 0; ++k) CK(cudaMemcpyAsync(dst[k], srcs[k], b, cudaMemcpyDeviceToHost, h->st));
+      if (n > 0) CK(cudaMemcpyAsync(id, p.id, b, cudaMemcpyDeviceToHost, h->st));
+    }
+    CK(cudaStreamSynchronize(h->st));
+    *n_inout = n;
+    return CYL_OK;
+  }
+  std::unique_ptr<double[]> buf(new double[(size_t)n * 8]);
   if (h->prec == CYL_PREC_MIXED) {
     double* st = h->sc.tmp;
     const int64_t cap = h->sc.cap;
     mixed_to_double(h->st, p, st, n, cap, h->xg0, h->rc);
     for (int k = 0; k < 8; ++k)
-      CK(cudaMemcpyAsync(buf.data() + (size_t)k * n, st + (size_t)k * cap, (size_t)n * 8, cudaMemcpyDeviceToHost,
+      CK(cudaMemcpyAsync(buf.get() + (size_t)k * n, st + (size_t)k * cap, (size_t)n * 8, cudaMemcpyDeviceToHost,
                          h->st));
     CK(cudaStreamSynchronize(h->st));
   } else {
     double* srcs[7] = {p.x, p.y, p.z, p.px, p.py, p.pz, p.w};
     for (int k = 0; k < 7; ++k)
-      CK(cudaMemcpy(buf.data() + (size_t)k * n, srcs[k], (size_t)n * 8, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(buf.data() + (size_t)7 * n, p.id, (size_t)n * 8, cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(buf.get() + (size_t)k * n, srcs[k], (size_t)n * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(buf.get() + (size_t)7 * n, p.id, (size_t)n * 8, cudaMemcpyDeviceToHost));
   }
   int64_t live = 0;
   for (int64_t i = 0; i < n; ++i)
     if (!std::isnan(buf[i])) live++;
-  if (!x) {
-    *n_inout = live;
-    return CYL_OK;
-  }
   if (*n_inout < live) return CYL_ERR_CAPACITY;
   int64_t k = 0;
   for (int64_t i = 0; i < n; ++i) {

@@ -194,4 +194,28 @@ constexpr int ERR_CELL_RANGE = 2;    // particle stencil left the ghosted grid
 constexpr int ERR_NONFINITE = 4;
 constexpr int ERR_TMA_TIMEOUT = 8;  // a TMA tile copy did not complete within its bounded wait
 
+#ifdef __CUDACC__
+// Sum K per-thread values over a 1-D block (warp shuffles, then the warps'
+// partial sums through shared memory) and add the block's totals to
+// out[0..K) with one atomic each.  Every thread of the block must call it.
+template <int K>
+__device__ __forceinline__ void block_sum_add(double (&v)[K], double* out) {
+  __shared__ double part[32][K];
+  for (int k = 0; k < K; ++k)
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0)
+    for (int k = 0; k < K; ++k) part[wid][k] = v[k];
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    for (int k = 0; k < K; ++k) {
+      double t = lane < nw ? part[lane][k] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+      if (lane == 0) atomicAdd(&out[k], t);
+    }
+  }
+}
+#endif
+
 }  // namespace cyl

@@ -218,14 +218,8 @@ __global__ void k_mixed_energy(SpeciesPtrs sp, const SpeciesCounters* cnt, doubl
     e += (double)sp.fw[i] * mc2 * (u2 / (sqrt(u2 + 1.0) + 1.0));
     c += 1.0;
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    e += __shfl_down_sync(0xffffffffu, e, o);
-    c += __shfl_down_sync(0xffffffffu, c, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    atomicAdd(&out[0], e);
-    atomicAdd(&out[1], c);
-  }
+  double v[2] = {e, c};
+  block_sum_add<2>(v, out);
 }
 void mixed_energy(cudaStream_t s, const SpeciesPtrs& sp, const SpeciesCounters* cnt, double* out, int nblocks) {
   k_mixed_energy<<<nblocks, 256, 0, s>>>(sp, cnt, out);

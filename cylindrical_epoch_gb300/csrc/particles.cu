@@ -190,14 +190,8 @@ __global__ void k_energy(SpeciesPtrs sp, const SpeciesCounters* cnt, double* out
     e += sp.w[i] * mc2 * (u2 / (sqrt(u2 + 1.0) + 1.0));
     c += 1.0;
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    e += __shfl_down_sync(0xffffffffu, e, o);
-    c += __shfl_down_sync(0xffffffffu, c, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    atomicAdd(&out[0], e);
-    atomicAdd(&out[1], c);
-  }
+  double v[2] = {e, c};
+  block_sum_add<2>(v, out);
 }
 
 void launch_energy(cudaStream_t s, const SpeciesPtrs& sp, const SpeciesCounters* cnt, double* out,
@@ -207,36 +201,32 @@ void launch_energy(cudaStream_t s, const SpeciesPtrs& sp, const SpeciesCounters*
 
 // Per-mode field energy over the interior: m = 0 contributes |F_0|^2, m >= 1
 // contributes |F_m|^2 / 2 (F = Re sum F_m e^{-im theta}), cell volume 2 pi r dx dr.
+// Blocks stride over the interior cells of mode blockIdx.y; one atomic per
+// block and sum.
 template <typename T>
 __global__ void k_field_energy(FieldSetT<T> F, RunConst rc, double* out) {
-  const int ix = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-  const int iy = 1 + blockIdx.y;
-  const int m = blockIdx.z;
-  double fe = 0.0, fb = 0.0, js = 0.0;
-  if (ix <= rc.nx) {
-    const double mf = (m == 0) ? 1.0 : 0.5;
+  const int m = blockIdx.y;
+  const int ncell = rc.nx * rc.ny;
+  const double mf = (m == 0) ? 1.0 : 0.5;
+  auto a2 = [](cplx v) { return v.re * v.re + v.im * v.im; };
+  double v[3] = {0.0, 0.0, 0.0};
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += gridDim.x * blockDim.x) {
+    const int iy = 1 + c / rc.nx, ix = 1 + (c - (iy - 1) * rc.nx);
     const double r = (double)iy * rc.dy;
     const double vol = 2.0 * PI * r * rc.dx * rc.dy;
-    auto a2 = [](cplx v) { return v.re * v.re + v.im * v.im; };
-    fe = mf * vol * (a2(F.ex(ix, iy, m)) + a2(F.er(ix, iy, m)) + a2(F.et(ix, iy, m)));
-    fb = mf * vol * (a2(F.bx(ix, iy, m)) + a2(F.br(ix, iy, m)) + a2(F.bt(ix, iy, m)));
-    js = sqrt(a2(F.jx(ix, iy, m))) + sqrt(a2(F.jr(ix, iy, m))) + sqrt(a2(F.jt(ix, iy, m)));
+    v[0] += mf * vol * (a2(F.ex(ix, iy, m)) + a2(F.er(ix, iy, m)) + a2(F.et(ix, iy, m)));
+    v[1] += mf * vol * (a2(F.bx(ix, iy, m)) + a2(F.br(ix, iy, m)) + a2(F.bt(ix, iy, m)));
+    v[2] += sqrt(a2(F.jx(ix, iy, m))) + sqrt(a2(F.jr(ix, iy, m))) + sqrt(a2(F.jt(ix, iy, m)));
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    fe += __shfl_down_sync(0xffffffffu, fe, o);
-    fb += __shfl_down_sync(0xffffffffu, fb, o);
-    js += __shfl_down_sync(0xffffffffu, js, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    atomicAdd(&out[0], fe);
-    atomicAdd(&out[1], fb);
-    atomicAdd(&out[2], js);
-  }
+  block_sum_add<3>(v, out);
 }
 
 template <typename T>
 void launch_field_energy(cudaStream_t s, const FieldSetT<T>& F, const RunConst& rc, double* out) {
-  dim3 blk(128), grd((rc.nx + 127) / 128, rc.ny, rc.M);
+  const int ncell = rc.nx * rc.ny;
+  int bx = (ncell + 255) / 256;
+  if (bx > 152 * 4) bx = 152 * 4;
+  dim3 blk(256), grd(bx, rc.M);
   k_field_energy<T><<<grd, blk, 0, s>>>(F, rc, out);
 }
 template void launch_field_energy<cplx>(cudaStream_t, const FieldSet&, const RunConst&, double*);

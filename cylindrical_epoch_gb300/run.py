@@ -180,11 +180,26 @@ class Run:
                   self.lib.cyl_upload_particles(self.h, isp, _p(p.x), _p(p.y), _p(p.z), _p(p.px),
                                                 _p(p.py), _p(p.pz), _p(p.w), _p(p.id, PI64), p.n))
 
-    def particles(self, isp=0):
+    def particles(self, isp=0, out=None):
+        """The live particles of species isp (device order).  out: a
+        Particles whose arrays (e.g. pinned) receive them, of at least the
+        live count; the result then views its first n entries."""
         n = C.c_int64(0)
         abi.check("cyl_download_particles",
                   self.lib.cyl_download_particles(self.h, isp, None, None, None, None, None, None,
                                                   None, None, C.byref(n)))
+        if out is not None:
+            if out.n < n.value:
+                raise ValueError(f"out holds {out.n} particles, {n.value} are live")
+            n = C.c_int64(out.n)
+            abi.check("cyl_download_particles",
+                      self.lib.cyl_download_particles(self.h, isp, _p(out.x), _p(out.y), _p(out.z), _p(out.px),
+                                                      _p(out.py), _p(out.pz), _p(out.w), _p(out.id, PI64),
+                                                      C.byref(n)))
+            v = Particles(0)
+            for k in v.__slots__:
+                setattr(v, k, getattr(out, k)[:n.value])
+            return v
         p = Particles(n.value)
         abi.check("cyl_download_particles",
                   self.lib.cyl_download_particles(self.h, isp, _p(p.x), _p(p.y), _p(p.z), _p(p.px),
@@ -192,11 +207,18 @@ class Run:
                                                   C.byref(n)))
         return p.resize(n.value)
 
-    def field(self, name):
+    def field(self, name, out=None):
         """Complex mode array F(1-ng:nx+ng, 1-ng:ny+ng, 0:M-1) as numpy
-        complex128 with shape (M, ny+2ng, nx+2ng) (Fortran order reversed)."""
+        complex128 with shape (M, ny+2ng, nx+2ng) (Fortran order reversed);
+        into `out` (a contiguous complex128 array of that shape) if given."""
         which = abi.FIELD_INDEX[name] if isinstance(name, str) else name
-        a = np.zeros((self.deck.n_mode, self.nyg, self.nxg), dtype=np.complex128)
+        shape = (self.deck.n_mode, self.nyg, self.nxg)
+        if out is not None:
+            if out.shape != shape or out.dtype != np.complex128 or not out.flags.c_contiguous:
+                raise ValueError("out must be a contiguous complex128 array of shape %s" % (shape,))
+            a = out
+        else:
+            a = np.zeros(shape, dtype=np.complex128)
         abi.check("cyl_download_field", self.lib.cyl_download_field(self.h, which, _p(a.view(np.float64))))
         return a
 

@@ -215,7 +215,11 @@ int cyl_set_injection_stream(cyl_handle h, int32_t mode, uint64_t seed);
  * seed (host only; for reproducing the stream outside the library). */
 int cyl_counter_block(uint64_t seed, const uint32_t* ctr4, uint32_t* out4);
 /* Download the live particles of one species, in device order.  n_inout in:
- * capacity of the host arrays; out: particles written. */
+ * capacity of the host arrays; out: particles written.  With x == NULL only
+ * the live count is returned (from the device counters, no copy).  Right
+ * after a sort (every 16-step chunk ends with one) the slots hold no holes
+ * and the copy goes straight into the caller's arrays (pinned arrays give
+ * the full copy bandwidth). */
 int cyl_download_particles(cyl_handle h, int32_t ispecies, double* x, double* y,
                            double* z, double* px, double* py, double* pz,
                            double* w, int64_t* id, int64_t* n_inout);
