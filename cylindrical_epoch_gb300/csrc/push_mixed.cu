@@ -56,9 +56,16 @@ constexpr int TW = RW + 1;
 static_assert((TW * 8) % 16 == 0, "TMA box rows must be whole 16-byte units");
 constexpr int TPLANE = ((TW * RH * 8 + 127) / 128) * 128 / 8;  // float2 per TMA plane
 constexpr int PUSH_THREADS = 256;
-#ifndef PUSH_MIN_BLOCKS
-#define PUSH_MIN_BLOCKS 3  // resident CTAs per SM the register budget is sized for
-#endif
+// Resident CTAs per SM the register budget is sized for: 3 (at most 80
+// registers a thread, 24 warps an SM) for m = 0..1, 2 (at most 128) for
+// three or more modes, whose per-mode gather and deposit state spills at
+// 80 registers.  Measured on the 2048x256 / 4096x512 wakefields: M = 2
+// 0.433 ms with 3 against 0.510 with 2; M = 3 0.797 against 0.742; M = 4
+// 15.8 ms against 14.5.
+template <int M>
+constexpr int push_min_blocks() {
+  return M >= 3 ? 2 : 3;
+}
 
 struct f2 {
   float re, im;
@@ -848,7 +855,7 @@ __device__ __forceinline__ bool process_tile(const FieldSetF& F, const SpeciesPt
 }
 
 template <int M>
-__global__ void __launch_bounds__(PUSH_THREADS, PUSH_MIN_BLOCKS) k_push_tiles(
+__global__ void __launch_bounds__(PUSH_THREADS, push_min_blocks<M>()) k_push_tiles(
     FieldSetF F, SpeciesPtrs sp, SpeciesCounters* cnt, const StepRec* rec, RunConst rc, MixedParams P, TileTable* tt,
     int apply_bcs, const __grid_constant__ TmaSet tma, int use_tma) {
   extern __shared__ float4 smem4[];
@@ -880,7 +887,7 @@ __global__ void __launch_bounds__(PUSH_THREADS, PUSH_MIN_BLOCKS) k_push_tiles(
 // table (one entry per run and step of the chunk).  Fields are staged by
 // plain loads.
 template <int M>
-__global__ void __launch_bounds__(PUSH_THREADS, PUSH_MIN_BLOCKS) k_push_tiles_batch(const BatchJob* jobs,
+__global__ void __launch_bounds__(PUSH_THREADS, push_min_blocks<M>()) k_push_tiles_batch(const BatchJob* jobs,
                                                                                    const int2* work,
                                                                                    const int* nwork) {
   extern __shared__ float4 smem4[];
