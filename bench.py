@@ -37,16 +37,20 @@ def _peaks():
         return 6800.0, "fallback"
 
 
-def _profile_traffic(form):
-    """DRAM bytes per push launch from the committed ncu summary, scaled to
-    the benchmark workload (profiles/push_<form>_traffic.json)."""
+def _profile_traffic(form, n_mode, ppc):
+    """DRAM bytes per particle of the push from the committed ncu summary of
+    a workload with the same modes and particles per cell
+    (profiles/push_<form>_traffic.json), or None when none was captured."""
     p = os.path.join(ROOT, "profiles", f"push_{form}_traffic.json")
     try:
         with open(p) as f:
             d = json.load(f)
-        return d
     except Exception:
         return None
+    for e in d.get("entries", [d]):
+        if e.get("n_mode") == n_mode and float(e.get("ppc", -1)) == float(ppc):
+            return e
+    return None
 
 
 class ClockSampler:
@@ -129,12 +133,14 @@ def cpu_baseline(deck, parts, rng, seconds=12.0, threads=None):
                                       f"{dt:.1f} s, {nt} OpenMP threads"}
 
 
-def build_deck(name, form):
+def build_deck(name, form, modes=None):
+    """The named deck; `modes` overrides the wakefield deck's mode count
+    (a profiling case of the same grid at m = 0..modes-1)."""
     import cylindrical_epoch_gb300 as cg
     from cylindrical_epoch_gb300 import abi
     prec = abi.PREC_MIXED if form == "mixed" else abi.PREC_FP64
     if name == "wakefield":
-        return cg.wakefield(precision=prec)
+        return cg.wakefield(precision=prec) if modes is None else cg.wakefield(n_mode=modes, precision=prec)
     if name == "thermal":
         return cg.thermal_plasma(precision=prec)
     if name == "large":
@@ -147,7 +153,7 @@ def run_reference(args, rank):
         return 0
     import cylindrical_epoch_gb300 as cg
     form = "fp64"
-    deck = build_deck(args.deck, form)
+    deck = build_deck(args.deck, form, args.modes)
     parts, rng = cg.host_load(deck)
     base = cpu_baseline(deck, parts, rng, seconds=min(60.0, 5.0 + 0.02 * args.steps))
     line = {
@@ -335,6 +341,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--form", default="auto", choices=["auto", "fp64", "mixed"])
     ap.add_argument("--deck", default="wakefield", choices=["wakefield", "thermal", "large"])
+    ap.add_argument("--modes", type=int, default=None, help="wakefield deck with m = 0..modes-1 (profiling)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--eager", action="store_true", help="no CUDA graphs")
@@ -382,7 +389,7 @@ def main():
         if rc == abi.CYL_OK:
             lib.cyl_destroy(h)
             form = "mixed"
-    deck = build_deck(args.deck, form)
+    deck = build_deck(args.deck, form, args.modes)
     parts, rng = cg.host_load(deck)
     run = cg.Run(deck, particles=parts, rng=rng)
     graph = not args.eager
@@ -436,7 +443,7 @@ def main():
     nparts = 0.5 * (n_start + n_end)
     peak, peak_kind = _peaks()
     achieved = per_particle * nparts / (push_ms * 1e-3) / 1e9 if push_ms > 0 else None
-    prof = _profile_traffic(form)
+    prof = _profile_traffic(form, M, ppc)
     traffic = None
     if prof and prof.get("bytes_per_particle"):
         traffic = prof["bytes_per_particle"] * nparts
@@ -451,7 +458,7 @@ def main():
         # the plain FP64 form on the same deck, seed and steps; with the whole
         # K steps (the default) its final state is compared with the mixed run
         k64 = args.steps if args.fp64_steps < 0 else args.fp64_steps
-        d64 = build_deck(args.deck, "fp64")
+        d64 = build_deck(args.deck, "fp64", args.modes)
         r64 = cg.Run(d64, particles=parts, rng=rng)
         r64.step(args.warmup, graph=False)
         s64a = r64.state()
@@ -482,7 +489,7 @@ def main():
             e2e["value"] = reduce_replicas(e2e["seconds"], e2e["psteps"], dist, "cuda")[2]
     base = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        base = cpu_baseline(build_deck(args.deck, "fp64"), parts, rng)
+        base = cpu_baseline(build_deck(args.deck, "fp64", args.modes), parts, rng)
 
     if rank == 0:
         line = {
