@@ -1191,8 +1191,12 @@ int cyl_load_species_device(cyl_handle hh, int32_t isp, uint64_t seed, int64_t i
   if (n > p.cap) return CYL_ERR_CAPACITY;
   cudaStream_t s = h->st;
   CK(cudaStreamSynchronize(s));
+  // every copy below is on the handle's stream, so the kernels on it see
+  // them (a cudaMemcpy from pageable memory may return before its DMA lands,
+  // and it is not ordered with a non-blocking stream)
   SpeciesCounters c{n, 0, 0u, 0u};
-  CK(cudaMemcpy(h->d_cnt + isp, &c, sizeof(c), cudaMemcpyHostToDevice));
+  CK(cudaMemcpyAsync(h->d_cnt + isp, &c, sizeof(c), cudaMemcpyHostToDevice, s));
+  if (n == 0) CK(cudaStreamSynchronize(s));
   if (n > 0) {
     double* d_dens = nullptr;
     int8_t* d_dmap = nullptr;
@@ -1214,10 +1218,10 @@ int cyl_load_species_device(cyl_handle hh, int32_t isp, uint64_t seed, int64_t i
     }
     std::vector<int8_t> dm(cells);
     for (size_t k = 0; k < cells; ++k) dm[k] = (int8_t)dmap[k];
-    cudaError_t e = cudaMemcpy(d_dens, dens.data(), cells * sizeof(double), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(d_dmap, dm.data(), cells, cudaMemcpyHostToDevice);
+    cudaError_t e = cudaMemcpyAsync(d_dens, dens.data(), cells * sizeof(double), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_dmap, dm.data(), cells, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess)
-      e = cudaMemcpy(d_valid, valid.data(), (size_t)nvalid * sizeof(int32_t), cudaMemcpyHostToDevice);
+      e = cudaMemcpyAsync(d_valid, valid.data(), (size_t)nvalid * sizeof(int32_t), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d_npic, 0, cells * sizeof(int), s);
     LoadParams P{};
     P.nx = h->g.nx;
@@ -1256,7 +1260,10 @@ int cyl_load_species_device(cyl_handle hh, int32_t isp, uint64_t seed, int64_t i
       mixed_from_double(s, p, st, n, cap, h->xg0, h->rc);
       e = cudaGetLastError();
     }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    // the host buffers above and the temporaries stay alive until the
+    // stream has used them
+    const cudaError_t es = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = es;
     release();
     if (e != cudaSuccess) {
       h->last_cuda_error = e;
@@ -1297,7 +1304,8 @@ int cyl_set_injection_stream(cyl_handle hh, int32_t mode, uint64_t seed) {
     }
     CK(cudaStreamSynchronize(h->st));
     if (cudaMalloc(&h->d_injsp, sizeof(tab)) != cudaSuccess) return CYL_ERR_OUT_OF_MEMORY;
-    CK(cudaMemcpy(h->d_injsp, tab, sizeof(tab), cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(h->d_injsp, tab, sizeof(tab), cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
   }
   h->inj_counter = mode == CYL_RNG_COUNTER;
   h->inj_seed = seed;
@@ -1399,7 +1407,9 @@ int cyl_upload_field(cyl_handle hh, int32_t which, const double* data) {
   if (fs >= 0) {
     std::vector<float> tmp(h->fcount * 2);
     for (size_t i = 0; i < tmp.size(); ++i) tmp[i] = (float)data[i];
-    CK(cudaMemcpy(h->Ff[fs], tmp.data(), tmp.size() * sizeof(float), cudaMemcpyHostToDevice));
+    // after the stream's earlier work on the array, before its later work
+    CK(cudaMemcpyAsync(h->Ff[fs], tmp.data(), tmp.size() * sizeof(float), cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
     return CYL_OK;
   }
   CK(cudaMemcpyAsync(h->F[field_slot(h, which)], data, h->fcount * sizeof(cplx), cudaMemcpyHostToDevice,
