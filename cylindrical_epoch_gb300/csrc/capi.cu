@@ -2033,17 +2033,40 @@ int cyl_batch_step(cyl_batch b, const cyl_handle* hs, int32_t n, int32_t nsteps)
       }
       const bool same = b->gexec && b->g_runs == serials && b->g_par == par0 && b->g_jobs == nj;
       if (!same) {
-        if (b->gexec) {
-          cudaGraphExecDestroy(b->gexec);
-          b->gexec = nullptr;
-        }
+        // capture the chunk for the new membership; when its graph has the
+        // old one's shape (a run replaced by one of the same kind), update
+        // the executable graph in place instead of instantiating a new one
+        // (an update does not touch launches still in flight)
         cudaGraph_t graph;
-        if (cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return CYL_ERR_CUDA;
+        auto drop_exec = [b]() {
+          if (b->gexec) cudaGraphExecDestroy(b->gexec);
+          b->gexec = nullptr;
+        };
+        if (cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+          drop_exec();
+          return CYL_ERR_CUDA;
+        }
         enqueue_batch_chunk(b, runs, nj, k, M);
-        if (cudaStreamEndCapture(b->st, &graph) != cudaSuccess) return CYL_ERR_CUDA;
-        const cudaError_t e = cudaGraphInstantiate(&b->gexec, graph, 0);
+        if (cudaStreamEndCapture(b->st, &graph) != cudaSuccess) {
+          drop_exec();
+          return CYL_ERR_CUDA;
+        }
+        bool updated = false;
+        if (b->gexec) {
+          cudaGraphExecUpdateResultInfo info;
+          updated = cudaGraphExecUpdate(b->gexec, graph, &info) == cudaSuccess;
+          if (!updated) {
+            (void)cudaGetLastError();
+            drop_exec();
+          }
+        }
+        cudaError_t e = cudaSuccess;
+        if (!updated) e = cudaGraphInstantiate(&b->gexec, graph, 0);
         cudaGraphDestroy(graph);
-        if (e != cudaSuccess) return CYL_ERR_CUDA;
+        if (e != cudaSuccess) {
+          b->gexec = nullptr;
+          return CYL_ERR_CUDA;
+        }
         b->g_runs = serials;
         b->g_par = par0;
         b->g_jobs = nj;

@@ -187,6 +187,9 @@ int open_job(cyl_server_s* srv, Job* job, bool tune, cyl_handle* out, int64_t* n
 int close_job(Job* job, cyl_handle h, int64_t done, int64_t n0, int r) {
   const cyl_job_desc& d = job->desc;
   if (r == CYL_OK) r = cyl_diagnostics(h, &job->res.diag);
+  // steps enqueued without a sync (batches, a batched job's last steps)
+  // report a raised device error word here
+  if (r == CYL_OK && job->res.diag.device_error != 0) r = CYL_ERR_DEVICE_FLAG;
   if (r == CYL_OK) r = cyl_get_run_state(h, &job->res.state);
   if (r == CYL_OK) {
     int64_t n1 = 0;
@@ -250,10 +253,9 @@ bool batchable(const cyl_server_s* srv, const cyl_job_desc& d) {
 // Batched mode (at most max_batch jobs open at once, counting those being
 // loaded and those run alone): advance every batched job by up to
 // CHUNK_STEPS steps per pass, those with the same number of modes together
-// (cyl_batch_step, at most max_batch per call); retire the finished ones.
-// A pass steps each group by the smallest number of steps any member has
-// left, so members finish at chunk boundaries and new jobs join at the next
-// pass.
+// (cyl_batch_step, at most max_batch per call, whole 16-step chunks; a job
+// with fewer steps left finishes alone on its own stream); retire the
+// finished ones.  New jobs join at the next pass.
 void stepper_main(cyl_server_s* srv) {
   cudaSetDevice(srv->device);
   std::map<int, cyl_batch> batches;
@@ -282,20 +284,27 @@ void stepper_main(cyl_server_s* srv) {
         }
         batches[M] = b;
       }
-      for (size_t s0 = 0; s0 < g.second.size(); s0 += (size_t)srv->max_batch) {
-        const size_t s1 = std::min(g.second.size(), s0 + (size_t)srv->max_batch);
-        int64_t k = CHUNK_STEPS;
-        std::vector<cyl_handle> hs;
-        for (size_t q = s0; q < s1; ++q) {
-          const size_t a = g.second[q];
-          k = std::min<int64_t>(k, act[a].job->desc.nsteps - act[a].done);
-          hs.push_back(act[a].h);
+      // a job with fewer than CHUNK_STEPS steps left takes its last steps
+      // alone (asynchronously, on its own stream), so that the batch keeps
+      // stepping whole graph-captured chunks
+      std::vector<size_t> full;
+      for (size_t a : g.second) {
+        const int64_t left = act[a].job->desc.nsteps - act[a].done;
+        if (left >= CHUNK_STEPS) {
+          full.push_back(a);
+        } else {
+          err[a] = cyl_step_async(act[a].h, (int32_t)left);
+          stepped[a] = err[a] == CYL_OK ? left : 0;
         }
-        const int rc = cyl_batch_step(batches[M], hs.data(), (int32_t)hs.size(), (int32_t)k);
+      }
+      for (size_t s0 = 0; s0 < full.size(); s0 += (size_t)srv->max_batch) {
+        const size_t s1 = std::min(full.size(), s0 + (size_t)srv->max_batch);
+        std::vector<cyl_handle> hs;
+        for (size_t q = s0; q < s1; ++q) hs.push_back(act[full[q]].h);
+        const int rc = cyl_batch_step(batches[M], hs.data(), (int32_t)hs.size(), CHUNK_STEPS);
         for (size_t q = s0; q < s1; ++q) {
-          const size_t a = g.second[q];
-          err[a] = rc;
-          stepped[a] = rc == CYL_OK ? k : 0;
+          err[full[q]] = rc;
+          stepped[full[q]] = rc == CYL_OK ? CHUNK_STEPS : 0;
         }
       }
     }
