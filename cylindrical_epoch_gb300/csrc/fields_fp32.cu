@@ -6,6 +6,8 @@
 // precomputed; the first radial cell (ir = 1, where the 1/r terms are
 // largest) is updated in FP64 arithmetic.  The FP64 -> FP32 conversion of
 // the currents is done with integer operations (GB300's FP64 pipe is narrow).
+#include <cmath>
+
 #include "cyl_common.cuh"
 #include "cyl_kernels.cuh"
 #include "cyl_convert.cuh"
@@ -21,29 +23,48 @@ __device__ __forceinline__ float2 ldj(const cplx* p) {
   return make_float2(d2f_bits(v.x), d2f_bits(v.y));
 }
 
-__global__ void k_update_e_f32(FieldSetF F, const float4* rowtab, float cdx, float cdy, float cj, RunConst rc) {
+// Coefficients of the first radial cell (ir = 1) in FP64, precomputed on the
+// host so that the row needs no FP64 division (h = dt/2, r_d, r_p of ir = 1):
+// E: a = c^2/r_p h/2, bm = c^2/r_p h (times i m), c = c^2/dy h, cx = c^2/dx h,
+//    d = h/eps0, erm = c^2/r_d h (times i m);
+// B: p = h/r_d (times i m), q = h/(2 r_d), r = h/dy, s = h/r_p (times i m),
+//    t = h/dx.
+struct Row1E {
+  double a, bm, c, cx, d, erm;
+};
+struct Row1B {
+  double p, q, r, s, t;
+};
+
+// Grid: (columns, modes, rows), so that the FP64 first row of every mode is
+// in the first wave of CTAs rather than the tail of the launch.
+__global__ void k_update_e_f32(FieldSetF F, const float4* rowtab, float cdx, float cdy, float cj, Row1E r1,
+                               RunConst rc) {
   const int ix = blockIdx.x * blockDim.x + threadIdx.x;  // 0..nx
-  const int ir = 1 + blockIdx.y;
-  const int im = blockIdx.z;
+  const int im = blockIdx.y;
+  const int ir = 1 + blockIdx.z;
   if (ix > rc.nx) return;
   if (ir == 1) {
-    // first radial cell in FP64 arithmetic (same equations as update_e_field)
-    const double dx = rc.dx, dy = rc.dy, dt = rc.dt, c2 = CLIGHT * CLIGHT;
-    const double r_d = fabs((double)(ir - 1) * dy + rc.y_grid_min);
-    const double r_p = r_d + 0.5 * dy;
-    const double fac_x = c2 / r_p;
-    const cplx im_fac_x = (IMAGI * (double)im) * fac_x;
-    const cplx im_fac_r = ((IMAGI * (double)im) * c2) / r_d;
+    // first radial cell in FP64 arithmetic (the equations of update_e_field)
+    const double m = (double)im;
     const cplx bt0 = F.bt(ix, ir, im), bt1 = F.bt(ix, ir + 1, im), btx = F.bt(ix + 1, ir, im);
     const cplx br0 = F.br(ix, ir, im), brx = F.br(ix + 1, ir, im);
     const cplx bx0 = F.bx(ix, ir, im), bx1 = F.bx(ix, ir + 1, im);
-    F.ex(ix, ir, im) = (cplx)F.ex(ix, ir, im) +
-        ((((fac_x * 0.5) * (bt1 + bt0) + im_fac_x * br0) + (c2 * (bt1 - bt0)) / dy) -
-         (cplx)F.jx(ix, ir, im) / EPS0) * 0.5 * dt;
-    F.er(ix, ir, im) = (cplx)F.er(ix, ir, im) +
-        ((-(im_fac_r * bx0) - (c2 * (btx - bt0)) / dx) - (cplx)F.jr(ix, ir, im) / EPS0) * 0.5 * dt;
-    F.et(ix, ir, im) = (cplx)F.et(ix, ir, im) +
-        (((c2 * (brx - br0)) / dx - (c2 * (bx1 - bx0)) / dy) - (cplx)F.jt(ix, ir, im) / EPS0) * 0.5 * dt;
+    const cplx jx = F.jx(ix, ir, im), jr = F.jr(ix, ir, im), jt = F.jt(ix, ir, im);
+    const double bmm = r1.bm * m, erm = r1.erm * m;
+    cplx ex = F.ex(ix, ir, im), er = F.er(ix, ir, im), et = F.et(ix, ir, im);
+    // ex += a (bt1 + bt0) + i m bm br0 + c (bt1 - bt0) - d jx
+    ex.re += r1.a * (bt1.re + bt0.re) - bmm * br0.im + r1.c * (bt1.re - bt0.re) - r1.d * jx.re;
+    ex.im += r1.a * (bt1.im + bt0.im) + bmm * br0.re + r1.c * (bt1.im - bt0.im) - r1.d * jx.im;
+    // er += -i m erm bx0 - cx (btx - bt0) - d jr
+    er.re += erm * bx0.im - r1.cx * (btx.re - bt0.re) - r1.d * jr.re;
+    er.im += -erm * bx0.re - r1.cx * (btx.im - bt0.im) - r1.d * jr.im;
+    // et += cx (brx - br0) - c (bx1 - bx0) - d jt
+    et.re += r1.cx * (brx.re - br0.re) - r1.c * (bx1.re - bx0.re) - r1.d * jt.re;
+    et.im += r1.cx * (brx.im - br0.im) - r1.c * (bx1.im - bx0.im) - r1.d * jt.im;
+    F.ex(ix, ir, im) = ex;
+    F.er(ix, ir, im) = er;
+    F.et(ix, ir, im) = et;
     return;
   }
   const float4 rt = rowtab[ir];
@@ -70,11 +91,11 @@ __global__ void k_update_e_f32(FieldSetF F, const float4* rowtab, float cdx, flo
   st2(F.et.ptr(ix, ir, im), e);
 }
 
-__global__ void k_update_b_f32(FieldSetF F, int save_old, const float4* rowtab, float hdx, float hdy,
+__global__ void k_update_b_f32(FieldSetF F, int save_old, const float4* rowtab, float hdx, float hdy, Row1B r1,
                                RunConst rc) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y;
-  const int im = blockIdx.z;
+  const int im = blockIdx.y;
+  const int j = blockIdx.z;
   if (i >= rc.nxg) return;
   const int ix = i + 1 - NG, ir = j + 1 - NG;
   if (save_old) {
@@ -84,18 +105,25 @@ __global__ void k_update_b_f32(FieldSetF F, int save_old, const float4* rowtab, 
   }
   if (ix < 0 || ix > rc.nx || ir < 1 || ir > rc.ny - 1) return;
   if (ir == 1) {
-    const double dx = rc.dx, dy = rc.dy, dt = rc.dt;
-    const double r_d = fabs((double)(ir - 1) * dy + rc.y_grid_min);
-    const double r_p = r_d + 0.5 * dy;
-    const cplx im_fac_x = (IMAGI * (double)im) / r_d;
-    const cplx im_fac_r = (IMAGI * (double)im) / r_p;
+    // first radial cell in FP64 arithmetic (the equations of update_b_field)
+    const double m = (double)im;
     const cplx et0 = F.et(ix, ir, im), etm1 = F.et(ix, ir - 1, im), etxm = F.et(ix - 1, ir, im);
     const cplx er0 = F.er(ix, ir, im), erxm = F.er(ix - 1, ir, im);
     const cplx ex0 = F.ex(ix, ir, im), exm1 = F.ex(ix, ir - 1, im);
-    F.bx(ix, ir, im) = (cplx)F.bx(ix, ir, im) -
-        ((im_fac_x * er0 + (0.5 * (et0 + etm1)) / r_d) + (et0 - etm1) / dy) * 0.5 * dt;
-    F.br(ix, ir, im) = (cplx)F.br(ix, ir, im) + (im_fac_r * ex0 + (et0 - etxm) / dx) * 0.5 * dt;
-    F.bt(ix, ir, im) = (cplx)F.bt(ix, ir, im) + (-((er0 - erxm) / dx) + (ex0 - exm1) / dy) * 0.5 * dt;
+    const double pm = r1.p * m, sm = r1.s * m;
+    cplx bx = F.bx(ix, ir, im), br = F.br(ix, ir, im), bt = F.bt(ix, ir, im);
+    // bx -= i m p er0 + q (et0 + etm1) + r (et0 - etm1)
+    bx.re -= -pm * er0.im + r1.q * (et0.re + etm1.re) + r1.r * (et0.re - etm1.re);
+    bx.im -= pm * er0.re + r1.q * (et0.im + etm1.im) + r1.r * (et0.im - etm1.im);
+    // br += i m s ex0 + t (et0 - etxm)
+    br.re += -sm * ex0.im + r1.t * (et0.re - etxm.re);
+    br.im += sm * ex0.re + r1.t * (et0.im - etxm.im);
+    // bt += -t (er0 - erxm) + r (ex0 - exm1)
+    bt.re += -r1.t * (er0.re - erxm.re) + r1.r * (ex0.re - exm1.re);
+    bt.im += -r1.t * (er0.im - erxm.im) + r1.r * (ex0.im - exm1.im);
+    F.bx(ix, ir, im) = bx;
+    F.br(ix, ir, im) = br;
+    F.bt(ix, ir, im) = bt;
     return;
   }
   const float4 rt = rowtab[ir];
@@ -123,17 +151,21 @@ __global__ void k_update_b_f32(FieldSetF F, int save_old, const float4* rowtab, 
 
 void launch_update_e_f32(cudaStream_t s, const FieldSetF& F, const double* rowtab, const RunConst& rc) {
   const double c2 = CLIGHT * CLIGHT, h = 0.5 * rc.dt;
-  dim3 blk(128), grd((rc.nx + 1 + 127) / 128, rc.ny, rc.M);
+  const double r_d = std::fabs(rc.y_grid_min), r_p = r_d + 0.5 * rc.dy;
+  const Row1E r1{c2 / r_p * 0.5 * h, c2 / r_p * h, c2 / rc.dy * h, c2 / rc.dx * h, h / EPS0, c2 / r_d * h};
+  dim3 blk(128), grd((rc.nx + 1 + 127) / 128, rc.M, rc.ny);
   k_update_e_f32<<<grd, blk, 0, s>>>(F, reinterpret_cast<const float4*>(rowtab), (float)(c2 / rc.dx * h),
-                                     (float)(c2 / rc.dy * h), (float)(h / EPS0), rc);
+                                     (float)(c2 / rc.dy * h), (float)(h / EPS0), r1, rc);
 }
 
 void launch_update_b_f32(cudaStream_t s, const FieldSetF& F, int save_old, const double* rowtab,
                          const RunConst& rc) {
   const double h = 0.5 * rc.dt;
-  dim3 blk(128), grd((rc.nxg + 127) / 128, rc.nyg, rc.M);
+  const double r_d = std::fabs(rc.y_grid_min), r_p = r_d + 0.5 * rc.dy;
+  const Row1B r1{h / r_d, 0.5 * h / r_d, h / rc.dy, h / r_p, h / rc.dx};
+  dim3 blk(128), grd((rc.nxg + 127) / 128, rc.M, rc.nyg);
   k_update_b_f32<<<grd, blk, 0, s>>>(F, save_old, reinterpret_cast<const float4*>(rowtab), (float)(h / rc.dx),
-                                     (float)(h / rc.dy), rc);
+                                     (float)(h / rc.dy), r1, rc);
 }
 
 }  // namespace cyl
