@@ -14,6 +14,8 @@
 // particle boundaries, stays one single-CTA kernel.
 #include <cstddef>
 
+#include <type_traits>
+
 #include "cyl_common.cuh"
 #include "cyl_kernels.cuh"
 
@@ -256,16 +258,63 @@ static void launch_ghost_bcs(cudaStream_t s, FViewT<T> a, FViewT<T> b, FViewT<T>
 // or >= 1 (B) that the axis sequence does not write (it writes row 0, and
 // row 1 of Er only for m > 1, which no mirror reads), so every
 // (column, mode, task) is an independent work item.
+// a / d: the exact IEEE division for the FP64 form (its results must be the
+// reference's), a multiplication by the host-rounded 1/d for the mixed
+// form, whose E and B are FP32 anyway.
+template <typename T>
+__device__ __forceinline__ cplx div_form(cplx a, double d, double inv_d) {
+  if constexpr (std::is_same<T, cplxf>::value) return a * inv_d;
+  else return a / d;
+}
+
+// Scalars of the axis, laser and r_max kernels, rounded once on the host
+// in the order the kernels used to evaluate them (no FMA contraction on
+// either side, so the FP64 form's values are unchanged).
+struct BcConst {
+  double c4dy;                 // 4 c^2 / dy
+  double inv_eps0, inv_dx, inv_dy, inv_9;
+  double lx, lr, sum, diff, dt_eps;  // k_laser_x
+  double rx_lx, rx_inv_r, rx_dtc2_4r, rx_ly, rx_sum_x, rx_sum_t, rx_dt_2eps, rx_lx_c;  // k_rmax_b
+  cplx rx_icdt_2r;
+};
+
+static BcConst bc_const(const RunConst& rc, double dt) {
+  BcConst k;
+  const double c2 = CLIGHT * CLIGHT;
+  k.c4dy = 4.0 * c2 / rc.dy;
+  k.inv_eps0 = 1.0 / EPS0;
+  k.inv_dx = 1.0 / rc.dx;
+  k.inv_dy = 1.0 / rc.dy;
+  k.inv_9 = 1.0 / 9.0;
+  const double dtc2 = dt * c2;
+  k.lx = dtc2 / rc.dx;
+  k.lr = dtc2 / rc.dy;
+  k.sum = 1.0 / (k.lx + CLIGHT);
+  k.diff = k.lx - CLIGHT;
+  k.dt_eps = dt / EPS0;
+  const double dtc2r = dt * CLIGHT * CLIGHT;
+  k.rx_lx = dtc2r / rc.dx;
+  k.rx_inv_r = 1.0 / ((double)((float)rc.ny - 1.5f) * rc.dy + rc.y_grid_min);
+  k.rx_dtc2_4r = 0.25 * dtc2r * k.rx_inv_r;
+  k.rx_icdt_2r = ((0.5 * IMAGI) * CLIGHT) * dt * k.rx_inv_r;
+  k.rx_ly = dtc2r / rc.dy;
+  k.rx_sum_x = 1.0 / (k.rx_ly + CLIGHT);
+  k.rx_sum_t = 1.0 / ((k.rx_ly + CLIGHT) + k.rx_dtc2_4r);
+  k.rx_dt_2eps = 0.5 * dt / EPS0;
+  k.rx_lx_c = (0.5 * k.rx_lx) / CLIGHT;
+  return k;
+}
+
 // mode_sign of the reference for m >= 2: +1 at m = 2, alternating.
 __device__ __forceinline__ double mode_sign_of(int im) { return ((im - 2) & 1) ? -1.0 : 1.0; }
 
 template <typename T>
 __device__ __forceinline__ void e_axis_item(FViewT<T> ex, FViewT<T> er, FViewT<T> et, FView jx, FViewT<T> bt,
-                                            const RunConst& rc, int ix, int im, int task) {
-  const double dy = rc.dy, dt = rc.dt, c2 = CLIGHT * CLIGHT;
+                                            const RunConst& rc, const BcConst& K, int ix, int im, int task) {
+  const double dt = rc.dt;
   if (task == 0) {
     if (im == 0) {
-      ex(ix, 0, 0) = ex(ix, 0, 0) + ((4.0 * c2 / dy) * bt(ix, 1, 0) - jx(ix, 0, 0) / EPS0) * 0.5 * dt;
+      ex(ix, 0, 0) = ex(ix, 0, 0) + (K.c4dy * bt(ix, 1, 0) - div_form<T>(jx(ix, 0, 0), EPS0, K.inv_eps0)) * 0.5 * dt;
       et(ix, 0, 0) = mk(0.0, 0.0);
       er(ix, 0, 0) = -er(ix, 1, 0);
     } else if (im == 1) {
@@ -276,7 +325,7 @@ __device__ __forceinline__ void e_axis_item(FViewT<T> ex, FViewT<T> er, FViewT<T
       ex(ix, 0, im) = mk(0.0, 0.0);
       et(ix, 0, im) = mk(0.0, 0.0);
       er(ix, 0, im) = -er(ix, 1, im);
-      er(ix, 1, im) = er(ix, 2, im) / 9.0;
+      er(ix, 1, im) = div_form<T>(er(ix, 2, im), 9.0, K.inv_9);
     }
     return;
   }
@@ -299,8 +348,8 @@ __device__ __forceinline__ void e_axis_item(FViewT<T> ex, FViewT<T> er, FViewT<T
 
 template <typename T>
 __device__ __forceinline__ void b_axis_item(FViewT<T> bx, FViewT<T> br, FViewT<T> bt, FViewT<T> ex, FViewT<T> et,
-                                            const RunConst& rc, int ix, int im, int task) {
-  const double dx = rc.dx, dy = rc.dy, dt = rc.dt;
+                                            const RunConst& rc, const BcConst& K, int ix, int im, int task) {
+  const double dx = rc.dx, dt = rc.dt;
   if (task == 0) {
     if (im == 0) {
       br(ix, 0, 0) = mk(0.0, 0.0);
@@ -310,7 +359,8 @@ __device__ __forceinline__ void b_axis_item(FViewT<T> bx, FViewT<T> br, FViewT<T
       bx(ix, 0, 1) = -bx(ix, 1, 1);
       if (ix >= 2 - NG)
         br(ix, 0, 1) = br(ix, 0, 1) +
-            ((IMAGI / dy) * ex(ix, 0, 1) + (et(ix, 0, 1) - et(ix - 1, 0, 1)) / dx) * 0.5 * dt;
+            (mk(0.0, K.inv_dy) * ex(ix, 0, 1) + div_form<T>(et(ix, 0, 1) - et(ix - 1, 0, 1), dx, K.inv_dx)) * 0.5 *
+                dt;
       bt(ix, 0, 1) = (-2.0 * IMAGI) * br(ix, 0, 1) - bt(ix, 1, 1);
     } else {
       bx(ix, 0, im) = -bx(ix, 1, im);
@@ -346,7 +396,7 @@ __device__ __forceinline__ void b_axis_item(FViewT<T> bx, FViewT<T> br, FViewT<T
 // at x_max; nx >= 8).
 template <typename T>
 __global__ void k_laser_x(FieldSetT<T> F, const StepRec* rec, const double* src, const cplx* cols, double dt,
-                          RunConst rc) {
+                          BcConst K, RunConst rc) {
   const int nx = rc.nx, ny = rc.ny, M = rc.M;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= 2 * (ny + 1) * M) return;
@@ -355,8 +405,7 @@ __global__ void k_laser_x(FieldSetT<T> F, const StepRec* rec, const double* src,
   const int bd = side == 0 ? CYL_BD_X_MIN : CYL_BD_X_MAX;
   if (!(rec->add_laser[bd] || rec->bc_field[bd] == CYL_BC_SIMPLE_OUTFLOW)) return;
   const double c2 = CLIGHT * CLIGHT;
-  const double dtc2 = dt * c2, lx = dtc2 / rc.dx, lr = dtc2 / rc.dy;
-  const double sum = 1.0 / (lx + CLIGHT), diff = lx - CLIGHT, dt_eps = dt / EPS0;
+  const double lr = K.lr, sum = K.sum, diff = K.diff, dt_eps = K.dt_eps;
   const int ncolv = ny + 2 * NG;
   const size_t cs = (size_t)ncolv * M;
   const cplx* erb = cols + (size_t)(side * 6 + 1) * cs;
@@ -372,12 +421,13 @@ __global__ void k_laser_x(FieldSetT<T> F, const StepRec* rec, const double* src,
   const cplx imc = ((IMAGI * (double)m) * c2) * dt;
   // Bt row: ir pairs with r_d_vals(ir-1) (whole array inside a 1:ny section)
   const double rdv = fabs((double)(ir - 2) * rc.dy + rc.y_grid_min);
+  const double inv_rdv = 1.0 / rdv;  // used by the mixed form only
   cplx nbt;
   if (side == 0) {
     cplx st = mk(0.0, 0.0);
     if (m == 1) st = s1[ir] + IMAGI * s2[ir];
     nbt = sum * (((((4.0 * st + 2.0 * (erb[cj] + CLIGHT * btb[cj])) - 2.0 * F.er(1, ir, m)) +
-                   (imc * F.bx(1, ir, m)) / rdv) +
+                   div_form<T>(imc * F.bx(1, ir, m), rdv, inv_rdv)) +
                   dt_eps * F.jr(1, ir, m)) +
                  diff * F.bt(2, ir, m));
   } else {
@@ -385,7 +435,7 @@ __global__ void k_laser_x(FieldSetT<T> F, const StepRec* rec, const double* src,
     cplx st = mk(0.0, 0.0);
     if (m == 1) st = s1[ir - 1] + IMAGI * s2[ir - 1];
     nbt = sum * ((((((-4.0) * st - 2.0 * (erb[cj] + CLIGHT * btb[cj])) + 2.0 * F.er(nx - 1, ir, m)) -
-                   (imc * F.bx(nx - 1, ir, m)) / rdv) -
+                   div_form<T>(imc * F.bx(nx - 1, ir, m), rdv, inv_rdv)) -
                   dt_eps * F.jr(nx - 1, ir, m)) +
                  diff * F.bt(nx - 1, ir, m));
   }
@@ -419,7 +469,7 @@ __global__ void k_laser_x(FieldSetT<T> F, const StepRec* rec, const double* src,
 // one thread per (ix, m).  The new Bx, Bt of row ny depend on row ny-1, row
 // ny of the other arrays and the B_old / J_old arrays only.
 template <typename T>
-__global__ void k_rmax_b(FieldSetT<T> F, const StepRec* rec, double dt, RunConst rc) {
+__global__ void k_rmax_b(FieldSetT<T> F, const StepRec* rec, double dt, BcConst K, RunConst rc) {
   const int nx = rc.nx, ny = rc.ny, M = rc.M;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int b = rec->bc_field[CYL_BD_Y_MAX];
@@ -433,14 +483,9 @@ __global__ void k_rmax_b(FieldSetT<T> F, const StepRec* rec, double dt, RunConst
   }
   if (b != CYL_BC_SIMPLE_OUTFLOW || t >= nx * M) return;
   const int ix = 1 + t % nx, m = t / nx;
-  const double dtc2 = dt * CLIGHT * CLIGHT, lx = dtc2 / rc.dx;
-  const double inv_r = 1.0 / ((double)((float)ny - 1.5f) * rc.dy + rc.y_grid_min);
-  const double dtc2_4r = 0.25 * dtc2 * inv_r;
-  const cplx icdt_2r = ((0.5 * IMAGI) * CLIGHT) * dt * inv_r;
-  const double ly = dtc2 / rc.dy;
-  const double sum_x = 1.0 / (ly + CLIGHT), sum_t = 1.0 / ((ly + CLIGHT) + dtc2_4r);
-  const double dt_2eps = 0.5 * dt / EPS0;
-  const cplx icm = icdt_2r * (double)m;
+  const double lx = K.rx_lx, inv_r = K.rx_inv_r, dtc2_4r = K.rx_dtc2_4r, ly = K.rx_ly;
+  const double sum_x = K.rx_sum_x, sum_t = K.rx_sum_t, dt_2eps = K.rx_dt_2eps;
+  const cplx icm = K.rx_icdt_2r * (double)m;
   if (ix <= nx - 1) {
     cplx v = (-F.bx(ix, ny - 1, m)) * (CLIGHT - ly);
     v = v - F.bxo(ix, ny, m) * ((-CLIGHT) + ly);
@@ -455,7 +500,7 @@ __global__ void k_rmax_b(FieldSetT<T> F, const StepRec* rec, double dt, RunConst
   cplx v = (-F.bt(ix, ny - 1, m)) * ((CLIGHT - ly) + dtc2_4r);
   v = v - F.bto(ix, ny, m) * (((-CLIGHT) + ly) + dtc2_4r);
   v = v - F.bto(ix, ny - 1, m) * (((-CLIGHT) - ly) + dtc2_4r);
-  v = v - ((0.5 * lx) / CLIGHT) * (((F.er(ix, ny, m) + F.er(ix, ny - 1, m)) - F.er(ix - 1, ny, m)) -
+  v = v - K.rx_lx_c * (((F.er(ix, ny, m) + F.er(ix, ny - 1, m)) - F.er(ix - 1, ny, m)) -
                                    F.er(ix - 1, ny - 1, m));
   v = v - (icm * CLIGHT) * (F.br(ix, ny - 1, m) + F.bro(ix, ny - 1, m));
   v = v + dt_2eps * (F.jx(ix, ny - 1, m) + F.jxo(ix, ny - 1, m));
@@ -683,20 +728,21 @@ __global__ void k_shift_fields(FieldSetT<T> F, const cplx* cols, const StepRec* 
 
 // Axis rules and J folding: one thread per independent work item.
 template <typename T>
-__global__ void k_e_axis(FViewT<T> ex, FViewT<T> er, FViewT<T> et, FView jx, FViewT<T> bt, RunConst rc) {
+__global__ void k_e_axis(FViewT<T> ex, FViewT<T> er, FViewT<T> et, FView jx, FViewT<T> bt, BcConst K, RunConst rc) {
   const int ncol = rc.nx + 2 * NG;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ncol * rc.M * NG) return;
   const int ix = 1 - NG + t % ncol, r = t / ncol;
-  e_axis_item(ex, er, et, jx, bt, rc, ix, r % rc.M, r / rc.M);
+  e_axis_item(ex, er, et, jx, bt, rc, K, ix, r % rc.M, r / rc.M);
 }
 template <typename T>
-__global__ void k_b_axis(FViewT<T> bx, FViewT<T> br, FViewT<T> bt, FViewT<T> ex, FViewT<T> et, RunConst rc) {
+__global__ void k_b_axis(FViewT<T> bx, FViewT<T> br, FViewT<T> bt, FViewT<T> ex, FViewT<T> et, BcConst K,
+                         RunConst rc) {
   const int ncol = rc.nx + 2 * NG;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ncol * rc.M * NG) return;
   const int ix = 1 - NG + t % ncol, r = t / ncol;
-  b_axis_item(bx, br, bt, ex, et, rc, ix, r % rc.M, r / rc.M);
+  b_axis_item(bx, br, bt, ex, et, rc, K, ix, r % rc.M, r / rc.M);
 }
 __global__ void k_j_rmin(FView jx, FView jr, FView jt, RunConst rc) {
   const int ncol = rc.nx + 2 * NG;
@@ -719,7 +765,7 @@ void launch_update_b(cudaStream_t s, const FieldSet& F, int save_old, const RunC
 }
 template <typename T>
 void launch_e_axis_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc) {
-  k_e_axis<T><<<axis_blocks(rc), 128, 0, s>>>(F.ex, F.er, F.et, F.jx, F.bt, rc);
+  k_e_axis<T><<<axis_blocks(rc), 128, 0, s>>>(F.ex, F.er, F.et, F.jx, F.bt, bc_const(rc, rc.dt), rc);
   launch_ghost_bcs<T>(s, F.ex, F.er, F.et, 0, false, bc_ptr(rec), rc);
 }
 template <typename T>
@@ -728,7 +774,7 @@ void launch_efield_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec
 }
 template <typename T>
 void launch_b_axis_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc) {
-  k_b_axis<T><<<axis_blocks(rc), 128, 0, s>>>(F.bx, F.br, F.bt, F.ex, F.et, rc);
+  k_b_axis<T><<<axis_blocks(rc), 128, 0, s>>>(F.bx, F.br, F.bt, F.ex, F.et, bc_const(rc, rc.dt), rc);
   launch_ghost_bcs<T>(s, F.bx, F.br, F.bt, 3, true, bc_ptr(rec), rc);
 }
 // update_b_field axis rules, then bfield_final_bcs (boundary.F90:1505-1537):
@@ -737,10 +783,11 @@ void launch_b_axis_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec
 template <typename T>
 void launch_b_final_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const double* src,
                         const cplx* cols, int do_axis, double dt, const RunConst& rc) {
-  if (do_axis) k_b_axis<T><<<axis_blocks(rc), 128, 0, s>>>(F.bx, F.br, F.bt, F.ex, F.et, rc);
+  const BcConst K = bc_const(rc, dt);
+  if (do_axis) k_b_axis<T><<<axis_blocks(rc), 128, 0, s>>>(F.bx, F.br, F.bt, F.ex, F.et, bc_const(rc, rc.dt), rc);
   launch_ghost_bcs<T>(s, F.bx, F.br, F.bt, 3, false, bc_ptr(rec), rc);
-  k_laser_x<T><<<(2 * (rc.ny + 1) * rc.M + 127) / 128, 128, 0, s>>>(F, rec, src, cols, dt, rc);
-  k_rmax_b<T><<<((rc.nx + 2 * NG) * rc.M + 127) / 128, 128, 0, s>>>(F, rec, dt, rc);
+  k_laser_x<T><<<(2 * (rc.ny + 1) * rc.M + 127) / 128, 128, 0, s>>>(F, rec, src, cols, dt, K, rc);
+  k_rmax_b<T><<<((rc.nx + 2 * NG) * rc.M + 127) / 128, 128, 0, s>>>(F, rec, dt, K, rc);
   launch_ghost_bcs<T>(s, F.bx, F.br, F.bt, 3, true, bc_ptr(rec), rc);
 }
 template <typename T>
