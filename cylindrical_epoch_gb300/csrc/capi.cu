@@ -418,7 +418,7 @@ static void push_all(Handle* h, cudaStream_t s, const FieldSetF& F, const StepRe
   for (int i = 0; i < h->nsp; ++i) {
     if (h->sp[i].immobile) continue;
     push_mixed_fns(h->tile_shape)
-        .launch(s, F, h->sp[i], h->d_cnt + i, rec, h->rc, apply_bcs, h->nblocks_mixed, h->nblocks, h->mp[i],
+        .launch(s, F, h->sp[i], h->d_cnt + i, rec, h->rc, apply_bcs, h->nblocks_mixed, h->nblocks / 4, h->mp[i],
                 h->d_tiles + i);
     count_launch(h, 2);
   }

@@ -794,7 +794,14 @@ template <typename T>
 void launch_current_finish(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc,
                            int smooth, int its, int comp_its, int stride, FView wk) {
   k_j_rmin<<<jrmin_blocks(rc), 128, 0, s>>>(F.jx, F.jr, F.jt, rc);
-  k_current_finish<<<1, CTA_THREADS, 0, s>>>(F.jx, F.jr, F.jt, rec, rc);
+  // the folding and halo pass has work only with a reflecting or periodic
+  // particle boundary or a periodic x field boundary (before or after the
+  // window starts); all of these are fixed for the run
+  const bool reflect = rc.bc_allspecies[CYL_BD_X_MIN] == CYL_BC_REFLECT ||
+                       rc.bc_allspecies[CYL_BD_X_MAX] == CYL_BC_REFLECT ||
+                       rc.bc_allspecies[CYL_BD_Y_MAX] == CYL_BC_REFLECT;
+  const bool periodic = rc.bc_allspecies[CYL_BD_X_MIN] == CYL_BC_PERIODIC || (rc.bc_mask & BCM_PERIODIC_X);
+  if (reflect || periodic) k_current_finish<<<1, CTA_THREADS, 0, s>>>(F.jx, F.jr, F.jt, rec, rc);
   if (!smooth) return;
   FView js[3] = {F.jx, F.jr, F.jt};
   dim3 blk(128), grd((rc.nx + 127) / 128, rc.ny, rc.M);
