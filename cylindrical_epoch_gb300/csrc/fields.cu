@@ -684,10 +684,10 @@ __device__ void shift_row(FViewT<U> f, int j, int m, const int* bcf, const RunCo
   }
   // periodic self-wrap (field_mode_bc) within this row
   if (bcf[CYL_BD_X_MAX] == CYL_BC_PERIODIC)
-    for (int i = 1 + threadIdx.x; i <= NG; i += blockDim.x) f(nx + i, j, m) = f(i, j, m);
+    for (int i = 1 + (int)threadIdx.x; i <= NG; i += (int)blockDim.x) f(nx + i, j, m) = f(i, j, m);
   __syncthreads();
   if (bcf[CYL_BD_X_MIN] == CYL_BC_PERIODIC)
-    for (int i = 1 - NG + threadIdx.x; i <= 0; i += blockDim.x) f(i, j, m) = f(nx + i, j, m);
+    for (int i = 1 - NG + (int)threadIdx.x; i <= 0; i += (int)blockDim.x) f(i, j, m) = f(nx + i, j, m);
 }
 
 template <typename T>
