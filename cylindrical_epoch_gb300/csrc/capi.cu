@@ -81,6 +81,7 @@ struct Handle {
   int inj_counter = 0;
   uint64_t inj_seed = 0;
   InjSpecies* d_injsp = nullptr;
+  int32_t* d_injrow = nullptr;  // (shift, species, row) of every injection slot (inj_cap)
   // diagnostics read without a stream sync: a ring of two pinned slots, each
   // the 8 reductions plus the device error word, with an event
   struct DiagSlot {
@@ -462,7 +463,7 @@ static void enqueue_step_post(Handle* h, cudaStream_t s, const FieldSetT<T>& F, 
   count_launch(h, 6);
   if (h->move_window) {
     if (h->inj_counter) {
-      launch_inject_counter(s, rec, h->d_injsp, h->nsp, rc, h->inj_seed, h->d_inj);
+      launch_inject_counter(s, rec, h->d_injsp, h->nsp, rc, h->inj_seed, h->d_injrow, h->d_inj);
       count_launch(h, 1);
     }
     for (int i = 0; i < h->nsp; ++i) {
@@ -1097,6 +1098,7 @@ int cyl_destroy(cyl_handle hh) {
   if (h->st) cudaStreamSynchronize(h->st);
   if (h->gexec) cudaGraphExecDestroy(h->gexec);
   cudaFree(h->d_injsp);
+  cudaFree(h->d_injrow);
   for (auto& d : h->diag_slot) {
     if (d.h) cudaFreeHost(d.h);
     if (d.ev) cudaEventDestroy(d.ev);
@@ -1304,6 +1306,11 @@ int cyl_set_injection_stream(cyl_handle hh, int32_t mode, uint64_t seed) {
     }
     CK(cudaStreamSynchronize(h->st));
     if (cudaMalloc(&h->d_injsp, sizeof(tab)) != cudaSuccess) return CYL_ERR_OUT_OF_MEMORY;
+    if (cudaMalloc(&h->d_injrow, sizeof(int32_t) * (size_t)h->inj_cap) != cudaSuccess) {
+      cudaFree(h->d_injsp);
+      h->d_injsp = nullptr;
+      return CYL_ERR_OUT_OF_MEMORY;
+    }
     CK(cudaMemcpyAsync(h->d_injsp, tab, sizeof(tab), cudaMemcpyHostToDevice, h->st));
     CK(cudaStreamSynchronize(h->st));
   }

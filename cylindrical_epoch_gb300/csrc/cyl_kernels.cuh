@@ -58,7 +58,7 @@ struct InjSpecies {  // per species: what insert_particles needs besides the col
 void launch_load_particles(cudaStream_t s, const LoadParams& P, const int32_t* valid, const double* dens,
                            const int8_t* dmap, int* npic, LoadOut o, uint32_t* wmax_bits);
 void launch_inject_counter(cudaStream_t s, const StepRec* rec, const InjSpecies* isp, int nsp, const RunConst& rc,
-                           uint64_t seed, double* inj);
+                           uint64_t seed, int32_t* rowmap, double* inj);
 
 // fields.cu (E/B boundary and axis kernels for either storage type)
 void launch_update_e(cudaStream_t s, const FieldSet& F, const RunConst& rc);

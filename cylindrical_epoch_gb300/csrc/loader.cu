@@ -132,40 +132,42 @@ __global__ void k_load_weights(LoadParams P, const double* __restrict__ dens, co
   atomicMax(wmax_bits, __float_as_uint(fabsf(__double2float_rn(w))));
 }
 
-// One block per (shift, species) of the step: rows in chunks of the block,
-// each thread one row (its count: floor(ppc) plus the row's fraction bit),
-// a block-wide exclusive scan for the rows' places, then the row's
-// particles.
+// Window injection in two passes, so that the particles' FP64 arithmetic is
+// spread over the GPU rather than one SM per (shift, species):
+//  1. k_inject_rows, one block per (shift, species): per row its count
+//     (floor(ppc) plus the row's fraction bit), a block-wide exclusive scan
+//     for the rows' places, and for every particle slot of the step's batch
+//     its (shift, species, row), packed as c << 28 | s << 24 | row;
+//  2. k_inject_particles, a grid-stride loop over the step's batch: each
+//     thread makes the particle of one slot from its counter.
 constexpr int INJ_THREADS = 256;
+constexpr int INJ_PART_THREADS = 128, INJ_PART_BLOCKS = 64;
 
-__global__ void __launch_bounds__(INJ_THREADS) k_inject_counter(const StepRec* __restrict__ rec,
-                                                                const InjSpecies* __restrict__ isp, int nsp,
-                                                                int ny, double dx, double dy, double y_grid_min,
-                                                                uint64_t seed, double* __restrict__ inj) {
+__device__ __forceinline__ int64_t inj_count(const InjSpecies& S, int iy, uint32_t shift, int s, uint64_t seed) {
+  int64_t bit = 0;
+  if (S.frac > 0.0 && u01(philox4x32_10((uint32_t)iy, shift, (uint32_t)s, TAG_INJ_COUNT, seed).v[0]) < S.frac)
+    bit = 1;
+  return S.nppc + bit;
+}
+
+__global__ void __launch_bounds__(INJ_THREADS) k_inject_rows(const StepRec* __restrict__ rec,
+                                                             const InjSpecies* __restrict__ isp, int nsp, int ny,
+                                                             uint64_t seed, int32_t* __restrict__ rowmap) {
   // blocks: MAX_INJ_SHIFTS x nsp; rows 1..ny in chunks of the block
   const int c = blockIdx.x / nsp, s = blockIdx.x - c * nsp;
   if (!rec->inj_counter || c >= rec->inj_nshift) return;
   const int64_t n = rec->inj_n[c][s];
   if (n <= 0) return;
   const InjSpecies& S = isp[s];
-  const double dens = rec->inj_dens[c][s];
-  const double x0 = rec->inj_x0[c];
   const uint32_t shift = (uint32_t)rec->inj_shift[c];
-  const int64_t base = rec->inj_base[c][s], id0 = rec->inj_id0[c][s];
+  const int64_t base = rec->inj_base[c][s];
   __shared__ int64_t scan[INJ_THREADS];
   __shared__ int64_t run;
   if (threadIdx.x == 0) run = 0;
   __syncthreads();
   for (int r0 = 1; r0 <= ny; r0 += INJ_THREADS) {
     const int iy = r0 + (int)threadIdx.x;
-    int64_t cnt = 0;
-    if (iy <= ny) {
-      int64_t bit = 0;
-      if (S.frac > 0.0 &&
-          u01(philox4x32_10((uint32_t)iy, shift, (uint32_t)s, TAG_INJ_COUNT, seed).v[0]) < S.frac)
-        bit = 1;
-      cnt = S.nppc + bit;
-    }
+    const int64_t cnt = iy <= ny ? inj_count(S, iy, shift, s, seed) : 0;
     scan[threadIdx.x] = cnt;
     __syncthreads();
     for (int d = 1; d < INJ_THREADS; d <<= 1) {  // inclusive Hillis-Steele scan
@@ -175,42 +177,62 @@ __global__ void __launch_bounds__(INJ_THREADS) k_inject_counter(const StepRec* _
       __syncthreads();
     }
     const int64_t j0 = run + scan[threadIdx.x] - cnt;
-    const double yg = y_grid_min + (double)(iy - 1) * dy;
-    for (int64_t ip = 0; ip < cnt; ++ip) {
-      const int64_t j = j0 + ip;
-      if (j >= n) break;  // the host's count bounds every row (same counter stream)
-      const U4 r = philox4x32_10((uint32_t)j, shift, (uint32_t)s, TAG_INJ_POS, seed);
-      const double cell_frac_y = 0.5 - u01(r.v[0]);
-      const double part_r = yg - cell_frac_y * dy;
-      double sn, cs;
-      cyl_sincos_turn(u01(r.v[1]), &sn, &cs);  // theta = 2 pi U
-      const double px0 = x0 + u01(r.v[2]) * dx;
-      const double wdata = (2.0 * PI * dx * dy * part_r) / (double)cnt;
-      const double cy2 = cell_frac_y * cell_frac_y;
-      const double gyv[3] = {0.5 * ((0.25 + cy2) + cell_frac_y), 0.75 - cy2, 0.5 * ((0.25 + cy2) - cell_frac_y)};
-      double nrm[3];
-      normals3(philox4x32_10((uint32_t)j, shift, (uint32_t)s, TAG_INJ_MOM, seed), nrm[0], nrm[1], nrm[2]);
-      double* q = inj + (base + j) * 8;
-      q[0] = px0;
-      q[1] = part_r * cs;
-      q[2] = part_r * sn;
-      for (int i = 0; i < 3; ++i) {
-        double tl = 0.0, dl = 0.0;
-        for (int k = 0; k < 3; ++k) {
-          tl = tl + gyv[k] * S.temp[i];
-          dl = dl + gyv[k] * S.drift[i];
-        }
-        q[3 + i] = nrm[i] * sqrt(tl * KB * S.mass) + dl;
-      }
-      double wl = 0.0;
-      for (int k = 0; k < 3; ++k) wl = wl + gyv[k] * dens;
-      q[6] = wl * wdata;
-      const int64_t id = id0 + j;
-      q[7] = __longlong_as_double(id);
-    }
+    const int32_t tag = (int32_t)(((uint32_t)c << 28) | ((uint32_t)s << 24) | (uint32_t)iy);
+    for (int64_t ip = 0; ip < cnt && j0 + ip < n; ++ip) rowmap[base + j0 + ip] = tag;
     __syncthreads();
     if (threadIdx.x == INJ_THREADS - 1) run += scan[INJ_THREADS - 1];
     __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(INJ_PART_THREADS) k_inject_particles(const StepRec* __restrict__ rec,
+                                                                       const InjSpecies* __restrict__ isp, int nsp,
+                                                                       double dx, double dy, double y_grid_min,
+                                                                       uint64_t seed, const int32_t* __restrict__ rowmap,
+                                                                       double* __restrict__ inj) {
+  if (!rec->inj_counter) return;
+  const int64_t g0 = rec->inject_off[0];
+  int64_t total = 0;
+  for (int s = 0; s < nsp; ++s) total += rec->inject_cnt[s];
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t g = g0 + t;
+    const uint32_t tag = (uint32_t)rowmap[g];
+    const int c = (int)(tag >> 28), s = (int)((tag >> 24) & 15u), iy = (int)(tag & 0xFFFFFFu);
+    const InjSpecies& S = isp[s];
+    const uint32_t shift = (uint32_t)rec->inj_shift[c];
+    const int64_t j = g - rec->inj_base[c][s];
+    const int64_t cnt = inj_count(S, iy, shift, s, seed);
+    const double dens = rec->inj_dens[c][s];
+    const double yg = y_grid_min + (double)(iy - 1) * dy;
+    const U4 r = philox4x32_10((uint32_t)j, shift, (uint32_t)s, TAG_INJ_POS, seed);
+    const double cell_frac_y = 0.5 - u01(r.v[0]);
+    const double part_r = yg - cell_frac_y * dy;
+    double sn, cs;
+    cyl_sincos_turn(u01(r.v[1]), &sn, &cs);  // theta = 2 pi U
+    const double px0 = rec->inj_x0[c] + u01(r.v[2]) * dx;
+    const double wdata = (2.0 * PI * dx * dy * part_r) / (double)cnt;
+    const double cy2 = cell_frac_y * cell_frac_y;
+    const double gyv[3] = {0.5 * ((0.25 + cy2) + cell_frac_y), 0.75 - cy2, 0.5 * ((0.25 + cy2) - cell_frac_y)};
+    double nrm[3];
+    normals3(philox4x32_10((uint32_t)j, shift, (uint32_t)s, TAG_INJ_MOM, seed), nrm[0], nrm[1], nrm[2]);
+    double* q = inj + g * 8;
+    q[0] = px0;
+    q[1] = part_r * cs;
+    q[2] = part_r * sn;
+    for (int i = 0; i < 3; ++i) {
+      double tl = 0.0, dl = 0.0;
+      for (int k = 0; k < 3; ++k) {
+        tl = tl + gyv[k] * S.temp[i];
+        dl = dl + gyv[k] * S.drift[i];
+      }
+      q[3 + i] = nrm[i] * sqrt(tl * KB * S.mass) + dl;
+    }
+    double wl = 0.0;
+    for (int k = 0; k < 3; ++k) wl = wl + gyv[k] * dens;
+    q[6] = wl * wdata;
+    const int64_t id = rec->inj_id0[c][s] + j;
+    q[7] = __longlong_as_double(id);
   }
 }
 
@@ -226,9 +248,10 @@ void launch_load_particles(cudaStream_t s, const LoadParams& P, const int32_t* v
 }
 
 void launch_inject_counter(cudaStream_t s, const StepRec* rec, const InjSpecies* isp, int nsp, const RunConst& rc,
-                           uint64_t seed, double* inj) {
-  k_inject_counter<<<MAX_INJ_SHIFTS * nsp, INJ_THREADS, 0, s>>>(rec, isp, nsp, rc.ny, rc.dx, rc.dy, rc.y_grid_min,
-                                                                seed, inj);
+                           uint64_t seed, int32_t* rowmap, double* inj) {
+  k_inject_rows<<<MAX_INJ_SHIFTS * nsp, INJ_THREADS, 0, s>>>(rec, isp, nsp, rc.ny, seed, rowmap);
+  k_inject_particles<<<INJ_PART_BLOCKS, INJ_PART_THREADS, 0, s>>>(rec, isp, nsp, rc.dx, rc.dy, rc.y_grid_min, seed,
+                                                                  rowmap, inj);
 }
 
 }  // namespace cyl
