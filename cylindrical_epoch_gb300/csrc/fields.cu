@@ -690,7 +690,41 @@ __device__ void shift_row(FViewT<U> f, int j, int m, const int* bcf, const RunCo
     for (int i = 1 - NG + (int)threadIdx.x; i <= 0; i += (int)blockDim.x) f(i, j, m) = f(nx + i, j, m);
 }
 
-template <typename T>
+// The same shift with the row held in registers: each thread loads all of
+// its elements of the row (strided by the block, at most SHIFT_VPT) before
+// one barrier, then stores each one place to the left (new(i) = old(i + 1)
+// for i < nxg - 1; the last element keeps its value), so a row costs one
+// load round trip instead of one per chunk.  Pure data movement: the FP64
+// form's values are unchanged.
+constexpr int SHIFT_THREADS = 512;
+constexpr int SHIFT_VPT_MAX = 16;  // rows of up to 8192 cells
+
+template <int VPT, typename U>
+__device__ void shift_row_regs(FViewT<U> f, int j, int m, const int* bcf, const RunConst& rc) {
+  const int nxg = rc.nxg, nx = rc.nx;
+  U v[VPT];
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < VPT; ++k) {
+    const int i = k * SHIFT_THREADS + (int)threadIdx.x;
+    if (i >= 1 && i < nxg) v[k] = *f.ptr(1 - NG + i, j, m);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < VPT; ++k) {
+    const int i = k * SHIFT_THREADS + (int)threadIdx.x;
+    if (i >= 1 && i < nxg) *f.ptr(1 - NG + i - 1, j, m) = v[k];
+  }
+  __syncthreads();
+  if (bcf[CYL_BD_X_MAX] == CYL_BC_PERIODIC)
+    for (int i = 1 + (int)threadIdx.x; i <= NG; i += (int)blockDim.x) f(nx + i, j, m) = f(i, j, m);
+  __syncthreads();
+  if (bcf[CYL_BD_X_MIN] == CYL_BC_PERIODIC)
+    for (int i = 1 - NG + (int)threadIdx.x; i <= 0; i += (int)blockDim.x) f(i, j, m) = f(nx + i, j, m);
+}
+
+// VPT: elements per thread of the register path (0: the chunked path)
+template <typename T, int VPT>
 __global__ void k_shift_fields(FieldSetT<T> F, const cplx* cols, const StepRec* rec, int which, RunConst rc) {
   const int j = 1 - NG + (int)blockIdx.x;
   const int m = blockIdx.y;
@@ -698,15 +732,27 @@ __global__ void k_shift_fields(FieldSetT<T> F, const cplx* cols, const StepRec* 
   __shared__ int bcf[4];
   if (threadIdx.x < 4) bcf[threadIdx.x] = rec->bc_field_after[threadIdx.x];
   if (rec->nshift <= which) return;
-  shift_row(F.ex, j, m, bcf, rc);
-  shift_row(F.er, j, m, bcf, rc);
-  shift_row(F.et, j, m, bcf, rc);
-  shift_row(F.bx, j, m, bcf, rc);
-  shift_row(F.br, j, m, bcf, rc);
-  shift_row(F.bt, j, m, bcf, rc);
-  shift_row(F.jx, j, m, bcf, rc);
-  shift_row(F.jr, j, m, bcf, rc);
-  shift_row(F.jt, j, m, bcf, rc);
+  if constexpr (VPT > 0) {
+    shift_row_regs<VPT>(F.ex, j, m, bcf, rc);
+    shift_row_regs<VPT>(F.er, j, m, bcf, rc);
+    shift_row_regs<VPT>(F.et, j, m, bcf, rc);
+    shift_row_regs<VPT>(F.bx, j, m, bcf, rc);
+    shift_row_regs<VPT>(F.br, j, m, bcf, rc);
+    shift_row_regs<VPT>(F.bt, j, m, bcf, rc);
+    shift_row_regs<VPT>(F.jx, j, m, bcf, rc);
+    shift_row_regs<VPT>(F.jr, j, m, bcf, rc);
+    shift_row_regs<VPT>(F.jt, j, m, bcf, rc);
+  } else {
+    shift_row(F.ex, j, m, bcf, rc);
+    shift_row(F.er, j, m, bcf, rc);
+    shift_row(F.et, j, m, bcf, rc);
+    shift_row(F.bx, j, m, bcf, rc);
+    shift_row(F.br, j, m, bcf, rc);
+    shift_row(F.bt, j, m, bcf, rc);
+    shift_row(F.jx, j, m, bcf, rc);
+    shift_row(F.jr, j, m, bcf, rc);
+    shift_row(F.jt, j, m, bcf, rc);
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
     const int ncolv = rc.ny + 2 * NG;
@@ -822,7 +868,12 @@ template <typename T>
 void launch_shift_fields(cudaStream_t s, const FieldSetT<T>& F, const cplx* cols, const StepRec* rec,
                          int which, const RunConst& rc) {
   dim3 grd(rc.nyg, rc.M);
-  k_shift_fields<T><<<grd, 256, 0, s>>>(F, cols, rec, which, rc);
+  const int vpt = (rc.nxg + SHIFT_THREADS - 1) / SHIFT_THREADS;
+  if (vpt <= 4) k_shift_fields<T, 4><<<grd, SHIFT_THREADS, 0, s>>>(F, cols, rec, which, rc);
+  else if (vpt <= 6) k_shift_fields<T, 6><<<grd, SHIFT_THREADS, 0, s>>>(F, cols, rec, which, rc);
+  else if (vpt <= 9) k_shift_fields<T, 9><<<grd, SHIFT_THREADS, 0, s>>>(F, cols, rec, which, rc);
+  else if (vpt <= SHIFT_VPT_MAX) k_shift_fields<T, SHIFT_VPT_MAX><<<grd, SHIFT_THREADS, 0, s>>>(F, cols, rec, which, rc);
+  else k_shift_fields<T, 0><<<grd, 256, 0, s>>>(F, cols, rec, which, rc);
 }
 
 #define INST(T)                                                                                          \
