@@ -19,6 +19,7 @@ CYL_ERR_DEVICE_FLAG = 6
 CYL_ERR_TIMEOUT = 7
 CYL_ERR_OUT_OF_MEMORY = 8
 CYL_ERR_SCRATCH = 9
+CYL_ERR_IO = 10
 NOALLOC_MAX_PARTICLES = 262144  # CYL_NOALLOC_MAX_PARTICLES
 N_TILE_SHAPES = 5  # CYL_N_TILE_SHAPES
 TUNE_SET = 0       # CYL_TUNE_SET
@@ -36,6 +37,7 @@ ERROR_NAMES = {
     CYL_ERR_TIMEOUT: "timed out waiting for the GPU",
     CYL_ERR_OUT_OF_MEMORY: "device out of memory",
     CYL_ERR_SCRATCH: "input larger than the fixed scratch (CYL_NOALLOC_MAX_PARTICLES slots)",
+    CYL_ERR_IO: "file could not be written",
 }
 
 BC_PERIODIC = 1
@@ -57,6 +59,7 @@ PREC_MIXED = 1
 FIELD_NAMES = ["exm", "erm", "etm", "bxm", "brm", "btm", "jxm", "jrm", "jtm",
                "bxm_old", "brm_old", "btm_old", "jxm_old", "jrm_old", "jtm_old"]
 FIELD_INDEX = {n: i for i, n in enumerate(FIELD_NAMES)}
+NFIELDS = len(FIELD_NAMES)  # CYL_NFIELDS
 
 
 class GridDesc(C.Structure):
@@ -106,6 +109,17 @@ class RngState(C.Structure):
         ("x", C.c_int32), ("y", C.c_int32), ("z", C.c_int32), ("w", C.c_int32),
         ("box_muller_cached", C.c_int32),
         ("cached_random_value", C.c_double),
+    ]
+
+
+class SdfDesc(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int32), ("ny", C.c_int32), ("n_mode", C.c_int32),
+        ("step", C.c_int32),
+        ("time", C.c_double),
+        ("xb_min", C.c_double),
+        ("dx", C.c_double), ("dy", C.c_double),
+        ("restart", C.c_int32),
     ]
 
 

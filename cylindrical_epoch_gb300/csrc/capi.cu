@@ -1325,6 +1325,29 @@ int cyl_set_injection_stream(cyl_handle hh, int32_t mode, uint64_t seed) {
   return CYL_OK;
 }
 
+int cyl_write_sdf(cyl_handle hh, const char* path, int32_t restart) {
+  if (!hh || !path) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  const int nf = restart ? CYL_NFIELDS : CYL_F_JTM + 1;
+  std::vector<std::vector<double>> host((size_t)nf, std::vector<double>(h->fcount * 2));
+  const double* arrays[CYL_NFIELDS] = {};
+  for (int k = 0; k < nf; ++k) {
+    if (int r = cyl_download_field(hh, k, host[(size_t)k].data())) return r;
+    arrays[k] = host[(size_t)k].data();
+  }
+  cyl_sdf_desc d{};
+  d.nx = h->g.nx;
+  d.ny = h->g.ny;
+  d.n_mode = h->rc.M;
+  d.step = (int32_t)h->step;
+  d.time = h->time;
+  d.xb_min = h->g.xb_min;
+  d.dx = h->g.dx;
+  d.dy = h->g.dy;
+  d.restart = restart ? 1 : 0;
+  return cyl_sdf_write(path, &d, arrays);
+}
+
 int cyl_download_particles(cyl_handle hh, int32_t isp, double* x, double* y, double* z, double* px,
                            double* py, double* pz, double* w, int64_t* id, int64_t* n_inout) {
   if (!hh || !n_inout) return CYL_ERR_BAD_ARG;

@@ -32,6 +32,8 @@ SIGNATURES = {
     "cyl_load_species_device": (C.c_int, [H, I32, C.c_uint64, I64, PI64]),
     "cyl_set_injection_stream": (C.c_int, [H, I32, C.c_uint64]),
     "cyl_counter_block": (C.c_int, [C.c_uint64, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+    "cyl_sdf_write": (C.c_int, [C.c_char_p, P(abi.SdfDesc), C.POINTER(PD)]),
+    "cyl_write_sdf": (C.c_int, [H, C.c_char_p, I32]),
     "cyl_download_particles": (C.c_int, [H, I32, PD, PD, PD, PD, PD, PD, PD, PI64, PI64]),
     "cyl_upload_field": (C.c_int, [H, I32, PD]),
     "cyl_download_field": (C.c_int, [H, I32, PD]),

@@ -6,6 +6,7 @@ C ABI, performs the start-up sequence and advances steps.  All calls go
 through libcylpic.so; there is no CPU path.
 """
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -96,6 +97,27 @@ def load_counts(deck: Deck):
                                                 None, None, None, C.byref(n)))
         out.append(n.value)
     return out
+
+
+def sdf_write_arrays(path, nx, ny, n_mode, arrays, step=0, time=0.0, xb_min=0.0, dx=1.0, dy=1.0, restart=False):
+    """Write mode arrays as the reference's SDF field dump (cyl_sdf_write).
+    arrays: {name or CYL_F_* index: complex128 array (n_mode, ny+2ng, nx+2ng)}
+    (the layout of Run.field); E, B, J and, with restart, B_old and J_old."""
+    lib = load()
+    d = abi.SdfDesc()
+    d.nx, d.ny, d.n_mode, d.step = int(nx), int(ny), int(n_mode), int(step)
+    d.time, d.xb_min, d.dx, d.dy = float(time), float(xb_min), float(dx), float(dy)
+    d.restart = 1 if restart else 0
+    ptrs = (PD * abi.NFIELDS)()
+    keep = []
+    for name, a in arrays.items():
+        k = abi.FIELD_INDEX[name] if isinstance(name, str) else int(name)
+        a = np.ascontiguousarray(a, dtype=np.complex128)
+        if a.shape != (n_mode, ny + 2 * abi.NG, nx + 2 * abi.NG):
+            raise ValueError(f"{name}: shape {a.shape}")
+        keep.append(a)
+        ptrs[k] = a.view(np.float64).ctypes.data_as(PD)
+    abi.check("cyl_sdf_write", lib.cyl_sdf_write(os.fsencode(path), C.byref(d), ptrs))
 
 
 class Run:
@@ -245,6 +267,11 @@ class Run:
     def step(self, n=1, graph=False):
         fn = self.lib.cyl_step_graph if graph else self.lib.cyl_step
         abi.check("cyl_step", fn(self.h, n))
+
+    def write_sdf(self, path, restart=False):
+        """Dump the mode fields of the current state as the reference's SDF
+        field dump (cyl_write_sdf)."""
+        abi.check("cyl_write_sdf", self.lib.cyl_write_sdf(self.h, os.fsencode(path), 1 if restart else 0))
 
     def step_async(self, n=1):
         """Enqueue n steps (graphs) and return without waiting (cyl_step_async)."""

@@ -49,6 +49,7 @@ extern "C" {
 #define CYL_ERR_TIMEOUT 7        /* a bounded host wait on the GPU ran out   */
 #define CYL_ERR_OUT_OF_MEMORY 8  /* device allocation failed                 */
 #define CYL_ERR_SCRATCH 9        /* input larger than a fixed scratch buffer */
+#define CYL_ERR_IO 10            /* a file could not be written              */
 
 /* ---- boundary codes: the values of constants.F90:56-72 ------------------- */
 #define CYL_BC_PERIODIC 1
@@ -193,6 +194,30 @@ int cyl_upload_particles(cyl_handle h, int32_t ispecies, const double* x,
                          const double* y, const double* z, const double* px,
                          const double* py, const double* pz, const double* w,
                          const int64_t* id, int64_t n);
+/* ---- SDF output of the mode fields ---------------------------------------
+ * The reference's field dump of the mode arrays (write_mode_field,
+ * diagnostics.F90:2033-2110, and the "grid" mesh, 870-882) in SDF, the
+ * reference's file format (SDF/FORTRAN sdf_output_*.f90): per mode array
+ * the blocks "<id>_real" and "<id>_imag", real8 (nx, ny, n_mode) on mesh id
+ * "mode_grid" with the reference's names, units and staggers; the rows of
+ * Ex, Etheta, Br, Jx, Jtheta shifted up by one so that row 1 holds the axis
+ * row 0, as the reference prints them; then the mesh "grid" of the cell
+ * edges.  E, B and J are written; with `restart` also B_old and J_old, and
+ * the header's restart flag is set.
+ * cyl_sdf_write: from host arrays, arrays[CYL_F_*] in the cyl_download_field
+ * layout (NULL leaves an array out); host only.
+ * cyl_write_sdf: the handle's current state (its grid, step and time). */
+typedef struct cyl_sdf_desc {
+  int32_t nx, ny, n_mode;
+  int32_t step;
+  double time;
+  double xb_min;           /* x of the first cell edge (moves with the window) */
+  double dx, dy;
+  int32_t restart;
+} cyl_sdf_desc;
+int cyl_sdf_write(const char* path, const cyl_sdf_desc* desc, const double* const* arrays);
+int cyl_write_sdf(cyl_handle h, const char* path, int32_t restart);
+
 /* Device loading and window injection from a counter-based stream
  * (Philox4x32-10 keyed by seed, one counter per particle) instead of the
  * reference's serial KISS stream: the loader and injector of the reference

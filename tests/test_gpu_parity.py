@@ -272,3 +272,34 @@ def test_async_steps_and_pipelined_diagnostics(gpu_lib, precision):
         for k in ("kinetic_energy", "field_energy_e", "field_energy_b"):
             assert abs(getattr(y, k) - getattr(x, k)) <= tol * abs(getattr(x, k)), k
     assert a.state().n_shifts == b.state().n_shifts > 10
+
+
+@pytest.mark.parametrize("restart", [False, True])
+def test_write_sdf_matches_fields(gpu_lib, tmp_path, restart):
+    """cyl_write_sdf on a windowed run: every block holds the run's own
+    downloaded mode array (rows of the Ex-staggered arrays shifted up by one,
+    as the reference prints them), the grid edges follow the moved window,
+    and the header carries the run's step and time."""
+    from oracle.sdf_read import read
+    deck = _small_wake()
+    run = cg.Run(deck)
+    run.step(48, graph=True)
+    p = tmp_path / "dump.sdf"
+    run.write_sdf(p, restart=restart)
+    h, inline, summary, data = read(p)
+    s = run.state()
+    assert h.step == s.step and h.time == s.time and h.restart_flag == int(restart)
+    assert s.n_shifts > 0
+    ng = abi.NG
+    shifted = {"exm", "etm", "brm", "jxm", "jtm", "brm_old", "jxm_old", "jtm_old"}
+    names = abi.FIELD_NAMES if restart else abi.FIELD_NAMES[:9]
+    assert h.nblocks == 2 * len(names) + 1
+    for name in names:
+        a = run.field(name)
+        sh = 1 if name in shifted else 0
+        for part, v in (("real", a.real), ("imag", a.imag)):
+            assert np.array_equal(data[f"{name}_{part}"], v[:, ng - sh:ng - sh + deck.ny, ng:ng + deck.nx]), name
+    x, y = data["grid"]
+    dx = (deck.x_max - deck.x_min) / deck.nx
+    assert abs(x[0] - s.xb_min) <= 1e-15 * abs(s.xb_min) + 1e-30
+    assert np.allclose(np.diff(x), dx, rtol=1e-12) and y[0] == 0.0
