@@ -18,7 +18,8 @@ def _jobs():
     w.window_start_time = 20 * 5.0e-17
     t64 = cg.thermal_plasma(nx=64, ny=32, ppc=4)
     t32 = cg.thermal_plasma(nx=96, ny=24, ppc=3, precision=abi.PREC_MIXED)
-    return [(w, 48, 1e-6), (t64, 40, 1e-8), (t32, 32, 1e-6)]
+    # 45 and 37 steps: the batched loop takes their last partial chunks alone
+    return [(w, 45, 1e-6), (t64, 40, 1e-8), (t32, 37, 1e-6)]
 
 
 def _rel(a, b):
