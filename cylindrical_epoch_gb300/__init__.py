@@ -10,7 +10,7 @@ the run handle.
 from . import abi, deck
 from .deck import Deck, Laser, Species, thermal_plasma, wakefield, large_wakefield
 from .lib import load
-from .run import Batch, Particles, Run, host_load, sdf_write_arrays
+from .run import Batch, Particles, Run, SdfFile, host_load, sdf_write_arrays
 
 __all__ = ["abi", "deck", "Deck", "Laser", "Species", "thermal_plasma", "wakefield",
-           "large_wakefield", "load", "Particles", "Run", "host_load", "Batch", "sdf_write_arrays"]
+           "large_wakefield", "load", "Particles", "Run", "host_load", "Batch", "sdf_write_arrays", "SdfFile"]

@@ -120,6 +120,30 @@ class SdfDesc(C.Structure):
         ("xb_min", C.c_double),
         ("dx", C.c_double), ("dy", C.c_double),
         ("restart", C.c_int32),
+        ("window_started", C.c_int32),
+        ("dt", C.c_double), ("x_grid_min", C.c_double), ("window_shift_fraction", C.c_double),
+    ]
+
+
+class SdfInfo(C.Structure):
+    _fields_ = [
+        ("step", C.c_int32), ("restart", C.c_int32),
+        ("time", C.c_double),
+        ("nx", C.c_int32), ("ny", C.c_int32), ("n_mode", C.c_int32),
+        ("has_grid", C.c_int32),
+        ("grid_x0", C.c_double), ("grid_x1", C.c_double), ("grid_y0", C.c_double), ("grid_y1", C.c_double),
+        ("has_dt", C.c_int32), ("has_window_shift_fraction", C.c_int32), ("has_x_grid_min", C.c_int32),
+        ("dt", C.c_double), ("window_shift_fraction", C.c_double), ("x_grid_min", C.c_double),
+        ("code_name", C.c_char * 33),
+    ]
+
+
+class SdfSpecies(C.Structure):
+    _fields_ = [
+        ("name", C.c_char_p), ("n", C.c_int64),
+        ("x", C.POINTER(C.c_double)), ("y", C.POINTER(C.c_double)), ("z", C.POINTER(C.c_double)),
+        ("px", C.POINTER(C.c_double)), ("py", C.POINTER(C.c_double)), ("pz", C.POINTER(C.c_double)),
+        ("w", C.POINTER(C.c_double)), ("id", C.POINTER(C.c_int64)),
     ]
 
 

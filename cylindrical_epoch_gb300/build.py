@@ -42,7 +42,7 @@ SOURCES = [
     ("mixed_particles.cu", ["--fmad=true"], "mixed_particles"),
     ("host_deck.cpp", [], "host_deck"),
     ("server.cpp", [], "server"),
-    ("sdf_writer.cpp", [], "sdf_writer"),
+    ("sdf_io.cpp", [], "sdf_io"),
 ]
 
 

@@ -46,6 +46,10 @@ struct HostLaser {
 };
 
 
+// Where a handle stands (Handle::at_output): between full steps, at the
+// output point inside a step, or loaded from a restart dump taken there.
+enum { AT_OUTPUT_NONE = 0, AT_OUTPUT_STEP = 1, AT_OUTPUT_RESTART = 2 };
+
 struct Handle {
   uint64_t serial = 0;  // unique per handle in the process (never reused, unlike the address)
   uint64_t topo_epoch = 0;  // bumped when the kernels of a step change (captured graphs are stale)
@@ -98,6 +102,15 @@ struct Handle {
   bool move_window = false, window_started = false;
   double window_v_x = 0, window_start_time = 0, window_stop_time = 0, wsf = 0;
   int64_t n_shifts = 0;
+  // Output point (cyl_step_to_output, cyl_restart_sdf): AT_OUTPUT_STEP after
+  // the first part of a step (through current_finish), AT_OUTPUT_RESTART after
+  // a restart dump was loaded; out_rec holds that step's record so far.  The
+  // next stepping call finishes the step first.
+  int at_output = 0;
+  StepRec out_rec;
+  // ic_from_restart: a window that starts keeps the restored shift fraction
+  // (window.F90:347)
+  bool from_restart = false;
   std::vector<HostLaser> lasers;
   KissRng rng;
   // staging
@@ -321,8 +334,10 @@ static void inject_counter_step(Handle* h, StepRec& r, int cells, int64_t& inj_u
   }
 }
 
-static void prepare_step(Handle* h, int k, int64_t& inj_used) {
-  StepRec& r = h->h_rec[k];
+// The record fields of a step that its first part (update_eb_fields_half,
+// the push, current_finish) reads: the grid and boundaries before the step's
+// window shift.
+static void step_head_fields(Handle* h, StepRec& r) {
   std::memset(&r, 0, sizeof(r));
   r.time_half = h->time;
   r.nshift_total = (int32_t)h->n_shifts;
@@ -331,8 +346,28 @@ static void prepare_step(Handle* h, int k, int64_t& inj_used) {
     r.bc_field[i] = h->bc_field[i];
     r.add_laser[i] = h->add_laser[i];
   }
+}
+
+// A step up to the reference's output point (epoch2d.F90:259-262): the
+// record's first part, step = step + 1, time = time + dt/2.
+static void step_head(Handle* h, StepRec& r) {
+  step_head_fields(h, r);
   h->step++;
   h->time = h->time + h->g.dt / 2.0;
+}
+
+static void step_tail(Handle* h, int k, int64_t& inj_used);
+
+static void prepare_step(Handle* h, int k, int64_t& inj_used) {
+  step_head(h, h->h_rec[k]);
+  step_tail(h, k, inj_used);
+}
+
+// The rest of a step from the output point: time = time + dt/2
+// (epoch2d.F90:263), the laser sources of update_eb_fields_final and
+// moving_window's host part (window.F90:330-376).
+static void step_tail(Handle* h, int k, int64_t& inj_used) {
+  StepRec& r = h->h_rec[k];
   h->time = h->time + h->g.dt / 2.0;
   r.time_final = h->time;
   r.src_off = (int64_t)k * (int64_t)h->src_per_step;
@@ -347,7 +382,7 @@ static void prepare_step(Handle* h, int k, int64_t& inj_used) {
       if (h->time >= h->window_start_time && h->time < h->window_stop_time) {
         for (int i = 0; i < 4; ++i) h->bc_deck[i] = h->bc_after_move[i];
         setup_boundaries(h);
-        h->wsf = 0.0;
+        if (!h->from_restart) h->wsf = 0.0;
         h->window_started = true;
       }
     }
@@ -446,16 +481,23 @@ static FieldSetT<T> enqueue_step_pre(Handle* h, cudaStream_t s, const StepRec* r
   return F;
 }
 
-// The kernels of one step after the push: current_bcs_r_min_final and
-// current_finish, update_eb_fields_final (fields.f90:341-353), moving_window.
+// The kernels of one step after the push up to the output point:
+// current_bcs_r_min_final and current_finish.
 template <typename T>
-static void enqueue_step_post(Handle* h, cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec,
-                              const double* src) {
+static void enqueue_current_finish(Handle* h, cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec) {
   const RunConst& rc = h->rc;
   FView wk{h->F[15], rc.nxg, rc.nyg};
   launch_current_finish(s, F, rec, rc, h->gd.smooth_currents, h->gd.smooth_its, h->gd.smooth_comp_its,
                         h->gd.smooth_stride > 0 ? h->gd.smooth_stride : 1, wk);
   count_launch(h, 2);
+}
+
+// The kernels of a step after the output point: update_eb_fields_final
+// (fields.f90:341-353) and moving_window.
+template <typename T>
+static void enqueue_step_final(Handle* h, cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec,
+                               const double* src) {
+  const RunConst& rc = h->rc;
   bulk_b(h, s, F, 0);
   launch_b_final_bcs(s, F, rec, src, h->cols, 1, rc.dt, rc);
   bulk_e(h, s, F);
@@ -477,6 +519,14 @@ static void enqueue_step_post(Handle* h, cudaStream_t s, const FieldSetT<T>& F, 
     launch_shift_fields(s, F, h->cols, rec, 1, rc);
     count_launch(h, 2);
   }
+}
+
+// The kernels of one step after the push.
+template <typename T>
+static void enqueue_step_post(Handle* h, cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec,
+                              const double* src) {
+  enqueue_current_finish<T>(h, s, F, rec);
+  enqueue_step_final<T>(h, s, F, rec, src);
 }
 
 // Enqueue the kernels of one step; rec/src point at this step's records.
@@ -1325,9 +1375,13 @@ int cyl_set_injection_stream(cyl_handle hh, int32_t mode, uint64_t seed) {
   return CYL_OK;
 }
 
-int cyl_write_sdf(cyl_handle hh, const char* path, int32_t restart) {
+int cyl_write_sdf(cyl_handle hh, const char* path, int32_t restart, const char* const* species_names) {
   if (!hh || !path) return CYL_ERR_BAD_ARG;
   Handle* h = &hh->h;
+  if (restart && !h->at_output) return CYL_ERR_BAD_ARG;
+  if (species_names)
+    for (int s = 0; s < h->nsp; ++s)
+      if (!species_names[s] || !species_names[s][0]) return CYL_ERR_BAD_ARG;
   const int nf = restart ? CYL_NFIELDS : CYL_F_JTM + 1;
   std::vector<std::vector<double>> host((size_t)nf, std::vector<double>(h->fcount * 2));
   const double* arrays[CYL_NFIELDS] = {};
@@ -1345,7 +1399,112 @@ int cyl_write_sdf(cyl_handle hh, const char* path, int32_t restart) {
   d.dx = h->g.dx;
   d.dy = h->g.dy;
   d.restart = restart ? 1 : 0;
-  return cyl_sdf_write(path, &d, arrays);
+  d.dt = h->g.dt;
+  d.x_grid_min = h->g.x_grid_min;
+  d.window_started = h->move_window && h->window_started ? 1 : 0;
+  d.window_shift_fraction = h->wsf;
+  // the live particles of every species, in device order
+  const int nsp = species_names ? h->nsp : 0;
+  std::vector<std::vector<double>> pd((size_t)nsp);
+  std::vector<std::vector<int64_t>> pid((size_t)nsp);
+  std::vector<cyl_sdf_species> sp((size_t)nsp);
+  for (int s = 0; s < nsp; ++s) {
+    int64_t n = 0;
+    if (int r = cyl_download_particles(hh, s, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                       &n))
+      return r;
+    pd[(size_t)s].resize((size_t)n * 7 + 1);
+    pid[(size_t)s].resize((size_t)n + 1);
+    double* b = pd[(size_t)s].data();
+    const size_t un = (size_t)n;
+    if (int r = cyl_download_particles(hh, s, b, b + un, b + 2 * un, b + 3 * un, b + 4 * un, b + 5 * un, b + 6 * un,
+                                       pid[(size_t)s].data(), &n))
+      return r;
+    cyl_sdf_species& e = sp[(size_t)s];
+    e.name = species_names[s];
+    e.n = n;
+    e.x = b;
+    e.y = b + un;
+    e.z = b + 2 * un;
+    e.px = b + 3 * un;
+    e.py = b + 4 * un;
+    e.pz = b + 5 * un;
+    e.w = b + 6 * un;
+    e.id = pid[(size_t)s].data();
+  }
+  return cyl_sdf_write(path, &d, arrays, sp.data(), nsp);
+}
+
+// restart_data (setup.F90:777-1569) and the restart branch of the start-up
+// (epoch2d.F90:116-153) for this path's state.
+int cyl_restart_sdf(cyl_handle hh, const char* path, const char* const* species_names) {
+  if (!hh || !path) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  if (h->at_output || h->step != 0) return CYL_ERR_BAD_ARG;
+  for (int s = 0; s < h->nsp; ++s) {
+    int64_t n = 0;
+    if (int r = cyl_download_particles(hh, s, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                       nullptr, &n))
+      return r;
+    if (n != 0) return CYL_ERR_BAD_ARG;
+    if (species_names && (!species_names[s] || !species_names[s][0])) return CYL_ERR_BAD_ARG;
+  }
+  cyl_sdf_file f = nullptr;
+  if (int r = cyl_sdf_open(path, &f)) return r;
+  struct Closer {
+    cyl_sdf_file f;
+    ~Closer() { cyl_sdf_close(f); }
+  } closer{f};
+  cyl_sdf_info info;
+  if (int r = cyl_sdf_get_info(f, &info)) return r;
+  // setup.F90:811-830: a restart dump of this code, grid as the deck's
+  if (!info.restart || std::strcmp(info.code_name, "Epoch2d") != 0) return CYL_ERR_BAD_ARG;
+  if (info.nx != h->g.nx || info.ny != h->g.ny || info.n_mode != h->rc.M) return CYL_ERR_BAD_ARG;
+  if (info.has_dt && info.dt > 0.0 && info.dt != h->g.dt) return CYL_ERR_BAD_ARG;
+  if (info.step == 0) return CYL_ERR_UNSUPPORTED;
+  // the mode arrays: zero, then the file's interiors (setup.F90:939-953, 1222-1390)
+  std::vector<double> buf(h->fcount * 2);
+  for (int k = 0; k < CYL_NFIELDS; ++k) {
+    if (int r = cyl_sdf_read_field(f, k, buf.data())) return r;
+    if (int r = cyl_upload_field(hh, k, buf.data())) return r;
+  }
+  // the particles of every named species (ids continue after the largest)
+  for (int s = 0; species_names && s < h->nsp; ++s) {
+    int64_t n = -1;
+    if (int r = cyl_sdf_species_count(f, species_names[s], &n)) return r;
+    if (n <= 0) continue;
+    std::vector<double> v((size_t)n * 7);
+    std::vector<int64_t> id((size_t)n);
+    const size_t un = (size_t)n;
+    double* b = v.data();
+    int64_t got = n;
+    if (int r = cyl_sdf_read_particles(f, species_names[s], b, b + un, b + 2 * un, b + 3 * un, b + 4 * un,
+                                       b + 5 * un, b + 6 * un, id.data(), &got))
+      return r;
+    if (int r = cyl_upload_particles(hh, s, b, b + un, b + 2 * un, b + 3 * un, b + 4 * un, b + 5 * un, b + 6 * un,
+                                     id.data(), got))
+      return r;
+  }
+  // the grid: a window that has moved puts the first edge elsewhere; the
+  // grid is then rebuilt from it and x_grid_min as a window shift builds it
+  if (info.has_grid && info.grid_x0 != h->g.xb_min) {
+    const int64_t shifts = (int64_t)std::llround((info.grid_x0 - h->g.xb_min) / h->g.dx);
+    h->g.xb_min = info.grid_x0;
+    h->g.x_grid_min = info.has_x_grid_min ? info.x_grid_min : h->g.xb_min + 0.5 * h->g.dx;
+    h->g.x_min = h->g.xb_min + h->g.dx * 0.0;
+    h->g.x_max = (h->g.xb_min + (double)(h->g.nx + 1 - 1) * h->g.dx) - h->g.dx * 0.0;
+    h->g.setup_grid_x();
+    h->n_shifts += shifts;
+  }
+  if (info.has_window_shift_fraction) h->wsf = info.window_shift_fraction;
+  h->from_restart = true;
+  h->window_started = false;
+  h->step = info.step;
+  h->time = info.time;
+  step_head_fields(h, h->out_rec);
+  h->at_output = AT_OUTPUT_RESTART;
+  CK(cudaStreamSynchronize(h->st));
+  return CYL_OK;
 }
 
 int cyl_download_particles(cyl_handle hh, int32_t isp, double* x, double* y, double* z, double* px,
@@ -1466,6 +1625,7 @@ int cyl_download_field(cyl_handle hh, int32_t which, double* data) {
 int cyl_initialise(cyl_handle hh) {
   if (!hh) return CYL_ERR_BAD_ARG;
   Handle* h = &hh->h;
+  if (h->at_output) return CYL_ERR_BAD_ARG;
   if (h->copy_pending) CK(cudaEventSynchronize(h->ev_copy));
   StepRec& r = h->h_rec[0];
   std::memset(&r, 0, sizeof(r));
@@ -1505,9 +1665,72 @@ int cyl_initialise(cyl_handle hh) {
   return sync_and_check(h);
 }
 
+// ---------------------------------------------------------------------------
+// The output point inside a step (cyl_step_to_output) and the restart from a
+// dump taken there (cyl_restart_sdf).
+
+extern "C++" {
+// A step's kernels up to the output point: update_eb_fields_half, the push,
+// current_finish.
+template <typename T>
+static void enqueue_step_head(Handle* h, const StepRec* rec) {
+  cudaStream_t s = h->st;
+  const FieldSetT<T> F = enqueue_step_pre<T>(h, s, rec);
+  push_all(h, s, F, rec, 1);
+  enqueue_current_finish<T>(h, s, F, rec);
+}
+
+// The rest of the step stopped at the output point.  After a restart dump
+// was loaded, first the restart start-up of epoch2d.F90:143-153 (particle_bcs,
+// efield_bcs, old_field_bcs), then update_eb_fields_final and moving_window,
+// and the sort that ends every chunk.
+template <typename T>
+static void enqueue_finish(Handle* h, bool restart) {
+  cudaStream_t s = h->st;
+  const FieldSetT<T> F = fieldset_t<T>(h, h->jpar);
+  if (restart) {
+    for (int i = 0; i < h->nsp; ++i) {
+      if (h->prec == CYL_PREC_MIXED)
+        mixed_particle_bcs(s, h->sp[i], h->d_cnt + i, h->d_rec, h->rc, h->nblocks);
+      else
+        launch_particle_bcs(s, h->sp[i], h->d_cnt + i, h->d_rec, 0, h->rc, h->nblocks);
+      count_launch(h, 1);
+    }
+    launch_efield_bcs(s, F, h->d_rec, h->rc);
+    launch_old_field_bcs(s, F, h->d_rec, h->rc);
+    count_launch(h, 2);
+  }
+  enqueue_step_final<T>(h, s, F, h->d_rec, h->d_src);
+  enqueue_sort(h, h->d_rec);
+}
+}  // extern "C++"
+
+static int finish_output(Handle* h) {
+  if (h->at_output == AT_OUTPUT_NONE) return CYL_OK;
+  if (h->copy_pending) CK(cudaEventSynchronize(h->ev_copy));
+  if (int r = flush_push_timing(h)) return r;
+  const bool restart = h->at_output == AT_OUTPUT_RESTART;
+  h->h_rec[0] = h->out_rec;
+  int64_t inj_used = 0;
+  step_tail(h, 0, inj_used);
+  CK(cudaMemcpyAsync(h->d_rec, h->h_rec, sizeof(StepRec), cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(h->d_src, h->h_src, sizeof(double) * h->src_per_step, cudaMemcpyHostToDevice, h->st));
+  if (inj_used > 0 && !h->inj_counter)
+    CK(cudaMemcpyAsync(h->d_inj, h->h_inj, sizeof(double) * 8 * inj_used, cudaMemcpyHostToDevice, h->st));
+  CK(cudaEventRecord(h->ev_copy, h->st));
+  h->copy_pending = true;
+  h->at_output = AT_OUTPUT_NONE;
+  (void)cudaGetLastError();
+  if (h->prec == CYL_PREC_MIXED) enqueue_finish<cplxf>(h, restart);
+  else enqueue_finish<cplx>(h, restart);
+  CK(cudaGetLastError());
+  return CYL_OK;
+}
+
 static int step_impl(cyl_handle hh, int32_t nsteps, bool graph, bool sync = true) {
   if (!hh || nsteps < 0) return CYL_ERR_BAD_ARG;
   Handle* h = &hh->h;
+  if (int r = finish_output(h)) return r;
   while (nsteps > 0) {
     const int k = nsteps < CHUNK ? nsteps : CHUNK;
     int r = run_chunk(h, k, graph);
@@ -1525,6 +1748,26 @@ static int step_impl(cyl_handle hh, int32_t nsteps, bool graph, bool sync = true
   return sync_and_check(h);
 }
 
+int cyl_step_to_output(cyl_handle hh, int32_t nsteps) {
+  if (!hh || nsteps < 1) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  if (int r = step_impl(hh, nsteps - 1, true, false)) return r;
+  if (h->copy_pending) CK(cudaEventSynchronize(h->ev_copy));
+  if (int r = flush_push_timing(h)) return r;
+  StepRec& r = h->h_rec[0];
+  step_head(h, r);
+  h->out_rec = r;
+  CK(cudaMemcpyAsync(h->d_rec, h->h_rec, sizeof(StepRec), cudaMemcpyHostToDevice, h->st));
+  CK(cudaEventRecord(h->ev_copy, h->st));
+  h->copy_pending = true;
+  h->at_output = AT_OUTPUT_STEP;
+  (void)cudaGetLastError();
+  if (h->prec == CYL_PREC_MIXED) enqueue_step_head<cplxf>(h, h->d_rec);
+  else enqueue_step_head<cplx>(h, h->d_rec);
+  CK(cudaGetLastError());
+  return sync_and_check(h);
+}
+
 int cyl_step(cyl_handle hh, int32_t nsteps) { return step_impl(hh, nsteps, false); }
 int cyl_step_graph(cyl_handle hh, int32_t nsteps) { return step_impl(hh, nsteps, true); }
 int cyl_step_async(cyl_handle hh, int32_t nsteps) { return step_impl(hh, nsteps, true, false); }
@@ -1532,6 +1775,7 @@ int cyl_step_async(cyl_handle hh, int32_t nsteps) { return step_impl(hh, nsteps,
 int cyl_push_only(cyl_handle hh) {
   if (!hh) return CYL_ERR_BAD_ARG;
   Handle* h = &hh->h;
+  if (int r = finish_output(h)) return r;
   if (h->copy_pending) CK(cudaEventSynchronize(h->ev_copy));
   if (int r = flush_push_timing(h)) return r;
   StepRec& r = h->h_rec[0];
@@ -1746,6 +1990,7 @@ int cyl_tune_tiles(cyl_handle hh, int32_t mode, int32_t* shape) {
   if (!hh || !shape) return CYL_ERR_BAD_ARG;
   Handle* h = &hh->h;
   if (h->prec != CYL_PREC_MIXED) return CYL_ERR_UNSUPPORTED;
+  if (int r = finish_output(h)) return r;
   if (mode == CYL_TUNE_SET) {
     if (*shape < 0 || *shape >= N_TILE_SHAPES) return CYL_ERR_BAD_ARG;
     set_tile_shape(h, *shape);
@@ -1978,6 +2223,12 @@ int cyl_batch_step(cyl_batch b, const cyl_handle* hs, int32_t n, int32_t nsteps)
   }
   const int nj = (int)jobs.size();
   if (nj > b->cap_jobs) return CYL_ERR_BAD_ARG;
+  // a run stopped at the output point finishes its step on its own stream
+  for (Handle* h : runs)
+    if (h->at_output != AT_OUTPUT_NONE) {
+      if (int rc = finish_output(h)) return rc;
+      CK(cudaStreamSynchronize(h->st));
+    }
   // every run on the batch kernel's tile shape (shape 0), sorted for it
   for (int r = 0; r < n; ++r)
     if (runs[r]->tile_shape != 0) {

@@ -68,6 +68,8 @@ void launch_e_axis_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec
 template <typename T>
 void launch_efield_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc);
 template <typename T>
+void launch_old_field_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc);
+template <typename T>
 void launch_b_axis_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc);
 template <typename T>
 void launch_b_final_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const double* src,

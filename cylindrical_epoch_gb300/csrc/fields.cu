@@ -818,6 +818,12 @@ template <typename T>
 void launch_efield_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc) {
   launch_ghost_bcs<T>(s, F.ex, F.er, F.et, 0, false, bc_ptr(rec), rc);
 }
+// old_field_bcs (boundary.F90:1480-1501): the halo exchange of B_old, Br_old
+// over rows 1-ng .. ny+ng-1.
+template <typename T>
+void launch_old_field_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc) {
+  launch_ghost_bcs<T>(s, F.bxo, F.bro, F.bto, 3, true, bc_ptr(rec), rc);
+}
 template <typename T>
 void launch_b_axis_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc) {
   k_b_axis<T><<<axis_blocks(rc), 128, 0, s>>>(F.bx, F.br, F.bt, F.ex, F.et, bc_const(rc, rc.dt), rc);
@@ -879,6 +885,7 @@ void launch_shift_fields(cudaStream_t s, const FieldSetT<T>& F, const cplx* cols
 #define INST(T)                                                                                          \
   template void launch_e_axis_bcs<T>(cudaStream_t, const FieldSetT<T>&, const StepRec*, const RunConst&);  \
   template void launch_efield_bcs<T>(cudaStream_t, const FieldSetT<T>&, const StepRec*, const RunConst&);  \
+  template void launch_old_field_bcs<T>(cudaStream_t, const FieldSetT<T>&, const StepRec*, const RunConst&); \
   template void launch_b_axis_bcs<T>(cudaStream_t, const FieldSetT<T>&, const StepRec*, const RunConst&);  \
   template void launch_b_final_bcs<T>(cudaStream_t, const FieldSetT<T>&, const StepRec*, const double*,    \
                                       const cplx*, int, double, const RunConst&);                          \

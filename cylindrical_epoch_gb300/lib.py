@@ -32,8 +32,15 @@ SIGNATURES = {
     "cyl_load_species_device": (C.c_int, [H, I32, C.c_uint64, I64, PI64]),
     "cyl_set_injection_stream": (C.c_int, [H, I32, C.c_uint64]),
     "cyl_counter_block": (C.c_int, [C.c_uint64, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
-    "cyl_sdf_write": (C.c_int, [C.c_char_p, P(abi.SdfDesc), C.POINTER(PD)]),
-    "cyl_write_sdf": (C.c_int, [H, C.c_char_p, I32]),
+    "cyl_sdf_write": (C.c_int, [C.c_char_p, P(abi.SdfDesc), C.POINTER(PD), P(abi.SdfSpecies), I32]),
+    "cyl_write_sdf": (C.c_int, [H, C.c_char_p, I32, C.POINTER(C.c_char_p)]),
+    "cyl_sdf_open": (C.c_int, [C.c_char_p, P(H)]),
+    "cyl_sdf_close": (C.c_int, [H]),
+    "cyl_sdf_get_info": (C.c_int, [H, P(abi.SdfInfo)]),
+    "cyl_sdf_read_field": (C.c_int, [H, I32, PD]),
+    "cyl_sdf_species_count": (C.c_int, [H, C.c_char_p, PI64]),
+    "cyl_sdf_read_particles": (C.c_int, [H, C.c_char_p, PD, PD, PD, PD, PD, PD, PD, PI64, PI64]),
+    "cyl_restart_sdf": (C.c_int, [H, C.c_char_p, C.POINTER(C.c_char_p)]),
     "cyl_download_particles": (C.c_int, [H, I32, PD, PD, PD, PD, PD, PD, PD, PI64, PI64]),
     "cyl_upload_field": (C.c_int, [H, I32, PD]),
     "cyl_download_field": (C.c_int, [H, I32, PD]),
@@ -41,6 +48,7 @@ SIGNATURES = {
     "cyl_step": (C.c_int, [H, I32]),
     "cyl_step_graph": (C.c_int, [H, I32]),
     "cyl_step_async": (C.c_int, [H, I32]),
+    "cyl_step_to_output": (C.c_int, [H, I32]),
     "cyl_diagnostics_async": (C.c_int, [H]),
     "cyl_diagnostics_read": (C.c_int, [H, P(abi.Diag)]),
     "cyl_get_run_state": (C.c_int, [H, P(abi.RunState)]),

@@ -99,15 +99,24 @@ def load_counts(deck: Deck):
     return out
 
 
-def sdf_write_arrays(path, nx, ny, n_mode, arrays, step=0, time=0.0, xb_min=0.0, dx=1.0, dy=1.0, restart=False):
+def sdf_write_arrays(path, nx, ny, n_mode, arrays, step=0, time=0.0, xb_min=0.0, dx=1.0, dy=1.0, restart=False,
+                     species=None, dt=0.0, x_grid_min=None, window_shift_fraction=None):
     """Write mode arrays as the reference's SDF field dump (cyl_sdf_write).
     arrays: {name or CYL_F_* index: complex128 array (n_mode, ny+2ng, nx+2ng)}
-    (the layout of Run.field); E, B, J and, with restart, B_old and J_old."""
+    (the layout of Run.field); E, B, J and, with restart, B_old and J_old.
+    species: [(name, Particles)] written as the reference's particle
+    variables and point meshes.  Restart dumps also carry dt (when > 0),
+    x_grid_min (default: the first cell centre) and window_shift_fraction
+    (when given: the window has started)."""
     lib = load()
     d = abi.SdfDesc()
     d.nx, d.ny, d.n_mode, d.step = int(nx), int(ny), int(n_mode), int(step)
     d.time, d.xb_min, d.dx, d.dy = float(time), float(xb_min), float(dx), float(dy)
     d.restart = 1 if restart else 0
+    d.dt = float(dt)
+    d.x_grid_min = float(xb_min + 0.5 * dx if x_grid_min is None else x_grid_min)
+    d.window_started = 0 if window_shift_fraction is None else 1
+    d.window_shift_fraction = float(window_shift_fraction or 0.0)
     ptrs = (PD * abi.NFIELDS)()
     keep = []
     for name, a in arrays.items():
@@ -117,7 +126,75 @@ def sdf_write_arrays(path, nx, ny, n_mode, arrays, step=0, time=0.0, xb_min=0.0,
             raise ValueError(f"{name}: shape {a.shape}")
         keep.append(a)
         ptrs[k] = a.view(np.float64).ctypes.data_as(PD)
-    abi.check("cyl_sdf_write", lib.cyl_sdf_write(os.fsencode(path), C.byref(d), ptrs))
+    species = list(species or [])
+    sp = (abi.SdfSpecies * max(1, len(species)))()
+    for i, (name, p) in enumerate(species):
+        e = sp[i]
+        e.name = name.encode()
+        e.n = p.n
+        for k in ("x", "y", "z", "px", "py", "pz", "w"):
+            a = np.ascontiguousarray(getattr(p, k), dtype=np.float64)
+            keep.append(a)
+            setattr(e, k, a.ctypes.data_as(PD))
+        a = np.ascontiguousarray(p.id, dtype=np.int64)
+        keep.append(a)
+        e.id = a.ctypes.data_as(PI64)
+    abi.check("cyl_sdf_write", lib.cyl_sdf_write(os.fsencode(path), C.byref(d), ptrs, sp, len(species)))
+
+
+class SdfFile:
+    """An SDF file opened by the restart reader (cyl_sdf_open): `info`
+    (cyl_sdf_info), `field(name)` and `particles(species)`."""
+
+    def __init__(self, path):
+        self.lib = load()
+        h = C.c_void_p()
+        abi.check("cyl_sdf_open", self.lib.cyl_sdf_open(os.fsencode(path), C.byref(h)))
+        self.h = h
+        self.info = abi.SdfInfo()
+        abi.check("cyl_sdf_get_info", self.lib.cyl_sdf_get_info(self.h, C.byref(self.info)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.cyl_sdf_close(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def field(self, name):
+        """A mode array in the layout of Run.field (zero ghosts)."""
+        which = abi.FIELD_INDEX[name] if isinstance(name, str) else int(name)
+        i = self.info
+        out = np.zeros((i.n_mode, i.ny + 2 * abi.NG, i.nx + 2 * abi.NG), dtype=np.complex128)
+        abi.check("cyl_sdf_read_field", self.lib.cyl_sdf_read_field(self.h, which, _p(out.view(np.float64))))
+        return out
+
+    def species_count(self, name):
+        n = C.c_int64(0)
+        abi.check("cyl_sdf_species_count", self.lib.cyl_sdf_species_count(self.h, name.encode(), C.byref(n)))
+        return n.value
+
+    def particles(self, name):
+        n = self.species_count(name)
+        if n < 0:
+            raise KeyError(name)
+        p = Particles(n)
+        got = C.c_int64(n)
+        abi.check("cyl_sdf_read_particles",
+                  self.lib.cyl_sdf_read_particles(self.h, name.encode(), _p(p.x), _p(p.y), _p(p.z), _p(p.px),
+                                                  _p(p.py), _p(p.pz), _p(p.w), p.id.ctypes.data_as(PI64),
+                                                  C.byref(got)))
+        return p
 
 
 class Run:
@@ -268,10 +345,50 @@ class Run:
         fn = self.lib.cyl_step_graph if graph else self.lib.cyl_step
         abi.check("cyl_step", fn(self.h, n))
 
-    def write_sdf(self, path, restart=False):
-        """Dump the mode fields of the current state as the reference's SDF
-        field dump (cyl_write_sdf)."""
-        abi.check("cyl_write_sdf", self.lib.cyl_write_sdf(self.h, os.fsencode(path), 1 if restart else 0))
+    def step_to_output(self, n=1):
+        """Advance to the reference's output point of the n-th step
+        (cyl_step_to_output); the next stepping call finishes that step."""
+        abi.check("cyl_step_to_output", self.lib.cyl_step_to_output(self.h, n))
+
+    @classmethod
+    def from_sdf(cls, deck: Deck, path, rng_mode=abi.RNG_KISS, counter_seed=None):
+        """A run restarted from a restart dump of the same deck
+        (cyl_restart_sdf), at the output point of the dumped step."""
+        with SdfFile(path) as f:
+            counts = [max(f.species_count(s.name), 0) for s in deck.species]
+        self = cls.__new__(cls)
+        self.lib = load()
+        self.deck = deck
+        g = deck.grid_desc()
+        self.dt = g.dt
+        sp = deck.species_descs()
+        for i, n in enumerate(counts):
+            if sp[i].capacity < n + 1024:
+                sp[i].capacity = int(n * 1.1) + 4096
+        las, self._keep = deck.laser_descs()
+        rng = abi.RngState()
+        self.lib.cyl_rng_init(C.byref(rng), deck.seed)
+        h = C.c_void_p()
+        abi.check("cyl_create", self.lib.cyl_create(C.byref(g), sp, len(deck.species), las, len(deck.lasers),
+                                                    C.byref(rng), C.byref(h)))
+        self.h = h
+        self.nxg = deck.nx + 2 * abi.NG
+        self.nyg = deck.ny + 2 * abi.NG
+        if rng_mode == abi.RNG_COUNTER:
+            seed = deck.seed if counter_seed is None else int(counter_seed)
+            abi.check("cyl_set_injection_stream", self.lib.cyl_set_injection_stream(self.h, abi.RNG_COUNTER, seed))
+        names = (C.c_char_p * len(deck.species))(*[s.name.encode() for s in deck.species])
+        abi.check("cyl_restart_sdf", self.lib.cyl_restart_sdf(self.h, os.fsencode(path), names))
+        return self
+
+    def write_sdf(self, path, restart=False, particles=True):
+        """Dump the current state as the reference's SDF output
+        (cyl_write_sdf): the mode fields and, with particles, every species'
+        live particles under the deck's species names."""
+        names = None
+        if particles:
+            names = (C.c_char_p * len(self.deck.species))(*[s.name.encode() for s in self.deck.species])
+        abi.check("cyl_write_sdf", self.lib.cyl_write_sdf(self.h, os.fsencode(path), 1 if restart else 0, names))
 
     def step_async(self, n=1):
         """Enqueue n steps (graphs) and return without waiting (cyl_step_async)."""

@@ -204,9 +204,26 @@ int cyl_upload_particles(cyl_handle h, int32_t ispecies, const double* x,
  * row 0, as the reference prints them; then the mesh "grid" of the cell
  * edges.  E, B and J are written; with `restart` also B_old and J_old, and
  * the header's restart flag is set.
+ * Particles follow as the reference writes them (write_particle_variable,
+ * write_particle_grid): per species the point variables weight, px, py, pz
+ * (real8) and id (integer8), "<var>/<species>" on mesh "grid/<species>",
+ * then the 3D point mesh "grid/<species>" of the Cartesian positions.
  * cyl_sdf_write: from host arrays, arrays[CYL_F_*] in the cyl_download_field
- * layout (NULL leaves an array out); host only.
- * cyl_write_sdf: the handle's current state (its grid, step and time). */
+ * layout (NULL leaves an array out), species[0..nspecies) particle arrays;
+ * host only.
+ * A restart dump (restart != 0) first holds the constants the restart reads
+ * back (diagnostics.F90:407-416): "dt", "window_shift_fraction" (only once the
+ * window has started) and "x_grid_min".
+ * cyl_sdf_write: from host arrays, arrays[CYL_F_*] in the cyl_download_field
+ * layout (NULL leaves an array out), species[0..nspecies) particle arrays;
+ * host only.
+ * cyl_write_sdf: the handle's current state (its grid, step, time and live
+ * particles); species_names[i] names species i (NULL: no particles).  The
+ * reference writes its dumps at the output point inside a step
+ * (epoch2d.F90:259-262, see cyl_step_to_output); between full steps the
+ * state is the one after moving_window instead.  A restart dump is only
+ * written at the output point (CYL_ERR_BAD_ARG otherwise), since the
+ * restart finishes the step it stopped in. */
 typedef struct cyl_sdf_desc {
   int32_t nx, ny, n_mode;
   int32_t step;
@@ -214,9 +231,73 @@ typedef struct cyl_sdf_desc {
   double xb_min;           /* x of the first cell edge (moves with the window) */
   double dx, dy;
   int32_t restart;
+  /* restart dumps only */
+  int32_t window_started;  /* write window_shift_fraction */
+  double dt;               /* written when > 0 */
+  double x_grid_min;
+  double window_shift_fraction;
 } cyl_sdf_desc;
-int cyl_sdf_write(const char* path, const cyl_sdf_desc* desc, const double* const* arrays);
-int cyl_write_sdf(cyl_handle h, const char* path, int32_t restart);
+typedef struct cyl_sdf_species {
+  const char* name;
+  int64_t n;
+  const double *x, *y, *z, *px, *py, *pz, *w;
+  const int64_t* id;
+} cyl_sdf_species;
+int cyl_sdf_write(const char* path, const cyl_sdf_desc* desc, const double* const* arrays,
+                  const cyl_sdf_species* species, int32_t nspecies);
+int cyl_write_sdf(cyl_handle h, const char* path, int32_t restart, const char* const* species_names);
+
+/* ---- SDF input: the restart reader ---------------------------------------
+ * Reads the SDF files above as restart_data does (setup.F90:777-1569):
+ * cyl_sdf_read_field gives a mode array in the cyl_download_field layout,
+ * zero where the file has no block and in the ghost cells, the interior
+ * from "<id>_real" / "<id>_imag" (the rows of the shifted arrays moved back
+ * down by one, setup.F90:1237-1247); species are found by the point mesh
+ * whose species id (or block id "grid/<name>") is the name, and their
+ * point variables by species id or mesh id; a point variable whose count
+ * differs from its mesh's is an error (setup.F90:1411-1425).  Host only.
+ * Errors: CYL_ERR_IO for a file that cannot be read or is not SDF,
+ * CYL_ERR_BAD_ARG for an array or species the file does not describe. */
+typedef struct cyl_sdf_file_s* cyl_sdf_file;
+typedef struct cyl_sdf_info {
+  int32_t step, restart;
+  double time;
+  int32_t nx, ny, n_mode;      /* from the mode blocks (0 without any) */
+  int32_t has_grid;            /* the "grid" mesh: x edges [x0, x1], y [y0, y1] */
+  double grid_x0, grid_x1, grid_y0, grid_y1;
+  int32_t has_dt, has_window_shift_fraction, has_x_grid_min;
+  double dt, window_shift_fraction, x_grid_min;
+  char code_name[33];
+} cyl_sdf_info;
+int cyl_sdf_open(const char* path, cyl_sdf_file* out);
+int cyl_sdf_close(cyl_sdf_file f);
+int cyl_sdf_get_info(cyl_sdf_file f, cyl_sdf_info* out);
+int cyl_sdf_read_field(cyl_sdf_file f, int32_t which, double* data);
+/* *n_out = the species' particle count, -1 when the file has none of it. */
+int cyl_sdf_species_count(cyl_sdf_file f, const char* name, int64_t* n_out);
+/* n_inout in: capacity; out: particles written.  Variables absent from the
+ * file read as zeros. */
+int cyl_sdf_read_particles(cyl_sdf_file f, const char* name, double* x, double* y, double* z,
+                           double* px, double* py, double* pz, double* w, int64_t* id,
+                           int64_t* n_inout);
+
+/* Load a restart dump into a handle created from the same deck, with no
+ * particles loaded, as restart_data and the restart start-up of
+ * epoch2d.F90:116-153 do: the mode arrays and every named species' particles
+ * from the file (species_names[i] names species i; species the file lacks
+ * stay empty), step and time from the header, the window's shift fraction,
+ * x_grid_min and the grid edges from their blocks.  The handle is left at
+ * the output point of the dumped step; the next stepping call runs
+ * particle_bcs, efield_bcs, old_field_bcs, time = time + dt/2,
+ * update_eb_fields_final and moving_window, then its steps.  The window
+ * restarts as in the reference (window_started false, kept shift fraction),
+ * ids continue from the largest loaded id + 1, and the host random stream
+ * is the one the handle was created with (the reference's non-exact
+ * restart).  Errors: CYL_ERR_IO (file), CYL_ERR_BAD_ARG (not a restart dump,
+ * another code, grid or mode count or dt unlike the handle's, particles
+ * already loaded), CYL_ERR_UNSUPPORTED (a step-0 dump, which a fresh start
+ * replaces), CYL_ERR_CAPACITY (a species larger than its capacity). */
+int cyl_restart_sdf(cyl_handle h, const char* path, const char* const* species_names);
 
 /* Device loading and window injection from a counter-based stream
  * (Philox4x32-10 keyed by seed, one counter per particle) instead of the
@@ -274,6 +355,17 @@ int cyl_step_graph(cyl_handle h, int32_t nsteps);
  * these steps is reported by the next call that syncs (cyl_diagnostics,
  * cyl_diagnostics_read's device_error, cyl_get_run_state, downloads). */
 int cyl_step_async(cyl_handle h, int32_t nsteps);
+/* Advance to the reference's output point of the nsteps-th step
+ * (nsteps >= 1): nsteps - 1 full steps, then of the last one
+ * update_eb_fields_half, the push and current_finish, with step = step + 1
+ * and time = time + dt/2 -- the state output_routines(step) sees
+ * (epoch2d.F90:259-262).  Downloads, cyl_write_sdf, cyl_get_run_state and
+ * diagnostics then read that state.  The next stepping call (cyl_step*,
+ * cyl_batch_step, cyl_push_only, cyl_tune_tiles, with nsteps 0 too) first
+ * finishes the step: time = time + dt/2, update_eb_fields_final,
+ * moving_window (epoch2d.F90:263-265).  Fields and particles after
+ * finishing equal those of nsteps full steps. */
+int cyl_step_to_output(cyl_handle h, int32_t nsteps);
 
 int cyl_get_run_state(cyl_handle h, cyl_run_state* out);
 int cyl_diagnostics(cyl_handle h, cyl_diag* out);

@@ -228,6 +228,7 @@ struct Sim {
   int bc_after_move[4];
   int64_t n_shifts;
   int64_t next_id;
+  bool from_restart = false;  // ic_from_restart: a starting window keeps its shift fraction
   bool inj_counter = false;  // window injection from the counter stream
   uint64_t inj_seed = 0;
   Field ex, er, et, bx, br, bt, jx, jr, jt, bx_old, br_old, bt_old, jx_old, jr_old, jt_old;
@@ -1650,7 +1651,7 @@ void moving_window(Sim& s) {
     if (s.time >= s.window_start_time && s.time < s.window_stop_time) {
       for (int i = 0; i < 4; ++i) s.bc_deck[i] = s.bc_after_move[i];
       s.setup_boundaries();
-      s.window_shift_fraction = 0.0;
+      if (!s.from_restart) s.window_shift_fraction = 0.0;  // window.F90:347
       s.window_started = true;
     }
   }
@@ -1684,8 +1685,8 @@ void update_eb_fields_final(Sim& s) {
   efield_bcs(s);
 }
 
-// One iteration of the driver loop (epoch2d.F90:213-265)
-void one_step(Sim& s) {
+// One iteration of the driver loop up to output_routines (epoch2d.F90:213-262)
+void step_to_output(Sim& s) {
   update_eb_fields_half(s);
   push_particles_core(s);
   current_bcs_r_min_final(s);
@@ -1693,9 +1694,17 @@ void one_step(Sim& s) {
   current_finish(s);
   s.step++;
   s.time = s.time + s.dt / 2.0;
+}
+// ... and the rest of it (epoch2d.F90:263-265)
+void finish_step(Sim& s) {
   s.time = s.time + s.dt / 2.0;
   update_eb_fields_final(s);
   moving_window(s);
+}
+// One iteration of the driver loop (epoch2d.F90:213-265)
+void one_step(Sim& s) {
+  step_to_output(s);
+  finish_step(s);
 }
 
 void compute_bc_allspecies(Sim& s) {
@@ -2151,6 +2160,52 @@ int orc_initialise(orc_handle h) {
 int orc_step(orc_handle h, int32_t nsteps) {
   Sim* s = (Sim*)h;
   for (int i = 0; i < nsteps; ++i) one_step(*s);
+  return CYL_OK;
+}
+
+// Advance to the output point of the n-th step (n - 1 full steps, then the
+// first part of the last one).
+int orc_step_to_output(orc_handle h, int32_t nsteps) {
+  Sim* s = (Sim*)h;
+  if (nsteps < 1) return CYL_ERR_BAD_ARG;
+  for (int i = 0; i < nsteps - 1; ++i) one_step(*s);
+  step_to_output(*s);
+  return CYL_OK;
+}
+int orc_finish_step(orc_handle h) {
+  finish_step(*(Sim*)h);
+  return CYL_OK;
+}
+
+// restart_data (setup.F90:777-1569) for the scalars, on fields and particles
+// already set (orc_set_field, orc_set_particles), then the restart start-up
+// (epoch2d.F90:143-153): particle_bcs, efield_bcs, old_field_bcs
+// (boundary.F90:1480-1501) and the rest of the dumped step.  A window that
+// has moved (xb_min differs) rebuilds the grid as a shift does.
+int orc_restart(orc_handle h, int64_t step, double time, double xb_min, double x_grid_min, int32_t has_wsf,
+                double wsf) {
+  Sim& s = *(Sim*)h;
+  if (step < 1) return CYL_ERR_UNSUPPORTED;
+  if (xb_min != s.xb_min) {
+    const int64_t shifts = (int64_t)std::llround((xb_min - s.xb_min) / s.dx);
+    s.xb_min = xb_min;
+    s.x_grid_min = x_grid_min;
+    s.x_min = s.xb_min + s.dx * 0.0;
+    s.x_max = (s.xb_min + (double)(s.nx + 1 - 1) * s.dx) - s.dx * 0.0;
+    s.setup_grid_x();
+    s.n_shifts += shifts;
+  }
+  if (has_wsf) s.window_shift_fraction = wsf;
+  s.from_restart = true;
+  s.window_started = false;
+  s.step = step;
+  s.time = time;
+  particle_bcs(s);
+  efield_bcs(s);
+  halo_full(s, s.bx_old);
+  halo_shifted(s, s.br_old);
+  halo_full(s, s.bt_old);
+  finish_step(s);
   return CYL_OK;
 }
 

@@ -68,6 +68,9 @@ def load():
         "orc_set_rng": (C.c_int, [H, C.POINTER(abi.RngState)]),
         "orc_initialise": (C.c_int, [H]),
         "orc_step": (C.c_int, [H, C.c_int32]),
+        "orc_step_to_output": (C.c_int, [H, C.c_int32]),
+        "orc_finish_step": (C.c_int, [H]),
+        "orc_restart": (C.c_int, [H, C.c_int64, C.c_double, C.c_double, C.c_double, C.c_int32, C.c_double]),
         "orc_stage": (C.c_int, [H, C.c_int32]),
         "orc_get_run_state": (C.c_int, [H, C.POINTER(abi.RunState)]),
         "orc_diagnostics": (C.c_int, [H, C.POINTER(abi.Diag)]),
@@ -180,6 +183,21 @@ class Oracle:
 
     def step(self, n=1):
         self.lib.orc_step(self.h, n)
+
+    def step_to_output(self, n=1):
+        if self.lib.orc_step_to_output(self.h, n) != 0:
+            raise RuntimeError("orc_step_to_output")
+
+    def finish_step(self):
+        self.lib.orc_finish_step(self.h)
+
+    def restart(self, step, time, xb_min, x_grid_min, window_shift_fraction=None):
+        """The restart of a dump's scalars, after set_field / set_particles
+        (orc_restart)."""
+        rc = self.lib.orc_restart(self.h, int(step), float(time), float(xb_min), float(x_grid_min),
+                                  0 if window_shift_fraction is None else 1, float(window_shift_fraction or 0.0))
+        if rc != 0:
+            raise RuntimeError(f"orc_restart: {rc}")
 
     def stage(self, name):
         rc = self.lib.orc_stage(self.h, STAGE[name])

@@ -9,7 +9,10 @@ first_block_location, each a block header (next, data location, id,
 data length, block type, data type, ndims, name, block-info length) with
 type-specific metadata; and a summary at summary_location repeating every
 block header and metadata.  Only the block types the product writes are
-decoded (plain mesh 1, plain variable 3).  Parity status: unpinned -- the
+decoded (plain mesh 1, point mesh 2, plain variable 3, point variable 4,
+constant 5; sdf_output_point_ru.f90 for the point types, sdf_output_ru.f90
+write_constant_meta for constants: the value in the metadata, no data).
+Parity status: unpinned -- the
 reference's SDF reader needs a header its build generates and no SDF files
 ship with the reference, so this restatement is the only reader here.
 """
@@ -77,6 +80,32 @@ def _block(buf, at, h):
         p += 16 * nd
         b["dims"] = list(struct.unpack_from("<" + "i" * nd, buf, p))
         meta = 8 * nd + 2 * ids * nd + 4 + 16 * nd + 4 * nd
+    elif b["blocktype"] == 2:  # point mesh
+        b["mults"] = list(struct.unpack_from("<" + "d" * nd, buf, o))
+        p = o + 8 * nd
+        b["labels"] = [_str(buf[p + ids * i:p + ids * (i + 1)]) for i in range(nd)]
+        p += ids * nd
+        b["units"] = [_str(buf[p + ids * i:p + ids * (i + 1)]) for i in range(nd)]
+        p += ids * nd
+        (b["geometry"],) = struct.unpack_from("<i", buf, p)
+        p += 4
+        b["extents"] = list(struct.unpack_from("<" + "d" * (2 * nd), buf, p))
+        p += 16 * nd
+        (b["npoints"],) = struct.unpack_from("<q", buf, p)
+        b["species_id"] = _str(buf[p + 8:p + 8 + ids])
+        meta = 8 * nd + 2 * ids * nd + 4 + 16 * nd + 8 + ids
+    elif b["blocktype"] == 4:  # point variable
+        (b["mult"],) = struct.unpack_from("<d", buf, o)
+        b["units"] = _str(buf[o + 8:o + 8 + ids])
+        b["mesh_id"] = _str(buf[o + 8 + ids:o + 8 + 2 * ids])
+        (b["npoints"],) = struct.unpack_from("<q", buf, o + 8 + 2 * ids)
+        b["species_id"] = _str(buf[o + 16 + 2 * ids:o + 16 + 3 * ids])
+        meta = 16 + 3 * ids
+    elif b["blocktype"] == 5:  # constant
+        fmt = {4: "<d", 2: "<q", 1: "<i"}[b["datatype"]]
+        (b["value"],) = struct.unpack_from(fmt, buf, o)
+        meta = struct.calcsize(fmt)
+        assert b["data_length"] == 0
     else:
         meta = b["info_length"]
     assert b["info_length"] == meta, (b["id"], b["info_length"], meta)
@@ -84,8 +113,13 @@ def _block(buf, at, h):
 
 
 def _data(buf, b):
-    assert b["datatype"] == 4, "real8 only"
-    a = np.frombuffer(buf, dtype="<f8", count=b["data_length"] // 8, offset=b["data_location"])
+    assert b["datatype"] in (2, 4), "integer8 and real8 only"
+    dt = "<i8" if b["datatype"] == 2 else "<f8"
+    a = np.frombuffer(buf, dtype=dt, count=b["data_length"] // 8, offset=b["data_location"])
+    if b["blocktype"] == 2:
+        return a.reshape(b["ndims"], b["npoints"]).copy()  # one row per dimension
+    if b["blocktype"] == 4:
+        return a.copy()
     if b["blocktype"] == 3:
         return a.reshape(b["dims"][::-1])  # Fortran order: (n_mode, ny, nx)
     if b["blocktype"] == 1:
@@ -109,6 +143,6 @@ def read(path):
         b = _block(buf, at, h)
         summary.append(b)
         at = b["next_block_location"]
-    data = {b["id"]: _data(buf, b) for b in summary}
+    data = {b["id"]: (b["value"] if b["blocktype"] == 5 else _data(buf, b)) for b in summary}
     h.file_size = len(buf)
     return h, inline, summary, data

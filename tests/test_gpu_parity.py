@@ -278,12 +278,16 @@ def test_async_steps_and_pipelined_diagnostics(gpu_lib, precision):
 def test_write_sdf_matches_fields(gpu_lib, tmp_path, restart):
     """cyl_write_sdf on a windowed run: every block holds the run's own
     downloaded mode array (rows of the Ex-staggered arrays shifted up by one,
-    as the reference prints them), the grid edges follow the moved window,
-    and the header carries the run's step and time."""
+    as the reference prints them), every species' particle blocks hold its
+    downloaded live particles, the grid edges follow the moved window, and
+    the header carries the run's step and time."""
     from oracle.sdf_read import read
     deck = _small_wake()
     run = cg.Run(deck)
-    run.step(48, graph=True)
+    if restart:
+        run.step_to_output(48)  # restart dumps are taken at the output point
+    else:
+        run.step(48, graph=True)
     p = tmp_path / "dump.sdf"
     run.write_sdf(p, restart=restart)
     h, inline, summary, data = read(p)
@@ -293,7 +297,17 @@ def test_write_sdf_matches_fields(gpu_lib, tmp_path, restart):
     ng = abi.NG
     shifted = {"exm", "etm", "brm", "jxm", "jtm", "brm_old", "jxm_old", "jtm_old"}
     names = abi.FIELD_NAMES if restart else abi.FIELD_NAMES[:9]
-    assert h.nblocks == 2 * len(names) + 1
+    sp = [(s_.name, run.particles(i)) for i, s_ in enumerate(deck.species)]
+    live = [(n_, p_) for n_, p_ in sp if p_.n > 0]
+    nconst = (3 if s.window_started else 2) if restart else 0  # dt, window_shift_fraction, x_grid_min
+    assert live and h.nblocks == nconst + 2 * len(names) + 6 * len(live) + 1
+    if restart:
+        assert data["dt"] == run.dt and data["x_grid_min"] == s.x_grid_min
+        assert data.get("window_shift_fraction", 0.0) == (s.window_shift_fraction if s.window_started else 0.0)
+    for n_, p_ in live:
+        assert np.array_equal(data[f"grid/{n_}"], np.stack([p_.x, p_.y, p_.z]))
+        for v, k in (("weight", "w"), ("px", "px"), ("py", "py"), ("pz", "pz"), ("id", "id")):
+            assert np.array_equal(data[f"{v}/{n_}"], getattr(p_, k)), (v, n_)
     for name in names:
         a = run.field(name)
         sh = 1 if name in shifted else 0
