@@ -111,6 +111,7 @@ struct Handle {
   // ic_from_restart: a window that starts keeps the restored shift fraction
   // (window.F90:347)
   bool from_restart = false;
+  bool restart_wsf = false;  // the loaded dump held window_shift_fraction
   std::vector<HostLaser> lasers;
   KissRng rng;
   // staging
@@ -1401,7 +1402,10 @@ int cyl_write_sdf(cyl_handle hh, const char* path, int32_t restart, const char* 
   d.restart = restart ? 1 : 0;
   d.dt = h->g.dt;
   d.x_grid_min = h->g.x_grid_min;
-  d.window_started = h->move_window && h->window_started ? 1 : 0;
+  // a run loaded from a dump restarts its window at its first moving_window;
+  // until then the loaded shift fraction is still the one to keep
+  const bool started = h->window_started || (h->at_output == AT_OUTPUT_RESTART && h->restart_wsf);
+  d.window_started = h->move_window && started ? 1 : 0;
   d.window_shift_fraction = h->wsf;
   // the live particles of every species, in device order
   const int nsp = species_names ? h->nsp : 0;
@@ -1497,6 +1501,7 @@ int cyl_restart_sdf(cyl_handle hh, const char* path, const char* const* species_
     h->n_shifts += shifts;
   }
   if (info.has_window_shift_fraction) h->wsf = info.window_shift_fraction;
+  h->restart_wsf = info.has_window_shift_fraction != 0;
   h->from_restart = true;
   h->window_started = false;
   h->step = info.step;

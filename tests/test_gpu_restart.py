@@ -143,3 +143,24 @@ def test_restart_rules(gpu_lib, tmp_path):
     # steps after the output point continue
     run.step(2)
     assert run.state().step == 7
+
+
+def test_restart_dump_of_loaded_run_keeps_shift_fraction(gpu_lib, tmp_path):
+    """A run loaded from a dump restarts its window at its first
+    moving_window; a restart dump written before that still carries the
+    loaded shift fraction, and the rest of the state as loaded."""
+    from oracle.sdf_read import read
+    deck = _deck()
+    a = cg.Run(deck, rng_mode=abi.RNG_COUNTER, counter_seed=9)
+    a.step_to_output(DUMP_STEP)
+    p1, p2 = tmp_path / "first.sdf", tmp_path / "second.sdf"
+    a.write_sdf(p1, restart=True)
+    b = cg.Run.from_sdf(deck, p1, rng_mode=abi.RNG_COUNTER, counter_seed=9)
+    b.write_sdf(p2, restart=True)
+    h1, _, _, d1 = read(p1)
+    h2, _, _, d2 = read(p2)
+    assert (h2.step, h2.time, h2.nblocks) == (h1.step, h1.time, h1.nblocks)
+    assert d2["window_shift_fraction"] == d1["window_shift_fraction"] > 0.5
+    for k in d1:
+        if k != "grid":
+            assert np.array_equal(np.asarray(d2[k]), np.asarray(d1[k])), k
