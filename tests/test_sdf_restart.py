@@ -161,3 +161,21 @@ def test_oracle_restart_continues_run(tmp_path):
     pa, pb = a.particles(0), b.particles(0)
     for k in pa.__slots__:
         assert np.array_equal(getattr(pa, k), getattr(pb, k)), k
+
+
+def test_reader_argument_checks(tmp_path):
+    p = tmp_path / "particles_only.sdf"
+    cg.sdf_write_arrays(p, NX, NY, M, {}, dx=1.0, dy=1.0, species=[("electron", _particles(5, 7))])
+    with cg.SdfFile(p) as f:
+        assert (f.info.nx, f.info.ny, f.info.n_mode) == (0, 0, 0)
+        # no mode arrays: the file does not say their shape
+        with pytest.raises(abi.CylError):
+            f.field("exm")
+        assert f.particles("electron").n == 5
+    p2 = tmp_path / "fields.sdf"
+    cg.sdf_write_arrays(p2, NX, NY, M, {"exm": _arrays(8)["exm"]}, dx=1.0, dy=1.0)
+    with cg.SdfFile(p2) as f:
+        with pytest.raises(abi.CylError):
+            f.field(abi.NFIELDS)
+        with pytest.raises(abi.CylError):
+            f.field(-1)
