@@ -1,7 +1,7 @@
 """ctypes wrapper of the CPU FP64 oracle (oracle/cyl_oracle.cpp).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
-the CPU-baseline leg of bench.py, as the checker.  The product never loads
+the CPU-baseline leg of bench.py, as the test oracle.  The product never loads
 it.  Parity status: the reference itself (Fortran + MPI) cannot be built
 here; the oracle is pinned by the analytic current of the reference's
 documentation (section 7.2), by discrete charge conservation and by the
