@@ -131,20 +131,48 @@ struct Tile {
   float s_xr, s_t;  // accumulator units per unit of jx / jr and of jtheta flux
 };
 
-// Fixed-point scales of a tile's current accumulators.  One particle adds at
-// most 16 |q fac| w_max / dt (jx, jr) or 16 |q fac| w_max c (jtheta) to one
-// accumulator value (|partial sums of the weight changes| <= 2, |mode
-// factors| <= 2, 1, 2/3 with the 2 e^{i m theta} prefactor).  That bound is
-// scaled to 2^30 / k, k = max(1, n / 2^16) for a tile of n particles.  The
-// bound is a worst case (a particle crossing a whole cell in one step): the
-// currents of slowly moving particles are 1e-3 of it and smaller, which is
-// why the accumulators are exact hi/lo pairs with a 2^-30 quantum rather
-// than single words (whose range would cap the quantum at n / 2^30).
-__device__ __forceinline__ void tile_scales(Tile& t, int64_t n, float qw_max, float idt, float c) {
+// Fixed-point scales of a tile's current accumulators.  One particle of
+// weight w and normalised momentum u after its push adds at most
+//   8 |q fac| w / dt * min(2, 3 d)   to a jx or jr accumulator value, and
+//   16 |q fac| w c * min(1, |u|)     to a jtheta value,
+// d = (c dt / min(dx, dy)) min(1, |u|) its displacement in cells over the
+// deposit's interval: the partial sums of its weight changes are the charge
+// its shape moves across a cell face, at most 1.5 d (the shape's peak
+// density, twice the reference's convention) and at most 2 (a whole cell
+// crossed); |v| <= c min(1, |u|); the flux weights with the 2 e^{i m theta}
+// prefactor are at most 4 and 8.  The tile's bound takes the tile's largest
+// weight, and for |u| the largest momentum before the push plus two
+// electric kicks at the largest staged field (the magnetic rotation keeps
+// |u|), with a margin for FP32 rounding.  It is scaled to 2^30 / k,
+// k = max(1, n / 2^16) for a tile of n particles, so that neither one add
+// (|v| <= 2^30) nor the sum of at most 2^16 adds of one hi word overflows.
+// The quantum is thus 2^-30 of what the tile's fastest, heaviest particle
+// could deposit, not of a worst case for the species: a tile of particles
+// at rest in a weak field gets a fine quantum, a tile with a relativistic
+// particle the coarse one, and within a tile the relative error of an add
+// grows only with the spread of the tile's currents.
+struct TileBound {
+  float w_max;   // largest |weight|
+  float u2_max;  // largest |u|^2 before the push
+  float e_sum;   // bound on |E| at a particle: 4 sum_comp sum_m max|F_m|
+};
+__device__ __forceinline__ void tile_scales(Tile& t, int64_t n, const TileBound& b, const MixedParams& P) {
   const float k = fmaxf(1.0f, (float)n * (1.0f / 65536.0f));
-  const float bxr = 16.0f * qw_max * idt * k, bt = 16.0f * qw_max * c * k;
+  const float u = (sqrtf(b.u2_max) + 2.0f * fabsf(P.cmratio) * b.e_sum) * 1.001f;
+  const float vfac = fminf(1.0f, u);
+  const float d = 2.0f * fmaxf(P.cdt2_dx, P.cdt2_dy) * vfac;
+  const float qw = fabsf(P.q_fac) * b.w_max;
+  const float bxr = 8.0f * qw * P.idt * k * fminf(2.0f, 3.0f * d), bt = 16.0f * qw * P.c * k * vfac;
   t.s_xr = bxr > 0.f ? 1073741824.0f / bxr : 0.f;
   t.s_t = bt > 0.f ? 1073741824.0f / bt : 0.f;
+}
+
+// Block-wide maximum of non-negative floats: their bit patterns order as
+// unsigned integers.  Every thread of the CTA takes part; the result is in
+// slot[0] after the next __syncthreads (slot must be 0 before).
+__device__ __forceinline__ void block_max_into(unsigned* slot, float v) {
+  const unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(v));
+  if ((threadIdx.x & 31) == 0) atomicMax(slot, m);
 }
 
 // Staged fields of a tile, in shared memory:
@@ -209,6 +237,12 @@ __device__ __forceinline__ void record(const MixedParams& P, int reason, int64_t
 __device__ __forceinline__ void gadd_f(cplx* p, float re, float im) {
   atomicAdd(&p->re, f2d_bits(re));
   if (im != 0.f) atomicAdd(&p->im, f2d_bits(im));
+}
+
+// 1 / gamma for a normalised momentum u (one expression for every use, so
+// that consecutive steps agree on a particle's drift to the last bit).
+__device__ __forceinline__ float inv_gamma(float ux, float uy, float uz) {
+  return 1.0f / sqrtf(fmaf(ux, ux, fmaf(uy, uy, fmaf(uz, uz, 1.0f))));
 }
 
 // Per-mode deposit weights of particles.F90:589-665 for one particle: mode
@@ -436,8 +470,7 @@ __device__ __forceinline__ bool push_one(int64_t i, const SpeciesPtrs& sp, Speci
   float ux = sp.ux[i], uy = sp.uy[i], uz = sp.uz[i];
   const float w = sp.fw[i];
 
-  float gam = sqrtf(fmaf(ux, ux, fmaf(uy, uy, fmaf(uz, uz, 1.0f))));
-  float igm = 1.0f / gam;
+  float igm = inv_gamma(ux, uy, uz);
   fx += ux * (P.cdt2_dx * igm);
   y += uy * (P.cdt2_dy * igm);
   z += uz * (P.cdt2_dy * igm);
@@ -551,8 +584,7 @@ __device__ __forceinline__ bool push_one(int64_t i, const SpeciesPtrs& sp, Speci
   // Boris rotation (particles.F90:404-451)
   const float cm = P.cmratio;
   const float uxm = ux + cm * exr, uym = uy + cm * eyr, uzm = uz + cm * ezr;
-  gam = sqrtf(uxm * uxm + uym * uym + uzm * uzm + 1.0f);
-  const float root = P.ccmratio / gam;
+  const float root = P.ccmratio * inv_gamma(uxm, uym, uzm);
   const float tx = bxr * root, ty = byr * root, tz = bzr * root;
   const float tx2 = tx * tx, ty2 = ty * ty, tz2 = tz * tz;
   const float tau = 1.0f / (1.0f + tx2 + ty2 + tz2);
@@ -567,8 +599,9 @@ __device__ __forceinline__ bool push_one(int64_t i, const SpeciesPtrs& sp, Speci
     record(P, 40 + (SHARED ? 10 : 0), i, exr, er_, etr, bxr, brr, btr, (float)cx1, (float)cy2);
     return true;
   }
-  gam = sqrtf(ux * ux + uy * uy + uz * uz + 1.0f);
-  igm = 1.0f / gam;
+  // the same expression as the next step's half drift, so that its t + dt/2
+  // position is this deposit's t + 3dt/2 one
+  igm = inv_gamma(ux, uy, uz);
   const float dxs = ux * (P.cdt2_dx * igm), dys = uy * (P.cdt2_dy * igm), dzs = uz * (P.cdt2_dy * igm);
   const float fxn = fx + dxs;
   float yn = y + dys, zn = z + dzs;
@@ -581,7 +614,15 @@ __device__ __forceinline__ bool push_one(int64_t i, const SpeciesPtrs& sp, Speci
   const float r3 = sqrtf(y3 * y3 + z3 * z3);
   const float ir3 = (r3 > 0.f) ? 1.0f / r3 : 0.f;
   const float c3 = (r3 > 0.f) ? y3 * ir3 : 1.f, s3 = (r3 > 0.f) ? z3 * ir3 : 0.f;
-  const float cyr3 = r3 - 0.5f;
+  // Displacements over the deposit's interval.  fx3 - fx and y3 - y, z3 - z
+  // are differences of nearby FP32 values, exact; the radial one is formed
+  // as (r3^2 - r^2) / (r3 + r), without the cancellation of r3 - r, whose
+  // terms each carry the absolute rounding of a radius (2^-24 r, up to 3e-5
+  // of a cell at r = 256 cells: the size of a slow particle's whole step).
+  const float ddx = fx3 - fx;
+  const float rs = r3 + r;
+  const float ddr = rs > 0.f ? ((y3 - y) * (y3 + y) + (z3 - z) * (z3 + z)) / rs : 0.f;
+  const float cyr3 = cyr + ddr;
   const int a3 = (int)floorf(fx3);
   const float frx3 = ((float)a3 - fx3) + 0.5f;
   const int b3 = (int)floorf(cyr3);
@@ -607,6 +648,24 @@ __device__ __forceinline__ bool push_one(int64_t i, const SpeciesPtrs& sp, Speci
       const float hny = (oy == -1) ? ny0 : (oy == 0) ? ny1 : (oy == 1) ? ny2 : 0.f;
       dgx[q] = hnx - og[q];
       dgy[q] = hny - oh[q];
+    }
+    // Without a cell change the weight changes are formed from the
+    // displacement d itself: with f' = f - d,
+    //   h(-1): (f'+f+1)(f'-f) = -(p + d),  h(0): -2 (f'^2 - f^2) = 2 p,
+    //   h(+1): (f'+f-1)(f'-f) = d - p,     p = d (2 f - d),
+    // so each change keeps the relative precision of d (a difference of
+    // new and old weights, each near 1, keeps only their absolute 2^-24).
+    if (dcx == 0) {
+      const float p = ddx * (2.0f * frx2 - ddx);
+      dgx[1] = -(p + ddx);
+      dgx[2] = 2.0f * p;
+      dgx[3] = ddx - p;
+    }
+    if (dcy == 0) {
+      const float p = ddr * (2.0f * fry2 - ddr);
+      dgy[1] = -(p + ddr);
+      dgy[2] = 2.0f * p;
+      dgy[3] = ddr - p;
     }
   }
   const float qwf = P.q_fac * w;  // q w fac
@@ -753,9 +812,9 @@ struct TileSmem {
 template <int M>
 __device__ __forceinline__ bool process_tile(const FieldSetF& F, const SpeciesPtrs& sp, SpeciesCounters* cnt,
                                              const RunConst& rc, const MixedParams& P, const TileTable* tt, int t,
-                                             int nsh, float qw_max, int apply_bcs, const TmaSet* tma, int use_tma,
+                                             int nsh, int apply_bcs, const TmaSet* tma, int use_tma,
                                              const TileSmem<M>& sm, uint64_t* tma_bar, int* tma_failed,
-                                             unsigned& tma_phase) {
+                                             unsigned* s_bound, unsigned& tma_phase) {
   float2* const tm = sm.tm;
   float2* const sf = sm.sf;
   int* const sj = sm.sj;
@@ -785,15 +844,27 @@ __device__ __forceinline__ bool process_tile(const FieldSetF& F, const SpeciesPt
           tma_load_3d(tm + (q * (M - 1) + m - 1) * TPLANE, &tma->map[q], tile.xs + NG - 1, tile.y0 + NG - 1, m,
                       tma_bar);
     }
+    // inputs of the tile's fixed-point bound (tile_scales): the largest
+    // weight and momentum of its particles, the largest staged E values
+    float b_w = 0.f, b_u2 = 0.f, b_ex = 0.f, b_er = 0.f, b_et = 0.f, b_em = 0.f;
+    for (int64_t i = p0 + threadIdx.x; i < p1; i += PUSH_THREADS) {
+      const float ux = sp.ux[i], uy = sp.uy[i], uz = sp.uz[i];
+      b_w = fmaxf(b_w, fabsf(sp.fw[i]));
+      b_u2 = fmaxf(b_u2, fmaf(ux, ux, fmaf(uy, uy, uz * uz)));
+    }
     {
       using G = Gather<M, false>;
       float* s_t = reinterpret_cast<float*>(sf + 2 * RCELLS);
       for (int c = threadIdx.x; c < RCELLS; c += PUSH_THREADS) {
         const int x = tile.x0 + c % RW, y = tile.y0 + c / RW;
-        sf[c] = make_float2(G::re0(F, 0, x, y), G::re0(F, 4, x, y));
-        sf[RCELLS + c] = make_float2(G::re0(F, 1, x, y), G::re0(F, 3, x, y));
-        s_t[c] = G::re0(F, 2, x, y);
+        const float ex = G::re0(F, 0, x, y), er = G::re0(F, 1, x, y), et = G::re0(F, 2, x, y);
+        sf[c] = make_float2(ex, G::re0(F, 4, x, y));
+        sf[RCELLS + c] = make_float2(er, G::re0(F, 3, x, y));
+        s_t[c] = et;
         s_t[RCELLS + c] = G::re0(F, 5, x, y);
+        b_ex = fmaxf(b_ex, fabsf(ex));
+        b_er = fmaxf(b_er, fabsf(er));
+        b_et = fmaxf(b_et, fabsf(et));
       }
       if (M > 1 && !use_tma) {
         // the same boxes by plain loads (row pitches that TMA cannot take)
@@ -823,14 +894,36 @@ __device__ __forceinline__ bool process_tile(const FieldSetF& F, const SpeciesPt
       tma_phase ^= 1u;
     }
     for (int e = threadIdx.x; e < 3 * M * 4 * RCELLS; e += PUSH_THREADS) sj[e] = 0;
-    tile_scales(tile, p1 - p0, qw_max, P.idt, P.c);
+    if (M > 1) {
+      // E_m of modes m >= 1 (TMA planes of Ex, Er, Et: q = 0, 1, 2)
+      for (int e = threadIdx.x; e < 3 * (M - 1) * TW * RH; e += PUSH_THREADS) {
+        const float2 v = tm[(e / (TW * RH)) * TPLANE + e % (TW * RH)];
+        b_em = fmaxf(b_em, fabsf(v.x) + fabsf(v.y));
+      }
+    }
+    block_max_into(s_bound + 0, b_w);
+    block_max_into(s_bound + 1, b_u2);
+    block_max_into(s_bound + 2, b_ex);
+    block_max_into(s_bound + 3, b_er);
+    block_max_into(s_bound + 4, b_et);
+    block_max_into(s_bound + 5, b_em);
     __syncthreads();
     if (*tma_failed) return false;  // uniform: read by every thread after the barrier
+    {
+      TileBound b;
+      b.w_max = __uint_as_float(s_bound[0]);
+      b.u2_max = __uint_as_float(s_bound[1]);
+      b.e_sum = 4.0f * (__uint_as_float(s_bound[2]) + __uint_as_float(s_bound[3]) + __uint_as_float(s_bound[4]) +
+                        3.0f * (float)(M - 1) * __uint_as_float(s_bound[5]));
+      tile_scales(tile, p1 - p0, b, P);
+    }
     for (int64_t i = p0 + threadIdx.x; i < p1; i += PUSH_THREADS) {
       if (!push_one<M, true>(i, sp, cnt, F, P, rc, tile, nsh, apply_bcs))
         P.fb_list[atomicAdd(P.fb_count, 1)] = (int)i;
     }
     __syncthreads();
+    // every thread read the bound before the barrier: clear it for the next tile
+    if (threadIdx.x < 6) s_bound[threadIdx.x] = 0u;
     // flush: one FP64 add per non-zero accumulator, with the geometric
     // factor of the row and the inverse fixed-point scale
     const float inv_xr = tile.s_xr > 0.f ? 1.0f / tile.s_xr : 0.f;
@@ -861,22 +954,23 @@ __global__ void __launch_bounds__(PUSH_THREADS, push_min_blocks<M>()) k_push_til
   extern __shared__ float4 smem4[];
   __shared__ uint64_t tma_bar;
   __shared__ int tma_failed;
+  __shared__ unsigned s_bound[6];
   const TileSmem<M> sm(smem4);
   if (threadIdx.x == 0) {
     tma_failed = 0;
     if (use_tma) mbar_init(&tma_bar);
   }
+  if (threadIdx.x < 6) s_bound[threadIdx.x] = 0u;
   __syncthreads();
   unsigned tma_phase = 0;
   const int nsh = rec->nshift_total;
-  const float qw_max = fabsf(P.q_fac) * __uint_as_float(cnt->wmax_bits);
   set_bounds(P, rec, rc);
   const int ntiles = tt->ntiles;
   // static round-robin over the tiles in decreasing order of particle count
   // (longest first)
   for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x) {
-    if (!process_tile<M>(F, sp, cnt, rc, P, tt, tt->order[ti], nsh, qw_max, apply_bcs, &tma, use_tma, sm, &tma_bar,
-                         &tma_failed, tma_phase))
+    if (!process_tile<M>(F, sp, cnt, rc, P, tt, tt->order[ti], nsh, apply_bcs, &tma, use_tma, sm, &tma_bar,
+                         &tma_failed, s_bound, tma_phase))
       return;
   }
 }
@@ -892,7 +986,9 @@ __global__ void __launch_bounds__(PUSH_THREADS, push_min_blocks<M>()) k_push_til
                                                                                    const int* nwork) {
   extern __shared__ float4 smem4[];
   __shared__ int tma_failed;
+  __shared__ unsigned s_bound[6];
   if (threadIdx.x == 0) tma_failed = 0;
+  if (threadIdx.x < 6) s_bound[threadIdx.x] = 0u;
   __syncthreads();
   const TileSmem<M> sm(smem4);
   unsigned tma_phase = 0;
@@ -902,9 +998,8 @@ __global__ void __launch_bounds__(PUSH_THREADS, push_min_blocks<M>()) k_push_til
     const BatchJob& J = jobs[jt.x];
     MixedParams P = J.P;
     set_bounds(P, J.rec, J.rc);
-    const float qw_max = fabsf(P.q_fac) * __uint_as_float(J.cnt->wmax_bits);
-    process_tile<M>(J.F, J.sp, J.cnt, J.rc, P, J.tt, jt.y, J.rec->nshift_total, qw_max, J.apply_bcs, nullptr, 0, sm,
-                    nullptr, &tma_failed, tma_phase);
+    process_tile<M>(J.F, J.sp, J.cnt, J.rc, P, J.tt, jt.y, J.rec->nshift_total, J.apply_bcs, nullptr, 0, sm,
+                    nullptr, &tma_failed, s_bound, tma_phase);
   }
 }
 
