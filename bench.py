@@ -149,20 +149,47 @@ def build_deck(name, form, modes=None):
 
 
 def run_reference(args, rank):
+    """The reference arm: the CPU restatement of the reference's step
+    (oracle/) on all host threads, with its own loader (the reference's
+    load_particles and KISS stream), so that this process maps no library of
+    the package.  It runs the same steps as the GPU arm: W untimed steps from
+    t = 0, then steps [W, W+K) timed, or the first of them that fit in about
+    a minute of host time (the sample is stated)."""
     if rank != 0:
         return 0
-    import cylindrical_epoch_gb300 as cg
+    from oracle.oracle import Oracle, load
     form = "fp64"
     deck = build_deck(args.deck, form, args.modes)
-    parts, rng = cg.host_load(deck)
-    base = cpu_baseline(deck, parts, rng, seconds=min(60.0, 5.0 + 0.02 * args.steps))
+    lib = load()
+    nt = os.cpu_count() or 1
+    lib.orc_set_threads(nt)
+    orc = Oracle(deck, load_species=True)
+    orc.initialise()
+    mobile = [i for i in range(len(deck.species)) if not deck.species[i].immobile]
+    orc.step(args.warmup)
+    n0 = sum(orc.state().n_live[i] for i in mobile)
+    budget = 60.0
+    t0 = time.perf_counter()
+    steps = 0
+    while steps < args.steps:
+        orc.step(1)
+        steps += 1
+        if time.perf_counter() - t0 >= budget:
+            break
+    dt = time.perf_counter() - t0
+    n1 = sum(orc.state().n_live[i] for i in mobile)
+    value = 0.5 * (n0 + n1) * steps / dt
+    sample = (f"steps [{args.warmup}, {args.warmup + steps}) of the deck from t=0 ({n0} particles), "
+              f"{dt:.1f} s, {nt} OpenMP threads, the restatement's own loader")
     line = {
-        "impl": "reference", "metric": "particle-steps/s", "value": base["value"],
+        "impl": "reference", "metric": "particle-steps/s", "value": value,
         "unit": "particle-steps/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * dt / steps, "steps_timed": steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "config": _config(args, deck, form),
-        "cpu_baseline": base,
-        "e2e": {"value": base["value"], "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+        "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": nt, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -348,6 +375,9 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=-1,
                     help="steps of the plain FP64 form timed beside the mixed form "
                          "(-1: the same K steps, compared with the mixed result; 0: skip)")
+    ap.add_argument("--window-start", type=int, default=1100,
+                    help="first step of the moving-window-phase leg (0: skip the leg)")
+    ap.add_argument("--window-steps", type=int, default=32)
     ap.add_argument("--serve", action="store_true", help="parameter-scan serving benchmark")
     ap.add_argument("--jobs", type=int, default=64)
     ap.add_argument("--arrival", type=float, default=0.5, help="mean Poisson arrival gap (s)")
@@ -484,9 +514,20 @@ def main():
 
     e2e = None
     if not args.no_e2e:
-        e2e = e2e_run(deck, parts, rng, args.steps, graph)
+        e2e = e2e_run(deck, parts, rng, args.steps, graph, tile[0] if tile else None)
         if dist:
             e2e["value"] = reduce_replicas(e2e["seconds"], e2e["psteps"], dist, "cuda")[2]
+        if fp64 is not None:
+            # the FP64 form end to end as well: the figure at the reference's precision
+            e64 = e2e_run(build_deck(args.deck, "fp64", args.modes), parts, rng, fp64["steps"], graph)
+            if dist:
+                e64["value"] = reduce_replicas(e64["seconds"], e64["psteps"], dist, "cuda")[2]
+            fp64["e2e"] = {"value": e64["value"], "unit": "particle-steps/s",
+                           "h2d_bytes_per_step": e64["h2d"] / fp64["steps"],
+                           "d2h_bytes_per_step": e64["d2h"] / fp64["steps"], "phases_s": e64["phases_s"]}
+    window = None
+    if form == "mixed" and args.deck == "wakefield" and args.window_start > 0:
+        window = window_phase(args, parts, rng, graph, tile[0] if tile else None)
     base = None
     if rank == 0 and world == 1 and not args.no_cpu:
         base = cpu_baseline(build_deck(args.deck, "fp64", args.modes), parts, rng)
@@ -513,6 +554,8 @@ def main():
             line["mixed_over_fp64"] = value / fp64["value"]
         if accuracy:
             line["accuracy"] = accuracy
+        if window:
+            line["window_phase"] = window
         print(json.dumps(line))
     run.close()
     if dist:
@@ -520,7 +563,52 @@ def main():
     return 0
 
 
-def e2e_run(deck, parts, rng, steps, graph):
+def window_phase(args, parts, rng, graph, tile_shape):
+    """The moving-window phase of the wakefield deck: both forms stepped
+    (untimed) from t = 0 to step S (after the window has started moving:
+    injection, removal and field shifts every step or two), then steps
+    [S, S + k) timed with CUDA events on each run's stream, and the mixed
+    state compared with the FP64 state there."""
+    import torch
+    import cylindrical_epoch_gb300 as cg
+    from cylindrical_epoch_gb300.diagnostics import compare_runs
+    S, k = args.window_start, args.window_steps
+    out = {"steps": [S, S + k]}
+    runs = {}
+    for form in ("mixed", "fp64"):
+        d = build_deck(args.deck, form, args.modes)
+        r = cg.Run(d, particles=parts, rng=rng)
+        if form == "mixed" and tile_shape is not None:
+            r.tune_tiles(tile_shape)
+        r.step(S, graph=graph)
+        s0 = r.state()
+        mob = [i for i in range(len(d.species)) if not d.species[i].immobile]
+        n0 = sum(s0.n_live[i] for i in mob)
+        ext = torch.cuda.ExternalStream(r.stream())
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        r.kernel_timing()
+        torch.cuda.synchronize()
+        e0.record(ext)
+        r.step(k, graph=graph)
+        e1.record(ext)
+        torch.cuda.synchronize()
+        dt = e0.elapsed_time(e1) * 1e-3
+        push_ms, _ = r.kernel_timing()
+        s1 = r.state()
+        n1 = sum(s1.n_live[i] for i in mob)
+        out[form] = {"value": 0.5 * (n0 + n1) * k / dt, "unit": "particle-steps/s", "ms_per_step": 1e3 * dt / k,
+                     "push_ms": push_ms, "n_shifts": [int(s0.n_shifts), int(s1.n_shifts)]}
+        runs[form] = (r, d)
+    out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    rm, dm = runs["mixed"]
+    out["accuracy"] = dict(against="plain FP64 GPU form, same deck, seed and steps", **compare_runs(rm, runs["fp64"][0], dm))
+    for r, _ in runs.values():
+        r.close()
+    return out
+
+
+def e2e_run(deck, parts, rng, steps, graph, tile_shape=None):
     """The same run through the C ABI with host buffers: the initial state
     is copied from pinned host memory, every 16 steps the diagnostics are
     read back, and the final particles and fields are copied to the host,
@@ -561,7 +649,9 @@ def e2e_run(deck, parts, rng, steps, graph):
     run = cg.Run(deck, particles=pinned, rng=rng)
     t_up = time.perf_counter()
     if deck.precision == abi.PREC_MIXED:
-        run.tune_tiles()
+        # the tile shape this process timed for this deck shape (the request
+        # loop likewise times each deck shape once per process), else timed now
+        run.tune_tiles(tile_shape)
     t_tune = time.perf_counter()
     d2h = 0
     left = steps

@@ -20,6 +20,7 @@ CYL_ERR_TIMEOUT = 7
 CYL_ERR_OUT_OF_MEMORY = 8
 CYL_ERR_SCRATCH = 9
 CYL_ERR_IO = 10
+CYL_ERR_CALLBACK = 11
 NOALLOC_MAX_PARTICLES = 262144  # CYL_NOALLOC_MAX_PARTICLES
 N_TILE_SHAPES = 5  # CYL_N_TILE_SHAPES
 TUNE_SET = 0       # CYL_TUNE_SET
@@ -38,6 +39,7 @@ ERROR_NAMES = {
     CYL_ERR_OUT_OF_MEMORY: "device out of memory",
     CYL_ERR_SCRATCH: "input larger than the fixed scratch (CYL_NOALLOC_MAX_PARTICLES slots)",
     CYL_ERR_IO: "file could not be written",
+    CYL_ERR_CALLBACK: "a deck-expression callback returned an error",
 }
 
 BC_PERIODIC = 1
@@ -101,6 +103,28 @@ class LaserDesc(C.Structure):
         ("t0", C.c_double), ("tw", C.c_double),
         ("profile", C.POINTER(C.c_double)),
         ("phase", C.POINTER(C.c_double)),
+    ]
+
+
+LaserTimeFn = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int32, C.c_double, C.POINTER(C.c_double))
+LaserOmegaFn = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int32, C.c_double, C.POINTER(C.c_double))
+LaserArrayFn = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int32, C.c_double, C.POINTER(C.c_double))
+InjectFn = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int32, C.c_double, C.c_double, C.POINTER(C.c_double),
+                       C.POINTER(C.c_double), C.POINTER(C.c_double))
+
+
+class DeckFns(C.Structure):
+    """cyl_deck_fns: callbacks that evaluate deck expressions while stepping."""
+    _fields_ = [
+        ("user", C.c_void_p),
+        ("laser_time", LaserTimeFn),
+        ("laser_omega", LaserOmegaFn),
+        ("laser_profile", LaserArrayFn),
+        ("laser_phase", LaserArrayFn),
+        ("omega_fn_mask", C.c_uint32),
+        ("profile_fn_mask", C.c_uint32),
+        ("phase_fn_mask", C.c_uint32),
+        ("inject", InjectFn),
     ]
 
 

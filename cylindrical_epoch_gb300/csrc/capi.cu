@@ -113,6 +113,10 @@ struct Handle {
   bool from_restart = false;
   bool restart_wsf = false;  // the loaded dump held window_shift_fraction
   std::vector<HostLaser> lasers;
+  // deck-expression callbacks (cyl_set_deck_fns); cb_failed is raised by a
+  // callback's error while a step is prepared and read by its caller
+  cyl_deck_fns fns{};
+  bool cb_failed = false;
   KissRng rng;
   // staging
   StepRec* h_rec = nullptr;
@@ -231,22 +235,51 @@ static int field_slot(const Handle* h, int which) {
   return which;
 }
 
-// Laser sources at the handle's current time (laser.f90:444-461):
-// out[side*2*(ny+1) + {0, ny+1} + ir] = source1, source2.
-static void laser_sources(Handle* h, double* out) {
+// update_laser_omegas (laser.f90:276-328) at the handle's current time, dt_eff
+// the step's dt (dt/2 at the start-up half step): a deck-function omega is
+// evaluated and its phase integrated, the others' phase is omega * time.
+static void update_laser_omegas(Handle* h, double dt_eff) {
+  for (size_t i = 0; i < h->lasers.size(); ++i) {
+    HostLaser& L = h->lasers[i];
+    if (h->fns.laser_omega && ((h->fns.omega_fn_mask >> i) & 1u)) {
+      double om = L.d.omega;
+      if (h->fns.laser_omega(h->fns.user, (int32_t)i, h->time, &om) != 0) h->cb_failed = true;
+      L.d.omega = om;
+      L.current_integral_phase = L.current_integral_phase + om * dt_eff;
+    } else {
+      L.current_integral_phase = L.d.omega * h->time;
+    }
+  }
+}
+
+// Laser sources at the handle's current time (laser.f90:444-461), after
+// update_laser_omegas: out[side*2*(ny+1) + {0, ny+1} + ir] = source1, source2.
+// A laser whose phase or profile is a function of time has it re-evaluated
+// first (laser.f90:449-450), then its time profile.
+static void laser_sources(Handle* h, double* out, double dt_eff) {
   const int ny = h->g.ny;
   std::memset(out, 0, sizeof(double) * 4 * (ny + 1));
-  for (auto& L : h->lasers) L.current_integral_phase = L.d.omega * h->time;  // update_laser_omegas
+  update_laser_omegas(h, dt_eff);
   for (int side = 0; side < 2; ++side) {
     const int bd = side == 0 ? CYL_BD_X_MIN : CYL_BD_X_MAX;
     if (!h->add_laser[bd]) continue;
     double* s1 = out + side * 2 * (ny + 1);
     double* s2 = s1 + (ny + 1);
-    for (auto& L : h->lasers) {
+    for (size_t i = 0; i < h->lasers.size(); ++i) {
+      HostLaser& L = h->lasers[i];
       if (L.d.boundary != bd) continue;
       if (h->time >= L.d.t_start && h->time <= L.d.t_end) {
+        const cyl_deck_fns& f = h->fns;
+        if (f.laser_phase && ((f.phase_fn_mask >> i) & 1u) &&
+            f.laser_phase(f.user, (int32_t)i, h->time, L.phase.data()) != 0)
+          h->cb_failed = true;
+        if (f.laser_profile && ((f.profile_fn_mask >> i) & 1u) &&
+            f.laser_profile(f.user, (int32_t)i, h->time, L.profile.data()) != 0)
+          h->cb_failed = true;
         double tp = 1.0;
-        if (L.d.t_profile == 1) {
+        if (f.laser_time) {
+          if (f.laser_time(f.user, (int32_t)i, h->time, &tp) != 0) h->cb_failed = true;
+        } else if (L.d.t_profile == 1) {
           const double v = (h->time - L.d.t0) / L.d.tw;
           tp = std::exp(-(v * v));
         }
@@ -259,6 +292,20 @@ static void laser_sources(Handle* h, double* out) {
       }
     }
   }
+}
+
+// insert_particles' columns of species s from the caller's callback (or
+// none: the descriptor's closed forms), at the grid before the shift.
+static const InjectColumns* inject_columns(Handle* h, int s, InjectColumns& cols) {
+  if (!h->fns.inject) return nullptr;
+  const int ny = h->g.ny;
+  cols.density.assign((size_t)ny + 2, 0.0);
+  cols.temperature.assign(3 * ((size_t)ny + 2), 0.0);
+  cols.drift.assign(3 * ((size_t)ny + 2), 0.0);
+  if (h->fns.inject(h->fns.user, s, h->time, h->g.xg(h->g.nx), cols.density.data(), cols.temperature.data(),
+                    cols.drift.data()) != 0)
+    h->cb_failed = true;
+  return &cols;
 }
 
 static void fill_grid(StepRec& r, const HostGrid& g, bool after) {
@@ -372,7 +419,7 @@ static void step_tail(Handle* h, int k, int64_t& inj_used) {
   h->time = h->time + h->g.dt / 2.0;
   r.time_final = h->time;
   r.src_off = (int64_t)k * (int64_t)h->src_per_step;
-  laser_sources(h, h->h_src + r.src_off);
+  laser_sources(h, h->h_src + r.src_off, h->g.dt);
   for (int s = 0; s < h->nsp; ++s) {
     r.inject_off[s] = inj_used;
     r.inject_cnt[s] = 0;
@@ -398,9 +445,10 @@ static void step_tail(Handle* h, int k, int64_t& inj_used) {
         std::vector<HostParticle> batch;
         // one buffer region per species: inject all species for every shift
         std::vector<std::vector<HostParticle>> per(h->nsp);
+        InjectColumns cols;
         for (int c = 0; c < cells; ++c) {
           for (int s = 0; s < h->nsp; ++s)
-            host_insert_particles(h->g, h->sd[s], h->rng, h->next_id, per[s]);
+            host_insert_particles(h->g, h->sd[s], h->rng, h->next_id, per[s], inject_columns(h, s, cols));
           h->g.x_grid_min = h->g.xg(1) + h->g.dx;
           h->g.xb_min = h->g.xb_min + h->g.dx;
           h->g.x_min = h->g.xb_min + h->g.dx * 0.0;
@@ -657,7 +705,9 @@ static int run_chunk(Handle* h, int k, bool use_graph) {
   if (h->copy_pending) CK(cudaEventSynchronize(h->ev_copy));
   // the host work of this chunk overlaps the device work of the previous one
   int64_t inj_used = 0;
+  h->cb_failed = false;
   for (int i = 0; i < k; ++i) prepare_step(h, i, inj_used);
+  if (h->cb_failed) return CYL_ERR_CALLBACK;
   if (int r = flush_push_timing(h)) return r;
   CK(cudaMemcpyAsync(h->d_rec, h->h_rec, sizeof(StepRec) * k, cudaMemcpyHostToDevice, h->st));
   CK(cudaMemcpyAsync(h->d_src, h->h_src, sizeof(double) * h->src_per_step * k, cudaMemcpyHostToDevice, h->st));
@@ -727,12 +777,10 @@ constexpr int MAX_SCRATCH_DEVICES = 64;
 static int32_t* g_cell_scratch_ptr[MAX_SCRATCH_DEVICES] = {};
 static std::mutex g_cell_scratch_mu;
 
-// Device address of the scratch on the current device, looked up by the first
-// call on each device (the lookup can load the module, so that first call
-// should come before any stream capture).
-static int cell_scratch(int32_t** out) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return CYL_ERR_CUDA;
+// Device address of the scratch on device `dev`, which must be the current
+// device; looked up by the first call on each device (the lookup can load
+// the module, so that first call should come before any stream capture).
+static int cell_scratch(int dev, int32_t** out) {
   if (dev < 0 || dev >= MAX_SCRATCH_DEVICES) return CYL_ERR_UNSUPPORTED;
   std::lock_guard<std::mutex> lock(g_cell_scratch_mu);
   if (!g_cell_scratch_ptr[dev]) {
@@ -1339,6 +1387,7 @@ int cyl_set_injection_stream(cyl_handle hh, int32_t mode, uint64_t seed) {
   if (!hh) return CYL_ERR_BAD_ARG;
   Handle* h = &hh->h;
   if (mode != CYL_RNG_KISS && mode != CYL_RNG_COUNTER) return CYL_ERR_BAD_ARG;
+  if (mode == CYL_RNG_COUNTER && h->fns.inject) return CYL_ERR_UNSUPPORTED;
   if (mode == CYL_RNG_COUNTER && h->move_window) {
     const double shifts_max = std::floor(h->g.dt * std::fabs(h->window_v_x) / h->g.dx) + 1.0;
     if (shifts_max > (double)MAX_INJ_SHIFTS) return CYL_ERR_UNSUPPORTED;
@@ -1646,7 +1695,9 @@ int cyl_initialise(cyl_handle hh) {
   const double dt_half = h->g.dt / 2.0;
   h->time = h->time + dt_half;
   r.time_final = h->time;
-  laser_sources(h, h->h_src);
+  h->cb_failed = false;
+  laser_sources(h, h->h_src, dt_half);
+  if (h->cb_failed) return CYL_ERR_CALLBACK;
   CK(cudaMemcpyAsync(h->d_rec, h->h_rec, sizeof(StepRec), cudaMemcpyHostToDevice, h->st));
   CK(cudaMemcpyAsync(h->d_src, h->h_src, sizeof(double) * h->src_per_step, cudaMemcpyHostToDevice, h->st));
   for (int i = 0; i < h->nsp; ++i) {
@@ -1717,7 +1768,9 @@ static int finish_output(Handle* h) {
   const bool restart = h->at_output == AT_OUTPUT_RESTART;
   h->h_rec[0] = h->out_rec;
   int64_t inj_used = 0;
+  h->cb_failed = false;
   step_tail(h, 0, inj_used);
+  if (h->cb_failed) return CYL_ERR_CALLBACK;
   CK(cudaMemcpyAsync(h->d_rec, h->h_rec, sizeof(StepRec), cudaMemcpyHostToDevice, h->st));
   CK(cudaMemcpyAsync(h->d_src, h->h_src, sizeof(double) * h->src_per_step, cudaMemcpyHostToDevice, h->st));
   if (inj_used > 0 && !h->inj_counter)
@@ -1802,6 +1855,44 @@ int cyl_push_only(cyl_handle hh) {
   CK(cudaEventSynchronize(h->ev_push[0][1]));
   collect_push_timing(h, 1);
   return sync_and_check(h);
+}
+
+int cyl_set_deck_fns(cyl_handle hh, const cyl_deck_fns* fns) {
+  if (!hh) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  if (!fns) {
+    h->fns = cyl_deck_fns{};
+    return CYL_OK;
+  }
+  const size_t nl = h->lasers.size();
+  const uint32_t valid = nl >= 32 ? 0xffffffffu : ((1u << nl) - 1u);
+  for (uint32_t m : {fns->omega_fn_mask, fns->profile_fn_mask, fns->phase_fn_mask})
+    if (m & ~valid) return CYL_ERR_BAD_ARG;
+  if ((fns->omega_fn_mask && !fns->laser_omega) || (fns->profile_fn_mask && !fns->laser_profile) ||
+      (fns->phase_fn_mask && !fns->laser_phase))
+    return CYL_ERR_BAD_ARG;
+  if (fns->inject && h->inj_counter) return CYL_ERR_UNSUPPORTED;
+  h->fns = *fns;
+  return CYL_OK;
+}
+
+int cyl_eval_atan2(int64_t n, const double* y, const double* x, double* out) {
+  if (n < 0 || (n > 0 && (!y || !x || !out))) return CYL_ERR_BAD_ARG;
+  if (n == 0) return CYL_OK;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return CYL_ERR_NO_DEVICE;
+  const size_t bytes = (size_t)n * sizeof(double);
+  double* d = nullptr;
+  if (cudaMalloc(&d, 3 * bytes) != cudaSuccess) return CYL_ERR_OUT_OF_MEMORY;
+  cudaError_t e = cudaMemcpy(d, y, bytes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d + n, x, bytes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    launch_eval_atan2(0, d, d + n, d + 2 * n, n);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(out, d + 2 * n, bytes, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  return e == cudaSuccess ? CYL_OK : CYL_ERR_CUDA;
 }
 
 int cyl_get_stream(cyl_handle hh, void** stream_out) {
@@ -2096,12 +2187,10 @@ int cyl_charge_density(cyl_handle hh, double* rho) {
   return sync_and_check(h);
 }
 
-int cyl_cell_indices_noalloc(cyl_handle hh, int32_t isp, int32_t* cx, int32_t* cy, int64_t* n_inout) {
-  if (!hh || !n_inout) return CYL_ERR_BAD_ARG;
-  Handle* h = &hh->h;
-  if (isp < 0 || isp >= h->nsp) return CYL_ERR_BAD_ARG;
+// The body of cyl_cell_indices_noalloc, with the handle's device current.
+static int cell_indices_noalloc(Handle* h, int32_t isp, int32_t* cx, int32_t* cy, int64_t* n_inout) {
   int32_t* sc = nullptr;
-  if (int r = cell_scratch(&sc)) return r;
+  if (int r = cell_scratch(h->device, &sc)) return r;
   CK(cudaStreamSynchronize(h->st));
   SpeciesCounters c;
   CK(cudaMemcpy(&c, h->d_cnt + isp, sizeof(c), cudaMemcpyDeviceToHost));
@@ -2137,8 +2226,22 @@ int cyl_cell_indices_noalloc(cyl_handle hh, int32_t isp, int32_t* cx, int32_t* c
   return CYL_OK;
 }
 
+int cyl_cell_indices_noalloc(cyl_handle hh, int32_t isp, int32_t* cx, int32_t* cy, int64_t* n_inout) {
+  if (!hh || !n_inout || (!cx) != (!cy)) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  if (isp < 0 || isp >= h->nsp) return CYL_ERR_BAD_ARG;
+  // the scratch address and the launches belong to the handle's device,
+  // whatever device the caller has current; the caller's is restored
+  int prev = 0;
+  CK(cudaGetDevice(&prev));
+  if (prev != h->device) CK(cudaSetDevice(h->device));
+  const int r = cell_indices_noalloc(h, isp, cx, cy, n_inout);
+  if (prev != h->device && cudaSetDevice(prev) != cudaSuccess && r == CYL_OK) return CYL_ERR_CUDA;
+  return r;
+}
+
 int cyl_cell_indices(cyl_handle hh, int32_t isp, int32_t* cx, int32_t* cy, int64_t* n_inout) {
-  if (!hh || !n_inout) return CYL_ERR_BAD_ARG;
+  if (!hh || !n_inout || (!cx) != (!cy)) return CYL_ERR_BAD_ARG;
   Handle* h = &hh->h;
   if (isp < 0 || isp >= h->nsp) return CYL_ERR_BAD_ARG;
   CK(cudaStreamSynchronize(h->st));
@@ -2269,7 +2372,12 @@ int cyl_batch_step(cyl_batch b, const cyl_handle* hs, int32_t n, int32_t nsteps)
         return;
       }
       int64_t inj_used = 0;
+      h->cb_failed = false;
       for (int i = 0; i < k; ++i) prepare_step(h, i, inj_used);
+      if (h->cb_failed) {
+        prep_err[(size_t)r] = CYL_ERR_CALLBACK;
+        return;
+      }
       cudaError_t e = cudaMemcpyAsync(h->d_rec, h->h_rec, sizeof(StepRec) * k, cudaMemcpyHostToDevice, h->st);
       if (e == cudaSuccess)
         e = cudaMemcpyAsync(h->d_src, h->h_src, sizeof(double) * h->src_per_step * k, cudaMemcpyHostToDevice,

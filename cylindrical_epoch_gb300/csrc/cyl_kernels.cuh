@@ -90,6 +90,7 @@ void launch_update_b_f32(cudaStream_t s, const FieldSetF& F, int save_old, const
 void launch_push_fp64(cudaStream_t s, const FieldSet& F, const GeomTables& g, const SpeciesPtrs& sp,
                       SpeciesCounters* cnt, const StepRec* rec, const RunConst& rc, int apply_bcs,
                       int* err, int nblocks);
+void launch_eval_atan2(cudaStream_t s, const double* y, const double* x, double* out, int64_t n);
 
 // charge.cu (continuity-residual and number-density diagnostics)
 void launch_number_density(cudaStream_t s, const SpeciesPtrs& sp, const SpeciesCounters* cnt, const RunConst& rc,

@@ -113,14 +113,16 @@ double species_density(const cyl_species_desc& d, double x) {
 }
 
 void host_density_map(const HostGrid& g, const cyl_grid_desc& gd, const cyl_species_desc& sp,
-                      std::vector<double>& dens, std::vector<char>& dmap, std::vector<int32_t>& valid) {
+                      std::vector<double>& dens, std::vector<char>& dmap, std::vector<int32_t>& valid,
+                      const double* dens_in) {
   const int nx = g.nx, ny = g.ny;
   const int W = nx + 2 * NG_H;
   auto at = [&](int ix, int iy) { return (size_t)(ix + NG_H - 1) + (size_t)W * (size_t)(iy + NG_H - 1); };
   dens.assign((size_t)W * (ny + 2 * NG_H), 0.0);
   dmap.assign(dens.size(), 0);
   for (int iy = 1 - NG_H; iy <= ny + NG_H; ++iy)
-    for (int ix = 1 - NG_H; ix <= nx + NG_H; ++ix) dens[at(ix, iy)] = species_density(sp, g.xg(ix));
+    for (int ix = 1 - NG_H; ix <= nx + NG_H; ++ix)
+      dens[at(ix, iy)] = dens_in ? dens_in[at(ix, iy)] : species_density(sp, g.xg(ix));
   if (gd.bc_field[CYL_BD_X_MAX] == CYL_BC_PERIODIC)
     for (int iy = 1 - NG_H; iy <= ny + NG_H; ++iy)
       for (int i = 1; i <= NG_H; ++i) dens[at(nx + i, iy)] = dens[at(i, iy)];
@@ -141,7 +143,7 @@ void host_density_map(const HostGrid& g, const cyl_grid_desc& gd, const cyl_spec
 // ------------------------------------------------------------ injection
 
 void host_insert_particles(const HostGrid& g, const cyl_species_desc& d, KissRng& rng,
-                           int64_t& next_id, std::vector<HostParticle>& out) {
+                           int64_t& next_id, std::vector<HostParticle>& out, const InjectColumns* cols) {
   const int ny = g.ny;
   const int64_t nppc = (int64_t)std::floor(d.npart_per_cell);
   const double npart_frac = d.npart_per_cell - (double)nppc;
@@ -150,11 +152,14 @@ void host_insert_particles(const HostGrid& g, const cyl_species_desc& d, KissRng
   const double dens_col = species_density(d, g.xg(g.nx));
   std::vector<double> density(ny + 2);
   for (int iy = 0; iy <= ny + 1; ++iy) {
-    double v = dens_col;
+    double v = cols ? cols->density[iy] : dens_col;
     if (v > dmax) v = dmax;
     if (v < dmin) v = 0.0;
     density[iy] = v;
   }
+  // temperature(iy, i), drift(iy, i) of the rows around iy
+  auto temp_at = [&](int iy, int i) { return cols ? cols->temperature[iy + (ny + 2) * i] : d.temp[i]; };
+  auto drift_at = [&](int iy, int i) { return cols ? cols->drift[iy + (ny + 2) * i] : d.drift[i]; };
   const double x0 = g.x_grid_max + 0.5 * g.dx;
   for (int iy = 1; iy <= ny; ++iy) {
     if (density[iy] < dmin) continue;
@@ -175,8 +180,8 @@ void host_insert_particles(const HostGrid& g, const cyl_species_desc& d, KissRng
       for (int i = 0; i < 3; ++i) {
         double tl = 0.0, dl = 0.0;
         for (int k = 0; k < 3; ++k) {
-          tl = tl + gyv[k] * d.temp[i];
-          dl = dl + gyv[k] * d.drift[i];
+          tl = tl + gyv[k] * temp_at(iy - 1 + k, i);
+          dl = dl + gyv[k] * drift_at(iy - 1 + k, i);
         }
         p.v[3 + i] = rng.box_muller(std::sqrt(tl * KB_H * d.mass), dl);
       }
@@ -225,6 +230,14 @@ double cyl_rng_box_muller(cyl_rng_state* s, double stdev, double mu) {
 int cyl_host_load_species(const cyl_grid_desc* gd, const cyl_species_desc* sp, cyl_rng_state* rs,
                           int64_t id_base, double* x, double* y, double* z, double* px, double* py,
                           double* pz, double* w, int64_t* id, int64_t* n_inout) {
+  return cyl_host_load_species_grid(gd, sp, rs, id_base, nullptr, nullptr, nullptr, x, y, z, px, py, pz, w, id,
+                                    n_inout);
+}
+
+int cyl_host_load_species_grid(const cyl_grid_desc* gd, const cyl_species_desc* sp, cyl_rng_state* rs,
+                               int64_t id_base, const double* density, const double* temperature,
+                               const double* drift, double* x, double* y, double* z, double* px, double* py,
+                               double* pz, double* w, int64_t* id, int64_t* n_inout) {
   if (!gd || !sp || !n_inout) return CYL_ERR_BAD_ARG;
   HostGrid g;
   g.init(*gd);
@@ -234,7 +247,7 @@ int cyl_host_load_species(const cyl_grid_desc* gd, const cyl_species_desc* sp, c
   std::vector<double> dens;
   std::vector<char> dmap;
   std::vector<int32_t> valid_cells;
-  host_density_map(g, *gd, *sp, dens, dmap, valid_cells);
+  host_density_map(g, *gd, *sp, dens, dmap, valid_cells, density);
   const int64_t nvalid = (int64_t)valid_cells.size();
   const int64_t nppc = (int64_t)std::floor(sp->npart_per_cell);
   const int64_t nnew = (int64_t)std::floor(sp->npart_per_cell * (double)nvalid);
@@ -330,6 +343,8 @@ int cyl_host_load_species(const cyl_grid_desc* gd, const cyl_species_desc* sp, c
     const double vol = 2.0 * PI_H * g.dx * g.dy * part_r;
     w[p] = w[p] * vol / (double)npic[at(cx, cy)];
   }
+  // temperature(cell_x + sx, cell_y + sy) and drift of direction dir
+  const size_t plane = dens.size();
   for (int dir = 0; dir < 3; ++dir) {
     double* pp = dir == 0 ? px : (dir == 1 ? py : pz);
     for (int64_t p = 0; p < n; ++p) {
@@ -337,8 +352,9 @@ int cyl_host_load_species(const cyl_grid_desc* gd, const cyl_species_desc* sp, c
       double tl = 0.0, dl = 0.0;
       for (int sy = -1; sy <= 1; ++sy)
         for (int sx = -1; sx <= 1; ++sx) {
-          tl = tl + (s.gx[sx + 1] * s.gy[sy + 1]) * sp->temp[dir];
-          dl = dl + (s.gx[sx + 1] * s.gy[sy + 1]) * sp->drift[dir];
+          const size_t c = at(s.cx + sx, s.cy + sy) + plane * (size_t)dir;
+          tl = tl + (s.gx[sx + 1] * s.gy[sy + 1]) * (temperature ? temperature[c] : sp->temp[dir]);
+          dl = dl + (s.gx[sx + 1] * s.gy[sy + 1]) * (drift ? drift[c] : sp->drift[dir]);
         }
       pp[p] = rng.box_muller(std::sqrt(tl * KB_H * sp->mass), dl);
     }

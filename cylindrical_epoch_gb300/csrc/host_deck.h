@@ -54,12 +54,24 @@ double species_density(const cyl_species_desc& d, double x);
 // W = nx + 2ng), with the periodic x self-wrap, clamped to density_max and
 // zeroed below density_min; dmap marks the cells at or above density_min.
 // valid lists the valid interior cells as (ix - 1) + nx (iy - 1), iy outer.
+// dens_in, when given, holds the deck's density on that grid (the caller's
+// evaluation of the density expression) in place of the closed form.
 void host_density_map(const HostGrid& g, const cyl_grid_desc& gd, const cyl_species_desc& sp,
-                      std::vector<double>& dens, std::vector<char>& dmap, std::vector<int32_t>& valid);
+                      std::vector<double>& dens, std::vector<char>& dmap, std::vector<int32_t>& valid,
+                      const double* dens_in = nullptr);
+
+// The columns insert_particles evaluates at pack_ix = nx (window.F90:196-222):
+// density(0:ny+1), temperature(0:ny+1, 1:3), drift(0:ny+1, 1:3).
+struct InjectColumns {
+  std::vector<double> density, temperature, drift;
+};
 
 // insert_particles (window.F90:157-300) for one species at the current grid
-// (before the shift): appends to out, advances rng and next_id.
+// (before the shift): appends to out, advances rng and next_id.  cols, when
+// given, holds the caller's evaluation of the deck's columns (the density
+// not yet clamped); else the descriptor's closed forms are used.
 void host_insert_particles(const HostGrid& g, const cyl_species_desc& d, KissRng& rng,
-                           int64_t& next_id, std::vector<HostParticle>& out);
+                           int64_t& next_id, std::vector<HostParticle>& out,
+                           const InjectColumns* cols = nullptr);
 
 }  // namespace cyl

@@ -356,6 +356,17 @@ __global__ void __launch_bounds__(256) k_push_fp64(FieldSet F, GeomTables g, Spe
   if (ndead_local) atomicAdd((unsigned long long*)&cnt->n_dead, (unsigned long long)ndead_local);
 }
 
+// The FP64 kernel's atan2 (include/cyl_math.h) on n arguments, for the test
+// that the device evaluates it bit for bit as the host does.
+__global__ void k_eval_atan2(const double* y, const double* x, double* out, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = cyl_atan2(y[i], x[i]);
+}
+
+void launch_eval_atan2(cudaStream_t s, const double* y, const double* x, double* out, int64_t n) {
+  k_eval_atan2<<<1216, 256, 0, s>>>(y, x, out, n);
+}
+
 void launch_push_fp64(cudaStream_t s, const FieldSet& F, const GeomTables& g, const SpeciesPtrs& sp,
                       SpeciesCounters* cnt, const StepRec* rec, const RunConst& rc, int apply_bcs,
                       int* err, int nblocks) {

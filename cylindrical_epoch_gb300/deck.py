@@ -114,6 +114,23 @@ class Deck:
     smooth_stride: int = 1
     seed: int = 7842432
     dt: float = 0.0
+    # Deck expressions evaluated by the driver while stepping (the parser's
+    # part, cyl_deck_fns): None keeps the closed forms of the descriptors.
+    #   laser_time(il, t) -> laser_time_profile; laser_omega(il, t) -> omega
+    #   for the lasers in omega_fn (a set of laser indices); laser_profile /
+    #   laser_phase(il, t) -> ny+1 values for the lasers in profile_fn /
+    #   phase_fn; inject(isp, t, x) -> (density (ny+2,), temperature (3, ny+2),
+    #   drift (3, ny+2)) at a window shift; load_grids(isp) -> (density,
+    #   temperature (3, ...), drift (3, ...)) on the ghosted grid, or None.
+    laser_time: Optional[object] = None
+    laser_omega: Optional[object] = None
+    laser_profile: Optional[object] = None
+    laser_phase: Optional[object] = None
+    omega_fn: frozenset = frozenset()
+    profile_fn: frozenset = frozenset()
+    phase_fn: frozenset = frozenset()
+    inject: Optional[object] = None
+    load_grids: Optional[object] = None
 
     @property
     def dx(self):
@@ -170,6 +187,67 @@ class Deck:
             d.profile = prof.ctypes.data_as(C.POINTER(C.c_double))
             d.phase = ph.ctypes.data_as(C.POINTER(C.c_double))
         return arr, keep
+
+    def has_deck_fns(self):
+        return any(f is not None for f in (self.laser_time, self.laser_omega, self.laser_profile,
+                                           self.laser_phase, self.inject))
+
+    def deck_fns(self):
+        """The cyl_deck_fns struct of this deck's expression hooks, plus the
+        ctypes callback objects it points to (keep both alive while the run
+        that holds it steps).  A Python exception in a hook is reported to
+        the step as a non-zero return (CYL_ERR_CALLBACK)."""
+        ny = self.ny
+        keep = []
+
+        def guard(fn):
+            def wrapped(*a):
+                try:
+                    fn(*a)
+                    return 0
+                except Exception:  # reported to the step, which fails with CYL_ERR_CALLBACK
+                    import traceback
+                    traceback.print_exc()
+                    return 1
+            return wrapped
+
+        f = abi.DeckFns()
+        if self.laser_time is not None:
+            def lt(user, il, t, out):
+                out[0] = float(self.laser_time(int(il), t))
+            f.laser_time = abi.LaserTimeFn(guard(lt))
+            keep.append(f.laser_time)
+        if self.laser_omega is not None:
+            def lo(user, il, t, out):
+                out[0] = float(self.laser_omega(int(il), t))
+            f.laser_omega = abi.LaserOmegaFn(guard(lo))
+            keep.append(f.laser_omega)
+            f.omega_fn_mask = sum(1 << i for i in self.omega_fn)
+        for name, fn, idx, mask in (("laser_profile", self.laser_profile, self.profile_fn, "profile_fn_mask"),
+                                    ("laser_phase", self.laser_phase, self.phase_fn, "phase_fn_mask")):
+            if fn is None:
+                continue
+
+            def la(user, il, t, out, fn=fn):
+                v = np.asarray(fn(int(il), t), dtype=np.float64)
+                for ir in range(ny + 1):
+                    out[ir] = float(v[ir])
+            cb = abi.LaserArrayFn(guard(la))
+            setattr(f, name, cb)
+            keep.append(cb)
+            setattr(f, mask, sum(1 << i for i in idx))
+        if self.inject is not None:
+            def inj(user, isp, t, x, dens, temp, drift):
+                d, tm, dr = self.inject(int(isp), t, x)
+                d = np.asarray(d, dtype=np.float64)
+                tm = np.asarray(tm, dtype=np.float64).reshape(3, ny + 2)
+                dr = np.asarray(dr, dtype=np.float64).reshape(3, ny + 2)
+                C.memmove(dens, d.ctypes.data, 8 * (ny + 2))
+                C.memmove(temp, np.ascontiguousarray(tm).ctypes.data, 8 * 3 * (ny + 2))
+                C.memmove(drift, np.ascontiguousarray(dr).ctypes.data, 8 * 3 * (ny + 2))
+            f.inject = abi.InjectFn(guard(inj))
+            keep.append(f.inject)
+        return f, keep
 
     def mobile_particles_estimate(self):
         n = 0
@@ -289,3 +367,62 @@ def large_wakefield(precision=abi.PREC_MIXED, nsteps=3000):
                    bc=(abi.BC_SIMPLE_LASER, abi.BC_OPEN, abi.BC_OTHER, abi.BC_OPEN))
     return wakefield(nx=4096, ny=512, n_mode=4, ppc=32, a0=4.0, waist=8.0e-6, density=3.0e24,
                      nsteps=nsteps, precision=precision, circular=True, ions=ions)
+
+
+def moving_window_deck(precision=abi.PREC_FP64):
+    """The reference's own moving-window example deck
+    (example_decks/moving_window.deck), with its deck expressions evaluated
+    here as the Fortran parser would and passed through the deck-expression
+    channel: 500 x 100 cells over 20 x 5 um, modes m = 0..1; a 1 um laser at
+    1e15 W/cm^2 from x_min with a curved-wavefront phase
+    2 pi / lambda0 y^2 / (2 RC) - gouy and profile gauss(y, 0, w_bnd); a
+    window at 2e8 m/s from 30 to 100 fs with simple_outflow x boundaries
+    after the move; one neutral species of mass 2000 m_e at 0.5 K with
+    npart = 2 nx ny (2 per cell: every cell is valid) and the x-dependent
+    density 0.5 + sin(x / 4 um)^2, used by the loader on the ghosted grid and
+    by insert_particles at every window shift."""
+    nx, ny = 500, 100
+    micron = 1.0e-6
+    lambda0 = 1.0 * micron
+    w_0 = 0.9 * micron
+    x_spot = 15.0 * micron
+    x_r = PI * w_0 ** 2 / lambda0
+    rc = x_spot * (1.0 + (x_r / x_spot) ** 2)
+    w_bnd = w_0 * math.sqrt(1.0 + (x_spot / x_r) ** 2)
+    gouy = math.atan(x_spot / x_r)
+    deck = Deck("moving_window", nx, ny, 2, 0.0, 20.0e-6, 5.0e-6,
+                (abi.BC_SIMPLE_LASER, abi.BC_OPEN, abi.BC_OTHER, abi.BC_OPEN), [], precision=precision)
+    yv = deck.y_grid(np.arange(0, ny + 1))
+    amp = math.sqrt(1.0e15 / (CL * EPS0 / 2.0)) * 100.0  # intensity_w_cm2 (deck_laser_block.f90:136-139)
+    omega = 2.0 * PI * CL / lambda0
+    deck.lasers = [Laser(abi.BD_X_MIN, amp, omega, np.exp(-((yv - 0.0) / w_bnd) ** 2),
+                         2.0 * PI / lambda0 * yv ** 2 / (2.0 * rc) - gouy)]
+    t_k = 0.5
+    n = Species("Neutron", 0.0, 2000.0 * M0, 2.0, 1.0, temp_k=(t_k, t_k, t_k),
+                bc=(abi.BC_SIMPLE_LASER, abi.BC_OPEN, abi.BC_OTHER, abi.BC_OPEN))
+    n.capacity = int(2 * nx * ny * 1.3) + 4096
+    deck.species = [n]
+    deck.move_window = True
+    deck.window_v_x = 2.0e8
+    deck.window_start_time = 30.0e-15
+    deck.window_stop_time = 100.0e-15
+    deck.bc_after_move = (abi.BC_SIMPLE_OUTFLOW, abi.BC_SIMPLE_OUTFLOW, abi.BC_OTHER, abi.BC_OPEN)
+    deck.nsteps = int(math.ceil(200.0e-15 / set_dt(deck)))
+
+    def density(x):
+        return 0.5 + np.sin(np.asarray(x, dtype=np.float64) / 4.0e-6) ** 2
+
+    def load_grids(isp):
+        ng = abi.NG
+        ix = np.arange(1 - ng, nx + ng + 1)
+        xg = (deck.x_min + deck.dx / 2.0) + (ix - 1.0) * deck.dx  # x(ix), setup.F90:189-195
+        dens = np.repeat(density(xg)[None, :], ny + 2 * ng, axis=0)
+        temp = np.full((3, ny + 2 * ng, nx + 2 * ng), t_k)
+        return dens, temp, np.zeros_like(temp)
+
+    def inject(isp, time, x):
+        return (np.full(ny + 2, float(density(x))), np.full((3, ny + 2), t_k), np.zeros((3, ny + 2)))
+
+    deck.load_grids = load_grids
+    deck.inject = inject
+    return deck

@@ -65,6 +65,10 @@ SIGNATURES = {
     "cyl_push_only": (C.c_int, [H]),
     "cyl_kernel_timing": (C.c_int, [H, PD, PI64]),
     "cyl_get_stream": (C.c_int, [H, P(C.c_void_p)]),
+    "cyl_eval_atan2": (C.c_int, [I64, PD, PD, PD]),
+    "cyl_set_deck_fns": (C.c_int, [H, P(abi.DeckFns)]),
+    "cyl_host_load_species_grid": (C.c_int, [P(abi.GridDesc), P(abi.SpeciesDesc), P(abi.RngState), I64,
+                                             PD, PD, PD, PD, PD, PD, PD, PD, PD, PD, PI64, PI64]),
     "cyl_estimate_device_bytes": (C.c_int, [P(abi.GridDesc), P(abi.SpeciesDesc), I32, PI64]),
     "cyl_batch_create": (C.c_int, [I32, P(H)]),
     "cyl_batch_step": (C.c_int, [H, P(H), I32, I32]),

@@ -62,20 +62,25 @@ def host_load(deck: Deck, rng=None):
     g = deck.grid_desc()
     out = []
     id_base = 0
-    for s in deck.species:
+    for isp, s in enumerate(deck.species):
         d = s.desc()
         n = C.c_int64(0)
-        abi.check("cyl_host_load_species",
-                  lib.cyl_host_load_species(C.byref(g), C.byref(d), C.byref(rng), id_base,
-                                            None, None, None, None, None, None, None, None, C.byref(n)))
+        grids = deck.load_grids(isp) if deck.load_grids is not None else None
+        ga = [None, None, None]
+        if grids is not None:
+            ga = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in grids]
+        gp = [None if a is None else _p(a) for a in ga]
+        abi.check("cyl_host_load_species_grid",
+                  lib.cyl_host_load_species_grid(C.byref(g), C.byref(d), C.byref(rng), id_base, *gp,
+                                                 None, None, None, None, None, None, None, None, C.byref(n)))
         p = Particles(n.value)
         if s.immobile:
             out.append(Particles(0))
             continue
-        abi.check("cyl_host_load_species",
-                  lib.cyl_host_load_species(C.byref(g), C.byref(d), C.byref(rng), id_base,
-                                            _p(p.x), _p(p.y), _p(p.z), _p(p.px), _p(p.py), _p(p.pz),
-                                            _p(p.w), _p(p.id, PI64), C.byref(n)))
+        abi.check("cyl_host_load_species_grid",
+                  lib.cyl_host_load_species_grid(C.byref(g), C.byref(d), C.byref(rng), id_base, *gp,
+                                                 _p(p.x), _p(p.y), _p(p.z), _p(p.px), _p(p.py), _p(p.pz),
+                                                 _p(p.w), _p(p.id, PI64), C.byref(n)))
         p.resize(n.value)
         id_base += n.value
         out.append(p)
@@ -236,6 +241,9 @@ class Run:
         self.h = h
         self.nxg = deck.nx + 2 * abi.NG
         self.nyg = deck.ny + 2 * abi.NG
+        if deck.has_deck_fns():
+            self._fns, self._fns_keep = deck.deck_fns()
+            abi.check("cyl_set_deck_fns", self.lib.cyl_set_deck_fns(self.h, C.byref(self._fns)))
         if counter:
             seed = deck.seed if counter_seed is None else int(counter_seed)
             id_base = 0

@@ -50,6 +50,7 @@ extern "C" {
 #define CYL_ERR_OUT_OF_MEMORY 8  /* device allocation failed                 */
 #define CYL_ERR_SCRATCH 9        /* input larger than a fixed scratch buffer */
 #define CYL_ERR_IO 10            /* a file could not be written              */
+#define CYL_ERR_CALLBACK 11      /* a deck-expression callback returned an error */
 
 /* ---- boundary codes: the values of constants.F90:56-72 ------------------- */
 #define CYL_BC_PERIODIC 1
@@ -299,6 +300,66 @@ int cyl_sdf_read_particles(cyl_sdf_file f, const char* name, double* x, double* 
  * replaces), CYL_ERR_CAPACITY (a species larger than its capacity). */
 int cyl_restart_sdf(cyl_handle h, const char* path, const char* const* species_names);
 
+/* ---- deck expressions evaluated by the caller --------------------------
+ * While it steps, the reference evaluates some deck expressions through its
+ * parser (evaluate_with_parameters, parser/evaluate.F90:461):
+ *  - update_laser_omegas (laser.f90:276-328, from bfield_final_bcs): every
+ *    laser's omega, when it is a deck function (use_omega_function);
+ *  - outflow_bcs_x_min / x_max (laser.f90:444-451): for each laser between
+ *    its t_start and t_end, its phase and profile when they are functions of
+ *    time (laser_update_phase / _profile, laser.f90:201-253) and its time
+ *    profile (laser_time_profile, laser.f90:182-199);
+ *  - insert_particles (window.F90:196-222): at every window shift, every
+ *    species' temperature, drift and density along the x_max column.
+ * A caller that keeps the reference's parser (the Fortran driver) registers
+ * callbacks that evaluate them.  A step calls them on the calling host thread
+ * while it prepares that step, in the reference's order, before any of the
+ * step's work is enqueued; a chunk of steps is prepared step by step.  Each
+ * returns 0, or a non-zero value that makes the step return
+ * CYL_ERR_CALLBACK.  Without callbacks the descriptors' closed forms are
+ * used (cyl_laser_desc.t_profile, omega, profile and phase;
+ * cyl_species_desc.density_kind, temp and drift).  Lasers are numbered by
+ * their place in cyl_create's array, species likewise. */
+
+/* *t_env = laser_time_profile of laser `ilaser` at `time` (the step
+ * multiplies it by amp). */
+typedef int (*cyl_laser_time_fn)(void* user, int32_t ilaser, double time, double* t_env);
+/* *omega = omega(time) in rad/s of a laser whose omega is a deck function
+ * (laser_update_omega, laser.f90:255-272, with the freq / lambda conversion
+ * done); the step integrates its phase, phase += omega dt (laser.f90:307-309).
+ * The phase of the other lasers is omega * time. */
+typedef int (*cyl_laser_omega_fn)(void* user, int32_t ilaser, double time, double* omega);
+/* The laser's profile or phase at y(ir), ir = 0..ny, at `time`: ny+1 values
+ * written over the laser's current array. */
+typedef int (*cyl_laser_array_fn)(void* user, int32_t ilaser, double time, double* values);
+/* insert_particles' columns of species `ispecies` at a window shift: at
+ * pack_ix = nx, i.e. x = x(nx) of the grid before the shift, and `time`, for
+ * rows iy = 0..ny+1: density[iy] (m^-3), temperature[iy + (ny+2) dir] (K) and
+ * drift[iy + (ny+2) dir] (kg m/s), dir = 0, 1, 2 (Fortran's (0:ny+1, 1:3)).
+ * The step clamps the density to density_max and zeroes it below
+ * density_min, as insert_particles does. */
+typedef int (*cyl_inject_fn)(void* user, int32_t ispecies, double time, double x, double* density,
+                             double* temperature, double* drift);
+
+typedef struct cyl_deck_fns {
+  void* user;                     /* passed back to every callback              */
+  cyl_laser_time_fn laser_time;   /* NULL: cyl_laser_desc.t_profile             */
+  cyl_laser_omega_fn laser_omega; /* called for the lasers of omega_fn_mask     */
+  cyl_laser_array_fn laser_profile; /* called for the lasers of profile_fn_mask */
+  cyl_laser_array_fn laser_phase;   /* called for the lasers of phase_fn_mask   */
+  uint32_t omega_fn_mask;         /* bit i: laser i's omega is a deck function  */
+  uint32_t profile_fn_mask;       /* bit i: laser i's profile depends on time   */
+  uint32_t phase_fn_mask;         /* bit i: laser i's phase depends on time     */
+  cyl_inject_fn inject;           /* NULL: cyl_species_desc density_kind, temp, drift */
+} cyl_deck_fns;
+
+/* Register the callbacks of a run (fns == NULL clears them); the struct is
+ * copied.  The window injection drawn on the device (CYL_RNG_COUNTER) takes
+ * its columns from the descriptors: an inject callback with it is
+ * CYL_ERR_UNSUPPORTED, here and in cyl_set_injection_stream.  A mask bit
+ * without its callback, or a bit beyond the run's lasers, is CYL_ERR_BAD_ARG. */
+int cyl_set_deck_fns(cyl_handle h, const cyl_deck_fns* fns);
+
 /* Device loading and window injection from a counter-based stream
  * (Philox4x32-10 keyed by seed, one counter per particle) instead of the
  * reference's serial KISS stream: the loader and injector of the reference
@@ -389,7 +450,9 @@ int cyl_sort_particles(cyl_handle h);
 
 /* Cell-sort indices of the live particles, in device order:
  * cell_x = FLOOR((x - x_grid_min_local)/dx + 1.5),
- * cell_y = FLOOR((r - y_grid_min_local)/dy + 1.5)  (split_particle.F90:61-62). */
+ * cell_y = FLOOR((r - y_grid_min_local)/dy + 1.5)  (split_particle.F90:61-62).
+ * With cell_x and cell_y both NULL, *n_inout receives the live count; passing
+ * only one of them is CYL_ERR_BAD_ARG. */
 int cyl_cell_indices(cyl_handle h, int32_t ispecies, int32_t* cell_x,
                      int32_t* cell_y, int64_t* n_inout);
 
@@ -405,8 +468,9 @@ int cyl_cell_indices(cyl_handle h, int32_t ispecies, int32_t* cell_x,
  * species with more particle slots (live + removed since the last sort) is
  * rejected with CYL_ERR_SCRATCH.  The first call on a device looks the scratch
  * up (cudaGetSymbolAddress) and should come before any stream capture.  The
- * scratch is shared by every handle of the process: calls that overlap in
- * time race on it. */
+ * call works on the handle's device whatever device the caller has current,
+ * and restores the caller's.  The scratch is shared by every handle of the
+ * process: calls that overlap in time race on it. */
 #define CYL_NOALLOC_MAX_PARTICLES 262144
 int cyl_cell_indices_noalloc(cyl_handle h, int32_t ispecies, int32_t* cell_x,
                              int32_t* cell_y, int64_t* n_inout);
@@ -468,6 +532,14 @@ int cyl_kernel_timing(cyl_handle h, double* push_ms_avg, int64_t* launches);
  * enqueued on, so that a caller can time the steps with its own CUDA events
  * on that stream.  No counterpart in the reference. */
 int cyl_get_stream(cyl_handle h, void** stream_out);
+
+/* out[i] = atan2(y[i], x[i]) as the FP64 form's push evaluates theta on the
+ * device (the correctly rounded routine of include/cyl_math.h, which the
+ * oracle also evaluates in its "shared" mode), for i < n.  Host arrays.  No
+ * counterpart in the reference: it lets a test show that the device and host
+ * builds of that routine agree bit for bit.  Synchronous; allocates device
+ * scratch for the call. */
+int cyl_eval_atan2(int64_t n, const double* y, const double* x, double* out);
 
 /* Device bytes cyl_create would allocate for these descriptors (an upper
  * bound; used for admission against an HBM budget).  Host only. */
@@ -574,6 +646,22 @@ int cyl_host_load_species(const cyl_grid_desc* grid, const cyl_species_desc* sp,
                           cyl_rng_state* rng, int64_t id_base, double* x,
                           double* y, double* z, double* px, double* py,
                           double* pz, double* w, int64_t* id, int64_t* n_inout);
+
+/* cyl_host_load_species with the deck's density, temperature and drift
+ * evaluated by the caller on the whole grid with ghosts, as
+ * setup_particle_density (helper.F90:669-811) and the temperature and
+ * drift arrays of auto_load (helper.F90:130-160, particle_temperature.F90:
+ * 30-81) hold them: index (ix + ng - 1) + (nx + 2 ng)(iy + ng - 1) for
+ * ix = 1-ng..nx+ng, iy = 1-ng..ny+ng (Fortran's (1-ng:nx+ng, 1-ng:ny+ng));
+ * temperature (K) and drift (kg m/s) hold three such planes, x, y, z.  The
+ * loader applies the density's periodic x wrap, density_max clamp and
+ * density_min cut as it does to the closed form.  A NULL array takes the
+ * descriptor's closed form for that quantity. */
+int cyl_host_load_species_grid(const cyl_grid_desc* grid, const cyl_species_desc* sp,
+                               cyl_rng_state* rng, int64_t id_base, const double* density,
+                               const double* temperature, const double* drift, double* x,
+                               double* y, double* z, double* px, double* py,
+                               double* pz, double* w, int64_t* id, int64_t* n_inout);
 
 #ifdef __cplusplus
 }

@@ -236,6 +236,7 @@ struct Sim {
   Col ex_xmax, er_xmax, et_xmax, bx_xmax, br_xmax, bt_xmax;
   std::vector<Species> sp;
   std::vector<Laser> lasers;
+  cyl_deck_fns fns{};  // deck-expression callbacks (orc_set_deck_fns)
   Rng rng;
   int smooth, smooth_its, smooth_comp_its, smooth_stride;
   std::vector<Field> thread_j;  // per-thread currents of the multi-threaded timing form
@@ -592,19 +593,40 @@ double laser_time_profile(const Laser& L, double time) {
   return 1.0;
 }
 
-// update_laser_omegas (laser.f90:276-328), constant omega
+// update_laser_omegas (laser.f90:276-328): an omega that is a deck function
+// (laser_update_omega, evaluated by the caller's callback) integrates the
+// phase with the current dt, the others give omega * time.
 void update_laser_omegas(Sim& s) {
-  for (auto& L : s.lasers) L.current_integral_phase = L.d.omega * s.time;
+  for (size_t i = 0; i < s.lasers.size(); ++i) {
+    Laser& L = s.lasers[i];
+    if (s.fns.laser_omega && ((s.fns.omega_fn_mask >> i) & 1u)) {
+      double om = L.d.omega;
+      s.fns.laser_omega(s.fns.user, (int32_t)i, s.time, &om);
+      L.d.omega = om;
+      L.current_integral_phase = L.current_integral_phase + L.d.omega * s.dt;
+    } else {
+      L.current_integral_phase = L.d.omega * s.time;
+    }
+  }
 }
 
 void laser_sources(Sim& s, int bd, std::vector<double>& s1, std::vector<double>& s2) {
   s1.assign(s.ny + 1, 0.0);
   s2.assign(s.ny + 1, 0.0);
   if (!s.add_laser[bd]) return;
-  for (auto& L : s.lasers) {
+  for (size_t i = 0; i < s.lasers.size(); ++i) {
+    Laser& L = s.lasers[i];
     if (L.d.boundary != bd) continue;
     if (s.time >= L.d.t_start && s.time <= L.d.t_end) {
-      double t_env = laser_time_profile(L, s.time) * L.d.amp;
+      // laser.f90:449-451: phase and profile functions, then the time profile
+      const cyl_deck_fns& f = s.fns;
+      if (f.laser_phase && ((f.phase_fn_mask >> i) & 1u)) f.laser_phase(f.user, (int32_t)i, s.time, L.phase.data());
+      if (f.laser_profile && ((f.profile_fn_mask >> i) & 1u))
+        f.laser_profile(f.user, (int32_t)i, s.time, L.profile.data());
+      double tp;
+      if (f.laser_time) f.laser_time(f.user, (int32_t)i, s.time, &tp);
+      else tp = laser_time_profile(L, s.time);
+      double t_env = tp * L.d.amp;
       for (int ir = 0; ir <= s.ny; ++ir) {
         double base = t_env * L.profile[ir] * std::sin(L.current_integral_phase + L.phase[ir]);
         s1[ir] = s1[ir] + base * std::cos(L.d.pol_angle);
@@ -915,6 +937,17 @@ void smooth_mode_array(Sim& s, Field& f) {
 
 int g_threads = 1;
 
+// theta = ATAN2(z, y) of push_particles (particles.F90:321,522).  The
+// reference calls the platform libm (gfortran's ATAN2 is the C library's
+// atan2), and so does the oracle by default.  Mode 1 evaluates the shared
+// correctly rounded cyl_atan2 of include/cyl_math.h instead, the routine the
+// CUDA kernel runs: libm's atan2 is one ulp off on about 0.09 % of
+// arguments (glibc 2.39), and the deposit's (m dtheta)^-2 factors carry such
+// an ulp into J_theta (2e-12 after one push, up to 7e-9 relative after 20
+// steps of a thermal plasma), so multi-step comparisons at 1e-10 use mode 1.
+int g_atan2_mode = 0;
+inline double theta_of(double z, double y) { return g_atan2_mode ? cyl_atan2(z, y) : std::atan2(z, y); }
+
 struct Geom {
   std::vector<double> inv_area_rt, inv_area_xt, inv_volume, ratio_area_xt;
   int lo;  // index offset: arrays start at 1-jng (inv_area_xt at 0-jng)
@@ -973,7 +1006,7 @@ void push_one(Sim& s, const Geom& g, Species& spc, size_t i, double part_q, doub
   double part_r = std::sqrt(part_y * part_y + part_z * part_z);
   double part_r_local = part_r - y_grid_min_local;
   cplx exp_min_itheta = mk(part_y / part_r, (-part_z) / part_r);
-  double theta_05 = cyl_atan2(part_z, part_y);
+  double theta_05 = theta_of(part_z, part_y);
   cplx exp_min_itheta_05 = exp_min_itheta;
   cplx exp_itheta_05 = crecip(exp_min_itheta_05);
 
@@ -1088,7 +1121,7 @@ void push_one(Sim& s, const Geom& g, Species& spc, size_t i, double part_q, doub
   part_r = std::sqrt(part_y * part_y + part_z * part_z);
   part_r_local = part_r - y_grid_min_local;
   cplx exp_itheta_15 = mk(part_y / part_r, part_z / part_r);
-  double theta_15 = cyl_atan2(part_z, part_y);
+  double theta_15 = theta_of(part_z, part_y);
   cplx exp_idtheta = exp_itheta_15 * exp_min_itheta_05;
   double dtheta = theta_15 - theta_05;
   for (int k = 0; k < 5; ++k) { gx[k] = hx[k]; gy[k] = hy[k]; }
@@ -1536,13 +1569,19 @@ void insert_particles(Sim& s) {
     double dmin = d.density_min, dmax = d.density_max;
     std::vector<double> density(ny + 2), temperature((ny + 2) * 3), drift((ny + 2) * 3);
     const double xpack = s.xg(s.nx);
-    for (int i = 0; i < 3; ++i)
-      for (int iy = 0; iy <= ny + 1; ++iy) {
-        temperature[iy + (ny + 2) * i] = d.temp[i];
-        drift[iy + (ny + 2) * i] = d.drift[i];
-      }
+    if (s.fns.inject) {
+      // window.F90:196-212: the deck's columns at pack_ix = nx
+      s.fns.inject(s.fns.user, (int32_t)(&spc - s.sp.data()), s.time, xpack, density.data(), temperature.data(),
+                   drift.data());
+    } else {
+      for (int i = 0; i < 3; ++i)
+        for (int iy = 0; iy <= ny + 1; ++iy) {
+          temperature[iy + (ny + 2) * i] = d.temp[i];
+          drift[iy + (ny + 2) * i] = d.drift[i];
+        }
+      for (int iy = 0; iy <= ny + 1; ++iy) density[iy] = density_at(d, xpack);
+    }
     for (int iy = 0; iy <= ny + 1; ++iy) {
-      density[iy] = density_at(d, xpack);
       if (density[iy] > dmax) density[iy] = dmax;
       if (density[iy] < dmin) density[iy] = 0.0;
     }
@@ -1761,15 +1800,20 @@ Shape shape_at(const Sim& s, double px, double py, double pz) {
 // auto_load for one thermal species: setup_particle_density + load_particles
 // (helper.F90:373-663, 669-811) and setup_particle_temperature x3
 // (particle_temperature.F90:30-81).
-void load_species(Sim& s, Species& spc) {
+// dens_in, temp_in, drift_in: the deck's density, temperature and drift on
+// the ghosted grid, evaluated by the caller (NULL: the closed forms).
+void load_species(Sim& s, Species& spc, const double* dens_in = nullptr, const double* temp_in = nullptr,
+                  const double* drift_in = nullptr) {
   const cyl_species_desc& d = spc.d;
   const int nx = s.nx, ny = s.ny;
   const int W = nx + 2 * NG;
   auto at = [&](int ix, int iy) { return (size_t)(ix + NG - 1) + (size_t)W * (size_t)(iy + NG - 1); };
   std::vector<double> density((size_t)W * (ny + 2 * NG));
   std::vector<char> dmap(density.size(), 0);
+  const size_t plane = density.size();
   for (int iy = 1 - NG; iy <= ny + NG; ++iy)
-    for (int ix = 1 - NG; ix <= nx + NG; ++ix) density[at(ix, iy)] = density_at(d, s.xg(ix));
+    for (int ix = 1 - NG; ix <= nx + NG; ++ix)
+      density[at(ix, iy)] = dens_in ? dens_in[at(ix, iy)] : density_at(d, s.xg(ix));
   // field_bc(density): periodic x self-wrap only
   if (s.bc_field[CYL_BD_X_MAX] == CYL_BC_PERIODIC)
     for (int iy = 1 - NG; iy <= ny + NG; ++iy)
@@ -1853,10 +1897,12 @@ void load_species(Sim& s, Species& spc) {
     for (size_t p = 0; p < spc.n(); ++p) {
       Shape sh = shape_at(s, spc.x[p], spc.y[p], spc.z[p]);
       double tl = 0.0, dl = 0.0;
+      // particle_temperature.F90:58-66: temperature(cell_x+ix, cell_y+iy)
       for (int iy = SF_MIN; iy <= SF_MAX; ++iy)
         for (int ix = SF_MIN; ix <= SF_MAX; ++ix) {
-          tl = tl + (sh.gx[ix + 1] * sh.gy[iy + 1]) * d.temp[dir];
-          dl = dl + (sh.gx[ix + 1] * sh.gy[iy + 1]) * d.drift[dir];
+          const size_t c = at(sh.cell_x + ix, sh.cell_y + iy) + plane * (size_t)dir;
+          tl = tl + (sh.gx[ix + 1] * sh.gy[iy + 1]) * (temp_in ? temp_in[c] : d.temp[dir]);
+          dl = dl + (sh.gx[ix + 1] * sh.gy[iy + 1]) * (drift_in ? drift_in[c] : d.drift[dir]);
         }
       double stdev = std::sqrt(tl * KB * d.mass);
       double v = s.rng.box_muller(stdev, dl);
@@ -2065,6 +2111,20 @@ int orc_load_species(orc_handle h, int32_t isp) {
   Sim* s = (Sim*)h;
   if (isp < 0 || isp >= (int)s->sp.size()) return CYL_ERR_BAD_ARG;
   load_species(*s, s->sp[isp]);
+  return CYL_OK;
+}
+
+int orc_load_species_grid(orc_handle h, int32_t isp, const double* density, const double* temperature,
+                          const double* drift) {
+  Sim* s = (Sim*)h;
+  if (isp < 0 || isp >= (int)s->sp.size()) return CYL_ERR_BAD_ARG;
+  load_species(*s, s->sp[isp], density, temperature, drift);
+  return CYL_OK;
+}
+
+int orc_set_deck_fns(orc_handle h, const cyl_deck_fns* fns) {
+  Sim* s = (Sim*)h;
+  s->fns = fns ? *fns : cyl_deck_fns{};
   return CYL_OK;
 }
 
@@ -2288,6 +2348,10 @@ int orc_number_density(orc_handle h, int32_t isp, double* data) {
 void orc_set_threads(int32_t n) { g_threads = n < 1 ? 1 : n; }
 
 double orc_atan2(double y, double x) { return cyl_atan2(y, x); }
+void orc_atan2_many(int64_t n, const double* y, const double* x, double* out) {
+  for (int64_t i = 0; i < n; ++i) out[i] = cyl_atan2(y[i], x[i]);
+}
+void orc_set_atan2(int32_t mode) { g_atan2_mode = mode ? 1 : 0; }
 void orc_sincos_turn(double u, double* s, double* c) { cyl_sincos_turn(u, s, c); }
 
 double orc_dx(orc_handle h) { return ((Sim*)h)->dx; }

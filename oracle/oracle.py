@@ -78,6 +78,10 @@ def load():
         "orc_charge_density": (C.c_int, [H, PD]),
         "orc_number_density": (C.c_int, [H, C.c_int32, PD]),
         "orc_atan2": (C.c_double, [C.c_double, C.c_double]),
+        "orc_atan2_many": (None, [C.c_int64, PD, PD, PD]),
+        "orc_set_deck_fns": (C.c_int, [H, C.POINTER(abi.DeckFns)]),
+        "orc_load_species_grid": (C.c_int, [H, C.c_int32, PD, PD, PD]),
+        "orc_set_atan2": (None, [C.c_int32]),
         "orc_sincos_turn": (None, [C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
         "orc_set_threads": (None, [C.c_int32]),
         "orc_dx": (C.c_double, [H]),
@@ -97,13 +101,24 @@ STAGE = {"update_e": 0, "efield_bcs": 1, "update_b": 2, "bfield_bcs_mpi": 3, "pu
          "moving_window": 9, "eb_half": 10, "eb_final": 11}
 
 
-class Oracle:
-    """One run of the CPU restatement, fed the same inputs as the GPU run."""
+ATAN2 = {"libm": 0, "shared": 1}
 
-    def __init__(self, deck, particles=None, rng=None, load_species=False, counter_seed=None):
+
+class Oracle:
+    """One run of the CPU restatement, fed the same inputs as the GPU run.
+
+    atan2: "libm" (default) takes theta with the platform's atan2, as the
+    reference does (particles.F90:321,522); "shared" with the correctly
+    rounded cyl_atan2 that the CUDA kernel evaluates (include/cyl_math.h).
+    They differ where libm is not correctly rounded (about 0.09 % of
+    arguments with glibc 2.39); tests that compare many steps at 1e-10 use
+    "shared"."""
+
+    def __init__(self, deck, particles=None, rng=None, load_species=False, counter_seed=None, atan2="libm"):
         from cylindrical_epoch_gb300 import abi
         self.abi = abi
         self.lib = load()
+        self.atan2_mode = ATAN2[atan2]
         self.deck = deck
         g = deck.grid_desc()
         sp = deck.species_descs()
@@ -127,8 +142,19 @@ class Oracle:
             self.lib.orc_set_injection_stream(self.h, abi.RNG_COUNTER, int(counter_seed))
         elif load_species:
             for i in range(len(deck.species)):
-                if not deck.species[i].immobile:
+                if deck.species[i].immobile:
+                    continue
+                grids = deck.load_grids(i) if deck.load_grids is not None else None
+                if grids is None:
                     self.lib.orc_load_species(self.h, i)
+                else:
+                    ga = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in grids]
+                    PDc = C.POINTER(C.c_double)
+                    self.lib.orc_load_species_grid(self.h, i, *[None if a is None else a.ctypes.data_as(PDc)
+                                                                for a in ga])
+        if deck.has_deck_fns():
+            self._fns, self._fns_keep = deck.deck_fns()
+            self.lib.orc_set_deck_fns(self.h, C.byref(self._fns))
         if particles is not None:
             for i, p in enumerate(particles):
                 self.set_particles(i, p)
@@ -179,16 +205,20 @@ class Oracle:
         return r
 
     def initialise(self):
+        self.lib.orc_set_atan2(self.atan2_mode)
         self.lib.orc_initialise(self.h)
 
     def step(self, n=1):
+        self.lib.orc_set_atan2(self.atan2_mode)
         self.lib.orc_step(self.h, n)
 
     def step_to_output(self, n=1):
+        self.lib.orc_set_atan2(self.atan2_mode)
         if self.lib.orc_step_to_output(self.h, n) != 0:
             raise RuntimeError("orc_step_to_output")
 
     def finish_step(self):
+        self.lib.orc_set_atan2(self.atan2_mode)
         self.lib.orc_finish_step(self.h)
 
     def restart(self, step, time, xb_min, x_grid_min, window_shift_fraction=None):
@@ -200,6 +230,7 @@ class Oracle:
             raise RuntimeError(f"orc_restart: {rc}")
 
     def stage(self, name):
+        self.lib.orc_set_atan2(self.atan2_mode)
         rc = self.lib.orc_stage(self.h, STAGE[name])
         if rc != 0:
             raise RuntimeError(name)

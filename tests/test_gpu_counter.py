@@ -37,7 +37,7 @@ def test_device_load_matches_oracle(gpu_lib, ppc):
     from oracle.oracle import Oracle
     deck = cg.thermal_plasma(nx=64, ny=32, ppc=ppc)
     gpu = cg.Run(deck, rng_mode=abi.RNG_COUNTER, counter_seed=11, initialise=False)
-    orc = Oracle(deck, counter_seed=11)
+    orc = Oracle(deck, counter_seed=11, atan2="shared")
     a, b = match_by_id(gpu.particles(0), orc.particles(0))
     assert a.n == b.n == int(np.floor(ppc * 64 * 32))
     for k in ("x", "y", "z", "w"):
@@ -54,7 +54,7 @@ def test_device_load_mixed_form(gpu_lib):
     from oracle.oracle import Oracle
     deck = cg.wakefield(nx=128, ny=32, ppc=2.5, density=3.0e24, ramp=2.0e-6, precision=abi.PREC_MIXED)
     gpu = cg.Run(deck, rng_mode=abi.RNG_COUNTER, counter_seed=5, initialise=False)
-    orc = Oracle(deck, counter_seed=5)
+    orc = Oracle(deck, counter_seed=5, atan2="shared")
     a, b = match_by_id(gpu.particles(0), orc.particles(0))
     for k in ("x", "y", "z", "w"):
         assert rel_l2(getattr(a, k), getattr(b, k)) < 1e-6, k
@@ -64,7 +64,7 @@ def test_counter_window_parity(gpu_lib):
     from oracle.oracle import Oracle
     deck = _wake()
     gpu = cg.Run(deck, rng_mode=abi.RNG_COUNTER, counter_seed=3, initialise=False)
-    orc = Oracle(deck, counter_seed=3)
+    orc = Oracle(deck, counter_seed=3, atan2="shared")
     gpu.lib.cyl_initialise(gpu.h)
     orc.initialise()
     for chunk in (1, 15, 24, 40):
@@ -164,7 +164,7 @@ def test_counter_two_species_window_parity(gpu_lib):
     deck = cg.wakefield(nx=128, ny=32, ppc=3, density=3.0e24, ramp=2.0e-6, ions=ions)
     deck.window_start_time = 20 * 5.0e-17
     gpu = cg.Run(deck, rng_mode=abi.RNG_COUNTER, counter_seed=17, initialise=False)
-    orc = Oracle(deck, counter_seed=17)
+    orc = Oracle(deck, counter_seed=17, atan2="shared")
     ids = np.concatenate([gpu.particles(0).id, gpu.particles(1).id])
     assert np.array_equal(np.sort(ids), np.arange(ids.size))
     gpu.lib.cyl_initialise(gpu.h)

@@ -51,7 +51,7 @@ def test_output_point_matches_oracle(gpu_lib):
     from oracle.oracle import Oracle
     deck = _deck()
     gpu = cg.Run(deck, rng_mode=abi.RNG_COUNTER, counter_seed=5, initialise=False)
-    orc = Oracle(deck, counter_seed=5)
+    orc = Oracle(deck, counter_seed=5, atan2="shared")
     gpu.lib.cyl_initialise(gpu.h)
     orc.initialise()
     gpu.step_to_output(DUMP_STEP)
@@ -80,7 +80,7 @@ def test_restart_matches_oracle(gpu_lib, tmp_path):
     assert (sb.step, sb.time, sb.xb_min, sb.x_grid_min, sb.n_shifts, sb.n_live[0]) == \
         (sa.step, sa.time, sa.xb_min, sa.x_grid_min, sa.n_shifts, sa.n_live[0])
     # the oracle restarted from the same file
-    orc = Oracle(deck)
+    orc = Oracle(deck, atan2="shared")
     orc.lib.orc_set_injection_stream(orc.h, abi.RNG_COUNTER, 6)
     with cg.SdfFile(p) as f:
         for n in abi.FIELD_NAMES:

@@ -41,6 +41,68 @@ def test_product_loader_bit_exact_vs_oracle(lib, name):
         assert getattr(rng, k) == getattr(r, k), k
 
 
+def _grid_deck():
+    """A wakefield deck whose density, temperature and drift are given as
+    grids (as the Fortran driver evaluates deck expressions): an x- and
+    r-dependent density with cells below density_min, a temperature that
+    varies per direction and cell, a drift in x."""
+    deck = cg.wakefield(nx=48, ny=20, ppc=3, density=3.0e24, ramp=1.0e-6)
+    ng, nx, ny = abi.NG, deck.nx, deck.ny
+    ix = np.arange(1 - ng, nx + ng + 1)
+    iy = np.arange(1 - ng, ny + ng + 1)
+    xg = (deck.x_min + deck.dx / 2.0) + (ix - 1.0) * deck.dx
+    yg = deck.dy / 2.0 + (iy - 1.0) * deck.dy
+    dens = 3.0e24 * (0.5 + np.sin(xg / 0.3e-6)[None, :] ** 2) * np.exp(-(yg[:, None] / 1.5e-6) ** 2)
+    dens[:, :8] = 0.0
+    temp = np.stack([1.0e5 * (1 + k + np.cos(yg[:, None] / 1e-6) + 0 * xg[None, :]) for k in range(3)])
+    drift = np.zeros_like(temp)
+    drift[0] = 1.0e-24 * (1.0 + xg[None, :] / deck.x_max)
+    deck.load_grids = lambda isp: (dens, temp, drift)
+    return deck
+
+
+def test_grid_loader_bit_exact_vs_oracle(lib):
+    """cyl_host_load_species_grid (density, temperature and drift as grids)
+    against the oracle's loader given the same grids: bit for bit."""
+    deck = _grid_deck()
+    parts, rng = cg.host_load(deck)
+    orc = oracle.Oracle(deck, load_species=True)
+    a = parts[0].sorted_by_id()
+    b = orc.particles(0).sorted_by_id()
+    assert a.n > 1000 and np.array_equal(a.id, b.id)
+    for k in ("x", "y", "z", "px", "py", "pz", "w"):
+        assert np.array_equal(getattr(a, k), getattr(b, k)), k
+    r = orc.rng_state()
+    for k in ("x", "y", "z", "w", "box_muller_cached"):
+        assert getattr(rng, k) == getattr(r, k), k
+    # the grids were used: no particle in the empty columns, drift visible
+    assert a.x.min() >= deck.x_min + 3 * deck.dx and a.px.mean() > 0.5e-24  # columns ix <= 3 are empty
+
+
+def test_moving_window_deck_loads_like_closed_form(lib):
+    """The reference's moving_window.deck: its x-dependent density through
+    the grid loader matches the oracle, and a uniform grid equal to the
+    closed form loads the same particles as the closed form."""
+    deck = cg.moving_window_deck()
+    parts, rng = cg.host_load(deck)
+    orc = oracle.Oracle(deck, load_species=True)
+    a, b = parts[0].sorted_by_id(), orc.particles(0).sorted_by_id()
+    assert a.n == 2 * deck.nx * deck.ny
+    for k in ("x", "y", "z", "px", "py", "pz", "w"):
+        assert np.array_equal(getattr(a, k), getattr(b, k)), k
+    plain = cg.wakefield(nx=32, ny=12, ppc=2, density=2.0e24, ramp=1.0)
+    p0, _ = cg.host_load(plain)
+    ng = abi.NG
+    shape = (plain.ny + 2 * ng, plain.nx + 2 * ng)
+    ix = np.arange(1 - ng, plain.nx + ng + 1)
+    xg = (plain.x_min + plain.dx / 2.0) + (ix - 1.0) * plain.dx
+    dens = np.repeat(plain.species[0].density_at(xg)[None, :], shape[0], axis=0)
+    plain.load_grids = lambda isp: (dens, None, None)
+    p1, _ = cg.host_load(plain)
+    for k in ("x", "y", "z", "px", "py", "pz", "w"):
+        assert np.array_equal(getattr(p0[0], k), getattr(p1[0], k)), k
+
+
 def test_kiss_stream_matches_oracle(lib):
     s = abi.RngState()
     lib.cyl_rng_init(C.byref(s), 7842432)

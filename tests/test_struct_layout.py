@@ -17,7 +17,7 @@ PAIRS = {
     "cyl_grid_desc": abi.GridDesc, "cyl_species_desc": abi.SpeciesDesc, "cyl_laser_desc": abi.LaserDesc,
     "cyl_rng_state": abi.RngState, "cyl_run_state": abi.RunState, "cyl_diag": abi.Diag,
     "cyl_sdf_desc": abi.SdfDesc, "cyl_sdf_species": abi.SdfSpecies, "cyl_sdf_info": abi.SdfInfo,
-    "cyl_job_desc": abi.JobDesc, "cyl_job_result": abi.JobResult,
+    "cyl_job_desc": abi.JobDesc, "cyl_job_result": abi.JobResult, "cyl_deck_fns": abi.DeckFns,
 }
 
 
