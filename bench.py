@@ -351,6 +351,67 @@ def run_serve(args):
     return 0
 
 
+def serving_leg(args):
+    """The scan of decks through the request loop (the C5 workload): a seeded
+    stream of args.jobs wakefield decks with Poisson arrivals, admitted
+    against the HBM budget, each run on its own stream as slots and memory
+    free up.  p50 / p99 completion latency (queueing included), the
+    aggregate particle-steps/s and its HBM-roofline fraction (each deck's
+    mixed-form push bytes, 60 B + (6 8 + 3 16 2) M / ppc B per particle-step,
+    summed over its particle-steps, over the makespan), beside the plain FP64
+    form run one deck at a time on a sample of the decks."""
+    import numpy as np
+    import torch
+    import cylindrical_epoch_gb300 as cg
+    from cylindrical_epoch_gb300 import abi, serve
+    decks = scan_decks(args.jobs)
+    gaps = np.random.default_rng(7).exponential(args.arrival, size=len(decks))
+    with serve.Server(0, args.workers) as srv:
+        ids = []
+        for (deck, steps), gap in zip(decks, gaps):
+            ids.append(srv.submit(deck, steps))
+            time.sleep(float(gap))
+        res = [srv.wait(i, 3600.0) for i in ids]
+    ok = [r for r in res if r.status == abi.JOB_DONE]
+    st = serve.latency_stats(ok) if ok else None
+    peak, peak_kind = _peaks()
+    alg = 0.0
+    for (deck, _), r in zip(decks, res):
+        if r.status == abi.JOB_DONE:
+            alg += r.particle_steps * (60.0 + (6 * 8 + 3 * 16 * 2) * deck.n_mode / deck.species[0].npart_per_cell)
+    fp64 = []
+    for deck, steps in decks[:args.fp64_sample]:
+        d64 = cg.wakefield(nx=deck.nx, ny=deck.ny, n_mode=deck.n_mode, ppc=int(deck.species[0].npart_per_cell),
+                           density=deck.species[0].density, precision=abi.PREC_FP64)
+        parts, rng = cg.host_load(d64)
+        run = cg.Run(d64, particles=parts, rng=rng)
+        k = min(steps, args.fp64_steps_max)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        run.step(k, graph=True)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        s = run.state()
+        fp64.append(0.5 * (sum(p.n for p in parts) + s.n_live[0]) * k / dt)
+        run.close()
+    fp64_rate = float(np.mean(fp64)) if fp64 else None
+    out = {"workload": f"{len(decks)} wakefield scan decks, Poisson arrivals mean {args.arrival} s, "
+                       "nz {512,1024,2048}, nr {64,128,256}, m 0..1|0..2, a0 U[0.5,3], n logU[5e23,5e24], "
+                       "4-16 ppc, 500-2000 steps, mixed form, host-loaded (the reference's KISS stream)",
+           "workers": args.workers, "hbm_budget": "free memory - 2 GiB", "failed_jobs": len(res) - len(ok)}
+    if st:
+        out.update({"value": st["aggregate"], "unit": "particle-steps/s", "p50_s": st["p50_s"], "p99_s": st["p99_s"],
+                    "mean_s": st["mean_s"], "makespan_s": st["makespan_s"], "particle_steps": st["particle_steps"],
+                    "roofline": {"bound": "hbm", "achieved": alg / st["makespan_s"] / 1e9, "peak": peak,
+                                 "unit": "GB/s", "frac": alg / st["makespan_s"] / 1e9 / peak, "peak_kind": peak_kind,
+                                 "note": "push algorithmic bytes of every job over the makespan"}})
+    out["fp64_one_at_a_time"] = {"value": fp64_rate, "unit": "particle-steps/s", "sample": len(fp64),
+                                 "steps_per_deck_max": args.fp64_steps_max,
+                                 "estimated_makespan_s": (st["particle_steps"] / fp64_rate) if (fp64_rate and st)
+                                 else None}
+    return out
+
+
 def _config(args, deck, form):
     return {"workload": f"{deck.name} {deck.nx}x{deck.ny} m=0..{deck.n_mode - 1} "
                         f"{deck.species[0].npart_per_cell:g} ppc, steps [W, W+K) of the deck from t=0",
@@ -378,6 +439,8 @@ def main():
     ap.add_argument("--window-start", type=int, default=1100,
                     help="first step of the moving-window-phase leg (0: skip the leg)")
     ap.add_argument("--window-steps", type=int, default=32)
+    ap.add_argument("--no-serve-leg", dest="serve_leg", action="store_false",
+                    help="skip the scan-serving leg of the default line")
     ap.add_argument("--serve", action="store_true", help="parameter-scan serving benchmark")
     ap.add_argument("--jobs", type=int, default=64)
     ap.add_argument("--arrival", type=float, default=0.5, help="mean Poisson arrival gap (s)")
@@ -528,6 +591,9 @@ def main():
     window = None
     if form == "mixed" and args.deck == "wakefield" and args.window_start > 0:
         window = window_phase(args, parts, rng, graph, tile[0] if tile else None)
+    serving = None
+    if rank == 0 and world == 1 and form == "mixed" and args.deck == "wakefield" and args.serve_leg:
+        serving = serving_leg(args)
     base = None
     if rank == 0 and world == 1 and not args.no_cpu:
         base = cpu_baseline(build_deck(args.deck, "fp64", args.modes), parts, rng)
@@ -556,6 +622,8 @@ def main():
             line["accuracy"] = accuracy
         if window:
             line["window_phase"] = window
+        if serving:
+            line["serving"] = serving
         print(json.dumps(line))
     run.close()
     if dist:
