@@ -10,9 +10,10 @@ with the rows of the arrays with Ex's or Etheta's stagger shifted up by one
 variant with the _old arrays; the particle blocks (diagnostics.F90:614-762,
 write_particle_variable and write_particle_grid): per variable one point
 variable per species, then one 3D point mesh per species, species without
-particles left out.  Parity status: unpinned (no reference SDF
-files or buildable reference reader here); the layout is restated from the
-reference's SDF library sources.
+particles left out.  The same dumps are read by the reference's own SDF C
+library in tests/test_sdf_reference_reader.py, which pins the layout; this
+file checks the byte-level details (block headers, summary, offsets) that a
+reader does not expose.
 """
 import numpy as np
 
