@@ -15,7 +15,9 @@ by results that do not come from the oracle itself:
 * energy conservation of the vacuum Yee update with conducting walls;
 * the deposit's discrete continuity identity (particles.F90:515-665): the
   change of the staggered-shape charge per mode against div J of the step,
-  at round-off for m = 0.
+  at round-off for m = 0;
+* the worked single-particle example of the documentation, section 6.3,
+  Tables 1-3: the m = 0 J_theta, J_x and J_r of one macro-electron push.
 """
 import math
 
@@ -166,3 +168,51 @@ def test_number_density_of_loaded_plasma():
     for row in range(deck.ny - 1):
         assert abs(n0[row].mean() / n_deck - 1.0) < 0.04, row
     assert abs(nd[1][NG:NG + deck.ny, NG:NG + deck.nx].mean()) < 0.02 * n_deck
+
+
+# The documentation's Tables 1-3 (section 6.3): m = 0 current densities of
+# one push of a macro-electron of weight 1 (Q = -1.602e-19 C), dx = dr = 50 nm,
+# x0 = r0 = 5 um, dt = 0.1 fs, v_theta = 0.1 c.  Rows are r, columns x.
+DOC_JT = np.array([[-15.0, -80.5, -25.5], [-62.2, -283, -77.1], [-9.79, -38.2, -8.44]]) * 1e5
+DOC_JX = np.array([[0.0, 5.05, 6.26, 0.0], [0.0, 17.6, 21.9, 0.0], [0.0, 2.35, 2.92, 0.0]]) * 1e7
+DOC_JR = np.array([[0.0, 0.0, 0.0], [-2.91, -13.5, -3.72], [-1.88, -8.67, -2.39], [0.0, 0.0, 0.0]]) * 1e7
+
+
+def test_documented_single_push_tables():
+    """The push's start and end positions come from the documentation's
+    Figure 8, an image; they are fitted here (a least-squares fit of the
+    three tables) and fixed: start (x, r) = (5.1163, 5.0866) um, displacement
+    (-28.28, +16.56) nm.  That displacement over 0.1 fs is faster than light
+    with v_theta = 0.1 c (the example's weights are hand-picked), so the push
+    spans 0.2 fs and the x and r currents, proportional to 1/dt for given
+    positions, are doubled; J_theta = Q v_theta <W>/V does not depend on dt.
+    Zero entries are exact; the others agree within 5 %, the precision of
+    the figure's printed weights.  A wrong area or volume factor, stagger or
+    weight convention misses by far more.  Grid: cell edges on multiples of
+    50 nm, so J_theta(cx, cy) sits at (x_min + cx dx, cy dr)."""
+    dx = 50e-9
+    e = Species("electron", -Q0, M0, 1, 1.0, bc=(abi.BC_PERIODIC, abi.BC_PERIODIC, abi.BC_OTHER, abi.BC_REFLECT))
+    e.capacity = 16
+    deck = Deck("doc_push", 20, 110, 2, 4.5e-6, 5.5e-6, 5.5e-6,
+                (abi.BC_PERIODIC, abi.BC_PERIODIC, abi.BC_OTHER, abi.BC_CONDUCT), [e])
+    deck.dt = dtp = 2.0e-16
+    xs, rs, ddx, ddr = 5.1e-6 + 0.32593 * dx, 5.1e-6 - 0.26859 * dx, -0.56558 * dx, 0.33120 * dx
+    vx, vr, vt = ddx / dtp, ddr / dtp, 0.1 * CL
+    g = 1.0 / math.sqrt(1.0 - (vx * vx + vr * vr + vt * vt) / CL ** 2)
+    from cylindrical_epoch_gb300.run import Particles
+    p = Particles(1)
+    # the deposit runs from the t + dt/2 position to the t + 3 dt/2 one
+    p.x[0], p.y[0], p.z[0] = xs - vx * dtp / 2, rs - vr * dtp / 2, -vt * dtp / 2
+    p.px[0], p.py[0], p.pz[0] = g * M0 * vx, g * M0 * vr, g * M0 * vt
+    p.w[0] = 1.0
+    orc = oracle.Oracle(deck, particles=[p])
+    orc.stage("push")
+    jx, jr, jt = orc.field("jxm")[0].real, orc.field("jrm")[0].real, orc.field("jtm")[0].real
+    at = lambda a, cy, cx: a[cy + NG - 1, cx + NG - 1]
+    got_t = np.array([[at(jt, cy, cx) for cx in (11, 12, 13)] for cy in (101, 102, 103)])
+    got_x = 2.0 * np.array([[at(jx, cy, cx) for cx in (11, 12, 13, 14)] for cy in (101, 102, 103)])
+    got_r = 2.0 * np.array([[at(jr, cy, cx) for cx in (11, 12, 13)] for cy in (101, 102, 103, 104)])
+    for got, doc in ((got_t, DOC_JT), (got_x, DOC_JX), (got_r, DOC_JR)):
+        zero = doc == 0.0
+        assert np.all(np.abs(got[zero]) < 1e-9 * np.abs(doc).max())
+        assert np.all(np.abs(got[~zero] - doc[~zero]) <= 0.05 * np.abs(doc[~zero])), (got, doc)
