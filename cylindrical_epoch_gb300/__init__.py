@@ -8,7 +8,7 @@ host-side mirror of the reference driver: deck descriptions, the loader and
 the run handle.
 """
 from . import abi, deck
-from .deck import Deck, Laser, Species, thermal_plasma, wakefield, large_wakefield, moving_window_deck
+from .deck import Deck, Laser, Species, thermal_plasma, wakefield, large_wakefield, moving_window_deck, field_ionisation_deck
 from .lib import load
 from .run import Batch, Particles, Run, SdfFile, host_load, sdf_write_arrays
 

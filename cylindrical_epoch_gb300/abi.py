@@ -128,6 +128,19 @@ class DeckFns(C.Structure):
     ]
 
 
+IONISE_MULTIPHOTON = 1
+IONISE_BSI = 2
+ION_NCONST = 15
+
+
+class IonisationSpecies(C.Structure):
+    """cyl_ionisation_species: one species' field-ionisation data."""
+    _fields_ = [
+        ("ionise", C.c_int32), ("ionise_to", C.c_int32), ("release", C.c_int32),
+        ("l", C.c_int32), ("n", C.c_int32), ("energy", C.c_double),
+    ]
+
+
 class RngState(C.Structure):
     _fields_ = [
         ("x", C.c_int32), ("y", C.c_int32), ("z", C.c_int32), ("w", C.c_int32),

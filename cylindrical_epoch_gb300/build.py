@@ -33,6 +33,7 @@ SOURCES = [
     ("particles.cu", ["--fmad=false"], "particles"),
     ("charge.cu", ["--fmad=false"], "charge"),
     ("loader.cu", ["--fmad=false"], "loader"),
+    ("ionise.cu", ["--fmad=false"], "ionise"),
 ] + [
     ("push_mixed.cu", ["--fmad=true", f"-DCYL_TILE_X={tx}", f"-DCYL_TILE_Y={ty}", f"-DCYL_TILE_NS=t{tx}x{ty}",
                        f"-DCYL_TILE_FNS=push_mixed_fns_{tx}x{ty}"], f"push_mixed_{tx}x{ty}")

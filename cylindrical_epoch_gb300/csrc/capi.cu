@@ -17,6 +17,7 @@
 #include <memory>
 #include <mutex>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 #include "cyl_common.cuh"
@@ -117,6 +118,11 @@ struct Handle {
   // callback's error while a step is prepared and read by its caller
   cyl_deck_fns fns{};
   bool cb_failed = false;
+  // field ionisation (cyl_set_ionisation): constants, device snapshot of the
+  // species' counts at the routine's start, capacities
+  IonParams ion{};
+  bool ion_on = false;
+  int64_t* d_ion = nullptr;  // [0, MAX_SPECIES) snapshot, [MAX_SPECIES, 2 MAX_SPECIES) capacities
   KissRng rng;
   // staging
   StepRec* h_rec = nullptr;
@@ -388,6 +394,7 @@ static void inject_counter_step(Handle* h, StepRec& r, int cells, int64_t& inj_u
 static void step_head_fields(Handle* h, StepRec& r) {
   std::memset(&r, 0, sizeof(r));
   r.time_half = h->time;
+  r.step = h->step;
   r.nshift_total = (int32_t)h->n_shifts;
   fill_grid(r, h->g, false);
   for (int i = 0; i < 4; ++i) {
@@ -536,8 +543,24 @@ template <typename T>
 static void enqueue_current_finish(Handle* h, cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec) {
   const RunConst& rc = h->rc;
   FView wk{h->F[15], rc.nxg, rc.nyg};
-  launch_current_finish(s, F, rec, rc, h->gd.smooth_currents, h->gd.smooth_its, h->gd.smooth_comp_its,
-                        h->gd.smooth_stride > 0 ? h->gd.smooth_stride : 1, wk);
+  const int stride = h->gd.smooth_stride > 0 ? h->gd.smooth_stride : 1;
+  if constexpr (std::is_same<T, cplx>::value) {
+    if (h->ion_on) {
+      // push_particles ends with current_bcs_r_min_final; ionise_particles
+      // runs before current_finish (epoch2d.F90:218-252)
+      launch_current_finish(s, F, rec, rc, h->gd.smooth_currents, h->gd.smooth_its, h->gd.smooth_comp_its, stride,
+                            wk, 1);
+      launch_ionise(s, F, h->sp, h->nsp, h->d_cnt, h->ion, rec, rc, h->d_ion, h->d_ion + MAX_SPECIES, h->d_err,
+                    h->nblocks);
+      launch_current_finish(s, F, rec, rc, h->gd.smooth_currents, h->gd.smooth_its, h->gd.smooth_comp_its, stride,
+                            wk, 2);
+      int nion = 0;
+      for (int i = 0; i < h->nsp; ++i) nion += h->ion.s[i].ionise;
+      count_launch(h, 4 + nion);
+      return;
+    }
+  }
+  launch_current_finish(s, F, rec, rc, h->gd.smooth_currents, h->gd.smooth_its, h->gd.smooth_comp_its, stride, wk);
   count_launch(h, 2);
 }
 
@@ -1213,6 +1236,7 @@ int cyl_destroy(cyl_handle hh) {
   cudaFree(h->rowtab);
   cudaFree(h->gtab_f);
   cudaFree(h->fb_buf);
+  cudaFree(h->d_ion);
   cudaFree(h->d_dbg);
   cudaFree(h->d_tile_start);
   cudaFree(h->d_tile_order);
@@ -1855,6 +1879,69 @@ int cyl_push_only(cyl_handle hh) {
   CK(cudaEventSynchronize(h->ev_push[0][1]));
   collect_push_timing(h, 1);
   return sync_and_check(h);
+}
+
+int cyl_ionisation_constants(const cyl_ionisation_species* io, const cyl_species_desc* sp, int32_t n,
+                             int32_t model, double laser_omega, double* out) {
+  if (!io || !sp || !out || n < 1 || n > MAX_SPECIES) return CYL_ERR_BAD_ARG;
+  for (int i = 0; i < n; ++i)
+    if (io[i].ionise && (io[i].ionise_to < 0 || io[i].ionise_to >= n || io[i].release < -1 || io[i].release >= n))
+      return CYL_ERR_BAD_ARG;
+  IonSpecies c[MAX_SPECIES];
+  ionisation_constants(io, sp, n, model, laser_omega, c);
+  for (int i = 0; i < n; ++i) {
+    const double v[CYL_ION_NCONST] = {c[i].released_mass_fraction, c[i].n_exp, c[i].adk_scaling,
+                                      c[i].ionisation_constant, c[i].smallest_e_mag, c[i].bsi_constant,
+                                      c[i].bsi_scaling, c[i].bsi_threshold, c[i].adk_maximum, c[i].adk_bsi_cap,
+                                      c[i].keldysh, c[i].multi_constant, c[i].k_photons_energy,
+                                      c[i].k_photons_exponent, c[i].adk_multiphoton_cap};
+    for (int k = 0; k < CYL_ION_NCONST; ++k) out[i * CYL_ION_NCONST + k] = v[k];
+  }
+  return CYL_OK;
+}
+
+int cyl_set_ionisation(cyl_handle hh, const cyl_ionisation_species* io, int32_t n, int32_t model,
+                       uint64_t seed) {
+  if (!hh) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  if (n == 0) {
+    h->ion_on = false;
+  } else {
+    if (!io || n != h->nsp) return CYL_ERR_BAD_ARG;
+    if (h->prec == CYL_PREC_MIXED) return CYL_ERR_UNSUPPORTED;
+    for (int i = 0; i < n; ++i)
+      if (io[i].ionise && (io[i].ionise_to < 0 || io[i].ionise_to >= n || io[i].release < -1 ||
+                           io[i].release >= n || io[i].energy <= 0.0))
+        return CYL_ERR_BAD_ARG;
+    double omega = 0.0;
+    if (model & CYL_IONISE_MULTIPHOTON) {
+      // one laser frequency on the x boundaries (ionise.F90:56-123)
+      if (h->lasers.empty()) return CYL_ERR_UNSUPPORTED;
+      omega = h->lasers[0].d.omega;
+      for (const auto& L : h->lasers)
+        if (std::fabs(L.d.omega - omega) > 2.2250738585072014e-308) return CYL_ERR_UNSUPPORTED;
+    }
+    IonParams P{};
+    ionisation_constants(io, h->sd, n, model, omega, P.s);
+    P.model = model;
+    P.nsp = n;
+    P.seed = seed;
+    if (!h->d_ion) {
+      if (cudaMalloc(&h->d_ion, sizeof(int64_t) * 2 * MAX_SPECIES) != cudaSuccess) return CYL_ERR_OUT_OF_MEMORY;
+      int64_t caps[2 * MAX_SPECIES] = {};
+      for (int i = 0; i < h->nsp; ++i) caps[MAX_SPECIES + i] = h->sp[i].cap;
+      CK(cudaMemcpy(h->d_ion, caps, sizeof(caps), cudaMemcpyHostToDevice));
+    }
+    h->ion = P;
+    h->ion_on = true;
+  }
+  // the step's kernels change: a captured step graph is rebuilt
+  if (h->gexec) {
+    cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+  }
+  h->topo_epoch++;
+  return CYL_OK;
 }
 
 int cyl_set_deck_fns(cyl_handle hh, const cyl_deck_fns* fns) {

@@ -18,6 +18,7 @@
 //   injection count   (row, shift, species, TAG_INJ_COUNT)
 //   injection place   (j, shift, species, TAG_INJ_POS)
 //   injection momentum(j, shift, species, TAG_INJ_MOM)
+//   ionisation trial  (id, id >> 32, step, TAG_IONISE + 16 species)
 // p is the particle's index in the species' load, j its index in the
 // injected column of one species at one window shift, shift the global
 // index of that shift (0 for the first shift of the run).
@@ -34,6 +35,8 @@
 namespace cyl {
 
 constexpr uint32_t TAG_LOAD_POS = 1, TAG_LOAD_MOM = 2, TAG_INJ_COUNT = 3, TAG_INJ_POS = 4, TAG_INJ_MOM = 5;
+// field ionisation trial: (id, id >> 32, step, TAG_IONISE + 16 charge-state species)
+constexpr uint32_t TAG_IONISE = 6;
 
 struct U4 {
   uint32_t v[4];

@@ -143,6 +143,7 @@ struct StepRec {
   int64_t src_off;           // offset of this step's laser source vectors
   int32_t nshift_total;      // window shifts before this step (mixed-form cell origin)
   int32_t nshift_total_after;
+  int64_t step;              // steps completed before this one (the reference's step during the push)
   // window injection drawn on the device from the counter stream (counter_rng.cuh):
   // per shift c of this step and species s, the column's left edge, the
   // global shift index, the clamped column density, and where its particles

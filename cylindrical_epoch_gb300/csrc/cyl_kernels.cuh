@@ -76,7 +76,7 @@ void launch_b_final_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* re
                         const cplx* cols, int do_axis, double dt, const RunConst& rc);
 template <typename T>
 void launch_current_finish(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc,
-                           int smooth, int its, int comp_its, int stride, FView wk);
+                           int smooth, int its, int comp_its, int stride, FView wk, int parts = 3);
 template <typename T>
 void launch_shift_fields(cudaStream_t s, const FieldSetT<T>& F, const cplx* cols, const StepRec* rec,
                          int which, const RunConst& rc);
@@ -91,6 +91,26 @@ void launch_push_fp64(cudaStream_t s, const FieldSet& F, const GeomTables& g, co
                       SpeciesCounters* cnt, const StepRec* rec, const RunConst& rc, int apply_bcs,
                       int* err, int nblocks);
 void launch_eval_atan2(cudaStream_t s, const double* y, const double* x, double* out, int64_t n);
+
+// ionise.cu: field ionisation of the FP64 form.  Per species the deck's data
+// and the constants of initialise_ionisation (ionise.F90:51-286): n_exp is
+// 2 n* - 1.5, k_photons_exponent 4 K - 2, fields in atomic units.
+struct IonSpecies {
+  int32_t ionise, ionise_to, release, l;
+  double energy, released_mass_fraction, n_exp, adk_scaling, ionisation_constant, smallest_e_mag;
+  double bsi_constant, bsi_scaling, bsi_threshold, adk_maximum, adk_bsi_cap;
+  double keldysh, multi_constant, k_photons_energy, k_photons_exponent, adk_multiphoton_cap;
+};
+struct IonParams {
+  IonSpecies s[MAX_SPECIES];
+  int32_t model, nsp;
+  uint64_t seed;
+};
+void ionisation_constants(const cyl_ionisation_species* io, const cyl_species_desc* sd, int n, int model,
+                          double omega, IonSpecies* out);
+void launch_ionise(cudaStream_t s, const FieldSet& F, const SpeciesPtrs* sp, int nsp, SpeciesCounters* cnt,
+                   const IonParams& P, const StepRec* rec, const RunConst& rc, int64_t* snap, const int64_t* caps,
+                   int* err, int nblocks);
 
 // charge.cu (continuity-residual and number-density diagnostics)
 void launch_number_density(cudaStream_t s, const SpeciesPtrs& sp, const SpeciesCounters* cnt, const RunConst& rc,

@@ -843,9 +843,13 @@ void launch_b_final_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* re
   launch_ghost_bcs<T>(s, F.bx, F.br, F.bt, 3, true, bc_ptr(rec), rc);
 }
 template <typename T>
+// parts: bit 0 the r_min fold (current_bcs_r_min_final, the end of
+// push_particles), bit 1 the rest (current_finish): field ionisation runs
+// between the two (epoch2d.F90:218-252).
 void launch_current_finish(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc,
-                           int smooth, int its, int comp_its, int stride, FView wk) {
-  k_j_rmin<<<jrmin_blocks(rc), 128, 0, s>>>(F.jx, F.jr, F.jt, rc);
+                           int smooth, int its, int comp_its, int stride, FView wk, int parts) {
+  if (parts & 1) k_j_rmin<<<jrmin_blocks(rc), 128, 0, s>>>(F.jx, F.jr, F.jt, rc);
+  if (!(parts & 2)) return;
   // the folding and halo pass has work only with a reflecting or periodic
   // particle boundary or a periodic x field boundary (before or after the
   // window starts); all of these are fixed for the run
@@ -890,7 +894,7 @@ void launch_shift_fields(cudaStream_t s, const FieldSetT<T>& F, const cplx* cols
   template void launch_b_final_bcs<T>(cudaStream_t, const FieldSetT<T>&, const StepRec*, const double*,    \
                                       const cplx*, int, double, const RunConst&);                          \
   template void launch_current_finish<T>(cudaStream_t, const FieldSetT<T>&, const StepRec*, const RunConst&, \
-                                         int, int, int, int, FView);                                       \
+                                         int, int, int, int, FView, int);                                  \
   template void launch_shift_fields<T>(cudaStream_t, const FieldSetT<T>&, const cplx*, const StepRec*, int,  \
                                        const RunConst&);
 INST(cplx)

@@ -131,6 +131,13 @@ class Deck:
     phase_fn: frozenset = frozenset()
     inject: Optional[object] = None
     load_grids: Optional[object] = None
+    # field ionisation (use_field_ionisation): per species a dict with
+    # ionise, ionise_to, release (species indices, -1 none), l, n and energy
+    # (J); the rate model (abi.IONISE_* bits; both = the reference's default)
+    # and the counter-stream key of the ionisation trials
+    ionisation: Optional[list] = None
+    ionisation_model: int = abi.IONISE_MULTIPHOTON | abi.IONISE_BSI
+    ionisation_seed: int = 1
 
     @property
     def dx(self):
@@ -187,6 +194,17 @@ class Deck:
             d.profile = prof.ctypes.data_as(C.POINTER(C.c_double))
             d.phase = ph.ctypes.data_as(C.POINTER(C.c_double))
         return arr, keep
+
+    def ionisation_descs(self):
+        arr = (abi.IonisationSpecies * max(1, len(self.species)))()
+        for i, d in enumerate(self.ionisation or []):
+            a = arr[i]
+            a.ionise = 1 if d.get("ionise") else 0
+            a.ionise_to = int(d.get("ionise_to", -1))
+            a.release = int(d.get("release", -1))
+            a.l, a.n = int(d.get("l", 0)), int(d.get("n", 1))
+            a.energy = float(d.get("energy", 0.0))
+        return arr
 
     def has_deck_fns(self):
         return any(f is not None for f in (self.laser_time, self.laser_omega, self.laser_profile,
@@ -425,4 +443,58 @@ def moving_window_deck(precision=abi.PREC_FP64):
 
     deck.load_grids = load_grids
     deck.inject = inject
+    return deck
+
+
+def field_ionisation_deck(precision=abi.PREC_FP64, model=None):
+    """The reference's field-ionisation example deck
+    (example_decks/field_ionisation.deck): 125 x 200 cells over 4 x 6.4 um,
+    modes m = 0..2; a 0.8 um laser at 3e15 W/cm^2 from x_min, constant in
+    time and radius; a neutral carbon slab (atomic_no 6, mass 12 x 1836.2 m_e,
+    temperature 0) of 2.91e20 m^-3 for r < 125 nm and 3.05 < x < 3.3 um,
+    npart = 1000 (250 nm / x_max) nx (125 nm / y_max) ny, ionisable up to C3+
+    (ionise_limit 3) with one electron species per level
+    (unique_electron_species).  The ionisation data of carbon are the
+    reference's tables (TABLES/ionisation_energies.table, ion_l.table,
+    ion_n.table, row 6): 11.2602880, 24.383154, 47.88778 eV; l = 1, 1, 0;
+    n = 2, 2, 2.  Species: 0 Carbon, 1-3 Carbon1..3, 4-6 the electrons of
+    each level."""
+    nx, ny = 125, 200
+    x_max, y_max = 4.0e-6, 6.4e-6
+    deck = Deck("field_ionisation", nx, ny, 3, 0.0, x_max, y_max,
+                (abi.BC_SIMPLE_LASER, abi.BC_OPEN, abi.BC_OTHER, abi.BC_OPEN), [], precision=precision)
+    lam = 0.8e-6
+    omega = 2.0 * PI * CL / lam
+    amp = math.sqrt(3.0e15 / (CL * EPS0 / 2.0)) * 100.0  # intensity_w_cm2 (deck_laser_block.f90:136-139)
+    deck.lasers = [Laser(abi.BD_X_MIN, amp, omega, np.ones(ny + 1), np.zeros(ny + 1))]
+    bc = (abi.BC_SIMPLE_LASER, abi.BC_OPEN, abi.BC_OTHER, abi.BC_OPEN)
+    mass_c = 12.0 * 1836.2 * M0
+    npart = 1000 * (250.0e-9 / x_max) * nx * (125.0e-9 / y_max) * ny
+    ng = abi.NG
+    ix = np.arange(1 - ng, nx + ng + 1)
+    iy = np.arange(1 - ng, ny + ng + 1)
+    dx, dy = x_max / nx, y_max / ny
+    xg = (dx / 2.0) + (ix - 1.0) * dx
+    yg = (dy / 2.0) + (iy - 1.0) * dy
+    dens = np.where(yg[:, None] < 125e-9, 2.91e20, 0.0) * np.ones((1, ix.size))
+    dens = np.where((xg[None, :] > 3.05e-6) & (xg[None, :] < 3.3e-6), dens, 0.0)
+    valid = int(np.count_nonzero(dens[ng:ng + ny, ng:ng + nx] >= C_EPS))
+    ppc = float(int(npart)) / valid  # npart spread over the valid cells (helper.F90:522-523)
+    species = [Species("Carbon", 0.0, mass_c, ppc, 2.91e20, bc=bc)]
+    for k in (1, 2, 3):
+        species.append(Species(f"Carbon{k}", k * Q0, mass_c - k * M0, ppc, 0.0, bc=bc))
+    for k in (1, 2, 3):
+        species.append(Species(f"Carbon{k}_electron", -Q0, M0, ppc, 0.0, bc=bc))
+    n_load = int(npart) + 1024
+    for s in species:
+        s.capacity = n_load
+    deck.species = species
+    zero = np.zeros((ny + 2 * ng, nx + 2 * ng))
+    deck.load_grids = lambda isp: (dens if isp == 0 else zero, None, None)
+    ev = [11.2602880, 24.383154, 47.88778]
+    ls = [1, 1, 0]
+    deck.ionisation = [dict(ionise=1, ionise_to=1 + k, release=4 + k, l=ls[k], n=2, energy=ev[k] * Q0)
+                       for k in range(3)] + [dict(ionise=0)] * 4
+    if model is not None:
+        deck.ionisation_model = model
     return deck

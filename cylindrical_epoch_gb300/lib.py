@@ -67,6 +67,8 @@ SIGNATURES = {
     "cyl_get_stream": (C.c_int, [H, P(C.c_void_p)]),
     "cyl_eval_atan2": (C.c_int, [I64, PD, PD, PD]),
     "cyl_set_deck_fns": (C.c_int, [H, P(abi.DeckFns)]),
+    "cyl_set_ionisation": (C.c_int, [H, P(abi.IonisationSpecies), I32, I32, C.c_uint64]),
+    "cyl_ionisation_constants": (C.c_int, [P(abi.IonisationSpecies), P(abi.SpeciesDesc), I32, I32, D, PD]),
     "cyl_host_load_species_grid": (C.c_int, [P(abi.GridDesc), P(abi.SpeciesDesc), P(abi.RngState), I64,
                                              PD, PD, PD, PD, PD, PD, PD, PD, PD, PD, PI64, PI64]),
     "cyl_estimate_device_bytes": (C.c_int, [P(abi.GridDesc), P(abi.SpeciesDesc), I32, PI64]),

@@ -244,6 +244,10 @@ class Run:
         if deck.has_deck_fns():
             self._fns, self._fns_keep = deck.deck_fns()
             abi.check("cyl_set_deck_fns", self.lib.cyl_set_deck_fns(self.h, C.byref(self._fns)))
+        if deck.ionisation:
+            abi.check("cyl_set_ionisation",
+                      self.lib.cyl_set_ionisation(self.h, deck.ionisation_descs(), len(deck.species),
+                                                  deck.ionisation_model, deck.ionisation_seed))
         if counter:
             seed = deck.seed if counter_seed is None else int(counter_seed)
             id_base = 0

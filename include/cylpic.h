@@ -360,6 +360,53 @@ typedef struct cyl_deck_fns {
  * without its callback, or a bit beyond the run's lasers, is CYL_ERR_BAD_ARG. */
 int cyl_set_deck_fns(cyl_handle h, const cyl_deck_fns* fns);
 
+/* ---- field ionisation (physics_packages/ionise.F90) -------------------
+ * Per species: whether it ionises (species%ionise), the species it becomes
+ * (ionise_to_species) and the species that receives the released electron
+ * (release_species; -1: none), 0-based as in cyl_create; the quantum numbers
+ * l and n of the electron removed and its ionisation energy in J, which the
+ * reference reads from its tables for the deck's atomic_no
+ * (deck_species_block.F90:1194-1310; TABLES/ionisation_energies.table,
+ * ion_l.table, ion_n.table). */
+typedef struct cyl_ionisation_species {
+  int32_t ionise;
+  int32_t ionise_to;
+  int32_t release;
+  int32_t l, n;
+  double energy;
+} cyl_ionisation_species;
+#define CYL_IONISE_MULTIPHOTON 1  /* use_multiphoton (on by default in the reference) */
+#define CYL_IONISE_BSI 2          /* use_bsi (on by default in the reference) */
+/* Switch on field ionisation (use_field_ionisation): from the next step on,
+ * ionise_particles runs after the push and current_bcs_r_min_final and
+ * before current_finish (epoch2d.F90:251), with the constants of
+ * initialise_ionisation (ionise.F90:51-286) computed here.  model: the
+ * CYL_IONISE_* bits; both is the reference's default
+ * (multiphoton_tunnelling_bsi, ionise.F90:355-657), none its plain
+ * tunnelling (ionise.F90:1236-1500).  Multiphoton needs every laser at one
+ * omega (ionise.F90:56-123).  The random number of each ionisation trial is
+ * the counter stream's word for (particle id, step, charge state) under key
+ * seed, where the reference draws from its serial KISS stream: same
+ * distribution, a different sequence.  A released electron takes the id
+ * 2^62 + 16 (parent id) + (index of the parent's species before the event).
+ * FP64 form only: the mixed form returns CYL_ERR_UNSUPPORTED.  Errors:
+ * CYL_ERR_BAD_ARG for species indices out of range or an ionising species
+ * without a next state; CYL_ERR_UNSUPPORTED for multiphoton without lasers
+ * or with lasers of different omega.  nspecies == 0 switches it off. */
+int cyl_set_ionisation(cyl_handle h, const cyl_ionisation_species* species, int32_t nspecies, int32_t model,
+                       uint64_t seed);
+/* The per-species constants of initialise_ionisation that the step uses, for
+ * the tests (host only): out[i * CYL_ION_NCONST + k] for species i, in the
+ * order released mass fraction, 2 n* - 1.5, ADK field scale, ADK constant,
+ * smallest usable E, BSI constant, BSI scale, BSI threshold, ADK maximum,
+ * ADK cap at the BSI threshold, Keldysh field, multiphoton constant, energy
+ * of the K photons, 4 K - 2, ADK cap at the multiphoton threshold (atomic
+ * units where the reference uses them).  No counterpart in the reference's
+ * interfaces. */
+#define CYL_ION_NCONST 15
+int cyl_ionisation_constants(const cyl_ionisation_species* species, const cyl_species_desc* sp,
+                             int32_t nspecies, int32_t model, double laser_omega, double* out);
+
 /* Device loading and window injection from a counter-based stream
  * (Philox4x32-10 keyed by seed, one counter per particle) instead of the
  * reference's serial KISS stream: the loader and injector of the reference

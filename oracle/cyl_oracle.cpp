@@ -237,6 +237,16 @@ struct Sim {
   std::vector<Species> sp;
   std::vector<Laser> lasers;
   cyl_deck_fns fns{};  // deck-expression callbacks (orc_set_deck_fns)
+  // field ionisation (orc_set_ionisation): per-species data and constants
+  bool ion_on = false;
+  int ion_model = 0;
+  uint64_t ion_seed = 0;
+  struct IonSp {
+    cyl_ionisation_species in;
+    double rmf, n_exp, adk_scaling, ion_const, smallest_e, bsi_const, bsi_scaling, bsi_threshold, adk_max;
+    double adk_bsi_cap, keldysh, multi_const, k_energy, k_exponent, adk_mp_cap;
+  };
+  std::vector<IonSp> ion;
   Rng rng;
   int smooth, smooth_its, smooth_comp_its, smooth_stride;
   std::vector<Field> thread_j;  // per-thread currents of the multi-threaded timing form
@@ -1708,6 +1718,277 @@ void moving_window(Sim& s) {
   }
 }
 
+// ------------------------------------------------------- field ionisation
+
+// constants.F90:172-198
+const double ION_Q0 = 1.602176565e-19, ION_M0 = 9.10938291e-31;
+const double ION_HBAR = 1.054571725336289397963133257349698e-34;
+const double ION_A0 = 5.291772101121111395947216558438464e-11;
+const double ION_HARTREE = 4.359744350823120007758594450644308e-18;
+const double ION_ATIME = 2.418884320905619591809404261549867e-17;
+const double ION_AFIELD = 5.142206538736485312185213306837419e11;
+const double ION_LARGEST_EXP = 1024.0 * 0.69314718055994530941723212145817657;
+const double ION_TINY = 2.2250738585072014e-308, ION_HUGE = 1.7976931348623157e308;
+const double ION_EXPONENT = -1.0 / 3.0;           // ionise.F90:27
+const double ION_BESSEL = 1.5957691216057308;     // SQRT(8/pi), ionise.F90:28
+
+// bessel_constant SQRT(x) EXP(x) RKBESL(x, 0.5, l + 1, 1): K_{l+1/2} by its
+// finite closed form (Abramowitz & Stegun 10.2.15).
+double ion_bessel_term(double x, int l) {
+  double sum = 0.0, term = 1.0;
+  for (int k = 0; k <= l; ++k) {
+    if (k > 0) term = term * ((double)((l + k) * (l - k + 1)) / (double)k) / (2.0 * x);
+    sum = sum + term;
+  }
+  const double kval = std::sqrt(PI / (2.0 * x)) * std::exp(-x) * sum;
+  return std::sqrt(8.0 / PI) * std::sqrt(x) * std::exp(x) * kval;
+}
+
+// factorial, numerics.f90:24-40
+double ion_factorial(double x) {
+  double f = 1.0;
+  for (int i = 2; i <= (int)x; ++i) {
+    if (f < std::sqrt(ION_HUGE)) f = f * (double)i;
+    else return ION_HUGE;
+  }
+  return f;
+}
+
+// initialise_ionisation (ionise.F90:51-286); GAMMA by the C library, integer
+// powers expanded as gfortran expands them.
+void initialise_ionisation(Sim& s, const cyl_ionisation_species* in, int n, int model, double omega) {
+  const bool mp = model & CYL_IONISE_MULTIPHOTON, bsi = model & CYL_IONISE_BSI;
+  const double omega_atomic = omega * ION_ATIME, c_atomic = C * ION_ATIME / ION_A0;
+  s.ion.assign(n, Sim::IonSp{});
+  for (int i = 0; i < n; ++i) {
+    Sim::IonSp& o = s.ion[i];
+    o.in = in[i];
+    if (!in[i].ionise) continue;
+    o.rmf = in[i].release >= 0 ? s.sp[in[i].release].d.mass / s.sp[i].d.mass : 0.0;
+    const double ip = in[i].energy / ION_HARTREE;
+    const double z = s.sp[in[i].ionise_to].d.charge / ION_Q0;
+    double neff = z / std::sqrt(2.0 * ip);
+    const double t = 2.0 * ip;
+    o.adk_scaling = 2.0 * std::sqrt((t * t) * t);
+    o.ion_const = std::sqrt(6.0 / PI) * ip * std::pow(2.0, 2.0 * neff) / (neff * std::tgamma(2.0 * neff));
+    if (bsi) {
+      o.bsi_const = ip * std::sqrt(2.0 * ip) / (2.0 * PI * z);
+      o.bsi_scaling = (ip * ip) / (4.0 * z);
+      const double u = 2.0 * neff, u2 = u * u;
+      o.bsi_threshold = ((z * z) * z) / (u2 * u2);
+      o.adk_max = std::fmax(o.adk_scaling / (3.0 * (2.0 * neff + (double)in[i].l - 1.5)), o.bsi_threshold);
+    }
+    if (mp) {
+      const double k = (double)((int64_t)std::floor(ip / omega_atomic) + 1);
+      double multi = ion_factorial(k);
+      if (multi < std::sqrt(ION_HUGE)) {
+        const int64_t nq = in[i].n, nq2 = nq * nq;
+        multi = c_atomic * (multi * multi) * (double)((nq2 * nq2) * nq) *
+                std::pow(omega_atomic, (10.0 * k - 1.0) / 3.0) * std::sqrt(k) * (2.0 * k + 1.0);
+      } else {
+        multi = 0.0;
+      }
+      if (std::fabs(multi) > ION_TINY) multi = 4.8 * std::pow(1.69 * c_atomic / (8.0 * PI * omega_atomic), k) / multi;
+      o.multi_const = multi;
+      o.k_energy = k * ION_HBAR * omega;
+      o.k_exponent = 4.0 * k - 2.0;
+    }
+    neff = 2.0 * neff - 1.5;
+    o.n_exp = neff;
+    if (bsi) {
+      const double x = o.adk_scaling / o.bsi_threshold;
+      o.adk_bsi_cap = o.ion_const * std::pow(x, neff) * std::exp(ION_EXPONENT * x) * (ion_bessel_term(x, in[i].l) - 1.0);
+    }
+    if (mp) {
+      o.keldysh = std::fmax(o.adk_scaling / (0.99472065388909858 * ION_LARGEST_EXP),
+                            omega_atomic * std::sqrt(2.0 * ip) / 0.5);
+      const double x = o.adk_scaling / o.keldysh;
+      o.adk_mp_cap = o.ion_const * std::pow(x, neff) * std::exp(ION_EXPONENT * x) * (ion_bessel_term(x, in[i].l) - 1.0);
+      if (std::fabs(o.multi_const) <= ION_TINY) o.smallest_e = ION_HUGE;
+      else o.smallest_e = std::pow(ION_TINY / std::fmin(o.multi_const, 1.0), 1.0 / o.k_exponent);
+    } else {
+      o.smallest_e = o.adk_scaling / (0.99472065388909858 * ION_LARGEST_EXP);
+    }
+  }
+}
+
+// ionise_particles (ionise.F90:325-351) and its four models
+// (multiphoton_tunnelling_bsi :355-657, multiphoton_tunnelling :661-950,
+// tunnelling_bsi :954-1232, tunnelling :1236-1500), single rank.  The trial's
+// random number is the counter stream's word (id, id >> 32, step,
+// 6 + 16 species) in place of random(); released electrons take the id
+// 2^62 + 16 parent id + species.
+void ionise_particles(Sim& s) {
+  const int nsp = (int)s.sp.size();
+  const bool mp = s.ion_model & CYL_IONISE_MULTIPHOTON, bsi = s.ion_model & CYL_IONISE_BSI;
+  const double fac = 0.25;
+  const double idx = 1.0 / s.dx, idy = 1.0 / s.dy;
+  const double dfac1 = fac * fac / (s.dt * 2.0 * PI * s.dx * s.dy);
+  std::vector<Species> ionised(nsp);
+  for (int i = 0; i < nsp; ++i) ionised[i].d = s.sp[i].d;
+  auto st3 = [&](Field& f, const double* wa, const double* wb, int ca, int cb, int m) {
+    cplx acc = mk(0, 0);
+    for (int jj = -1; jj <= 1; ++jj) {
+      cplx inner = (wb[1] * f(ca - 1, cb + jj, m) + wb[2] * f(ca, cb + jj, m)) + wb[3] * f(ca + 1, cb + jj, m);
+      if (jj == -1) acc = wa[jj + 2] * inner;
+      else acc = acc + wa[jj + 2] * inner;
+    }
+    return acc;
+  };
+  for (int i = 0; i < nsp; ++i) {
+    if (!s.ion[i].in.ionise) continue;
+    Species& spc = s.sp[i];
+    const size_t n0 = spc.n();
+    std::vector<char> gone(n0, 0);
+    for (size_t p = 0; p < n0; ++p) {
+      const double x0 = spc.x[p], y0 = spc.y[p], z0 = spc.z[p];
+      const double part_x_local = x0 - s.x_grid_min;
+      const double part_r = std::sqrt(y0 * y0 + z0 * z0);
+      const double part_r_local = part_r - s.y_grid_min;
+      const cplx exp_min_itheta = mk(y0 / part_r, (-z0) / part_r);
+      const cplx exp_itheta = crecip(exp_min_itheta);
+      const double dfac = dfac1 / part_r;
+      double gx[5] = {0, 0, 0, 0, 0}, gy[5] = {0, 0, 0, 0, 0}, hx[5] = {0, 0, 0, 0, 0}, hy[5] = {0, 0, 0, 0, 0};
+      const double cell_x_r = part_x_local * idx, cell_y_r = part_r_local * idy;
+      int cell_x1 = ffloor(cell_x_r + 0.5);
+      double cell_frac_x = (double)cell_x1 - cell_x_r;
+      cell_x1 = cell_x1 + 1;
+      int cell_y1 = ffloor(cell_y_r + 0.5);
+      double cell_frac_y = (double)cell_y1 - cell_y_r;
+      cell_y1 = cell_y1 + 1;
+      double cf2 = cell_frac_x * cell_frac_x;
+      gx[1] = (0.25 + cf2) + cell_frac_x;
+      gx[2] = 1.5 - 2.0 * cf2;
+      gx[3] = (0.25 + cf2) - cell_frac_x;
+      cf2 = cell_frac_y * cell_frac_y;
+      gy[1] = (0.25 + cf2) + cell_frac_y;
+      gy[2] = 1.5 - 2.0 * cf2;
+      gy[3] = (0.25 + cf2) - cell_frac_y;
+      int cell_x2 = ffloor(cell_x_r);
+      cell_frac_x = ((double)cell_x2 - cell_x_r) + 0.5;
+      cell_x2 = cell_x2 + 1;
+      int cell_y2 = ffloor(cell_y_r);
+      cell_frac_y = ((double)cell_y2 - cell_y_r) + 0.5;
+      cell_y2 = cell_y2 + 1;
+      cf2 = cell_frac_x * cell_frac_x;
+      hx[1] = (0.25 + cf2) + cell_frac_x;
+      hx[2] = 1.5 - 2.0 * cf2;
+      hx[3] = (0.25 + cf2) - cell_frac_x;
+      cf2 = cell_frac_y * cell_frac_y;
+      hy[1] = (0.25 + cf2) + cell_frac_y;
+      hy[2] = 1.5 - 2.0 * cf2;
+      hy[3] = (0.25 + cf2) - cell_frac_y;
+      // e_part.inc
+      double ex_part = 0.0, er_part = 0.0, et_part = 0.0;
+      cplx emi = mk(1.0, 0.0);
+      for (int im = 0; im < s.M; ++im) {
+        ex_part = ex_part + (emi * st3(s.ex, hy, gx, cell_x1, cell_y2, im)).re;
+        er_part = er_part + (emi * st3(s.er, gy, hx, cell_x2, cell_y1, im)).re;
+        et_part = et_part + (emi * st3(s.et, hy, hx, cell_x2, cell_y2, im)).re;
+        emi = emi * exp_min_itheta;
+      }
+      const double ey_part = er_part * exp_min_itheta.re + et_part * exp_min_itheta.im;
+      const double ez_part = (-er_part) * exp_min_itheta.im + et_part * exp_min_itheta.re;
+      const double e_mag = fac * std::sqrt((ex_part * ex_part + ey_part * ey_part) + ez_part * ez_part) / ION_AFIELD;
+      const int64_t pid = spc.id[p];
+      double ppx = spc.px[p], ppy = spc.py[p], ppz = spc.pz[p];
+      const double weight = spc.w[p];
+      int cs = i;
+      double time_left = s.dt / ION_ATIME, j_ion = 0.0;
+      while (time_left > 0.0 && s.ion[cs].in.ionise) {
+        const Sim::IonSp& q = s.ion[cs];
+        bool multi = false;
+        double rate;
+        auto adk = [&]() {
+          const double x = q.adk_scaling / e_mag;
+          return q.ion_const * std::pow(x, q.n_exp) * std::exp(ION_EXPONENT * x) * (ion_bessel_term(x, q.in.l) - 1.0);
+        };
+        auto bsi_rate = [&]() { return q.bsi_const * (1.0 - q.bsi_scaling / e_mag) + q.adk_bsi_cap; };
+        if (mp && bsi) {
+          if (e_mag > q.adk_max) rate = bsi_rate();
+          else if (e_mag > q.keldysh) {
+            rate = adk();
+            if (e_mag > q.bsi_threshold) rate = std::fmin(bsi_rate(), rate);
+          } else if (e_mag > q.smallest_e) {
+            rate = std::fmin(q.adk_mp_cap, q.multi_const * std::pow(e_mag, q.k_exponent));
+            multi = true;
+          } else break;
+        } else if (mp) {
+          if (e_mag > q.keldysh) rate = adk();
+          else if (e_mag > q.smallest_e) {
+            rate = std::fmin(q.adk_mp_cap, q.multi_const * std::pow(e_mag, q.k_exponent));
+            multi = true;
+          } else break;
+        } else if (bsi) {
+          if (e_mag > q.adk_max) rate = bsi_rate();
+          else if (e_mag > q.smallest_e) {
+            rate = adk();
+            if (e_mag > q.bsi_threshold) rate = std::fmin(bsi_rate(), rate);
+          } else break;
+        } else {
+          if (e_mag > q.smallest_e) rate = adk();
+          else break;
+        }
+        const Ctr4 r = philox10(Ctr4{{(uint32_t)pid, (uint32_t)((uint64_t)pid >> 32), (uint32_t)s.step,
+                                      6u | ((uint32_t)cs << 4)}}, s.ion_seed);
+        const double sample = ctr_u01(r.w[0]);
+        if (sample < 1.0 - std::exp(-1.0 * rate * time_left)) {
+          if (q.in.release >= 0) {
+            double ex_ = ppx * q.rmf, ey_ = ppy * q.rmf, ez_ = ppz * q.rmf;
+            ppx = ppx - ex_;
+            ppy = ppy - ey_;
+            ppz = ppz - ez_;
+            if (multi) {
+              const double kick = std::sqrt(2.0 * ION_M0 * (q.k_energy - q.in.energy));
+              const double den = e_mag * ION_AFIELD;
+              ex_ = ex_ + kick * fac * ex_part / den;
+              ey_ = ey_ + kick * fac * ey_part / den;
+              ez_ = ez_ + kick * fac * ez_part / den;
+            }
+            s.sp[q.in.release].push_back(x0, y0, z0, ex_, ey_, ez_, weight,
+                                         (int64_t)(((uint64_t)1 << 62) | ((uint64_t)pid << 4) | (uint64_t)cs));
+          }
+          time_left = time_left + std::log(1.0 - sample) / rate;
+          j_ion = j_ion + (multi ? q.k_energy : q.in.energy);
+          cs = q.in.ionise_to;
+        } else {
+          time_left = 0.0;
+        }
+      }
+      if (cs == i) continue;
+      gone[p] = 1;
+      ionised[cs].push_back(x0, y0, z0, ppx, ppy, ppz, weight, pid);
+      const double den = ION_AFIELD * e_mag;
+      const double jf = dfac * j_ion * weight;
+      const double jx_ion = jf * ex_part / (den * den), jy_ion = jf * ey_part / (den * den),
+                   jz_ion = jf * ez_part / (den * den);
+      if (std::fabs(jx_ion) > ION_TINY || std::fabs(jy_ion) > ION_TINY || std::fabs(jz_ion) > ION_TINY) {
+        const double jr_ion = jy_ion * exp_itheta.re + jz_ion * exp_itheta.im;
+        const double jt_ion = (-jy_ion) * exp_itheta.im + jz_ion * exp_itheta.re;
+        cplx eim = mk(1.0, 0.0);
+        for (int im = 0; im < s.M; ++im) {
+          for (int iy = -1; iy <= 1; ++iy)
+            for (int ix = -1; ix <= 1; ++ix) {
+              s.jx(cell_x1 + ix, cell_y2 + iy, im) =
+                  s.jx(cell_x1 + ix, cell_y2 + iy, im) + ((gx[ix + 2] * hy[iy + 2]) * jx_ion) * eim;
+              s.jr(cell_x2 + ix, cell_y1 + iy, im) =
+                  s.jr(cell_x2 + ix, cell_y1 + iy, im) + ((hx[ix + 2] * gy[iy + 2]) * jr_ion) * eim;
+              s.jt(cell_x2 + ix, cell_y2 + iy, im) =
+                  s.jt(cell_x2 + ix, cell_y2 + iy, im) + ((hx[ix + 2] * hy[iy + 2]) * jt_ion) * eim;
+            }
+          eim = eim * exp_itheta;
+          if (im == 0) eim = eim * 2.0;
+        }
+      }
+    }
+    spc.erase_mask(gone);
+  }
+  for (int i = 0; i < nsp; ++i)
+    for (size_t k = 0; k < ionised[i].n(); ++k)
+      s.sp[i].push_back(ionised[i].x[k], ionised[i].y[k], ionised[i].z[k], ionised[i].px[k], ionised[i].py[k],
+                        ionised[i].pz[k], ionised[i].w[k], ionised[i].id[k]);
+}
+
 // ---------------------------------------------------------------- driver
 
 void update_eb_fields_half(Sim& s) {
@@ -1730,6 +2011,7 @@ void step_to_output(Sim& s) {
   push_particles_core(s);
   current_bcs_r_min_final(s);
   particle_bcs(s);
+  if (s.ion_on) ionise_particles(s);  // epoch2d.F90:251
   current_finish(s);
   s.step++;
   s.time = s.time + s.dt / 2.0;
@@ -2119,6 +2401,36 @@ int orc_load_species_grid(orc_handle h, int32_t isp, const double* density, cons
   Sim* s = (Sim*)h;
   if (isp < 0 || isp >= (int)s->sp.size()) return CYL_ERR_BAD_ARG;
   load_species(*s, s->sp[isp], density, temperature, drift);
+  return CYL_OK;
+}
+
+int orc_set_ionisation(orc_handle h, const cyl_ionisation_species* in, int32_t n, int32_t model, uint64_t seed) {
+  Sim* s = (Sim*)h;
+  if (n == 0) {
+    s->ion_on = false;
+    return CYL_OK;
+  }
+  if (!in || n != (int)s->sp.size()) return CYL_ERR_BAD_ARG;
+  double omega = 0.0;
+  if ((model & CYL_IONISE_MULTIPHOTON) && !s->lasers.empty()) omega = s->lasers[0].d.omega;
+  initialise_ionisation(*s, in, n, model, omega);
+  s->ion_model = model;
+  s->ion_seed = seed;
+  s->ion_on = true;
+  return CYL_OK;
+}
+
+// The constants of initialise_ionisation per species, in the order of
+// cyl_ionisation_constants.
+int orc_ionisation_constants(orc_handle h, double* out) {
+  Sim* s = (Sim*)h;
+  for (size_t i = 0; i < s->ion.size(); ++i) {
+    const Sim::IonSp& o = s->ion[i];
+    const double v[15] = {o.rmf, o.n_exp, o.adk_scaling, o.ion_const, o.smallest_e, o.bsi_const, o.bsi_scaling,
+                          o.bsi_threshold, o.adk_max, o.adk_bsi_cap, o.keldysh, o.multi_const, o.k_energy,
+                          o.k_exponent, o.adk_mp_cap};
+    for (int k = 0; k < 15; ++k) out[i * 15 + k] = v[k];
+  }
   return CYL_OK;
 }
 

@@ -80,6 +80,8 @@ def load():
         "orc_atan2": (C.c_double, [C.c_double, C.c_double]),
         "orc_atan2_many": (None, [C.c_int64, PD, PD, PD]),
         "orc_set_deck_fns": (C.c_int, [H, C.POINTER(abi.DeckFns)]),
+        "orc_set_ionisation": (C.c_int, [H, C.POINTER(abi.IonisationSpecies), C.c_int32, C.c_int32, C.c_uint64]),
+        "orc_ionisation_constants": (C.c_int, [H, PD]),
         "orc_load_species_grid": (C.c_int, [H, C.c_int32, PD, PD, PD]),
         "orc_set_atan2": (None, [C.c_int32]),
         "orc_sincos_turn": (None, [C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
@@ -155,11 +157,21 @@ class Oracle:
         if deck.has_deck_fns():
             self._fns, self._fns_keep = deck.deck_fns()
             self.lib.orc_set_deck_fns(self.h, C.byref(self._fns))
+        if deck.ionisation:
+            arr = deck.ionisation_descs()
+            if self.lib.orc_set_ionisation(self.h, arr, len(deck.species), deck.ionisation_model,
+                                           deck.ionisation_seed) != 0:
+                raise RuntimeError("orc_set_ionisation")
         if particles is not None:
             for i, p in enumerate(particles):
                 self.set_particles(i, p)
         if rng is not None:
             self.lib.orc_set_rng(self.h, C.byref(rng))
+
+    def ionisation_constants(self):
+        out = np.zeros((len(self.deck.species), self.abi.ION_NCONST))
+        self.lib.orc_ionisation_constants(self.h, out.ctypes.data_as(C.POINTER(C.c_double)))
+        return out
 
     def close(self):
         if getattr(self, "h", None):

@@ -138,11 +138,14 @@ def test_c1_thermal_full_deck(gpu_lib, threads):
     print("C1 200 steps, (gpu against the oracle, oracle order spread):", err)
     assert all(v[0] < 1e-9 for k, v in err.items() if k.endswith("[m=0]"))
     a, b = match_by_id(gpu.particles(0), orc.particles(0))
-    _, c = match_by_id(alt.particles(0), orc.particles(0))
+    c, _ = match_by_id(alt.particles(0), orc.particles(0))
     for k in ("x", "y", "z", "px", "py", "pz"):
         e, sp = rel_l2(getattr(a, k), getattr(b, k)), rel_l2(getattr(c, k), getattr(b, k))
         print("C1 particles", k, "gpu", e, "oracle order spread", sp)
-        assert e < max(1e-12, 10 * sp), k
+        # Positions and momenta follow the fields, whose m=1 parts already
+        # differ by ~1e-7 between the two oracle summation orders, so the
+        # bar is ten times that spread with a 1e-11 floor.
+        assert e < max(1e-11, 10 * sp), k
     # diagnostics (calc_df.F90:1246-1291 kinetic energy, per-mode field energy)
     e1g, e1o = gpu.diagnostics(), orc.diagnostics()
     for k in ("kinetic_energy", "field_energy_e", "field_energy_b"):
