@@ -10,7 +10,8 @@ the run handle.
 from . import abi, deck
 from .deck import Deck, Laser, Species, thermal_plasma, wakefield, large_wakefield, moving_window_deck, field_ionisation_deck
 from .lib import load
-from .run import Batch, Particles, Run, SdfFile, host_load, sdf_write_arrays
+from .run import Batch, Particles, Run, SdfFile, host_load, sdf_write_arrays, set_wait_timeout
 
 __all__ = ["abi", "deck", "Deck", "Laser", "Species", "thermal_plasma", "wakefield",
-           "large_wakefield", "load", "Particles", "Run", "host_load", "Batch", "sdf_write_arrays", "SdfFile"]
+           "large_wakefield", "load", "Particles", "Run", "host_load", "Batch", "sdf_write_arrays", "SdfFile",
+           "set_wait_timeout"]

@@ -10,6 +10,7 @@
 // once into a CUDA graph and replayed.
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -692,10 +693,72 @@ static void make_geom(const HostGrid& g, std::vector<double>& out) {
   }
 }
 
+// Host waits on the device.  The library's waits for a run's work poll the
+// stream or event and give up after the process-wide limit
+// (cyl_set_wait_timeout, 600 s unless set) with CYL_ERR_TIMEOUT: the work
+// stays queued, the handle's bookkeeping is left as it was before the wait,
+// and a later call waits for the same work again.  The first 2 ms are polled
+// with yields, later polls are 50 us apart.
+static std::atomic<double> g_wait_timeout_s{600.0};
+
+template <class Query>
+static int poll_device(Query query, cudaError_t* err) {
+  const double lim = g_wait_timeout_s.load();
+  const auto t0 = std::chrono::steady_clock::now();
+  for (;;) {
+    const cudaError_t e = query();
+    if (e != cudaErrorNotReady) {
+      *err = e;
+      return e == cudaSuccess ? CYL_OK : CYL_ERR_CUDA;
+    }
+    const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (lim > 0.0 && el > lim) {
+      *err = cudaSuccess;
+      return CYL_ERR_TIMEOUT;
+    }
+    if (el < 2e-3)
+      std::this_thread::yield();
+    else
+      std::this_thread::sleep_for(std::chrono::microseconds(50));
+  }
+}
+
+static int wait_stream(Handle* h, cudaStream_t s) {
+  cudaError_t e = cudaSuccess;
+  const int rc = poll_device([s] { return cudaStreamQuery(s); }, &e);
+  if (rc == CYL_ERR_CUDA) h->last_cuda_error = e;
+  return rc;
+}
+
+static int wait_event(Handle* h, cudaEvent_t ev) {
+  cudaError_t e = cudaSuccess;
+  const int rc = poll_device([ev] { return cudaEventQuery(ev); }, &e);
+  if (rc == CYL_ERR_CUDA) h->last_cuda_error = e;
+  return rc;
+}
+
+// The end of copies to or from host memory that the caller or this frame
+// owns.  The stream's earlier work has been waited for with the limit before
+// the copies were queued, so this wait is for the copies alone; it is not
+// cut short, because the memory must stay valid until they are done.
+static int copies_done(Handle* h, cudaStream_t s) {
+  const cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    h->last_cuda_error = e;
+    return CYL_ERR_CUDA;
+  }
+  return CYL_OK;
+}
+
+#define WAIT(call)                    \
+  do {                                \
+    if (int rc_ = (call)) return rc_; \
+  } while (0)
+
 static int flush_push_timing(Handle* h);
 
 static int sync_and_check(Handle* h) {
-  CK(cudaStreamSynchronize(h->st));
+  WAIT(wait_stream(h, h->st));
   if (int r = flush_push_timing(h)) return r;
   int err = 0;
   CK(cudaMemcpy(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost));
@@ -716,7 +779,7 @@ static void collect_push_timing(Handle* h, int nsteps) {
 // Read the push events of the last chunk (they are re-recorded by the next).
 static int flush_push_timing(Handle* h) {
   if (h->timing_pending > 0) {
-    CK(cudaEventSynchronize(h->ev_push[h->timing_pending - 1][1]));
+    WAIT(wait_event(h, h->ev_push[h->timing_pending - 1][1]));
     collect_push_timing(h, h->timing_pending);
     h->timing_pending = 0;
   }
@@ -725,13 +788,16 @@ static int flush_push_timing(Handle* h) {
 
 static int run_chunk(Handle* h, int k, bool use_graph) {
   // staging buffers are reused: wait until the previous chunk's copies are done
-  if (h->copy_pending) CK(cudaEventSynchronize(h->ev_copy));
-  // the host work of this chunk overlaps the device work of the previous one
+  if (h->copy_pending) WAIT(wait_event(h, h->ev_copy));
+  // the push events of the previous chunk are read (and re-recorded by this
+  // one); both waits come before the host state moves, so a wait that runs
+  // out leaves the run as it was.  The previous chunk's field stages and
+  // sort still run on the device while this chunk is prepared and queued.
+  if (int r = flush_push_timing(h)) return r;
   int64_t inj_used = 0;
   h->cb_failed = false;
   for (int i = 0; i < k; ++i) prepare_step(h, i, inj_used);
   if (h->cb_failed) return CYL_ERR_CALLBACK;
-  if (int r = flush_push_timing(h)) return r;
   CK(cudaMemcpyAsync(h->d_rec, h->h_rec, sizeof(StepRec) * k, cudaMemcpyHostToDevice, h->st));
   CK(cudaMemcpyAsync(h->d_src, h->h_src, sizeof(double) * h->src_per_step * k, cudaMemcpyHostToDevice, h->st));
   if (inj_used > 0 && !h->inj_counter)
@@ -1214,6 +1280,12 @@ int cyl_create(const cyl_grid_desc* gd, const cyl_species_desc* spd, int32_t nsp
   return CYL_OK;
 }
 
+int cyl_set_wait_timeout(double seconds) {
+  if (std::isnan(seconds)) return CYL_ERR_BAD_ARG;
+  g_wait_timeout_s.store(seconds);
+  return CYL_OK;
+}
+
 int cyl_destroy(cyl_handle hh) {
   if (!hh) return CYL_ERR_BAD_ARG;
   Handle* h = &hh->h;
@@ -1269,6 +1341,7 @@ int cyl_upload_particles(cyl_handle hh, int32_t isp, const double* x, const doub
   SpeciesPtrs& p = h->sp[isp];
   if (n > p.cap) return CYL_ERR_CAPACITY;
   cudaStream_t s = h->st;
+  WAIT(wait_stream(h, s));
   const size_t b = (size_t)n * 8;
   if (n > 0 && h->prec == CYL_PREC_MIXED) {
     // stage the FP64 arrays in the sort scratch, convert on the device
@@ -1296,7 +1369,7 @@ int cyl_upload_particles(cyl_handle hh, int32_t isp, const double* x, const doub
   }
   std::memcpy(&c.wmax_bits, &wmax, sizeof(float));
   CK(cudaMemcpyAsync(h->d_cnt + isp, &c, sizeof(c), cudaMemcpyHostToDevice, s));
-  CK(cudaStreamSynchronize(s));
+  WAIT(copies_done(h, s));
   return CYL_OK;
 }
 
@@ -1315,13 +1388,13 @@ int cyl_load_species_device(cyl_handle hh, int32_t isp, uint64_t seed, int64_t i
   const int64_t n = (int64_t)std::floor(d.npart_per_cell * (double)nvalid);
   if (n > p.cap) return CYL_ERR_CAPACITY;
   cudaStream_t s = h->st;
-  CK(cudaStreamSynchronize(s));
+  WAIT(wait_stream(h, s));
   // every copy below is on the handle's stream, so the kernels on it see
   // them (a cudaMemcpy from pageable memory may return before its DMA lands,
   // and it is not ordered with a non-blocking stream)
   SpeciesCounters c{n, 0, 0u, 0u};
   CK(cudaMemcpyAsync(h->d_cnt + isp, &c, sizeof(c), cudaMemcpyHostToDevice, s));
-  if (n == 0) CK(cudaStreamSynchronize(s));
+  if (n == 0) WAIT(copies_done(h, s));
   if (n > 0) {
     double* d_dens = nullptr;
     int8_t* d_dmap = nullptr;
@@ -1428,7 +1501,7 @@ int cyl_set_injection_stream(cyl_handle hh, int32_t mode, uint64_t seed) {
       }
       tab[s].mass = d.mass;
     }
-    CK(cudaStreamSynchronize(h->st));
+    WAIT(wait_stream(h, h->st));
     if (cudaMalloc(&h->d_injsp, sizeof(tab)) != cudaSuccess) return CYL_ERR_OUT_OF_MEMORY;
     if (cudaMalloc(&h->d_injrow, sizeof(int32_t) * (size_t)h->inj_cap) != cudaSuccess) {
       cudaFree(h->d_injsp);
@@ -1436,7 +1509,7 @@ int cyl_set_injection_stream(cyl_handle hh, int32_t mode, uint64_t seed) {
       return CYL_ERR_OUT_OF_MEMORY;
     }
     CK(cudaMemcpyAsync(h->d_injsp, tab, sizeof(tab), cudaMemcpyHostToDevice, h->st));
-    CK(cudaStreamSynchronize(h->st));
+    WAIT(copies_done(h, h->st));
   }
   h->inj_counter = mode == CYL_RNG_COUNTER;
   h->inj_seed = seed;
@@ -1581,7 +1654,7 @@ int cyl_restart_sdf(cyl_handle hh, const char* path, const char* const* species_
   h->time = info.time;
   step_head_fields(h, h->out_rec);
   h->at_output = AT_OUTPUT_RESTART;
-  CK(cudaStreamSynchronize(h->st));
+  WAIT(wait_stream(h, h->st));
   return CYL_OK;
 }
 
@@ -1590,7 +1663,7 @@ int cyl_download_particles(cyl_handle hh, int32_t isp, double* x, double* y, dou
   if (!hh || !n_inout) return CYL_ERR_BAD_ARG;
   Handle* h = &hh->h;
   if (isp < 0 || isp >= h->nsp) return CYL_ERR_BAD_ARG;
-  CK(cudaStreamSynchronize(h->st));
+  WAIT(wait_stream(h, h->st));
   SpeciesCounters c;
   CK(cudaMemcpy(&c, h->d_cnt + isp, sizeof(c), cudaMemcpyDeviceToHost));
   const int64_t n = c.n_used;
@@ -1619,7 +1692,7 @@ int cyl_download_particles(cyl_handle hh, int32_t isp, double* x, double* y, dou
       for (int k = 0; k < 7 && n > 0; ++k) CK(cudaMemcpyAsync(dst[k], srcs[k], b, cudaMemcpyDeviceToHost, h->st));
       if (n > 0) CK(cudaMemcpyAsync(id, p.id, b, cudaMemcpyDeviceToHost, h->st));
     }
-    CK(cudaStreamSynchronize(h->st));
+    WAIT(copies_done(h, h->st));
     *n_inout = n;
     return CYL_OK;
   }
@@ -1631,7 +1704,7 @@ int cyl_download_particles(cyl_handle hh, int32_t isp, double* x, double* y, dou
     for (int k = 0; k < 8; ++k)
       CK(cudaMemcpyAsync(buf.get() + (size_t)k * n, st + (size_t)k * cap, (size_t)n * 8, cudaMemcpyDeviceToHost,
                          h->st));
-    CK(cudaStreamSynchronize(h->st));
+    WAIT(copies_done(h, h->st));
   } else {
     double* srcs[7] = {p.x, p.y, p.z, p.px, p.py, p.pz, p.w};
     for (int k = 0; k < 7; ++k)
@@ -1670,25 +1743,26 @@ static int f32_slot(const Handle* h, int which) {
 int cyl_upload_field(cyl_handle hh, int32_t which, const double* data) {
   if (!hh || !data || which < 0 || which >= CYL_NFIELDS) return CYL_ERR_BAD_ARG;
   Handle* h = &hh->h;
+  WAIT(wait_stream(h, h->st));
   const int fs = f32_slot(h, which);
   if (fs >= 0) {
     std::vector<float> tmp(h->fcount * 2);
     for (size_t i = 0; i < tmp.size(); ++i) tmp[i] = (float)data[i];
     // after the stream's earlier work on the array, before its later work
     CK(cudaMemcpyAsync(h->Ff[fs], tmp.data(), tmp.size() * sizeof(float), cudaMemcpyHostToDevice, h->st));
-    CK(cudaStreamSynchronize(h->st));
+    WAIT(copies_done(h, h->st));
     return CYL_OK;
   }
   CK(cudaMemcpyAsync(h->F[field_slot(h, which)], data, h->fcount * sizeof(cplx), cudaMemcpyHostToDevice,
                      h->st));
-  CK(cudaStreamSynchronize(h->st));
+  WAIT(copies_done(h, h->st));
   return CYL_OK;
 }
 
 int cyl_download_field(cyl_handle hh, int32_t which, double* data) {
   if (!hh || !data || which < 0 || which >= CYL_NFIELDS) return CYL_ERR_BAD_ARG;
   Handle* h = &hh->h;
-  CK(cudaStreamSynchronize(h->st));
+  WAIT(wait_stream(h, h->st));
   const int fs = f32_slot(h, which);
   if (fs >= 0) {
     std::vector<float> tmp(h->fcount * 2);
@@ -1704,7 +1778,7 @@ int cyl_initialise(cyl_handle hh) {
   if (!hh) return CYL_ERR_BAD_ARG;
   Handle* h = &hh->h;
   if (h->at_output) return CYL_ERR_BAD_ARG;
-  if (h->copy_pending) CK(cudaEventSynchronize(h->ev_copy));
+  if (h->copy_pending) WAIT(wait_event(h, h->ev_copy));
   StepRec& r = h->h_rec[0];
   std::memset(&r, 0, sizeof(r));
   fill_grid(r, h->g, false);
@@ -1787,7 +1861,7 @@ static void enqueue_finish(Handle* h, bool restart) {
 
 static int finish_output(Handle* h) {
   if (h->at_output == AT_OUTPUT_NONE) return CYL_OK;
-  if (h->copy_pending) CK(cudaEventSynchronize(h->ev_copy));
+  if (h->copy_pending) WAIT(wait_event(h, h->ev_copy));
   if (int r = flush_push_timing(h)) return r;
   const bool restart = h->at_output == AT_OUTPUT_RESTART;
   h->h_rec[0] = h->out_rec;
@@ -1834,7 +1908,7 @@ int cyl_step_to_output(cyl_handle hh, int32_t nsteps) {
   if (!hh || nsteps < 1) return CYL_ERR_BAD_ARG;
   Handle* h = &hh->h;
   if (int r = step_impl(hh, nsteps - 1, true, false)) return r;
-  if (h->copy_pending) CK(cudaEventSynchronize(h->ev_copy));
+  if (h->copy_pending) WAIT(wait_event(h, h->ev_copy));
   if (int r = flush_push_timing(h)) return r;
   StepRec& r = h->h_rec[0];
   step_head(h, r);
@@ -1858,7 +1932,7 @@ int cyl_push_only(cyl_handle hh) {
   if (!hh) return CYL_ERR_BAD_ARG;
   Handle* h = &hh->h;
   if (int r = finish_output(h)) return r;
-  if (h->copy_pending) CK(cudaEventSynchronize(h->ev_copy));
+  if (h->copy_pending) WAIT(wait_event(h, h->ev_copy));
   if (int r = flush_push_timing(h)) return r;
   StepRec& r = h->h_rec[0];
   std::memset(&r, 0, sizeof(r));
@@ -1876,7 +1950,7 @@ int cyl_push_only(cyl_handle hh) {
   if (h->prec == CYL_PREC_MIXED) push_all(h, h->st, fieldset_f(h, h->jpar), h->d_rec, 0);
   else push_all(h, h->st, F, h->d_rec, 0);
   CK(cudaEventRecord(h->ev_push[0][1], h->st));
-  CK(cudaEventSynchronize(h->ev_push[0][1]));
+  WAIT(wait_event(h, h->ev_push[0][1]));
   collect_push_timing(h, 1);
   return sync_and_check(h);
 }
@@ -2002,7 +2076,7 @@ int cyl_kernel_timing(cyl_handle hh, double* push_ms_avg, int64_t* launches) {
 int cyl_get_run_state(cyl_handle hh, cyl_run_state* out) {
   if (!hh || !out) return CYL_ERR_BAD_ARG;
   Handle* h = &hh->h;
-  CK(cudaStreamSynchronize(h->st));
+  WAIT(wait_stream(h, h->st));
   std::memset(out, 0, sizeof(*out));
   out->time = h->time;
   out->step = h->step;
@@ -2043,10 +2117,11 @@ static void fill_diag(const double* red, int err, cyl_diag* out) {
 int cyl_diagnostics(cyl_handle hh, cyl_diag* out) {
   if (!hh || !out) return CYL_ERR_BAD_ARG;
   Handle* h = &hh->h;
+  WAIT(wait_stream(h, h->st));
   enqueue_diag_reductions(h);
   double red[8];
   CK(cudaMemcpyAsync(red, h->d_red, sizeof(red), cudaMemcpyDeviceToHost, h->st));
-  CK(cudaStreamSynchronize(h->st));
+  WAIT(copies_done(h, h->st));
   int err = 0;
   CK(cudaMemcpy(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost));
   fill_diag(red, err, out);
@@ -2076,7 +2151,7 @@ int cyl_diagnostics_read(cyl_handle hh, cyl_diag* out) {
   Handle* h = &hh->h;
   if (h->diag_count == 0) return CYL_ERR_BAD_ARG;
   Handle::DiagSlot& d = h->diag_slot[h->diag_head];
-  CK(cudaEventSynchronize(d.ev));
+  WAIT(wait_event(h, d.ev));
   int err = 0;
   std::memcpy(&err, d.h + 8, sizeof(int));
   fill_diag(d.h, err, out);
@@ -2089,7 +2164,7 @@ int cyl_diagnostics_read(cyl_handle hh, cyl_diag* out) {
 int cyl_debug_record(cyl_handle hh, float* out16) {
   if (!hh || !out16) return CYL_ERR_BAD_ARG;
   Handle* h = &hh->h;
-  CK(cudaStreamSynchronize(h->st));
+  WAIT(wait_stream(h, h->st));
   CK(cudaMemcpy(out16, h->d_dbg, 16 * sizeof(float), cudaMemcpyDeviceToHost));
   return CYL_OK;
 }
@@ -2103,7 +2178,7 @@ int cyl_get_rng_state(cyl_handle hh, cyl_rng_state* out) {
 int cyl_sort_particles(cyl_handle hh) {
   if (!hh) return CYL_ERR_BAD_ARG;
   Handle* h = &hh->h;
-  if (h->copy_pending) CK(cudaEventSynchronize(h->ev_copy));
+  if (h->copy_pending) WAIT(wait_event(h, h->ev_copy));
   StepRec& r = h->h_rec[0];
   std::memset(&r, 0, sizeof(r));
   fill_grid(r, h->g, false);
@@ -2156,7 +2231,7 @@ static void set_tile_shape(Handle* h, int k) {
 
 // The step record of the current grid (no step in progress) at d_rec + CHUNK.
 static int current_rec(Handle* h) {
-  if (h->copy_pending) CK(cudaEventSynchronize(h->ev_copy));
+  if (h->copy_pending) WAIT(wait_event(h, h->ev_copy));
   StepRec& r = h->h_rec[0];
   std::memset(&r, 0, sizeof(r));
   fill_grid(r, h->g, false);
@@ -2183,7 +2258,7 @@ int cyl_tune_tiles(cyl_handle hh, int32_t mode, int32_t* shape) {
   if (int r = flush_push_timing(h)) return r;
   if (int r = current_rec(h)) return r;
   const StepRec* rec = h->d_rec + CHUNK;
-  CK(cudaStreamSynchronize(h->st));
+  WAIT(wait_stream(h, h->st));
   // Copy of the state a push changes: the mixed particle words of every
   // species (kx, fx, fy, fz, ux, uy, uz, fw: bytes [0, 32 cap) of the species
   // buffer; id: bytes [56 cap, 64 cap)) and the counters.  The trial pushes
@@ -2278,7 +2353,7 @@ int cyl_charge_density(cyl_handle hh, double* rho) {
 static int cell_indices_noalloc(Handle* h, int32_t isp, int32_t* cx, int32_t* cy, int64_t* n_inout) {
   int32_t* sc = nullptr;
   if (int r = cell_scratch(h->device, &sc)) return r;
-  CK(cudaStreamSynchronize(h->st));
+  WAIT(wait_stream(h, h->st));
   SpeciesCounters c;
   CK(cudaMemcpy(&c, h->d_cnt + isp, sizeof(c), cudaMemcpyDeviceToHost));
   const int64_t n = c.n_used;
@@ -2302,12 +2377,12 @@ static int cell_indices_noalloc(Handle* h, int32_t isp, int32_t* cx, int32_t* cy
   CK(cudaGetLastError());
   int32_t k = 0;
   CK(cudaMemcpyAsync(&k, sc + 5 * N, sizeof(int32_t), cudaMemcpyDeviceToHost, h->st));
-  CK(cudaStreamSynchronize(h->st));
+  WAIT(copies_done(h, h->st));
   if (k > *n_inout) return CYL_ERR_CAPACITY;
   if (k > 0) {
     CK(cudaMemcpyAsync(cx, sc + 3 * N, (size_t)k * sizeof(int32_t), cudaMemcpyDeviceToHost, h->st));
     CK(cudaMemcpyAsync(cy, sc + 4 * N, (size_t)k * sizeof(int32_t), cudaMemcpyDeviceToHost, h->st));
-    CK(cudaStreamSynchronize(h->st));
+    WAIT(copies_done(h, h->st));
   }
   *n_inout = k;
   return CYL_OK;
@@ -2331,7 +2406,7 @@ int cyl_cell_indices(cyl_handle hh, int32_t isp, int32_t* cx, int32_t* cy, int64
   if (!hh || !n_inout || (!cx) != (!cy)) return CYL_ERR_BAD_ARG;
   Handle* h = &hh->h;
   if (isp < 0 || isp >= h->nsp) return CYL_ERR_BAD_ARG;
-  CK(cudaStreamSynchronize(h->st));
+  WAIT(wait_stream(h, h->st));
   SpeciesCounters c;
   CK(cudaMemcpy(&c, h->d_cnt + isp, sizeof(c), cudaMemcpyDeviceToHost));
   const int64_t n = c.n_used;
@@ -2422,7 +2497,7 @@ int cyl_batch_step(cyl_batch b, const cyl_handle* hs, int32_t n, int32_t nsteps)
   for (Handle* h : runs)
     if (h->at_output != AT_OUTPUT_NONE) {
       if (int rc = finish_output(h)) return rc;
-      CK(cudaStreamSynchronize(h->st));
+      WAIT(wait_stream(h, h->st));
     }
   // every run on the batch kernel's tile shape (shape 0), sorted for it
   for (int r = 0; r < n; ++r)
@@ -2444,20 +2519,23 @@ int cyl_batch_step(cyl_batch b, const cyl_handle* hs, int32_t n, int32_t nsteps)
   int32_t done = 0;
   while (done < nsteps) {
     const int k = nsteps - done < CHUNK ? nsteps - done : CHUNK;
+    // the waits of the chunk come first, so that a wait that runs out
+    // returns before any run's host state has moved: every run's staging
+    // buffers and push events of the previous chunk, and the job table
+    for (Handle* h : runs) {
+      if (h->copy_pending) WAIT(wait_event(h, h->ev_copy));
+      if (int rc = flush_push_timing(h)) return rc;
+    }
+    if (b->jobs_pending) {
+      cudaError_t e = cudaSuccess;
+      if (int rc = poll_device([b] { return cudaEventQuery(b->ev_jobs); }, &e)) return rc;
+    }
     // each run's step records and host inputs (as run_chunk), copied on its
     // stream; runs share no host state, so the pool prepares them in parallel
     std::vector<int> prep_err(runs.size(), CYL_OK);
     b->pool->run((int)runs.size(), [&](int r) {
       Handle* h = runs[(size_t)r];
       cudaSetDevice(h->device);
-      if (h->copy_pending && cudaEventSynchronize(h->ev_copy) != cudaSuccess) {
-        prep_err[(size_t)r] = CYL_ERR_CUDA;
-        return;
-      }
-      if (int rc = flush_push_timing(h)) {
-        prep_err[(size_t)r] = rc;
-        return;
-      }
       int64_t inj_used = 0;
       h->cb_failed = false;
       for (int i = 0; i < k; ++i) prepare_step(h, i, inj_used);
@@ -2484,7 +2562,6 @@ int cyl_batch_step(cyl_batch b, const cyl_handle* hs, int32_t n, int32_t nsteps)
       if (rc != CYL_OK) return rc;
     // the job table of the chunk: per step, the fields of the J parity after
     // that step's swap
-    if (b->jobs_pending && cudaEventSynchronize(b->ev_jobs) != cudaSuccess) return CYL_ERR_CUDA;
     std::vector<int> par0(runs.size());
     for (size_t r = 0; r < runs.size(); ++r) par0[r] = runs[r]->jpar;
     for (int i = 0; i < k; ++i)
@@ -2567,7 +2644,10 @@ int cyl_batch_step(cyl_batch b, const cyl_handle* hs, int32_t n, int32_t nsteps)
       if (cudaStreamWaitEvent(h->st, b->ev_done, 0) != cudaSuccess) return CYL_ERR_CUDA;
     done += k;
   }
-  if (cudaStreamSynchronize(b->st) != cudaSuccess) return CYL_ERR_CUDA;
+  {
+    cudaError_t e = cudaSuccess;
+    if (int rc = poll_device([b] { return cudaStreamQuery(b->st); }, &e)) return rc;
+  }
   for (Handle* h : runs)
     if (int r = sync_and_check(h)) return r;
   return CYL_OK;

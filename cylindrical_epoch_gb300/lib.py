@@ -66,6 +66,7 @@ SIGNATURES = {
     "cyl_kernel_timing": (C.c_int, [H, PD, PI64]),
     "cyl_get_stream": (C.c_int, [H, P(C.c_void_p)]),
     "cyl_eval_atan2": (C.c_int, [I64, PD, PD, PD]),
+    "cyl_set_wait_timeout": (C.c_int, [C.c_double]),
     "cyl_set_deck_fns": (C.c_int, [H, P(abi.DeckFns)]),
     "cyl_set_ionisation": (C.c_int, [H, P(abi.IonisationSpecies), I32, I32, C.c_uint64]),
     "cyl_ionisation_constants": (C.c_int, [P(abi.IonisationSpecies), P(abi.SpeciesDesc), I32, I32, D, PD]),

@@ -53,6 +53,14 @@ class Particles:
         return [getattr(self, k) for k in self.__slots__]
 
 
+def set_wait_timeout(seconds):
+    """Limit of every host wait of the library on device work, in seconds
+    (cyl_set_wait_timeout; <= 0: no limit).  A call whose wait runs out
+    raises CylError with code CYL_ERR_TIMEOUT and leaves its run as it was
+    before the wait."""
+    abi.check("cyl_set_wait_timeout", load().cyl_set_wait_timeout(float(seconds)))
+
+
 def host_load(deck: Deck, rng=None):
     """Load every species as auto_load does; returns (list of Particles, rng)."""
     lib = load()

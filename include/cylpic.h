@@ -188,6 +188,16 @@ int cyl_create(const cyl_grid_desc* grid, const cyl_species_desc* species,
                const cyl_rng_state* rng, cyl_handle* out);
 int cyl_destroy(cyl_handle h);
 
+/* Limit of every host wait of the library on a run's device work (stepping,
+ * state, field and particle reads, diagnostics, batches), in seconds;
+ * seconds <= 0 removes the limit.  Process-wide, 600 s unless set.  A wait
+ * that runs out returns CYL_ERR_TIMEOUT before the run's host state moves:
+ * the queued work continues, and a later call waits for it again.  Copies
+ * into or out of caller memory are queued only after the run's earlier work
+ * is done, and their own end is always waited for.  The reference has no
+ * equivalent (its MPI waits are unbounded). */
+int cyl_set_wait_timeout(double seconds);
+
 /* Upload one species' particles (SoA host arrays of length n: Cartesian
  * position x, y, z (m), momentum px, py, pz (kg m/s), weight, id).  The
  * Fortran side packs these from its list (shared_data.F90:93-142). */

@@ -51,3 +51,14 @@ def test_create_without_device_reports_status():
     h = C.c_void_p()
     rc = lib.cyl_create(C.byref(g), sp, 1, None, 0, None, C.byref(h))
     assert rc == abi.CYL_ERR_NO_DEVICE
+
+
+def test_wait_timeout_setter():
+    """cyl_set_wait_timeout touches no device: NaN is refused, other values
+    (<= 0 meaning no limit) are taken."""
+    import cylindrical_epoch_gb300 as cg
+    from cylindrical_epoch_gb300 import abi
+    lib = cg.load()
+    assert lib.cyl_set_wait_timeout(float("nan")) == abi.CYL_ERR_BAD_ARG
+    assert lib.cyl_set_wait_timeout(0.0) == abi.CYL_OK
+    cg.set_wait_timeout(600.0)

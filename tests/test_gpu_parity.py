@@ -95,24 +95,32 @@ def test_thermal_steps_parity(gpu_lib):
     a, b = match_by_id(gpu.particles(0), orc.particles(0))
     for k in ("x", "y", "z"):
         assert rel_l2(getattr(a, k), getattr(b, k)) < 1e-12
-    # Mode 0 within 1e-10.  Modes m >= 1 of a thermal plasma amplify a
-    # last-bit change of a particle's angle through the deposit's
-    # (m dtheta)^-2 factors (particles.F90:603-625), and the device's atomic
-    # current additions change last bits of the fields from step 2 on.  The
-    # bar for m >= 1 is therefore the oracle's own response to last-bit
-    # angle changes: the same oracle with libm atan2, which differs from
-    # the correctly rounded one by one ulp on about 0.1 % of the angles.
+    _cmp_fields_noisy(gpu, orc, deck, 10, ["exm", "erm", "etm", "bxm", "brm", "btm", "jxm", "jrm", "jtm"])
+
+
+def _cmp_fields_noisy(gpu, orc, deck, nsteps, names):
+    """Fields of a thermal-noise run after nsteps steps from t = 0.  Mode 0
+    within 1e-10.  Modes m >= 1 of a thermal plasma amplify a last-bit change
+    of a particle's angle through the deposit's (m dtheta)^-2 factors
+    (particles.F90:603-625), and the device's atomic current additions
+    change last bits of the fields from step 2 on.  The bar for m >= 1 is
+    therefore the oracle's own response to last-bit angle changes: the same
+    oracle with libm atan2, which differs from the correctly rounded one by
+    one ulp on about 0.1 % of the angles (or 1e-10, if larger)."""
     from oracle.oracle import Oracle
     parts, rng = cg.host_load(deck)
     ulp = Oracle(deck, particles=parts, rng=rng, atan2="libm")
     ulp.initialise()
-    ulp.step(10)
-    names = ["exm", "erm", "etm", "bxm", "brm", "btm", "jxm", "jrm", "jtm"]
+    ulp.step(nsteps)
     for n in names:
         g, o, u = gpu.field(n), orc.field(n), ulp.field(n)
+        if np.all(o == 0) and np.all(g == 0):
+            continue
         e0 = rel_l2(g[0], o[0])
         assert e0 < TOL_FIELD, f"{n} mode 0: rel L2 {e0:.3e}"
         for m in range(1, g.shape[0]):
+            if np.all(o[m] == 0) and np.all(g[m] == 0):
+                continue
             e, s = rel_l2(g[m], o[m]), rel_l2(u[m], o[m])
             assert e < max(TOL_FIELD, s), f"{n} mode {m}: rel L2 {e:.3e}, one-ulp response {s:.3e}"
 
@@ -220,7 +228,7 @@ def _steps_parity(deck, nsteps=10, fields=("exm", "erm", "etm", "bxm", "brm", "b
     sg, so = gpu.state(), orc.state()
     for isp in range(len(deck.species)):
         assert sg.n_live[isp] == so.n_live[isp], isp
-    _cmp_fields(gpu, orc, list(fields))
+    _cmp_fields_noisy(gpu, orc, deck, nsteps, list(fields))
     return gpu, orc
 
 
