@@ -674,18 +674,10 @@ __device__ __forceinline__ bool push_one(int64_t i, const SpeciesPtrs& sp, Speci
   const f2 e05 = fm(ct, st);
   const f2 edt = fm(c3, s3) * fm(ct, -st);
   const float dth = atan2f(z3, y3) - atan2f(z, y);
-  // A particle that neither moves nor turns over the deposit's interval
-  // adds exactly zero to every current value (its weight changes and v_theta
-  // are zero): a warp all of whose particles are such skips the deposit.
-  // That is most of the plasma ahead of a laser, cold and in zero field.
-  const bool moving = (dxs != 0.f) || (dys != 0.f) || (dzs != 0.f) || (vt != 0.f);
-  if (SHARED) {
-    if (__any_sync(__activemask(), moving))
-      deposit_tile_warp<M>(tile, og, oh, dgx, dgy, dcx, dcy, cx2, cy2, fc, fcz, e05, edt, dth);
-  } else if (moving) {
-    deposit_global<M>(F, P, og, oh, dgx, dgy, dcx, dcy, cx2, cy2, fc, fcz, e05, edt, dth);
-  }
-  // position at t + dt, then particle_bcs in the cell units of this grid
+  // position at t + dt, then particle_bcs in the cell units of this grid.
+  // The particle is stored before its deposit (whose inputs are all formed
+  // above), so that its new state is not held in registers across the
+  // deposit; a particle that leaves still deposits the current of its move.
   const int kk = (int)floorf(fxn);
   int knew = k + kk;
   float fnew = fxn - (float)kk;
@@ -732,15 +724,26 @@ __device__ __forceinline__ bool push_one(int64_t i, const SpeciesPtrs& sp, Speci
   if (dead) {
     sp.kx[i] = INT32_MIN;
     atomicAdd((unsigned long long*)&cnt->n_dead, 1ull);
-    return true;
+  } else {
+    sp.kx[i] = knew + nsh;
+    sp.fx[i] = fnew;
+    sp.fy[i] = yn;
+    sp.fz[i] = zn;
+    sp.ux[i] = ux;
+    sp.uy[i] = uy;
+    sp.uz[i] = uz;
   }
-  sp.kx[i] = knew + nsh;
-  sp.fx[i] = fnew;
-  sp.fy[i] = yn;
-  sp.fz[i] = zn;
-  sp.ux[i] = ux;
-  sp.uy[i] = uy;
-  sp.uz[i] = uz;
+  // A particle that neither moves nor turns over the deposit's interval
+  // adds exactly zero to every current value (its weight changes and v_theta
+  // are zero): a warp all of whose particles are such skips the deposit.
+  // That is most of the plasma ahead of a laser, cold and in zero field.
+  const bool moving = (dxs != 0.f) || (dys != 0.f) || (dzs != 0.f) || (vt != 0.f);
+  if (SHARED) {
+    if (__any_sync(__activemask(), moving))
+      deposit_tile_warp<M>(tile, og, oh, dgx, dgy, dcx, dcy, cx2, cy2, fc, fcz, e05, edt, dth);
+  } else if (moving) {
+    deposit_global<M>(F, P, og, oh, dgx, dgy, dcx, dcy, cx2, cy2, fc, fcz, e05, edt, dth);
+  }
   return true;
 }
 
