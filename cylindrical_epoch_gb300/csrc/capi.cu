@@ -1361,15 +1361,23 @@ int cyl_upload_particles(cyl_handle hh, int32_t isp, const double* x, const doub
     CK(cudaMemcpyAsync(p.w, w, b, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(p.id, id, b, cudaMemcpyHostToDevice, s));
   }
+  // the counters, with the largest FP32 weight (the mixed form's fixed-point
+  // deposit scale) and the largest id (the next id of window injection)
+  // reduced on the device from the copied arrays
   SpeciesCounters c{n, 0, 0u, 0u};
-  float wmax = 0.f;  // largest FP32 weight, for the mixed form's fixed-point deposit scale
-  for (int64_t i = 0; i < n; ++i) {
-    if (id[i] >= h->next_id) h->next_id = id[i] + 1;
-    wmax = std::max(wmax, std::fabs((float)w[i]));
-  }
-  std::memcpy(&c.wmax_bits, &wmax, sizeof(float));
+  long long max_id = -1;
+  long long* d_max = reinterpret_cast<long long*>(h->d_red);  // reduction scratch
   CK(cudaMemcpyAsync(h->d_cnt + isp, &c, sizeof(c), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d_max, &max_id, sizeof(max_id), cudaMemcpyHostToDevice, s));
+  if (h->prec == CYL_PREC_MIXED)
+    upload_stats(s, h->sc.tmp + (size_t)6 * h->sc.cap, reinterpret_cast<const int64_t*>(h->sc.tmp + (size_t)7 * h->sc.cap),
+                 n, h->d_cnt + isp, d_max);
+  else
+    upload_stats(s, p.w, p.id, n, h->d_cnt + isp, d_max);
+  CK(cudaGetLastError());
   WAIT(copies_done(h, s));
+  CK(cudaMemcpy(&max_id, d_max, sizeof(max_id), cudaMemcpyDeviceToHost));
+  if (max_id >= h->next_id) h->next_id = max_id + 1;
   return CYL_OK;
 }
 
@@ -1765,6 +1773,16 @@ int cyl_download_field(cyl_handle hh, int32_t which, double* data) {
   WAIT(wait_stream(h, h->st));
   const int fs = f32_slot(h, which);
   if (fs >= 0) {
+    const int64_t nval = (int64_t)h->fcount * 2;
+    if (nval <= h->sc.cap * 7) {
+      // widened on the device into the sort scratch, then one copy into the
+      // caller's array (no host-side pass over the values)
+      widen_f32(h->st, reinterpret_cast<const float*>(h->Ff[fs]), h->sc.tmp, nval);
+      CK(cudaGetLastError());
+      CK(cudaMemcpyAsync(data, h->sc.tmp, (size_t)nval * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+      WAIT(copies_done(h, h->st));
+      return CYL_OK;
+    }
     std::vector<float> tmp(h->fcount * 2);
     CK(cudaMemcpy(tmp.data(), h->Ff[fs], tmp.size() * sizeof(float), cudaMemcpyDeviceToHost));
     for (size_t i = 0; i < tmp.size(); ++i) data[i] = (double)tmp[i];

@@ -88,6 +88,48 @@ void mixed_to_double(cudaStream_t s, const SpeciesPtrs& sp, double* stage, int64
   k_to_double<<<1024, 256, 0, s>>>(sp, stage, n, cap, xg0, rc);
 }
 
+// FP32 values widened to FP64 (exact), for the downloads of the mixed form's
+// FP32 field arrays.
+__global__ void k_widen(const float* src, double* dst, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = (double)src[i];
+}
+
+void widen_f32(cudaStream_t s, const float* src, double* dst, int64_t n) {
+  k_widen<<<1024, 256, 0, s>>>(src, dst, n);
+}
+
+// What an upload of n particles (weights w, ids id, on the device) adds to
+// its species' counters: the largest |w| rounded to FP32 (its bits, which
+// order as the non-negative values do) into cnt->wmax_bits, and the largest
+// id into *max_id (the caller sets both to their starting values).
+__global__ void k_upload_stats(const double* w, const int64_t* id, int64_t n, SpeciesCounters* cnt,
+                               long long* max_id) {
+  unsigned wb = 0u;
+  long long mid = -1;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned b = __float_as_uint(fabsf((float)w[i]));
+    wb = b > wb ? b : wb;
+    const long long v = (long long)id[i];
+    mid = v > mid ? v : mid;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned wo = __shfl_down_sync(0xffffffffu, wb, o);
+    const long long mo = __shfl_down_sync(0xffffffffu, mid, o);
+    wb = wo > wb ? wo : wb;
+    mid = mo > mid ? mo : mid;
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(&cnt->wmax_bits, wb);
+    atomicMax(max_id, mid);
+  }
+}
+
+void upload_stats(cudaStream_t s, const double* w, const int64_t* id, int64_t n, SpeciesCounters* cnt,
+                  long long* max_id) {
+  if (n > 0) k_upload_stats<<<256, 256, 0, s>>>(w, id, n, cnt, max_id);
+}
+
 // particle_bcs in the cell units of a grid whose cell_x_r origin is
 // x_grid_min: xc = kx - nsh + fx (boundary.F90:1584-1860).
 __device__ __forceinline__ bool mixed_bc(const SpeciesPtrs& sp, int64_t i, int nsh, float xlo, float xhi,

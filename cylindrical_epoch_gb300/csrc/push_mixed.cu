@@ -604,11 +604,84 @@ __device__ __forceinline__ bool push_one(int64_t i, const SpeciesPtrs& sp, Speci
   igm = inv_gamma(ux, uy, uz);
   const float dxs = ux * (P.cdt2_dx * igm), dys = uy * (P.cdt2_dy * igm), dzs = uz * (P.cdt2_dy * igm);
   const float fxn = fx + dxs;
-  float yn = y + dys, zn = z + dzs;
+  const float yn = y + dys, zn = z + dzs;
   const float rn = sqrtf(yn * yn + zn * zn);
   float vt = 0.f;  // v_theta at t + dt (m/s)
   if (rn > 0.f) vt = (P.c * igm) * ((uz * yn - uy * zn) / rn);
 
+  // position at t + dt, then particle_bcs in the cell units of this grid.
+  // The particle is stored before its deposit (whose inputs are all formed
+  // above), so that its new state is not held in registers across the
+  // deposit; a particle that leaves still deposits the current of its move.
+  const int kk = (int)floorf(fxn);
+  int knew = k + kk;
+  float fnew = fxn - (float)kk;
+  if (fnew >= 1.0f) { fnew -= 1.0f; knew += 1; }
+  if (fnew < 0.0f) fnew = 0.0f;
+  // the stored radial position (a reflection at r_max moves it); the
+  // deposit below uses the unreflected move
+  float ys = yn, zs = zn;
+  bool dead = false;
+  if (apply_bcs) {
+    const float xc = (float)knew + fnew;
+    if (xc < P.x_lo) {
+      const int b = sp.bc[CYL_BD_X_MIN];
+      if (b == CYL_BC_REFLECT) {
+        const float v = 2.0f * P.x_sys_lo - xc;
+        knew = (int)floorf(v); fnew = v - (float)knew; ux = -ux;
+      } else if (b == CYL_BC_PERIODIC) {
+        knew += rc.nx;
+      }
+      if (xc < P.x_out_lo && b != CYL_BC_PERIODIC) dead = true;
+    }
+    if (xc >= P.x_hi) {
+      const int b = sp.bc[CYL_BD_X_MAX];
+      if (b == CYL_BC_REFLECT) {
+        const float v = 2.0f * P.x_sys_hi - xc;
+        knew = (int)floorf(v); fnew = v - (float)knew; ux = -ux;
+      } else if (b == CYL_BC_PERIODIC) {
+        knew -= rc.nx;
+      }
+      if (xc >= P.x_out_hi && b != CYL_BC_PERIODIC) dead = true;
+    }
+    if (rn >= P.r_hi) {
+      const int b = sp.bc[CYL_BD_Y_MAX];
+      if (b == CYL_BC_REFLECT) {
+        const float f = 2.0f * P.r_sys / rn - 1.0f;
+        ys *= f;
+        zs *= f;
+        const float rr = sqrtf(ys * ys + zs * zs);
+        const float cc = ys / rr, ss = zs / rr;
+        const float pr = uy * cc + uz * ss, pt = -uy * ss + uz * cc;
+        uy = -pr * cc - pt * ss;
+        uz = -pr * ss + pt * cc;
+      }
+      if (rn >= P.r_out && b != CYL_BC_PERIODIC) dead = true;
+    }
+  }
+  if (dead) {
+    sp.kx[i] = INT32_MIN;
+    atomicAdd((unsigned long long*)&cnt->n_dead, 1ull);
+  } else {
+    sp.kx[i] = knew + nsh;
+    sp.fx[i] = fnew;
+    sp.fy[i] = ys;
+    sp.fz[i] = zs;
+    sp.ux[i] = ux;
+    sp.uy[i] = uy;
+    sp.uz[i] = uz;
+  }
+  // A particle that neither moves nor turns over the deposit's interval
+  // adds exactly zero to every current value (its weight changes and v_theta
+  // are zero): a warp all of whose particles are such skips the deposit and its
+  // preparation.
+  // That is most of the plasma ahead of a laser, cold and in zero field.
+  const bool moving = (dxs != 0.f) || (dys != 0.f) || (dzs != 0.f) || (vt != 0.f);
+  if (SHARED) {
+    if (!__any_sync(__activemask(), moving)) return true;
+  } else if (!moving) {
+    return true;
+  }
   // deposit: shape change from t+dt/2 to t+3dt/2 (particles.F90:515-665)
   const float fx3 = fxn + dxs, y3 = yn + dys, z3 = zn + dzs;
   const float r3 = sqrtf(y3 * y3 + z3 * z3);
@@ -674,76 +747,10 @@ __device__ __forceinline__ bool push_one(int64_t i, const SpeciesPtrs& sp, Speci
   const f2 e05 = fm(ct, st);
   const f2 edt = fm(c3, s3) * fm(ct, -st);
   const float dth = atan2f(z3, y3) - atan2f(z, y);
-  // position at t + dt, then particle_bcs in the cell units of this grid.
-  // The particle is stored before its deposit (whose inputs are all formed
-  // above), so that its new state is not held in registers across the
-  // deposit; a particle that leaves still deposits the current of its move.
-  const int kk = (int)floorf(fxn);
-  int knew = k + kk;
-  float fnew = fxn - (float)kk;
-  if (fnew >= 1.0f) { fnew -= 1.0f; knew += 1; }
-  if (fnew < 0.0f) fnew = 0.0f;
-  bool dead = false;
-  if (apply_bcs) {
-    const float xc = (float)knew + fnew;
-    if (xc < P.x_lo) {
-      const int b = sp.bc[CYL_BD_X_MIN];
-      if (b == CYL_BC_REFLECT) {
-        const float v = 2.0f * P.x_sys_lo - xc;
-        knew = (int)floorf(v); fnew = v - (float)knew; ux = -ux;
-      } else if (b == CYL_BC_PERIODIC) {
-        knew += rc.nx;
-      }
-      if (xc < P.x_out_lo && b != CYL_BC_PERIODIC) dead = true;
-    }
-    if (xc >= P.x_hi) {
-      const int b = sp.bc[CYL_BD_X_MAX];
-      if (b == CYL_BC_REFLECT) {
-        const float v = 2.0f * P.x_sys_hi - xc;
-        knew = (int)floorf(v); fnew = v - (float)knew; ux = -ux;
-      } else if (b == CYL_BC_PERIODIC) {
-        knew -= rc.nx;
-      }
-      if (xc >= P.x_out_hi && b != CYL_BC_PERIODIC) dead = true;
-    }
-    if (rn >= P.r_hi) {
-      const int b = sp.bc[CYL_BD_Y_MAX];
-      if (b == CYL_BC_REFLECT) {
-        const float f = 2.0f * P.r_sys / rn - 1.0f;
-        yn *= f;
-        zn *= f;
-        const float rr = sqrtf(yn * yn + zn * zn);
-        const float cc = yn / rr, ss = zn / rr;
-        const float pr = uy * cc + uz * ss, pt = -uy * ss + uz * cc;
-        uy = -pr * cc - pt * ss;
-        uz = -pr * ss + pt * cc;
-      }
-      if (rn >= P.r_out && b != CYL_BC_PERIODIC) dead = true;
-    }
-  }
-  if (dead) {
-    sp.kx[i] = INT32_MIN;
-    atomicAdd((unsigned long long*)&cnt->n_dead, 1ull);
-  } else {
-    sp.kx[i] = knew + nsh;
-    sp.fx[i] = fnew;
-    sp.fy[i] = yn;
-    sp.fz[i] = zn;
-    sp.ux[i] = ux;
-    sp.uy[i] = uy;
-    sp.uz[i] = uz;
-  }
-  // A particle that neither moves nor turns over the deposit's interval
-  // adds exactly zero to every current value (its weight changes and v_theta
-  // are zero): a warp all of whose particles are such skips the deposit.
-  // That is most of the plasma ahead of a laser, cold and in zero field.
-  const bool moving = (dxs != 0.f) || (dys != 0.f) || (dzs != 0.f) || (vt != 0.f);
-  if (SHARED) {
-    if (__any_sync(__activemask(), moving))
-      deposit_tile_warp<M>(tile, og, oh, dgx, dgy, dcx, dcy, cx2, cy2, fc, fcz, e05, edt, dth);
-  } else if (moving) {
+  if (SHARED)
+    deposit_tile_warp<M>(tile, og, oh, dgx, dgy, dcx, dcy, cx2, cy2, fc, fcz, e05, edt, dth);
+  else
     deposit_global<M>(F, P, og, oh, dgx, dgy, dcx, dcy, cx2, cy2, fc, fcz, e05, edt, dth);
-  }
   return true;
 }
 

@@ -89,6 +89,9 @@ void mixed_from_double(cudaStream_t s, const SpeciesPtrs& sp, const double* stag
                        double xg0, const RunConst& rc);
 void mixed_to_double(cudaStream_t s, const SpeciesPtrs& sp, double* stage, int64_t n, int64_t cap,
                      double xg0, const RunConst& rc);
+void widen_f32(cudaStream_t s, const float* src, double* dst, int64_t n);
+void upload_stats(cudaStream_t s, const double* w, const int64_t* id, int64_t n, SpeciesCounters* cnt,
+                  long long* max_id);
 void mixed_window_particles(cudaStream_t s, const SpeciesPtrs& sp, SpeciesCounters* cnt, const double* inject,
                             const StepRec* rec, int isp, double xg0, const RunConst& rc, int* err, int nblocks);
 void mixed_particle_bcs(cudaStream_t s, const SpeciesPtrs& sp, SpeciesCounters* cnt, const StepRec* rec,
