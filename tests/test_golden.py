@@ -33,3 +33,19 @@ def test_oracle_matches_golden_fixture():
             ref = np.asarray(b[name][key])
             scale = max(np.max(np.abs(b[name]["l2"])), 1e-300)
             np.testing.assert_allclose(a[name][key], ref, rtol=1e-10, atol=1e-10 * scale, err_msg=f"{name}.{key}")
+
+
+def test_full_deck_record():
+    """The committed record of the whole 2000-step wakefield deck (written on
+    a GB300 by the opt-in test_full_wakefield_deck_against_oracle): the FP64
+    form against the oracle with equal counts and window shifts and per-mode
+    Ez within 1e-9, the mixed form within its 1e-3 Ez bar."""
+    with open(os.path.join(HERE, "golden", "full_deck_summary.json")) as f:
+        rec = json.load(f)
+    assert rec["steps"] == 2000
+    fp, mx = rec["against_oracle"]["fp64"], rec["against_oracle"]["mixed"]
+    assert fp["n_live"]["run"] == fp["n_live"]["against"]
+    assert fp["n_shifts"]["run"] == fp["n_shifts"]["against"] > 500
+    assert max(fp["ez_rel_l2_per_mode"]) < 1e-9
+    assert max(mx["ez_rel_l2_per_mode"]) <= 1e-3
+    assert mx["n_shifts"]["run"] == mx["n_shifts"]["against"]
