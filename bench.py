@@ -467,7 +467,7 @@ def main():
     ap.add_argument("--serve", action="store_true", help="parameter-scan serving benchmark")
     ap.add_argument("--jobs", type=int, default=64)
     ap.add_argument("--arrival", type=float, default=0.5, help="mean Poisson arrival gap (s)")
-    ap.add_argument("--workers", type=int, default=4)
+    ap.add_argument("--workers", type=int, default=8)
     ap.add_argument("--max-batch", type=int, default=16)
     ap.add_argument("--fp64-sample", type=int, default=3)
     ap.add_argument("--fp64-steps-max", type=int, default=100)

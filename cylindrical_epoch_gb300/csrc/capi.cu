@@ -554,7 +554,7 @@ static void enqueue_current_finish(Handle* h, cudaStream_t s, const FieldSetT<T>
       launch_ionise(s, F, h->sp, h->nsp, h->d_cnt, h->ion, rec, rc, h->d_ion, h->d_ion + MAX_SPECIES, h->d_err,
                     h->nblocks);
       launch_current_finish(s, F, rec, rc, h->gd.smooth_currents, h->gd.smooth_its, h->gd.smooth_comp_its, stride,
-                            wk, 2);
+                            wk, 6);
       int nion = 0;
       for (int i = 0; i < h->nsp; ++i) nion += h->ion.s[i].ionise;
       count_launch(h, 4 + nion);
@@ -948,6 +948,10 @@ struct cyl_batch_s {
   std::vector<cudaEvent_t> ev_run;  // one per run slot
   BatchJob* h_jobs = nullptr;       // pinned, CHUNK x cap_jobs (step-major)
   BatchJob* d_jobs = nullptr;
+  StageJob* h_stage = nullptr;      // pinned, CHUNK x cap_runs (step-major)
+  StageJob* d_stage = nullptr;
+  WindowJob* h_win = nullptr;       // pinned, CHUNK x cap_jobs (step-major)
+  WindowJob* d_win = nullptr;
   int2* d_work = nullptr;
   int* d_nwork = nullptr;
   int64_t work_cap = 0;
@@ -966,39 +970,97 @@ struct JobRef {
   int isp;
 };
 
-// The kernels of k steps of a batch, on b->st with each run's stream forked
-// and joined around every push; the chunk's (job, tile) table first, every
-// run's sort last.
-static void enqueue_batch_chunk(cyl_batch_s* b, const std::vector<Handle*>& runs, int njobs, int k, int M) {
+// The extents and boundary kinds of a batch's runs (one M for all).
+static StageDims stage_dims(const std::vector<Handle*>& runs, int* mask_any, bool* any_window) {
+  StageDims d{0, 0, runs[0]->rc.M};
+  *mask_any = 0;
+  *any_window = false;
+  for (Handle* h : runs) {
+    d.nx_max = std::max(d.nx_max, h->rc.nx);
+    d.ny_max = std::max(d.ny_max, h->rc.ny);
+    *mask_any |= h->rc.bc_mask;
+    *any_window = *any_window || h->move_window;
+  }
+  return d;
+}
+
+// The kernels of k steps of a batch on b->st: per step, each field and
+// boundary stage of every run in one launch from the chunk's stage table
+// (update_eb_fields_half, the J swap, the (run, tile) push, current_finish,
+// update_eb_fields_final, the window's particle stages and field shift), the
+// stages that only some runs have (current smoothing, counter injection) per
+// run on the same stream; the chunk's (job, tile) table first, every run's
+// sort last on its own stream.  The step's node count depends on the number
+// of runs with those extra stages, not on the number of runs.
+static void enqueue_batch_chunk(cyl_batch_s* b, const std::vector<Handle*>& runs, int njobs, int nwin, int k,
+                                int M, const std::vector<int>& par0) {
   const PushMixedFns& fns = push_mixed_fns(0);
   const int nbt = runs[0]->nblocks_by_shape[0], nbg = runs[0]->nblocks;
+  const int nr = (int)runs.size();
+  int mask_any = 0;
+  bool any_window = false;
+  const StageDims d = stage_dims(runs, &mask_any, &any_window);
+  bool any_finish = false;
+  for (Handle* h : runs) any_finish = any_finish || stage_finish_needed(h->rc);
   batch_schedule(b->st, b->d_jobs, njobs, b->d_work, b->d_nwork);
-  cudaEventRecord(b->ev_sched, b->st);
-  std::vector<FieldSetF> F(runs.size());
+  int launches = 1;
   for (int i = 0; i < k; ++i) {
-    for (size_t r = 0; r < runs.size(); ++r) {
-      Handle* h = runs[r];
-      cudaStreamWaitEvent(h->st, i == 0 ? b->ev_sched : b->ev_push, 0);
-      F[r] = enqueue_step_pre<cplxf>(h, h->st, h->d_rec + i);
-      cudaEventRecord(b->ev_run[r], h->st);
-      cudaStreamWaitEvent(b->st, b->ev_run[r], 0);
-    }
+    const StageJob* st = b->d_stage + (size_t)i * b->cap_runs;
+    batch_update_e_f32(b->st, st, nr, 0, d);
+    batch_e_axis_bcs(b->st, st, nr, 0, mask_any, d);
+    batch_update_b_f32(b->st, st, nr, 0, 1, d);
+    batch_b_axis_bcs(b->st, st, nr, 0, mask_any, d);
+    batch_zero_j(b->st, st, nr, d);
     const BatchJob* tab = b->d_jobs + (size_t)i * b->cap_jobs;
     batch_reset(b->st, tab, njobs);
     fns.launch_batch(b->st, M, tab, njobs, b->d_work, b->d_nwork, nbt, nbg);
-    cudaEventRecord(b->ev_push, b->st);
-    for (size_t r = 0; r < runs.size(); ++r) {
-      Handle* h = runs[r];
-      cudaStreamWaitEvent(h->st, b->ev_push, 0);
-      enqueue_step_post<cplxf>(h, h->st, F[r], h->d_rec + i, h->d_src + h->src_per_step * i);
+    batch_j_rmin(b->st, st, nr, d);
+    launches += 10;
+    if (any_finish) {
+      batch_current_finish(b->st, st, nr);
+      launches += 1;
+    }
+    for (int r = 0; r < nr; ++r) {
+      Handle* h = runs[(size_t)r];
+      if (!h->gd.smooth_currents) continue;
+      // smoothing (rare): per run
+      const FieldSetF F1 = fieldset_f(h, par0[(size_t)r] ^ ((i + 1) & 1));
+      const RunConst& rc = h->rc;
+      FView wk{h->F[15], rc.nxg, rc.nyg};
+      const int stride = h->gd.smooth_stride > 0 ? h->gd.smooth_stride : 1;
+      launch_current_finish(b->st, F1, h->d_rec + i, rc, h->gd.smooth_currents, h->gd.smooth_its,
+                            h->gd.smooth_comp_its, stride, wk, 4);
+      launches += 1;
+    }
+    batch_update_b_f32(b->st, st, nr, 1, 0, d);
+    batch_b_final_bcs(b->st, st, nr, mask_any, d);
+    batch_update_e_f32(b->st, st, nr, 1, d);
+    batch_e_axis_bcs(b->st, st, nr, 1, mask_any, d);
+    launches += 8;
+    if (any_window) {
+      for (Handle* h : runs)
+        if (h->move_window && h->inj_counter) {
+          launch_inject_counter(b->st, h->d_rec + i, h->d_injsp, h->nsp, h->rc, h->inj_seed, h->d_injrow,
+                                h->d_inj);
+          launches += 1;
+        }
+      batch_window_particles(b->st, b->d_win + (size_t)i * b->cap_jobs, nwin, nbg);
+      batch_shift_fields(b->st, st, nr, 0, d);
+      batch_shift_fields(b->st, st, nr, 1, d);
+      launches += 5;
     }
   }
+  runs[0]->kernel_launches += launches;
+  cudaEventRecord(b->ev_push, b->st);
   for (size_t r = 0; r < runs.size(); ++r) {
     Handle* h = runs[r];
+    cudaStreamWaitEvent(h->st, b->ev_push, 0);
     enqueue_sort(h, h->d_rec + (k - 1));
     cudaEventRecord(b->ev_run[r], h->st);
     cudaStreamWaitEvent(b->st, b->ev_run[r], 0);
   }
+  // the chunk advanced each run's J parity by k
+  for (Handle* h : runs) h->jpar ^= (k & 1);
 }
 
 }  // namespace cyl
@@ -2476,6 +2538,12 @@ int cyl_batch_create(int32_t max_runs, cyl_batch* out) {
   const size_t tab = sizeof(BatchJob) * (size_t)CHUNK * b->cap_jobs;
   ok(cudaMallocHost(&b->h_jobs, tab));
   ok(cudaMalloc(&b->d_jobs, tab));
+  const size_t stab = sizeof(StageJob) * (size_t)CHUNK * b->cap_runs;
+  ok(cudaMallocHost(&b->h_stage, stab));
+  ok(cudaMalloc(&b->d_stage, stab));
+  const size_t wtab = sizeof(WindowJob) * (size_t)CHUNK * b->cap_jobs;
+  ok(cudaMallocHost(&b->h_win, wtab));
+  ok(cudaMalloc(&b->d_win, wtab));
   ok(cudaMalloc(&b->d_nwork, sizeof(int)));
   const int hw = (int)std::thread::hardware_concurrency();
   b->pool.reset(new HostPool(std::max(0, std::min({max_runs - 1, hw / 2, 8}))));
@@ -2582,6 +2650,39 @@ int cyl_batch_step(cyl_batch b, const cyl_handle* hs, int32_t n, int32_t nsteps)
     // that step's swap
     std::vector<int> par0(runs.size());
     for (size_t r = 0; r < runs.size(); ++r) par0[r] = runs[r]->jpar;
+    // the stage table (per step, one row per run) and the window's
+    // (run, species) table
+    int nwin = 0;
+    for (int i = 0; i < k; ++i) {
+      int w = 0;
+      for (size_t r = 0; r < runs.size(); ++r) {
+        Handle* h = runs[r];
+        StageJob& S = b->h_stage[(size_t)i * b->cap_runs + r];
+        S.F0 = fieldset_f(h, par0[r] ^ (i & 1));
+        S.F1 = fieldset_f(h, par0[r] ^ ((i + 1) & 1));
+        S.rec = h->d_rec + i;
+        S.src = h->d_src + h->src_per_step * i;
+        S.cols = h->cols;
+        S.rowtab = reinterpret_cast<const float4*>(h->rowtab);
+        S.rc = h->rc;
+        stage_job_bc_consts(S);
+        stage_job_yee_consts(S);
+        if (!h->move_window) continue;
+        for (int isp = 0; isp < h->nsp; ++isp) {
+          WindowJob& W = b->h_win[(size_t)i * b->cap_jobs + w++];
+          W.sp = h->sp[isp];
+          W.cnt = h->d_cnt + isp;
+          W.inject = h->d_inj;
+          W.rec = h->d_rec + i;
+          W.P = h->mp[isp];
+          W.rc = h->rc;
+          W.xg0 = h->xg0;
+          W.isp = isp;
+          W.err = h->d_err;
+        }
+      }
+      nwin = w;
+    }
     for (int i = 0; i < k; ++i)
       for (int j = 0; j < nj; ++j) {
         Handle* h = jobs[j].h;
@@ -2598,6 +2699,10 @@ int cyl_batch_step(cyl_batch b, const cyl_handle* hs, int32_t n, int32_t nsteps)
       }
     if (cudaMemcpyAsync(b->d_jobs, b->h_jobs, sizeof(BatchJob) * (size_t)k * b->cap_jobs, cudaMemcpyHostToDevice,
                         b->st) != cudaSuccess ||
+        cudaMemcpyAsync(b->d_stage, b->h_stage, sizeof(StageJob) * (size_t)k * b->cap_runs,
+                        cudaMemcpyHostToDevice, b->st) != cudaSuccess ||
+        (nwin > 0 && cudaMemcpyAsync(b->d_win, b->h_win, sizeof(WindowJob) * (size_t)k * b->cap_jobs,
+                                     cudaMemcpyHostToDevice, b->st) != cudaSuccess) ||
         cudaEventRecord(b->ev_jobs, b->st) != cudaSuccess)
       return CYL_ERR_CUDA;
     b->jobs_pending = true;
@@ -2622,7 +2727,7 @@ int cyl_batch_step(cyl_batch b, const cyl_handle* hs, int32_t n, int32_t nsteps)
           drop_exec();
           return CYL_ERR_CUDA;
         }
-        enqueue_batch_chunk(b, runs, nj, k, M);
+        enqueue_batch_chunk(b, runs, nj, nwin, k, M, par0);
         if (cudaStreamEndCapture(b->st, &graph) != cudaSuccess) {
           drop_exec();
           return CYL_ERR_CUDA;
@@ -2653,7 +2758,7 @@ int cyl_batch_step(cyl_batch b, const cyl_handle* hs, int32_t n, int32_t nsteps)
       if (cudaGraphLaunch(b->gexec, b->st) != cudaSuccess) return CYL_ERR_CUDA;
     } else {
       (void)cudaGetLastError();
-      enqueue_batch_chunk(b, runs, nj, k, M);
+      enqueue_batch_chunk(b, runs, nj, nwin, k, M, par0);
       if (cudaGetLastError() != cudaSuccess) return CYL_ERR_CUDA;
     }
     // each run's later work (its next copies, reads) comes after the chunk
@@ -2677,6 +2782,10 @@ int cyl_batch_destroy(cyl_batch b) {
   if (b->gexec) cudaGraphExecDestroy(b->gexec);
   cudaFreeHost(b->h_jobs);
   cudaFree(b->d_jobs);
+  cudaFreeHost(b->h_stage);
+  cudaFree(b->d_stage);
+  cudaFreeHost(b->h_win);
+  cudaFree(b->d_win);
   cudaFree(b->d_work);
   cudaFree(b->d_nwork);
   for (cudaEvent_t ev : {b->ev_sched, b->ev_push, b->ev_done, b->ev_jobs})

@@ -18,6 +18,79 @@ struct FieldSetT {
 using FieldSet = FieldSetT<cplx>;
 using FieldSetF = FieldSetT<cplxf>;
 
+// Scalars of the axis, laser and r_max kernels, rounded once on the host
+// in the order the kernels used to evaluate them (no FMA contraction on
+// either side, so the FP64 form's values are unchanged).
+struct BcConst {
+  double c4dy;                 // 4 c^2 / dy
+  double inv_eps0, inv_dx, inv_dy, inv_9;
+  double lx, lr, sum, diff, dt_eps;  // k_laser_x
+  double rx_lx, rx_inv_r, rx_dtc2_4r, rx_ly, rx_sum_x, rx_sum_t, rx_dt_2eps, rx_lx_c;  // k_rmax_b
+  cplx rx_icdt_2r;
+};
+
+// Coefficients of the first radial cell (ir = 1) of the mixed form's Yee
+// updates in FP64, precomputed on the host so that the row needs no FP64
+// division (h = dt/2, r_d, r_p of ir = 1):
+// E: a = c^2/r_p h/2, bm = c^2/r_p h (times i m), c = c^2/dy h, cx = c^2/dx h,
+//    d = h/eps0, erm = c^2/r_d h (times i m);
+// B: p = h/r_d (times i m), q = h/(2 r_d), r = h/dy, s = h/r_p (times i m),
+//    t = h/dx.
+struct Row1E {
+  double a, bm, c, cx, d, erm;
+};
+struct Row1B {
+  double p, q, r, s, t;
+};
+
+// One run of a batch in one step, for the batched field and boundary stages
+// (one launch per stage for every run of the batch, blockIdx.y = run): the
+// field sets of the step's first half (F0, J of the step before) and of the
+// push (F1, after the J swap), the step's record and laser sources, and the
+// run's constants with the host-rounded coefficients of each stage.
+struct StageJob {
+  FieldSetF F0, F1;
+  const StepRec* rec;
+  const double* src;
+  const cplx* cols;
+  const float4* rowtab;
+  RunConst rc;
+  BcConst K;
+  Row1E r1e;
+  Row1B r1b;
+  float cdx, cdy, cj, hdx, hdy;
+};
+// The host-rounded constants of a stage job from its rc (K in fields.cu,
+// the Yee coefficients in fields_fp32.cu).
+void stage_job_bc_consts(StageJob& J);
+void stage_job_yee_consts(StageJob& J);
+// Grid extents of a batch: the largest nx, ny of its runs (one M for all).
+struct StageDims {
+  int nx_max, ny_max, M;
+};
+// The mixed form's step stages for all runs of a batch (jobs: njobs
+// consecutive StageJobs of one step).  use_f1 selects F1 over F0.
+void batch_update_e_f32(cudaStream_t s, const StageJob* jobs, int njobs, int use_f1, const StageDims& d);
+void batch_update_b_f32(cudaStream_t s, const StageJob* jobs, int njobs, int use_f1, int save_old,
+                        const StageDims& d);
+// k_e_axis and efield_bcs; k_b_axis and the halo of bfield_bcs (the
+// update_eb_fields_half sequence); bc_mask_any: the OR of the runs' masks
+void batch_e_axis_bcs(cudaStream_t s, const StageJob* jobs, int njobs, int use_f1, int bc_mask_any,
+                      const StageDims& d);
+void batch_b_axis_bcs(cudaStream_t s, const StageJob* jobs, int njobs, int use_f1, int bc_mask_any,
+                      const StageDims& d);
+// update_b_field's axis rules and bfield_final_bcs, on F1
+void batch_b_final_bcs(cudaStream_t s, const StageJob* jobs, int njobs, int bc_mask_any, const StageDims& d);
+// current_bcs_r_min_final on F1; J = 0 of F1 (the swap's zeroing)
+void batch_j_rmin(cudaStream_t s, const StageJob* jobs, int njobs, const StageDims& d);
+void batch_zero_j(cudaStream_t s, const StageJob* jobs, int njobs, const StageDims& d);
+// current_finish's folding and halo pass of the runs that need it (reflecting
+// or periodic boundaries: stage_finish_needed), on F1
+void batch_current_finish(cudaStream_t s, const StageJob* jobs, int njobs);
+bool stage_finish_needed(const RunConst& rc);
+// shift_fields of a window shift (which = the shift's index in the step), on F1
+void batch_shift_fields(cudaStream_t s, const StageJob* jobs, int njobs, int which, const StageDims& d);
+
 // Geometry tables of push_particles (particles.F90:189-217), run constant.
 struct GeomTables {
   const double* inv_area_rt;    // index iy - (1-jng)
@@ -76,7 +149,7 @@ void launch_b_final_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* re
                         const cplx* cols, int do_axis, double dt, const RunConst& rc);
 template <typename T>
 void launch_current_finish(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc,
-                           int smooth, int its, int comp_its, int stride, FView wk, int parts = 3);
+                           int smooth, int its, int comp_its, int stride, FView wk, int parts = 7);
 template <typename T>
 void launch_shift_fields(cudaStream_t s, const FieldSetT<T>& F, const cplx* cols, const StepRec* rec,
                          int which, const RunConst& rc);

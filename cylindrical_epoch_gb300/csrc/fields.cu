@@ -12,6 +12,7 @@
 // each other at the domain corners).  current_finish (current_smooth.F90:
 // 29-45), which is cheap and only active for periodic or reflecting
 // particle boundaries, stays one single-CTA kernel.
+#include <algorithm>
 #include <cstddef>
 
 #include <type_traits>
@@ -162,9 +163,9 @@ struct Triplet {
 
 // st0 = 0 for (ex, er, et), 3 for (bx, br, bt)
 template <typename T>
-__global__ void k_ghost_phase(Triplet<T> tr, int st0, int ph, const int32_t* bcp, RunConst rc) {
+__device__ __forceinline__ void ghost_phase_item(const Triplet<T>& tr, int st0, int ph, const int32_t* bcp,
+                                                 const RunConst& rc, int64_t t) {
   const int nx = rc.nx, ny = rc.ny, M = rc.M;
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (ph == PH_CONDUCT_Y || ph == PH_OTHER_Y) {
     // r_max: items (ix fastest, i = 1..NG, m, q)
     const int ncol = nx + 2 * NG;
@@ -225,9 +226,13 @@ __global__ void k_ghost_phase(Triplet<T> tr, int st0, int ph, const int32_t* bcp
     }
   }
 }
+template <typename T>
+__global__ void k_ghost_phase(Triplet<T> tr, int st0, int ph, const int32_t* bcp, RunConst rc) {
+  ghost_phase_item<T>(tr, st0, ph, bcp, rc, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // Device address of a step record's field bc codes (no host dereference).
-static const int32_t* bc_ptr(const StepRec* rec) {
+__host__ __device__ static const int32_t* bc_ptr(const StepRec* rec) {
   return reinterpret_cast<const int32_t*>(reinterpret_cast<const char*>(rec) + offsetof(StepRec, bc_field));
 }
 
@@ -266,17 +271,6 @@ __device__ __forceinline__ cplx div_form(cplx a, double d, double inv_d) {
   if constexpr (std::is_same<T, cplxf>::value) return a * inv_d;
   else return a / d;
 }
-
-// Scalars of the axis, laser and r_max kernels, rounded once on the host
-// in the order the kernels used to evaluate them (no FMA contraction on
-// either side, so the FP64 form's values are unchanged).
-struct BcConst {
-  double c4dy;                 // 4 c^2 / dy
-  double inv_eps0, inv_dx, inv_dy, inv_9;
-  double lx, lr, sum, diff, dt_eps;  // k_laser_x
-  double rx_lx, rx_inv_r, rx_dtc2_4r, rx_ly, rx_sum_x, rx_sum_t, rx_dt_2eps, rx_lx_c;  // k_rmax_b
-  cplx rx_icdt_2r;
-};
 
 static BcConst bc_const(const RunConst& rc, double dt) {
   BcConst k;
@@ -395,10 +389,10 @@ __device__ __forceinline__ void b_axis_item(FViewT<T> bx, FViewT<T> br, FViewT<T
 // is of a column other than the ones written (columns 0, 1 at x_min and nx
 // at x_max; nx >= 8).
 template <typename T>
-__global__ void k_laser_x(FieldSetT<T> F, const StepRec* rec, const double* src, const cplx* cols, double dt,
-                          BcConst K, RunConst rc) {
+__device__ __forceinline__ void laser_x_item(const FieldSetT<T>& F, const StepRec* rec, const double* src,
+                                             const cplx* cols, double dt, const BcConst& K, const RunConst& rc,
+                                             int t) {
   const int nx = rc.nx, ny = rc.ny, M = rc.M;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= 2 * (ny + 1) * M) return;
   const int side = t / ((ny + 1) * M);
   const int ir = t % (ny + 1), m = (t / (ny + 1)) % M;
@@ -464,14 +458,19 @@ __global__ void k_laser_x(FieldSetT<T> F, const StepRec* rec, const double* src,
     if (do_br) F.br(nx, ir, m) = nbr;
   }
 }
+template <typename T>
+__global__ void k_laser_x(FieldSetT<T> F, const StepRec* rec, const double* src, const cplx* cols, double dt,
+                          BcConst K, RunConst rc) {
+  laser_x_item<T>(F, rec, src, cols, dt, K, rc, blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // outflow_bcs_r_max (laser.f90:637-690) or zero_b (boundary.F90:1528-1531),
 // one thread per (ix, m).  The new Bx, Bt of row ny depend on row ny-1, row
 // ny of the other arrays and the B_old / J_old arrays only.
 template <typename T>
-__global__ void k_rmax_b(FieldSetT<T> F, const StepRec* rec, double dt, BcConst K, RunConst rc) {
+__device__ __forceinline__ void rmax_b_item(const FieldSetT<T>& F, const StepRec* rec, double dt, const BcConst& K,
+                                            const RunConst& rc, int t) {
   const int nx = rc.nx, ny = rc.ny, M = rc.M;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int b = rec->bc_field[CYL_BD_Y_MAX];
   if (b == CYL_BC_ZERO_B) {
     if (t >= (nx + 2 * NG) * M) return;
@@ -505,6 +504,10 @@ __global__ void k_rmax_b(FieldSetT<T> F, const StepRec* rec, double dt, BcConst 
   v = v - (icm * CLIGHT) * (F.br(ix, ny - 1, m) + F.bro(ix, ny - 1, m));
   v = v + dt_2eps * (F.jx(ix, ny - 1, m) + F.jxo(ix, ny - 1, m));
   F.bt(ix, ny, m) = sum_t * v;
+}
+template <typename T>
+__global__ void k_rmax_b(FieldSetT<T> F, const StepRec* rec, double dt, BcConst K, RunConst rc) {
+  rmax_b_item<T>(F, rec, dt, K, rc, blockIdx.x * blockDim.x + threadIdx.x);
 }
 // ------------------------------------------------------------- currents
 
@@ -616,7 +619,8 @@ __device__ void periodic_sum_dev(FView f, const RunConst& rc) {
 
 // current_bcs_r_min_final, then current_finish (current_smooth.F90:29-45)
 // without smoothing (one CTA).
-__global__ void __launch_bounds__(CTA_THREADS) k_current_finish(FView jx, FView jr, FView jt, const StepRec* rec, RunConst rc) {
+__device__ __forceinline__ void current_finish_cta(FView jx, FView jr, FView jt, const StepRec* rec,
+                                                   const RunConst& rc) {
   __shared__ int bcf[4];
   if (threadIdx.x < 4) bcf[threadIdx.x] = rec->bc_field[threadIdx.x];
   __syncthreads();
@@ -636,6 +640,19 @@ __global__ void __launch_bounds__(CTA_THREADS) k_current_finish(FView jx, FView 
   halo_x(jx, 1 - NG, rc.ny + NG, bcf, rc);
   halo_x(jr, 1 - NG, rc.ny + NG, bcf, rc);
   halo_x(jt, 1 - NG, rc.ny + NG, bcf, rc);
+}
+__global__ void __launch_bounds__(CTA_THREADS) k_current_finish(FView jx, FView jr, FView jt, const StepRec* rec, RunConst rc) {
+  current_finish_cta(jx, jr, jt, rec, rc);
+}
+// The folding and halo pass has work only with a reflecting or periodic
+// particle boundary or a periodic x field boundary (before or after the
+// window starts); all of these are fixed for the run.
+__host__ __device__ static bool finish_needed(const RunConst& rc) {
+  const bool reflect = rc.bc_allspecies[CYL_BD_X_MIN] == CYL_BC_REFLECT ||
+                       rc.bc_allspecies[CYL_BD_X_MAX] == CYL_BC_REFLECT ||
+                       rc.bc_allspecies[CYL_BD_Y_MAX] == CYL_BC_REFLECT;
+  const bool periodic = rc.bc_allspecies[CYL_BD_X_MIN] == CYL_BC_PERIODIC || (rc.bc_mask & BCM_PERIODIC_X);
+  return reflect || periodic;
 }
 
 // One pass of smooth_mode_array (current_smooth.F90:172-190): the halo of wk
@@ -723,11 +740,11 @@ __device__ void shift_row_regs(FViewT<U> f, int j, int m, const int* bcf, const 
     for (int i = 1 - NG + (int)threadIdx.x; i <= 0; i += (int)blockDim.x) f(i, j, m) = f(nx + i, j, m);
 }
 
-// VPT: elements per thread of the register path (0: the chunked path)
+// VPT: elements per thread of the register path (0: the chunked path).
+// One CTA per row j and mode m.
 template <typename T, int VPT>
-__global__ void k_shift_fields(FieldSetT<T> F, const cplx* cols, const StepRec* rec, int which, RunConst rc) {
-  const int j = 1 - NG + (int)blockIdx.x;
-  const int m = blockIdx.y;
+__device__ __forceinline__ void shift_fields_row(const FieldSetT<T>& F, const cplx* cols, const StepRec* rec,
+                                                 int which, const RunConst& rc, int j, int m) {
   const int nx = rc.nx;
   __shared__ int bcf[4];
   if (threadIdx.x < 4) bcf[threadIdx.x] = rec->bc_field_after[threadIdx.x];
@@ -770,6 +787,10 @@ __global__ void k_shift_fields(FieldSetT<T> F, const cplx* cols, const StepRec* 
     F.br(nx, j, m) = 0.5 * (F.br(nx - 1, j, m) + F.br(nx + 1, j, m));
     F.bt(nx, j, m) = 0.5 * (F.bt(nx - 1, j, m) + F.bt(nx + 1, j, m));
   }
+}
+template <typename T, int VPT>
+__global__ void k_shift_fields(FieldSetT<T> F, const cplx* cols, const StepRec* rec, int which, RunConst rc) {
+  shift_fields_row<T, VPT>(F, cols, rec, which, rc, 1 - NG + (int)blockIdx.x, blockIdx.y);
 }
 
 // Axis rules and J folding: one thread per independent work item.
@@ -844,21 +865,14 @@ void launch_b_final_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* re
 }
 template <typename T>
 // parts: bit 0 the r_min fold (current_bcs_r_min_final, the end of
-// push_particles), bit 1 the rest (current_finish): field ionisation runs
-// between the two (epoch2d.F90:218-252).
+// push_particles), bits 1 and 2 current_finish (the folding and halo pass,
+// the smoothing): field ionisation runs between the fold and current_finish
+// (epoch2d.F90:218-252).
 void launch_current_finish(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc,
                            int smooth, int its, int comp_its, int stride, FView wk, int parts) {
   if (parts & 1) k_j_rmin<<<jrmin_blocks(rc), 128, 0, s>>>(F.jx, F.jr, F.jt, rc);
-  if (!(parts & 2)) return;
-  // the folding and halo pass has work only with a reflecting or periodic
-  // particle boundary or a periodic x field boundary (before or after the
-  // window starts); all of these are fixed for the run
-  const bool reflect = rc.bc_allspecies[CYL_BD_X_MIN] == CYL_BC_REFLECT ||
-                       rc.bc_allspecies[CYL_BD_X_MAX] == CYL_BC_REFLECT ||
-                       rc.bc_allspecies[CYL_BD_Y_MAX] == CYL_BC_REFLECT;
-  const bool periodic = rc.bc_allspecies[CYL_BD_X_MIN] == CYL_BC_PERIODIC || (rc.bc_mask & BCM_PERIODIC_X);
-  if (reflect || periodic) k_current_finish<<<1, CTA_THREADS, 0, s>>>(F.jx, F.jr, F.jt, rec, rc);
-  if (!smooth) return;
+  if ((parts & 2) && finish_needed(rc)) k_current_finish<<<1, CTA_THREADS, 0, s>>>(F.jx, F.jr, F.jt, rec, rc);
+  if (!(parts & 4) || !smooth) return;
   FView js[3] = {F.jx, F.jr, F.jt};
   dim3 blk(128), grd((rc.nx + 127) / 128, rc.ny, rc.M);
   const size_t bytes = (size_t)rc.nxg * rc.nyg * rc.M * sizeof(cplx);
@@ -884,6 +898,155 @@ void launch_shift_fields(cudaStream_t s, const FieldSetT<T>& F, const cplx* cols
   else if (vpt <= 9) k_shift_fields<T, 9><<<grd, SHIFT_THREADS, 0, s>>>(F, cols, rec, which, rc);
   else if (vpt <= SHIFT_VPT_MAX) k_shift_fields<T, SHIFT_VPT_MAX><<<grd, SHIFT_THREADS, 0, s>>>(F, cols, rec, which, rc);
   else k_shift_fields<T, 0><<<grd, 256, 0, s>>>(F, cols, rec, which, rc);
+}
+
+// ------------------------------------- batched stages of the mixed form
+//
+// One launch per stage for every run of a batch: blockIdx.y (blockIdx.z for
+// the shift) is the run's StageJob, the rest of the grid covers the largest
+// run, and each run's items are the single-run kernel's (the same item
+// functions, so a run's arithmetic is the one it gets alone).
+
+void stage_job_bc_consts(StageJob& J) { J.K = bc_const(J.rc, J.rc.dt); }
+
+__device__ __forceinline__ bool ghost_phase_needed(int mask, int ph) {
+  const int need = ph == PH_HALO ? BCM_PERIODIC_X
+                                 : (ph == PH_CONDUCT_X || ph == PH_CONDUCT_Y) ? BCM_CONDUCT : BCM_OTHER;
+  return (mask & need) != 0;
+}
+
+// which: 0 the E triplet, 1 the B triplet of the job's field set
+__global__ void k_ghost_phase_batch(const StageJob* __restrict__ jobs, int which, int use_f1, int st0, int ph) {
+  const StageJob& J = jobs[blockIdx.y];
+  if (!ghost_phase_needed(J.rc.bc_mask, ph)) return;
+  const RunConst rc = J.rc;
+  const FieldSetF& Fr = use_f1 ? J.F1 : J.F0;
+  const Triplet<cplxf> tr = which == 0 ? Triplet<cplxf>{{Fr.ex, Fr.er, Fr.et}} : Triplet<cplxf>{{Fr.bx, Fr.br, Fr.bt}};
+  ghost_phase_item<cplxf>(tr, st0, ph, bc_ptr(J.rec), rc, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+__global__ void k_e_axis_batch(const StageJob* __restrict__ jobs, int use_f1) {
+  const StageJob& J = jobs[blockIdx.y];
+  const RunConst rc = J.rc;
+  const int ncol = rc.nx + 2 * NG;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ncol * rc.M * NG) return;
+  const FieldSetF& F = use_f1 ? J.F1 : J.F0;
+  const int ix = 1 - NG + t % ncol, r = t / ncol;
+  e_axis_item(F.ex, F.er, F.et, F.jx, F.bt, rc, J.K, ix, r % rc.M, r / rc.M);
+}
+__global__ void k_b_axis_batch(const StageJob* __restrict__ jobs, int use_f1) {
+  const StageJob& J = jobs[blockIdx.y];
+  const RunConst rc = J.rc;
+  const int ncol = rc.nx + 2 * NG;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ncol * rc.M * NG) return;
+  const FieldSetF& F = use_f1 ? J.F1 : J.F0;
+  const int ix = 1 - NG + t % ncol, r = t / ncol;
+  b_axis_item(F.bx, F.br, F.bt, F.ex, F.et, rc, J.K, ix, r % rc.M, r / rc.M);
+}
+__global__ void k_laser_x_batch(const StageJob* __restrict__ jobs) {
+  const StageJob& J = jobs[blockIdx.y];
+  const RunConst rc = J.rc;
+  laser_x_item<cplxf>(J.F1, J.rec, J.src, J.cols, rc.dt, J.K, rc, blockIdx.x * blockDim.x + threadIdx.x);
+}
+__global__ void k_rmax_b_batch(const StageJob* __restrict__ jobs) {
+  const StageJob& J = jobs[blockIdx.y];
+  const RunConst rc = J.rc;
+  rmax_b_item<cplxf>(J.F1, J.rec, rc.dt, J.K, rc, blockIdx.x * blockDim.x + threadIdx.x);
+}
+__global__ void k_j_rmin_batch(const StageJob* __restrict__ jobs) {
+  const StageJob& J = jobs[blockIdx.y];
+  const int ncol = J.rc.nx + 2 * NG;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ncol * J.rc.M) return;
+  j_rmin_item(J.F1.jx, J.F1.jr, J.F1.jt, 1 - NG + t % ncol, t / ncol);
+}
+__global__ void k_zero_j_batch(const StageJob* __restrict__ jobs) {
+  const StageJob& J = jobs[blockIdx.y];
+  const int64_t n = (int64_t)J.rc.nxg * J.rc.nyg * J.rc.M;
+  cplx* const a = J.F1.jx.p;
+  cplx* const b = J.F1.jr.p;
+  cplx* const c = J.F1.jt.p;
+  const cplx z = mk(0, 0);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    a[i] = z;
+    b[i] = z;
+    c[i] = z;
+  }
+}
+template <int VPT>
+__global__ void k_shift_fields_batch(const StageJob* __restrict__ jobs, int which) {
+  const StageJob& J = jobs[blockIdx.z];
+  const RunConst rc = J.rc;
+  if ((int)blockIdx.x >= rc.nyg) return;  // the whole CTA
+  shift_fields_row<cplxf, VPT>(J.F1, J.cols, J.rec, which, rc, 1 - NG + (int)blockIdx.x, blockIdx.y);
+}
+
+// current_finish's folding and halo pass: one CTA per run (runs without it
+// leave at once)
+__global__ void __launch_bounds__(CTA_THREADS) k_current_finish_batch(const StageJob* __restrict__ jobs) {
+  const StageJob& J = jobs[blockIdx.x];
+  const RunConst rc = J.rc;
+  if (!finish_needed(rc)) return;  // the whole CTA
+  current_finish_cta(J.F1.jx, J.F1.jr, J.F1.jt, J.rec, rc);
+}
+
+static void batch_ghost(cudaStream_t s, const StageJob* jobs, int njobs, int which, int use_f1, int st0,
+                        bool halo_only, int mask_any, const StageDims& d) {
+  const int nx_items = 2 * 3 * d.M * (d.ny_max + 2 * NG) * NG;
+  const int ny_items = (d.nx_max + 2 * NG) * NG * d.M * 3;
+  const dim3 gx((nx_items + 255) / 256, njobs), gy((ny_items + 255) / 256, njobs);
+  if (mask_any & BCM_PERIODIC_X) k_ghost_phase_batch<<<gx, 256, 0, s>>>(jobs, which, use_f1, st0, PH_HALO);
+  if (halo_only) return;
+  if (mask_any & BCM_CONDUCT) {
+    k_ghost_phase_batch<<<gx, 256, 0, s>>>(jobs, which, use_f1, st0, PH_CONDUCT_X);
+    k_ghost_phase_batch<<<gy, 256, 0, s>>>(jobs, which, use_f1, st0, PH_CONDUCT_Y);
+  }
+  if (mask_any & BCM_OTHER) {
+    k_ghost_phase_batch<<<gx, 256, 0, s>>>(jobs, which, use_f1, st0, PH_OTHER_X);
+    k_ghost_phase_batch<<<gy, 256, 0, s>>>(jobs, which, use_f1, st0, PH_OTHER_Y);
+  }
+}
+static dim3 batch_axis_grid(int njobs, const StageDims& d) {
+  return dim3(((d.nx_max + 2 * NG) * d.M * NG + 127) / 128, njobs);
+}
+void batch_e_axis_bcs(cudaStream_t s, const StageJob* jobs, int njobs, int use_f1, int bc_mask_any,
+                      const StageDims& d) {
+  k_e_axis_batch<<<batch_axis_grid(njobs, d), 128, 0, s>>>(jobs, use_f1);
+  batch_ghost(s, jobs, njobs, 0, use_f1, 0, false, bc_mask_any, d);
+}
+void batch_b_axis_bcs(cudaStream_t s, const StageJob* jobs, int njobs, int use_f1, int bc_mask_any,
+                      const StageDims& d) {
+  k_b_axis_batch<<<batch_axis_grid(njobs, d), 128, 0, s>>>(jobs, use_f1);
+  batch_ghost(s, jobs, njobs, 1, use_f1, 3, true, bc_mask_any, d);
+}
+void batch_b_final_bcs(cudaStream_t s, const StageJob* jobs, int njobs, int bc_mask_any, const StageDims& d) {
+  k_b_axis_batch<<<batch_axis_grid(njobs, d), 128, 0, s>>>(jobs, 1);
+  batch_ghost(s, jobs, njobs, 1, 1, 3, false, bc_mask_any, d);
+  k_laser_x_batch<<<dim3((2 * (d.ny_max + 1) * d.M + 127) / 128, njobs), 128, 0, s>>>(jobs);
+  k_rmax_b_batch<<<dim3(((d.nx_max + 2 * NG) * d.M + 127) / 128, njobs), 128, 0, s>>>(jobs);
+  batch_ghost(s, jobs, njobs, 1, 1, 3, true, bc_mask_any, d);
+}
+void batch_j_rmin(cudaStream_t s, const StageJob* jobs, int njobs, const StageDims& d) {
+  k_j_rmin_batch<<<dim3(((d.nx_max + 2 * NG) * d.M + 127) / 128, njobs), 128, 0, s>>>(jobs);
+}
+void batch_current_finish(cudaStream_t s, const StageJob* jobs, int njobs) {
+  k_current_finish_batch<<<njobs, CTA_THREADS, 0, s>>>(jobs);
+}
+bool stage_finish_needed(const RunConst& rc) { return finish_needed(rc); }
+void batch_zero_j(cudaStream_t s, const StageJob* jobs, int njobs, const StageDims& d) {
+  const int64_t n = (int64_t)(d.nx_max + 2 * NG) * (d.ny_max + 2 * NG) * d.M;
+  const int nb = (int)std::min<int64_t>((n + 255) / 256, 256);
+  k_zero_j_batch<<<dim3(nb, njobs), 256, 0, s>>>(jobs);
+}
+void batch_shift_fields(cudaStream_t s, const StageJob* jobs, int njobs, int which, const StageDims& d) {
+  const dim3 grd(d.ny_max + 2 * NG, d.M, njobs);
+  const int vpt = (d.nx_max + 2 * NG + SHIFT_THREADS - 1) / SHIFT_THREADS;
+  if (vpt <= 4) k_shift_fields_batch<4><<<grd, SHIFT_THREADS, 0, s>>>(jobs, which);
+  else if (vpt <= 6) k_shift_fields_batch<6><<<grd, SHIFT_THREADS, 0, s>>>(jobs, which);
+  else if (vpt <= 9) k_shift_fields_batch<9><<<grd, SHIFT_THREADS, 0, s>>>(jobs, which);
+  else if (vpt <= SHIFT_VPT_MAX) k_shift_fields_batch<SHIFT_VPT_MAX><<<grd, SHIFT_THREADS, 0, s>>>(jobs, which);
+  else k_shift_fields_batch<0><<<grd, 256, 0, s>>>(jobs, which);
 }
 
 #define INST(T)                                                                                          \

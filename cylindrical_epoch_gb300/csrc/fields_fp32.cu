@@ -23,27 +23,10 @@ __device__ __forceinline__ float2 ldj(const cplx* p) {
   return make_float2(d2f_bits(v.x), d2f_bits(v.y));
 }
 
-// Coefficients of the first radial cell (ir = 1) in FP64, precomputed on the
-// host so that the row needs no FP64 division (h = dt/2, r_d, r_p of ir = 1):
-// E: a = c^2/r_p h/2, bm = c^2/r_p h (times i m), c = c^2/dy h, cx = c^2/dx h,
-//    d = h/eps0, erm = c^2/r_d h (times i m);
-// B: p = h/r_d (times i m), q = h/(2 r_d), r = h/dy, s = h/r_p (times i m),
-//    t = h/dx.
-struct Row1E {
-  double a, bm, c, cx, d, erm;
-};
-struct Row1B {
-  double p, q, r, s, t;
-};
-
-// Grid: (columns, modes, rows), so that the FP64 first row of every mode is
-// in the first wave of CTAs rather than the tail of the launch.
-__global__ void k_update_e_f32(FieldSetF F, const float4* rowtab, float cdx, float cdy, float cj, Row1E r1,
-                               RunConst rc) {
-  const int ix = blockIdx.x * blockDim.x + threadIdx.x;  // 0..nx
-  const int im = blockIdx.y;
-  const int ir = 1 + blockIdx.z;
-  if (ix > rc.nx) return;
+// One cell and mode of update_e_field's bulk: (ix, ir) for ix = 0..nx,
+// ir = 1..ny.
+__device__ __forceinline__ void update_e_item(const FieldSetF& F, const float4* rowtab, float cdx, float cdy,
+                                              float cj, const Row1E& r1, int ix, int im, int ir) {
   if (ir == 1) {
     // first radial cell in FP64 arithmetic (the equations of update_e_field)
     const double m = (double)im;
@@ -91,12 +74,11 @@ __global__ void k_update_e_f32(FieldSetF F, const float4* rowtab, float cdx, flo
   st2(F.et.ptr(ix, ir, im), e);
 }
 
-__global__ void k_update_b_f32(FieldSetF F, int save_old, const float4* rowtab, float hdx, float hdy, Row1B r1,
-                               RunConst rc) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int im = blockIdx.y;
-  const int j = blockIdx.z;
-  if (i >= rc.nxg) return;
+// One cell and mode of update_b_field over the whole ghosted array (index
+// i, j from the first ghost), with the optional B_old save.
+__device__ __forceinline__ void update_b_item(const FieldSetF& F, int save_old, const float4* rowtab, float hdx,
+                                              float hdy, const Row1B& r1, const RunConst& rc, int i, int im,
+                                              int j) {
   const int ix = i + 1 - NG, ir = j + 1 - NG;
   if (save_old) {
     st2(F.bxo.ptr(ix, ir, im), ld2(F.bx.ptr(ix, ir, im)));
@@ -149,23 +131,88 @@ __global__ void k_update_b_f32(FieldSetF F, int save_old, const float4* rowtab, 
   st2(F.bt.ptr(ix, ir, im), b);
 }
 
-void launch_update_e_f32(cudaStream_t s, const FieldSetF& F, const double* rowtab, const RunConst& rc) {
+// Grid: (columns, modes, rows), so that the FP64 first row of every mode is
+// in the first wave of CTAs rather than the tail of the launch.
+__global__ void k_update_e_f32(FieldSetF F, const float4* rowtab, float cdx, float cdy, float cj, Row1E r1,
+                               RunConst rc) {
+  const int ix = blockIdx.x * blockDim.x + threadIdx.x;  // 0..nx
+  if (ix > rc.nx) return;
+  update_e_item(F, rowtab, cdx, cdy, cj, r1, ix, blockIdx.y, 1 + blockIdx.z);
+}
+__global__ void k_update_b_f32(FieldSetF F, int save_old, const float4* rowtab, float hdx, float hdy, Row1B r1,
+                               RunConst rc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= rc.nxg) return;
+  update_b_item(F, save_old, rowtab, hdx, hdy, r1, rc, i, blockIdx.y, blockIdx.z);
+}
+
+// The batched forms: run blockIdx.z, (mode, row) blockIdx.y = m + M row.
+__global__ void k_update_e_f32_batch(const StageJob* __restrict__ jobs, int use_f1) {
+  const StageJob& J = jobs[blockIdx.z];
+  const int M = J.rc.M;
+  const int ix = blockIdx.x * blockDim.x + threadIdx.x;
+  const int im = blockIdx.y % M, ir = 1 + blockIdx.y / M;
+  if (ix > J.rc.nx || ir > J.rc.ny) return;
+  const FieldSetF F = use_f1 ? J.F1 : J.F0;
+  update_e_item(F, J.rowtab, J.cdx, J.cdy, J.cj, J.r1e, ix, im, ir);
+}
+__global__ void k_update_b_f32_batch(const StageJob* __restrict__ jobs, int use_f1, int save_old) {
+  const StageJob& J = jobs[blockIdx.z];
+  const int M = J.rc.M;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int im = blockIdx.y % M, j = blockIdx.y / M;
+  if (i >= J.rc.nxg || j >= J.rc.nyg) return;
+  const FieldSetF F = use_f1 ? J.F1 : J.F0;
+  const RunConst rc = J.rc;
+  update_b_item(F, save_old, J.rowtab, J.hdx, J.hdy, J.r1b, rc, i, im, j);
+}
+
+static void yee_e_consts(const RunConst& rc, float& cdx, float& cdy, float& cj, Row1E& r1) {
   const double c2 = CLIGHT * CLIGHT, h = 0.5 * rc.dt;
   const double r_d = std::fabs(rc.y_grid_min), r_p = r_d + 0.5 * rc.dy;
-  const Row1E r1{c2 / r_p * 0.5 * h, c2 / r_p * h, c2 / rc.dy * h, c2 / rc.dx * h, h / EPS0, c2 / r_d * h};
+  r1 = Row1E{c2 / r_p * 0.5 * h, c2 / r_p * h, c2 / rc.dy * h, c2 / rc.dx * h, h / EPS0, c2 / r_d * h};
+  cdx = (float)(c2 / rc.dx * h);
+  cdy = (float)(c2 / rc.dy * h);
+  cj = (float)(h / EPS0);
+}
+static void yee_b_consts(const RunConst& rc, float& hdx, float& hdy, Row1B& r1) {
+  const double h = 0.5 * rc.dt;
+  const double r_d = std::fabs(rc.y_grid_min), r_p = r_d + 0.5 * rc.dy;
+  r1 = Row1B{h / r_d, 0.5 * h / r_d, h / rc.dy, h / r_p, h / rc.dx};
+  hdx = (float)(h / rc.dx);
+  hdy = (float)(h / rc.dy);
+}
+
+void stage_job_yee_consts(StageJob& J) {
+  yee_e_consts(J.rc, J.cdx, J.cdy, J.cj, J.r1e);
+  yee_b_consts(J.rc, J.hdx, J.hdy, J.r1b);
+}
+
+void launch_update_e_f32(cudaStream_t s, const FieldSetF& F, const double* rowtab, const RunConst& rc) {
+  float cdx, cdy, cj;
+  Row1E r1;
+  yee_e_consts(rc, cdx, cdy, cj, r1);
   dim3 blk(128), grd((rc.nx + 1 + 127) / 128, rc.M, rc.ny);
-  k_update_e_f32<<<grd, blk, 0, s>>>(F, reinterpret_cast<const float4*>(rowtab), (float)(c2 / rc.dx * h),
-                                     (float)(c2 / rc.dy * h), (float)(h / EPS0), r1, rc);
+  k_update_e_f32<<<grd, blk, 0, s>>>(F, reinterpret_cast<const float4*>(rowtab), cdx, cdy, cj, r1, rc);
 }
 
 void launch_update_b_f32(cudaStream_t s, const FieldSetF& F, int save_old, const double* rowtab,
                          const RunConst& rc) {
-  const double h = 0.5 * rc.dt;
-  const double r_d = std::fabs(rc.y_grid_min), r_p = r_d + 0.5 * rc.dy;
-  const Row1B r1{h / r_d, 0.5 * h / r_d, h / rc.dy, h / r_p, h / rc.dx};
+  float hdx, hdy;
+  Row1B r1;
+  yee_b_consts(rc, hdx, hdy, r1);
   dim3 blk(128), grd((rc.nxg + 127) / 128, rc.M, rc.nyg);
-  k_update_b_f32<<<grd, blk, 0, s>>>(F, save_old, reinterpret_cast<const float4*>(rowtab), (float)(h / rc.dx),
-                                     (float)(h / rc.dy), r1, rc);
+  k_update_b_f32<<<grd, blk, 0, s>>>(F, save_old, reinterpret_cast<const float4*>(rowtab), hdx, hdy, r1, rc);
+}
+
+void batch_update_e_f32(cudaStream_t s, const StageJob* jobs, int njobs, int use_f1, const StageDims& d) {
+  dim3 blk(128), grd((d.nx_max + 1 + 127) / 128, d.M * d.ny_max, njobs);
+  k_update_e_f32_batch<<<grd, blk, 0, s>>>(jobs, use_f1);
+}
+void batch_update_b_f32(cudaStream_t s, const StageJob* jobs, int njobs, int use_f1, int save_old,
+                        const StageDims& d) {
+  dim3 blk(128), grd((d.nx_max + 2 * NG + 127) / 128, d.M * (d.ny_max + 2 * NG), njobs);
+  k_update_b_f32_batch<<<grd, blk, 0, s>>>(jobs, use_f1, save_old);
 }
 
 }  // namespace cyl

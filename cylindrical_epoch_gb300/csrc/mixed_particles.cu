@@ -190,8 +190,10 @@ __device__ __forceinline__ bool mixed_bc(const SpeciesPtrs& sp, int64_t i, int n
   return false;
 }
 
-__global__ void k_mixed_bcs(SpeciesPtrs sp, SpeciesCounters* cnt, const StepRec* rec, int after, MixedParams P,
-                            RunConst rc) {
+// bid, nb: the block index and block count of the grid-stride loop
+__device__ __forceinline__ void mixed_bcs_body(const SpeciesPtrs& sp, SpeciesCounters* cnt, const StepRec* rec,
+                                               int after, const MixedParams& P, const RunConst& rc, int bid,
+                                               int nb) {
   if (after && rec->nshift == 0) return;
   const int64_t n = cnt->n_used;
   const int nsh = after ? rec->nshift_total_after : rec->nshift_total;
@@ -200,7 +202,7 @@ __global__ void k_mixed_bcs(SpeciesPtrs sp, SpeciesCounters* cnt, const StepRec*
   const float xs_hi = (float)(((after ? rec->x_max_after : rec->x_max) - xgm) / rc.dx);
   const float xlo = -0.5f, xhi = (float)rc.nx - 0.5f;
   int64_t dead = 0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t i = (int64_t)bid * blockDim.x + threadIdx.x; i < n; i += (int64_t)nb * blockDim.x) {
     if (sp.kx[i] == INT32_MIN) continue;
     if (after && ((float)(sp.kx[i] - nsh) + sp.fx[i]) < xs_lo) {  // remove_particles (window.F90:304-325)
       sp.kx[i] = INT32_MIN;
@@ -213,17 +215,22 @@ __global__ void k_mixed_bcs(SpeciesPtrs sp, SpeciesCounters* cnt, const StepRec*
   }
   if (dead) atomicAdd((unsigned long long*)&cnt->n_dead, (unsigned long long)dead);
 }
+__global__ void k_mixed_bcs(SpeciesPtrs sp, SpeciesCounters* cnt, const StepRec* rec, int after, MixedParams P,
+                            RunConst rc) {
+  mixed_bcs_body(sp, cnt, rec, after, P, rc, blockIdx.x, gridDim.x);
+}
 
-__global__ void k_mixed_append(SpeciesPtrs sp, SpeciesCounters* cnt, const double* inject, const StepRec* rec,
-                               int isp, double xg0, RunConst rc, int* err) {
+__device__ __forceinline__ void mixed_append_body(const SpeciesPtrs& sp, SpeciesCounters* cnt, const double* inject,
+                                                  const StepRec* rec, int isp, double xg0, const RunConst& rc,
+                                                  int* err, int bid, int nb) {
   const int64_t off = rec->inject_off[isp], k = rec->inject_cnt[isp];
   const int64_t base = cnt->n_used;
   if (base + k > sp.cap) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err, ERR_CAPACITY);
+    if (bid == 0 && threadIdx.x == 0) atomicOr(err, ERR_CAPACITY);
     return;
   }
   unsigned wb = 0u;  // bits of the largest |FP32 weight| (positive floats order as integers)
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < k; i += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t i = (int64_t)bid * blockDim.x + threadIdx.x; i < k; i += (int64_t)nb * blockDim.x) {
     const double* q = inject + (off + i) * 8;
     to_mixed(sp, base + i, q[0], q[1], q[2], q[3], q[4], q[5], q[6], xg0, rc);
     sp.id[base + i] = __double_as_longlong(q[7]);
@@ -232,9 +239,44 @@ __global__ void k_mixed_append(SpeciesPtrs sp, SpeciesCounters* cnt, const doubl
   wb = __reduce_max_sync(0xffffffffu, wb);
   if ((threadIdx.x & 31) == 0 && wb != 0u) atomicMax(&cnt->wmax_bits, wb);
 }
-__global__ void k_mixed_append_commit(SpeciesPtrs sp, SpeciesCounters* cnt, const StepRec* rec, int isp) {
+__global__ void k_mixed_append(SpeciesPtrs sp, SpeciesCounters* cnt, const double* inject, const StepRec* rec,
+                               int isp, double xg0, RunConst rc, int* err) {
+  mixed_append_body(sp, cnt, inject, rec, isp, xg0, rc, err, blockIdx.x, gridDim.x);
+}
+__device__ __forceinline__ void mixed_append_commit_body(const SpeciesPtrs& sp, SpeciesCounters* cnt,
+                                                         const StepRec* rec, int isp) {
   const int64_t k = rec->inject_cnt[isp];
   if (cnt->n_used + k <= sp.cap) cnt->n_used += k;
+}
+__global__ void k_mixed_append_commit(SpeciesPtrs sp, SpeciesCounters* cnt, const StepRec* rec, int isp) {
+  mixed_append_commit_body(sp, cnt, rec, isp);
+}
+
+// The same three stages of the window for every (run, species) of a batch:
+// blockIdx.y is the WindowJob.
+__global__ void k_mixed_append_batch(const WindowJob* __restrict__ jobs) {
+  const WindowJob& J = jobs[blockIdx.y];
+  const RunConst rc = J.rc;
+  mixed_append_body(J.sp, J.cnt, J.inject, J.rec, J.isp, J.xg0, rc, J.err, blockIdx.x, gridDim.x);
+}
+__global__ void k_mixed_append_commit_batch(const WindowJob* __restrict__ jobs, int njobs) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= njobs) return;
+  const WindowJob& J = jobs[j];
+  mixed_append_commit_body(J.sp, J.cnt, J.rec, J.isp);
+}
+__global__ void k_mixed_bcs_batch(const WindowJob* __restrict__ jobs) {
+  const WindowJob& J = jobs[blockIdx.y];
+  const RunConst rc = J.rc;
+  const MixedParams P = J.P;
+  mixed_bcs_body(J.sp, J.cnt, J.rec, 1, P, rc, blockIdx.x, gridDim.x);
+}
+
+void batch_window_particles(cudaStream_t s, const WindowJob* jobs, int njobs, int nblocks) {
+  if (njobs == 0) return;
+  k_mixed_append_batch<<<dim3(64, njobs), 256, 0, s>>>(jobs);
+  k_mixed_append_commit_batch<<<(njobs + 63) / 64, 64, 0, s>>>(jobs, njobs);
+  k_mixed_bcs_batch<<<dim3(nblocks, njobs), 256, 0, s>>>(jobs);
 }
 
 void mixed_window_particles(cudaStream_t s, const SpeciesPtrs& sp, SpeciesCounters* cnt, const double* inject,

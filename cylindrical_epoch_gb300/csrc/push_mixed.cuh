@@ -89,6 +89,21 @@ void mixed_from_double(cudaStream_t s, const SpeciesPtrs& sp, const double* stag
                        double xg0, const RunConst& rc);
 void mixed_to_double(cudaStream_t s, const SpeciesPtrs& sp, double* stage, int64_t n, int64_t cap,
                      double xg0, const RunConst& rc);
+// One (run, species) of a batch in one step, for the window's particle
+// stages (append the step's injected particles, commit, particle_bcs after
+// the shift and remove_particles) of every member in one launch each.
+struct WindowJob {
+  SpeciesPtrs sp;
+  SpeciesCounters* cnt;
+  const double* inject;
+  const StepRec* rec;
+  MixedParams P;
+  RunConst rc;
+  double xg0;
+  int isp;
+  int* err;
+};
+void batch_window_particles(cudaStream_t s, const WindowJob* jobs, int njobs, int nblocks);
 void widen_f32(cudaStream_t s, const float* src, double* dst, int64_t n);
 void upload_stats(cudaStream_t s, const double* w, const int64_t* id, int64_t n, SpeciesCounters* cnt,
                   long long* max_id);

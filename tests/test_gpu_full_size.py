@@ -147,9 +147,13 @@ def test_c1_thermal_full_deck(gpu_lib, threads):
         # bar is ten times that spread with a 1e-11 floor.
         assert e < max(1e-11, 10 * sp), k
     # diagnostics (calc_df.F90:1246-1291 kinetic energy, per-mode field energy)
-    e1g, e1o = gpu.diagnostics(), orc.diagnostics()
+    # The energy of the noise-level B field (mostly m = 1) inherits that
+    # mode's summation-order spread: its bar is ten times the spread between
+    # the two oracle orders, or 1e-10 relative.
+    e1g, e1o, e1a = gpu.diagnostics(), orc.diagnostics(), alt.diagnostics()
     for k in ("kinetic_energy", "field_energy_e", "field_energy_b"):
-        assert abs(getattr(e1g, k) - getattr(e1o, k)) <= 1e-10 * abs(getattr(e1o, k)), k
+        bar = max(1e-10 * abs(getattr(e1o, k)), 10 * abs(getattr(e1a, k) - getattr(e1o, k)))
+        assert abs(getattr(e1g, k) - getattr(e1o, k)) <= bar, k
         assert abs(getattr(e0g, k) - getattr(e0o, k)) <= 1e-12 * max(abs(getattr(e0o, k)), 1e-300), k
     assert e1g.n_live == e1o.n_live
     # energy conservation of the 1 keV plasma over 200 steps, the same in both
