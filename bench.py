@@ -441,7 +441,7 @@ def _config(args, deck, form):
             "form": form, "nx": deck.nx, "ny": deck.ny, "n_mode": deck.n_mode,
             "ppc": deck.species[0].npart_per_cell, "moving_window": deck.move_window,
             "l2": "state larger than L2 (fields 15 x (nx+10)(ny+10) M complex + particles)",
-            "parallelism": f"replicas x{args.gpus}"}
+            "parallelism": f"replicas x{args.gpus}", "rng": getattr(args, "rng", "kiss")}
 
 
 def main():
@@ -456,6 +456,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--eager", action="store_true", help="no CUDA graphs")
+    ap.add_argument("--rng", default="kiss", choices=["kiss", "counter"],
+                    help="species load and window injection: host KISS stream or device counter stream")
     ap.add_argument("--fp64-steps", type=int, default=-1,
                     help="steps of the plain FP64 form timed beside the mixed form "
                          "(-1: the same K steps, compared with the mixed result; 0: skip)")
@@ -507,7 +509,13 @@ def main():
             form = "mixed"
     deck = build_deck(args.deck, form, args.modes)
     parts, rng = cg.host_load(deck)
-    run = cg.Run(deck, particles=parts, rng=rng)
+    if args.rng == "counter":
+        # species loaded and window columns injected on the device from the
+        # counter stream (profiling of the device injector; the e2e and CPU
+        # legs keep the host KISS load)
+        run = cg.Run(deck, rng_mode=abi.RNG_COUNTER, counter_seed=deck.seed)
+    else:
+        run = cg.Run(deck, particles=parts, rng=rng)
     graph = not args.eager
     tile = None
     if form == "mixed":

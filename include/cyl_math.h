@@ -18,10 +18,12 @@
  *
  * Method (table-driven argument reduction in double-double arithmetic,
  * Dekker's exact products and Knuth's two-sum): with a = |y|, b = |x|,
- * t = min(a,b)/max(a,b) in [0,1] is formed as t_hi + t_lo with the exact
- * remainder of the division; c = k/128 is the grid point nearest to t and
+ * t = min(a,b)/max(a,b) in [0,1] is formed as t_hi + t_lo from a reciprocal
+ * and the remainder of the product (an FMA); c = k/128 is the grid point nearest to t and
  * atan(t) = atan(c) + atan(u), u = (t - c)/(1 + t c), |u| <= 1/256 + ulp,
- * with u as a double-double.  atan(u) = u + u q, q = -u^2/3 (double-double)
+ * with u as a double-double (the same reciprocal-and-remainder form: the
+ * routine divides twice, by max(a,b) and by 1 + t c; the narrow FP64 pipe
+ * of the GPU makes each division cost about ten FP64 operations).  atan(u) = u + u q, q = -u^2/3 (double-double)
  * + u^4/5 - u^6/7 + u^8/9 - u^10/11 (double; the first omitted term is below
  * 2^-99 of q).  atan(k/128) is tabulated as a double-double (mpmath at 300
  * bits), and the quadrant is restored with pi/2 and pi as double-doubles.
@@ -246,14 +248,17 @@ CYLM_FN double cyl_atan2(double y, double x) {
     const int e = ilogb(den);
     num = scalbn(num, -e);
     den = scalbn(den, -e);
-    const double th = num / den;
+    /* one division: th = num (1/den) need not be the rounded quotient,
+       only the head of th + tl, whose tail comes from the remainder */
+    const double rden = 1.0 / den;
+    const double th = num * rden;
     if (th < 0x1p-1000) {
       /* atan(t) = t to far below the last bit: the ratio of the unscaled
          arguments, rounded once (also into the subnormal range) */
       ah = num0 / den0;
       al = 0.0;
     } else {
-      const double tl = cylm_fma(-th, den, num) / den;
+      const double tl = cylm_fma(-th, den, num) * rden;
       const int k = (int)(th * 128.0 + 0.5);
       const double c = (double)k * 0.0078125;
       double uh, ul;
@@ -269,17 +274,19 @@ CYLM_FN double cyl_atan2(double y, double x) {
         cylm_fast_two_sum(1.0, p, &dh, &dl);
         dl = dl + (pe + tl * c);
         cylm_fast_two_sum(dh, dl, &dh, &dl);
-        uh = nh / dh;
+        const double rdh = 1.0 / dh;
+        uh = nh * rdh;
         double rem = cylm_fma(-uh, dh, nh);
         rem = (rem + nl) - uh * dl;
-        ul = rem / dh;
+        ul = rem * rdh;
       }
       /* q = -u^2/3 + u^4/5 - u^6/7 + u^8/9 - u^10/11 */
       const double sh = uh * uh;
       const double sl = cylm_fma(uh, uh, -sh) + 2.0 * uh * ul;
-      const double qh = -sh / 3.0;
+      const double third = 1.0 / 3.0;
+      const double qh = -(sh * third);
       const double qr = cylm_fma(-3.0, qh, -sh); /* -sh = 3 qh + qr exactly */
-      const double ql = (qr - sl) / 3.0;
+      const double ql = (qr - sl) * third;
       double q1 = 1.0 / 9.0 - sh * (1.0 / 11.0);
       q1 = 1.0 / 7.0 - sh * q1;
       q1 = 1.0 / 5.0 - sh * q1;
