@@ -545,21 +545,23 @@ static void enqueue_current_finish(Handle* h, cudaStream_t s, const FieldSetT<T>
   const RunConst& rc = h->rc;
   FView wk{h->F[15], rc.nxg, rc.nyg};
   const int stride = h->gd.smooth_stride > 0 ? h->gd.smooth_stride : 1;
-  if constexpr (std::is_same<T, cplx>::value) {
-    if (h->ion_on) {
-      // push_particles ends with current_bcs_r_min_final; ionise_particles
-      // runs before current_finish (epoch2d.F90:218-252)
-      launch_current_finish(s, F, rec, rc, h->gd.smooth_currents, h->gd.smooth_its, h->gd.smooth_comp_its, stride,
-                            wk, 1);
+  if (h->ion_on) {
+    // push_particles ends with current_bcs_r_min_final; ionise_particles
+    // runs before current_finish (epoch2d.F90:218-252)
+    launch_current_finish(s, F, rec, rc, h->gd.smooth_currents, h->gd.smooth_its, h->gd.smooth_comp_its, stride,
+                          wk, 1);
+    if constexpr (std::is_same<T, cplx>::value)
       launch_ionise(s, F, h->sp, h->nsp, h->d_cnt, h->ion, rec, rc, h->d_ion, h->d_ion + MAX_SPECIES, h->d_err,
                     h->nblocks);
-      launch_current_finish(s, F, rec, rc, h->gd.smooth_currents, h->gd.smooth_its, h->gd.smooth_comp_its, stride,
-                            wk, 6);
-      int nion = 0;
-      for (int i = 0; i < h->nsp; ++i) nion += h->ion.s[i].ionise;
-      count_launch(h, 4 + nion);
-      return;
-    }
+    else
+      launch_ionise(s, F, h->sp, h->nsp, h->d_cnt, h->ion, rec, rc, h->d_ion, h->d_ion + MAX_SPECIES, h->d_err,
+                    h->nblocks, h->xg0);
+    launch_current_finish(s, F, rec, rc, h->gd.smooth_currents, h->gd.smooth_its, h->gd.smooth_comp_its, stride,
+                          wk, 6);
+    int nion = 0;
+    for (int i = 0; i < h->nsp; ++i) nion += h->ion.s[i].ionise;
+    count_launch(h, 4 + nion);
+    return;
   }
   launch_current_finish(s, F, rec, rc, h->gd.smooth_currents, h->gd.smooth_its, h->gd.smooth_comp_its, stride, wk);
   count_launch(h, 2);
@@ -2062,7 +2064,6 @@ int cyl_set_ionisation(cyl_handle hh, const cyl_ionisation_species* io, int32_t 
     h->ion_on = false;
   } else {
     if (!io || n != h->nsp) return CYL_ERR_BAD_ARG;
-    if (h->prec == CYL_PREC_MIXED) return CYL_ERR_UNSUPPORTED;
     for (int i = 0; i < n; ++i)
       if (io[i].ionise && (io[i].ionise_to < 0 || io[i].ionise_to >= n || io[i].release < -1 ||
                            io[i].release >= n || io[i].energy <= 0.0))
@@ -2565,6 +2566,7 @@ int cyl_batch_step(cyl_batch b, const cyl_handle* hs, int32_t n, int32_t nsteps)
     if (!hs[r]) return CYL_ERR_BAD_ARG;
     Handle* h = &hs[r]->h;
     if (h->prec != CYL_PREC_MIXED) return CYL_ERR_UNSUPPORTED;
+    if (h->ion_on) return CYL_ERR_UNSUPPORTED;  // the batched stages have no ionisation
     if (h->device != b->device) return CYL_ERR_BAD_ARG;
     if (M < 0) M = h->rc.M;
     if (h->rc.M != M) return CYL_ERR_UNSUPPORTED;

@@ -184,6 +184,10 @@ void ionisation_constants(const cyl_ionisation_species* io, const cyl_species_de
 void launch_ionise(cudaStream_t s, const FieldSet& F, const SpeciesPtrs* sp, int nsp, SpeciesCounters* cnt,
                    const IonParams& P, const StepRec* rec, const RunConst& rc, int64_t* snap, const int64_t* caps,
                    int* err, int nblocks);
+// The mixed form's storage (xg0: its x origin); J stays FP64 in both forms.
+void launch_ionise(cudaStream_t s, const FieldSetF& F, const SpeciesPtrs* sp, int nsp, SpeciesCounters* cnt,
+                   const IonParams& P, const StepRec* rec, const RunConst& rc, int64_t* snap, const int64_t* caps,
+                   int* err, int nblocks, double xg0);
 
 // charge.cu (continuity-residual and number-density diagnostics)
 void launch_number_density(cudaStream_t s, const SpeciesPtrs& sp, const SpeciesCounters* cnt, const RunConst& rc,

@@ -24,10 +24,12 @@
 // reference's order.
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 
 #include "counter_rng.cuh"
 #include "cyl_common.cuh"
 #include "cyl_kernels.cuh"
+#include "push_mixed.cuh"
 
 namespace cyl {
 
@@ -151,7 +153,9 @@ void ionisation_constants(const cyl_ionisation_species* io, const cyl_species_de
 
 namespace {
 
-__device__ __forceinline__ cplx gather3(const FView& f, const double* wa, const double* wb, int ca, int cb, int m) {
+template <typename T>
+__device__ __forceinline__ cplx gather3(const FViewT<T>& f, const double* wa, const double* wb, int ca, int cb,
+                                       int m) {
   cplx acc;
 #pragma unroll
   for (int jj = -1; jj <= 1; ++jj) {
@@ -174,12 +178,78 @@ __device__ __forceinline__ int64_t take_slot(SpeciesCounters* cnt, const Species
 struct IonLaunch {
   SpeciesPtrs sp[MAX_SPECIES];
   IonParams P;
+  double xg0;  // the mixed form's x origin
+};
+
+// One particle's state as the routine reads and writes it: the FP64 form's
+// arrays, or the mixed form's storage (converted to FP64 on the way in, as
+// the mixed form's download does, and back on the way out).
+template <bool MIXED>
+struct IonState;
+template <>
+struct IonState<false> {
+  __device__ static bool load(const SpeciesPtrs& S, int64_t i, double, const RunConst&, double& x, double& y,
+                              double& z) {
+    x = S.x[i];
+    if (isnan(x)) return false;
+    y = S.y[i];
+    z = S.z[i];
+    return true;
+  }
+  __device__ static void momenta(const SpeciesPtrs& S, int64_t i, double& px, double& py, double& pz, double& w) {
+    px = S.px[i];
+    py = S.py[i];
+    pz = S.pz[i];
+    w = S.w[i];
+  }
+  __device__ static void store(const SpeciesPtrs& T, SpeciesCounters*, int64_t k, double x, double y, double z,
+                               double px, double py, double pz, double w, int64_t id, double, const RunConst&) {
+    T.x[k] = x;
+    T.y[k] = y;
+    T.z[k] = z;
+    T.px[k] = px;
+    T.py[k] = py;
+    T.pz[k] = pz;
+    T.w[k] = w;
+    T.id[k] = id;
+  }
+  __device__ static void remove(const SpeciesPtrs& S, int64_t i) { S.x[i] = nan_slot(); }
+};
+template <>
+struct IonState<true> {
+  __device__ static bool load(const SpeciesPtrs& S, int64_t i, double xg0, const RunConst& rc, double& x,
+                              double& y, double& z) {
+    const int32_t k = S.kx[i];
+    if (k == INT32_MIN) return false;
+    x = xg0 + ((double)k + (double)S.fx[i]) * rc.dx;
+    y = (double)S.fy[i] * rc.dy;
+    z = (double)S.fz[i] * rc.dy;
+    return true;
+  }
+  __device__ static void momenta(const SpeciesPtrs& S, int64_t i, double& px, double& py, double& pz, double& w) {
+    const double mc = S.mass * CLIGHT;
+    px = (double)S.ux[i] * mc;
+    py = (double)S.uy[i] * mc;
+    pz = (double)S.uz[i] * mc;
+    w = (double)S.fw[i];
+  }
+  __device__ static void store(const SpeciesPtrs& T, SpeciesCounters* c, int64_t k, double x, double y, double z,
+                               double px, double py, double pz, double w, int64_t id, double xg0,
+                               const RunConst& rc) {
+    to_mixed(T, k, x, y, z, px, py, pz, w, xg0, rc);
+    T.id[k] = id;
+    atomicMax(&c->wmax_bits, __float_as_uint(fabsf(T.fw[k])));
+  }
+  __device__ static void remove(const SpeciesPtrs& S, int64_t i) { S.kx[i] = INT32_MIN; }
 };
 
 // ionise_particles over the particles species `isp` held when the routine
 // started (snap[isp]); one thread per particle.
-__global__ void __launch_bounds__(256) k_ionise(FieldSet F, IonLaunch L, SpeciesCounters* cnt, const int64_t* snap,
-                                                int isp, const StepRec* rec, RunConst rc, int* err) {
+template <bool MIXED>
+__global__ void __launch_bounds__(256) k_ionise(FieldSetT<typename std::conditional<MIXED, cplxf, cplx>::type> F,
+                                                IonLaunch L, SpeciesCounters* cnt, const int64_t* snap, int isp,
+                                                const StepRec* rec, RunConst rc, int* err) {
+  using IO = IonState<MIXED>;
   const IonParams& P = L.P;
   const SpeciesPtrs& S = L.sp[isp];
   const int64_t n = snap[isp];
@@ -190,9 +260,8 @@ __global__ void __launch_bounds__(256) k_ionise(FieldSet F, IonLaunch L, Species
   const int M = rc.M;
   const bool mp = (P.model & CYL_IONISE_MULTIPHOTON) != 0, bsi = (P.model & CYL_IONISE_BSI) != 0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double px0 = S.x[i];
-    if (isnan(px0)) continue;
-    const double py0 = S.y[i], pz0 = S.z[i];
+    double px0, py0, pz0;
+    if (!IO::load(S, i, L.xg0, rc, px0, py0, pz0)) continue;
     const double part_x_local = px0 - x_grid_min_local;
     const double part_r = sqrt(py0 * py0 + pz0 * pz0);
     const double part_r_local = part_r - y_grid_min_local;
@@ -248,8 +317,8 @@ __global__ void __launch_bounds__(256) k_ionise(FieldSet F, IonLaunch L, Species
     const double e_part_mag = fac * sqrt((ex_part * ex_part + ey_part * ey_part) + ez_part * ez_part) / ATOMIC_E;
 
     const int64_t pid = S.id[i];
-    double ppx = S.px[i], ppy = S.py[i], ppz = S.pz[i];
-    const double weight = S.w[i];
+    double ppx, ppy, ppz, weight;
+    IO::momenta(S, i, ppx, ppy, ppz, weight);
     int cs = isp;
     double time_left = rc.dt / ATOMIC_TIME;
     double j_ion = 0.0;
@@ -318,14 +387,8 @@ __global__ void __launch_bounds__(256) k_ionise(FieldSet F, IonLaunch L, Species
           }
           const int64_t k = take_slot(cnt + q.release, E);
           if (k >= 0) {
-            E.x[k] = px0;
-            E.y[k] = py0;
-            E.z[k] = pz0;
-            E.px[k] = nx_;
-            E.py[k] = ny_;
-            E.pz[k] = nz_;
-            E.w[k] = weight;
-            E.id[k] = (int64_t)(((uint64_t)1 << 62) | ((uint64_t)pid << 4) | (uint64_t)cs);
+            IO::store(E, cnt + q.release, k, px0, py0, pz0, nx_, ny_, nz_, weight,
+                      (int64_t)(((uint64_t)1 << 62) | ((uint64_t)pid << 4) | (uint64_t)cs), L.xg0, rc);
           } else {
             atomicOr(err, ERR_CAPACITY);
           }
@@ -342,18 +405,11 @@ __global__ void __launch_bounds__(256) k_ionise(FieldSet F, IonLaunch L, Species
     const SpeciesPtrs& T = L.sp[cs];
     const int64_t k = take_slot(cnt + cs, T);
     if (k >= 0) {
-      T.x[k] = px0;
-      T.y[k] = py0;
-      T.z[k] = pz0;
-      T.px[k] = ppx;
-      T.py[k] = ppy;
-      T.pz[k] = ppz;
-      T.w[k] = weight;
-      T.id[k] = pid;
+      IO::store(T, cnt + cs, k, px0, py0, pz0, ppx, ppy, ppz, weight, pid, L.xg0, rc);
     } else {
       atomicOr(err, ERR_CAPACITY);
     }
-    S.x[i] = nan_slot();
+    IO::remove(S, i);
     atomicAdd((unsigned long long*)&cnt[isp].n_dead, 1ull);
     // ionisation current (ionise.F90:608-639)
     const double den = ATOMIC_E * e_part_mag;
@@ -399,17 +455,30 @@ __global__ void k_ion_clamp(SpeciesCounters* cnt, const int64_t* caps, int nsp) 
 
 }  // namespace
 
-void launch_ionise(cudaStream_t s, const FieldSet& F, const SpeciesPtrs* sp, int nsp, SpeciesCounters* cnt,
-                   const IonParams& P, const StepRec* rec, const RunConst& rc, int64_t* snap, const int64_t* caps,
-                   int* err, int nblocks) {
+template <bool MIXED, typename FS>
+static void launch_ionise_t(cudaStream_t s, const FS& F, const SpeciesPtrs* sp, int nsp, SpeciesCounters* cnt,
+                            const IonParams& P, const StepRec* rec, const RunConst& rc, int64_t* snap,
+                            const int64_t* caps, int* err, int nblocks, double xg0) {
   IonLaunch L;
   std::memset(&L, 0, sizeof(L));
   for (int i = 0; i < nsp && i < MAX_SPECIES; ++i) L.sp[i] = sp[i];
   L.P = P;
+  L.xg0 = xg0;
   k_ion_snapshot<<<1, 32, 0, s>>>(cnt, nsp, snap);
   for (int i = 0; i < nsp; ++i)
-    if (P.s[i].ionise) k_ionise<<<nblocks, 256, 0, s>>>(F, L, cnt, snap, i, rec, rc, err);
+    if (P.s[i].ionise) k_ionise<MIXED><<<nblocks, 256, 0, s>>>(F, L, cnt, snap, i, rec, rc, err);
   k_ion_clamp<<<1, 32, 0, s>>>(cnt, caps, nsp);
+}
+
+void launch_ionise(cudaStream_t s, const FieldSet& F, const SpeciesPtrs* sp, int nsp, SpeciesCounters* cnt,
+                   const IonParams& P, const StepRec* rec, const RunConst& rc, int64_t* snap, const int64_t* caps,
+                   int* err, int nblocks) {
+  launch_ionise_t<false>(s, F, sp, nsp, cnt, P, rec, rc, snap, caps, err, nblocks, 0.0);
+}
+void launch_ionise(cudaStream_t s, const FieldSetF& F, const SpeciesPtrs* sp, int nsp, SpeciesCounters* cnt,
+                   const IonParams& P, const StepRec* rec, const RunConst& rc, int64_t* snap, const int64_t* caps,
+                   int* err, int nblocks, double xg0) {
+  launch_ionise_t<true>(s, F, sp, nsp, cnt, P, rec, rc, snap, caps, err, nblocks, xg0);
 }
 
 }  // namespace cyl

@@ -29,30 +29,7 @@ MixedParams mixed_params(const SpeciesPtrs& sp, const RunConst& rc) {
   return P;
 }
 
-__device__ __forceinline__ void to_mixed(const SpeciesPtrs& sp, int64_t d, double x, double y, double z,
-                                         double px, double py, double pz, double w, double xg0,
-                                         const RunConst& rc) {
-  if (isnan(x)) {
-    sp.kx[d] = INT32_MIN;
-    return;
-  }
-  const double xi = (x - xg0) / rc.dx;
-  double kf = floor(xi);
-  float f = (float)(xi - kf);
-  if (f >= 1.0f) {
-    f = 0.0f;
-    kf += 1.0;
-  }
-  const double imc = 1.0 / (sp.mass * CLIGHT);
-  sp.kx[d] = (int32_t)kf;
-  sp.fx[d] = f;
-  sp.fy[d] = (float)(y / rc.dy);
-  sp.fz[d] = (float)(z / rc.dy);
-  sp.ux[d] = (float)(px * imc);
-  sp.uy[d] = (float)(py * imc);
-  sp.uz[d] = (float)(pz * imc);
-  sp.fw[d] = (float)w;
-}
+
 
 __global__ void k_from_double(SpeciesPtrs sp, const double* st, int64_t n, int64_t cap, double xg0,
                               RunConst rc) {

@@ -89,6 +89,34 @@ void mixed_from_double(cudaStream_t s, const SpeciesPtrs& sp, const double* stag
                        double xg0, const RunConst& rc);
 void mixed_to_double(cudaStream_t s, const SpeciesPtrs& sp, double* stage, int64_t n, int64_t cap,
                      double xg0, const RunConst& rc);
+// One particle from FP64 state into the mixed form's storage at slot d
+// (integer cell + FP32 offset of x from xg0, y and z in units of dy,
+// normalised momenta, FP32 weight; a NaN x marks a hole).
+__device__ __forceinline__ void to_mixed(const SpeciesPtrs& sp, int64_t d, double x, double y, double z,
+                                         double px, double py, double pz, double w, double xg0,
+                                         const RunConst& rc) {
+  if (isnan(x)) {
+    sp.kx[d] = INT32_MIN;
+    return;
+  }
+  const double xi = (x - xg0) / rc.dx;
+  double kf = floor(xi);
+  float f = (float)(xi - kf);
+  if (f >= 1.0f) {
+    f = 0.0f;
+    kf += 1.0;
+  }
+  const double imc = 1.0 / (sp.mass * CLIGHT);
+  sp.kx[d] = (int32_t)kf;
+  sp.fx[d] = f;
+  sp.fy[d] = (float)(y / rc.dy);
+  sp.fz[d] = (float)(z / rc.dy);
+  sp.ux[d] = (float)(px * imc);
+  sp.uy[d] = (float)(py * imc);
+  sp.uz[d] = (float)(pz * imc);
+  sp.fw[d] = (float)w;
+}
+
 // One (run, species) of a batch in one step, for the window's particle
 // stages (append the step's injected particles, commit, particle_bcs after
 // the shift and remove_particles) of every member in one launch each.

@@ -399,7 +399,10 @@ typedef struct cyl_ionisation_species {
  * seed, where the reference draws from its serial KISS stream: same
  * distribution, a different sequence.  A released electron takes the id
  * 2^62 + 16 (parent id) + (index of the parent's species before the event).
- * FP64 form only: the mixed form returns CYL_ERR_UNSUPPORTED.  Errors:
+ * Both forms; in the mixed form the trials read the FP32 fields and the
+ * ions and electrons enter the species' unsorted tails (pushed on the
+ * global path until the next sort); a batch (cyl_batch_step) refuses runs
+ * with ionisation (CYL_ERR_UNSUPPORTED).  Errors:
  * CYL_ERR_BAD_ARG for species indices out of range or an ionising species
  * without a next state; CYL_ERR_UNSUPPORTED for multiphoton without lasers
  * or with lasers of different omega.  nspecies == 0 switches it off. */
