@@ -141,6 +141,7 @@ struct Handle {
   // graph
   cudaGraphExec_t gexec = nullptr;
   int graph_parity = -1;
+  bool graph_window = true;  // the captured chunk has the window's kernels
   // timing of the push kernel (events around each push in eager mode and in graphs)
   cudaEvent_t ev_push[CHUNK][2];
   int push_events_used = 0;
@@ -571,14 +572,16 @@ static void enqueue_current_finish(Handle* h, cudaStream_t s, const FieldSetT<T>
 // (fields.f90:341-353) and moving_window.
 template <typename T>
 static void enqueue_step_final(Handle* h, cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec,
-                               const double* src) {
+                               const double* src, bool window = true) {
   const RunConst& rc = h->rc;
   bulk_b(h, s, F, 0);
   launch_b_final_bcs(s, F, rec, src, h->cols, 1, rc.dt, rc);
   bulk_e(h, s, F);
   launch_e_axis_bcs(s, F, rec, rc);
   count_launch(h, 6);
-  if (h->move_window) {
+  // window: false when no step of the chunk shifts (the window's kernels
+  // would do nothing: no injected particles, no removals, no field shift)
+  if (h->move_window && window) {
     if (h->inj_counter) {
       launch_inject_counter(s, rec, h->d_injsp, h->nsp, rc, h->inj_seed, h->d_injrow, h->d_inj);
       count_launch(h, 1);
@@ -599,28 +602,28 @@ static void enqueue_step_final(Handle* h, cudaStream_t s, const FieldSetT<T>& F,
 // The kernels of one step after the push.
 template <typename T>
 static void enqueue_step_post(Handle* h, cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec,
-                              const double* src) {
+                              const double* src, bool window = true) {
   enqueue_current_finish<T>(h, s, F, rec);
-  enqueue_step_final<T>(h, s, F, rec, src);
+  enqueue_step_final<T>(h, s, F, rec, src, window);
 }
 
 // Enqueue the kernels of one step; rec/src point at this step's records.
 template <typename T>
 static void enqueue_step_t(Handle* h, const StepRec* rec, const double* src, int k_in_chunk, bool timing,
-                           bool capturing) {
+                           bool capturing, bool window) {
   const unsigned evflag = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
   cudaStream_t s = h->st;
   const FieldSetT<T> F = enqueue_step_pre<T>(h, s, rec);
   if (timing) cudaEventRecordWithFlags(h->ev_push[k_in_chunk][0], s, evflag);
   push_all(h, s, F, rec, 1);
   if (timing) cudaEventRecordWithFlags(h->ev_push[k_in_chunk][1], s, evflag);
-  enqueue_step_post<T>(h, s, F, rec, src);
+  enqueue_step_post<T>(h, s, F, rec, src, window);
 }
 
 static void enqueue_step(Handle* h, const StepRec* rec, const double* src, int k_in_chunk, bool timing,
-                         bool capturing) {
-  if (h->prec == CYL_PREC_MIXED) enqueue_step_t<cplxf>(h, rec, src, k_in_chunk, timing, capturing);
-  else enqueue_step_t<cplx>(h, rec, src, k_in_chunk, timing, capturing);
+                         bool capturing, bool window = true) {
+  if (h->prec == CYL_PREC_MIXED) enqueue_step_t<cplxf>(h, rec, src, k_in_chunk, timing, capturing, window);
+  else enqueue_step_t<cplx>(h, rec, src, k_in_chunk, timing, capturing, window);
 }
 
 // Counting sort of every species by cell; xgm points at the device copy of
@@ -807,9 +810,14 @@ static int run_chunk(Handle* h, int k, bool use_graph) {
   CK(cudaEventRecord(h->ev_copy, h->st));
   h->copy_pending = true;
   const StepRec* last = h->d_rec + (k - 1);
+  // whether any step of the chunk shifts the window (the host has just
+  // prepared their records): a chunk without shifts leaves out the window's
+  // kernels, which would find nothing to inject, remove or shift
+  bool window = false;
+  for (int i = 0; i < k; ++i) window = window || h->h_rec[i].nshift > 0;
   if (use_graph && k == CHUNK) {
     const int par0 = h->jpar;
-    if (!h->gexec || h->graph_parity != par0) {
+    if (!h->gexec || h->graph_parity != par0 || h->graph_window != window) {
       if (h->gexec) {
         cudaGraphExecDestroy(h->gexec);
         h->gexec = nullptr;
@@ -818,12 +826,13 @@ static int run_chunk(Handle* h, int k, bool use_graph) {
       const int64_t launches0 = h->kernel_launches;
       CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
       for (int i = 0; i < k; ++i)
-        enqueue_step(h, h->d_rec + i, h->d_src + h->src_per_step * i, i, true, true);
+        enqueue_step(h, h->d_rec + i, h->d_src + h->src_per_step * i, i, true, true, window);
       enqueue_sort(h, last);
       CK(cudaStreamEndCapture(h->st, &graph));
       CK(cudaGraphInstantiate(&h->gexec, graph, 0));
       cudaGraphDestroy(graph);
       h->graph_parity = par0;
+      h->graph_window = window;
       h->graph_launches = h->kernel_launches - launches0;
       h->kernel_launches = launches0;
       h->jpar = par0;
@@ -837,7 +846,7 @@ static int run_chunk(Handle* h, int k, bool use_graph) {
     // the thread's last error: clear it before the launches, read it after
     (void)cudaGetLastError();
     for (int i = 0; i < k; ++i)
-      enqueue_step(h, h->d_rec + i, h->d_src + h->src_per_step * i, i, true, false);
+      enqueue_step(h, h->d_rec + i, h->d_src + h->src_per_step * i, i, true, false, window);
     enqueue_sort(h, last);
     CK(cudaGetLastError());
   }
