@@ -501,19 +501,22 @@ static void bulk_b(Handle* h, cudaStream_t s, const FieldSet& F, int save_old) {
 static void bulk_b(Handle* h, cudaStream_t s, const FieldSetF& F, int save_old) {
   launch_update_b_f32(s, F, save_old, (const double*)h->rowtab, h->rc);
 }
-static void push_all(Handle* h, cudaStream_t s, const FieldSet& F, const StepRec* rec, int apply_bcs) {
+static void push_all(Handle* h, cudaStream_t s, const FieldSet& F, const StepRec* rec, int apply_bcs,
+                     int = 0) {
   for (int i = 0; i < h->nsp; ++i) {
     if (h->sp[i].immobile) continue;
     launch_push_fp64(s, F, h->geom, h->sp[i], h->d_cnt + i, rec, h->rc, apply_bcs, h->d_err, h->nblocks);
     count_launch(h, 1);
   }
 }
-static void push_all(Handle* h, cudaStream_t s, const FieldSetF& F, const StepRec* rec, int apply_bcs) {
+// count_zeroed: the step's zeroing launch already cleared the deferred counts
+static void push_all(Handle* h, cudaStream_t s, const FieldSetF& F, const StepRec* rec, int apply_bcs,
+                     int count_zeroed = 0) {
   for (int i = 0; i < h->nsp; ++i) {
     if (h->sp[i].immobile) continue;
     push_mixed_fns(h->tile_shape)
         .launch(s, F, h->sp[i], h->d_cnt + i, rec, h->rc, apply_bcs, h->nblocks_mixed, h->nblocks / 4, h->mp[i],
-                h->d_tiles + i);
+                h->d_tiles + i, count_zeroed);
     count_launch(h, 2);
   }
 }
@@ -532,10 +535,13 @@ static FieldSetT<T> enqueue_step_pre(Handle* h, cudaStream_t s, const StepRec* r
   count_launch(h, 6);
   h->jpar ^= 1;
   F = fieldset_t<T>(h, h->jpar);
-  const size_t bytes = h->fcount * sizeof(cplx);
-  cudaMemsetAsync(F.jx.p, 0, bytes, s);
-  cudaMemsetAsync(F.jr.p, 0, bytes, s);
-  cudaMemsetAsync(F.jt.p, 0, bytes, s);
+  // J = 0, and the mixed push's deferred counts, in one launch
+  ZeroCounts zc{};
+  if constexpr (std::is_same<T, cplxf>::value)
+    for (int i = 0; i < h->nsp; ++i)
+      if (!h->sp[i].immobile) zc.p[zc.n++] = h->mp[i].fb_count;
+  launch_zero_step(s, F, rc, zc);
+  count_launch(h, 1);
   return F;
 }
 
@@ -615,7 +621,7 @@ static void enqueue_step_t(Handle* h, const StepRec* rec, const double* src, int
   cudaStream_t s = h->st;
   const FieldSetT<T> F = enqueue_step_pre<T>(h, s, rec);
   if (timing) cudaEventRecordWithFlags(h->ev_push[k_in_chunk][0], s, evflag);
-  push_all(h, s, F, rec, 1);
+  push_all(h, s, F, rec, 1, 1);
   if (timing) cudaEventRecordWithFlags(h->ev_push[k_in_chunk][1], s, evflag);
   enqueue_step_post<T>(h, s, F, rec, src, window);
 }
@@ -1921,7 +1927,7 @@ template <typename T>
 static void enqueue_step_head(Handle* h, const StepRec* rec) {
   cudaStream_t s = h->st;
   const FieldSetT<T> F = enqueue_step_pre<T>(h, s, rec);
-  push_all(h, s, F, rec, 1);
+  push_all(h, s, F, rec, 1, 1);
   enqueue_current_finish<T>(h, s, F, rec);
 }
 

@@ -150,6 +150,15 @@ void launch_b_final_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* re
 template <typename T>
 void launch_current_finish(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc,
                            int smooth, int its, int comp_its, int stride, FView wk, int parts = 7);
+// The zeroing at the start of a step's push: J = 0 of the three current
+// arrays (the J swap of update_eb_fields_half) and up to MAX_SPECIES int
+// counters (the mixed push's deferred-particle counts), in one launch.
+struct ZeroCounts {
+  int* p[MAX_SPECIES];
+  int n;
+};
+template <typename T>
+void launch_zero_step(cudaStream_t s, const FieldSetT<T>& F, const RunConst& rc, const ZeroCounts& zc);
 template <typename T>
 void launch_shift_fields(cudaStream_t s, const FieldSetT<T>& F, const cplx* cols, const StepRec* rec,
                          int which, const RunConst& rc);

@@ -900,6 +900,22 @@ void launch_shift_fields(cudaStream_t s, const FieldSetT<T>& F, const cplx* cols
   else k_shift_fields<T, 0><<<grd, 256, 0, s>>>(F, cols, rec, which, rc);
 }
 
+__global__ void k_zero_step(FView jx, FView jr, FView jt, int64_t n, ZeroCounts zc) {
+  if (blockIdx.x == 0 && (int)threadIdx.x < zc.n) *zc.p[threadIdx.x] = 0;
+  const cplx z = mk(0, 0);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    jx.p[i] = z;
+    jr.p[i] = z;
+    jt.p[i] = z;
+  }
+}
+template <typename T>
+void launch_zero_step(cudaStream_t s, const FieldSetT<T>& F, const RunConst& rc, const ZeroCounts& zc) {
+  const int64_t n = (int64_t)rc.nxg * rc.nyg * rc.M;
+  const int nb = (int)std::min<int64_t>((n + 255) / 256, 1216);
+  k_zero_step<<<nb, 256, 0, s>>>(F.jx, F.jr, F.jt, n, zc);
+}
+
 // ------------------------------------- batched stages of the mixed form
 //
 // One launch per stage for every run of a batch: blockIdx.y (blockIdx.z for
@@ -1059,7 +1075,8 @@ void batch_shift_fields(cudaStream_t s, const StageJob* jobs, int njobs, int whi
   template void launch_current_finish<T>(cudaStream_t, const FieldSetT<T>&, const StepRec*, const RunConst&, \
                                          int, int, int, int, FView, int);                                  \
   template void launch_shift_fields<T>(cudaStream_t, const FieldSetT<T>&, const cplx*, const StepRec*, int,  \
-                                       const RunConst&);
+                                       const RunConst&);                                                  \
+  template void launch_zero_step<T>(cudaStream_t, const FieldSetT<T>&, const RunConst&, const ZeroCounts&);
 INST(cplx)
 INST(cplxf)
 #undef INST

@@ -1121,12 +1121,12 @@ int push_mixed_blocks_per_sm(int M) {
 
 void launch_push_mixed(cudaStream_t s, const FieldSetF& F, const SpeciesPtrs& sp, SpeciesCounters* cnt,
                        const StepRec* rec, const RunConst& rc, int apply_bcs, int nblocks_tiles,
-                       int nblocks_global, const MixedParams& P, TileTable* tt) {
+                       int nblocks_global, const MixedParams& P, TileTable* tt, int count_zeroed) {
   const size_t smem = push_mixed_smem(rc.M);
   TmaSet tma;
   std::memset(&tma, 0, sizeof(tma));
   const int use_tma = make_tma_set(F, rc, &tma) ? 1 : 0;
-  cudaMemsetAsync(P.fb_count, 0, sizeof(int), s);
+  if (!count_zeroed) cudaMemsetAsync(P.fb_count, 0, sizeof(int), s);
   switch (rc.M) {
 #define CASE(MM)                                                                                    \
   case MM:                                                                                          \

@@ -70,9 +70,10 @@ struct BatchJob {
 struct PushMixedFns {
   size_t (*smem)(int M);
   int (*blocks_per_sm)(int M);
+  // (count_zeroed: the deferred-particle count P.fb_count is already 0)
   void (*launch)(cudaStream_t s, const FieldSetF& F, const SpeciesPtrs& sp, SpeciesCounters* cnt,
                  const StepRec* rec, const RunConst& rc, int apply_bcs, int nblocks_tiles, int nblocks_global,
-                 const MixedParams& P, TileTable* tt);
+                 const MixedParams& P, TileTable* tt, int count_zeroed);
   // the batched push: jobs[0, njobs) of one step, work = (job, tile) items
   void (*launch_batch)(cudaStream_t s, int M, const BatchJob* jobs, int njobs, const int2* work, const int* nwork,
                        int nblocks_tiles, int nblocks_global);
