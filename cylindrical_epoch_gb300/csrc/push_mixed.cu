@@ -129,6 +129,7 @@ struct Tile {
   int xs;           // Fortran x index of the TMA boxes' first column
   int x0, y0;       // Fortran indices of the staged region's first cell
   float s_xr, s_t;  // accumulator units per unit of jx / jr and of jtheta flux
+  int* dirty;       // set by every warp that deposits into the accumulators
 };
 
 // Fixed-point scales of a tile's current accumulators.  One particle of
@@ -747,8 +748,10 @@ __device__ __forceinline__ bool push_one(int64_t i, const SpeciesPtrs& sp, Speci
   const f2 e05 = fm(ct, st);
   const f2 edt = fm(c3, s3) * fm(ct, -st);
   const float dth = atan2f(z3, y3) - atan2f(z, y);
-  if (SHARED)
+  if (SHARED) {
+    *tile.dirty = 1;
     deposit_tile_warp<M>(tile, og, oh, dgx, dgy, dcx, dcy, cx2, cy2, fc, fcz, e05, edt, dth);
+  }
   else
     deposit_global<M>(F, P, og, oh, dgx, dgy, dcx, dcy, cx2, cy2, fc, fcz, e05, edt, dth);
   return true;
@@ -830,7 +833,7 @@ __device__ __forceinline__ bool process_tile(const FieldSetF& F, const SpeciesPt
                                              const RunConst& rc, const MixedParams& P, const TileTable* tt, int t,
                                              int nsh, int apply_bcs, const TmaSet* tma, int use_tma,
                                              const TileSmem<M>& sm, uint64_t* tma_bar, int* tma_failed,
-                                             unsigned* s_bound, unsigned& tma_phase) {
+                                             unsigned* s_bound, int* s_dirty, unsigned& tma_phase) {
   float2* const tm = sm.tm;
   float2* const sf = sm.sf;
   int* const sj = sm.sj;
@@ -840,6 +843,7 @@ __device__ __forceinline__ bool process_tile(const FieldSetF& F, const SpeciesPt
     tile.sf = sf;
     tile.tm = tm;
     tile.sj = sj;
+    tile.dirty = s_dirty;
     tile.x0 = (tt->tx_min + t % ntx) * TILE_X - nsh + 1 - DRIFT - 2;
     tile.y0 = (t / ntx) * TILE_Y + 1 - DRIFT - 2;
     tile.xs = tile.x0 - (((tile.x0 % 2) + 2) % 2);  // rounded down to even
@@ -909,7 +913,6 @@ __device__ __forceinline__ bool process_tile(const FieldSetF& F, const SpeciesPt
       }
       tma_phase ^= 1u;
     }
-    for (int e = threadIdx.x; e < 3 * M * 4 * RCELLS; e += PUSH_THREADS) sj[e] = 0;
     if (M > 1) {
       // E_m of modes m >= 1 (TMA planes of Ex, Er, Et: q = 0, 1, 2)
       for (int e = threadIdx.x; e < 3 * (M - 1) * TW * RH; e += PUSH_THREADS) {
@@ -940,16 +943,23 @@ __device__ __forceinline__ bool process_tile(const FieldSetF& F, const SpeciesPt
     __syncthreads();
     // every thread read the bound before the barrier: clear it for the next tile
     if (threadIdx.x < 6) s_bound[threadIdx.x] = 0u;
+    // accumulators that no warp wrote are still zero: no flush
+    const bool dirty = *s_dirty != 0;
     // flush: one FP64 add per non-zero accumulator, with the geometric
     // factor of the row and the inverse fixed-point scale
     const float inv_xr = tile.s_xr > 0.f ? 1.0f / tile.s_xr : 0.f;
     const float inv_t = tile.s_t > 0.f ? 1.0f / tile.s_t : 0.f;
-    for (int e = threadIdx.x; e < 3 * M * RCELLS; e += PUSH_THREADS) {
+    for (int e = threadIdx.x; dirty && e < 3 * M * RCELLS; e += PUSH_THREADS) {
       const int cell = e % RCELLS, cm = e / RCELLS;
       const int comp = cm / M, m = cm % M;
-      const int* a = sj + cm * 4 * RCELLS + cell;
+      int* a = sj + cm * 4 * RCELLS + cell;
       const int rh = a[0], rl = a[RCELLS], ih = a[2 * RCELLS], il = a[3 * RCELLS];
       if ((rh | rl | ih | il) == 0) continue;
+      // left at zero for the next tile
+      a[0] = 0;
+      a[RCELLS] = 0;
+      a[2 * RCELLS] = 0;
+      a[3 * RCELLS] = 0;
       const float vr = fmaf((float)rh, 32768.0f, (float)rl), vi = fmaf((float)ih, 32768.0f, (float)il);
       const int cx = tile.x0 + cell % RW, cy = tile.y0 + cell / RW;
       float f;
@@ -960,7 +970,16 @@ __device__ __forceinline__ bool process_tile(const FieldSetF& F, const SpeciesPt
       gadd_f(dst, vr * f, vi * f);
     }
     __syncthreads();
+    if (threadIdx.x == 0) *s_dirty = 0;  // read by every thread before the barrier above
   return true;
+}
+
+// Accumulators at zero and the dirty flag clear, before a CTA's first tile
+// (each tile's flush leaves them so for the next).
+template <int M>
+__device__ __forceinline__ void tile_acc_init(const TileSmem<M>& sm, int* s_dirty) {
+  for (int e = threadIdx.x; e < 3 * M * 4 * RCELLS; e += PUSH_THREADS) sm.sj[e] = 0;
+  if (threadIdx.x == 0) *s_dirty = 0;
 }
 
 template <int M>
@@ -971,12 +990,14 @@ __global__ void __launch_bounds__(PUSH_THREADS, push_min_blocks<M>()) k_push_til
   __shared__ uint64_t tma_bar;
   __shared__ int tma_failed;
   __shared__ unsigned s_bound[6];
+  __shared__ int s_dirty;
   const TileSmem<M> sm(smem4);
   if (threadIdx.x == 0) {
     tma_failed = 0;
     if (use_tma) mbar_init(&tma_bar);
   }
   if (threadIdx.x < 6) s_bound[threadIdx.x] = 0u;
+  tile_acc_init<M>(sm, &s_dirty);
   __syncthreads();
   unsigned tma_phase = 0;
   const int nsh = rec->nshift_total;
@@ -986,7 +1007,7 @@ __global__ void __launch_bounds__(PUSH_THREADS, push_min_blocks<M>()) k_push_til
   // (longest first)
   for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x) {
     if (!process_tile<M>(F, sp, cnt, rc, P, tt, tt->order[ti], nsh, apply_bcs, &tma, use_tma, sm, &tma_bar,
-                         &tma_failed, s_bound, tma_phase))
+                         &tma_failed, s_bound, &s_dirty, tma_phase))
       return;
   }
 }
@@ -1003,10 +1024,12 @@ __global__ void __launch_bounds__(PUSH_THREADS, push_min_blocks<M>()) k_push_til
   extern __shared__ float4 smem4[];
   __shared__ int tma_failed;
   __shared__ unsigned s_bound[6];
+  __shared__ int s_dirty;
+  const TileSmem<M> sm(smem4);
   if (threadIdx.x == 0) tma_failed = 0;
   if (threadIdx.x < 6) s_bound[threadIdx.x] = 0u;
+  tile_acc_init<M>(sm, &s_dirty);
   __syncthreads();
-  const TileSmem<M> sm(smem4);
   unsigned tma_phase = 0;
   const int n = *nwork;
   for (int w = blockIdx.x; w < n; w += gridDim.x) {
@@ -1015,7 +1038,7 @@ __global__ void __launch_bounds__(PUSH_THREADS, push_min_blocks<M>()) k_push_til
     MixedParams P = J.P;
     set_bounds(P, J.rec, J.rc);
     process_tile<M>(J.F, J.sp, J.cnt, J.rc, P, J.tt, jt.y, J.rec->nshift_total, J.apply_bcs, nullptr, 0, sm,
-                    nullptr, &tma_failed, s_bound, tma_phase);
+                    nullptr, &tma_failed, s_bound, &s_dirty, tma_phase);
   }
 }
 
