@@ -1,4 +1,4 @@
-// ionise.cu -- field ionisation of the FP64 form (physics_packages/ionise.F90):
+// ionise.cu -- field ionisation (physics_packages/ionise.F90), for both forms:
 // the constants of initialise_ionisation (:51-286) on the host, and
 // ionise_particles (:325-351) with its four rate models (multiphoton /
 // tunnelling / barrier suppression, :355-1500) as one kernel.
@@ -21,7 +21,10 @@
 // order of slots differs from the reference's lists, ids do not.
 //
 // Compiled with --fmad=false: every FP64 operation rounds once, in the
-// reference's order.
+// reference's order.  The mixed form runs the same kernel over its own
+// storage (IonState<true>): particles converted to FP64 as its download does,
+// fields gathered from its FP32 arrays, ions and electrons written back
+// through its upload's conversion into the species' unsorted tails.
 #include <cmath>
 #include <cstring>
 #include <type_traits>
