@@ -797,6 +797,40 @@ static int flush_push_timing(Handle* h) {
   return CYL_OK;
 }
 
+// Capture the CHUNK steps of a chunk that starts at the current J parity
+// (with or without the window's kernels) and the sort after them into a
+// graph, and instantiate it.  Nothing runs: the host state that enqueueing
+// moves (J parity, the launch count) is put back.  The graph reads the
+// chunk's step records and laser sources from the staging buffers when it
+// is launched.  The stream may still hold earlier work: the capture does
+// not depend on it, and the graph's launch is ordered after it.
+static int capture_chunk_graph(Handle* h, bool window) {
+  if (h->gexec) {
+    cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+  }
+  const int par0 = h->jpar;
+  const int64_t launches0 = h->kernel_launches;
+  cudaGraph_t graph;
+  CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+  for (int i = 0; i < CHUNK; ++i)
+    enqueue_step(h, h->d_rec + i, h->d_src + h->src_per_step * i, i, true, true, window);
+  enqueue_sort(h, h->d_rec + (CHUNK - 1));
+  h->graph_launches = h->kernel_launches - launches0;
+  h->kernel_launches = launches0;
+  h->jpar = par0;
+  CK(cudaStreamEndCapture(h->st, &graph));
+  const cudaError_t e = cudaGraphInstantiate(&h->gexec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    h->gexec = nullptr;
+    return CYL_ERR_CUDA;
+  }
+  h->graph_parity = par0;
+  h->graph_window = window;
+  return CYL_OK;
+}
+
 static int run_chunk(Handle* h, int k, bool use_graph) {
   // staging buffers are reused: wait until the previous chunk's copies are done
   if (h->copy_pending) WAIT(wait_event(h, h->ev_copy));
@@ -821,31 +855,11 @@ static int run_chunk(Handle* h, int k, bool use_graph) {
   // kernels, which would find nothing to inject, remove or shift
   bool window = false;
   for (int i = 0; i < k; ++i) window = window || h->h_rec[i].nshift > 0;
-  if (use_graph && k == CHUNK) {
-    const int par0 = h->jpar;
-    if (!h->gexec || h->graph_parity != par0 || h->graph_window != window) {
-      if (h->gexec) {
-        cudaGraphExecDestroy(h->gexec);
-        h->gexec = nullptr;
-      }
-      cudaGraph_t graph;
-      const int64_t launches0 = h->kernel_launches;
-      CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
-      for (int i = 0; i < k; ++i)
-        enqueue_step(h, h->d_rec + i, h->d_src + h->src_per_step * i, i, true, true, window);
-      enqueue_sort(h, last);
-      CK(cudaStreamEndCapture(h->st, &graph));
-      CK(cudaGraphInstantiate(&h->gexec, graph, 0));
-      cudaGraphDestroy(graph);
-      h->graph_parity = par0;
-      h->graph_window = window;
-      h->graph_launches = h->kernel_launches - launches0;
-      h->kernel_launches = launches0;
-      h->jpar = par0;
-    }
+  const bool have_graph = h->gexec && h->graph_parity == h->jpar && h->graph_window == window;
+  if (use_graph && k == CHUNK && have_graph) {
     CK(cudaGraphLaunch(h->gexec, h->st));
     h->kernel_launches += h->graph_launches;
-    // a chunk swaps J and J_old an even number of times
+    // a chunk swaps J and J_old CHUNK times
     h->jpar = h->graph_parity ^ (CHUNK & 1);
   } else {
     // a launch that cannot start (a bad configuration) reports only through
@@ -855,6 +869,14 @@ static int run_chunk(Handle* h, int k, bool use_graph) {
       enqueue_step(h, h->d_rec + i, h->d_src + h->src_per_step * i, i, true, false, window);
     enqueue_sort(h, last);
     CK(cudaGetLastError());
+    // No graph of this chunk's kind (J parity, window kernels) yet: the chunk
+    // ran from single launches, and the graph of the next chunk of the same
+    // kind is captured and instantiated now, while the device works through
+    // this one.  Built before the launch instead, the capture and the
+    // instantiation (about a millisecond of host time) would leave the
+    // stream idle.
+    if (use_graph && k == CHUNK)
+      if (int r = capture_chunk_graph(h, window)) return r;
   }
   h->timing_pending = k;
   return CYL_OK;
