@@ -33,9 +33,10 @@ MixedParams mixed_params(const SpeciesPtrs& sp, const RunConst& rc) {
 
 __global__ void k_from_double(SpeciesPtrs sp, const double* st, int64_t n, int64_t cap, double xg0,
                               RunConst rc) {
+  const MixedScale k = mixed_scale(sp, rc);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     to_mixed(sp, i, st[i], st[cap + i], st[2 * cap + i], st[3 * cap + i], st[4 * cap + i], st[5 * cap + i],
-             st[6 * cap + i], xg0, rc);
+             st[6 * cap + i], xg0, k);
     sp.id[i] = __double_as_longlong(st[7 * cap + i]);
   }
 }

@@ -90,32 +90,47 @@ void mixed_from_double(cudaStream_t s, const SpeciesPtrs& sp, const double* stag
                        double xg0, const RunConst& rc);
 void mixed_to_double(cudaStream_t s, const SpeciesPtrs& sp, double* stage, int64_t n, int64_t cap,
                      double xg0, const RunConst& rc);
+// Reciprocals of the mixed form's units (the cell sizes, m c of the
+// species), computed once by a thread and used by all its conversions.
+struct MixedScale {
+  double idx, idy, imc;
+};
+__device__ __forceinline__ MixedScale mixed_scale(const SpeciesPtrs& sp, const RunConst& rc) {
+  return MixedScale{1.0 / rc.dx, 1.0 / rc.dy, 1.0 / (sp.mass * CLIGHT)};
+}
+
 // One particle from FP64 state into the mixed form's storage at slot d
 // (integer cell + FP32 offset of x from xg0, y and z in units of dy,
-// normalised momenta, FP32 weight; a NaN x marks a hole).
+// normalised momenta, FP32 weight; a NaN x marks a hole).  Products with
+// the reciprocals instead of divisions: the FP64 pipe is narrow, and every
+// result but the cell index is rounded to FP32 at once.
 __device__ __forceinline__ void to_mixed(const SpeciesPtrs& sp, int64_t d, double x, double y, double z,
                                          double px, double py, double pz, double w, double xg0,
-                                         const RunConst& rc) {
+                                         const MixedScale& k) {
   if (isnan(x)) {
     sp.kx[d] = INT32_MIN;
     return;
   }
-  const double xi = (x - xg0) / rc.dx;
+  const double xi = (x - xg0) * k.idx;
   double kf = floor(xi);
   float f = (float)(xi - kf);
   if (f >= 1.0f) {
     f = 0.0f;
     kf += 1.0;
   }
-  const double imc = 1.0 / (sp.mass * CLIGHT);
   sp.kx[d] = (int32_t)kf;
   sp.fx[d] = f;
-  sp.fy[d] = (float)(y / rc.dy);
-  sp.fz[d] = (float)(z / rc.dy);
-  sp.ux[d] = (float)(px * imc);
-  sp.uy[d] = (float)(py * imc);
-  sp.uz[d] = (float)(pz * imc);
+  sp.fy[d] = (float)(y * k.idy);
+  sp.fz[d] = (float)(z * k.idy);
+  sp.ux[d] = (float)(px * k.imc);
+  sp.uy[d] = (float)(py * k.imc);
+  sp.uz[d] = (float)(pz * k.imc);
   sp.fw[d] = (float)w;
+}
+__device__ __forceinline__ void to_mixed(const SpeciesPtrs& sp, int64_t d, double x, double y, double z,
+                                         double px, double py, double pz, double w, double xg0,
+                                         const RunConst& rc) {
+  to_mixed(sp, d, x, y, z, px, py, pz, w, xg0, mixed_scale(sp, rc));
 }
 
 // One (run, species) of a batch in one step, for the window's particle
