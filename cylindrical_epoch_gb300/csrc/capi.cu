@@ -142,6 +142,7 @@ struct Handle {
   cudaGraphExec_t gexec = nullptr;
   int graph_parity = -1;
   bool graph_window = true;  // the captured chunk has the window's kernels
+  bool merge_e = true;       // mixed form: merged E half-steps inside a chunk (cyl_set_merge_e_halves)
   // timing of the push kernel (events around each push in eager mode and in graphs)
   cudaEvent_t ev_push[CHUNK][2];
   int push_events_used = 0;
@@ -495,6 +496,17 @@ static void bulk_e(Handle* h, cudaStream_t s, const FieldSet& F) { launch_update
 static void bulk_e(Handle* h, cudaStream_t s, const FieldSetF& F) {
   launch_update_e_f32(s, F, (const double*)h->rowtab, h->rc);
 }
+// The E half-steps at a step boundary inside a chunk (mixed form): `half`
+// 1 is the closing half of a step (its edge cells alone), 2 the opening half
+// of the next (see launch_update_e_f32_edge / _fused), 0 a plain half-step.
+template <typename T>
+static void bulk_e_half(Handle* h, cudaStream_t s, const FieldSetT<T>& F, int half) {
+  if constexpr (std::is_same<T, cplxf>::value) {
+    if (half == 1) return launch_update_e_f32_edge(s, F, (const double*)h->rowtab, h->rc);
+    if (half == 2) return launch_update_e_f32_fused(s, F, (const double*)h->rowtab, h->rc);
+  }
+  bulk_e(h, s, F);
+}
 static void bulk_b(Handle* h, cudaStream_t s, const FieldSet& F, int save_old) {
   launch_update_b(s, F, save_old, h->rc);
 }
@@ -525,10 +537,10 @@ static void push_all(Handle* h, cudaStream_t s, const FieldSetF& F, const StepRe
 // (fields.f90:316-337), then J_old = J, J = 0 (particles.F90:163-169) by
 // buffer swap.  Returns the field set of the push.
 template <typename T>
-static FieldSetT<T> enqueue_step_pre(Handle* h, cudaStream_t s, const StepRec* rec) {
+static FieldSetT<T> enqueue_step_pre(Handle* h, cudaStream_t s, const StepRec* rec, bool fused_in = false) {
   const RunConst& rc = h->rc;
   FieldSetT<T> F = fieldset_t<T>(h, h->jpar);
-  bulk_e(h, s, F);
+  bulk_e_half<T>(h, s, F, fused_in ? 2 : 0);
   launch_e_axis_bcs(s, F, rec, rc);
   bulk_b(h, s, F, 1);
   launch_b_axis_bcs(s, F, rec, rc);
@@ -578,11 +590,11 @@ static void enqueue_current_finish(Handle* h, cudaStream_t s, const FieldSetT<T>
 // (fields.f90:341-353) and moving_window.
 template <typename T>
 static void enqueue_step_final(Handle* h, cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec,
-                               const double* src, bool window = true) {
+                               const double* src, bool window = true, bool fused_out = false) {
   const RunConst& rc = h->rc;
   bulk_b(h, s, F, 0);
   launch_b_final_bcs(s, F, rec, src, h->cols, 1, rc.dt, rc);
-  bulk_e(h, s, F);
+  bulk_e_half<T>(h, s, F, fused_out ? 1 : 0);
   launch_e_axis_bcs(s, F, rec, rc);
   count_launch(h, 6);
   // window: false when no step of the chunk shifts (the window's kernels
@@ -608,28 +620,39 @@ static void enqueue_step_final(Handle* h, cudaStream_t s, const FieldSetT<T>& F,
 // The kernels of one step after the push.
 template <typename T>
 static void enqueue_step_post(Handle* h, cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec,
-                              const double* src, bool window = true) {
+                              const double* src, bool window = true, bool fused_out = false) {
   enqueue_current_finish<T>(h, s, F, rec);
-  enqueue_step_final<T>(h, s, F, rec, src, window);
+  enqueue_step_final<T>(h, s, F, rec, src, window, fused_out);
 }
 
 // Enqueue the kernels of one step; rec/src point at this step's records.
+// fused_in: the step before left its closing E half-step to this step's
+// opening one (bulk_e_half); fused_out: this step leaves it to the next.
 template <typename T>
 static void enqueue_step_t(Handle* h, const StepRec* rec, const double* src, int k_in_chunk, bool timing,
-                           bool capturing, bool window) {
+                           bool capturing, bool window, bool fused_in, bool fused_out) {
   const unsigned evflag = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
   cudaStream_t s = h->st;
-  const FieldSetT<T> F = enqueue_step_pre<T>(h, s, rec);
+  const FieldSetT<T> F = enqueue_step_pre<T>(h, s, rec, fused_in);
   if (timing) cudaEventRecordWithFlags(h->ev_push[k_in_chunk][0], s, evflag);
   push_all(h, s, F, rec, 1, 1);
   if (timing) cudaEventRecordWithFlags(h->ev_push[k_in_chunk][1], s, evflag);
-  enqueue_step_post<T>(h, s, F, rec, src, window);
+  enqueue_step_post<T>(h, s, F, rec, src, window, fused_out);
 }
 
-static void enqueue_step(Handle* h, const StepRec* rec, const double* src, int k_in_chunk, bool timing,
-                         bool capturing, bool window = true) {
-  if (h->prec == CYL_PREC_MIXED) enqueue_step_t<cplxf>(h, rec, src, k_in_chunk, timing, capturing, window);
-  else enqueue_step_t<cplx>(h, rec, src, k_in_chunk, timing, capturing, window);
+// Step i of a chunk of k steps.  In the mixed form, a chunk whose steps do
+// not shift the window (no field shift between a step's closing E half-step
+// and the next step's opening one) merges those two half-steps at each step
+// boundary inside the chunk; the chunk's last step ends with a whole E
+// half-step, so the state between chunks is the plain one.
+static void enqueue_chunk_step(Handle* h, int i, int k, bool timing, bool capturing, bool window) {
+  const StepRec* rec = h->d_rec + i;
+  const double* src = h->d_src + h->src_per_step * i;
+  const bool fuse = h->prec == CYL_PREC_MIXED && h->merge_e && !window;
+  if (h->prec == CYL_PREC_MIXED)
+    enqueue_step_t<cplxf>(h, rec, src, i, timing, capturing, window, fuse && i > 0, fuse && i < k - 1);
+  else
+    enqueue_step_t<cplx>(h, rec, src, i, timing, capturing, window, false, false);
 }
 
 // Counting sort of every species by cell; xgm points at the device copy of
@@ -813,8 +836,7 @@ static int capture_chunk_graph(Handle* h, bool window) {
   const int64_t launches0 = h->kernel_launches;
   cudaGraph_t graph;
   CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
-  for (int i = 0; i < CHUNK; ++i)
-    enqueue_step(h, h->d_rec + i, h->d_src + h->src_per_step * i, i, true, true, window);
+  for (int i = 0; i < CHUNK; ++i) enqueue_chunk_step(h, i, CHUNK, true, true, window);
   enqueue_sort(h, h->d_rec + (CHUNK - 1));
   h->graph_launches = h->kernel_launches - launches0;
   h->kernel_launches = launches0;
@@ -865,8 +887,7 @@ static int run_chunk(Handle* h, int k, bool use_graph) {
     // a launch that cannot start (a bad configuration) reports only through
     // the thread's last error: clear it before the launches, read it after
     (void)cudaGetLastError();
-    for (int i = 0; i < k; ++i)
-      enqueue_step(h, h->d_rec + i, h->d_src + h->src_per_step * i, i, true, false, window);
+    for (int i = 0; i < k; ++i) enqueue_chunk_step(h, i, k, true, false, window);
     enqueue_sort(h, last);
     CK(cudaGetLastError());
     // No graph of this chunk's kind (J parity, window kernels) yet: the chunk
@@ -2127,6 +2148,19 @@ int cyl_set_ionisation(cyl_handle hh, const cyl_ionisation_species* io, int32_t 
     h->ion = P;
     h->ion_on = true;
   }
+  // the step's kernels change: a captured step graph is rebuilt
+  if (h->gexec) {
+    cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+  }
+  h->topo_epoch++;
+  return CYL_OK;
+}
+
+int cyl_set_merge_e_halves(cyl_handle hh, int32_t on) {
+  if (!hh) return CYL_ERR_BAD_ARG;
+  Handle* h = &hh->h;
+  h->merge_e = on != 0;
   // the step's kernels change: a captured step graph is rebuilt
   if (h->gexec) {
     cudaGraphExecDestroy(h->gexec);

@@ -165,6 +165,12 @@ void launch_shift_fields(cudaStream_t s, const FieldSetT<T>& F, const cplx* cols
 
 // fields_fp32.cu (bulk Yee updates of the mixed form, FP32 storage)
 void launch_update_e_f32(cudaStream_t s, const FieldSetF& F, const double* rowtab, const RunConst& rc);
+// Two consecutive E half-steps (the closing half of a step, then the E
+// boundary rules, then the opening half of the next step): the edge cells'
+// first half, and after the rules the edge cells' second half with both
+// halves of every other cell (fields_fp32.cu).
+void launch_update_e_f32_edge(cudaStream_t s, const FieldSetF& F, const double* rowtab, const RunConst& rc);
+void launch_update_e_f32_fused(cudaStream_t s, const FieldSetF& F, const double* rowtab, const RunConst& rc);
 void launch_update_b_f32(cudaStream_t s, const FieldSetF& F, int save_old, const double* rowtab,
                          const RunConst& rc);
 

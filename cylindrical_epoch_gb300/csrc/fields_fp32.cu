@@ -24,9 +24,27 @@ __device__ __forceinline__ float2 ldj(const cplx* p) {
 }
 
 // One cell and mode of update_e_field's bulk: (ix, ir) for ix = 0..nx,
-// ir = 1..ny.
+// ir = 1..ny.  reps = 2 applies two consecutive half-step updates at once
+// (the closing half of one step and the opening half of the next, which see
+// the same B and J): the increment is formed once and added twice, with the
+// FP32 roundings of two separate updates.  The increments are written with
+// explicit roundings, so that one add and two adds of the same increment
+// give the results of one and of two separate launches bit for bit.
+__device__ __forceinline__ double dinc2(double s0, double c1, double v1, double c2, double v2) {
+  return __fma_rn(c2, v2, __fma_rn(c1, v1, s0));
+}
+__device__ __forceinline__ double dinc3(double s0, double c1, double v1, double c2, double v2, double c3,
+                                        double v3) {
+  return __fma_rn(c3, v3, dinc2(s0, c1, v1, c2, v2));
+}
+__device__ __forceinline__ float inc2(float s0, float c1, float v1, float c2, float v2) {
+  return __fmaf_rn(c2, v2, __fmaf_rn(c1, v1, s0));
+}
+__device__ __forceinline__ float inc3(float s0, float c1, float v1, float c2, float v2, float c3, float v3) {
+  return __fmaf_rn(c3, v3, inc2(s0, c1, v1, c2, v2));
+}
 __device__ __forceinline__ void update_e_item(const FieldSetF& F, const float4* rowtab, float cdx, float cdy,
-                                              float cj, const Row1E& r1, int ix, int im, int ir) {
+                                              float cj, const Row1E& r1, int ix, int im, int ir, int reps = 1) {
   if (ir == 1) {
     // first radial cell in FP64 arithmetic (the equations of update_e_field)
     const double m = (double)im;
@@ -37,14 +55,18 @@ __device__ __forceinline__ void update_e_item(const FieldSetF& F, const float4* 
     const double bmm = r1.bm * m, erm = r1.erm * m;
     cplx ex = F.ex(ix, ir, im), er = F.er(ix, ir, im), et = F.et(ix, ir, im);
     // ex += a (bt1 + bt0) + i m bm br0 + c (bt1 - bt0) - d jx
-    ex.re += r1.a * (bt1.re + bt0.re) - bmm * br0.im + r1.c * (bt1.re - bt0.re) - r1.d * jx.re;
-    ex.im += r1.a * (bt1.im + bt0.im) + bmm * br0.re + r1.c * (bt1.im - bt0.im) - r1.d * jx.im;
+    ex.re = __dadd_rn(ex.re, dinc3(__dmul_rn(r1.a, __dadd_rn(bt1.re, bt0.re)), -bmm, br0.im, r1.c,
+                                   __dsub_rn(bt1.re, bt0.re), -r1.d, jx.re));
+    ex.im = __dadd_rn(ex.im, dinc3(__dmul_rn(r1.a, __dadd_rn(bt1.im, bt0.im)), bmm, br0.re, r1.c,
+                                   __dsub_rn(bt1.im, bt0.im), -r1.d, jx.im));
     // er += -i m erm bx0 - cx (btx - bt0) - d jr
-    er.re += erm * bx0.im - r1.cx * (btx.re - bt0.re) - r1.d * jr.re;
-    er.im += -erm * bx0.re - r1.cx * (btx.im - bt0.im) - r1.d * jr.im;
+    er.re = __dadd_rn(er.re, dinc2(__dmul_rn(erm, bx0.im), -r1.cx, __dsub_rn(btx.re, bt0.re), -r1.d, jr.re));
+    er.im = __dadd_rn(er.im, dinc2(__dmul_rn(-erm, bx0.re), -r1.cx, __dsub_rn(btx.im, bt0.im), -r1.d, jr.im));
     // et += cx (brx - br0) - c (bx1 - bx0) - d jt
-    et.re += r1.cx * (brx.re - br0.re) - r1.c * (bx1.re - bx0.re) - r1.d * jt.re;
-    et.im += r1.cx * (brx.im - br0.im) - r1.c * (bx1.im - bx0.im) - r1.d * jt.im;
+    et.re = __dadd_rn(et.re, dinc2(__dmul_rn(r1.cx, __dsub_rn(brx.re, br0.re)), -r1.c, __dsub_rn(bx1.re, bx0.re),
+                                   -r1.d, jt.re));
+    et.im = __dadd_rn(et.im, dinc2(__dmul_rn(r1.cx, __dsub_rn(brx.im, br0.im)), -r1.c, __dsub_rn(bx1.im, bx0.im),
+                                   -r1.d, jt.im));
     F.ex(ix, ir, im) = ex;
     F.er(ix, ir, im) = er;
     F.et(ix, ir, im) = et;
@@ -56,22 +78,27 @@ __device__ __forceinline__ void update_e_item(const FieldSetF& F, const float4* 
   const float2 br0 = ld2(F.br.ptr(ix, ir, im)), brx = ld2(F.br.ptr(ix + 1, ir, im));
   const float2 bx0 = ld2(F.bx.ptr(ix, ir, im)), bx1 = ld2(F.bx.ptr(ix, ir + 1, im));
   const float2 jx = ldj(F.jx.ptr(ix, ir, im)), jr = ldj(F.jr.ptr(ix, ir, im)), jt = ldj(F.jt.ptr(ix, ir, im));
+  const float ah = __fmul_rn(rt.x, 0.5f), am = __fmul_rn(rt.x, m), b = __fmul_rn(rt.y, m);
   // ex += c^2/r_p*dt/2 * (0.5 (bt1 + bt0) + i m br0) + c^2 dt/(2 dy) (bt1 - bt0) - dt/(2 eps0) jx
-  float2 e = ld2(F.ex.ptr(ix, ir, im));
-  const float a = rt.x, am = rt.x * m, b = rt.y * m;
-  e.x += a * 0.5f * (bt1.x + bt0.x) - am * br0.y + cdy * (bt1.x - bt0.x) - cj * jx.x;
-  e.y += a * 0.5f * (bt1.y + bt0.y) + am * br0.x + cdy * (bt1.y - bt0.y) - cj * jx.y;
-  st2(F.ex.ptr(ix, ir, im), e);
+  const float2 dex = make_float2(
+      inc3(__fmul_rn(ah, __fadd_rn(bt1.x, bt0.x)), -am, br0.y, cdy, __fsub_rn(bt1.x, bt0.x), -cj, jx.x),
+      inc3(__fmul_rn(ah, __fadd_rn(bt1.y, bt0.y)), am, br0.x, cdy, __fsub_rn(bt1.y, bt0.y), -cj, jx.y));
   // er += -i m c^2/r_d dt/2 bx0 - c^2 dt/(2 dx) (btx - bt0) - dt/(2 eps0) jr
-  e = ld2(F.er.ptr(ix, ir, im));
-  e.x += b * bx0.y - cdx * (btx.x - bt0.x) - cj * jr.x;
-  e.y += -b * bx0.x - cdx * (btx.y - bt0.y) - cj * jr.y;
-  st2(F.er.ptr(ix, ir, im), e);
+  const float2 der = make_float2(inc2(__fmul_rn(b, bx0.y), -cdx, __fsub_rn(btx.x, bt0.x), -cj, jr.x),
+                                 inc2(__fmul_rn(-b, bx0.x), -cdx, __fsub_rn(btx.y, bt0.y), -cj, jr.y));
   // et += c^2 dt/(2 dx) (brx - br0) - c^2 dt/(2 dy) (bx1 - bx0) - dt/(2 eps0) jt
-  e = ld2(F.et.ptr(ix, ir, im));
-  e.x += cdx * (brx.x - br0.x) - cdy * (bx1.x - bx0.x) - cj * jt.x;
-  e.y += cdx * (brx.y - br0.y) - cdy * (bx1.y - bx0.y) - cj * jt.y;
-  st2(F.et.ptr(ix, ir, im), e);
+  const float2 det = make_float2(
+      inc2(__fmul_rn(cdx, __fsub_rn(brx.x, br0.x)), -cdy, __fsub_rn(bx1.x, bx0.x), -cj, jt.x),
+      inc2(__fmul_rn(cdx, __fsub_rn(brx.y, br0.y)), -cdy, __fsub_rn(bx1.y, bx0.y), -cj, jt.y));
+  float2 ex = ld2(F.ex.ptr(ix, ir, im)), er = ld2(F.er.ptr(ix, ir, im)), et = ld2(F.et.ptr(ix, ir, im));
+  for (int k = 0; k < reps; ++k) {
+    ex = make_float2(__fadd_rn(ex.x, dex.x), __fadd_rn(ex.y, dex.y));
+    er = make_float2(__fadd_rn(er.x, der.x), __fadd_rn(er.y, der.y));
+    et = make_float2(__fadd_rn(et.x, det.x), __fadd_rn(et.y, det.y));
+  }
+  st2(F.ex.ptr(ix, ir, im), ex);
+  st2(F.er.ptr(ix, ir, im), er);
+  st2(F.et.ptr(ix, ir, im), et);
 }
 
 // One cell and mode of update_b_field over the whole ghosted array (index
@@ -139,6 +166,46 @@ __global__ void k_update_e_f32(FieldSetF F, const float4* rowtab, float cdx, flo
   if (ix > rc.nx) return;
   update_e_item(F, rowtab, cdx, cdy, cj, r1, ix, blockIdx.y, 1 + blockIdx.z);
 }
+
+// Two consecutive E half-steps with the E boundary rules between them (the
+// closing half of one step, the opening half of the next) in two launches
+// instead of two bulk passes.  Between the halves, the axis rules and the
+// ghost phases read E of rows 1 and 2, column 1 and column nx, and write
+// rows <= 0 and ghost cells; inside the update range they write only row 1
+// (modes >= 2), row ny, columns 0 and nx.  These edge cells take the two
+// halves one at a time: the first by k_update_e_edge_f32 before the rules,
+// the second by k_update_e_fused_f32 after them.  Every other cell reads
+// only its own E, so it takes both halves in k_update_e_fused_f32.
+__device__ __forceinline__ bool e_edge_cell(int ix, int ir, const RunConst& rc) {
+  return ir <= 2 || ir == rc.ny || ix <= 1 || ix == rc.nx;
+}
+__global__ void k_update_e_edge_f32(FieldSetF F, const float4* rowtab, float cdx, float cdy, float cj, Row1E r1,
+                                    RunConst rc) {
+  const int nx = rc.nx, ny = rc.ny;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nrow = 3 * (nx + 1), ncol = 3 * (ny - 3);
+  int ix, ir;
+  if (t < nrow) {
+    const int k = t / (nx + 1);
+    ix = t - k * (nx + 1);
+    ir = k == 0 ? 1 : k == 1 ? 2 : ny;
+  } else if (t < nrow + ncol) {
+    const int u = t - nrow, k = u / (ny - 3);
+    ir = 3 + (u - k * (ny - 3));
+    ix = k == 0 ? 0 : k == 1 ? 1 : nx;
+  } else {
+    return;
+  }
+  update_e_item(F, rowtab, cdx, cdy, cj, r1, ix, blockIdx.y, ir);
+}
+__global__ void k_update_e_fused_f32(FieldSetF F, const float4* rowtab, float cdx, float cdy, float cj, Row1E r1,
+                                     RunConst rc) {
+  const int ix = blockIdx.x * blockDim.x + threadIdx.x;  // 0..nx
+  if (ix > rc.nx) return;
+  const int ir = 1 + blockIdx.z;
+  update_e_item(F, rowtab, cdx, cdy, cj, r1, ix, blockIdx.y, ir, e_edge_cell(ix, ir, rc) ? 1 : 2);
+}
+
 __global__ void k_update_b_f32(FieldSetF F, int save_old, const float4* rowtab, float hdx, float hdy, Row1B r1,
                                RunConst rc) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -194,6 +261,23 @@ void launch_update_e_f32(cudaStream_t s, const FieldSetF& F, const double* rowta
   yee_e_consts(rc, cdx, cdy, cj, r1);
   dim3 blk(128), grd((rc.nx + 1 + 127) / 128, rc.M, rc.ny);
   k_update_e_f32<<<grd, blk, 0, s>>>(F, reinterpret_cast<const float4*>(rowtab), cdx, cdy, cj, r1, rc);
+}
+
+void launch_update_e_f32_edge(cudaStream_t s, const FieldSetF& F, const double* rowtab, const RunConst& rc) {
+  float cdx, cdy, cj;
+  Row1E r1;
+  yee_e_consts(rc, cdx, cdy, cj, r1);
+  const int n = 3 * (rc.nx + 1) + 3 * (rc.ny - 3);
+  dim3 blk(128), grd((n + 127) / 128, rc.M);
+  k_update_e_edge_f32<<<grd, blk, 0, s>>>(F, reinterpret_cast<const float4*>(rowtab), cdx, cdy, cj, r1, rc);
+}
+
+void launch_update_e_f32_fused(cudaStream_t s, const FieldSetF& F, const double* rowtab, const RunConst& rc) {
+  float cdx, cdy, cj;
+  Row1E r1;
+  yee_e_consts(rc, cdx, cdy, cj, r1);
+  dim3 blk(128), grd((rc.nx + 1 + 127) / 128, rc.M, rc.ny);
+  k_update_e_fused_f32<<<grd, blk, 0, s>>>(F, reinterpret_cast<const float4*>(rowtab), cdx, cdy, cj, r1, rc);
 }
 
 void launch_update_b_f32(cudaStream_t s, const FieldSetF& F, int save_old, const double* rowtab,

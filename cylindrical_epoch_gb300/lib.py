@@ -31,6 +31,7 @@ SIGNATURES = {
     "cyl_upload_particles": (C.c_int, [H, I32, PD, PD, PD, PD, PD, PD, PD, PI64, I64]),
     "cyl_load_species_device": (C.c_int, [H, I32, C.c_uint64, I64, PI64]),
     "cyl_set_injection_stream": (C.c_int, [H, I32, C.c_uint64]),
+    "cyl_set_merge_e_halves": (C.c_int, [H, I32]),
     "cyl_counter_block": (C.c_int, [C.c_uint64, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     "cyl_sdf_write": (C.c_int, [C.c_char_p, P(abi.SdfDesc), C.POINTER(PD), P(abi.SdfSpecies), I32]),
     "cyl_write_sdf": (C.c_int, [H, C.c_char_p, I32, C.POINTER(C.c_char_p)]),

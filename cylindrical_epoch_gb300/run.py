@@ -433,6 +433,12 @@ class Run:
     def push_only(self):
         abi.check("cyl_push_only", self.lib.cyl_push_only(self.h))
 
+    def merge_e_halves(self, on=True):
+        """Mixed form: merge each step's closing E half-step with the next
+        step's opening one inside a chunk (the default; the results are
+        those of separate half-steps).  cyl_set_merge_e_halves."""
+        abi.check("cyl_set_merge_e_halves", self.lib.cyl_set_merge_e_halves(self.h, 1 if on else 0))
+
     def tune_tiles(self, shape=None):
         """Mixed form: with shape=None time one push of the current state with
         every tile shape and keep the fastest, else use tile shape `shape`

@@ -438,6 +438,14 @@ int cyl_ionisation_constants(const cyl_ionisation_species* species, const cyl_sp
 #define CYL_RNG_COUNTER 1
 int cyl_load_species_device(cyl_handle h, int32_t ispecies, uint64_t seed, int64_t id_base, int64_t* n_out);
 int cyl_set_injection_stream(cyl_handle h, int32_t mode, uint64_t seed);
+/* Mixed form: inside one cyl_step call's chunk of steps that does not shift
+ * the window, the closing E half-step of each step and the opening one of
+ * the next see the same B and J; they are merged into one pass over the
+ * bulk of the grid (on, the default), with the cells that the E boundary
+ * rules touch between them updated one half at a time.  The results are
+ * those of separate half-steps; on = 0 runs every half-step as its own
+ * pass.  The FP64 form never merges. */
+int cyl_set_merge_e_halves(cyl_handle h, int32_t on);
 /* One block of the counter stream: Philox4x32-10 of counter ctr under key
  * seed (host only; for reproducing the stream outside the library). */
 int cyl_counter_block(uint64_t seed, const uint32_t* ctr4, uint32_t* out4);

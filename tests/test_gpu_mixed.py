@@ -203,3 +203,40 @@ def test_mixed_large_deck_physics(gpu_lib):
     print("M=4 mixed vs fp64 Ez error per mode:", errs, "mode norms:", norms)
     assert max(errs) < TOL_EZ
     assert b.diagnostics().device_error == 0
+
+
+@pytest.mark.parametrize("kind", ["wakefield", "thermal", "thermal3"])
+def test_merged_e_half_steps(gpu_lib, kind):
+    """Inside a chunk, the mixed form merges each step's closing E half-step
+    with the next step's opening one; the edge cells that the E boundary rules
+    touch between them take the halves one at a time.  Against runs with
+    every half-step separate (cyl_set_merge_e_halves(h, 0)), under the x_min
+    laser and outflow boundaries, periodic x with a conducting r_max, and the
+    axis rule of modes m >= 2.  The arithmetic is the same, but the mixed form
+    is not bit-reproducible from run to run (the order of its FP64 current
+    atomics), so the bar is the spread of two separate-half-step runs: a
+    mistake at the edge cells would put O(1) errors on whole rows or columns
+    (relative L2 of order 1e-2)."""
+    if kind == "wakefield":
+        deck = _wake(abi.PREC_MIXED)
+    else:
+        deck = cg.thermal_plasma(nx=128, ny=32, ppc=4, n_mode=3 if kind == "thermal3" else 2,
+                                 precision=abi.PREC_MIXED)
+    parts, rng = cg.host_load(deck)
+    runs = [cg.Run(deck, particles=parts, rng=rng) for _ in range(3)]
+    runs[0].merge_e_halves(False)
+    runs[1].merge_e_halves(False)
+    for k in (16, 16, 8):
+        for r in runs:
+            r.step(k, graph=True)
+    sep, sep2, merged = runs
+    assert sep.state().n_live[0] == merged.state().n_live[0]
+    for n in ("exm", "erm", "etm", "bxm", "brm", "btm"):
+        fa, fb, fm_ = sep.field(n), sep2.field(n), merged.field(n)
+        for m in range(fa.shape[0]):
+            if not np.any(fa[m] != 0):
+                continue
+            spread = rel_l2(fb[m], fa[m])
+            assert rel_l2(fm_[m], fa[m]) <= max(1e3 * spread, 1e-9), (n, m, spread)
+    for r in runs:
+        assert r.diagnostics().device_error == 0
