@@ -541,10 +541,10 @@ static FieldSetT<T> enqueue_step_pre(Handle* h, cudaStream_t s, const StepRec* r
   const RunConst& rc = h->rc;
   FieldSetT<T> F = fieldset_t<T>(h, h->jpar);
   bulk_e_half<T>(h, s, F, fused_in ? 2 : 0);
-  launch_e_axis_bcs(s, F, rec, rc);
+  int n = 1 + launch_e_axis_bcs(s, F, rec, rc);
   bulk_b(h, s, F, 1);
-  launch_b_axis_bcs(s, F, rec, rc);
-  count_launch(h, 6);
+  n += 1 + launch_b_axis_bcs(s, F, rec, rc);
+  count_launch(h, n);
   h->jpar ^= 1;
   F = fieldset_t<T>(h, h->jpar);
   // J = 0, and the mixed push's deferred counts, in one launch
@@ -567,23 +567,23 @@ static void enqueue_current_finish(Handle* h, cudaStream_t s, const FieldSetT<T>
   if (h->ion_on) {
     // push_particles ends with current_bcs_r_min_final; ionise_particles
     // runs before current_finish (epoch2d.F90:218-252)
-    launch_current_finish(s, F, rec, rc, h->gd.smooth_currents, h->gd.smooth_its, h->gd.smooth_comp_its, stride,
-                          wk, 1);
+    int n = launch_current_finish(s, F, rec, rc, h->gd.smooth_currents, h->gd.smooth_its, h->gd.smooth_comp_its,
+                                  stride, wk, 1);
     if constexpr (std::is_same<T, cplx>::value)
       launch_ionise(s, F, h->sp, h->nsp, h->d_cnt, h->ion, rec, rc, h->d_ion, h->d_ion + MAX_SPECIES, h->d_err,
                     h->nblocks);
     else
       launch_ionise(s, F, h->sp, h->nsp, h->d_cnt, h->ion, rec, rc, h->d_ion, h->d_ion + MAX_SPECIES, h->d_err,
                     h->nblocks, h->xg0);
-    launch_current_finish(s, F, rec, rc, h->gd.smooth_currents, h->gd.smooth_its, h->gd.smooth_comp_its, stride,
-                          wk, 6);
+    n += launch_current_finish(s, F, rec, rc, h->gd.smooth_currents, h->gd.smooth_its, h->gd.smooth_comp_its,
+                               stride, wk, 6);
     int nion = 0;
     for (int i = 0; i < h->nsp; ++i) nion += h->ion.s[i].ionise;
-    count_launch(h, 4 + nion);
+    count_launch(h, n + 2 + nion);  // the ionisation: a count snapshot, a kernel per species, the clamp
     return;
   }
-  launch_current_finish(s, F, rec, rc, h->gd.smooth_currents, h->gd.smooth_its, h->gd.smooth_comp_its, stride, wk);
-  count_launch(h, 2);
+  count_launch(h, launch_current_finish(s, F, rec, rc, h->gd.smooth_currents, h->gd.smooth_its,
+                                        h->gd.smooth_comp_its, stride, wk));
 }
 
 // The kernels of a step after the output point: update_eb_fields_final
@@ -593,10 +593,10 @@ static void enqueue_step_final(Handle* h, cudaStream_t s, const FieldSetT<T>& F,
                                const double* src, bool window = true, bool fused_out = false) {
   const RunConst& rc = h->rc;
   bulk_b(h, s, F, 0);
-  launch_b_final_bcs(s, F, rec, src, h->cols, 1, rc.dt, rc);
+  int n = 1 + launch_b_final_bcs(s, F, rec, src, h->cols, 1, rc.dt, rc);
   bulk_e_half<T>(h, s, F, fused_out ? 1 : 0);
-  launch_e_axis_bcs(s, F, rec, rc);
-  count_launch(h, 6);
+  n += 1 + launch_e_axis_bcs(s, F, rec, rc);
+  count_launch(h, n);
   // window: false when no step of the chunk shifts (the window's kernels
   // would do nothing: no injected particles, no removals, no field shift)
   if (h->move_window && window) {

@@ -137,18 +137,18 @@ void launch_inject_counter(cudaStream_t s, const StepRec* rec, const InjSpecies*
 void launch_update_e(cudaStream_t s, const FieldSet& F, const RunConst& rc);
 void launch_update_b(cudaStream_t s, const FieldSet& F, int save_old, const RunConst& rc);
 template <typename T>
-void launch_e_axis_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc);
+int launch_e_axis_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc);
 template <typename T>
-void launch_efield_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc);
+int launch_efield_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc);
 template <typename T>
-void launch_old_field_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc);
+int launch_old_field_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc);
 template <typename T>
-void launch_b_axis_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc);
+int launch_b_axis_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc);
 template <typename T>
-void launch_b_final_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const double* src,
+int launch_b_final_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const double* src,
                         const cplx* cols, int do_axis, double dt, const RunConst& rc);
 template <typename T>
-void launch_current_finish(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc,
+int launch_current_finish(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc,
                            int smooth, int its, int comp_its, int stride, FView wk, int parts = 7);
 // The zeroing at the start of a step's push: J = 0 of the three current
 // arrays (the J swap of update_eb_fields_half) and up to MAX_SPECIES int

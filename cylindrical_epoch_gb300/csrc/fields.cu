@@ -226,9 +226,130 @@ __device__ __forceinline__ void ghost_phase_item(const Triplet<T>& tr, int st0, 
     }
   }
 }
+
+// All phases of one efield_bcs / bfield_bcs call in one launch.  Every
+// boundary has one rule per field: none, a zero, or a copy (with a sign) of
+// a cell of the same row (x boundaries) or column (r_max).  The x rules
+// write ghost columns (and column 0 or nx), the r_max rules rows ny..ny+NG.
+// A cell in both sets (a corner) takes the copy of the cell at the x rule's
+// source column and the r rule's source row, with both signs, or zero if
+// either rule zeroes it: the x-then-r order of the phases gives the same
+// value (the rules are separable), and so does the opposite order.  No
+// rule's source cell is another rule's target, so one launch reads every
+// source before any write that could concern it.
+enum GhostOp { GO_NONE = 0, GO_ZERO = 1, GO_COPY = 2 };
+struct GhostRule {
+  int op, src;  // src: source column (x rules) or row (r_max rules)
+  bool neg;
+};
+// The x rule of field st at the side's i-th target (i = 1..NG) in row j, and
+// its target column.
+__device__ __forceinline__ GhostRule ghost_x_rule(int st, int side, int i, int j, bool halo_only,
+                                                  const int32_t* bcp, const RunConst& rc, int& col) {
+  const int nx = rc.nx, ny = rc.ny;
+  const int bd = side == 0 ? CYL_BD_X_MIN : CYL_BD_X_MAX;
+  const GhostRule none{GO_NONE, 0, false};
+  if (bcp[bd] == CYL_BC_PERIODIC) {
+    // halo exchange: rows 1-ng .. ny+ng, one fewer for r-staggered arrays
+    col = side == 0 ? i - NG : nx + i;
+    if (!(rc.bc_mask & BCM_PERIODIC_X) || j > ny + NG - (stag_y(st) ? 1 : 0)) return none;
+    return GhostRule{GO_COPY, side == 0 ? nx + i - NG : i, false};
+  }
+  const bool stag = stag_x(st);
+  col = stag && i == NG ? (side == 0 ? 0 : nx) : (side == 0 ? i - NG : nx + i);
+  if (halo_only) return none;
+  const int ph = bcp[bd] == CYL_BC_CONDUCT ? PH_CONDUCT_X : PH_OTHER_X;
+  if (!(rc.bc_mask & (ph == PH_CONDUCT_X ? BCM_CONDUCT : BCM_OTHER))) return none;
+  const int kind = ghost_kind(ph, st, bd, bcp);
+  if (kind == GK_NONE) return none;
+  if (stag && i == NG) return kind == GK_CLAMP ? GhostRule{GO_ZERO, 0, false} : none;
+  const int src = side == 0 ? (stag ? NG - i : NG + 1 - i) : (stag ? nx - i : nx + 1 - i);
+  return GhostRule{GO_COPY, src, kind == GK_CLAMP};
+}
+// The r_max rule of field st at its i-th target (i = 1..NG), and its target
+// row.
+__device__ __forceinline__ GhostRule ghost_y_rule(int st, int i, bool halo_only, const int32_t* bcp,
+                                                  const RunConst& rc, int& row) {
+  const int ny = rc.ny;
+  const GhostRule none{GO_NONE, 0, false};
+  const bool stag = stag_y(st);
+  row = stag && i == NG ? ny : ny + i;
+  if (halo_only) return none;
+  const int ph = bcp[CYL_BD_Y_MAX] == CYL_BC_CONDUCT ? PH_CONDUCT_Y : PH_OTHER_Y;
+  if (!(rc.bc_mask & (ph == PH_CONDUCT_Y ? BCM_CONDUCT : BCM_OTHER))) return none;
+  const int kind = ghost_kind(ph, st, CYL_BD_Y_MAX, bcp);
+  if (kind == GK_NONE) return none;
+  if (stag && i == NG) return kind == GK_CLAMP ? GhostRule{GO_ZERO, 0, false} : none;
+  return GhostRule{GO_COPY, stag ? ny - i : ny + 1 - i, kind == GK_CLAMP};
+}
+// The r_max rule that targets row j (i = 0: none).
+__device__ __forceinline__ int ghost_y_index(int st, int j, const RunConst& rc) {
+  const int ny = rc.ny;
+  if (stag_y(st)) return j == ny ? NG : (j > ny && j < ny + NG) ? j - ny : 0;
+  return (j > ny && j <= ny + NG) ? j - ny : 0;
+}
 template <typename T>
-__global__ void k_ghost_phase(Triplet<T> tr, int st0, int ph, const int32_t* bcp, RunConst rc) {
-  ghost_phase_item<T>(tr, st0, ph, bcp, rc, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+__device__ __forceinline__ void ghost_apply(FViewT<T> f, int col, int row, int m, const GhostRule& rx,
+                                            const GhostRule& ry) {
+  if (rx.op == GO_ZERO || ry.op == GO_ZERO) return gzero(f, col, row, m);
+  const int sc = rx.op == GO_COPY ? rx.src : col, sr = ry.op == GO_COPY ? ry.src : row;
+  gset(f, col, row, m, (rx.neg != ry.neg) ? GK_CLAMP : GK_ZERO_GRADIENT, sc, sr);
+}
+// Items: the x targets (i = 1..NG fastest, row j, m, q, side), which take
+// the corners, then the r_max targets (column fastest, i, m, q) outside the
+// x target columns.
+template <typename T>
+__device__ __forceinline__ void ghost_all_item(const Triplet<T>& tr, int st0, bool halo_only, const int32_t* bcp,
+                                               const RunConst& rc, int64_t t) {
+  const int nx = rc.nx, ny = rc.ny, M = rc.M;
+  const int nrow = ny + 2 * NG, ncol = nx + 2 * NG;
+  const int64_t nxi = (int64_t)2 * 3 * M * nrow * NG;
+  if (t < nxi) {
+    const int i = 1 + (int)(t % NG);
+    int r = (int)(t / NG);
+    const int j = 1 - NG + r % nrow;
+    r /= nrow;
+    const int m = r % M;
+    r /= M;
+    const int q = r % 3, side = r / 3;
+    const int st = st0 + q;
+    int col, row;
+    const GhostRule rx = ghost_x_rule(st, side, i, j, halo_only, bcp, rc, col);
+    const int iy = ghost_y_index(st, j, rc);
+    const GhostRule ry = iy ? ghost_y_rule(st, iy, halo_only, bcp, rc, row) : GhostRule{GO_NONE, 0, false};
+    if (rx.op == GO_NONE && ry.op == GO_NONE) return;
+    // a column that is an x target in some row belongs to these items
+    if (rx.op == GO_NONE) {
+      int c2;
+      if (ghost_x_rule(st, side, i, 1, halo_only, bcp, rc, c2).op == GO_NONE) return;
+    }
+    ghost_apply(tr.f[q], col, j, m, rx, ry);
+    return;
+  }
+  t -= nxi;
+  if (t >= (int64_t)ncol * NG * M * 3) return;
+  const int ix = 1 - NG + (int)(t % ncol);
+  int r = (int)(t / ncol);
+  const int i = 1 + r % NG;
+  r /= NG;
+  const int m = r % M, q = r / M;
+  const int st = st0 + q;
+  int row;
+  const GhostRule ry = ghost_y_rule(st, i, halo_only, bcp, rc, row);
+  if (ry.op == GO_NONE) return;
+  if (ix <= 0 || ix >= nx) {
+    // columns that an x rule targets (in any row) are written by the x items
+    for (int side = 0; side < 2; ++side)
+      for (int k = 1; k <= NG; ++k) {
+        int c;
+        if (ghost_x_rule(st, side, k, 1, halo_only, bcp, rc, c).op != GO_NONE && c == ix) return;
+      }
+  }
+  ghost_apply(tr.f[q], ix, row, m, GhostRule{GO_NONE, 0, false}, ry);
+}
+template <typename T>
+__global__ void k_ghost_all(Triplet<T> tr, int st0, int halo_only, const int32_t* bcp, RunConst rc) {
+  ghost_all_item<T>(tr, st0, halo_only != 0, bcp, rc, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // Device address of a step record's field bc codes (no host dereference).
@@ -238,23 +359,16 @@ __host__ __device__ static const int32_t* bc_ptr(const StepRec* rec) {
 
 // Launch the phases of efield_bcs / bfield_bcs (halo_only: bfield_bcs(.TRUE.),
 // the halo exchange alone) that this run's bc kinds can need.
+// Returns the number of kernels launched (0 or 1); so do the launchers below.
 template <typename T>
-static void launch_ghost_bcs(cudaStream_t s, FViewT<T> a, FViewT<T> b, FViewT<T> c, int st0, bool halo_only,
-                             const int32_t* bcp, const RunConst& rc) {
+static int launch_ghost_bcs(cudaStream_t s, FViewT<T> a, FViewT<T> b, FViewT<T> c, int st0, bool halo_only,
+                            const int32_t* bcp, const RunConst& rc) {
   const Triplet<T> tr{{a, b, c}};
-  const int nx_items = 2 * 3 * rc.M * (rc.ny + 2 * NG) * NG;
-  const int ny_items = (rc.nx + 2 * NG) * NG * rc.M * 3;
-  const int bx = (nx_items + 255) / 256, by = (ny_items + 255) / 256;
-  if (rc.bc_mask & BCM_PERIODIC_X) k_ghost_phase<T><<<bx, 256, 0, s>>>(tr, st0, PH_HALO, bcp, rc);
-  if (halo_only) return;
-  if (rc.bc_mask & BCM_CONDUCT) {
-    k_ghost_phase<T><<<bx, 256, 0, s>>>(tr, st0, PH_CONDUCT_X, bcp, rc);
-    k_ghost_phase<T><<<by, 256, 0, s>>>(tr, st0, PH_CONDUCT_Y, bcp, rc);
-  }
-  if (rc.bc_mask & BCM_OTHER) {
-    k_ghost_phase<T><<<bx, 256, 0, s>>>(tr, st0, PH_OTHER_X, bcp, rc);
-    k_ghost_phase<T><<<by, 256, 0, s>>>(tr, st0, PH_OTHER_Y, bcp, rc);
-  }
+  if (halo_only && !(rc.bc_mask & BCM_PERIODIC_X)) return 0;
+  if (!(rc.bc_mask & (BCM_PERIODIC_X | BCM_CONDUCT | BCM_OTHER))) return 0;
+  const int64_t items = (int64_t)2 * 3 * rc.M * (rc.ny + 2 * NG) * NG + (int64_t)(rc.nx + 2 * NG) * NG * rc.M * 3;
+  k_ghost_all<T><<<(unsigned)((items + 255) / 256), 256, 0, s>>>(tr, st0, halo_only ? 1 : 0, bcp, rc);
+  return 1;
 }
 // Axis rules of update_e_field (fields.f90:116-180) and update_b_field
 // (fields.f90:249-310).  Per column and mode they are one short sequence on
@@ -831,48 +945,55 @@ void launch_update_b(cudaStream_t s, const FieldSet& F, int save_old, const RunC
   k_update_b<<<grd, blk, 0, s>>>(F.ex, F.er, F.et, F.bx, F.br, F.bt, F.bxo, F.bro, F.bto, save_old, rc);
 }
 template <typename T>
-void launch_e_axis_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc) {
+int launch_e_axis_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc) {
   k_e_axis<T><<<axis_blocks(rc), 128, 0, s>>>(F.ex, F.er, F.et, F.jx, F.bt, bc_const(rc, rc.dt), rc);
-  launch_ghost_bcs<T>(s, F.ex, F.er, F.et, 0, false, bc_ptr(rec), rc);
+  return 1 + launch_ghost_bcs<T>(s, F.ex, F.er, F.et, 0, false, bc_ptr(rec), rc);
 }
 template <typename T>
-void launch_efield_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc) {
-  launch_ghost_bcs<T>(s, F.ex, F.er, F.et, 0, false, bc_ptr(rec), rc);
+int launch_efield_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc) {
+  return launch_ghost_bcs<T>(s, F.ex, F.er, F.et, 0, false, bc_ptr(rec), rc);
 }
 // old_field_bcs (boundary.F90:1480-1501): the halo exchange of B_old, Br_old
 // over rows 1-ng .. ny+ng-1.
 template <typename T>
-void launch_old_field_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc) {
-  launch_ghost_bcs<T>(s, F.bxo, F.bro, F.bto, 3, true, bc_ptr(rec), rc);
+int launch_old_field_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc) {
+  return launch_ghost_bcs<T>(s, F.bxo, F.bro, F.bto, 3, true, bc_ptr(rec), rc);
 }
 template <typename T>
-void launch_b_axis_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc) {
+int launch_b_axis_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc) {
   k_b_axis<T><<<axis_blocks(rc), 128, 0, s>>>(F.bx, F.br, F.bt, F.ex, F.et, bc_const(rc, rc.dt), rc);
-  launch_ghost_bcs<T>(s, F.bx, F.br, F.bt, 3, true, bc_ptr(rec), rc);
+  return 1 + launch_ghost_bcs<T>(s, F.bx, F.br, F.bt, 3, true, bc_ptr(rec), rc);
 }
 // update_b_field axis rules, then bfield_final_bcs (boundary.F90:1505-1537):
 // bfield_bcs, the x boundary laser / outflow, the r_max outflow or zero_b,
 // and the closing halo exchange (bfield_bcs(.TRUE.)).
 template <typename T>
-void launch_b_final_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const double* src,
-                        const cplx* cols, int do_axis, double dt, const RunConst& rc) {
+int launch_b_final_bcs(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const double* src,
+                       const cplx* cols, int do_axis, double dt, const RunConst& rc) {
   const BcConst K = bc_const(rc, dt);
   if (do_axis) k_b_axis<T><<<axis_blocks(rc), 128, 0, s>>>(F.bx, F.br, F.bt, F.ex, F.et, bc_const(rc, rc.dt), rc);
-  launch_ghost_bcs<T>(s, F.bx, F.br, F.bt, 3, false, bc_ptr(rec), rc);
+  int n = (do_axis ? 1 : 0) + launch_ghost_bcs<T>(s, F.bx, F.br, F.bt, 3, false, bc_ptr(rec), rc);
   k_laser_x<T><<<(2 * (rc.ny + 1) * rc.M + 127) / 128, 128, 0, s>>>(F, rec, src, cols, dt, K, rc);
   k_rmax_b<T><<<((rc.nx + 2 * NG) * rc.M + 127) / 128, 128, 0, s>>>(F, rec, dt, K, rc);
-  launch_ghost_bcs<T>(s, F.bx, F.br, F.bt, 3, true, bc_ptr(rec), rc);
+  return n + 2 + launch_ghost_bcs<T>(s, F.bx, F.br, F.bt, 3, true, bc_ptr(rec), rc);
 }
 template <typename T>
 // parts: bit 0 the r_min fold (current_bcs_r_min_final, the end of
 // push_particles), bits 1 and 2 current_finish (the folding and halo pass,
 // the smoothing): field ionisation runs between the fold and current_finish
 // (epoch2d.F90:218-252).
-void launch_current_finish(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc,
-                           int smooth, int its, int comp_its, int stride, FView wk, int parts) {
-  if (parts & 1) k_j_rmin<<<jrmin_blocks(rc), 128, 0, s>>>(F.jx, F.jr, F.jt, rc);
-  if ((parts & 2) && finish_needed(rc)) k_current_finish<<<1, CTA_THREADS, 0, s>>>(F.jx, F.jr, F.jt, rec, rc);
-  if (!(parts & 4) || !smooth) return;
+int launch_current_finish(cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, const RunConst& rc,
+                          int smooth, int its, int comp_its, int stride, FView wk, int parts) {
+  int n = 0;
+  if (parts & 1) {
+    k_j_rmin<<<jrmin_blocks(rc), 128, 0, s>>>(F.jx, F.jr, F.jt, rc);
+    ++n;
+  }
+  if ((parts & 2) && finish_needed(rc)) {
+    k_current_finish<<<1, CTA_THREADS, 0, s>>>(F.jx, F.jr, F.jt, rec, rc);
+    ++n;
+  }
+  if (!(parts & 4) || !smooth) return n;
   FView js[3] = {F.jx, F.jr, F.jt};
   dim3 blk(128), grd((rc.nx + 127) / 128, rc.ny, rc.M);
   const size_t bytes = (size_t)rc.nxg * rc.nyg * rc.M * sizeof(cplx);
@@ -886,7 +1007,9 @@ void launch_current_finish(cudaStream_t s, const FieldSetT<T>& F, const StepRec*
       if (it > its) alpha = (double)its * 0.5 + 1.0;
     }
     k_copy_interior<<<grd, blk, 0, s>>>(js[a], wk, rc);
+    n += 3 * (its + comp_its) + 1;
   }
+  return n;
 }
 template <typename T>
 void launch_shift_fields(cudaStream_t s, const FieldSetT<T>& F, const cplx* cols, const StepRec* rec,
@@ -1066,13 +1189,13 @@ void batch_shift_fields(cudaStream_t s, const StageJob* jobs, int njobs, int whi
 }
 
 #define INST(T)                                                                                          \
-  template void launch_e_axis_bcs<T>(cudaStream_t, const FieldSetT<T>&, const StepRec*, const RunConst&);  \
-  template void launch_efield_bcs<T>(cudaStream_t, const FieldSetT<T>&, const StepRec*, const RunConst&);  \
-  template void launch_old_field_bcs<T>(cudaStream_t, const FieldSetT<T>&, const StepRec*, const RunConst&); \
-  template void launch_b_axis_bcs<T>(cudaStream_t, const FieldSetT<T>&, const StepRec*, const RunConst&);  \
-  template void launch_b_final_bcs<T>(cudaStream_t, const FieldSetT<T>&, const StepRec*, const double*,    \
+  template int launch_e_axis_bcs<T>(cudaStream_t, const FieldSetT<T>&, const StepRec*, const RunConst&);  \
+  template int launch_efield_bcs<T>(cudaStream_t, const FieldSetT<T>&, const StepRec*, const RunConst&);  \
+  template int launch_old_field_bcs<T>(cudaStream_t, const FieldSetT<T>&, const StepRec*, const RunConst&); \
+  template int launch_b_axis_bcs<T>(cudaStream_t, const FieldSetT<T>&, const StepRec*, const RunConst&);  \
+  template int launch_b_final_bcs<T>(cudaStream_t, const FieldSetT<T>&, const StepRec*, const double*,    \
                                       const cplx*, int, double, const RunConst&);                          \
-  template void launch_current_finish<T>(cudaStream_t, const FieldSetT<T>&, const StepRec*, const RunConst&, \
+  template int launch_current_finish<T>(cudaStream_t, const FieldSetT<T>&, const StepRec*, const RunConst&, \
                                          int, int, int, int, FView, int);                                  \
   template void launch_shift_fields<T>(cudaStream_t, const FieldSetT<T>&, const cplx*, const StepRec*, int,  \
                                        const RunConst&);                                                  \
