@@ -107,17 +107,15 @@ __device__ void halo_x(FViewT<T> f, int j0, int j1, const int* bcf, const RunCon
 // ---------------------------------------------------- ghost-cell phases
 //
 // efield_bcs (boundary.F90:1355-1413) and bfield_bcs (boundary.F90:1417-1476)
-// in five phases, each one launch over many CTAs:
+// are, in the reference's order, five phases:
 //   PH_HALO       periodic self-wrap in x (boundary.F90:500-593 on one rank)
 //   PH_CONDUCT_X  conducting x boundaries      PH_CONDUCT_Y  conducting r_max
 //   PH_OTHER_X    clamp / laser / outflow / zero-gradient x boundaries
 //   PH_OTHER_Y    the same at r_max
 // with the ghost mirrors of field_mode_clamp_zero (boundary.F90:772-829) and
-// field_mode_zero_gradient (boundary.F90:654-707).  Within a phase every work
-// item writes ghost or boundary cells and reads only cells that no item of
-// the phase writes (nx, ny >= 8), so the items are independent; the phases
-// run in the reference's order.  Copies and sign flips act on the storage
-// type, so they are exact in both forms.
+// field_mode_zero_gradient (boundary.F90:654-707).  They run as one launch
+// (k_ghost_all below, which composes the phases cell by cell).  Copies and
+// sign flips act on the storage type, so they are exact in both forms.
 enum GhostPhase { PH_HALO = 0, PH_CONDUCT_X = 1, PH_CONDUCT_Y = 2, PH_OTHER_X = 3, PH_OTHER_Y = 4 };
 enum GhostKind { GK_NONE = 0, GK_CLAMP = 1, GK_ZERO_GRADIENT = 2 };
 
@@ -160,72 +158,6 @@ template <typename T>
 struct Triplet {
   FViewT<T> f[3];
 };
-
-// st0 = 0 for (ex, er, et), 3 for (bx, br, bt)
-template <typename T>
-__device__ __forceinline__ void ghost_phase_item(const Triplet<T>& tr, int st0, int ph, const int32_t* bcp,
-                                                 const RunConst& rc, int64_t t) {
-  const int nx = rc.nx, ny = rc.ny, M = rc.M;
-  if (ph == PH_CONDUCT_Y || ph == PH_OTHER_Y) {
-    // r_max: items (ix fastest, i = 1..NG, m, q)
-    const int ncol = nx + 2 * NG;
-    if (t >= (int64_t)ncol * NG * M * 3) return;
-    const int ix = 1 - NG + (int)(t % ncol);
-    int r = (int)(t / ncol);
-    const int i = 1 + r % NG;
-    r /= NG;
-    const int m = r % M, q = r / M;
-    const int st = st0 + q;
-    const int kind = ghost_kind(ph, st, CYL_BD_Y_MAX, bcp);
-    if (kind == GK_NONE) return;
-    const FViewT<T> f = tr.f[q];
-    if (stag_y(st)) {
-      if (i < NG) gset(f, ix, ny + i, m, kind, ix, ny - i);
-      else if (kind == GK_CLAMP) gzero(f, ix, ny, m);
-    } else {
-      gset(f, ix, ny + i, m, kind, ix, ny + 1 - i);
-    }
-    return;
-  }
-  // x boundaries: items (i = 1..NG fastest, row j, m, q, side)
-  const int nrow = ny + 2 * NG;
-  if (t >= (int64_t)2 * 3 * M * nrow * NG) return;
-  const int i = 1 + (int)(t % NG);
-  int r = (int)(t / NG);
-  const int j = 1 - NG + r % nrow;
-  r /= nrow;
-  const int m = r % M;
-  r /= M;
-  const int q = r % 3, side = r / 3;
-  const int st = st0 + q;
-  const int bd = side == 0 ? CYL_BD_X_MIN : CYL_BD_X_MAX;
-  const FViewT<T> f = tr.f[q];
-  if (ph == PH_HALO) {
-    if (bcp[bd] != CYL_BC_PERIODIC) return;
-    // rows 1-ng .. ny+ng, one fewer for r-staggered arrays (boundary.F90:1362-1371)
-    if (j > ny + NG - (stag_y(st) ? 1 : 0)) return;
-    if (side == 1) gset(f, nx + i, j, m, GK_ZERO_GRADIENT, i, j);
-    else gset(f, i - NG, j, m, GK_ZERO_GRADIENT, nx + i - NG, j);
-    return;
-  }
-  const int kind = ghost_kind(ph, st, bd, bcp);
-  if (kind == GK_NONE) return;
-  if (side == 0) {
-    if (stag_x(st)) {
-      if (i < NG) gset(f, i - NG, j, m, kind, NG - i, j);
-      else if (kind == GK_CLAMP) gzero(f, 0, j, m);
-    } else {
-      gset(f, i - NG, j, m, kind, NG + 1 - i, j);
-    }
-  } else {
-    if (stag_x(st)) {
-      if (i < NG) gset(f, nx + i, j, m, kind, nx - i, j);
-      else if (kind == GK_CLAMP) gzero(f, nx, j, m);
-    } else {
-      gset(f, nx + i, j, m, kind, nx + 1 - i, j);
-    }
-  }
-}
 
 // All phases of one efield_bcs / bfield_bcs call in one launch.  Every
 // boundary has one rule per field: none, a zero, or a copy (with a sign) of
@@ -1048,20 +980,13 @@ void launch_zero_step(cudaStream_t s, const FieldSetT<T>& F, const RunConst& rc,
 
 void stage_job_bc_consts(StageJob& J) { J.K = bc_const(J.rc, J.rc.dt); }
 
-__device__ __forceinline__ bool ghost_phase_needed(int mask, int ph) {
-  const int need = ph == PH_HALO ? BCM_PERIODIC_X
-                                 : (ph == PH_CONDUCT_X || ph == PH_CONDUCT_Y) ? BCM_CONDUCT : BCM_OTHER;
-  return (mask & need) != 0;
-}
-
 // which: 0 the E triplet, 1 the B triplet of the job's field set
-__global__ void k_ghost_phase_batch(const StageJob* __restrict__ jobs, int which, int use_f1, int st0, int ph) {
+__global__ void k_ghost_all_batch(const StageJob* __restrict__ jobs, int which, int use_f1, int st0, int halo_only) {
   const StageJob& J = jobs[blockIdx.y];
-  if (!ghost_phase_needed(J.rc.bc_mask, ph)) return;
   const RunConst rc = J.rc;
   const FieldSetF& Fr = use_f1 ? J.F1 : J.F0;
   const Triplet<cplxf> tr = which == 0 ? Triplet<cplxf>{{Fr.ex, Fr.er, Fr.et}} : Triplet<cplxf>{{Fr.bx, Fr.br, Fr.bt}};
-  ghost_phase_item<cplxf>(tr, st0, ph, bc_ptr(J.rec), rc, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+  ghost_all_item<cplxf>(tr, st0, halo_only != 0, bc_ptr(J.rec), rc, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 __global__ void k_e_axis_batch(const StageJob* __restrict__ jobs, int use_f1) {
   const StageJob& J = jobs[blockIdx.y];
@@ -1130,21 +1055,16 @@ __global__ void __launch_bounds__(CTA_THREADS) k_current_finish_batch(const Stag
   current_finish_cta(J.F1.jx, J.F1.jr, J.F1.jt, J.rec, rc);
 }
 
+// All ghost phases of one call for every run of the batch in one launch (as
+// launch_ghost_bcs; each run's own bc codes and mask decide its rules).
 static void batch_ghost(cudaStream_t s, const StageJob* jobs, int njobs, int which, int use_f1, int st0,
                         bool halo_only, int mask_any, const StageDims& d) {
-  const int nx_items = 2 * 3 * d.M * (d.ny_max + 2 * NG) * NG;
-  const int ny_items = (d.nx_max + 2 * NG) * NG * d.M * 3;
-  const dim3 gx((nx_items + 255) / 256, njobs), gy((ny_items + 255) / 256, njobs);
-  if (mask_any & BCM_PERIODIC_X) k_ghost_phase_batch<<<gx, 256, 0, s>>>(jobs, which, use_f1, st0, PH_HALO);
-  if (halo_only) return;
-  if (mask_any & BCM_CONDUCT) {
-    k_ghost_phase_batch<<<gx, 256, 0, s>>>(jobs, which, use_f1, st0, PH_CONDUCT_X);
-    k_ghost_phase_batch<<<gy, 256, 0, s>>>(jobs, which, use_f1, st0, PH_CONDUCT_Y);
-  }
-  if (mask_any & BCM_OTHER) {
-    k_ghost_phase_batch<<<gx, 256, 0, s>>>(jobs, which, use_f1, st0, PH_OTHER_X);
-    k_ghost_phase_batch<<<gy, 256, 0, s>>>(jobs, which, use_f1, st0, PH_OTHER_Y);
-  }
+  if (halo_only && !(mask_any & BCM_PERIODIC_X)) return;
+  if (!(mask_any & (BCM_PERIODIC_X | BCM_CONDUCT | BCM_OTHER))) return;
+  const int64_t items =
+      (int64_t)2 * 3 * d.M * (d.ny_max + 2 * NG) * NG + (int64_t)(d.nx_max + 2 * NG) * NG * d.M * 3;
+  k_ghost_all_batch<<<dim3((unsigned)((items + 255) / 256), njobs), 256, 0, s>>>(jobs, which, use_f1, st0,
+                                                                             halo_only ? 1 : 0);
 }
 static dim3 batch_axis_grid(int njobs, const StageDims& d) {
   return dim3(((d.nx_max + 2 * NG) * d.M * NG + 127) / 128, njobs);
