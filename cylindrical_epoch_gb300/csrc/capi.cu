@@ -542,19 +542,27 @@ static FieldSetT<T> enqueue_step_pre(Handle* h, cudaStream_t s, const StepRec* r
   FieldSetT<T> F = fieldset_t<T>(h, h->jpar);
   bulk_e_half<T>(h, s, F, fused_in ? 2 : 0);
   int n = 1 + launch_e_axis_bcs(s, F, rec, rc);
-  bulk_b(h, s, F, 1);
-  n += 1 + launch_b_axis_bcs(s, F, rec, rc);
-  count_launch(h, n);
-  h->jpar ^= 1;
-  F = fieldset_t<T>(h, h->jpar);
-  // J = 0, and the mixed push's deferred counts, in one launch
+  // J = 0 of the field set after the swap (its J held the step before's
+  // J_old, which nothing reads any more), and the mixed push's deferred
+  // counts: in the mixed form inside the B half-step's launch, else in one
+  // launch of their own
+  const FieldSetT<T> Fn = fieldset_t<T>(h, h->jpar ^ 1);
   ZeroCounts zc{};
-  if constexpr (std::is_same<T, cplxf>::value)
+  if constexpr (std::is_same<T, cplxf>::value) {
     for (int i = 0; i < h->nsp; ++i)
       if (!h->sp[i].immobile) zc.p[zc.n++] = h->mp[i].fb_count;
-  launch_zero_step(s, F, rc, zc);
-  count_launch(h, 1);
-  return F;
+    launch_update_b_f32_zero(s, F, (const double*)h->rowtab, rc, Fn, zc);
+  } else {
+    bulk_b(h, s, F, 1);
+  }
+  n += 1 + launch_b_axis_bcs(s, F, rec, rc);
+  if constexpr (!std::is_same<T, cplxf>::value) {
+    launch_zero_step(s, Fn, rc, zc);
+    ++n;
+  }
+  count_launch(h, n);
+  h->jpar ^= 1;
+  return Fn;
 }
 
 // The kernels of one step after the push up to the output point:

@@ -173,6 +173,10 @@ void launch_update_e_f32_edge(cudaStream_t s, const FieldSetF& F, const double* 
 void launch_update_e_f32_fused(cudaStream_t s, const FieldSetF& F, const double* rowtab, const RunConst& rc);
 void launch_update_b_f32(cudaStream_t s, const FieldSetF& F, int save_old, const double* rowtab,
                          const RunConst& rc);
+// The opening B half-step (B_old saved) together with launch_zero_step's
+// zeroing of Fz's currents and the counts zc, in one launch.
+void launch_update_b_f32_zero(cudaStream_t s, const FieldSetF& F, const double* rowtab, const RunConst& rc,
+                              const FieldSetF& Fz, const ZeroCounts& zc);
 
 // push_fp64.cu
 void launch_push_fp64(cudaStream_t s, const FieldSet& F, const GeomTables& g, const SpeciesPtrs& sp,

@@ -212,6 +212,23 @@ __global__ void k_update_b_f32(FieldSetF F, int save_old, const float4* rowtab, 
   if (i >= rc.nxg) return;
   update_b_item(F, save_old, rowtab, hdx, hdy, r1, rc, i, blockIdx.y, blockIdx.z);
 }
+// The opening B half-step of a step (B_old saved) with the step's zeroing
+// folded in: every cell of the ghosted grid also clears its values of the
+// three current arrays jx, jr, jt of Fz (the push's J after the J swap,
+// which nothing reads any more), and the first CTA clears the deferred
+// counts.  The grid covers the current arrays' whole extent.
+__global__ void k_update_b_f32_zero(FieldSetF F, const float4* rowtab, float hdx, float hdy, Row1B r1, RunConst rc,
+                                    FView jx, FView jr, FView jt, ZeroCounts zc) {
+  if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && (int)threadIdx.x < zc.n) *zc.p[threadIdx.x] = 0;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= rc.nxg) return;
+  const int ix = i + 1 - NG, ir = (int)blockIdx.z + 1 - NG, im = blockIdx.y;
+  const cplx z = mk(0.0, 0.0);
+  *jx.ptr(ix, ir, im) = z;
+  *jr.ptr(ix, ir, im) = z;
+  *jt.ptr(ix, ir, im) = z;
+  update_b_item(F, 1, rowtab, hdx, hdy, r1, rc, i, blockIdx.y, blockIdx.z);
+}
 
 // The batched forms: run blockIdx.z, (mode, row) blockIdx.y = m + M row.
 __global__ void k_update_e_f32_batch(const StageJob* __restrict__ jobs, int use_f1) {
@@ -287,6 +304,16 @@ void launch_update_b_f32(cudaStream_t s, const FieldSetF& F, int save_old, const
   yee_b_consts(rc, hdx, hdy, r1);
   dim3 blk(128), grd((rc.nxg + 127) / 128, rc.M, rc.nyg);
   k_update_b_f32<<<grd, blk, 0, s>>>(F, save_old, reinterpret_cast<const float4*>(rowtab), hdx, hdy, r1, rc);
+}
+
+void launch_update_b_f32_zero(cudaStream_t s, const FieldSetF& F, const double* rowtab, const RunConst& rc,
+                              const FieldSetF& Fz, const ZeroCounts& zc) {
+  float hdx, hdy;
+  Row1B r1;
+  yee_b_consts(rc, hdx, hdy, r1);
+  dim3 blk(128), grd((rc.nxg + 127) / 128, rc.M, rc.nyg);
+  k_update_b_f32_zero<<<grd, blk, 0, s>>>(F, reinterpret_cast<const float4*>(rowtab), hdx, hdy, r1, rc, Fz.jx,
+                                          Fz.jr, Fz.jt, zc);
 }
 
 void batch_update_e_f32(cudaStream_t s, const StageJob* jobs, int njobs, int use_f1, const StageDims& d) {
