@@ -206,8 +206,14 @@ __global__ void k_update_e_fused_f32(FieldSetF F, const float4* rowtab, float cd
   update_e_item(F, rowtab, cdx, cdy, cj, r1, ix, blockIdx.y, ir, e_edge_cell(ix, ir, rc) ? 1 : 2);
 }
 
-__global__ void k_update_b_f32(FieldSetF F, int save_old, const float4* rowtab, float hdx, float hdy, Row1B r1,
-                               RunConst rc) {
+// The B updates wait on memory (long-scoreboard stalls, a third of the HBM
+// bandwidth at 32 warps an SM, the register-bound occupancy): a 40-register
+// cap gives 48 warps an SM (the FP64 first row's few spills are in one row
+// of the grid).
+constexpr int B_BLOCKS_PER_SM = 12;
+__global__ void __launch_bounds__(128, B_BLOCKS_PER_SM) k_update_b_f32(FieldSetF F, int save_old,
+                                                                      const float4* rowtab, float hdx, float hdy,
+                                                                      Row1B r1, RunConst rc) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= rc.nxg) return;
   update_b_item(F, save_old, rowtab, hdx, hdy, r1, rc, i, blockIdx.y, blockIdx.z);
@@ -217,8 +223,10 @@ __global__ void k_update_b_f32(FieldSetF F, int save_old, const float4* rowtab, 
 // three current arrays jx, jr, jt of Fz (the push's J after the J swap,
 // which nothing reads any more), and the first CTA clears the deferred
 // counts.  The grid covers the current arrays' whole extent.
-__global__ void k_update_b_f32_zero(FieldSetF F, const float4* rowtab, float hdx, float hdy, Row1B r1, RunConst rc,
-                                    FView jx, FView jr, FView jt, ZeroCounts zc) {
+__global__ void __launch_bounds__(128, B_BLOCKS_PER_SM) k_update_b_f32_zero(FieldSetF F, const float4* rowtab,
+                                                                           float hdx, float hdy, Row1B r1,
+                                                                           RunConst rc, FView jx, FView jr,
+                                                                           FView jt, ZeroCounts zc) {
   if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && (int)threadIdx.x < zc.n) *zc.p[threadIdx.x] = 0;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= rc.nxg) return;
@@ -240,7 +248,8 @@ __global__ void k_update_e_f32_batch(const StageJob* __restrict__ jobs, int use_
   const FieldSetF F = use_f1 ? J.F1 : J.F0;
   update_e_item(F, J.rowtab, J.cdx, J.cdy, J.cj, J.r1e, ix, im, ir);
 }
-__global__ void k_update_b_f32_batch(const StageJob* __restrict__ jobs, int use_f1, int save_old) {
+__global__ void __launch_bounds__(128, B_BLOCKS_PER_SM) k_update_b_f32_batch(const StageJob* __restrict__ jobs,
+                                                                            int use_f1, int save_old) {
   const StageJob& J = jobs[blockIdx.z];
   const int M = J.rc.M;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
