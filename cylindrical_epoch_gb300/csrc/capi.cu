@@ -904,8 +904,12 @@ static int run_chunk(Handle* h, int k, bool use_graph) {
     // this one.  Built before the launch instead, the capture and the
     // instantiation (about a millisecond of host time) would leave the
     // stream idle.
+    // the chunk is queued: its push events are read with the next chunk
+    // even when the capture fails
+    h->timing_pending = k;
     if (use_graph && k == CHUNK)
       if (int r = capture_chunk_graph(h, window)) return r;
+    return CYL_OK;
   }
   h->timing_pending = k;
   return CYL_OK;
