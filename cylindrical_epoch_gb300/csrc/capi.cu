@@ -496,16 +496,25 @@ static void bulk_e(Handle* h, cudaStream_t s, const FieldSet& F) { launch_update
 static void bulk_e(Handle* h, cudaStream_t s, const FieldSetF& F) {
   launch_update_e_f32(s, F, (const double*)h->rowtab, h->rc);
 }
-// The E half-steps at a step boundary inside a chunk (mixed form): `half`
-// 1 is the closing half of a step (its edge cells alone), 2 the opening half
-// of the next (see launch_update_e_f32_edge / _fused), 0 a plain half-step.
+// An E half-step and the E boundary rules after it (the axis rules and
+// efield_bcs).  At a step boundary inside a chunk (mixed form), `half` 1 is
+// the closing half of a step (its edge cells alone), 2 the opening half of
+// the next (see launch_update_e_f32_edge_axis / _fused_axis, which apply the
+// axis rules themselves); 0 is a plain half-step.  Returns the launches.
 template <typename T>
-static void bulk_e_half(Handle* h, cudaStream_t s, const FieldSetT<T>& F, int half) {
+static int e_half_and_bcs(Handle* h, cudaStream_t s, const FieldSetT<T>& F, const StepRec* rec, int half) {
   if constexpr (std::is_same<T, cplxf>::value) {
-    if (half == 1) return launch_update_e_f32_edge(s, F, (const double*)h->rowtab, h->rc);
-    if (half == 2) return launch_update_e_f32_fused(s, F, (const double*)h->rowtab, h->rc);
+    if (half == 1) {
+      launch_update_e_f32_edge_axis(s, F, (const double*)h->rowtab, h->rc);
+      return 1 + launch_efield_bcs(s, F, rec, h->rc);
+    }
+    if (half == 2) {
+      launch_update_e_f32_fused_axis(s, F, (const double*)h->rowtab, h->rc);
+      return 1 + launch_efield_bcs(s, F, rec, h->rc);
+    }
   }
   bulk_e(h, s, F);
+  return 1 + launch_e_axis_bcs(s, F, rec, h->rc);
 }
 static void bulk_b(Handle* h, cudaStream_t s, const FieldSet& F, int save_old) {
   launch_update_b(s, F, save_old, h->rc);
@@ -540,8 +549,7 @@ template <typename T>
 static FieldSetT<T> enqueue_step_pre(Handle* h, cudaStream_t s, const StepRec* rec, bool fused_in = false) {
   const RunConst& rc = h->rc;
   FieldSetT<T> F = fieldset_t<T>(h, h->jpar);
-  bulk_e_half<T>(h, s, F, fused_in ? 2 : 0);
-  int n = 1 + launch_e_axis_bcs(s, F, rec, rc);
+  int n = e_half_and_bcs<T>(h, s, F, rec, fused_in ? 2 : 0);
   // J = 0 of the field set after the swap (its J held the step before's
   // J_old, which nothing reads any more), and the mixed push's deferred
   // counts: in the mixed form inside the B half-step's launch, else in one
@@ -602,8 +610,7 @@ static void enqueue_step_final(Handle* h, cudaStream_t s, const FieldSetT<T>& F,
   const RunConst& rc = h->rc;
   bulk_b(h, s, F, 0);
   int n = 1 + launch_b_final_bcs(s, F, rec, src, h->cols, 1, rc.dt, rc);
-  bulk_e_half<T>(h, s, F, fused_out ? 1 : 0);
-  n += 1 + launch_e_axis_bcs(s, F, rec, rc);
+  n += e_half_and_bcs<T>(h, s, F, rec, fused_out ? 1 : 0);
   count_launch(h, n);
   // window: false when no step of the chunk shifts (the window's kernels
   // would do nothing: no injected particles, no removals, no field shift)

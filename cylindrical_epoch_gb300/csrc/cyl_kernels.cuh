@@ -167,10 +167,11 @@ void launch_shift_fields(cudaStream_t s, const FieldSetT<T>& F, const cplx* cols
 void launch_update_e_f32(cudaStream_t s, const FieldSetF& F, const double* rowtab, const RunConst& rc);
 // Two consecutive E half-steps (the closing half of a step, then the E
 // boundary rules, then the opening half of the next step): the edge cells'
-// first half, and after the rules the edge cells' second half with both
-// halves of every other cell (fields_fp32.cu).
-void launch_update_e_f32_edge(cudaStream_t s, const FieldSetF& F, const double* rowtab, const RunConst& rc);
-void launch_update_e_f32_fused(cudaStream_t s, const FieldSetF& F, const double* rowtab, const RunConst& rc);
+// first half with the axis row's rule, then (after the ghost phases) the
+// edge cells' second half and both halves of every other cell, with the
+// axis rules (fields_fp32.cu).  Each is followed by the ghost phases alone.
+void launch_update_e_f32_edge_axis(cudaStream_t s, const FieldSetF& F, const double* rowtab, const RunConst& rc);
+void launch_update_e_f32_fused_axis(cudaStream_t s, const FieldSetF& F, const double* rowtab, const RunConst& rc);
 void launch_update_b_f32(cudaStream_t s, const FieldSetF& F, int save_old, const double* rowtab,
                          const RunConst& rc);
 // The opening B half-step (B_old saved) together with launch_zero_step's

@@ -11,6 +11,7 @@
 #include "cyl_common.cuh"
 #include "cyl_kernels.cuh"
 #include "cyl_convert.cuh"
+#include "axis_rules.cuh"
 
 namespace cyl {
 
@@ -169,41 +170,73 @@ __global__ void k_update_e_f32(FieldSetF F, const float4* rowtab, float cdx, flo
 
 // Two consecutive E half-steps with the E boundary rules between them (the
 // closing half of one step, the opening half of the next) in two launches
-// instead of two bulk passes.  Between the halves, the axis rules and the
-// ghost phases read E of rows 1 and 2, column 1 and column nx, and write
-// rows <= 0 and ghost cells; inside the update range they write only row 1
-// (modes >= 2), row ny, columns 0 and nx.  These edge cells take the two
-// halves one at a time: the first by k_update_e_edge_f32 before the rules,
-// the second by k_update_e_fused_f32 after them.  Every other cell reads
-// only its own E, so it takes both halves in k_update_e_fused_f32.
+// instead of two bulk passes and two axis launches.  Between the halves, the
+// axis rules and the ghost phases read E of rows 1 and 2, column 1 and column
+// nx, and write rows <= 0 and ghost cells; inside the update range they
+// write only row 1 (modes >= 2), row ny, columns 0 and nx.  These edge cells
+// take the two halves one at a time: the first by k_update_e_edge_axis_f32
+// before the rules, the second by k_update_e_fused_axis_f32 after them.
+// Every other cell reads only its own E, so it takes both halves in
+// k_update_e_fused_axis_f32.
+//
+// The axis rules run inside the same launches, per column: the first launch
+// updates rows 1 and 2 of its column, then applies the axis row's sequence
+// (task 0, which reads rows 0..2 of the column); its ghost-row mirrors
+// (tasks >= 1) are left out, as every value they would write is rewritten
+// by the mirrors after the second half before anything reads it.  The second
+// launch updates rows 1 .. NG of its column, then applies all the column's
+// axis tasks (the mirrors read rows 1 .. NG).  Both cover the ghost columns
+// too, for the axis rules alone.
 __device__ __forceinline__ bool e_edge_cell(int ix, int ir, const RunConst& rc) {
   return ir <= 2 || ir == rc.ny || ix <= 1 || ix == rc.nx;
 }
-__global__ void k_update_e_edge_f32(FieldSetF F, const float4* rowtab, float cdx, float cdy, float cj, Row1E r1,
-                                    RunConst rc) {
-  const int nx = rc.nx, ny = rc.ny;
+// Items: (column 1-NG .. nx+NG) for rows 1, 2 and the axis row, then the
+// other edge cells: row ny, and columns 0, 1, nx of rows 3 .. ny-1.
+__global__ void k_update_e_edge_axis_f32(FieldSetF F, const float4* rowtab, float cdx, float cdy, float cj, Row1E r1,
+                                         BcConst K, RunConst rc) {
+  const int nx = rc.nx, ny = rc.ny, im = blockIdx.y;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nrow = 3 * (nx + 1), ncol = 3 * (ny - 3);
-  int ix, ir;
-  if (t < nrow) {
-    const int k = t / (nx + 1);
-    ix = t - k * (nx + 1);
-    ir = k == 0 ? 1 : k == 1 ? 2 : ny;
-  } else if (t < nrow + ncol) {
-    const int u = t - nrow, k = u / (ny - 3);
+  const int ncolg = nx + 2 * NG, nrow = nx + 1, ncol = 3 * (ny - 3);
+  if (t < ncolg) {
+    const int ix = 1 - NG + t;
+    if (ix >= 0 && ix <= nx) {
+      update_e_item(F, rowtab, cdx, cdy, cj, r1, ix, im, 1);
+      update_e_item(F, rowtab, cdx, cdy, cj, r1, ix, im, 2);
+    }
+    e_axis_item<cplxf>(F.ex, F.er, F.et, F.jx, F.bt, rc, K, ix, im, 0);
+    return;
+  }
+  int u = t - ncolg, ix, ir;
+  if (u < nrow) {
+    ix = u;
+    ir = ny;
+  } else if ((u -= nrow) < ncol) {
+    const int k = u / (ny - 3);
     ir = 3 + (u - k * (ny - 3));
     ix = k == 0 ? 0 : k == 1 ? 1 : nx;
   } else {
     return;
   }
-  update_e_item(F, rowtab, cdx, cdy, cj, r1, ix, blockIdx.y, ir);
+  update_e_item(F, rowtab, cdx, cdy, cj, r1, ix, im, ir);
 }
-__global__ void k_update_e_fused_f32(FieldSetF F, const float4* rowtab, float cdx, float cdy, float cj, Row1E r1,
-                                     RunConst rc) {
-  const int ix = blockIdx.x * blockDim.x + threadIdx.x;  // 0..nx
-  if (ix > rc.nx) return;
-  const int ir = 1 + blockIdx.z;
-  update_e_item(F, rowtab, cdx, cdy, cj, r1, ix, blockIdx.y, ir, e_edge_cell(ix, ir, rc) ? 1 : 2);
+// blockIdx.z = 0: per column (1-NG .. nx+NG), rows 1 .. NG, then the
+// column's axis tasks; blockIdx.z = z >= 1: row NG + z of columns 0 .. nx.
+__global__ void k_update_e_fused_axis_f32(FieldSetF F, const float4* rowtab, float cdx, float cdy, float cj,
+                                          Row1E r1, BcConst K, RunConst rc) {
+  const int nx = rc.nx, im = blockIdx.y;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (blockIdx.z == 0) {
+    if (t >= nx + 2 * NG) return;
+    const int ix = 1 - NG + t;
+    if (ix >= 0 && ix <= nx)
+      for (int ir = 1; ir <= NG; ++ir)
+        update_e_item(F, rowtab, cdx, cdy, cj, r1, ix, im, ir, e_edge_cell(ix, ir, rc) ? 1 : 2);
+    for (int task = 0; task < NG; ++task) e_axis_item<cplxf>(F.ex, F.er, F.et, F.jx, F.bt, rc, K, ix, im, task);
+    return;
+  }
+  if (t > nx) return;
+  const int ir = NG + (int)blockIdx.z;
+  update_e_item(F, rowtab, cdx, cdy, cj, r1, t, im, ir, e_edge_cell(t, ir, rc) ? 1 : 2);
 }
 
 // The B updates wait on memory (long-scoreboard stalls, a third of the HBM
@@ -289,21 +322,23 @@ void launch_update_e_f32(cudaStream_t s, const FieldSetF& F, const double* rowta
   k_update_e_f32<<<grd, blk, 0, s>>>(F, reinterpret_cast<const float4*>(rowtab), cdx, cdy, cj, r1, rc);
 }
 
-void launch_update_e_f32_edge(cudaStream_t s, const FieldSetF& F, const double* rowtab, const RunConst& rc) {
+void launch_update_e_f32_edge_axis(cudaStream_t s, const FieldSetF& F, const double* rowtab, const RunConst& rc) {
   float cdx, cdy, cj;
   Row1E r1;
   yee_e_consts(rc, cdx, cdy, cj, r1);
-  const int n = 3 * (rc.nx + 1) + 3 * (rc.ny - 3);
+  const int n = (rc.nx + 2 * NG) + (rc.nx + 1) + 3 * (rc.ny - 3);
   dim3 blk(128), grd((n + 127) / 128, rc.M);
-  k_update_e_edge_f32<<<grd, blk, 0, s>>>(F, reinterpret_cast<const float4*>(rowtab), cdx, cdy, cj, r1, rc);
+  k_update_e_edge_axis_f32<<<grd, blk, 0, s>>>(F, reinterpret_cast<const float4*>(rowtab), cdx, cdy, cj, r1,
+                                               bc_const(rc, rc.dt), rc);
 }
 
-void launch_update_e_f32_fused(cudaStream_t s, const FieldSetF& F, const double* rowtab, const RunConst& rc) {
+void launch_update_e_f32_fused_axis(cudaStream_t s, const FieldSetF& F, const double* rowtab, const RunConst& rc) {
   float cdx, cdy, cj;
   Row1E r1;
   yee_e_consts(rc, cdx, cdy, cj, r1);
-  dim3 blk(128), grd((rc.nx + 1 + 127) / 128, rc.M, rc.ny);
-  k_update_e_fused_f32<<<grd, blk, 0, s>>>(F, reinterpret_cast<const float4*>(rowtab), cdx, cdy, cj, r1, rc);
+  dim3 blk(128), grd((rc.nx + 2 * NG + 127) / 128, rc.M, rc.ny - NG + 1);
+  k_update_e_fused_axis_f32<<<grd, blk, 0, s>>>(F, reinterpret_cast<const float4*>(rowtab), cdx, cdy, cj, r1,
+                                                bc_const(rc, rc.dt), rc);
 }
 
 void launch_update_b_f32(cudaStream_t s, const FieldSetF& F, int save_old, const double* rowtab,
